@@ -1,0 +1,405 @@
+// Cell grid, device-wide scans, counting sort by cell, and the exact neighbor search
+// exported for the neighborSearch drop-in (src/diffSPH/v2/modules/neighborhood.py:491-593).
+#include <math.h>
+
+#include "../../include/sph103.h"
+#include "sph_internal.cuh"
+
+namespace sph {
+
+Geo make_geo(const double mn[2], const double mx[2], const int per[2]) {
+    Geo g;
+    for (int a = 0; a < 2; ++a) {
+        g.mn[a] = (float)mn[a];
+        g.ext[a] = (float)(mx[a] - mn[a]);
+        g.half[a] = (float)((mx[a] - mn[a]) / 2.0);
+        g.per[a] = per[a] ? 1 : 0;
+    }
+    return g;
+}
+
+Grid make_grid(const double mn[2], const double mx[2], const int per[2], double cell_min,
+               int64_t* ncells_out) {
+    Grid g;
+    int64_t total = 1;
+    for (int a = 0; a < 2; ++a) {
+        double ext = mx[a] - mn[a];
+        int nc;
+        double cell;
+        if (per[a]) {
+            nc = (int)floor(ext / cell_min);
+            if (nc < 1) nc = 1;
+            cell = ext / nc;
+        } else {
+            nc = (int)ceil(ext / cell_min);
+            if (nc < 1) nc = 1;
+            cell = cell_min;
+        }
+        g.mn[a] = (float)mn[a];
+        g.inv_cell[a] = (float)(1.0 / cell);
+        g.nc[a] = nc;
+        g.per[a] = per[a] ? 1 : 0;
+        total *= nc;
+    }
+    if (ncells_out) *ncells_out = total;
+    return g;
+}
+
+// ------------------------------------------------------------------------------------
+// Exclusive scan: 256 threads x 8 items per block, block totals scanned by one block.
+// ------------------------------------------------------------------------------------
+constexpr int kScanItems = 8;
+constexpr int kScanTile = kBlock * kScanItems;
+
+int64_t scan_tmp_elems(int64_t n) { return (n + kScanTile - 1) / kScanTile + 1; }
+
+template <typename O>
+__device__ __forceinline__ O block_exclusive(O v, O* total) {
+    __shared__ O warp_tot[kBlock / 32];
+    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    O x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        O y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) warp_tot[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+        O w = lane < kBlock / 32 ? warp_tot[lane] : O(0);
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            O y = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w += y;
+        }
+        if (lane < kBlock / 32) warp_tot[lane] = w;
+    }
+    __syncthreads();
+    O base = wid > 0 ? warp_tot[wid - 1] : O(0);
+    if (total) *total = warp_tot[kBlock / 32 - 1];
+    O res = base + x - v;
+    __syncthreads();
+    return res;
+}
+
+template <typename I, typename O>
+__global__ void k_scan_local(const I* __restrict__ in, O* __restrict__ out, O* __restrict__ sums, int64_t n) {
+    int64_t base = (int64_t)blockIdx.x * kScanTile + (int64_t)threadIdx.x * kScanItems;
+    O v[kScanItems];
+    O t = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        int64_t i = base + k;
+        v[k] = i < n ? (O)in[i] : O(0);
+        t += v[k];
+    }
+    O tot;
+    O ex = block_exclusive<O>(t, &tot);
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        int64_t i = base + k;
+        if (i < n) out[i] = ex;
+        ex += v[k];
+    }
+    if (threadIdx.x == 0) sums[blockIdx.x] = tot;
+}
+
+template <typename O>
+__global__ void k_scan_sums(O* sums, int64_t nb) {
+    O carry = 0;
+    for (int64_t c0 = 0; c0 < nb; c0 += kBlock) {
+        int64_t i = c0 + threadIdx.x;
+        O v = i < nb ? sums[i] : O(0);
+        O tot;
+        O ex = block_exclusive<O>(v, &tot);
+        if (i < nb) sums[i] = ex + carry;
+        carry += tot;
+    }
+    if (threadIdx.x == 0) sums[nb] = carry;
+}
+
+template <typename O>
+__global__ void k_scan_add(O* __restrict__ out, const O* __restrict__ sums, int64_t n, int64_t nb) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] += sums[i / kScanTile];
+    if (i == 0) out[n] = sums[nb];
+}
+
+template <typename I, typename O>
+static cudaError_t scan_impl(const I* in, O* out, int64_t n, O* tmp, cudaStream_t s) {
+    int64_t nb = (n + kScanTile - 1) / kScanTile;
+    if (nb == 0) {
+        return cudaMemsetAsync(out, 0, sizeof(O), s);
+    }
+    k_scan_local<I, O><<<(unsigned)nb, kBlock, 0, s>>>(in, out, tmp, n);
+    k_scan_sums<O><<<1, kBlock, 0, s>>>(tmp, nb);
+    k_scan_add<O><<<(unsigned)((n + kBlock - 1) / kBlock), kBlock, 0, s>>>(out, tmp, n, nb);
+    return cudaGetLastError();
+}
+
+cudaError_t scan_exclusive(const int32_t* in, int32_t* out, int64_t n, int32_t* tmp, cudaStream_t s) {
+    return scan_impl<int32_t, int32_t>(in, out, n, tmp, s);
+}
+cudaError_t scan_exclusive(const int32_t* in, int64_t* out, int64_t n, int64_t* tmp, cudaStream_t s) {
+    return scan_impl<int32_t, int64_t>(in, out, n, tmp, s);
+}
+
+// ------------------------------------------------------------------------------------
+// Counting sort by cell
+// ------------------------------------------------------------------------------------
+__global__ void k_cell_keys(const float* __restrict__ xy, int stride, int64_t n, Grid g,
+                            int32_t* __restrict__ key, int32_t* __restrict__ count) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float x = xy[i * stride], y = xy[i * stride + 1];
+    int cx = cell_coord(x, g.mn[0], g.inv_cell[0], g.nc[0]);
+    int cy = cell_coord(y, g.mn[1], g.inv_cell[1], g.nc[1]);
+    int k = cy * g.nc[0] + cx;
+    key[i] = k;
+    atomicAdd(&count[k], 1);
+}
+
+__global__ void k_cell_scatter(int64_t n, const int32_t* __restrict__ key, const int32_t* __restrict__ start,
+                               int32_t* __restrict__ fill, int32_t* __restrict__ perm) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int k = key[i];
+    int slot = start[k] + atomicAdd(&fill[k], 1);
+    perm[slot] = (int32_t)i;
+}
+
+// Cells hold a few tens of particles: one thread sorts its cell's slots by input index.
+__global__ void k_cell_order(int64_t ncells, const int32_t* __restrict__ start, int32_t* __restrict__ perm) {
+    int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= ncells) return;
+    int b = start[c], e = start[c + 1];
+    for (int a = b + 1; a < e; ++a) {
+        int v = perm[a];
+        int k = a - 1;
+        while (k >= b && perm[k] > v) {
+            perm[k + 1] = perm[k];
+            --k;
+        }
+        perm[k + 1] = v;
+    }
+}
+
+cudaError_t cell_sort(const float* xy, int stride, int64_t n, const Grid& g, int64_t ncells,
+                      int32_t* key, int32_t* perm, int32_t* count, int32_t* fill, int32_t* start,
+                      int32_t* scan_tmp, cudaStream_t s) {
+    cudaError_t e;
+    if ((e = cudaMemsetAsync(count, 0, sizeof(int32_t) * ncells, s)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(fill, 0, sizeof(int32_t) * ncells, s)) != cudaSuccess) return e;
+    unsigned gb = (unsigned)((n + kBlock - 1) / kBlock);
+    if (n > 0) k_cell_keys<<<gb, kBlock, 0, s>>>(xy, stride, n, g, key, count);
+    if ((e = scan_exclusive(count, start, ncells, scan_tmp, s)) != cudaSuccess) return e;
+    if (n > 0) k_cell_scatter<<<gb, kBlock, 0, s>>>(n, key, start, fill, perm);
+    k_cell_order<<<(unsigned)((ncells + kBlock - 1) / kBlock), kBlock, 0, s>>>(ncells, start, perm);
+    return cudaGetLastError();
+}
+
+// ------------------------------------------------------------------------------------
+// Exact neighbor search, separate query and reference sets, per-particle h_j.
+// ------------------------------------------------------------------------------------
+struct NbWork {
+    Grid grid;
+    Geo geo;
+    int64_t ncells;
+    int32_t *key, *perm, *count, *fill, *start, *scan32;
+    int64_t* scan64;
+    float2* ref_tmp;    // wrapped reference positions, input order
+    float2* ref_xy;     // sorted, wrapped reference positions
+    float* ref_h;       // sorted supports
+    int32_t* ref_idx;   // sorted -> original index
+    float2* qry_xy;     // wrapped query positions
+};
+
+static int nb_layout(int64_t nq, int64_t nr, const sph_domain_t* d, double hmax, void* ws, NbWork* w,
+                     size_t* bytes) {
+    if (!d || hmax <= 0 || nq < 0 || nr < 0) return SPH_ERR_ARGUMENT;
+    int per[2] = {d->periodic[0], d->periodic[1]};
+    w->grid = make_grid(d->min, d->max, per, hmax * (1.0 + 1e-4), &w->ncells);
+    w->geo = make_geo(d->min, d->max, per);
+    if (w->ncells > (int64_t)1 << 30) return SPH_ERR_ARGUMENT;
+    Carver c{(char*)ws};
+    w->key = c.take<int32_t>(nr);
+    w->perm = c.take<int32_t>(nr);
+    w->count = c.take<int32_t>(w->ncells);
+    w->fill = c.take<int32_t>(w->ncells);
+    w->start = c.take<int32_t>(w->ncells + 1);
+    w->scan32 = c.take<int32_t>(scan_tmp_elems(w->ncells > nq ? w->ncells : nq));
+    w->scan64 = c.take<int64_t>(scan_tmp_elems(nq));
+    w->ref_tmp = c.take<float2>(nr);
+    w->ref_xy = c.take<float2>(nr);
+    w->ref_h = c.take<float>(nr);
+    w->ref_idx = c.take<int32_t>(nr);
+    w->qry_xy = c.take<float2>(nq);
+    *bytes = c.off;
+    return SPH_OK;
+}
+
+__global__ void k_wrap_copy(const float* __restrict__ x, int64_t n, Geo geo, float2* __restrict__ out) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    out[i] = wrap_pos(make_float2(x[2 * i], x[2 * i + 1]), geo);
+}
+
+__global__ void k_ref_gather(int64_t n, const int32_t* __restrict__ perm, const float2* __restrict__ wrapped,
+                             const float* __restrict__ h, float2* __restrict__ sxy, float* __restrict__ sh,
+                             int32_t* __restrict__ sidx) {
+    int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    int o = perm[s];
+    sxy[s] = wrapped[o];
+    sh[s] = h[o];
+    sidx[s] = o;
+}
+
+template <bool FILL>
+__global__ void k_nb_query(int64_t nq, const float2* __restrict__ qxy, const float2* __restrict__ rxy,
+                           const float* __restrict__ rh, const int32_t* __restrict__ ridx,
+                           const int32_t* __restrict__ start, Grid g, Geo geo, int32_t* __restrict__ counts,
+                           const int64_t* __restrict__ offsets, int64_t* __restrict__ pi, int64_t* __restrict__ pj,
+                           float* __restrict__ pq, float* __restrict__ px, float* __restrict__ ph) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nq) return;
+    float2 p = qxy[i];
+    int cx = cell_coord(p.x, g.mn[0], g.inv_cell[0], g.nc[0]);
+    int cy = cell_coord(p.y, g.mn[1], g.inv_cell[1], g.nc[1]);
+    int rows[3], lo[2], hi[2];
+    int nr = stencil_rows(cy, g, rows);
+    int ncr = stencil_cols(cx, g, lo, hi);
+    int64_t w = FILL ? offsets[i] : 0;
+    int cnt = 0;
+    for (int a = 0; a < nr; ++a) {
+        for (int b = 0; b < ncr; ++b) {
+            int c0 = rows[a] * g.nc[0] + lo[b], c1 = rows[a] * g.nc[0] + hi[b];
+            int s0 = start[c0], s1 = start[c1 + 1];
+            for (int s = s0; s < s1; ++s) {
+                float x0, x1;
+                pair_vec<true>(p, rxy[s], geo, x0, x1);
+                float r, q;
+                if (!exact_in(sq_norm_ref(x0, x1), rh[s], r, q)) continue;
+                if (FILL) {
+                    float den = __fadd_rn(r, 1e-7f);
+                    int64_t o = w + cnt;
+                    pi[o] = i;
+                    pj[o] = ridx[s];
+                    pq[o] = q;
+                    px[2 * o] = __fdiv_rn(x0, den);
+                    px[2 * o + 1] = __fdiv_rn(x1, den);
+                    ph[o] = rh[s];
+                }
+                ++cnt;
+            }
+        }
+    }
+    if (!FILL) counts[i] = cnt;
+    if (FILL) {
+        // canonical order: ascending reference index inside the row
+        int64_t b0 = w, e0 = w + cnt;
+        for (int64_t a2 = b0 + 1; a2 < e0; ++a2) {
+            int64_t vj = pj[a2];
+            float vq = pq[a2], vx0 = px[2 * a2], vx1 = px[2 * a2 + 1], vh = ph[a2];
+            int64_t k = a2 - 1;
+            while (k >= b0 && pj[k] > vj) {
+                pj[k + 1] = pj[k];
+                pq[k + 1] = pq[k];
+                px[2 * (k + 1)] = px[2 * k];
+                px[2 * (k + 1) + 1] = px[2 * k + 1];
+                ph[k + 1] = ph[k];
+                --k;
+            }
+            pj[k + 1] = vj;
+            pq[k + 1] = vq;
+            px[2 * (k + 1)] = vx0;
+            px[2 * (k + 1) + 1] = vx1;
+            ph[k + 1] = vh;
+        }
+    }
+}
+
+__global__ void k_pair_kernels(int64_t np, const float* __restrict__ q, const float* __restrict__ xh,
+                               const float* __restrict__ h, float* __restrict__ W, float* __restrict__ G) {
+    int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= np) return;
+    float hh = h[k];
+    KernelCoef kc;
+    kc.cw = kCd / (hh * hh);
+    kc.cg = kCd / (hh * hh * hh);
+    float qq = q[k];
+    if (W) W[k] = wendland_w(qq, kc);
+    if (G) {
+        float d = wendland_dw(qq, kc);
+        G[2 * k] = xh[2 * k] * d;
+        G[2 * k + 1] = xh[2 * k + 1] * d;
+    }
+}
+
+}  // namespace sph
+
+using namespace sph;
+
+extern "C" int sph_neighbor_workspace_bytes(int64_t n_query, int64_t n_ref, const sph_domain_t* domain,
+                                            double max_support, size_t* bytes) {
+    if (!bytes) return SPH_ERR_ARGUMENT;
+    NbWork w;
+    return nb_layout(n_query, n_ref, domain, max_support, nullptr, &w, bytes);
+}
+
+static int nb_prepare(const float* xq, int64_t nq, const float* xr, const float* hr, int64_t nr,
+                      const sph_domain_t* d, double hmax, void* ws, size_t wsb, NbWork* w, cudaStream_t s) {
+    size_t need;
+    int st = nb_layout(nq, nr, d, hmax, ws, w, &need);
+    if (st) return st;
+    if (!ws || wsb < need) return SPH_ERR_WORKSPACE;
+    if ((nq > 0 && !xq) || (nr > 0 && (!xr || !hr))) return SPH_ERR_ARGUMENT;
+    unsigned gr = (unsigned)((nr + kBlock - 1) / kBlock), gq = (unsigned)((nq + kBlock - 1) / kBlock);
+    if (nr > 0) k_wrap_copy<<<gr, kBlock, 0, s>>>(xr, nr, w->geo, w->ref_tmp);
+    if (cell_sort((const float*)w->ref_tmp, 2, nr, w->grid, w->ncells, w->key, w->perm, w->count, w->fill,
+                  w->start, w->scan32, s) != cudaSuccess)
+        return SPH_ERR_CUDA;
+    if (nr > 0) k_ref_gather<<<gr, kBlock, 0, s>>>(nr, w->perm, w->ref_tmp, hr, w->ref_xy, w->ref_h, w->ref_idx);
+    if (nq > 0) k_wrap_copy<<<gq, kBlock, 0, s>>>(xq, nq, w->geo, w->qry_xy);
+    return cudaGetLastError() == cudaSuccess ? SPH_OK : SPH_ERR_CUDA;
+}
+
+extern "C" int sph_neighbor_count(const float* x_query, int64_t n_query, const float* x_ref, const float* h_ref,
+                                  int64_t n_ref, const sph_domain_t* domain, double max_support, void* workspace,
+                                  size_t workspace_bytes, int32_t* counts, int64_t* offsets, sph_stream_t stream) {
+    cudaStream_t s = (cudaStream_t)stream;
+    NbWork w;
+    int st = nb_prepare(x_query, n_query, x_ref, h_ref, n_ref, domain, max_support, workspace, workspace_bytes, &w, s);
+    if (st) return st;
+    if (!offsets || (n_query > 0 && !counts)) return SPH_ERR_ARGUMENT;
+    if (n_query > 0)
+        k_nb_query<false><<<(unsigned)((n_query + kBlock - 1) / kBlock), kBlock, 0, s>>>(
+            n_query, w.qry_xy, w.ref_xy, w.ref_h, w.ref_idx, w.start, w.grid, w.geo, counts, nullptr, nullptr,
+            nullptr, nullptr, nullptr, nullptr);
+    if (scan_exclusive(counts, offsets, n_query, w.scan64, s) != cudaSuccess) return SPH_ERR_CUDA;
+    return cudaGetLastError() == cudaSuccess ? SPH_OK : SPH_ERR_CUDA;
+}
+
+extern "C" int sph_neighbor_fill(const float* x_query, int64_t n_query, const float* x_ref, const float* h_ref,
+                                 int64_t n_ref, const sph_domain_t* domain, double max_support, void* workspace,
+                                 size_t workspace_bytes, const int64_t* offsets, int64_t n_pairs,
+                                 int64_t* pair_i, int64_t* pair_j,
+                                 float* q, float* xhat, float* h_pair, float* kernels, float* gradients,
+                                 sph_stream_t stream) {
+    cudaStream_t s = (cudaStream_t)stream;
+    NbWork w;
+    size_t need;
+    int st = nb_layout(n_query, n_ref, domain, max_support, workspace, &w, &need);
+    if (st) return st;
+    if (!workspace || workspace_bytes < need) return SPH_ERR_WORKSPACE;
+    if (!offsets || (n_pairs > 0 && (!pair_i || !pair_j || !q || !xhat || !h_pair))) return SPH_ERR_ARGUMENT;
+    // the sorted reference set from sph_neighbor_count is still in the workspace
+    if (n_query > 0)
+        k_nb_query<true><<<(unsigned)((n_query + kBlock - 1) / kBlock), kBlock, 0, s>>>(
+            n_query, w.qry_xy, w.ref_xy, w.ref_h, w.ref_idx, w.start, w.grid, w.geo, nullptr, offsets, pair_i,
+            pair_j, q, xhat, h_pair);
+    if ((kernels || gradients) && n_pairs > 0)
+        k_pair_kernels<<<(unsigned)((n_pairs + kBlock - 1) / kBlock), kBlock, 0, s>>>(n_pairs, q, xhat, h_pair,
+                                                                                       kernels, gradients);
+    return cudaGetLastError() == cudaSuccess ? SPH_OK : SPH_ERR_CUDA;
+}

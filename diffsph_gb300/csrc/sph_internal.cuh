@@ -1,0 +1,91 @@
+// Internal (C++) interface shared by the sph103 translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#include "sph_common.cuh"
+
+namespace sph {
+
+constexpr int kBlock = 256;
+
+// Uniform cell grid over the domain. Periodic axes are tiled by an integer number of
+// cells (cell >= the requested size); non-periodic axes clamp out-of-range particles
+// into the edge cells (clamping is 1-Lipschitz, so the 3x3 stencil stays a superset).
+struct Grid {
+    float mn[2];
+    float inv_cell[2];
+    int nc[2];
+    int per[2];
+};
+
+__device__ __forceinline__ int cell_coord(float v, float mn, float inv, int nc) {
+    int c = (int)floorf((v - mn) * inv);
+    return c < 0 ? 0 : (c >= nc ? nc - 1 : c);
+}
+
+// Rows (y cells) of the 3x3 stencil around cy, each listed once.
+__device__ __forceinline__ int stencil_rows(int cy, const Grid& g, int rows[3]) {
+    int nc = g.nc[1];
+    if (g.per[1] && nc < 3) {
+        for (int k = 0; k < nc; ++k) rows[k] = k;
+        return nc;
+    }
+    int n = 0;
+    for (int dy = -1; dy <= 1; ++dy) {
+        int y = cy + dy;
+        if (g.per[1]) y = (y + nc) % nc;
+        else if (y < 0 || y >= nc) continue;
+        rows[n++] = y;
+    }
+    return n;
+}
+
+// Column ranges [lo, hi] (inclusive) of the stencil around cx: one contiguous range, or
+// two when a periodic axis wraps.
+__device__ __forceinline__ int stencil_cols(int cx, const Grid& g, int lo[2], int hi[2]) {
+    int nc = g.nc[0];
+    if (g.per[0]) {
+        if (nc < 3) { lo[0] = 0; hi[0] = nc - 1; return 1; }
+        if (cx == 0) { lo[0] = nc - 1; hi[0] = nc - 1; lo[1] = 0; hi[1] = 1; return 2; }
+        if (cx == nc - 1) { lo[0] = nc - 2; hi[0] = nc - 1; lo[1] = 0; hi[1] = 0; return 2; }
+    }
+    lo[0] = cx > 0 ? cx - 1 : 0;
+    hi[0] = cx < nc - 1 ? cx + 1 : nc - 1;
+    return 1;
+}
+
+// Host helpers
+Grid make_grid(const double mn[2], const double mx[2], const int per[2], double cell_min,
+               int64_t* ncells_out);
+Geo make_geo(const double mn[2], const double mx[2], const int per[2]);
+
+// Device-wide exclusive scans: out[0..n] with out[n] = total. tmp holds scan_tmp_elems(n).
+int64_t scan_tmp_elems(int64_t n);
+cudaError_t scan_exclusive(const int32_t* in, int32_t* out, int64_t n, int32_t* tmp, cudaStream_t s);
+cudaError_t scan_exclusive(const int32_t* in, int64_t* out, int64_t n, int64_t* tmp, cudaStream_t s);
+
+// Counting sort of points (xy of a float2 or float4 array given by stride in floats) by
+// cell, with ascending input index inside each cell (deterministic order).
+// key[n], perm[n] (slot -> input index), count/fill[ncells], start[ncells+1].
+cudaError_t cell_sort(const float* xy, int stride, int64_t n, const Grid& g, int64_t ncells,
+                      int32_t* key, int32_t* perm, int32_t* count, int32_t* fill, int32_t* start,
+                      int32_t* scan_tmp, cudaStream_t s);
+
+inline size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
+
+// Sequential carve-out of a caller workspace.
+struct Carver {
+    char* base;
+    size_t off = 0;
+    template <typename T>
+    T* take(int64_t count) {
+        T* p = base ? reinterpret_cast<T*>(base + off) : nullptr;
+        off += align256(sizeof(T) * (size_t)(count > 0 ? count : 1));
+        return p;
+    }
+};
+
+}  // namespace sph

@@ -1,0 +1,935 @@
+// Fused delta-SPH time step for sm_103a.
+//
+// One step reproduces the reference runner (src/diffSPH/v2/runner.py:37-42):
+//   integrate(simulationStep) with scheme symplecticEuler (modules/integration.py:357-392),
+//   then solveShifting (modules/shifting.py:882-1019, delta+ branch, one iteration).
+//
+// Data layout (structure of arrays, particles in cell-sorted order, rebuilt every step):
+//   Xr[n]  float2  raw positions (never wrapped, like the reference state)
+//   X4[n]  float4  (wrapped x, wrapped y, rho, p)      read by every neighbor loop
+//   V4[n]  float4  (u, v, gradRho^L x, gradRho^L y)    read by pass B
+//   nbr[K][n] int32 candidate lists (slot-major, so a warp's loads of slot k coalesce);
+//                   bit 31 marks a boundary particle
+// Fluid and boundary particles share the arrays; per-step work:
+//   sort by cell -> gather -> candidate lists (radius skin*H)
+//   stage 1: mDBC ghosts -> pass A -> pass B (+ half-step update)
+//   stage 2: mDBC ghosts -> pass A -> pass B (+ final update, max |u|)
+//   shift pass (+ position update)
+// Every pass re-applies the exact reference filter q = r/h <= 1, so the pairs used are
+// exactly the reference's.
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <vector>
+
+#include "../../include/sph103.h"
+#include "sph_internal.cuh"
+
+namespace sph {
+
+enum KernelClass { KC_SORT = 0, KC_GATHER, KC_BUILD, KC_MDBC, KC_PASS_A, KC_PASS_B, KC_SHIFT, KC_COUNT };
+static const char* kClassNames[KC_COUNT] = {"cell_sort", "gather", "build_lists", "mdbc_ghosts",
+                                             "pass_a_gradient", "pass_b_rates", "shift"};
+
+struct Phys {
+    Geo geo;
+    float h;            // support
+    float h_cut;        // cheap pre-reject bound on the squared distance (just above h^2)
+    float skin2;        // candidate radius^2 (slightly enlarged)
+    float m;            // particle mass
+    float dt, dth;      // dt, dt/2
+    KernelCoef kc;
+    Eos eos;
+    float rho0;
+    float diff_coef;    // delta * h / kappa * cs
+    float diff_eps;     // 1e-6 * h
+    int visc;           // 0 viscid, 1 inviscid
+    float v_eps;        // eps * h^2
+    float v_num;        // viscid 8 nu rho0 ; inviscid alpha h cs rho0   (divided by rho_i)
+    int bvisc;
+    float bv_eps, bv_num;
+    float gx, gy;
+    int nF;
+    float W0;           // W(dx/h) for the shifting term
+    float shR, shN, sh_thr;
+    float sh_scale;     // -CFL * (h/kappa*2)^2 (times Ma)
+    float inv_cs;
+    int compute_mach;
+    int density_update;
+    float verlet_lim;   // (skin - 1) * h
+};
+
+struct RhsOut {
+    float* dudt;
+    float* drhodt;
+    float* grad;
+    float* L;
+    float* pressure;
+    float* rho_b;
+};
+
+// ------------------------------------------------------------------------------------
+// upload / download / gather
+// ------------------------------------------------------------------------------------
+__global__ void k_upload(int64_t nF, int64_t nB, const float* __restrict__ xf, const float* __restrict__ uf,
+                         const float* __restrict__ rf, const float* __restrict__ xb, const float* __restrict__ nb,
+                         const float* __restrict__ db, const float* __restrict__ rb, Phys P, float2* Xr, float4* X4,
+                         float4* V4, int32_t* uid, float2* bnormal, float* bdist) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nF + nB) return;
+    float2 x;
+    float2 u = make_float2(0.f, 0.f);
+    float rho;
+    if (i < nF) {
+        x = make_float2(xf[2 * i], xf[2 * i + 1]);
+        u = make_float2(uf[2 * i], uf[2 * i + 1]);
+        rho = rf[i];
+    } else {
+        int64_t b = i - nF;
+        x = make_float2(xb[2 * b], xb[2 * b + 1]);
+        rho = rb ? rb[b] : P.rho0;
+        bnormal[b] = make_float2(nb[2 * b], nb[2 * b + 1]);
+        bdist[b] = db[b];
+    }
+    Xr[i] = x;
+    float2 w = wrap_pos(x, P.geo);
+    X4[i] = make_float4(w.x, w.y, rho, eos_p(rho, P.eos));
+    V4[i] = make_float4(u.x, u.y, 0.f, 0.f);
+    uid[i] = (int32_t)i;
+}
+
+__global__ void k_download(int64_t n, int nF, const int32_t* __restrict__ uid, const float2* __restrict__ Xr,
+                           const float4* __restrict__ X4, const float4* __restrict__ V4, float* xf, float* uf,
+                           float* rf, float* rb) {
+    int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    int o = uid[s];
+    if (o < nF) {
+        if (xf) { xf[2 * o] = Xr[s].x; xf[2 * o + 1] = Xr[s].y; }
+        if (uf) { uf[2 * o] = V4[s].x; uf[2 * o + 1] = V4[s].y; }
+        if (rf) rf[o] = X4[s].z;
+    } else if (rb) {
+        rb[o - nF] = X4[s].z;
+    }
+}
+
+__global__ void k_gather(int64_t n, int nF, const int32_t* __restrict__ perm, const float2* __restrict__ Xr_in,
+                         const float4* __restrict__ X4_in, const float4* __restrict__ V4_in,
+                         const int32_t* __restrict__ uid_in, float2* __restrict__ Xr_out, float4* __restrict__ X4_out,
+                         float4* __restrict__ V4_out, int32_t* __restrict__ uid_out, int32_t* __restrict__ bidx,
+                         uint32_t* __restrict__ words) {
+    int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    int o = perm[s];
+    Xr_out[s] = Xr_in[o];
+    X4_out[s] = X4_in[o];
+    V4_out[s] = V4_in[o];
+    int u = uid_in[o];
+    uid_out[s] = u;
+    if (u >= nF) bidx[atomicAdd(&words[2], 1u)] = (int32_t)s;
+}
+
+// candidate lists: every particle within skin*h (squared test with a margin, so the list
+// is a superset of the exact reference set at every evaluation of the step)
+template <bool PER>
+__global__ void k_build(int64_t n, int K, const float4* __restrict__ X4, const int32_t* __restrict__ uid,
+                        const int32_t* __restrict__ start, Grid g, Phys P, int32_t* __restrict__ nbr,
+                        int32_t* __restrict__ ncnt, uint32_t* __restrict__ words) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (uid[i] >= P.nF) {
+        ncnt[i] = 0;
+        return;
+    }
+    float4 xi = X4[i];
+    float2 pi = make_float2(xi.x, xi.y);
+    int cx = cell_coord(pi.x, g.mn[0], g.inv_cell[0], g.nc[0]);
+    int cy = cell_coord(pi.y, g.mn[1], g.inv_cell[1], g.nc[1]);
+    int rows[3], lo[2], hi[2];
+    int nr = stencil_rows(cy, g, rows);
+    int ncr = stencil_cols(cx, g, lo, hi);
+    int cnt = 0;
+    for (int a = 0; a < nr; ++a) {
+        for (int b = 0; b < ncr; ++b) {
+            int s0 = start[rows[a] * g.nc[0] + lo[b]], s1 = start[rows[a] * g.nc[0] + hi[b] + 1];
+            for (int s = s0; s < s1; ++s) {
+                float4 xj = X4[s];
+                float x0, x1;
+                pair_vec<PER>(pi, make_float2(xj.x, xj.y), P.geo, x0, x1);
+                if (sq_norm_ref(x0, x1) <= P.skin2) {
+                    if (cnt < K) {
+                        int e = s | (uid[s] >= P.nF ? (int)0x80000000 : 0);
+                        nbr[(size_t)cnt * n + i] = e;
+                    }
+                    ++cnt;
+                }
+            }
+        }
+    }
+    if (cnt > K) {
+        atomicOr(&words[0], SPH_FLAG_CAPACITY);
+        cnt = K;
+    }
+    ncnt[i] = cnt;
+}
+
+// ------------------------------------------------------------------------------------
+// mDBC boundary density (src/diffSPH/v2/modules/mDBC.py:9-36 ghosts, :50-163 density)
+// ------------------------------------------------------------------------------------
+template <bool PER>
+__global__ void k_mdbc(int nB, const int32_t* __restrict__ bidx, const int32_t* __restrict__ uid,
+                       const float2* __restrict__ Xr, float4* X4, const float2* __restrict__ bnormal,
+                       const float* __restrict__ bdist, const int32_t* __restrict__ start, Grid g, Phys P,
+                       float* __restrict__ rho_b_out) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nB) return;
+    int s = bidx[k];
+    int b = uid[s] - P.nF;
+    float2 xb = Xr[s];
+    float2 nrm = bnormal[b];
+    float d = bdist[b];
+    // mappingDistance = d + max(d, -h); ghost = x_b + mappingDistance * n
+    float mapd = __fadd_rn(d, fmaxf(d, -P.h));
+    float2 gp = make_float2(__fadd_rn(xb.x, __fmul_rn(mapd, nrm.x)), __fadd_rn(xb.y, __fmul_rn(mapd, nrm.y)));
+    float2 gw = wrap_pos(gp, P.geo);
+    int cx = cell_coord(gw.x, g.mn[0], g.inv_cell[0], g.nc[0]);
+    int cy = cell_coord(gw.y, g.mn[1], g.inv_cell[1], g.nc[1]);
+    int rows[3], lo[2], hi[2];
+    int nr = stencil_rows(cy, g, rows);
+    int ncr = stencil_cols(cx, g, lo, hi);
+    float num = 0.f, den = 0.f, gs0 = 0.f, gs1 = 0.f, vg0 = 0.f, vg1 = 0.f, ps0 = 0.f, ps1 = 0.f;
+    float pm00 = 0.f, pm01 = 0.f, pm10 = 0.f, pm11 = 0.f;
+    int cnt = 0;
+    for (int a = 0; a < nr; ++a) {
+        for (int c = 0; c < ncr; ++c) {
+            int s0 = start[rows[a] * g.nc[0] + lo[c]], s1 = start[rows[a] * g.nc[0] + hi[c] + 1];
+            for (int j = s0; j < s1; ++j) {
+                if (uid[j] >= P.nF) continue;
+                float4 xj = X4[j];
+                float x0, x1;
+                pair_vec<PER>(gw, make_float2(xj.x, xj.y), P.geo, x0, x1);
+                float sq = sq_norm_ref(x0, x1);
+                if (sq > P.h_cut) continue;
+                float r, q;
+                if (!exact_in(sq, P.h, r, q)) continue;
+                float den_r = __fadd_rn(r, 1e-7f);
+                float xh0 = __fdiv_rn(x0, den_r), xh1 = __fdiv_rn(x1, den_r);
+                float W = wendland_w(q, P.kc);
+                float dW = wendland_dw(q, P.kc);
+                float g0 = xh0 * dW, g1 = xh1 * dW;
+                float V = P.m / xj.z;
+                num += P.m * W;
+                den += V * W;
+                float k0 = V * g0, k1 = V * g1;
+                gs0 += xj.z * k0;
+                gs1 += xj.z * k1;
+                vg0 += k0;
+                vg1 += k1;
+                float xr = -q * P.h;
+                float xi0 = xh0 * xr, xi1 = xh1 * xr;
+                float vw = V * W;
+                ps0 += xi0 * vw;
+                ps1 += xi1 * vw;
+                pm00 += xi0 * k0;
+                pm01 += xi0 * k1;
+                pm10 += xi1 * k0;
+                pm11 += xi1 * k1;
+                ++cnt;
+            }
+        }
+    }
+    float rho;
+    if (cnt > 5) {
+        double A[9] = {den, ps0, ps1, vg0, pm00, pm01, vg1, pm10, pm11};
+        double Pi[9];
+        pinv3_f64(A, Pi, 3.0 * 1.1920928955078125e-07);
+        double r0 = Pi[0] * num + Pi[1] * gs0 + Pi[2] * gs1;
+        double r1 = Pi[3] * num + Pi[4] * gs0 + Pi[5] * gs1;
+        double r2 = Pi[6] * num + Pi[7] * gs0 + Pi[8] * gs1;
+        float rel0 = __fsub_rn(xb.x, gp.x), rel1 = __fsub_rn(xb.y, gp.y);
+        rho = (float)(r0 + (double)rel0 * r1 + (double)rel1 * r2);
+    } else if (cnt > 0) {
+        rho = num / (den + 1e-7f);
+    } else {
+        rho = P.rho0;
+    }
+    X4[s].z = rho;
+    X4[s].w = eos_p(rho, P.eos);
+    if (rho_b_out) rho_b_out[b] = rho;
+}
+
+// ------------------------------------------------------------------------------------
+// Pass A: normalisation matrix, its pseudo-inverse and the renormalised density gradient
+//   M_i = sum_j (-r x_ij) (m_j/rho_j gradW)       (normalizationMatrices.py:18-23, fluid + boundary)
+//   M_i = I where the fluid neighbor count < 4; L_i = pinv2x2(M_i)  (deltaPlus.py:240-252)
+//   gradRho^L_i = L_i sum_fluid (rho_i - rho_j) V_j gradW + sum_boundary (rho_i - rho_j) V_j gradW
+//                                                 (densityDiffusion.py:7-46, deltaPlus.py:256-262)
+// ------------------------------------------------------------------------------------
+template <bool PER>
+__global__ void __launch_bounds__(256) k_pass_a(int64_t n, const float4* __restrict__ X4, float4* __restrict__ V4,
+                                                const int32_t* __restrict__ nbr, const int32_t* __restrict__ ncnt,
+                                                const int32_t* __restrict__ uid, Phys P, RhsOut out) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int cnt = ncnt[i];
+    if (cnt == 0) return;  // boundary rows
+    float4 xi = X4[i];
+    float2 pi = make_float2(xi.x, xi.y);
+    float M00 = 0.f, M01 = 0.f, M10 = 0.f, M11 = 0.f;
+    float gf0 = 0.f, gf1 = 0.f, gb0 = 0.f, gb1 = 0.f;
+    int nf = 0;
+    for (int k = 0; k < cnt; ++k) {
+        int e = __ldg(&nbr[(size_t)k * n + i]);
+        int j = e & 0x7fffffff;
+        float4 xj = __ldg(&X4[j]);
+        float x0, x1;
+        pair_vec<PER>(pi, make_float2(xj.x, xj.y), P.geo, x0, x1);
+        float sq = sq_norm_ref(x0, x1);
+        if (sq > P.h_cut) continue;
+        float r, q;
+        if (!exact_in(sq, P.h, r, q)) continue;
+        float den_r = __fadd_rn(r, 1e-7f);
+        float xh0 = __fdiv_rn(x0, den_r), xh1 = __fdiv_rn(x1, den_r);
+        float dW = wendland_dw(q, P.kc);
+        float V = P.m / xj.z;
+        float k0 = V * (xh0 * dW), k1 = V * (xh1 * dW);
+        float dr = -(q * P.h);
+        float d0 = dr * xh0, d1 = dr * xh1;
+        M00 += d0 * k0;
+        M01 += d0 * k1;
+        M10 += d1 * k0;
+        M11 += d1 * k1;
+        float drho = xi.z - xj.z;
+        if (e < 0) {
+            gb0 += drho * k0;
+            gb1 += drho * k1;
+        } else {
+            gf0 += drho * k0;
+            gf1 += drho * k1;
+            ++nf;
+        }
+    }
+    if (nf < 4) {
+        M00 = 1.f; M01 = 0.f; M10 = 0.f; M11 = 1.f;
+    }
+    float L[4];
+    pinv2x2_ref(M00, M01, M10, M11, L);
+    float g0 = L[0] * gf0 + L[1] * gf1 + gb0;
+    float g1 = L[2] * gf0 + L[3] * gf1 + gb1;
+    *reinterpret_cast<float2*>(&V4[i].z) = make_float2(g0, g1);
+    if (out.grad || out.L) {
+        int o = uid[i];
+        if (out.grad) { out.grad[2 * o] = g0; out.grad[2 * o + 1] = g1; }
+        if (out.L) { out.L[4 * o] = L[0]; out.L[4 * o + 1] = L[1]; out.L[4 * o + 2] = L[2]; out.L[4 * o + 3] = L[3]; }
+    }
+}
+
+// ------------------------------------------------------------------------------------
+// Pass B: rates of one right-hand side and the fused integrator stage.
+//   continuity   -sum m_j (u_j - u_i).gradW rho_i/rho_j          (momentumEquation.py:6-39)
+//   diffusion    delta h/kappa cs sum psi_ij . V_j gradW (fluid)   (densityDiffusion.py:49-73)
+//   pressure     -(1/rho_i) sum (p_i + p_j) V_j gradW              (pressureForce.py:10-12)
+//   viscosity    c/rho_i sum V_j pi_ij gradW                       (viscosity.py:123-218,
+//                                                                   boundaryViscosity.py:123-219)
+//   gravity                                                        (gravity.py:8-29)
+// MODE 0: write the rates (original order); 1: half step (integration.py:23-32);
+// MODE 2: final symplectic Euler update (integration.py:381-392, 439-513).
+// ------------------------------------------------------------------------------------
+template <bool PER, int MODE>
+__global__ void __launch_bounds__(256) k_pass_b(int64_t n, const float4* __restrict__ X4, const float4* __restrict__ V4,
+                                                const int32_t* __restrict__ nbr, const int32_t* __restrict__ ncnt,
+                                                const int32_t* __restrict__ uid, Phys P, RhsOut out,
+                                                float2* __restrict__ Xr, const float4* __restrict__ X4n,
+                                                const float4* __restrict__ V4n, float4* __restrict__ X4o,
+                                                float4* __restrict__ V4o, uint32_t* __restrict__ words) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int cnt = ncnt[i];
+    if (cnt == 0) {  // boundary rows: static, carried over to the next stage
+        if (MODE != 0) {
+            X4o[i] = X4[i];
+            V4o[i] = V4[i];
+        }
+        return;
+    }
+    float4 xi = X4[i];
+    float4 vi = V4[i];
+    float2 pi = make_float2(xi.x, xi.y);
+    float rhoi = xi.z, pri = xi.w;
+    float ac = 0.f, ad = 0.f, ap0 = 0.f, ap1 = 0.f, av0 = 0.f, av1 = 0.f, ab0 = 0.f, ab1 = 0.f;
+    for (int k = 0; k < cnt; ++k) {
+        int e = __ldg(&nbr[(size_t)k * n + i]);
+        int j = e & 0x7fffffff;
+        float4 xj = __ldg(&X4[j]);
+        float x0, x1;
+        pair_vec<PER>(pi, make_float2(xj.x, xj.y), P.geo, x0, x1);
+        float sq = sq_norm_ref(x0, x1);
+        if (sq > P.h_cut) continue;
+        float r, q;
+        if (!exact_in(sq, P.h, r, q)) continue;
+        float4 vj = __ldg(&V4[j]);
+        float den_r = __fadd_rn(r, 1e-7f);
+        float xh0 = __fdiv_rn(x0, den_r), xh1 = __fdiv_rn(x1, den_r);
+        float dW = wendland_dw(q, P.kc);
+        float g0 = xh0 * dW, g1 = xh1 * dW;
+        float rhoj = xj.z;
+        float V = P.m / rhoj;
+        // continuity
+        float kq = ((vj.x - vi.x) * P.m) * g0 + ((vj.y - vi.y) * P.m) * g1;
+        ac += kq * rhoi / rhoj;
+        // pressure
+        float pp = (pri + xj.w) * V;
+        ap0 += pp * g0;
+        ap1 += pp * g1;
+        // viscosity
+        float vr = (vi.x - vj.x) * xh0 + (vi.y - vj.y) * xh1;
+        float rr = q * P.h;
+        if (e < 0) {
+            float piv = vr / (rr + P.bv_eps);
+            float Vb = P.bvisc ? P.m / (rhoi + rhoj) : V;
+            float kv = Vb * piv;
+            ab0 += kv * g0;
+            ab1 += kv * g1;
+        } else {
+            float piv = vr / (rr + P.v_eps);
+            float kv = V * piv;
+            av0 += kv * g0;
+            av1 += kv * g1;
+            // delta-SPH density diffusion (fluid neighbors only)
+            float rij = 2.f * (rhoj - rhoi) / (rr + P.diff_eps);
+            float psi0 = -rij * xh0 + (vi.z + vj.z);
+            float psi1 = -rij * xh1 + (vi.w + vj.w);
+            ad += psi0 * (V * g0) + psi1 * (V * g1);
+        }
+    }
+    float vcoef = (P.visc ? P.v_num : P.v_num) / rhoi;
+    float bcoef = P.bv_num / rhoi;
+    float du0 = (-ap0 / rhoi + P.gx) + (vcoef * av0 + bcoef * ab0);
+    float du1 = (-ap1 / rhoi + P.gy) + (vcoef * av1 + bcoef * ab1);
+    float drho = -ac + P.diff_coef * ad;
+    if (MODE == 0) {
+        int o = uid[i];
+        out.dudt[2 * o] = du0;
+        out.dudt[2 * o + 1] = du1;
+        out.drhodt[o] = drho;
+        if (out.pressure) out.pressure[o] = pri;
+        return;
+    }
+    float2 x = Xr[i];
+    if (MODE == 1) {
+        // updateStates(dt/2): x += u dt/2, u += dudt dt/2, rho += drhodt dt/2
+        float2 xh = make_float2(__fadd_rn(x.x, __fmul_rn(vi.x, P.dth)), __fadd_rn(x.y, __fmul_rn(vi.y, P.dth)));
+        float u0 = __fadd_rn(vi.x, __fmul_rn(du0, P.dth)), u1 = __fadd_rn(vi.y, __fmul_rn(du1, P.dth));
+        float rh = __fadd_rn(rhoi, __fmul_rn(drho, P.dth));
+        float2 w = wrap_pos(xh, P.geo);
+        X4o[i] = make_float4(w.x, w.y, rh, eos_p(rh, P.eos));
+        V4o[i] = make_float4(u0, u1, 0.f, 0.f);
+        float dx0 = __fsub_rn(xh.x, x.x), dx1 = __fsub_rn(xh.y, x.y);
+        if (2.f * sqrtf(dx0 * dx0 + dx1 * dx1) > P.verlet_lim) atomicOr(&words[0], SPH_FLAG_VERLET);
+    } else {
+        // v' = v + dudt dt; x' = x + 0.5 (v + v') dt; rho' per density_update
+        float4 vn = V4n[i];
+        float4 xn = X4n[i];
+        float u0 = __fadd_rn(vn.x, __fmul_rn(du0, P.dt)), u1 = __fadd_rn(vn.y, __fmul_rn(du1, P.dt));
+        float d0 = __fmul_rn(__fmul_rn(0.5f, __fadd_rn(vn.x, u0)), P.dt);
+        float d1 = __fmul_rn(__fmul_rn(0.5f, __fadd_rn(vn.y, u1)), P.dt);
+        float2 xp = make_float2(__fadd_rn(x.x, d0), __fadd_rn(x.y, d1));
+        float rnew;
+        if (P.density_update == 0) {
+            rnew = rhoi;  // the half-step density (the reference's observable update)
+        } else {
+            float eps = __fdiv_rn(__fmul_rn(-P.dt, drho), rhoi);
+            rnew = __fdiv_rn(__fmul_rn(xn.z, __fsub_rn(2.f, eps)), __fadd_rn(2.f, eps));
+        }
+        Xr[i] = xp;
+        float2 w = wrap_pos(xp, P.geo);
+        X4o[i] = make_float4(w.x, w.y, rnew, eos_p(rnew, P.eos));
+        V4o[i] = make_float4(u0, u1, 0.f, 0.f);
+        float sp = __fsqrt_rn(__fmaf_rn(u1, u1, __fmul_rn(u0, u0)));
+        atomicMax(&words[1], __float_as_uint(sp));
+        float dx0 = __fsub_rn(xp.x, x.x), dx1 = __fsub_rn(xp.y, x.y);
+        if (2.f * sqrtf(dx0 * dx0 + dx1 * dx1) > P.verlet_lim) atomicOr(&words[0], SPH_FLAG_VERLET);
+        if (!isfinite(u0) || !isfinite(u1) || !isfinite(rnew) || !isfinite(xp.x) || !isfinite(xp.y))
+            atomicOr(&words[0], SPH_FLAG_NONFINITE);
+    }
+}
+
+// ------------------------------------------------------------------------------------
+// delta+ shifting (shifting.py:119-147, applied as in solveShifting :990-1005)
+//   dx_i = clamp(-CFL Ma (2h/kappa)^2 sum (1 + R (W/W0)^n) m_j/(rho_i+rho_j) gradW, +-thr dx)
+// ------------------------------------------------------------------------------------
+template <bool PER>
+__global__ void __launch_bounds__(256) k_shift(int64_t n, const float4* __restrict__ X4, const float4* __restrict__ V4,
+                                               const int32_t* __restrict__ nbr, const int32_t* __restrict__ ncnt,
+                                               Phys P, float2* __restrict__ Xr, float4* __restrict__ X4o,
+                                               float4* __restrict__ V4o, const uint32_t* __restrict__ words,
+                                               int enabled, const int32_t* __restrict__ uid, float* __restrict__ dx_out) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int cnt = ncnt[i];
+    float4 xi = X4[i];
+    float4 vi = V4[i];
+    if (cnt == 0 || !enabled) {
+        X4o[i] = xi;
+        V4o[i] = vi;
+        if (dx_out && cnt != 0) {
+            int o = uid[i];
+            dx_out[2 * o] = 0.f;
+            dx_out[2 * o + 1] = 0.f;
+        }
+        return;
+    }
+    float2 pi = make_float2(xi.x, xi.y);
+    float s0 = 0.f, s1 = 0.f;
+    for (int k = 0; k < cnt; ++k) {
+        int e = __ldg(&nbr[(size_t)k * n + i]);
+        int j = e & 0x7fffffff;
+        float4 xj = __ldg(&X4[j]);
+        float x0, x1;
+        pair_vec<PER>(pi, make_float2(xj.x, xj.y), P.geo, x0, x1);
+        float sq = sq_norm_ref(x0, x1);
+        if (sq > P.h_cut) continue;
+        float r, q;
+        if (!exact_in(sq, P.h, r, q)) continue;
+        float den_r = __fadd_rn(r, 1e-7f);
+        float xh0 = __fdiv_rn(x0, den_r), xh1 = __fdiv_rn(x1, den_r);
+        float W = wendland_w(q, P.kc);
+        float dW = wendland_dw(q, P.kc);
+        float kk = W / P.W0;
+        float term = 1.f + P.shR * powf(kk, P.shN);
+        float dens = P.m / (xi.z + xj.z);
+        float c = term * dens;
+        s0 += c * (xh0 * dW);
+        s1 += c * (xh1 * dW);
+    }
+    float Ma = P.compute_mach ? __uint_as_float(words[1]) * P.inv_cs : 0.1f;
+    float sc = P.sh_scale * Ma;
+    // update = clamp(-(sc * s)); x_new = x - update; the reference then adds (x_new - x) to x
+    float up0 = fminf(fmaxf(-(sc * s0), -P.sh_thr), P.sh_thr);
+    float up1 = fminf(fmaxf(-(sc * s1), -P.sh_thr), P.sh_thr);
+    float2 x = Xr[i];
+    float y0 = __fsub_rn(x.x, up0), y1 = __fsub_rn(x.y, up1);
+    float2 xn = make_float2(__fadd_rn(x.x, __fsub_rn(y0, x.x)), __fadd_rn(x.y, __fsub_rn(y1, x.y)));
+    Xr[i] = xn;
+    float2 w = wrap_pos(xn, P.geo);
+    X4o[i] = make_float4(w.x, w.y, xi.z, xi.w);
+    V4o[i] = vi;
+    if (dx_out) {
+        int o = uid[i];
+        dx_out[2 * o] = __fsub_rn(y0, x.x);
+        dx_out[2 * o + 1] = __fsub_rn(y1, x.y);
+    }
+}
+
+// max |u| over all particles (the Mach number of shifting.py:139-142)
+__global__ void k_maxvel(int64_t n, const float4* __restrict__ V4, uint32_t* __restrict__ words) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    float sp = 0.f;
+    if (i < n) {
+        float4 v = V4[i];
+        sp = __fsqrt_rn(__fmaf_rn(v.y, v.y, __fmul_rn(v.x, v.x)));
+    }
+    for (int o = 16; o > 0; o >>= 1) sp = fmaxf(sp, __shfl_xor_sync(0xffffffffu, sp, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(&words[1], __float_as_uint(sp));
+}
+
+}  // namespace sph
+
+using namespace sph;
+
+// ------------------------------------------------------------------------------------
+// Solver handle
+// ------------------------------------------------------------------------------------
+struct sph_solver {
+    sph_params_t prm;
+    Phys P;
+    int64_t nF, nB, n;
+    int K;
+    Grid grid;
+    int64_t ncells;
+    bool periodic;
+    float2 *Xr, *Xr_t;
+    float4 *Xc, *Xh, *Xf, *Xt;
+    float4 *Vc, *Vh, *Vf, *Vt;
+    int32_t *uid, *uid_t;
+    int32_t *key, *perm, *count, *fill, *start, *scan32;
+    int32_t *nbr, *ncnt, *bidx;
+    uint32_t* words;  // [0] flags, [1] max |u| bits, [2] boundary count
+    float2* bnormal;
+    float* bdist;
+    // timing
+    uint32_t timing_mask = 0;
+    struct Ev { cudaEvent_t a, b; int cls; };
+    std::vector<Ev> pool;
+    size_t used = 0;
+};
+
+static size_t solver_layout(const sph_params_t* p, int64_t nF, int64_t nB, void* ws, sph_solver* S) {
+    int64_t n = nF + nB;
+    int per[2] = {p->domain.periodic[0], p->domain.periodic[1]};
+    int64_t ncells = 0;
+    Grid g = make_grid(p->domain.min, p->domain.max, per, p->support * p->skin * (1.0 + 1e-4), &ncells);
+    Carver c{(char*)ws};
+    float2* Xr = c.take<float2>(n);
+    float2* Xr_t = c.take<float2>(n);
+    float4* X[4];
+    float4* V[4];
+    for (int k = 0; k < 4; ++k) X[k] = c.take<float4>(n);
+    for (int k = 0; k < 4; ++k) V[k] = c.take<float4>(n);
+    int32_t* uid = c.take<int32_t>(n);
+    int32_t* uid_t = c.take<int32_t>(n);
+    int32_t* key = c.take<int32_t>(n);
+    int32_t* perm = c.take<int32_t>(n);
+    int32_t* count = c.take<int32_t>(ncells);
+    int32_t* fill = c.take<int32_t>(ncells);
+    int32_t* start = c.take<int32_t>(ncells + 1);
+    int32_t* scan32 = c.take<int32_t>(scan_tmp_elems(ncells));
+    int32_t* nbr = c.take<int32_t>((int64_t)p->capacity * n);
+    int32_t* ncnt = c.take<int32_t>(n);
+    int32_t* bidx = c.take<int32_t>(nB);
+    uint32_t* words = c.take<uint32_t>(8);
+    float2* bnormal = c.take<float2>(nB);
+    float* bdist = c.take<float>(nB);
+    if (S) {
+        S->n = n;
+        S->grid = g;
+        S->ncells = ncells;
+        S->Xr = Xr; S->Xr_t = Xr_t;
+        S->Xc = X[0]; S->Xh = X[1]; S->Xf = X[2]; S->Xt = X[3];
+        S->Vc = V[0]; S->Vh = V[1]; S->Vf = V[2]; S->Vt = V[3];
+        S->uid = uid; S->uid_t = uid_t;
+        S->key = key; S->perm = perm; S->count = count; S->fill = fill; S->start = start; S->scan32 = scan32;
+        S->nbr = nbr; S->ncnt = ncnt; S->bidx = bidx; S->words = words;
+        S->bnormal = bnormal; S->bdist = bdist;
+    }
+    return c.off;
+}
+
+static int check_params(const sph_params_t* p, int64_t nF, int64_t nB) {
+    if (!p || nF < 1 || nB < 0 || nF + nB >= ((int64_t)1 << 31) - 1) return SPH_ERR_ARGUMENT;
+    if (!(p->support > 0) || !(p->dx > 0) || !(p->mass > 0) || !(p->rho0 > 0) || !(p->cs > 0)) return SPH_ERR_ARGUMENT;
+    if (!(p->skin >= 1.0) || p->capacity < 1 || !(p->kernel_scale > 0)) return SPH_ERR_ARGUMENT;
+    for (int a = 0; a < 2; ++a)
+        if (!(p->domain.max[a] > p->domain.min[a])) return SPH_ERR_ARGUMENT;
+    int per[2] = {p->domain.periodic[0], p->domain.periodic[1]};
+    int64_t ncells = 0;
+    make_grid(p->domain.min, p->domain.max, per, p->support * p->skin * (1.0 + 1e-4), &ncells);
+    if (ncells > ((int64_t)1 << 28)) return SPH_ERR_ARGUMENT;
+    if ((int64_t)p->capacity * (nF + nB) >= ((int64_t)1 << 40)) return SPH_ERR_ARGUMENT;
+    return SPH_OK;
+}
+
+static Phys make_phys(const sph_params_t* p, int64_t nF) {
+    Phys P;
+    int per[2] = {p->domain.periodic[0], p->domain.periodic[1]};
+    P.geo = make_geo(p->domain.min, p->domain.max, per);
+    double h = p->support;
+    P.h = (float)h;
+    P.h_cut = (float)(h * h * (1.0 + 1e-5));
+    double rs = p->skin * h;
+    P.skin2 = (float)(rs * rs * (1.0 + 1e-5));
+    P.m = (float)p->mass;
+    P.dt = (float)p->dt;
+    P.dth = (float)(p->dt / 2.0);
+    P.kc.cw = (float)(kCd / (h * h));
+    P.kc.cg = (float)(kCd / (h * h * h));
+    P.eos.B = (float)(p->rho0 * p->cs * p->cs / p->gamma);
+    P.eos.rho0 = (float)p->rho0;
+    P.eos.gamma = (float)p->gamma;
+    P.rho0 = (float)p->rho0;
+    P.diff_coef = (float)((float)((float)p->delta * (float)h) / (float)p->kernel_scale * (float)p->cs);
+    P.diff_eps = (float)(1e-6f * (float)h);
+    P.visc = p->visc_scheme;
+    P.v_eps = (float)p->eps * (float)(h * h);
+    P.v_num = p->visc_scheme ? (float)((float)((float)p->alpha * (float)h) * (float)p->cs * (float)p->rho0)
+                             : (float)(2.0 * (2 + 2) * p->nu * p->rho0);
+    P.bvisc = p->bvisc_scheme;
+    P.bv_eps = (float)p->b_eps * (float)(h * h);
+    P.bv_num = p->bvisc_scheme ? (float)((float)((float)p->b_alpha * (float)h) * (float)p->cs * (float)p->rho0)
+                               : (float)(2.0 * (2 + 2) * p->b_nu * p->rho0);
+    P.gx = p->gravity_on ? (float)p->gravity[0] : 0.f;
+    P.gy = p->gravity_on ? (float)p->gravity[1] : 0.f;
+    P.nF = (int)nF;
+    // W0 = W(dx/h, h) evaluated in fp32 like the reference (shifting.py:122)
+    {
+        float q0 = (float)p->dx / (float)h;
+        float om = 1.f - q0;
+        float hh = (float)h;
+        P.W0 = (om * om) * (om * om) * (1.f + 4.f * q0) * (float)(7.0 / M_PI) / (hh * hh);
+    }
+    P.shR = (float)p->shift_R;
+    P.shN = (float)p->shift_n;
+    P.sh_thr = (float)(p->shift_threshold * p->dx);
+    {
+        float t = (float)h / (float)p->kernel_scale * 2.f;
+        P.sh_scale = -(float)p->shift_CFL * (t * t);
+    }
+    P.inv_cs = (float)(1.0 / p->cs);
+    P.compute_mach = p->compute_mach;
+    P.density_update = p->density_update;
+    P.verlet_lim = (float)((p->skin - 1.0) * h);
+    return P;
+}
+
+extern "C" int sph_solver_workspace_bytes(const sph_params_t* params, int64_t n_fluid, int64_t n_boundary,
+                                          size_t* bytes) {
+    int st = check_params(params, n_fluid, n_boundary);
+    if (st) return st;
+    if (!bytes) return SPH_ERR_ARGUMENT;
+    *bytes = solver_layout(params, n_fluid, n_boundary, nullptr, nullptr);
+    return SPH_OK;
+}
+
+extern "C" int sph_solver_create(const sph_params_t* params, int64_t n_fluid, int64_t n_boundary, void* workspace,
+                                 size_t workspace_bytes, sph_solver_t** out) {
+    int st = check_params(params, n_fluid, n_boundary);
+    if (st) return st;
+    if (!out) return SPH_ERR_ARGUMENT;
+    size_t need = solver_layout(params, n_fluid, n_boundary, nullptr, nullptr);
+    if (!workspace || workspace_bytes < need) return SPH_ERR_WORKSPACE;
+    if (((uintptr_t)workspace & 255) != 0) return SPH_ERR_ARGUMENT;
+    sph_solver* S = new sph_solver();
+    S->prm = *params;
+    S->nF = n_fluid;
+    S->nB = n_boundary;
+    S->K = params->capacity;
+    solver_layout(params, n_fluid, n_boundary, workspace, S);
+    S->P = make_phys(params, n_fluid);
+    S->periodic = params->domain.periodic[0] || params->domain.periodic[1];
+    *out = S;
+    return SPH_OK;
+}
+
+extern "C" void sph_solver_destroy(sph_solver_t* s) {
+    if (!s) return;
+    for (auto& e : s->pool) {
+        cudaEventDestroy(e.a);
+        cudaEventDestroy(e.b);
+    }
+    delete s;
+}
+
+static inline unsigned blocks_for(int64_t n) { return (unsigned)((n + kBlock - 1) / kBlock); }
+
+// timing brackets (only for classes in the mask)
+static void tbeg(sph_solver* S, int cls, cudaStream_t st) {
+    if (!(S->timing_mask & (1u << cls))) return;
+    if (S->used == S->pool.size()) {
+        sph_solver::Ev e;
+        cudaEventCreate(&e.a);
+        cudaEventCreate(&e.b);
+        S->pool.push_back(e);
+    }
+    S->pool[S->used].cls = cls;
+    cudaEventRecord(S->pool[S->used].a, st);
+}
+static void tend(sph_solver* S, int cls, cudaStream_t st) {
+    if (!(S->timing_mask & (1u << cls))) return;
+    cudaEventRecord(S->pool[S->used].b, st);
+    S->used++;
+}
+
+extern "C" int sph_solver_upload(sph_solver_t* S, const float* x_fluid, const float* u_fluid, const float* rho_fluid,
+                                 const float* x_boundary, const float* normal_boundary, const float* dist_boundary,
+                                 const float* rho_boundary, sph_stream_t stream) {
+    if (!S || !x_fluid || !u_fluid || !rho_fluid) return SPH_ERR_ARGUMENT;
+    if (S->nB > 0 && (!x_boundary || !normal_boundary || !dist_boundary)) return SPH_ERR_ARGUMENT;
+    cudaStream_t st = (cudaStream_t)stream;
+    k_upload<<<blocks_for(S->n), kBlock, 0, st>>>(S->nF, S->nB, x_fluid, u_fluid, rho_fluid, x_boundary,
+                                                    normal_boundary, dist_boundary, rho_boundary, S->P, S->Xr, S->Xc,
+                                                    S->Vc, S->uid, S->bnormal, S->bdist);
+    if (cudaMemsetAsync(S->words, 0, sizeof(uint32_t) * 8, st) != cudaSuccess) return SPH_ERR_CUDA;
+    return cudaGetLastError() == cudaSuccess ? SPH_OK : SPH_ERR_CUDA;
+}
+
+// sort by cell, gather the state into the new order, build candidate lists
+static int rebuild(sph_solver* S, cudaStream_t st) {
+    tbeg(S, KC_SORT, st);
+    if (cell_sort((const float*)S->Xc, 4, S->n, S->grid, S->ncells, S->key, S->perm, S->count, S->fill, S->start,
+                  S->scan32, st) != cudaSuccess)
+        return SPH_ERR_CUDA;
+    tend(S, KC_SORT, st);
+    if (cudaMemsetAsync(S->words + 2, 0, sizeof(uint32_t), st) != cudaSuccess) return SPH_ERR_CUDA;
+    tbeg(S, KC_GATHER, st);
+    k_gather<<<blocks_for(S->n), kBlock, 0, st>>>(S->n, (int)S->nF, S->perm, S->Xr, S->Xc, S->Vc, S->uid, S->Xr_t,
+                                                    S->Xt, S->Vt, S->uid_t, S->bidx, S->words);
+    tend(S, KC_GATHER, st);
+    std::swap(S->Xr, S->Xr_t);
+    std::swap(S->Xc, S->Xt);
+    std::swap(S->Vc, S->Vt);
+    std::swap(S->uid, S->uid_t);
+    tbeg(S, KC_BUILD, st);
+    if (S->periodic)
+        k_build<true><<<blocks_for(S->n), kBlock, 0, st>>>(S->n, S->K, S->Xc, S->uid, S->start, S->grid, S->P, S->nbr,
+                                                           S->ncnt, S->words);
+    else
+        k_build<false><<<blocks_for(S->n), kBlock, 0, st>>>(S->n, S->K, S->Xc, S->uid, S->start, S->grid, S->P,
+                                                            S->nbr, S->ncnt, S->words);
+    tend(S, KC_BUILD, st);
+    return cudaGetLastError() == cudaSuccess ? SPH_OK : SPH_ERR_CUDA;
+}
+
+static void launch_mdbc(sph_solver* S, float4* X4, float* rho_b_out, cudaStream_t st) {
+    if (S->nB == 0) return;
+    tbeg(S, KC_MDBC, st);
+    if (S->periodic)
+        k_mdbc<true><<<blocks_for(S->nB), kBlock, 0, st>>>((int)S->nB, S->bidx, S->uid, S->Xr, X4, S->bnormal,
+                                                           S->bdist, S->start, S->grid, S->P, rho_b_out);
+    else
+        k_mdbc<false><<<blocks_for(S->nB), kBlock, 0, st>>>((int)S->nB, S->bidx, S->uid, S->Xr, X4, S->bnormal,
+                                                            S->bdist, S->start, S->grid, S->P, rho_b_out);
+    tend(S, KC_MDBC, st);
+}
+
+static void launch_a(sph_solver* S, float4* X4, float4* V4, RhsOut o, cudaStream_t st) {
+    tbeg(S, KC_PASS_A, st);
+    if (S->periodic)
+        k_pass_a<true><<<blocks_for(S->n), kBlock, 0, st>>>(S->n, X4, V4, S->nbr, S->ncnt, S->uid, S->P, o);
+    else
+        k_pass_a<false><<<blocks_for(S->n), kBlock, 0, st>>>(S->n, X4, V4, S->nbr, S->ncnt, S->uid, S->P, o);
+    tend(S, KC_PASS_A, st);
+}
+
+template <int MODE>
+static void launch_b(sph_solver* S, float4* X4, float4* V4, RhsOut o, float4* X4o, float4* V4o, cudaStream_t st) {
+    tbeg(S, KC_PASS_B, st);
+    if (S->periodic)
+        k_pass_b<true, MODE><<<blocks_for(S->n), kBlock, 0, st>>>(S->n, X4, V4, S->nbr, S->ncnt, S->uid, S->P, o,
+                                                                  S->Xr, S->Xc, S->Vc, X4o, V4o, S->words);
+    else
+        k_pass_b<false, MODE><<<blocks_for(S->n), kBlock, 0, st>>>(S->n, X4, V4, S->nbr, S->ncnt, S->uid, S->P, o,
+                                                                   S->Xr, S->Xc, S->Vc, X4o, V4o, S->words);
+    tend(S, KC_PASS_B, st);
+}
+
+static int run_stages(sph_solver* S, cudaStream_t st) {
+    RhsOut none = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    int rc = rebuild(S, st);
+    if (rc) return rc;
+    // stage 1 at t^n
+    launch_mdbc(S, S->Xc, nullptr, st);
+    launch_a(S, S->Xc, S->Vc, none, st);
+    launch_b<1>(S, S->Xc, S->Vc, none, S->Xh, S->Vh, st);
+    // stage 2 at the half step; the epilogue also reduces max |u'| for the shifting Mach number
+    launch_mdbc(S, S->Xh, nullptr, st);
+    launch_a(S, S->Xh, S->Vh, none, st);
+    if (cudaMemsetAsync(S->words + 1, 0, sizeof(uint32_t), st) != cudaSuccess) return SPH_ERR_CUDA;
+    launch_b<2>(S, S->Xh, S->Vh, none, S->Xf, S->Vf, st);
+    return cudaGetLastError() == cudaSuccess ? SPH_OK : SPH_ERR_CUDA;
+}
+
+static void launch_shift(sph_solver* S, float4* Xin, float4* Vin, float4* Xout, float4* Vout, float* dx_out,
+                         cudaStream_t st) {
+    tbeg(S, KC_SHIFT, st);
+    if (S->periodic)
+        k_shift<true><<<blocks_for(S->n), kBlock, 0, st>>>(S->n, Xin, Vin, S->nbr, S->ncnt, S->P, S->Xr, Xout, Vout,
+                                                           S->words, S->prm.shift_on, S->uid, dx_out);
+    else
+        k_shift<false><<<blocks_for(S->n), kBlock, 0, st>>>(S->n, Xin, Vin, S->nbr, S->ncnt, S->P, S->Xr, Xout, Vout,
+                                                            S->words, S->prm.shift_on, S->uid, dx_out);
+    tend(S, KC_SHIFT, st);
+}
+
+extern "C" int sph_solver_step(sph_solver_t* S, int32_t n_steps, sph_stream_t stream) {
+    if (!S || n_steps < 0) return SPH_ERR_ARGUMENT;
+    cudaStream_t st = (cudaStream_t)stream;
+    for (int it = 0; it < n_steps; ++it) {
+        int rc = run_stages(S, st);
+        if (rc) return rc;
+        // delta+ shifting at the integrated positions, on the same candidate lists
+        launch_shift(S, S->Xf, S->Vf, S->Xc, S->Vc, nullptr, st);
+        if (cudaGetLastError() != cudaSuccess) return SPH_ERR_CUDA;
+    }
+    return SPH_OK;
+}
+
+extern "C" int sph_solver_integrate(sph_solver_t* S, sph_stream_t stream) {
+    if (!S) return SPH_ERR_ARGUMENT;
+    cudaStream_t st = (cudaStream_t)stream;
+    int rc = run_stages(S, st);
+    if (rc) return rc;
+    std::swap(S->Xc, S->Xf);
+    std::swap(S->Vc, S->Vf);
+    return SPH_OK;
+}
+
+extern "C" int sph_solver_shift(sph_solver_t* S, float* dx_out, sph_stream_t stream) {
+    if (!S) return SPH_ERR_ARGUMENT;
+    cudaStream_t st = (cudaStream_t)stream;
+    int rc = rebuild(S, st);
+    if (rc) return rc;
+    if (cudaMemsetAsync(S->words + 1, 0, sizeof(uint32_t), st) != cudaSuccess) return SPH_ERR_CUDA;
+    k_maxvel<<<blocks_for(S->n), kBlock, 0, st>>>(S->n, S->Vc, S->words);
+    launch_shift(S, S->Xc, S->Vc, S->Xt, S->Vt, dx_out, st);
+    std::swap(S->Xc, S->Xt);
+    std::swap(S->Vc, S->Vt);
+    return cudaGetLastError() == cudaSuccess ? SPH_OK : SPH_ERR_CUDA;
+}
+
+extern "C" int sph_solver_rhs(sph_solver_t* S, float* dudt, float* drhodt, float* grad_rho, float* L, float* pressure,
+                              float* rho_boundary, sph_stream_t stream) {
+    if (!S || !dudt || !drhodt) return SPH_ERR_ARGUMENT;
+    cudaStream_t st = (cudaStream_t)stream;
+    int rc = rebuild(S, st);
+    if (rc) return rc;
+    RhsOut o = {dudt, drhodt, grad_rho, L, pressure, rho_boundary};
+    launch_mdbc(S, S->Xc, rho_boundary, st);
+    launch_a(S, S->Xc, S->Vc, o, st);
+    launch_b<0>(S, S->Xc, S->Vc, o, nullptr, nullptr, st);
+    return cudaGetLastError() == cudaSuccess ? SPH_OK : SPH_ERR_CUDA;
+}
+
+extern "C" int sph_solver_download(sph_solver_t* S, float* x_fluid, float* u_fluid, float* rho_fluid,
+                                   float* rho_boundary, sph_stream_t stream) {
+    if (!S) return SPH_ERR_ARGUMENT;
+    cudaStream_t st = (cudaStream_t)stream;
+    k_download<<<blocks_for(S->n), kBlock, 0, st>>>(S->n, (int)S->nF, S->uid, S->Xr, S->Xc, S->Vc, x_fluid, u_fluid,
+                                                      rho_fluid, rho_boundary);
+    return cudaGetLastError() == cudaSuccess ? SPH_OK : SPH_ERR_CUDA;
+}
+
+extern "C" int sph_solver_flags(sph_solver_t* S, uint32_t* flags_host, sph_stream_t stream) {
+    if (!S || !flags_host) return SPH_ERR_ARGUMENT;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (cudaMemcpyAsync(flags_host, S->words, sizeof(uint32_t), cudaMemcpyDeviceToHost, st) != cudaSuccess)
+        return SPH_ERR_CUDA;
+    if (cudaStreamSynchronize(st) != cudaSuccess) return SPH_ERR_CUDA;
+    return SPH_OK;
+}
+
+extern "C" int sph_solver_launches_per_step(const sph_solver_t* S) {
+    if (!S) return -1;
+    // keys, scan (3), scatter, cell order, gather, build, 2 x (mdbc?, pass A, pass B), shift
+    return 8 + 2 * ((S->nB > 0 ? 1 : 0) + 2) + 1;
+}
+
+extern "C" int sph_solver_kernel_classes(void) { return KC_COUNT; }
+
+extern "C" const char* sph_solver_kernel_name(int cls) {
+    return (cls >= 0 && cls < KC_COUNT) ? kClassNames[cls] : nullptr;
+}
+
+extern "C" int sph_solver_set_timing(sph_solver_t* S, int32_t enabled) {
+    if (!S) return SPH_ERR_ARGUMENT;
+    S->timing_mask = (uint32_t)enabled;
+    return SPH_OK;
+}
+
+extern "C" int sph_solver_kernel_times(sph_solver_t* S, float* ms_host, int32_t* launches_host, sph_stream_t stream) {
+    if (!S || !ms_host || !launches_host) return SPH_ERR_ARGUMENT;
+    if (cudaStreamSynchronize((cudaStream_t)stream) != cudaSuccess) return SPH_ERR_CUDA;
+    for (int c = 0; c < KC_COUNT; ++c) {
+        ms_host[c] = 0.f;
+        launches_host[c] = 0;
+    }
+    for (size_t k = 0; k < S->used; ++k) {
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, S->pool[k].a, S->pool[k].b) != cudaSuccess) return SPH_ERR_CUDA;
+        ms_host[S->pool[k].cls] += ms;
+        launches_host[S->pool[k].cls] += 1;
+    }
+    S->used = 0;
+    return SPH_OK;
+}

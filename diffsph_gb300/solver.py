@@ -1,0 +1,253 @@
+"""Host wrapper of the fused sm_103a solver (libsph103.so, include/sph103.h).
+
+``Solver`` owns one caller-allocated workspace (a torch uint8 tensor on the GPU) and the
+library handle. All device work runs on torch's current CUDA stream. The configuration
+is the reference's nested config dict (src/diffSPH/v2/parameters.py keys).
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+
+import numpy as np
+import torch
+
+from . import _lib
+
+VISC_SCHEMES = {"deltaSPH_viscid": 0, "deltaSPH_inviscid": 1}
+DEFAULT_SKIN = 1.15
+
+
+def _f(x) -> float:
+    if isinstance(x, torch.Tensor):
+        return float(x.detach().cpu().reshape(-1)[0])
+    if isinstance(x, np.ndarray):
+        return float(x.reshape(-1)[0])
+    return float(x)
+
+
+def _pair(x):
+    if isinstance(x, torch.Tensor):
+        x = x.detach().cpu().tolist()
+    if isinstance(x, np.ndarray):
+        x = x.tolist()
+    if isinstance(x, (list, tuple)):
+        return [float(v) for v in x][:2]
+    return [float(x)] * 2
+
+
+def _periodic(cfg):
+    per = cfg["domain"].get("periodicity", cfg["domain"].get("periodic", False))
+    if isinstance(per, torch.Tensor):
+        per = per.detach().cpu().tolist()
+    if isinstance(per, np.ndarray):
+        per = per.tolist()
+    if isinstance(per, bool):
+        per = [per, per]
+    return [bool(per[0]), bool(per[1])]
+
+
+def domain_struct(cfg) -> _lib.Domain:
+    d = _lib.Domain()
+    mn, mx = _pair(cfg["domain"]["minExtent"]), _pair(cfg["domain"]["maxExtent"])
+    per = _periodic(cfg)
+    for a in range(2):
+        d.min[a], d.max[a], d.periodic[a] = mn[a], mx[a], int(per[a])
+    return d
+
+
+def default_capacity(skin: float, support: float, dx: float) -> int:
+    """Candidate slots per particle: 1.5x the lattice count within skin*H, plus margin."""
+    n = math.pi * (skin * support / dx) ** 2
+    return int(math.ceil((1.5 * n + 16) / 8.0) * 8)
+
+
+def _uniform(arr, name):
+    a = arr.detach() if isinstance(arr, torch.Tensor) else torch.as_tensor(arr)
+    v = a.reshape(-1)
+    if v.numel() and not bool((v == v[0]).all()):
+        raise ValueError(f"the fused solver needs a uniform particle {name}")
+    return float(v[0]) if v.numel() else 0.0
+
+
+def params_from_config(cfg, mass: float, skin: float = DEFAULT_SKIN, capacity: int | None = None) -> _lib.Params:
+    p = _lib.Params()
+    p.domain = domain_struct(cfg)
+    p.support = _f(cfg["particle"]["support"])
+    p.dx = _f(cfg["particle"]["dx"])
+    p.mass = mass
+    p.rho0 = _f(cfg["fluid"]["rho0"])
+    p.cs = _f(cfg["fluid"]["cs"])
+    eos = cfg.get("EOS", {})
+    if eos.get("type", "stiffTait") != "stiffTait":
+        raise ValueError(f"EOS {eos.get('type')} is not implemented by the fused solver (stiffTait is)")
+    p.gamma = _f(eos.get("polytropicExponent", 7.0))
+    p.kernel_scale = _f(cfg["kernel"]["kernelScale"])
+    diff = cfg["diffusion"]
+    if diff.get("densityScheme", "deltaSPH") != "deltaSPH":
+        raise ValueError("only the deltaSPH density diffusion scheme is implemented")
+    if diff.get("pi-switch", False):
+        raise ValueError("the viscosity pi-switch is not implemented")
+    p.delta = _f(diff.get("delta", 0.1))
+    vs = diff.get("velocityScheme", "deltaSPH_inviscid")
+    if vs not in VISC_SCHEMES:
+        raise ValueError(f"viscosity scheme {vs} is not implemented (deltaSPH_viscid, deltaSPH_inviscid are)")
+    p.visc_scheme = VISC_SCHEMES[vs]
+    p.nu, p.alpha, p.eps = _f(diff.get("nu", 0.01)), _f(diff.get("alpha", 0.01)), _f(diff.get("eps", 1e-6))
+    bd = dict(diff)
+    bd.update({k: v for k, v in cfg.get("boundaryDiffusion", {}).items() if v is not None})
+    bvs = bd.get("velocityScheme", vs)
+    if bvs not in VISC_SCHEMES:
+        raise ValueError(f"boundary viscosity scheme {bvs} is not implemented")
+    p.bvisc_scheme = VISC_SCHEMES[bvs]
+    p.b_nu, p.b_alpha, p.b_eps = _f(bd.get("nu", p.nu)), _f(bd.get("alpha", p.alpha)), _f(bd.get("eps", p.eps))
+    g = cfg.get("gravity", {})
+    p.gravity_on = int(bool(g.get("active", False)))
+    if p.gravity_on and g.get("gravityMode", "constant") != "constant":
+        raise ValueError("only constant gravity is implemented")
+    direction = _pair(g.get("direction", [0.0, -1.0]))
+    mag = _f(g.get("magnitude", 9.81))
+    p.gravity[0], p.gravity[1] = direction[0] * mag, direction[1] * mag
+    p.dt = _f(cfg["timestep"]["dt"])
+    sh = cfg.get("shifting", {})
+    if sh.get("scheme", "deltaSPH") != "deltaSPH" or sh.get("freeSurface", False) or int(sh.get("maxIterations", 1)) != 1:
+        raise ValueError("only delta+ shifting with one iteration and no free-surface handling is implemented")
+    p.shift_on = int(bool(sh.get("active", True)))
+    p.shift_R, p.shift_n = _f(sh.get("R", 0.25)), _f(sh.get("n", 4))
+    p.shift_CFL, p.shift_threshold = _f(sh.get("CFL", 1.5)), _f(sh.get("threshold", 0.5))
+    p.compute_mach = int(bool(sh.get("computeMach", True)))
+    p.density_update = 0 if cfg.get("integration", {}).get("densityUpdate", "reference") == "reference" else 1
+    p.skin = skin
+    p.capacity = capacity or default_capacity(skin, p.support, p.dx)
+    return p
+
+
+def _dev(t, dtype=torch.float32):
+    t = torch.as_tensor(t)
+    return t.to(device="cuda", dtype=dtype).contiguous()
+
+
+def _ptr(t):
+    return ctypes.c_void_p(t.data_ptr()) if t is not None else None
+
+
+def _stream():
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+class Solver:
+    """One fluid (plus optional static mDBC boundary) particle set advanced on the GPU."""
+
+    def __init__(self, config, fluid, boundary=None, skin: float = DEFAULT_SKIN, capacity: int | None = None):
+        if not torch.cuda.is_available():
+            raise RuntimeError("the sph103 solver needs a CUDA device")
+        self.lib = _lib.load()
+        self.config = config
+        use_b = boundary is not None and bool(config.get("boundary", {}).get("active", boundary is not None))
+        self.nF = int(torch.as_tensor(fluid["positions"]).shape[0])
+        self.nB = int(torch.as_tensor(boundary["positions"]).shape[0]) if use_b else 0
+        mass = _uniform(fluid["masses"], "mass")
+        if self.nB and abs(_uniform(boundary["masses"], "mass") - mass) > 1e-6 * mass:
+            raise ValueError("fluid and boundary particles must share one mass")
+        for part in ([fluid, boundary] if self.nB else [fluid]):
+            if abs(_uniform(part["supports"], "support") - _f(config["particle"]["support"])) > 1e-6 * _f(config["particle"]["support"]):
+                raise ValueError("particle supports must equal config['particle']['support']")
+        self.params = params_from_config(config, mass, skin, capacity)
+        nbytes = ctypes.c_size_t()
+        _lib.check("sph_solver_workspace_bytes",
+                   self.lib.sph_solver_workspace_bytes(ctypes.byref(self.params), self.nF, self.nB, ctypes.byref(nbytes)))
+        self.workspace = torch.empty(int(nbytes.value) + 256, dtype=torch.uint8, device="cuda")
+        base = self.workspace.data_ptr()
+        self._ws_ptr = (base + 255) & ~255
+        h = ctypes.c_void_p()
+        _lib.check("sph_solver_create", self.lib.sph_solver_create(
+            ctypes.byref(self.params), self.nF, self.nB, ctypes.c_void_p(self._ws_ptr), nbytes.value, ctypes.byref(h)))
+        self.handle = h
+        self.upload(fluid, boundary if self.nB else None)
+
+    def __del__(self):
+        h = getattr(self, "handle", None)
+        if h is not None and h.value:
+            self.lib.sph_solver_destroy(h)
+            self.handle = None
+
+    # -- state transfer ------------------------------------------------------------------
+    def upload(self, fluid, boundary=None):
+        xf, uf, rf = _dev(fluid["positions"]), _dev(fluid["velocities"]), _dev(fluid["densities"])
+        args = [xf, uf, rf, None, None, None, None]
+        if self.nB:
+            args[3:] = [_dev(boundary["positions"]), _dev(boundary["normals"]), _dev(boundary["distances"]),
+                        _dev(boundary["densities"]) if "densities" in boundary else None]
+        self._keep = args
+        _lib.check("sph_solver_upload", self.lib.sph_solver_upload(self.handle, *[_ptr(a) for a in args], _stream()))
+
+    def download(self):
+        out = {"positions": torch.empty(self.nF, 2, device="cuda"), "velocities": torch.empty(self.nF, 2, device="cuda"),
+               "densities": torch.empty(self.nF, device="cuda")}
+        rb = torch.empty(self.nB, device="cuda") if self.nB else None
+        _lib.check("sph_solver_download", self.lib.sph_solver_download(
+            self.handle, _ptr(out["positions"]), _ptr(out["velocities"]), _ptr(out["densities"]), _ptr(rb), _stream()))
+        if self.nB:
+            out["boundary_densities"] = rb
+        return out
+
+    # -- compute ---------------------------------------------------------------------------
+    def step(self, n: int = 1):
+        _lib.check("sph_solver_step", self.lib.sph_solver_step(self.handle, int(n), _stream()))
+
+    def integrate(self):
+        _lib.check("sph_solver_integrate", self.lib.sph_solver_integrate(self.handle, _stream()))
+
+    def shift(self):
+        dx = torch.empty(self.nF, 2, device="cuda")
+        _lib.check("sph_solver_shift", self.lib.sph_solver_shift(self.handle, _ptr(dx), _stream()))
+        return dx
+
+    def rhs(self):
+        o = {"dudt": torch.empty(self.nF, 2, device="cuda"), "drhodt": torch.empty(self.nF, device="cuda"),
+             "gradRho^L": torch.empty(self.nF, 2, device="cuda"), "L": torch.empty(self.nF, 2, 2, device="cuda"),
+             "pressures": torch.empty(self.nF, device="cuda")}
+        rb = torch.empty(self.nB, device="cuda") if self.nB else None
+        _lib.check("sph_solver_rhs", self.lib.sph_solver_rhs(
+            self.handle, _ptr(o["dudt"]), _ptr(o["drhodt"]), _ptr(o["gradRho^L"]), _ptr(o["L"]), _ptr(o["pressures"]),
+            _ptr(rb), _stream()))
+        if self.nB:
+            o["boundary_densities"] = rb
+        return o
+
+    def flags(self) -> int:
+        f = ctypes.c_uint32()
+        _lib.check("sph_solver_flags", self.lib.sph_solver_flags(self.handle, ctypes.byref(f), _stream()))
+        return int(f.value)
+
+    def check(self):
+        """Raise if the device recorded a capacity overflow, a skin violation or a NaN."""
+        f = self.flags()
+        if f & _lib.FLAG_CAPACITY:
+            raise _lib.SphError("sph_solver_step", 3)
+        if f & _lib.FLAG_VERLET:
+            raise _lib.SphError("sph_solver_step", 5)
+        if f & _lib.FLAG_NONFINITE:
+            raise _lib.SphError("sph_solver_step", 6)
+
+    def launches_per_step(self) -> int:
+        return int(self.lib.sph_solver_launches_per_step(self.handle))
+
+    # -- kernel timing -----------------------------------------------------------------------
+    def kernel_classes(self):
+        return [self.lib.sph_solver_kernel_name(c).decode() for c in range(self.lib.sph_solver_kernel_classes())]
+
+    def set_timing(self, classes):
+        names = self.kernel_classes()
+        mask = 0
+        for c in classes:
+            mask |= 1 << names.index(c)
+        _lib.check("sph_solver_set_timing", self.lib.sph_solver_set_timing(self.handle, mask))
+
+    def kernel_times(self):
+        k = self.lib.sph_solver_kernel_classes()
+        ms = (ctypes.c_float * k)()
+        cnt = (ctypes.c_int32 * k)()
+        _lib.check("sph_solver_kernel_times", self.lib.sph_solver_kernel_times(self.handle, ms, cnt, _stream()))
+        names = self.kernel_classes()
+        return {names[c]: (float(ms[c]), int(cnt[c])) for c in range(k)}

@@ -1,0 +1,167 @@
+/*
+ * sph103 — C ABI of the GB300 (sm_103a) delta-SPH particle path.
+ *
+ * All pointers are device pointers unless named *_host. All sizes are element counts.
+ * Every entry point returns an int status (SPH_OK = 0) and launches its work on the
+ * given stream; none of them allocates device memory: callers query a workspace size
+ * and pass the memory in. Nothing here synchronises the stream unless stated.
+ *
+ * Float arithmetic is fp32 (the reference's default precision). The neighbor filter
+ * reproduces the reference's fp32 operation order bit for bit, so neighbor sets are
+ * identical to the reference's on the same inputs.
+ */
+#ifndef SPH103_H
+#define SPH103_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st* sph_stream_t; /* a cudaStream_t */
+
+enum sph_status {
+    SPH_OK = 0,
+    SPH_ERR_ARGUMENT = 1,       /* invalid size, pointer or parameter */
+    SPH_ERR_WORKSPACE = 2,      /* workspace smaller than the queried size */
+    SPH_ERR_CAPACITY = 3,       /* a neighbor row exceeded the list capacity */
+    SPH_ERR_CUDA = 4,           /* a CUDA launch or copy failed */
+    SPH_ERR_VERLET = 5,         /* particles moved farther than the list skin allows */
+    SPH_ERR_NONFINITE = 6       /* a NaN / Inf appeared in the state */
+};
+
+/* Error flag bits accumulated on the device (sph_solver_flags). */
+#define SPH_FLAG_CAPACITY 1u
+#define SPH_FLAG_VERLET 2u
+#define SPH_FLAG_NONFINITE 4u
+
+typedef struct sph_domain {
+    double min[2];   /* config['domain']['minExtent'] */
+    double max[2];   /* config['domain']['maxExtent'] */
+    int32_t periodic[2];
+} sph_domain_t;
+
+/* Scheme constants; names follow the reference's config keys. */
+typedef struct sph_params {
+    sph_domain_t domain;
+    double support;          /* particle.support  (H, uniform) */
+    double dx;               /* particle.dx */
+    double mass;             /* uniform particle mass (fluid and boundary) */
+    double rho0;             /* fluid.rho0 */
+    double cs;               /* fluid.cs */
+    double gamma;            /* EOS.polytropicExponent (stiff Tait) */
+    double kernel_scale;     /* kernel.kernelScale */
+    double delta;            /* diffusion.delta (density diffusion, deltaSPH scheme) */
+    int32_t visc_scheme;     /* 0 deltaSPH_viscid, 1 deltaSPH_inviscid (diffusion.velocityScheme) */
+    double nu, alpha, eps;   /* diffusion.nu / alpha / eps */
+    int32_t bvisc_scheme;    /* boundaryDiffusion.velocityScheme (0 viscid, 1 inviscid) */
+    double b_nu, b_alpha, b_eps;
+    int32_t gravity_on;      /* gravity.active (constant mode) */
+    double gravity[2];       /* direction * magnitude */
+    double dt;               /* timestep.dt */
+    int32_t shift_on;        /* shifting active (delta+ scheme, one iteration) */
+    double shift_R, shift_n, shift_CFL, shift_threshold;
+    int32_t compute_mach;    /* shifting.computeMach */
+    int32_t density_update;  /* 0: the reference's observable update (half-step density),
+                                1: rational symplectic update rho (2-eps)/(2+eps) */
+    double skin;             /* candidate list radius factor (>= 1); lists are rebuilt every step */
+    int32_t capacity;        /* candidate slots per particle */
+} sph_params_t;
+
+/* ------------------------------------------------------------------------------------
+ * Neighbor search (drop-in for neighborSearch, src/diffSPH/v2/modules/neighborhood.py:491-593,
+ * whose candidate stage is the external torchCompactRadius package and whose exact filter is
+ * computeNeighborhood, neighborhood.py:433-460). Scatter mode: pairs with |x_i - x_j| <= h_j.
+ * Rows ordered by query index, columns by reference index (original indices).
+ * ------------------------------------------------------------------------------------ */
+
+/* Workspace bytes for sph_neighbor_count / sph_neighbor_fill. */
+int sph_neighbor_workspace_bytes(int64_t n_query, int64_t n_ref, const sph_domain_t* domain,
+                                 double max_support, size_t* bytes);
+
+/* Pass 1: sorts the reference particles into cells (inside the workspace) and writes the
+ * exact per-query counts to counts[n_query] and the CSR row offsets to offsets[n_query+1]
+ * (offsets[n_query] = total pairs). The caller reads offsets[n_query] to size the outputs. */
+int sph_neighbor_count(const float* x_query, int64_t n_query, const float* x_ref,
+                       const float* h_ref, int64_t n_ref, const sph_domain_t* domain,
+                       double max_support, void* workspace, size_t workspace_bytes,
+                       int32_t* counts, int64_t* offsets, sph_stream_t stream);
+
+/* Pass 2 (same workspace, after pass 1): per pair i, j (int64), q = r/h_j, unit x_ij (2),
+ * h_j, and when kernels / gradients != NULL the Wendland C2 kernel W and gradient grad W (2).
+ * n_pairs = offsets[n_query] as read back by the caller. */
+int sph_neighbor_fill(const float* x_query, int64_t n_query, const float* x_ref,
+                      const float* h_ref, int64_t n_ref, const sph_domain_t* domain,
+                      double max_support, void* workspace, size_t workspace_bytes,
+                      const int64_t* offsets, int64_t n_pairs, int64_t* pair_i, int64_t* pair_j,
+                      float* q, float* xhat, float* h_pair, float* kernels, float* gradients,
+                      sph_stream_t stream);
+
+/* ------------------------------------------------------------------------------------
+ * Fused solver: one time step of the reference runner (src/diffSPH/v2/runner.py:37-42):
+ * integrate(simulationStep) with scheme symplecticEuler (integration.py:357-392), whose two
+ * right-hand sides are simulationStep (deltaPlus.py:176-422) with mDBC walls (mDBC.py:9-163),
+ * followed by solveShifting (shifting.py:882-1019, delta+ branch).
+ * Fluid particles come first in the original order (0..n_fluid-1), boundary particles after.
+ * ------------------------------------------------------------------------------------ */
+typedef struct sph_solver sph_solver_t;
+
+int sph_solver_workspace_bytes(const sph_params_t* params, int64_t n_fluid, int64_t n_boundary,
+                               size_t* bytes);
+
+/* Creates a host-side handle over the caller's workspace (no device allocation). */
+int sph_solver_create(const sph_params_t* params, int64_t n_fluid, int64_t n_boundary,
+                      void* workspace, size_t workspace_bytes, sph_solver_t** out);
+void sph_solver_destroy(sph_solver_t* solver);
+
+/* Loads the state (original order; float2 arrays as [n][2]). Boundary arrays may be NULL
+ * when n_boundary == 0. normals point into the wall, distances are negative depths. */
+int sph_solver_upload(sph_solver_t* s, const float* x_fluid, const float* u_fluid,
+                      const float* rho_fluid, const float* x_boundary, const float* normal_boundary,
+                      const float* dist_boundary, const float* rho_boundary, sph_stream_t stream);
+
+/* Advances n_steps full time steps (integrate + shifting, fused). */
+int sph_solver_step(sph_solver_t* s, int32_t n_steps, sph_stream_t stream);
+
+/* The two halves of a step as the reference runner calls them: integrate (both
+ * right-hand sides and the symplectic Euler update; integration.py:92-513) ... */
+int sph_solver_integrate(sph_solver_t* s, sph_stream_t stream);
+
+/* ... and solveShifting (shifting.py:882-1019): rebuilds the lists at the current
+ * positions, applies the delta+ shift and writes the fluid increments dx[nF][2] in the
+ * original order when dx != NULL. */
+int sph_solver_shift(sph_solver_t* s, float* dx, sph_stream_t stream);
+
+/* Evaluates one right-hand side at the current state (the first stage of a step) and
+ * writes, in the original order, dudt[nF][2], drhodt[nF], and optionally (NULL to skip)
+ * gradRho^L[nF][2], L[nF][4], pressures[nF], boundary densities[nB]. */
+int sph_solver_rhs(sph_solver_t* s, float* dudt, float* drhodt, float* grad_rho, float* L,
+                   float* pressure, float* rho_boundary, sph_stream_t stream);
+
+/* Writes the current state back in the original order (NULL entries are skipped). */
+int sph_solver_download(sph_solver_t* s, float* x_fluid, float* u_fluid, float* rho_fluid,
+                        float* rho_boundary, sph_stream_t stream);
+
+/* Copies the device error flags (SPH_FLAG_*) to *flags_host; synchronises the stream. */
+int sph_solver_flags(sph_solver_t* s, uint32_t* flags_host, sph_stream_t stream);
+
+/* Number of kernel launches one sph_solver_step(s, 1, ...) issues. */
+int sph_solver_launches_per_step(const sph_solver_t* s);
+
+/* Kernel timing: when enabled, sph_solver_step brackets every launch with CUDA events on
+ * its stream and accumulates per-kernel-class device time. Classes are listed by
+ * sph_solver_kernel_name (index < sph_solver_kernel_classes()). */
+int sph_solver_kernel_classes(void);
+const char* sph_solver_kernel_name(int cls);
+int sph_solver_set_timing(sph_solver_t* s, int32_t enabled);
+/* Synchronises the stream, writes per-class total ms and launch counts, and resets them. */
+int sph_solver_kernel_times(sph_solver_t* s, float* ms_host, int32_t* launches_host,
+                            sph_stream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SPH103_H */

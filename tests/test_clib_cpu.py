@@ -1,0 +1,92 @@
+"""The C-ABI library loads and exports every entry point include/sph103.h declares.
+
+Runs without a GPU: only host-side queries (workspace sizes, parameter validation) are
+called here; compute calls are covered by the gpu-marked tests.
+"""
+import ctypes
+import os
+import re
+
+import pytest
+
+from diffsph_gb300 import _lib, build, scenes
+from diffsph_gb300.solver import default_capacity, domain_struct, params_from_config
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    try:
+        build.build()
+    except RuntimeError as e:  # no nvcc on this machine
+        pytest.skip(str(e))
+    return _lib.load()
+
+
+def declared_functions():
+    text = open(os.path.join(ROOT, "include", "sph103.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(sph_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_every_declared_symbol_is_exported(lib):
+    names = declared_functions()
+    assert len(names) >= 18
+    for n in names:
+        assert hasattr(lib, n), n
+    assert sorted(_lib.EXPORTS) == names
+
+
+def test_solver_workspace_query(lib):
+    cfg, st = scenes.taylor_green(64)
+    p = params_from_config(cfg, float(st["fluid"]["masses"][0]))
+    nbytes = ctypes.c_size_t()
+    assert lib.sph_solver_workspace_bytes(ctypes.byref(p), 4096, 0, ctypes.byref(nbytes)) == 0
+    # lists dominate: capacity * n * 4 bytes
+    assert nbytes.value > p.capacity * 4096 * 4
+    assert nbytes.value < 4096 * (p.capacity * 4 + 2048)
+
+
+def test_solver_rejects_bad_parameters(lib):
+    cfg, st = scenes.taylor_green(16)
+    p = params_from_config(cfg, float(st["fluid"]["masses"][0]))
+    nbytes = ctypes.c_size_t()
+    bad = _lib.Params.from_buffer_copy(p)
+    bad.skin = 0.9
+    assert lib.sph_solver_workspace_bytes(ctypes.byref(bad), 256, 0, ctypes.byref(nbytes)) == 1
+    bad = _lib.Params.from_buffer_copy(p)
+    bad.support = -1
+    assert lib.sph_solver_workspace_bytes(ctypes.byref(bad), 256, 0, ctypes.byref(nbytes)) == 1
+    assert lib.sph_solver_workspace_bytes(ctypes.byref(p), 0, 0, ctypes.byref(nbytes)) == 1
+    # creating over a too-small workspace fails cleanly, before touching the device
+    h = ctypes.c_void_p()
+    assert lib.sph_solver_create(ctypes.byref(p), 256, 0, ctypes.c_void_p(256), 16, ctypes.byref(h)) == 2
+
+
+def test_neighbor_workspace_query(lib):
+    cfg, _ = scenes.dam_break(dx=1.0 / 64)
+    d = domain_struct(cfg)
+    nbytes = ctypes.c_size_t()
+    assert lib.sph_neighbor_workspace_bytes(1000, 2000, ctypes.byref(d), cfg["particle"]["support"],
+                                            ctypes.byref(nbytes)) == 0
+    assert nbytes.value > 2000 * 8
+    assert lib.sph_neighbor_workspace_bytes(10, 10, ctypes.byref(d), -1.0, ctypes.byref(nbytes)) == 1
+
+
+def test_kernel_classes(lib):
+    k = lib.sph_solver_kernel_classes()
+    names = [lib.sph_solver_kernel_name(c).decode() for c in range(k)]
+    assert "pass_b_rates" in names and "build_lists" in names
+    assert lib.sph_solver_kernel_name(k) is None
+
+
+def test_params_from_reference_config_keys():
+    cfg, st = scenes.dam_break(dx=1.0 / 64)
+    p = params_from_config(cfg, float(st["fluid"]["masses"][0]))
+    assert p.visc_scheme == 1 and p.bvisc_scheme == 1 and p.gravity_on == 1
+    assert abs(p.gravity[1] + 9.81) < 1e-12
+    assert p.capacity == default_capacity(1.15, p.support, p.dx)
+    cfg["diffusion"]["velocityScheme"] = "Monaghan1992"
+    with pytest.raises(ValueError):
+        params_from_config(cfg, 1.0)

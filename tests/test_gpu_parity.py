@@ -1,0 +1,196 @@
+"""GPU parity: the sm_103a library (through its C ABI) against the CPU oracle.
+
+Tolerances (stated per check):
+* neighbor sets bit-exact: identical (i, j) lists, q = r/h and the unit vectors bit-exact;
+* per-particle fields: 1e-5 of the field's magnitude for densities and density rates,
+  1e-4 for accelerations and velocities. Several fields are near-cancelling pair sums
+  (the continuity rate of a divergence-free lattice flow, gradients downstream of the
+  ill-conditioned mDBC moment solve), where any fp32 evaluation, the reference's included,
+  carries rounding noise well above those bounds. Every field is therefore compared with
+  an fp64 run of the oracle: the GPU error must stay within 4x the error of the fp32
+  oracle (the reference's operation order) plus the stated tolerance times the magnitude.
+"""
+import copy
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+from golden_io import CASES, load_case, rel_max  # noqa: E402
+from oracle import sph_oracle as O  # noqa: E402
+from diffsph_gb300 import scenes  # noqa: E402
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _lib_built():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from diffsph_gb300 import _lib
+    _lib.load()
+
+
+def _np(t):
+    return t.detach().cpu().numpy()
+
+
+def _as64(st):
+    return {p: {k: (v.astype(np.float64) if v.dtype == np.float32 else v.copy()) for k, v in a.items()}
+            for p, a in st.items()}
+
+
+def assert_fp32_parity(gpu, o32, o64, tol, what=""):
+    """|gpu - o64| <= 4 |o32 - o64| + tol * max|o64| (element-wise maxima)."""
+    gpu, o32, o64 = (np.asarray(a, np.float64) for a in (gpu, o32, o64))
+    e_gpu = float(np.max(np.abs(gpu - o64)))
+    e_32 = float(np.max(np.abs(o32 - o64)))
+    scale = float(np.max(np.abs(o64)))
+    assert e_gpu <= 4 * e_32 + tol * scale, f"{what}: gpu err {e_gpu:.3e}, fp32 err {e_32:.3e}, scale {scale:.3e}"
+
+
+def _cfg32(cfg):
+    c = copy.deepcopy(cfg)
+    c["oracle"] = {"pinv": "torch"}  # the reference's own fp32 moment solve
+    return c
+
+
+def _case_list():
+    out = []
+    for c in CASES:
+        z, cfg, st = load_case(c)
+        out.append((c, cfg, st))
+    cfg, st = scenes.taylor_green(64)
+    out.append(("tgv64_lattice", cfg, st))
+    cfg, st = scenes.fourier_periodic(96, seed=5)
+    out.append(("fourier96", cfg, st))
+    cfg, st = scenes.dam_break(dx=1.0 / 32)
+    out.append(("dambreak32", cfg, st))
+    return out
+
+
+CASE_LIST = _case_list()
+IDS = [c[0] for c in CASE_LIST]
+
+
+@pytest.mark.parametrize("name,cfg,st", CASE_LIST, ids=IDS)
+def test_neighbor_search_bit_exact(name, cfg, st):
+    from diffsph_gb300.neighborhood import neighborSearch
+    fl = st["fluid"]
+    ref = O.neighbor_search(fl, fl, cfg)
+    _, nb = neighborSearch({k: torch.from_numpy(v) for k, v in fl.items()},
+                           {k: torch.from_numpy(v) for k, v in fl.items()}, cfg)
+    i, j = _np(nb["indices"][0]), _np(nb["indices"][1])
+    assert np.array_equal(i, ref["indices"][0]) and np.array_equal(j, ref["indices"][1])
+    assert np.array_equal(_np(nb["distances"]), ref["distances"])
+    assert np.array_equal(_np(nb["vectors"]), ref["vectors"])
+    assert np.array_equal(_np(nb["numNeighbors"]), ref["numNeighbors"])
+    assert rel_max(_np(nb["kernels"]), ref["kernels"]) < 1e-6
+    assert rel_max(_np(nb["gradients"]), ref["gradients"]) < 1e-6
+
+
+def test_neighbor_search_query_vs_reference_sets():
+    """Boundary -> fluid style search: separate query and reference sets, per-particle h."""
+    from diffsph_gb300.neighborhood import neighborSearch
+    cfg, st = scenes.dam_break(dx=1.0 / 32)
+    fl, bd = st["fluid"], st["boundary"]
+    ref = O.neighbor_search(fl, bd, cfg)
+    _, nb = neighborSearch({k: torch.from_numpy(v) for k, v in fl.items()},
+                           {k: torch.from_numpy(v) for k, v in bd.items()}, cfg)
+    assert np.array_equal(_np(nb["indices"][0]), ref["indices"][0])
+    assert np.array_equal(_np(nb["indices"][1]), ref["indices"][1])
+    assert np.array_equal(_np(nb["distances"]), ref["distances"])
+
+
+def test_neighbor_search_empty_and_isolated():
+    from diffsph_gb300.neighborhood import exact_pairs
+    cfg, _ = scenes.taylor_green(16)
+    x = np.array([[0.0, 0.0], [0.9, 0.9]], np.float32)  # farther apart than h = 0.5
+    h = np.full(2, 0.5, np.float32)
+    i, j, *_ = exact_pairs(x, x, h, cfg)
+    assert _np(i).tolist() == [0, 1] and _np(j).tolist() == [0, 1]
+    i, j, *_ = exact_pairs(np.zeros((0, 2), np.float32), x, h, cfg)
+    assert i.numel() == 0
+
+
+def _solver(cfg, st):
+    from diffsph_gb300.solver import Solver
+    b = st.get("boundary")
+    return Solver(cfg, st["fluid"], b)
+
+
+@pytest.mark.parametrize("name,cfg,st", CASE_LIST, ids=IDS)
+def test_rhs_matches_oracle(name, cfg, st):
+    s32 = copy.deepcopy(st)
+    (_, dudt32, drhodt32), _ = O.simulation_step(s32, _cfg32(cfg))
+    s64 = _as64(st)
+    (_, dudt64, drhodt64), _ = O.simulation_step(s64, cfg)
+    sol = _solver(cfg, st)
+    out = sol.rhs()
+    torch.cuda.synchronize()
+    f32, f64 = s32["fluid"], s64["fluid"]
+    assert_fp32_parity(_np(out["pressures"]), f32["pressures"], f64["pressures"], 1e-5, "pressures")
+    assert_fp32_parity(_np(out["gradRho^L"]), f32["gradRho^L"], f64["gradRho^L"], 1e-5, "gradRho^L")
+    assert_fp32_parity(_np(out["drhodt"]), drhodt32, drhodt64, 1e-5, "drhodt")
+    assert_fp32_parity(_np(out["dudt"]), dudt32, dudt64, 1e-4, "dudt")
+    if "boundary" in st:
+        assert_fp32_parity(_np(out["boundary_densities"]), s32["boundary"]["densities"],
+                           s64["boundary"]["densities"], 1e-5, "boundary densities")
+    else:
+        # fluid-only: the direct bound holds as well
+        assert rel_max(_np(out["dudt"]), dudt32) < 1e-4
+
+
+@pytest.mark.parametrize("name,cfg,st", CASE_LIST, ids=IDS)
+def test_full_step_matches_oracle(name, cfg, st):
+    r32, _ = O.full_step(copy.deepcopy(st), _cfg32(cfg))
+    r64, _ = O.full_step(_as64(st), cfg)
+    sol = _solver(cfg, st)
+    sol.step(1)
+    sol.check()
+    got = sol.download()
+    a, b = r32["fluid"], r64["fluid"]
+    assert_fp32_parity(_np(got["velocities"]), a["velocities"], b["velocities"], 1e-4, "velocities")
+    assert_fp32_parity(_np(got["densities"]), a["densities"], b["densities"], 1e-5, "densities")
+    dx = float(cfg["particle"]["dx"])
+    # positions: the shift is clamped to 0.05 dx; compare the increment x' - x^n
+    x0 = st["fluid"]["positions"]
+    assert_fp32_parity(_np(got["positions"]) - x0, a["positions"] - x0, b["positions"] - x0, 1e-4, "dx")
+    if "boundary" not in st:
+        # fluid-only: the direct bounds against the reference-order fp32 run hold as well
+        assert rel_max(_np(got["velocities"]), a["velocities"]) < 1e-4
+        assert rel_max(_np(got["densities"]), a["densities"]) < 1e-5
+    if "boundary" in st:
+        assert_fp32_parity(_np(got["boundary_densities"]), r32["boundary"]["densities"],
+                           r64["boundary"]["densities"], 1e-5, "boundary densities")
+
+
+def test_integrate_then_shift_equals_step():
+    """The runner's two calls (integrate, solveShifting) give the fused step's result; the
+    standalone shift re-sorts the particles, so sums differ only in summation order."""
+    cfg, st = scenes.fourier_periodic(64, seed=2)
+    a = _solver(cfg, st)
+    a.step(1)
+    b = _solver(cfg, st)
+    b.integrate()
+    dx = b.shift()
+    ga, gb = a.download(), b.download()
+    assert torch.equal(ga["velocities"], gb["velocities"])
+    assert torch.equal(ga["densities"], gb["densities"])
+    d = float(cfg["particle"]["dx"])
+    assert float((ga["positions"] - gb["positions"]).abs().max()) < 1e-6 * d + 2.5e-7
+    # clamp at 0.05 dx per component, plus one fp32 rounding of x_new - x (|x| <= 1)
+    assert float(dx.abs().max()) <= 0.05 * d + 1.2e-7
+
+
+def test_ten_steps_track_oracle():
+    cfg, st = scenes.taylor_green(32)
+    s = copy.deepcopy(st)
+    for _ in range(10):
+        s, _ = O.full_step(s, cfg)
+    sol = _solver(cfg, st)
+    sol.step(10)
+    sol.check()
+    got = sol.download()
+    assert rel_max(_np(got["velocities"]), s["fluid"]["velocities"]) < 1e-4
+    assert rel_max(_np(got["densities"]) - 1.0, s["fluid"]["densities"] - 1.0) < 1e-3
