@@ -28,6 +28,7 @@ sys.path.insert(0, ROOT)
 METRIC = "particle-steps/s (plain delta-SPH step)"
 WORKLOADS = {
     "dambreak_dx1024": dict(scene="dam_break", dx=1.0 / 1024),
+    "dambreak_dx512": dict(scene="dam_break", dx=1.0 / 512),
     "dambreak_dx256": dict(scene="dam_break", dx=1.0 / 256),
     "tgv_64": dict(scene="taylor_green", nx=64),
 }
@@ -188,7 +189,7 @@ def run_ours(args):
     sol.check()
     torch.cuda.synchronize()
     # timed region: device-resident state, CUDA events on the launching stream
-    sol.set_timing(["pass_b_rates", "pass_a_gradient", "build_lists", "shift"])
+    sol.set_timing(["pass_b_rates", "pass_a_gradient", "shift", "cell_sort", "gather", "mdbc_ghosts"])
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     if world > 1:
         torch.distributed.barrier()

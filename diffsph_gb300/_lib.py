@@ -85,7 +85,7 @@ def load(build_if_missing: bool = False):
         "sph_solver_step": ([P, I32, P], ctypes.c_int),
         "sph_solver_integrate": ([P, P], ctypes.c_int),
         "sph_solver_shift": ([P, P, P], ctypes.c_int),
-        "sph_solver_rhs": ([P, P, P, P, P, P, P, P], ctypes.c_int),
+        "sph_solver_rhs": ([P, P, P, P, P, P, P, P, P], ctypes.c_int),
         "sph_solver_download": ([P, P, P, P, P, P], ctypes.c_int),
         "sph_solver_flags": ([P, ctypes.POINTER(ctypes.c_uint32), P], ctypes.c_int),
         "sph_solver_launches_per_step": ([P], ctypes.c_int),

@@ -64,6 +64,22 @@ __device__ __forceinline__ float sq_norm_ref(float x0, float x1) {
     return __fmaf_rn(x1, x1, __fmul_rn(x0, x0));
 }
 
+// Geometry of a pair that passed the exact inclusion test. r, q and the unit vector feed
+// tolerance-checked sums only, so they use the fast reciprocal square root / reciprocal.
+struct PairG {
+    float r, q, xh0, xh1;
+};
+
+__device__ __forceinline__ PairG pair_fast(float x0, float x1, float sq, float inv_h) {
+    PairG g;
+    g.r = sq > 0.0f ? sq * rsqrtf(sq) : 0.0f;
+    g.q = g.r * inv_h;
+    float inv = __fdividef(1.0f, g.r + 1e-7f);
+    g.xh0 = x0 * inv;
+    g.xh1 = x1 * inv;
+    return g;
+}
+
 // Exact reference test: q = sqrt(s) / h <= 1. Returns q, r.
 __device__ __forceinline__ bool exact_in(float s, float h, float& r, float& q) {
     r = __fsqrt_rn(s);
@@ -93,7 +109,11 @@ __device__ __forceinline__ float sgnf(float x) { return (x > 0.0f) ? 1.0f : ((x 
 // The reference's closed-form 2x2 pseudo-inverse (src/diffSPH/v2/math.py:11-57): an SVD
 // assembled from two half-angle rotations, the smaller singular value regularised by
 // 1e-7 under the square root, singular values <= 1e-5 dropped.
-__device__ __forceinline__ void pinv2x2_ref(float a, float b, float c, float d, float L[4]) {
+struct M2 {
+    float a, b, c, d;
+};
+
+__device__ __forceinline__ M2 pinv2x2_ref(float a, float b, float c, float d) {
     float aa = a * a, bb = b * b, cc = c * c, dd = d * d;
     float theta = 0.5f * atan2f(2.0f * a * c + 2.0f * b * d, aa + bb - cc - dd);
     float ct, st;
@@ -114,10 +134,12 @@ __device__ __forceinline__ void pinv2x2_ref(float a, float b, float c, float d, 
     // pinv = V diag(i1, i2) U^T with U = [[ct,-st],[st,ct]], V = [[cp s11, -sp s22],[sp s11, cp s22]]
     float v00 = cp * s11 * i1, v01 = -sp * s22 * i2;
     float v10 = sp * s11 * i1, v11 = cp * s22 * i2;
-    L[0] = v00 * ct - v01 * st;
-    L[1] = v00 * st + v01 * ct;
-    L[2] = v10 * ct - v11 * st;
-    L[3] = v10 * st + v11 * ct;
+    M2 L;
+    L.a = v00 * ct - v01 * st;
+    L.b = v00 * st + v01 * ct;
+    L.c = v10 * ct - v11 * st;
+    L.d = v10 * st + v11 * ct;
+    return L;
 }
 
 // 3x3 pseudo-inverse in fp64 with torch.linalg.pinv's truncation rule (singular values

@@ -19,8 +19,9 @@ Geo make_geo(const double mn[2], const double mx[2], const int per[2]) {
 }
 
 Grid make_grid(const double mn[2], const double mx[2], const int per[2], double cell_min,
-               int64_t* ncells_out) {
+               int64_t* ncells_out, int rad) {
     Grid g;
+    g.rad = rad;
     int64_t total = 1;
     for (int a = 0; a < 2; ++a) {
         double ext = mx[a] - mn[a];
@@ -266,7 +267,7 @@ __global__ void k_nb_query(int64_t nq, const float2* __restrict__ qxy, const flo
     float2 p = qxy[i];
     int cx = cell_coord(p.x, g.mn[0], g.inv_cell[0], g.nc[0]);
     int cy = cell_coord(p.y, g.mn[1], g.inv_cell[1], g.nc[1]);
-    int rows[3], lo[2], hi[2];
+    int rows[kMaxRows], lo[2], hi[2];
     int nr = stencil_rows(cy, g, rows);
     int ncr = stencil_cols(cx, g, lo, hi);
     int64_t w = FILL ? offsets[i] : 0;

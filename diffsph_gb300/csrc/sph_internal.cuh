@@ -19,6 +19,7 @@ struct Grid {
     float inv_cell[2];
     int nc[2];
     int per[2];
+    int rad;  // stencil radius in cells: (2 rad + 1)^2 cells cover the search radius
 };
 
 __device__ __forceinline__ int cell_coord(float v, float mn, float inv, int nc) {
@@ -26,15 +27,19 @@ __device__ __forceinline__ int cell_coord(float v, float mn, float inv, int nc) 
     return c < 0 ? 0 : (c >= nc ? nc - 1 : c);
 }
 
-// Rows (y cells) of the 3x3 stencil around cy, each listed once.
-__device__ __forceinline__ int stencil_rows(int cy, const Grid& g, int rows[3]) {
+constexpr int kMaxRad = 2;
+constexpr int kMaxRows = 2 * kMaxRad + 1;
+constexpr int kMaxRanges = 2 * kMaxRows;
+
+// Rows (y cells) of the stencil around cy, each listed once.
+__device__ __forceinline__ int stencil_rows(int cy, const Grid& g, int rows[kMaxRows]) {
     int nc = g.nc[1];
-    if (g.per[1] && nc < 3) {
+    if (g.per[1] && nc < 2 * g.rad + 1) {
         for (int k = 0; k < nc; ++k) rows[k] = k;
         return nc;
     }
     int n = 0;
-    for (int dy = -1; dy <= 1; ++dy) {
+    for (int dy = -g.rad; dy <= g.rad; ++dy) {
         int y = cy + dy;
         if (g.per[1]) y = (y + nc) % nc;
         else if (y < 0 || y >= nc) continue;
@@ -46,20 +51,20 @@ __device__ __forceinline__ int stencil_rows(int cy, const Grid& g, int rows[3]) 
 // Column ranges [lo, hi] (inclusive) of the stencil around cx: one contiguous range, or
 // two when a periodic axis wraps.
 __device__ __forceinline__ int stencil_cols(int cx, const Grid& g, int lo[2], int hi[2]) {
-    int nc = g.nc[0];
+    int nc = g.nc[0], R = g.rad;
     if (g.per[0]) {
-        if (nc < 3) { lo[0] = 0; hi[0] = nc - 1; return 1; }
-        if (cx == 0) { lo[0] = nc - 1; hi[0] = nc - 1; lo[1] = 0; hi[1] = 1; return 2; }
-        if (cx == nc - 1) { lo[0] = nc - 2; hi[0] = nc - 1; lo[1] = 0; hi[1] = 0; return 2; }
+        if (nc < 2 * R + 1) { lo[0] = 0; hi[0] = nc - 1; return 1; }
+        if (cx - R < 0) { lo[0] = cx - R + nc; hi[0] = nc - 1; lo[1] = 0; hi[1] = cx + R; return 2; }
+        if (cx + R > nc - 1) { lo[0] = cx - R; hi[0] = nc - 1; lo[1] = 0; hi[1] = cx + R - nc; return 2; }
     }
-    lo[0] = cx > 0 ? cx - 1 : 0;
-    hi[0] = cx < nc - 1 ? cx + 1 : nc - 1;
+    lo[0] = cx - R > 0 ? cx - R : 0;
+    hi[0] = cx + R < nc - 1 ? cx + R : nc - 1;
     return 1;
 }
 
 // Host helpers
 Grid make_grid(const double mn[2], const double mx[2], const int per[2], double cell_min,
-               int64_t* ncells_out);
+               int64_t* ncells_out, int rad = 1);
 Geo make_geo(const double mn[2], const double mx[2], const int per[2]);
 
 // Device-wide exclusive scans: out[0..n] with out[n] = total. tmp holds scan_tmp_elems(n).

@@ -4,24 +4,25 @@
 //   integrate(simulationStep) with scheme symplecticEuler (modules/integration.py:357-392),
 //   then solveShifting (modules/shifting.py:882-1019, delta+ branch, one iteration).
 //
-// Data layout (structure of arrays, particles in cell-sorted order, rebuilt every step):
+// Data layout (structure of arrays, particles in cell-sorted order, re-sorted every step):
 //   Xr[n]  float2  raw positions (never wrapped, like the reference state)
-//   X4[n]  float4  (wrapped x, wrapped y, rho, p)      read by every neighbor loop
-//   V4[n]  float4  (u, v, gradRho^L x, gradRho^L y)    read by pass B
-//   nbr[K][n] int32 candidate lists (slot-major, so a warp's loads of slot k coalesce);
-//                   bit 31 marks a boundary particle
-// Fluid and boundary particles share the arrays; per-step work:
-//   sort by cell -> gather -> candidate lists (radius skin*H)
+//   X4[n]  float4  (wrapped x, wrapped y, rho, p); rho carries the sign bit for boundary
+//                  particles (-rho), so a neighbor's kind costs no extra load
+//   V4[n]  float4  (u, v, gradRho^L x, gradRho^L y)
+// There is no stored neighbor list. Each pass walks the 3x3 cell stencil of every particle
+// over the sorted arrays (a warp's lanes sit in one or two cells, so their loads are
+// broadcasts), keeps the exact neighbors (the reference's fp32 test) in a per-warp
+// shared-memory list, and then evaluates the pair terms over those lists. Per step:
+//   sort by cell -> gather
 //   stage 1: mDBC ghosts -> pass A -> pass B (+ half-step update)
 //   stage 2: mDBC ghosts -> pass A -> pass B (+ final update, max |u|)
 //   shift pass (+ position update)
-// Every pass re-applies the exact reference filter q = r/h <= 1, so the pairs used are
-// exactly the reference's.
 #include <math.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 
+#include <utility>
 #include <vector>
 
 #include "../../include/sph103.h"
@@ -29,15 +30,21 @@
 
 namespace sph {
 
-enum KernelClass { KC_SORT = 0, KC_GATHER, KC_BUILD, KC_MDBC, KC_PASS_A, KC_PASS_B, KC_SHIFT, KC_COUNT };
-static const char* kClassNames[KC_COUNT] = {"cell_sort", "gather", "build_lists", "mdbc_ghosts",
-                                             "pass_a_gradient", "pass_b_rates", "shift"};
+enum KernelClass { KC_SORT = 0, KC_GATHER, KC_MDBC, KC_PASS_A, KC_PASS_B, KC_SHIFT, KC_COUNT };
+static const char* kClassNames[KC_COUNT] = {"cell_sort", "gather", "mdbc_ghosts", "pass_a_gradient",
+                                             "pass_b_rates", "shift"};
+
+constexpr int kPassWarps = 4;
+constexpr int kPassThreads = 32 * kPassWarps;
+constexpr int kCap = 56;  // exact neighbors held per lane before the pair terms are evaluated
+constexpr int kUnroll = 4;  // stencil candidates tested per lane per step of the scan
+constexpr unsigned kFull = 0xffffffffu;
 
 struct Phys {
     Geo geo;
     float h;            // support
-    float h_cut;        // cheap pre-reject bound on the squared distance (just above h^2)
-    float skin2;        // candidate radius^2 (slightly enlarged)
+    float T;            // exact inclusion threshold: s <= T  <=>  fl(fl(sqrt(s)) / h) <= 1
+    float inv_h;
     float m;            // particle mass
     float dt, dth;      // dt, dt/2
     KernelCoef kc;
@@ -45,20 +52,20 @@ struct Phys {
     float rho0;
     float diff_coef;    // delta * h / kappa * cs
     float diff_eps;     // 1e-6 * h
-    int visc;           // 0 viscid, 1 inviscid
     float v_eps;        // eps * h^2
     float v_num;        // viscid 8 nu rho0 ; inviscid alpha h cs rho0   (divided by rho_i)
     int bvisc;
     float bv_eps, bv_num;
     float gx, gy;
     int nF;
-    float W0;           // W(dx/h) for the shifting term
+    float invW0;        // 1 / W(dx/h) for the shifting term
     float shR, shN, sh_thr;
+    int shN4;           // n == 4
     float sh_scale;     // -CFL * (h/kappa*2)^2 (times Ma)
     float inv_cs;
     int compute_mach;
     int density_update;
-    float verlet_lim;   // (skin - 1) * h
+    float verlet_lim;   // (skin - 1) * h: largest displacement since the sort
 };
 
 struct RhsOut {
@@ -68,7 +75,10 @@ struct RhsOut {
     float* L;
     float* pressure;
     float* rho_b;
+    int32_t* nn;    // [nF][2]: fluid and boundary neighbors (incl. self) per fluid particle
 };
+
+__device__ __forceinline__ bool is_boundary(float rho_signed) { return __float_as_int(rho_signed) < 0; }
 
 // ------------------------------------------------------------------------------------
 // upload / download / gather
@@ -81,21 +91,23 @@ __global__ void k_upload(int64_t nF, int64_t nB, const float* __restrict__ xf, c
     if (i >= nF + nB) return;
     float2 x;
     float2 u = make_float2(0.f, 0.f);
-    float rho;
+    float rho, rho_s;
     if (i < nF) {
         x = make_float2(xf[2 * i], xf[2 * i + 1]);
         u = make_float2(uf[2 * i], uf[2 * i + 1]);
         rho = rf[i];
+        rho_s = rho;
     } else {
         int64_t b = i - nF;
         x = make_float2(xb[2 * b], xb[2 * b + 1]);
         rho = rb ? rb[b] : P.rho0;
+        rho_s = -rho;
         bnormal[b] = make_float2(nb[2 * b], nb[2 * b + 1]);
         bdist[b] = db[b];
     }
     Xr[i] = x;
     float2 w = wrap_pos(x, P.geo);
-    X4[i] = make_float4(w.x, w.y, rho, eos_p(rho, P.eos));
+    X4[i] = make_float4(w.x, w.y, rho_s, eos_p(rho, P.eos));
     V4[i] = make_float4(u.x, u.y, 0.f, 0.f);
     uid[i] = (int32_t)i;
 }
@@ -111,7 +123,7 @@ __global__ void k_download(int64_t n, int nF, const int32_t* __restrict__ uid, c
         if (uf) { uf[2 * o] = V4[s].x; uf[2 * o + 1] = V4[s].y; }
         if (rf) rf[o] = X4[s].z;
     } else if (rb) {
-        rb[o - nF] = X4[s].z;
+        rb[o - nF] = fabsf(X4[s].z);
     }
 }
 
@@ -131,48 +143,81 @@ __global__ void k_gather(int64_t n, int nF, const int32_t* __restrict__ perm, co
     if (u >= nF) bidx[atomicAdd(&words[2], 1u)] = (int32_t)s;
 }
 
-// candidate lists: every particle within skin*h (squared test with a margin, so the list
-// is a superset of the exact reference set at every evaluation of the step)
-template <bool PER>
-__global__ void k_build(int64_t n, int K, const float4* __restrict__ X4, const int32_t* __restrict__ uid,
-                        const int32_t* __restrict__ start, Grid g, Phys P, int32_t* __restrict__ nbr,
-                        int32_t* __restrict__ ncnt, uint32_t* __restrict__ words) {
-    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    if (uid[i] >= P.nF) {
-        ncnt[i] = 0;
-        return;
-    }
-    float4 xi = X4[i];
-    float2 pi = make_float2(xi.x, xi.y);
-    int cx = cell_coord(pi.x, g.mn[0], g.inv_cell[0], g.nc[0]);
-    int cy = cell_coord(pi.y, g.mn[1], g.inv_cell[1], g.nc[1]);
-    int rows[3], lo[2], hi[2];
+// ------------------------------------------------------------------------------------
+// Neighbor loop: candidates from the 3x3 cell stencil of the sort, exact filter, per-warp
+// shared-memory list of accepted slots, then f(j) for every exact neighbor j. Every lane of
+// the warp must call it (it votes); lanes with active == false contribute no pairs.
+// The cells are >= (h + largest displacement since the sort), so the stencil of the
+// particle's current cell holds every particle within h.
+// ------------------------------------------------------------------------------------
+__device__ __forceinline__ int stencil_ranges(float2 p, const Grid& g, const int32_t* __restrict__ start,
+                                              int rs[kMaxRanges], int re[kMaxRanges]) {
+    int cx = cell_coord(p.x, g.mn[0], g.inv_cell[0], g.nc[0]);
+    int cy = cell_coord(p.y, g.mn[1], g.inv_cell[1], g.nc[1]);
+    int rows[kMaxRows], lo[2], hi[2];
     int nr = stencil_rows(cy, g, rows);
-    int ncr = stencil_cols(cx, g, lo, hi);
-    int cnt = 0;
+    int ncol = stencil_cols(cx, g, lo, hi);
+    int n = 0;
     for (int a = 0; a < nr; ++a) {
-        for (int b = 0; b < ncr; ++b) {
-            int s0 = start[rows[a] * g.nc[0] + lo[b]], s1 = start[rows[a] * g.nc[0] + hi[b] + 1];
-            for (int s = s0; s < s1; ++s) {
-                float4 xj = X4[s];
-                float x0, x1;
-                pair_vec<PER>(pi, make_float2(xj.x, xj.y), P.geo, x0, x1);
-                if (sq_norm_ref(x0, x1) <= P.skin2) {
-                    if (cnt < K) {
-                        int e = s | (uid[s] >= P.nF ? (int)0x80000000 : 0);
-                        nbr[(size_t)cnt * n + i] = e;
-                    }
-                    ++cnt;
-                }
+        int base = rows[a] * g.nc[0];
+        for (int b = 0; b < ncol; ++b) {
+            int s0 = __ldg(&start[base + lo[b]]), s1 = __ldg(&start[base + hi[b] + 1]);
+            if (s1 > s0) {
+                rs[n] = s0;
+                re[n] = s1;
+                ++n;
             }
         }
     }
-    if (cnt > K) {
-        atomicOr(&words[0], SPH_FLAG_CAPACITY);
-        cnt = K;
+    return n;
+}
+
+// Each scan step takes up to kUnroll consecutive candidates of the lane's current range,
+// so that several independent loads are in flight per lane.
+template <bool PER, class F>
+__device__ __forceinline__ void neighbor_loop(bool active, float2 pi, const float4* __restrict__ X4,
+                                              const int32_t* __restrict__ start, const Grid& g, const Phys& P,
+                                              int32_t* __restrict__ lst, F&& f) {
+    const int lane = threadIdx.x & 31;
+    int rs[kMaxRanges], re[kMaxRanges];
+    int nrng = active ? stencil_ranges(pi, g, start, rs, re) : 0;
+    int r = 0;
+    int s = nrng > 0 ? rs[0] : 0, se = nrng > 0 ? re[0] : 0;
+    int cnt = 0;
+    while (__any_sync(kFull, r < nrng)) {
+        if (r < nrng) {
+            int m = se - s < kUnroll ? se - s : kUnroll;
+            float4 xj[kUnroll];
+#pragma unroll
+            for (int u = 0; u < kUnroll; ++u)
+                if (u < m) xj[u] = __ldg(&X4[s + u]);
+#pragma unroll
+            for (int u = 0; u < kUnroll; ++u) {
+                if (u < m) {
+                    float x0, x1;
+                    pair_vec<PER>(pi, make_float2(xj[u].x, xj[u].y), P.geo, x0, x1);
+                    if (sq_norm_ref(x0, x1) <= P.T) lst[(cnt++) * 32 + lane] = s + u;
+                }
+            }
+            s += m;
+            if (s == se) {
+                ++r;
+                if (r < nrng) {
+                    s = rs[r];
+                    se = re[r];
+                }
+            }
+        }
+        if (__any_sync(kFull, cnt > kCap - kUnroll)) {
+            int mc = (int)__reduce_max_sync(kFull, (unsigned)cnt);
+            for (int k = 0; k < mc; ++k)
+                if (k < cnt) f(lst[k * 32 + lane]);
+            cnt = 0;
+        }
     }
-    ncnt[i] = cnt;
+    int mc = (int)__reduce_max_sync(kFull, (unsigned)cnt);
+    for (int k = 0; k < mc; ++k)
+        if (k < cnt) f(lst[k * 32 + lane]);
 }
 
 // ------------------------------------------------------------------------------------
@@ -194,50 +239,41 @@ __global__ void k_mdbc(int nB, const int32_t* __restrict__ bidx, const int32_t* 
     float mapd = __fadd_rn(d, fmaxf(d, -P.h));
     float2 gp = make_float2(__fadd_rn(xb.x, __fmul_rn(mapd, nrm.x)), __fadd_rn(xb.y, __fmul_rn(mapd, nrm.y)));
     float2 gw = wrap_pos(gp, P.geo);
-    int cx = cell_coord(gw.x, g.mn[0], g.inv_cell[0], g.nc[0]);
-    int cy = cell_coord(gw.y, g.mn[1], g.inv_cell[1], g.nc[1]);
-    int rows[3], lo[2], hi[2];
-    int nr = stencil_rows(cy, g, rows);
-    int ncr = stencil_cols(cx, g, lo, hi);
+    int rs[kMaxRanges], re[kMaxRanges];
+    int nr = stencil_ranges(gw, g, start, rs, re);
     float num = 0.f, den = 0.f, gs0 = 0.f, gs1 = 0.f, vg0 = 0.f, vg1 = 0.f, ps0 = 0.f, ps1 = 0.f;
     float pm00 = 0.f, pm01 = 0.f, pm10 = 0.f, pm11 = 0.f;
     int cnt = 0;
     for (int a = 0; a < nr; ++a) {
-        for (int c = 0; c < ncr; ++c) {
-            int s0 = start[rows[a] * g.nc[0] + lo[c]], s1 = start[rows[a] * g.nc[0] + hi[c] + 1];
-            for (int j = s0; j < s1; ++j) {
-                if (uid[j] >= P.nF) continue;
-                float4 xj = X4[j];
-                float x0, x1;
-                pair_vec<PER>(gw, make_float2(xj.x, xj.y), P.geo, x0, x1);
-                float sq = sq_norm_ref(x0, x1);
-                if (sq > P.h_cut) continue;
-                float r, q;
-                if (!exact_in(sq, P.h, r, q)) continue;
-                float den_r = __fadd_rn(r, 1e-7f);
-                float xh0 = __fdiv_rn(x0, den_r), xh1 = __fdiv_rn(x1, den_r);
-                float W = wendland_w(q, P.kc);
-                float dW = wendland_dw(q, P.kc);
-                float g0 = xh0 * dW, g1 = xh1 * dW;
-                float V = P.m / xj.z;
-                num += P.m * W;
-                den += V * W;
-                float k0 = V * g0, k1 = V * g1;
-                gs0 += xj.z * k0;
-                gs1 += xj.z * k1;
-                vg0 += k0;
-                vg1 += k1;
-                float xr = -q * P.h;
-                float xi0 = xh0 * xr, xi1 = xh1 * xr;
-                float vw = V * W;
-                ps0 += xi0 * vw;
-                ps1 += xi1 * vw;
-                pm00 += xi0 * k0;
-                pm01 += xi0 * k1;
-                pm10 += xi1 * k0;
-                pm11 += xi1 * k1;
-                ++cnt;
-            }
+        for (int j = rs[a]; j < re[a]; ++j) {
+            float4 xj = __ldg(&X4[j]);
+            if (is_boundary(xj.z)) continue;
+            float x0, x1;
+            pair_vec<PER>(gw, make_float2(xj.x, xj.y), P.geo, x0, x1);
+            float sq = sq_norm_ref(x0, x1);
+            if (sq > P.T) continue;
+            PairG pg = pair_fast(x0, x1, sq, P.inv_h);
+            float W = wendland_w(pg.q, P.kc);
+            float dW = wendland_dw(pg.q, P.kc);
+            float g0 = pg.xh0 * dW, g1 = pg.xh1 * dW;
+            float V = P.m / xj.z;
+            num += P.m * W;
+            den += V * W;
+            float k0 = V * g0, k1 = V * g1;
+            gs0 += xj.z * k0;
+            gs1 += xj.z * k1;
+            vg0 += k0;
+            vg1 += k1;
+            float xr = -pg.q * P.h;
+            float xi0 = pg.xh0 * xr, xi1 = pg.xh1 * xr;
+            float vw = V * W;
+            ps0 += xi0 * vw;
+            ps1 += xi1 * vw;
+            pm00 += xi0 * k0;
+            pm01 += xi0 * k1;
+            pm10 += xi1 * k0;
+            pm11 += xi1 * k1;
+            ++cnt;
         }
     }
     float rho;
@@ -255,7 +291,7 @@ __global__ void k_mdbc(int nB, const int32_t* __restrict__ bidx, const int32_t* 
     } else {
         rho = P.rho0;
     }
-    X4[s].z = rho;
+    X4[s].z = -rho;  // boundary particles carry the sign bit
     X4[s].w = eos_p(rho, P.eos);
     if (rho_b_out) rho_b_out[b] = rho;
 }
@@ -266,63 +302,63 @@ __global__ void k_mdbc(int nB, const int32_t* __restrict__ bidx, const int32_t* 
 //   M_i = I where the fluid neighbor count < 4; L_i = pinv2x2(M_i)  (deltaPlus.py:240-252)
 //   gradRho^L_i = L_i sum_fluid (rho_i - rho_j) V_j gradW + sum_boundary (rho_i - rho_j) V_j gradW
 //                                                 (densityDiffusion.py:7-46, deltaPlus.py:256-262)
+// The uniform mass m is factored out of the sums.
 // ------------------------------------------------------------------------------------
 template <bool PER>
-__global__ void __launch_bounds__(256) k_pass_a(int64_t n, const float4* __restrict__ X4, float4* __restrict__ V4,
-                                                const int32_t* __restrict__ nbr, const int32_t* __restrict__ ncnt,
-                                                const int32_t* __restrict__ uid, Phys P, RhsOut out) {
-    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    int cnt = ncnt[i];
-    if (cnt == 0) return;  // boundary rows
-    float4 xi = X4[i];
+__global__ void __launch_bounds__(kPassThreads) k_pass_a(int64_t n, const float4* __restrict__ X4,
+                                                         float4* __restrict__ V4, const int32_t* __restrict__ start,
+                                                         Grid g, const int32_t* __restrict__ uid, Phys P, RhsOut out) {
+    __shared__ int32_t s_list[kPassWarps][kCap * 32];
+    int64_t i = (int64_t)blockIdx.x * kPassThreads + threadIdx.x;
+    bool inb = i < n;
+    float4 xi = inb ? X4[i] : make_float4(0.f, 0.f, -1.f, 0.f);
+    bool active = inb && !is_boundary(xi.z);
     float2 pi = make_float2(xi.x, xi.y);
+    float rhoi = xi.z;
     float M00 = 0.f, M01 = 0.f, M10 = 0.f, M11 = 0.f;
     float gf0 = 0.f, gf1 = 0.f, gb0 = 0.f, gb1 = 0.f;
-    int nf = 0;
-    for (int k = 0; k < cnt; ++k) {
-        int e = __ldg(&nbr[(size_t)k * n + i]);
-        int j = e & 0x7fffffff;
+    int nf = 0, nbnd = 0;
+    neighbor_loop<PER>(active, pi, X4, start, g, P, s_list[threadIdx.x >> 5], [&](int j) {
         float4 xj = __ldg(&X4[j]);
         float x0, x1;
         pair_vec<PER>(pi, make_float2(xj.x, xj.y), P.geo, x0, x1);
-        float sq = sq_norm_ref(x0, x1);
-        if (sq > P.h_cut) continue;
-        float r, q;
-        if (!exact_in(sq, P.h, r, q)) continue;
-        float den_r = __fadd_rn(r, 1e-7f);
-        float xh0 = __fdiv_rn(x0, den_r), xh1 = __fdiv_rn(x1, den_r);
-        float dW = wendland_dw(q, P.kc);
-        float V = P.m / xj.z;
-        float k0 = V * (xh0 * dW), k1 = V * (xh1 * dW);
-        float dr = -(q * P.h);
-        float d0 = dr * xh0, d1 = dr * xh1;
-        M00 += d0 * k0;
-        M01 += d0 * k1;
-        M10 += d1 * k0;
-        M11 += d1 * k1;
-        float drho = xi.z - xj.z;
-        if (e < 0) {
-            gb0 += drho * k0;
-            gb1 += drho * k1;
+        PairG pg = pair_fast(x0, x1, sq_norm_ref(x0, x1), P.inv_h);
+        float dW = wendland_dw(pg.q, P.kc);
+        float rj = fabsf(xj.z);
+        float w = dW * __fdividef(1.0f, rj);
+        float k0 = pg.xh0 * w, k1 = pg.xh1 * w;
+        float d0 = -pg.r * pg.xh0, d1 = -pg.r * pg.xh1;
+        M00 = fmaf(d0, k0, M00);
+        M01 = fmaf(d0, k1, M01);
+        M10 = fmaf(d1, k0, M10);
+        M11 = fmaf(d1, k1, M11);
+        float drho = rhoi - rj;
+        if (is_boundary(xj.z)) {
+            gb0 = fmaf(drho, k0, gb0);
+            gb1 = fmaf(drho, k1, gb1);
+            ++nbnd;
         } else {
-            gf0 += drho * k0;
-            gf1 += drho * k1;
+            gf0 = fmaf(drho, k0, gf0);
+            gf1 = fmaf(drho, k1, gf1);
             ++nf;
         }
-    }
+    });
+    if (!active) return;
+    float m = P.m;
     if (nf < 4) {
         M00 = 1.f; M01 = 0.f; M10 = 0.f; M11 = 1.f;
+    } else {
+        M00 *= m; M01 *= m; M10 *= m; M11 *= m;
     }
-    float L[4];
-    pinv2x2_ref(M00, M01, M10, M11, L);
-    float g0 = L[0] * gf0 + L[1] * gf1 + gb0;
-    float g1 = L[2] * gf0 + L[3] * gf1 + gb1;
+    M2 L = pinv2x2_ref(M00, M01, M10, M11);
+    float g0 = m * (L.a * gf0 + L.b * gf1 + gb0);
+    float g1 = m * (L.c * gf0 + L.d * gf1 + gb1);
     *reinterpret_cast<float2*>(&V4[i].z) = make_float2(g0, g1);
-    if (out.grad || out.L) {
+    if (out.grad || out.L || out.nn) {
         int o = uid[i];
+        if (out.nn) { out.nn[2 * o] = nf; out.nn[2 * o + 1] = nbnd; }
         if (out.grad) { out.grad[2 * o] = g0; out.grad[2 * o + 1] = g1; }
-        if (out.L) { out.L[4 * o] = L[0]; out.L[4 * o + 1] = L[1]; out.L[4 * o + 2] = L[2]; out.L[4 * o + 3] = L[3]; }
+        if (out.L) { out.L[4 * o] = L.a; out.L[4 * o + 1] = L.b; out.L[4 * o + 2] = L.c; out.L[4 * o + 3] = L.d; }
     }
 }
 
@@ -338,77 +374,70 @@ __global__ void __launch_bounds__(256) k_pass_a(int64_t n, const float4* __restr
 // MODE 2: final symplectic Euler update (integration.py:381-392, 439-513).
 // ------------------------------------------------------------------------------------
 template <bool PER, int MODE>
-__global__ void __launch_bounds__(256) k_pass_b(int64_t n, const float4* __restrict__ X4, const float4* __restrict__ V4,
-                                                const int32_t* __restrict__ nbr, const int32_t* __restrict__ ncnt,
-                                                const int32_t* __restrict__ uid, Phys P, RhsOut out,
-                                                float2* __restrict__ Xr, const float4* __restrict__ X4n,
-                                                const float4* __restrict__ V4n, float4* __restrict__ X4o,
-                                                float4* __restrict__ V4o, uint32_t* __restrict__ words) {
-    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    int cnt = ncnt[i];
-    if (cnt == 0) {  // boundary rows: static, carried over to the next stage
-        if (MODE != 0) {
-            X4o[i] = X4[i];
-            V4o[i] = V4[i];
-        }
-        return;
-    }
-    float4 xi = X4[i];
-    float4 vi = V4[i];
+__global__ void __launch_bounds__(kPassThreads) k_pass_b(int64_t n, const float4* __restrict__ X4,
+                                                         const float4* __restrict__ V4,
+                                                         const int32_t* __restrict__ start, Grid g,
+                                                         const int32_t* __restrict__ uid, Phys P, RhsOut out,
+                                                         float2* __restrict__ Xr, const float4* __restrict__ X4n,
+                                                         const float4* __restrict__ V4n, float4* __restrict__ X4o,
+                                                         float4* __restrict__ V4o, uint32_t* __restrict__ words) {
+    __shared__ int32_t s_list[kPassWarps][kCap * 32];
+    int64_t i = (int64_t)blockIdx.x * kPassThreads + threadIdx.x;
+    bool inb = i < n;
+    float4 xi = inb ? X4[i] : make_float4(0.f, 0.f, -1.f, 0.f);
+    float4 vi = inb ? V4[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    bool active = inb && !is_boundary(xi.z);
     float2 pi = make_float2(xi.x, xi.y);
     float rhoi = xi.z, pri = xi.w;
     float ac = 0.f, ad = 0.f, ap0 = 0.f, ap1 = 0.f, av0 = 0.f, av1 = 0.f, ab0 = 0.f, ab1 = 0.f;
-    for (int k = 0; k < cnt; ++k) {
-        int e = __ldg(&nbr[(size_t)k * n + i]);
-        int j = e & 0x7fffffff;
+    neighbor_loop<PER>(active, pi, X4, start, g, P, s_list[threadIdx.x >> 5], [&](int j) {
         float4 xj = __ldg(&X4[j]);
+        float4 vj = __ldg(&V4[j]);
         float x0, x1;
         pair_vec<PER>(pi, make_float2(xj.x, xj.y), P.geo, x0, x1);
-        float sq = sq_norm_ref(x0, x1);
-        if (sq > P.h_cut) continue;
-        float r, q;
-        if (!exact_in(sq, P.h, r, q)) continue;
-        float4 vj = __ldg(&V4[j]);
-        float den_r = __fadd_rn(r, 1e-7f);
-        float xh0 = __fdiv_rn(x0, den_r), xh1 = __fdiv_rn(x1, den_r);
-        float dW = wendland_dw(q, P.kc);
-        float g0 = xh0 * dW, g1 = xh1 * dW;
-        float rhoj = xj.z;
-        float V = P.m / rhoj;
-        // continuity
-        float kq = ((vj.x - vi.x) * P.m) * g0 + ((vj.y - vi.y) * P.m) * g1;
-        ac += kq * rhoi / rhoj;
-        // pressure
-        float pp = (pri + xj.w) * V;
-        ap0 += pp * g0;
-        ap1 += pp * g1;
-        // viscosity
-        float vr = (vi.x - vj.x) * xh0 + (vi.y - vj.y) * xh1;
-        float rr = q * P.h;
-        if (e < 0) {
-            float piv = vr / (rr + P.bv_eps);
-            float Vb = P.bvisc ? P.m / (rhoi + rhoj) : V;
-            float kv = Vb * piv;
-            ab0 += kv * g0;
-            ab1 += kv * g1;
+        PairG pg = pair_fast(x0, x1, sq_norm_ref(x0, x1), P.inv_h);
+        float dW = wendland_dw(pg.q, P.kc);
+        float g0 = pg.xh0 * dW, g1 = pg.xh1 * dW;
+        float rj = fabsf(xj.z);
+        float irj = __fdividef(1.0f, rj);
+        // continuity: sum (u_j - u_i).gradW / rho_j          (x -m rho_i below)
+        float dug = (vj.x - vi.x) * g0 + (vj.y - vi.y) * g1;
+        ac = fmaf(dug, irj, ac);
+        // pressure: sum (p_i + p_j) / rho_j gradW            (x -m / rho_i below)
+        float pp = (pri + xj.w) * irj;
+        ap0 = fmaf(pp, g0, ap0);
+        ap1 = fmaf(pp, g1, ap1);
+        // viscosity: pi_ij = (u_i - u_j).xhat / (r + eps h^2)
+        float vr = (vi.x - vj.x) * pg.xh0 + (vi.y - vj.y) * pg.xh1;
+        if (is_boundary(xj.z)) {
+            float piv = __fdividef(vr, pg.r + P.bv_eps);
+            float w = P.bvisc ? __fdividef(piv, rhoi + rj) : piv * irj;
+            ab0 = fmaf(w, g0, ab0);
+            ab1 = fmaf(w, g1, ab1);
         } else {
-            float piv = vr / (rr + P.v_eps);
-            float kv = V * piv;
-            av0 += kv * g0;
-            av1 += kv * g1;
-            // delta-SPH density diffusion (fluid neighbors only)
-            float rij = 2.f * (rhoj - rhoi) / (rr + P.diff_eps);
-            float psi0 = -rij * xh0 + (vi.z + vj.z);
-            float psi1 = -rij * xh1 + (vi.w + vj.w);
-            ad += psi0 * (V * g0) + psi1 * (V * g1);
+            float piv = __fdividef(vr, pg.r + P.v_eps);
+            float w = piv * irj;
+            av0 = fmaf(w, g0, av0);
+            av1 = fmaf(w, g1, av1);
+            // delta-SPH density diffusion: psi = -2 (rho_j - rho_i)/(r + 1e-6 h) xhat + (gradRho_i + gradRho_j)
+            float rij = __fdividef(2.f * (rj - rhoi), pg.r + P.diff_eps);
+            float psig = -rij * (pg.xh0 * g0 + pg.xh1 * g1) + (vi.z + vj.z) * g0 + (vi.w + vj.w) * g1;
+            ad = fmaf(psig, irj, ad);
         }
+    });
+    if (!inb) return;
+    if (!active) {  // boundary rows: static, carried over to the next stage
+        if (MODE != 0) {
+            X4o[i] = xi;
+            V4o[i] = vi;
+        }
+        return;
     }
-    float vcoef = (P.visc ? P.v_num : P.v_num) / rhoi;
-    float bcoef = P.bv_num / rhoi;
-    float du0 = (-ap0 / rhoi + P.gx) + (vcoef * av0 + bcoef * ab0);
-    float du1 = (-ap1 / rhoi + P.gy) + (vcoef * av1 + bcoef * ab1);
-    float drho = -ac + P.diff_coef * ad;
+    float m = P.m;
+    float irhoi = 1.0f / rhoi;
+    float du0 = (-m * ap0 * irhoi + P.gx) + (P.v_num * irhoi * m * av0 + P.bv_num * irhoi * m * ab0);
+    float du1 = (-m * ap1 * irhoi + P.gy) + (P.v_num * irhoi * m * av1 + P.bv_num * irhoi * m * ab1);
+    float drho = -m * rhoi * ac + P.diff_coef * m * ad;
     if (MODE == 0) {
         int o = uid[i];
         out.dudt[2 * o] = du0;
@@ -426,8 +455,6 @@ __global__ void __launch_bounds__(256) k_pass_b(int64_t n, const float4* __restr
         float2 w = wrap_pos(xh, P.geo);
         X4o[i] = make_float4(w.x, w.y, rh, eos_p(rh, P.eos));
         V4o[i] = make_float4(u0, u1, 0.f, 0.f);
-        float dx0 = __fsub_rn(xh.x, x.x), dx1 = __fsub_rn(xh.y, x.y);
-        if (2.f * sqrtf(dx0 * dx0 + dx1 * dx1) > P.verlet_lim) atomicOr(&words[0], SPH_FLAG_VERLET);
     } else {
         // v' = v + dudt dt; x' = x + 0.5 (v + v') dt; rho' per density_update
         float4 vn = V4n[i];
@@ -449,10 +476,12 @@ __global__ void __launch_bounds__(256) k_pass_b(int64_t n, const float4* __restr
         V4o[i] = make_float4(u0, u1, 0.f, 0.f);
         float sp = __fsqrt_rn(__fmaf_rn(u1, u1, __fmul_rn(u0, u0)));
         atomicMax(&words[1], __float_as_uint(sp));
-        float dx0 = __fsub_rn(xp.x, x.x), dx1 = __fsub_rn(xp.y, x.y);
-        if (2.f * sqrtf(dx0 * dx0 + dx1 * dx1) > P.verlet_lim) atomicOr(&words[0], SPH_FLAG_VERLET);
         if (!isfinite(u0) || !isfinite(u1) || !isfinite(rnew) || !isfinite(xp.x) || !isfinite(xp.y))
             atomicOr(&words[0], SPH_FLAG_NONFINITE);
+        // the cells of this step's sort must still cover h + the displacement at the shift pass
+        // (the shift clamp adds at most sqrt(2) thr dx, covered by the margin of verlet_lim)
+        float e0 = xp.x - x.x, e1 = xp.y - x.y;
+        if (sqrtf(e0 * e0 + e1 * e1) > P.verlet_lim) atomicOr(&words[0], SPH_FLAG_VERLET);
     }
 }
 
@@ -461,51 +490,48 @@ __global__ void __launch_bounds__(256) k_pass_b(int64_t n, const float4* __restr
 //   dx_i = clamp(-CFL Ma (2h/kappa)^2 sum (1 + R (W/W0)^n) m_j/(rho_i+rho_j) gradW, +-thr dx)
 // ------------------------------------------------------------------------------------
 template <bool PER>
-__global__ void __launch_bounds__(256) k_shift(int64_t n, const float4* __restrict__ X4, const float4* __restrict__ V4,
-                                               const int32_t* __restrict__ nbr, const int32_t* __restrict__ ncnt,
-                                               Phys P, float2* __restrict__ Xr, float4* __restrict__ X4o,
-                                               float4* __restrict__ V4o, const uint32_t* __restrict__ words,
-                                               int enabled, const int32_t* __restrict__ uid, float* __restrict__ dx_out) {
-    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    int cnt = ncnt[i];
-    float4 xi = X4[i];
+__global__ void __launch_bounds__(kPassThreads) k_shift(int64_t n, const float4* __restrict__ X4,
+                                                        const float4* __restrict__ V4,
+                                                        const int32_t* __restrict__ start, Grid g, Phys P,
+                                                        float2* __restrict__ Xr, float4* __restrict__ X4o,
+                                                        float4* __restrict__ V4o, const uint32_t* __restrict__ words,
+                                                        int enabled, const int32_t* __restrict__ uid,
+                                                        float* __restrict__ dx_out) {
+    __shared__ int32_t s_list[kPassWarps][kCap * 32];
+    int64_t i = (int64_t)blockIdx.x * kPassThreads + threadIdx.x;
+    bool inb = i < n;
+    float4 xi = inb ? X4[i] : make_float4(0.f, 0.f, -1.f, 0.f);
+    bool active = inb && !is_boundary(xi.z) && enabled;
+    float2 pi = make_float2(xi.x, xi.y);
+    float rhoi = xi.z;
+    float s0 = 0.f, s1 = 0.f;
+    neighbor_loop<PER>(active, pi, X4, start, g, P, s_list[threadIdx.x >> 5], [&](int j) {
+        float4 xj = __ldg(&X4[j]);
+        float x0, x1;
+        pair_vec<PER>(pi, make_float2(xj.x, xj.y), P.geo, x0, x1);
+        PairG pg = pair_fast(x0, x1, sq_norm_ref(x0, x1), P.inv_h);
+        float W = wendland_w(pg.q, P.kc);
+        float dW = wendland_dw(pg.q, P.kc);
+        float kk = W * P.invW0;
+        float kn = P.shN4 ? (kk * kk) * (kk * kk) : powf(kk, P.shN);
+        float c = (1.f + P.shR * kn) * __fdividef(1.0f, rhoi + fabsf(xj.z));
+        s0 = fmaf(c, pg.xh0 * dW, s0);
+        s1 = fmaf(c, pg.xh1 * dW, s1);
+    });
+    if (!inb) return;
     float4 vi = V4[i];
-    if (cnt == 0 || !enabled) {
+    if (!active) {
         X4o[i] = xi;
         V4o[i] = vi;
-        if (dx_out && cnt != 0) {
+        if (dx_out && !is_boundary(xi.z)) {
             int o = uid[i];
             dx_out[2 * o] = 0.f;
             dx_out[2 * o + 1] = 0.f;
         }
         return;
     }
-    float2 pi = make_float2(xi.x, xi.y);
-    float s0 = 0.f, s1 = 0.f;
-    for (int k = 0; k < cnt; ++k) {
-        int e = __ldg(&nbr[(size_t)k * n + i]);
-        int j = e & 0x7fffffff;
-        float4 xj = __ldg(&X4[j]);
-        float x0, x1;
-        pair_vec<PER>(pi, make_float2(xj.x, xj.y), P.geo, x0, x1);
-        float sq = sq_norm_ref(x0, x1);
-        if (sq > P.h_cut) continue;
-        float r, q;
-        if (!exact_in(sq, P.h, r, q)) continue;
-        float den_r = __fadd_rn(r, 1e-7f);
-        float xh0 = __fdiv_rn(x0, den_r), xh1 = __fdiv_rn(x1, den_r);
-        float W = wendland_w(q, P.kc);
-        float dW = wendland_dw(q, P.kc);
-        float kk = W / P.W0;
-        float term = 1.f + P.shR * powf(kk, P.shN);
-        float dens = P.m / (xi.z + xj.z);
-        float c = term * dens;
-        s0 += c * (xh0 * dW);
-        s1 += c * (xh1 * dW);
-    }
     float Ma = P.compute_mach ? __uint_as_float(words[1]) * P.inv_cs : 0.1f;
-    float sc = P.sh_scale * Ma;
+    float sc = P.sh_scale * Ma * P.m;
     // update = clamp(-(sc * s)); x_new = x - update; the reference then adds (x_new - x) to x
     float up0 = fminf(fmaxf(-(sc * s0), -P.sh_thr), P.sh_thr);
     float up1 = fminf(fmaxf(-(sc * s1), -P.sh_thr), P.sh_thr);
@@ -531,7 +557,7 @@ __global__ void k_maxvel(int64_t n, const float4* __restrict__ V4, uint32_t* __r
         float4 v = V4[i];
         sp = __fsqrt_rn(__fmaf_rn(v.y, v.y, __fmul_rn(v.x, v.x)));
     }
-    for (int o = 16; o > 0; o >>= 1) sp = fmaxf(sp, __shfl_xor_sync(0xffffffffu, sp, o));
+    for (int o = 16; o > 0; o >>= 1) sp = fmaxf(sp, __shfl_xor_sync(kFull, sp, o));
     if ((threadIdx.x & 31) == 0) atomicMax(&words[1], __float_as_uint(sp));
 }
 
@@ -546,7 +572,6 @@ struct sph_solver {
     sph_params_t prm;
     Phys P;
     int64_t nF, nB, n;
-    int K;
     Grid grid;
     int64_t ncells;
     bool periodic;
@@ -555,22 +580,30 @@ struct sph_solver {
     float4 *Vc, *Vh, *Vf, *Vt;
     int32_t *uid, *uid_t;
     int32_t *key, *perm, *count, *fill, *start, *scan32;
-    int32_t *nbr, *ncnt, *bidx;
+    int32_t* bidx;
     uint32_t* words;  // [0] flags, [1] max |u| bits, [2] boundary count
     float2* bnormal;
     float* bdist;
     // timing
     uint32_t timing_mask = 0;
-    struct Ev { cudaEvent_t a, b; int cls; };
+    struct Ev {
+        cudaEvent_t a, b;
+        int cls;
+    };
     std::vector<Ev> pool;
     size_t used = 0;
 };
+
+// Cells of half the search radius with a 5x5 stencil: the stencil covers skin * h around
+// the cell, with fewer candidates than a 3x3 stencil of full-radius cells.
+constexpr int kSolverRad = 2;
+static double cell_size(const sph_params_t* p) { return p->support * p->skin * (1.0 + 1e-4) / kSolverRad; }
 
 static size_t solver_layout(const sph_params_t* p, int64_t nF, int64_t nB, void* ws, sph_solver* S) {
     int64_t n = nF + nB;
     int per[2] = {p->domain.periodic[0], p->domain.periodic[1]};
     int64_t ncells = 0;
-    Grid g = make_grid(p->domain.min, p->domain.max, per, p->support * p->skin * (1.0 + 1e-4), &ncells);
+    Grid g = make_grid(p->domain.min, p->domain.max, per, cell_size(p), &ncells, kSolverRad);
     Carver c{(char*)ws};
     float2* Xr = c.take<float2>(n);
     float2* Xr_t = c.take<float2>(n);
@@ -586,8 +619,6 @@ static size_t solver_layout(const sph_params_t* p, int64_t nF, int64_t nB, void*
     int32_t* fill = c.take<int32_t>(ncells);
     int32_t* start = c.take<int32_t>(ncells + 1);
     int32_t* scan32 = c.take<int32_t>(scan_tmp_elems(ncells));
-    int32_t* nbr = c.take<int32_t>((int64_t)p->capacity * n);
-    int32_t* ncnt = c.take<int32_t>(n);
     int32_t* bidx = c.take<int32_t>(nB);
     uint32_t* words = c.take<uint32_t>(8);
     float2* bnormal = c.take<float2>(nB);
@@ -601,7 +632,7 @@ static size_t solver_layout(const sph_params_t* p, int64_t nF, int64_t nB, void*
         S->Vc = V[0]; S->Vh = V[1]; S->Vf = V[2]; S->Vt = V[3];
         S->uid = uid; S->uid_t = uid_t;
         S->key = key; S->perm = perm; S->count = count; S->fill = fill; S->start = start; S->scan32 = scan32;
-        S->nbr = nbr; S->ncnt = ncnt; S->bidx = bidx; S->words = words;
+        S->bidx = bidx; S->words = words;
         S->bnormal = bnormal; S->bdist = bdist;
     }
     return c.off;
@@ -610,15 +641,29 @@ static size_t solver_layout(const sph_params_t* p, int64_t nF, int64_t nB, void*
 static int check_params(const sph_params_t* p, int64_t nF, int64_t nB) {
     if (!p || nF < 1 || nB < 0 || nF + nB >= ((int64_t)1 << 31) - 1) return SPH_ERR_ARGUMENT;
     if (!(p->support > 0) || !(p->dx > 0) || !(p->mass > 0) || !(p->rho0 > 0) || !(p->cs > 0)) return SPH_ERR_ARGUMENT;
-    if (!(p->skin >= 1.0) || p->capacity < 1 || !(p->kernel_scale > 0)) return SPH_ERR_ARGUMENT;
+    if (!(p->skin >= 1.0) || !(p->kernel_scale > 0)) return SPH_ERR_ARGUMENT;
     for (int a = 0; a < 2; ++a)
         if (!(p->domain.max[a] > p->domain.min[a])) return SPH_ERR_ARGUMENT;
     int per[2] = {p->domain.periodic[0], p->domain.periodic[1]};
     int64_t ncells = 0;
-    make_grid(p->domain.min, p->domain.max, per, p->support * p->skin * (1.0 + 1e-4), &ncells);
+    make_grid(p->domain.min, p->domain.max, per, cell_size(p), &ncells, kSolverRad);
     if (ncells > ((int64_t)1 << 28)) return SPH_ERR_ARGUMENT;
-    if ((int64_t)p->capacity * (nF + nB) >= ((int64_t)1 << 40)) return SPH_ERR_ARGUMENT;
     return SPH_OK;
+}
+
+// Largest fp32 s with fl(fl(sqrt(s)) / h) <= 1 under IEEE round-to-nearest. Both steps are
+// monotone in s, so the reference's test q <= 1 is exactly s <= T for a uniform h.
+static float exact_threshold(float h) {
+    volatile float hv = h;
+    auto ok = [&](float s) {
+        volatile float r = sqrtf(s);
+        volatile float q = r / hv;
+        return q <= 1.0f;
+    };
+    float s = h * h;
+    for (int k = 0; k < 64 && !ok(s); ++k) s = nextafterf(s, 0.0f);
+    for (int k = 0; k < 64 && ok(nextafterf(s, INFINITY)); ++k) s = nextafterf(s, INFINITY);
+    return s;
 }
 
 static Phys make_phys(const sph_params_t* p, int64_t nF) {
@@ -627,9 +672,8 @@ static Phys make_phys(const sph_params_t* p, int64_t nF) {
     P.geo = make_geo(p->domain.min, p->domain.max, per);
     double h = p->support;
     P.h = (float)h;
-    P.h_cut = (float)(h * h * (1.0 + 1e-5));
-    double rs = p->skin * h;
-    P.skin2 = (float)(rs * rs * (1.0 + 1e-5));
+    P.T = exact_threshold((float)h);
+    P.inv_h = (float)(1.0 / h);
     P.m = (float)p->mass;
     P.dt = (float)p->dt;
     P.dth = (float)(p->dt / 2.0);
@@ -641,7 +685,6 @@ static Phys make_phys(const sph_params_t* p, int64_t nF) {
     P.rho0 = (float)p->rho0;
     P.diff_coef = (float)((float)((float)p->delta * (float)h) / (float)p->kernel_scale * (float)p->cs);
     P.diff_eps = (float)(1e-6f * (float)h);
-    P.visc = p->visc_scheme;
     P.v_eps = (float)p->eps * (float)(h * h);
     P.v_num = p->visc_scheme ? (float)((float)((float)p->alpha * (float)h) * (float)p->cs * (float)p->rho0)
                              : (float)(2.0 * (2 + 2) * p->nu * p->rho0);
@@ -652,15 +695,16 @@ static Phys make_phys(const sph_params_t* p, int64_t nF) {
     P.gx = p->gravity_on ? (float)p->gravity[0] : 0.f;
     P.gy = p->gravity_on ? (float)p->gravity[1] : 0.f;
     P.nF = (int)nF;
-    // W0 = W(dx/h, h) evaluated in fp32 like the reference (shifting.py:122)
-    {
+    {  // W0 = W(dx/h, h) evaluated in fp32 like the reference (shifting.py:122)
         float q0 = (float)p->dx / (float)h;
         float om = 1.f - q0;
         float hh = (float)h;
-        P.W0 = (om * om) * (om * om) * (1.f + 4.f * q0) * (float)(7.0 / M_PI) / (hh * hh);
+        float W0 = (om * om) * (om * om) * (1.f + 4.f * q0) * (float)(7.0 / M_PI) / (hh * hh);
+        P.invW0 = 1.0f / W0;
     }
     P.shR = (float)p->shift_R;
     P.shN = (float)p->shift_n;
+    P.shN4 = p->shift_n == 4.0;
     P.sh_thr = (float)(p->shift_threshold * p->dx);
     {
         float t = (float)h / (float)p->kernel_scale * 2.f;
@@ -669,7 +713,9 @@ static Phys make_phys(const sph_params_t* p, int64_t nF) {
     P.inv_cs = (float)(1.0 / p->cs);
     P.compute_mach = p->compute_mach;
     P.density_update = p->density_update;
-    P.verlet_lim = (float)((p->skin - 1.0) * h);
+    // displacement allowed between the sort and the last pass of the step; the shift clamp
+    // (at most sqrt(2) threshold dx) is reserved out of the cell margin
+    P.verlet_lim = (float)((p->skin - 1.0) * h - 1.5 * p->shift_threshold * p->dx);
     return P;
 }
 
@@ -694,7 +740,6 @@ extern "C" int sph_solver_create(const sph_params_t* params, int64_t n_fluid, in
     S->prm = *params;
     S->nF = n_fluid;
     S->nB = n_boundary;
-    S->K = params->capacity;
     solver_layout(params, n_fluid, n_boundary, workspace, S);
     S->P = make_phys(params, n_fluid);
     S->periodic = params->domain.periodic[0] || params->domain.periodic[1];
@@ -711,7 +756,7 @@ extern "C" void sph_solver_destroy(sph_solver_t* s) {
     delete s;
 }
 
-static inline unsigned blocks_for(int64_t n) { return (unsigned)((n + kBlock - 1) / kBlock); }
+static inline unsigned blocks_for(int64_t n, int threads = kBlock) { return (unsigned)((n + threads - 1) / threads); }
 
 // timing brackets (only for classes in the mask)
 static void tbeg(sph_solver* S, int cls, cudaStream_t st) {
@@ -744,7 +789,7 @@ extern "C" int sph_solver_upload(sph_solver_t* S, const float* x_fluid, const fl
     return cudaGetLastError() == cudaSuccess ? SPH_OK : SPH_ERR_CUDA;
 }
 
-// sort by cell, gather the state into the new order, build candidate lists
+// sort by cell and gather the state into the new order
 static int rebuild(sph_solver* S, cudaStream_t st) {
     tbeg(S, KC_SORT, st);
     if (cell_sort((const float*)S->Xc, 4, S->n, S->grid, S->ncells, S->key, S->perm, S->count, S->fill, S->start,
@@ -760,14 +805,6 @@ static int rebuild(sph_solver* S, cudaStream_t st) {
     std::swap(S->Xc, S->Xt);
     std::swap(S->Vc, S->Vt);
     std::swap(S->uid, S->uid_t);
-    tbeg(S, KC_BUILD, st);
-    if (S->periodic)
-        k_build<true><<<blocks_for(S->n), kBlock, 0, st>>>(S->n, S->K, S->Xc, S->uid, S->start, S->grid, S->P, S->nbr,
-                                                           S->ncnt, S->words);
-    else
-        k_build<false><<<blocks_for(S->n), kBlock, 0, st>>>(S->n, S->K, S->Xc, S->uid, S->start, S->grid, S->P,
-                                                            S->nbr, S->ncnt, S->words);
-    tend(S, KC_BUILD, st);
     return cudaGetLastError() == cudaSuccess ? SPH_OK : SPH_ERR_CUDA;
 }
 
@@ -785,27 +822,29 @@ static void launch_mdbc(sph_solver* S, float4* X4, float* rho_b_out, cudaStream_
 
 static void launch_a(sph_solver* S, float4* X4, float4* V4, RhsOut o, cudaStream_t st) {
     tbeg(S, KC_PASS_A, st);
+    unsigned gb = blocks_for(S->n, kPassThreads);
     if (S->periodic)
-        k_pass_a<true><<<blocks_for(S->n), kBlock, 0, st>>>(S->n, X4, V4, S->nbr, S->ncnt, S->uid, S->P, o);
+        k_pass_a<true><<<gb, kPassThreads, 0, st>>>(S->n, X4, V4, S->start, S->grid, S->uid, S->P, o);
     else
-        k_pass_a<false><<<blocks_for(S->n), kBlock, 0, st>>>(S->n, X4, V4, S->nbr, S->ncnt, S->uid, S->P, o);
+        k_pass_a<false><<<gb, kPassThreads, 0, st>>>(S->n, X4, V4, S->start, S->grid, S->uid, S->P, o);
     tend(S, KC_PASS_A, st);
 }
 
 template <int MODE>
 static void launch_b(sph_solver* S, float4* X4, float4* V4, RhsOut o, float4* X4o, float4* V4o, cudaStream_t st) {
     tbeg(S, KC_PASS_B, st);
+    unsigned gb = blocks_for(S->n, kPassThreads);
     if (S->periodic)
-        k_pass_b<true, MODE><<<blocks_for(S->n), kBlock, 0, st>>>(S->n, X4, V4, S->nbr, S->ncnt, S->uid, S->P, o,
-                                                                  S->Xr, S->Xc, S->Vc, X4o, V4o, S->words);
+        k_pass_b<true, MODE><<<gb, kPassThreads, 0, st>>>(S->n, X4, V4, S->start, S->grid, S->uid, S->P, o, S->Xr,
+                                                          S->Xc, S->Vc, X4o, V4o, S->words);
     else
-        k_pass_b<false, MODE><<<blocks_for(S->n), kBlock, 0, st>>>(S->n, X4, V4, S->nbr, S->ncnt, S->uid, S->P, o,
-                                                                   S->Xr, S->Xc, S->Vc, X4o, V4o, S->words);
+        k_pass_b<false, MODE><<<gb, kPassThreads, 0, st>>>(S->n, X4, V4, S->start, S->grid, S->uid, S->P, o, S->Xr,
+                                                           S->Xc, S->Vc, X4o, V4o, S->words);
     tend(S, KC_PASS_B, st);
 }
 
 static int run_stages(sph_solver* S, cudaStream_t st) {
-    RhsOut none = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    RhsOut none = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     int rc = rebuild(S, st);
     if (rc) return rc;
     // stage 1 at t^n
@@ -823,12 +862,13 @@ static int run_stages(sph_solver* S, cudaStream_t st) {
 static void launch_shift(sph_solver* S, float4* Xin, float4* Vin, float4* Xout, float4* Vout, float* dx_out,
                          cudaStream_t st) {
     tbeg(S, KC_SHIFT, st);
+    unsigned gb = blocks_for(S->n, kPassThreads);
     if (S->periodic)
-        k_shift<true><<<blocks_for(S->n), kBlock, 0, st>>>(S->n, Xin, Vin, S->nbr, S->ncnt, S->P, S->Xr, Xout, Vout,
-                                                           S->words, S->prm.shift_on, S->uid, dx_out);
+        k_shift<true><<<gb, kPassThreads, 0, st>>>(S->n, Xin, Vin, S->start, S->grid, S->P, S->Xr, Xout, Vout,
+                                                   S->words, S->prm.shift_on, S->uid, dx_out);
     else
-        k_shift<false><<<blocks_for(S->n), kBlock, 0, st>>>(S->n, Xin, Vin, S->nbr, S->ncnt, S->P, S->Xr, Xout, Vout,
-                                                            S->words, S->prm.shift_on, S->uid, dx_out);
+        k_shift<false><<<gb, kPassThreads, 0, st>>>(S->n, Xin, Vin, S->start, S->grid, S->P, S->Xr, Xout, Vout,
+                                                    S->words, S->prm.shift_on, S->uid, dx_out);
     tend(S, KC_SHIFT, st);
 }
 
@@ -838,7 +878,7 @@ extern "C" int sph_solver_step(sph_solver_t* S, int32_t n_steps, sph_stream_t st
     for (int it = 0; it < n_steps; ++it) {
         int rc = run_stages(S, st);
         if (rc) return rc;
-        // delta+ shifting at the integrated positions, on the same candidate lists
+        // delta+ shifting at the integrated positions, on the same cell sort
         launch_shift(S, S->Xf, S->Vf, S->Xc, S->Vc, nullptr, st);
         if (cudaGetLastError() != cudaSuccess) return SPH_ERR_CUDA;
     }
@@ -869,12 +909,12 @@ extern "C" int sph_solver_shift(sph_solver_t* S, float* dx_out, sph_stream_t str
 }
 
 extern "C" int sph_solver_rhs(sph_solver_t* S, float* dudt, float* drhodt, float* grad_rho, float* L, float* pressure,
-                              float* rho_boundary, sph_stream_t stream) {
+                              float* rho_boundary, int32_t* num_neighbors, sph_stream_t stream) {
     if (!S || !dudt || !drhodt) return SPH_ERR_ARGUMENT;
     cudaStream_t st = (cudaStream_t)stream;
     int rc = rebuild(S, st);
     if (rc) return rc;
-    RhsOut o = {dudt, drhodt, grad_rho, L, pressure, rho_boundary};
+    RhsOut o = {dudt, drhodt, grad_rho, L, pressure, rho_boundary, num_neighbors};
     launch_mdbc(S, S->Xc, rho_boundary, st);
     launch_a(S, S->Xc, S->Vc, o, st);
     launch_b<0>(S, S->Xc, S->Vc, o, nullptr, nullptr, st);
@@ -901,8 +941,8 @@ extern "C" int sph_solver_flags(sph_solver_t* S, uint32_t* flags_host, sph_strea
 
 extern "C" int sph_solver_launches_per_step(const sph_solver_t* S) {
     if (!S) return -1;
-    // keys, scan (3), scatter, cell order, gather, build, 2 x (mdbc?, pass A, pass B), shift
-    return 8 + 2 * ((S->nB > 0 ? 1 : 0) + 2) + 1;
+    // cell keys, scan (3), scatter, cell order, gather, 2 x (mdbc?, pass A, pass B), shift
+    return 7 + 2 * ((S->nB > 0 ? 1 : 0) + 2) + 1;
 }
 
 extern "C" int sph_solver_kernel_classes(void) { return KC_COUNT; }

@@ -206,11 +206,12 @@ class Solver:
     def rhs(self):
         o = {"dudt": torch.empty(self.nF, 2, device="cuda"), "drhodt": torch.empty(self.nF, device="cuda"),
              "gradRho^L": torch.empty(self.nF, 2, device="cuda"), "L": torch.empty(self.nF, 2, 2, device="cuda"),
-             "pressures": torch.empty(self.nF, device="cuda")}
+             "pressures": torch.empty(self.nF, device="cuda"),
+             "numNeighbors": torch.empty(self.nF, 2, dtype=torch.int32, device="cuda")}
         rb = torch.empty(self.nB, device="cuda") if self.nB else None
         _lib.check("sph_solver_rhs", self.lib.sph_solver_rhs(
             self.handle, _ptr(o["dudt"]), _ptr(o["drhodt"]), _ptr(o["gradRho^L"]), _ptr(o["L"]), _ptr(o["pressures"]),
-            _ptr(rb), _stream()))
+            _ptr(rb), _ptr(o["numNeighbors"]), _stream()))
         if self.nB:
             o["boundary_densities"] = rb
         return o

@@ -134,11 +134,12 @@ int sph_solver_integrate(sph_solver_t* s, sph_stream_t stream);
  * original order when dx != NULL. */
 int sph_solver_shift(sph_solver_t* s, float* dx, sph_stream_t stream);
 
-/* Evaluates one right-hand side at the current state (the first stage of a step) and
- * writes, in the original order, dudt[nF][2], drhodt[nF], and optionally (NULL to skip)
- * gradRho^L[nF][2], L[nF][4], pressures[nF], boundary densities[nB]. */
+/* Evaluates one right-hand side at the current state (simulationStep, deltaPlus.py:176-422)
+ * and writes, in the original order, dudt[nF][2], drhodt[nF], and optionally (NULL to
+ * skip) gradRho^L[nF][2], L[nF][4], pressures[nF], boundary densities[nB], and the number
+ * of fluid and of boundary neighbors (self included) of every fluid particle nn[nF][2]. */
 int sph_solver_rhs(sph_solver_t* s, float* dudt, float* drhodt, float* grad_rho, float* L,
-                   float* pressure, float* rho_boundary, sph_stream_t stream);
+                   float* pressure, float* rho_boundary, int32_t* num_neighbors, sph_stream_t stream);
 
 /* Writes the current state back in the original order (NULL entries are skipped). */
 int sph_solver_download(sph_solver_t* s, float* x_fluid, float* u_fluid, float* rho_fluid,

@@ -43,9 +43,10 @@ def test_solver_workspace_query(lib):
     p = params_from_config(cfg, float(st["fluid"]["masses"][0]))
     nbytes = ctypes.c_size_t()
     assert lib.sph_solver_workspace_bytes(ctypes.byref(p), 4096, 0, ctypes.byref(nbytes)) == 0
-    # lists dominate: capacity * n * 4 bytes
-    assert nbytes.value > p.capacity * 4096 * 4
-    assert nbytes.value < 4096 * (p.capacity * 4 + 2048)
+    # state: raw positions (2x8 B), four float4 position/density and four velocity buffers
+    # (8x16 B), ids, sort keys (4x4 B) plus the cell tables
+    assert nbytes.value > 4096 * (16 + 128 + 16)
+    assert nbytes.value < 4096 * 1024
 
 
 def test_solver_rejects_bad_parameters(lib):
@@ -77,7 +78,7 @@ def test_neighbor_workspace_query(lib):
 def test_kernel_classes(lib):
     k = lib.sph_solver_kernel_classes()
     names = [lib.sph_solver_kernel_name(c).decode() for c in range(k)]
-    assert "pass_b_rates" in names and "build_lists" in names
+    assert "pass_b_rates" in names and "cell_sort" in names
     assert lib.sph_solver_kernel_name(k) is None
 
 

@@ -129,6 +129,11 @@ def test_rhs_matches_oracle(name, cfg, st):
     out = sol.rhs()
     torch.cuda.synchronize()
     f32, f64 = s32["fluid"], s64["fluid"]
+    # the fused passes select exactly the reference's pairs
+    nn = _np(out["numNeighbors"])
+    assert np.array_equal(nn[:, 0], f32["neighborhood"]["numNeighbors"])
+    if "boundary" in st:
+        assert np.array_equal(nn[:, 1], s32["boundaryToFluidNeighborhood"]["numNeighbors"])
     assert_fp32_parity(_np(out["pressures"]), f32["pressures"], f64["pressures"], 1e-5, "pressures")
     assert_fp32_parity(_np(out["gradRho^L"]), f32["gradRho^L"], f64["gradRho^L"], 1e-5, "gradRho^L")
     assert_fp32_parity(_np(out["drhodt"]), drhodt32, drhodt64, 1e-5, "drhodt")
