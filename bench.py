@@ -184,6 +184,7 @@ def run_ours(args):
     nbar = int(offsets[-1].item()) / nF
     del offsets
     stream = torch.cuda.current_stream()
+    shape, shape_ms = sol.autotune()
     for _ in range(args.warmup):
         sol.step(1)
     sol.check()
@@ -274,7 +275,8 @@ def run_ours(args):
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": args.workload, "fluid_particles": nF, "boundary_particles": nB,
                    "mean_neighbors": round(nbar, 3), "l2": "state and lists (> 1 GB) exceed L2; no flush",
-                   "parallelism": "replicas" if world > 1 else "single"},
+                   "parallelism": "replicas" if world > 1 else "single",
+                   "launch_shape": shape, "shape_ms": [round(v, 4) for v in shape_ms]},
         "e2e": e2e,
         "roofline": {"bound": "hbm", "kernel": "pass_b_rates", "achieved": achieved, "peak": pk,
                      "peak_kind": pk_kind, "unit": "GB/s",

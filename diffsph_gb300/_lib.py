@@ -52,7 +52,8 @@ EXPORTS = [
     "sph_solver_workspace_bytes", "sph_solver_create", "sph_solver_destroy", "sph_solver_upload",
     "sph_solver_step", "sph_solver_integrate", "sph_solver_shift", "sph_solver_rhs", "sph_solver_download", "sph_solver_flags",
     "sph_solver_launches_per_step", "sph_solver_kernel_classes", "sph_solver_kernel_name",
-    "sph_solver_set_timing", "sph_solver_kernel_times",
+    "sph_solver_set_timing", "sph_solver_kernel_times", "sph_solver_autotune", "sph_solver_shapes",
+    "sph_solver_set_shape",
 ]
 
 _lib = None
@@ -92,6 +93,9 @@ def load(build_if_missing: bool = False):
         "sph_solver_kernel_classes": ([], ctypes.c_int),
         "sph_solver_kernel_name": ([ctypes.c_int], ctypes.c_char_p),
         "sph_solver_set_timing": ([P, I32], ctypes.c_int),
+        "sph_solver_autotune": ([P, ctypes.POINTER(I32), ctypes.POINTER(ctypes.c_float), P], ctypes.c_int),
+        "sph_solver_shapes": ([], ctypes.c_int),
+        "sph_solver_set_shape": ([P, I32], ctypes.c_int),
         "sph_solver_kernel_times": ([P, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(I32), P], ctypes.c_int),
     }
     for name, (args, res) in sig.items():

@@ -34,9 +34,15 @@ enum KernelClass { KC_SORT = 0, KC_GATHER, KC_MDBC, KC_PASS_A, KC_PASS_B, KC_SHI
 static const char* kClassNames[KC_COUNT] = {"cell_sort", "gather", "mdbc_ghosts", "pass_a_gradient",
                                              "pass_b_rates", "shift"};
 
-constexpr int kPassWarps = 4;
-constexpr int kPassThreads = 32 * kPassWarps;
-constexpr int kCap = 56;  // exact neighbors held per lane before the pair terms are evaluated
+// Launch shapes of the neighbor passes (warps per block, list entry width), picked per
+// problem by sph_solver_autotune; shape 0 is the default.
+struct Shape {
+    int warps;
+    int list16;
+};
+constexpr int kNumShapes = 4;
+static const Shape kShapes[kNumShapes] = {{4, 0}, {4, 1}, {8, 1}, {16, 1}};
+constexpr int kCap = 64;  // exact neighbors held per lane before the pair terms are evaluated
 constexpr int kUnroll = 4;  // stencil candidates tested per lane per step of the scan
 constexpr unsigned kFull = 0xffffffffu;
 
@@ -173,17 +179,26 @@ __device__ __forceinline__ int stencil_ranges(float2 p, const Grid& g, const int
 }
 
 // Each scan step takes up to kUnroll consecutive candidates of the lane's current range,
-// so that several independent loads are in flight per lane.
-template <bool PER, class F>
-__device__ __forceinline__ void neighbor_loop(bool active, float2 pi, const float4* __restrict__ X4,
+// so that several independent loads are in flight per lane. List entries are slot offsets
+// relative to the particle's own slot: int16_t halves the shared memory (leaving more of
+// the unified L1 for the neighbor data) and is used when the grid keeps every stencil
+// within +-32767 slots; an entry that does not fit raises SPH_FLAG_CAPACITY.
+template <typename LT>
+__device__ __forceinline__ bool fits(int d) {
+    return sizeof(LT) >= 4 || (d >= -32768 && d <= 32767);
+}
+
+template <bool PER, typename LT, class F>
+__device__ __forceinline__ void neighbor_loop(bool active, int self, float2 pi, const float4* __restrict__ X4,
                                               const int32_t* __restrict__ start, const Grid& g, const Phys& P,
-                                              int32_t* __restrict__ lst, F&& f) {
+                                              LT* __restrict__ lst, uint32_t* __restrict__ words, F&& f) {
     const int lane = threadIdx.x & 31;
     int rs[kMaxRanges], re[kMaxRanges];
     int nrng = active ? stencil_ranges(pi, g, start, rs, re) : 0;
     int r = 0;
     int s = nrng > 0 ? rs[0] : 0, se = nrng > 0 ? re[0] : 0;
     int cnt = 0;
+    bool overflow = false;
     while (__any_sync(kFull, r < nrng)) {
         if (r < nrng) {
             int m = se - s < kUnroll ? se - s : kUnroll;
@@ -196,7 +211,11 @@ __device__ __forceinline__ void neighbor_loop(bool active, float2 pi, const floa
                 if (u < m) {
                     float x0, x1;
                     pair_vec<PER>(pi, make_float2(xj[u].x, xj[u].y), P.geo, x0, x1);
-                    if (sq_norm_ref(x0, x1) <= P.T) lst[(cnt++) * 32 + lane] = s + u;
+                    if (sq_norm_ref(x0, x1) <= P.T) {
+                        int d = s + u - self;
+                        if (fits<LT>(d)) lst[(cnt++) * 32 + lane] = (LT)d;
+                        else overflow = true;
+                    }
                 }
             }
             s += m;
@@ -211,13 +230,14 @@ __device__ __forceinline__ void neighbor_loop(bool active, float2 pi, const floa
         if (__any_sync(kFull, cnt > kCap - kUnroll)) {
             int mc = (int)__reduce_max_sync(kFull, (unsigned)cnt);
             for (int k = 0; k < mc; ++k)
-                if (k < cnt) f(lst[k * 32 + lane]);
+                if (k < cnt) f(self + (int)lst[k * 32 + lane]);
             cnt = 0;
         }
     }
     int mc = (int)__reduce_max_sync(kFull, (unsigned)cnt);
     for (int k = 0; k < mc; ++k)
-        if (k < cnt) f(lst[k * 32 + lane]);
+        if (k < cnt) f(self + (int)lst[k * 32 + lane]);
+    if (overflow) atomicOr(&words[0], SPH_FLAG_CAPACITY);
 }
 
 // ------------------------------------------------------------------------------------
@@ -304,12 +324,11 @@ __global__ void k_mdbc(int nB, const int32_t* __restrict__ bidx, const int32_t* 
 //                                                 (densityDiffusion.py:7-46, deltaPlus.py:256-262)
 // The uniform mass m is factored out of the sums.
 // ------------------------------------------------------------------------------------
-template <bool PER>
-__global__ void __launch_bounds__(kPassThreads) k_pass_a(int64_t n, const float4* __restrict__ X4,
-                                                         float4* __restrict__ V4, const int32_t* __restrict__ start,
-                                                         Grid g, const int32_t* __restrict__ uid, Phys P, RhsOut out) {
-    __shared__ int32_t s_list[kPassWarps][kCap * 32];
-    int64_t i = (int64_t)blockIdx.x * kPassThreads + threadIdx.x;
+template <bool PER, typename LT>
+__device__ __forceinline__ void pass_a_tile(int64_t i, int64_t n, const float4* __restrict__ X4,
+                                            float4* __restrict__ V4, const int32_t* __restrict__ start, const Grid& g,
+                                            const int32_t* __restrict__ uid, const Phys& P, const RhsOut& out,
+                                            LT* __restrict__ lst, uint32_t* __restrict__ words) {
     bool inb = i < n;
     float4 xi = inb ? X4[i] : make_float4(0.f, 0.f, -1.f, 0.f);
     bool active = inb && !is_boundary(xi.z);
@@ -318,7 +337,7 @@ __global__ void __launch_bounds__(kPassThreads) k_pass_a(int64_t n, const float4
     float M00 = 0.f, M01 = 0.f, M10 = 0.f, M11 = 0.f;
     float gf0 = 0.f, gf1 = 0.f, gb0 = 0.f, gb1 = 0.f;
     int nf = 0, nbnd = 0;
-    neighbor_loop<PER>(active, pi, X4, start, g, P, s_list[threadIdx.x >> 5], [&](int j) {
+    neighbor_loop<PER, LT>(active, (int)i, pi, X4, start, g, P, lst, words, [&](int j) {
         float4 xj = __ldg(&X4[j]);
         float x0, x1;
         pair_vec<PER>(pi, make_float2(xj.x, xj.y), P.geo, x0, x1);
@@ -362,6 +381,20 @@ __global__ void __launch_bounds__(kPassThreads) k_pass_a(int64_t n, const float4
     }
 }
 
+// One block handles 32 W consecutive slots: its warps sit in neighboring cells and share
+// most of their stencil data in L1.
+
+template <bool PER, typename LT, int W>
+__global__ void __launch_bounds__(32 * W) k_pass_a(int64_t n, const float4* __restrict__ X4,
+                                                         float4* __restrict__ V4, const int32_t* __restrict__ start,
+                                                         Grid g, const int32_t* __restrict__ uid, Phys P, RhsOut out,
+                                                         uint32_t* __restrict__ words) {
+    extern __shared__ __align__(16) unsigned char s_dyn[];
+    LT* lst = reinterpret_cast<LT*>(s_dyn) + (threadIdx.x >> 5) * (kCap * 32);
+    pass_a_tile<PER, LT>((int64_t)blockIdx.x * (32 * W) + threadIdx.x, n, X4, V4, start, g, uid, P, out,
+                             lst, words);
+}
+
 // ------------------------------------------------------------------------------------
 // Pass B: rates of one right-hand side and the fused integrator stage.
 //   continuity   -sum m_j (u_j - u_i).gradW rho_i/rho_j          (momentumEquation.py:6-39)
@@ -373,16 +406,14 @@ __global__ void __launch_bounds__(kPassThreads) k_pass_a(int64_t n, const float4
 // MODE 0: write the rates (original order); 1: half step (integration.py:23-32);
 // MODE 2: final symplectic Euler update (integration.py:381-392, 439-513).
 // ------------------------------------------------------------------------------------
-template <bool PER, int MODE>
-__global__ void __launch_bounds__(kPassThreads) k_pass_b(int64_t n, const float4* __restrict__ X4,
-                                                         const float4* __restrict__ V4,
-                                                         const int32_t* __restrict__ start, Grid g,
-                                                         const int32_t* __restrict__ uid, Phys P, RhsOut out,
-                                                         float2* __restrict__ Xr, const float4* __restrict__ X4n,
-                                                         const float4* __restrict__ V4n, float4* __restrict__ X4o,
-                                                         float4* __restrict__ V4o, uint32_t* __restrict__ words) {
-    __shared__ int32_t s_list[kPassWarps][kCap * 32];
-    int64_t i = (int64_t)blockIdx.x * kPassThreads + threadIdx.x;
+template <bool PER, int MODE, typename LT>
+__device__ __forceinline__ void pass_b_tile(int64_t i, int64_t n, const float4* __restrict__ X4,
+                                            const float4* __restrict__ V4, const int32_t* __restrict__ start,
+                                            const Grid& g, const int32_t* __restrict__ uid, const Phys& P,
+                                            const RhsOut& out, float2* __restrict__ Xr,
+                                            const float4* __restrict__ X4n, const float4* __restrict__ V4n,
+                                            float4* __restrict__ X4o, float4* __restrict__ V4o,
+                                            uint32_t* __restrict__ words, LT* __restrict__ lst) {
     bool inb = i < n;
     float4 xi = inb ? X4[i] : make_float4(0.f, 0.f, -1.f, 0.f);
     float4 vi = inb ? V4[i] : make_float4(0.f, 0.f, 0.f, 0.f);
@@ -390,7 +421,7 @@ __global__ void __launch_bounds__(kPassThreads) k_pass_b(int64_t n, const float4
     float2 pi = make_float2(xi.x, xi.y);
     float rhoi = xi.z, pri = xi.w;
     float ac = 0.f, ad = 0.f, ap0 = 0.f, ap1 = 0.f, av0 = 0.f, av1 = 0.f, ab0 = 0.f, ab1 = 0.f;
-    neighbor_loop<PER>(active, pi, X4, start, g, P, s_list[threadIdx.x >> 5], [&](int j) {
+    neighbor_loop<PER, LT>(active, (int)i, pi, X4, start, g, P, lst, words, [&](int j) {
         float4 xj = __ldg(&X4[j]);
         float4 vj = __ldg(&V4[j]);
         float x0, x1;
@@ -485,27 +516,39 @@ __global__ void __launch_bounds__(kPassThreads) k_pass_b(int64_t n, const float4
     }
 }
 
+template <bool PER, int MODE, typename LT, int W>
+__global__ void __launch_bounds__(32 * W) k_pass_b(int64_t n, const float4* __restrict__ X4,
+                                                         const float4* __restrict__ V4,
+                                                         const int32_t* __restrict__ start, Grid g,
+                                                         const int32_t* __restrict__ uid, Phys P, RhsOut out,
+                                                         float2* __restrict__ Xr, const float4* __restrict__ X4n,
+                                                         const float4* __restrict__ V4n, float4* __restrict__ X4o,
+                                                         float4* __restrict__ V4o, uint32_t* __restrict__ words) {
+    extern __shared__ __align__(16) unsigned char s_dyn[];
+    LT* lst = reinterpret_cast<LT*>(s_dyn) + (threadIdx.x >> 5) * (kCap * 32);
+    pass_b_tile<PER, MODE, LT>((int64_t)blockIdx.x * (32 * W) + threadIdx.x, n, X4, V4, start, g, uid, P, out, Xr, X4n,
+                                   V4n, X4o, V4o, words, lst);
+}
+
 // ------------------------------------------------------------------------------------
 // delta+ shifting (shifting.py:119-147, applied as in solveShifting :990-1005)
 //   dx_i = clamp(-CFL Ma (2h/kappa)^2 sum (1 + R (W/W0)^n) m_j/(rho_i+rho_j) gradW, +-thr dx)
 // ------------------------------------------------------------------------------------
-template <bool PER>
-__global__ void __launch_bounds__(kPassThreads) k_shift(int64_t n, const float4* __restrict__ X4,
-                                                        const float4* __restrict__ V4,
-                                                        const int32_t* __restrict__ start, Grid g, Phys P,
-                                                        float2* __restrict__ Xr, float4* __restrict__ X4o,
-                                                        float4* __restrict__ V4o, const uint32_t* __restrict__ words,
-                                                        int enabled, const int32_t* __restrict__ uid,
-                                                        float* __restrict__ dx_out) {
-    __shared__ int32_t s_list[kPassWarps][kCap * 32];
-    int64_t i = (int64_t)blockIdx.x * kPassThreads + threadIdx.x;
+template <bool PER, typename LT>
+__device__ __forceinline__ void shift_tile(int64_t i, int64_t n, const float4* __restrict__ X4,
+                                           const float4* __restrict__ V4, const int32_t* __restrict__ start,
+                                           const Grid& g, const Phys& P, float2* __restrict__ Xr,
+                                           float4* __restrict__ X4o, float4* __restrict__ V4o,
+                                           uint32_t* __restrict__ words, int enabled,
+                                           const int32_t* __restrict__ uid, float* __restrict__ dx_out,
+                                           LT* __restrict__ lst) {
     bool inb = i < n;
     float4 xi = inb ? X4[i] : make_float4(0.f, 0.f, -1.f, 0.f);
     bool active = inb && !is_boundary(xi.z) && enabled;
     float2 pi = make_float2(xi.x, xi.y);
     float rhoi = xi.z;
     float s0 = 0.f, s1 = 0.f;
-    neighbor_loop<PER>(active, pi, X4, start, g, P, s_list[threadIdx.x >> 5], [&](int j) {
+    neighbor_loop<PER, LT>(active, (int)i, pi, X4, start, g, P, lst, words, [&](int j) {
         float4 xj = __ldg(&X4[j]);
         float x0, x1;
         pair_vec<PER>(pi, make_float2(xj.x, xj.y), P.geo, x0, x1);
@@ -549,6 +592,20 @@ __global__ void __launch_bounds__(kPassThreads) k_shift(int64_t n, const float4*
     }
 }
 
+template <bool PER, typename LT, int W>
+__global__ void __launch_bounds__(32 * W) k_shift(int64_t n, const float4* __restrict__ X4,
+                                                        const float4* __restrict__ V4,
+                                                        const int32_t* __restrict__ start, Grid g, Phys P,
+                                                        float2* __restrict__ Xr, float4* __restrict__ X4o,
+                                                        float4* __restrict__ V4o, uint32_t* __restrict__ words,
+                                                        int enabled, const int32_t* __restrict__ uid,
+                                                        float* __restrict__ dx_out) {
+    extern __shared__ __align__(16) unsigned char s_dyn[];
+    LT* lst = reinterpret_cast<LT*>(s_dyn) + (threadIdx.x >> 5) * (kCap * 32);
+    shift_tile<PER, LT>((int64_t)blockIdx.x * (32 * W) + threadIdx.x, n, X4, V4, start, g, P, Xr, X4o, V4o, words, enabled,
+                            uid, dx_out, lst);
+}
+
 // max |u| over all particles (the Mach number of shifting.py:139-142)
 __global__ void k_maxvel(int64_t n, const float4* __restrict__ V4, uint32_t* __restrict__ words) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -582,8 +639,12 @@ struct sph_solver {
     int32_t *key, *perm, *count, *fill, *start, *scan32;
     int32_t* bidx;
     uint32_t* words;  // [0] flags, [1] max |u| bits, [2] boundary count
+    unsigned long long* counters;  // tile counters of the passes (zeroed before each launch)
     float2* bnormal;
     float* bdist;
+    bool list16;          // relative int16 list entries fit every stencil of the grid
+    int shape = 0;        // index into kShapes
+    bool attrs_set = false;
     // timing
     uint32_t timing_mask = 0;
     struct Ev {
@@ -621,6 +682,7 @@ static size_t solver_layout(const sph_params_t* p, int64_t nF, int64_t nB, void*
     int32_t* scan32 = c.take<int32_t>(scan_tmp_elems(ncells));
     int32_t* bidx = c.take<int32_t>(nB);
     uint32_t* words = c.take<uint32_t>(8);
+    unsigned long long* counters = c.take<unsigned long long>(8);
     float2* bnormal = c.take<float2>(nB);
     float* bdist = c.take<float>(nB);
     if (S) {
@@ -632,7 +694,7 @@ static size_t solver_layout(const sph_params_t* p, int64_t nF, int64_t nB, void*
         S->Vc = V[0]; S->Vh = V[1]; S->Vf = V[2]; S->Vt = V[3];
         S->uid = uid; S->uid_t = uid_t;
         S->key = key; S->perm = perm; S->count = count; S->fill = fill; S->start = start; S->scan32 = scan32;
-        S->bidx = bidx; S->words = words;
+        S->bidx = bidx; S->words = words; S->counters = counters;
         S->bnormal = bnormal; S->bdist = bdist;
     }
     return c.off;
@@ -743,6 +805,13 @@ extern "C" int sph_solver_create(const sph_params_t* params, int64_t n_fluid, in
     solver_layout(params, n_fluid, n_boundary, workspace, S);
     S->P = make_phys(params, n_fluid);
     S->periodic = params->domain.periodic[0] || params->domain.periodic[1];
+    {
+        // one-sided slot span of a stencil: rad rows of cells plus rad + 1 cells, at the rest
+        // density (cell/dx)^2 per cell with a 1.5x compression margin
+        double ppc = (cell_size(params) / params->dx) * (cell_size(params) / params->dx);
+        double span = ((double)kSolverRad * S->grid.nc[0] + kSolverRad + 1) * ppc * 1.5;
+        S->list16 = span < 32767.0;
+    }
     *out = S;
     return SPH_OK;
 }
@@ -820,26 +889,80 @@ static void launch_mdbc(sph_solver* S, float4* X4, float* rho_b_out, cudaStream_
     tend(S, KC_MDBC, st);
 }
 
-static void launch_a(sph_solver* S, float4* X4, float4* V4, RhsOut o, cudaStream_t st) {
-    tbeg(S, KC_PASS_A, st);
-    unsigned gb = blocks_for(S->n, kPassThreads);
+template <typename LT, int W>
+static constexpr size_t list_bytes() { return (size_t)W * kCap * 32 * sizeof(LT); }
+
+template <typename LT, int W>
+static void allow_lists_s() {
+    const int b = (int)list_bytes<LT, W>();
+    cudaFuncSetAttribute(k_pass_a<true, LT, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+    cudaFuncSetAttribute(k_pass_a<false, LT, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+    cudaFuncSetAttribute(k_pass_b<true, 0, LT, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+    cudaFuncSetAttribute(k_pass_b<false, 0, LT, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+    cudaFuncSetAttribute(k_pass_b<true, 1, LT, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+    cudaFuncSetAttribute(k_pass_b<false, 1, LT, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+    cudaFuncSetAttribute(k_pass_b<true, 2, LT, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+    cudaFuncSetAttribute(k_pass_b<false, 2, LT, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+    cudaFuncSetAttribute(k_shift<true, LT, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+    cudaFuncSetAttribute(k_shift<false, LT, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+}
+
+static void set_attrs(sph_solver* S) {
+    if (S->attrs_set) return;
+    allow_lists_s<int32_t, 4>();
+    allow_lists_s<int16_t, 4>();
+    allow_lists_s<int16_t, 8>();
+    allow_lists_s<int16_t, 16>();
+    S->attrs_set = true;
+}
+
+// dispatch a launcher template over the shape table
+#define SPH_SHAPE_DISPATCH(S, CALL)                   \
+    switch ((S)->shape) {                             \
+        case 1: CALL(int16_t, 4); break;              \
+        case 2: CALL(int16_t, 8); break;              \
+        case 3: CALL(int16_t, 16); break;             \
+        default: CALL(int32_t, 4); break;             \
+    }
+
+template <typename LT, int W>
+static void launch_a_t(sph_solver* S, float4* X4, float4* V4, RhsOut o, cudaStream_t st) {
+    unsigned gb = (unsigned)((S->n + 32 * W - 1) / (32 * W));
     if (S->periodic)
-        k_pass_a<true><<<gb, kPassThreads, 0, st>>>(S->n, X4, V4, S->start, S->grid, S->uid, S->P, o);
+        k_pass_a<true, LT, W><<<gb, 32 * W, list_bytes<LT, W>(), st>>>(S->n, X4, V4, S->start, S->grid, S->uid, S->P,
+                                                                      o, S->words);
     else
-        k_pass_a<false><<<gb, kPassThreads, 0, st>>>(S->n, X4, V4, S->start, S->grid, S->uid, S->P, o);
+        k_pass_a<false, LT, W><<<gb, 32 * W, list_bytes<LT, W>(), st>>>(S->n, X4, V4, S->start, S->grid, S->uid,
+                                                                       S->P, o, S->words);
+}
+
+static void launch_a(sph_solver* S, float4* X4, float4* V4, RhsOut o, cudaStream_t st) {
+    set_attrs(S);
+    tbeg(S, KC_PASS_A, st);
+#define SPH_CALL_A(LT, W) launch_a_t<LT, W>(S, X4, V4, o, st)
+    SPH_SHAPE_DISPATCH(S, SPH_CALL_A)
+#undef SPH_CALL_A
     tend(S, KC_PASS_A, st);
+}
+
+template <int MODE, typename LT, int W>
+static void launch_b_t(sph_solver* S, float4* X4, float4* V4, RhsOut o, float4* X4o, float4* V4o, cudaStream_t st) {
+    unsigned gb = (unsigned)((S->n + 32 * W - 1) / (32 * W));
+    if (S->periodic)
+        k_pass_b<true, MODE, LT, W><<<gb, 32 * W, list_bytes<LT, W>(), st>>>(
+            S->n, X4, V4, S->start, S->grid, S->uid, S->P, o, S->Xr, S->Xc, S->Vc, X4o, V4o, S->words);
+    else
+        k_pass_b<false, MODE, LT, W><<<gb, 32 * W, list_bytes<LT, W>(), st>>>(
+            S->n, X4, V4, S->start, S->grid, S->uid, S->P, o, S->Xr, S->Xc, S->Vc, X4o, V4o, S->words);
 }
 
 template <int MODE>
 static void launch_b(sph_solver* S, float4* X4, float4* V4, RhsOut o, float4* X4o, float4* V4o, cudaStream_t st) {
+    set_attrs(S);
     tbeg(S, KC_PASS_B, st);
-    unsigned gb = blocks_for(S->n, kPassThreads);
-    if (S->periodic)
-        k_pass_b<true, MODE><<<gb, kPassThreads, 0, st>>>(S->n, X4, V4, S->start, S->grid, S->uid, S->P, o, S->Xr,
-                                                          S->Xc, S->Vc, X4o, V4o, S->words);
-    else
-        k_pass_b<false, MODE><<<gb, kPassThreads, 0, st>>>(S->n, X4, V4, S->start, S->grid, S->uid, S->P, o, S->Xr,
-                                                           S->Xc, S->Vc, X4o, V4o, S->words);
+#define SPH_CALL_B(LT, W) launch_b_t<MODE, LT, W>(S, X4, V4, o, X4o, V4o, st)
+    SPH_SHAPE_DISPATCH(S, SPH_CALL_B)
+#undef SPH_CALL_B
     tend(S, KC_PASS_B, st);
 }
 
@@ -859,16 +982,27 @@ static int run_stages(sph_solver* S, cudaStream_t st) {
     return cudaGetLastError() == cudaSuccess ? SPH_OK : SPH_ERR_CUDA;
 }
 
+template <typename LT, int W>
+static void launch_shift_t(sph_solver* S, float4* Xin, float4* Vin, float4* Xout, float4* Vout, float* dx_out,
+                           cudaStream_t st) {
+    unsigned gb = (unsigned)((S->n + 32 * W - 1) / (32 * W));
+    if (S->periodic)
+        k_shift<true, LT, W><<<gb, 32 * W, list_bytes<LT, W>(), st>>>(S->n, Xin, Vin, S->start, S->grid, S->P, S->Xr,
+                                                                     Xout, Vout, S->words, S->prm.shift_on, S->uid,
+                                                                     dx_out);
+    else
+        k_shift<false, LT, W><<<gb, 32 * W, list_bytes<LT, W>(), st>>>(S->n, Xin, Vin, S->start, S->grid, S->P,
+                                                                      S->Xr, Xout, Vout, S->words, S->prm.shift_on,
+                                                                      S->uid, dx_out);
+}
+
 static void launch_shift(sph_solver* S, float4* Xin, float4* Vin, float4* Xout, float4* Vout, float* dx_out,
                          cudaStream_t st) {
+    set_attrs(S);
     tbeg(S, KC_SHIFT, st);
-    unsigned gb = blocks_for(S->n, kPassThreads);
-    if (S->periodic)
-        k_shift<true><<<gb, kPassThreads, 0, st>>>(S->n, Xin, Vin, S->start, S->grid, S->P, S->Xr, Xout, Vout,
-                                                   S->words, S->prm.shift_on, S->uid, dx_out);
-    else
-        k_shift<false><<<gb, kPassThreads, 0, st>>>(S->n, Xin, Vin, S->start, S->grid, S->P, S->Xr, Xout, Vout,
-                                                    S->words, S->prm.shift_on, S->uid, dx_out);
+#define SPH_CALL_S(LT, W) launch_shift_t<LT, W>(S, Xin, Vin, Xout, Vout, dx_out, st)
+    SPH_SHAPE_DISPATCH(S, SPH_CALL_S)
+#undef SPH_CALL_S
     tend(S, KC_SHIFT, st);
 }
 
@@ -905,6 +1039,44 @@ extern "C" int sph_solver_shift(sph_solver_t* S, float* dx_out, sph_stream_t str
     launch_shift(S, S->Xc, S->Vc, S->Xt, S->Vt, dx_out, st);
     std::swap(S->Xc, S->Xt);
     std::swap(S->Vc, S->Vt);
+    return cudaGetLastError() == cudaSuccess ? SPH_OK : SPH_ERR_CUDA;
+}
+
+extern "C" int sph_solver_autotune(sph_solver_t* S, int32_t* shape_out, float* ms_out, sph_stream_t stream) {
+    if (!S) return SPH_ERR_ARGUMENT;
+    cudaStream_t st = (cudaStream_t)stream;
+    int rc = rebuild(S, st);
+    if (rc) return rc;
+    RhsOut none = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    cudaEvent_t a, b;
+    if (cudaEventCreate(&a) != cudaSuccess || cudaEventCreate(&b) != cudaSuccess) return SPH_ERR_CUDA;
+    uint32_t saved_mask = S->timing_mask;
+    S->timing_mask = 0;
+    float best = 1e30f;
+    int best_shape = 0;
+    for (int k = 0; k < kNumShapes; ++k) {
+        float ms = -1.f;
+        if (!kShapes[k].list16 || S->list16) {
+            S->shape = k;
+            launch_a(S, S->Xc, S->Vc, none, st);  // warm-up
+            cudaEventRecord(a, st);
+            for (int r = 0; r < 3; ++r) launch_a(S, S->Xc, S->Vc, none, st);
+            cudaEventRecord(b, st);
+            if (cudaEventSynchronize(b) != cudaSuccess) return SPH_ERR_CUDA;
+            cudaEventElapsedTime(&ms, a, b);
+            ms /= 3.f;
+            if (ms < best) {
+                best = ms;
+                best_shape = k;
+            }
+        }
+        if (ms_out) ms_out[k] = ms;
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    S->shape = best_shape;
+    S->timing_mask = saved_mask;
+    if (shape_out) *shape_out = best_shape;
     return cudaGetLastError() == cudaSuccess ? SPH_OK : SPH_ERR_CUDA;
 }
 
@@ -946,6 +1118,15 @@ extern "C" int sph_solver_launches_per_step(const sph_solver_t* S) {
 }
 
 extern "C" int sph_solver_kernel_classes(void) { return KC_COUNT; }
+
+extern "C" int sph_solver_shapes(void) { return kNumShapes; }
+
+extern "C" int sph_solver_set_shape(sph_solver_t* S, int32_t shape) {
+    if (!S || shape < 0 || shape >= kNumShapes) return SPH_ERR_ARGUMENT;
+    if (kShapes[shape].list16 && !S->list16) return SPH_ERR_ARGUMENT;
+    S->shape = shape;
+    return SPH_OK;
+}
 
 extern "C" const char* sph_solver_kernel_name(int cls) {
     return (cls >= 0 && cls < KC_COUNT) ? kClassNames[cls] : nullptr;

@@ -231,6 +231,17 @@ class Solver:
         if f & _lib.FLAG_NONFINITE:
             raise _lib.SphError("sph_solver_step", 6)
 
+    def autotune(self):
+        """Pick the fastest launch shape of the neighbor passes for this problem."""
+        k = self.lib.sph_solver_shapes()
+        ms = (ctypes.c_float * k)()
+        shape = ctypes.c_int32()
+        _lib.check("sph_solver_autotune", self.lib.sph_solver_autotune(self.handle, ctypes.byref(shape), ms, _stream()))
+        return int(shape.value), [float(v) for v in ms]
+
+    def set_shape(self, shape: int):
+        _lib.check("sph_solver_set_shape", self.lib.sph_solver_set_shape(self.handle, int(shape)))
+
     def launches_per_step(self) -> int:
         return int(self.lib.sph_solver_launches_per_step(self.handle))
 

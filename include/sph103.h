@@ -148,6 +148,16 @@ int sph_solver_download(sph_solver_t* s, float* x_fluid, float* u_fluid, float* 
 /* Copies the device error flags (SPH_FLAG_*) to *flags_host; synchronises the stream. */
 int sph_solver_flags(sph_solver_t* s, uint32_t* flags_host, sph_stream_t stream);
 
+/* Autotuner: times the neighbor passes under each launch shape (warps per block, width
+ * of the per-warp neighbor list) on the current state and keeps the fastest for all
+ * later launches. Writes the chosen shape and the time of each (ms; -1 when a shape does
+ * not apply) to ms_out[sph_solver_shapes()] when non-NULL. Synchronises the stream. */
+int sph_solver_autotune(sph_solver_t* s, int32_t* shape_out, float* ms_out, sph_stream_t stream);
+int sph_solver_shapes(void);
+/* Forces a launch shape (0 <= shape < sph_solver_shapes()); rejects shapes whose 16-bit
+ * list entries cannot address the grid's stencils. */
+int sph_solver_set_shape(sph_solver_t* s, int32_t shape);
+
 /* Number of kernel launches one sph_solver_step(s, 1, ...) issues. */
 int sph_solver_launches_per_step(const sph_solver_t* s);
 
