@@ -1,0 +1,94 @@
+"""Drop-in versions of the reference's step functions, backed by the sm_103a solver.
+
+Same signatures and return values as:
+
+* ``simulationStep(state, config)``            src/diffSPH/v2/simulationSchemes/deltaPlus.py:176-422
+* ``integrate(simulationStep, perennialState, config, previousStep=None)``
+                                              src/diffSPH/v2/modules/integration.py:92-513
+                                              (scheme 'symplecticEuler')
+* ``solveShifting(simulationState, config)``   src/diffSPH/v2/modules/shifting.py:882-1019
+
+State dicts hold torch tensors (any device). The solver keeps its own copy of the particle
+state on the GPU between calls of one state dict (cached under the key ``'sph103'``), so a
+runner loop ``integrate -> solveShifting -> positions += dx`` re-uploads only what the
+caller changed. ``simulationStep`` writes the intermediates the reference leaves in the
+state (``L``, ``gradRho^L``, ``pressures``, wall densities, ``numNeighbors``).
+"""
+from __future__ import annotations
+
+import torch
+
+from .solver import Solver
+
+_KEY = "sph103"
+
+
+def _boundary(state, config):
+    if bool(config.get("boundary", {}).get("active", False)) and "boundary" in state:
+        return state["boundary"]
+    return None
+
+
+def _solver_for(state, config, upload=True):
+    fl = state["fluid"]
+    bd = _boundary(state, config)
+    sol = state.get(_KEY)
+    nF = int(fl["positions"].shape[0])
+    nB = int(bd["positions"].shape[0]) if bd is not None else 0
+    if sol is None or sol.nF != nF or sol.nB != nB or sol.config is not config:
+        sol = Solver(config, fl, bd)
+        state[_KEY] = sol
+    elif upload:
+        sol.upload(fl, bd)
+    return sol
+
+
+def simulationStep(state, config):
+    """One right-hand side; returns ((u, dudt, drhodt), (u_b, None, drhodt_b))."""
+    sol = _solver_for(state, config)
+    out = sol.rhs()
+    fl = state["fluid"]
+    dev = fl["positions"].device
+    fl["L"] = out["L"].to(dev)
+    fl["gradRho^L"] = out["gradRho^L"].to(dev)
+    fl["pressures"] = out["pressures"].to(dev)
+    fl["numNeighbors"] = out["numNeighbors"][:, 0].to(dev)
+    dudt, drhodt = out["dudt"].to(dev), out["drhodt"].to(dev)
+    u = torch.as_tensor(fl["velocities"]).clone()
+    bd = _boundary(state, config)
+    if bd is None:
+        return (u, dudt, drhodt), (None, None, None)
+    bd["densities"] = out["boundary_densities"].to(bd["positions"].device)
+    return (u, dudt, drhodt), (torch.as_tensor(bd["velocities"]).clone(), None, torch.zeros_like(bd["densities"]))
+
+
+def integrate(simulationStep_, perennialState, config, previousStep=None):
+    """symplecticEuler step of the reference (both right-hand sides fused on the GPU).
+
+    ``simulationStep_`` is accepted for signature compatibility; the fused kernels
+    evaluate the δ-SPH right-hand side themselves. Returns
+    (perennialState, tempState, dxdt, dudt, drhodt) like the reference; the rates of
+    the fused step are not materialised, so the last three are None."""
+    scheme = config.get("integration", {}).get("scheme", "symplecticEuler")
+    if scheme != "symplecticEuler":
+        raise ValueError(f"integration scheme {scheme} is not implemented (symplecticEuler is)")
+    sol = _solver_for(perennialState, config)
+    sol.integrate()
+    got = sol.download()
+    fl = perennialState["fluid"]
+    dev = fl["positions"].device
+    fl["positions"] = got["positions"].to(dev)
+    fl["velocities"] = got["velocities"].to(dev)
+    fl["densities"] = got["densities"].to(dev)
+    bd = _boundary(perennialState, config)
+    if bd is not None:
+        bd["densities"] = got["boundary_densities"].to(bd["positions"].device)
+    return perennialState, {"fluid": fl}, None, None, None
+
+
+def solveShifting(simulationState, config):
+    """δ+ shifting; returns (dx, overallStates) like the reference (overallStates is empty:
+    it only collects IPS solver diagnostics)."""
+    sol = _solver_for(simulationState, config)
+    dx = sol.shift()
+    return dx.to(simulationState["fluid"]["positions"].device), []
