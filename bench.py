@@ -26,8 +26,13 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "particle-steps/s (plain delta-SPH step)"
+# dram__bytes_read + dram__bytes_write of one k_pass_b launch per fluid particle, from the ncu
+# capture summarised in profiles/pass_b_rates_dambreak_dx512.md (22.06 MB / 524,288)
+PASS_B_DRAM_BYTES_PER_PARTICLE = 42.1
+
 WORKLOADS = {
     "dambreak_dx1024": dict(scene="dam_break", dx=1.0 / 1024),
+    "batched_256": dict(scene="batched", domains=256, seed=0),
     "dambreak_dx512": dict(scene="dam_break", dx=1.0 / 512),
     "dambreak_dx256": dict(scene="dam_break", dx=1.0 / 256),
     "tgv_64": dict(scene="taylor_green", nx=64),
@@ -110,7 +115,10 @@ def cpu_baseline(workload, budget_s=20.0):
     from oracle import sph_oracle as O
     from diffsph_gb300 import scenes
     w = WORKLOADS[workload]
-    if w["scene"] == "dam_break":
+    if w["scene"] == "batched":
+        cfg, st = scenes.batched_fourier(1, seed=w.get("seed", 0), n_min=4096, n_max=4096)[0]
+        sample = "one 64x64 domain of the batch generator"
+    elif w["scene"] == "dam_break":
         cfg, st = scenes.dam_break(dx=1.0 / 64)
         sample = "dam break dx=1/64 (same scene and parameters, coarser lattice)"
     else:
@@ -137,7 +145,13 @@ def run_reference(args):
     steps, warm = args.steps, args.warmup
     from oracle import sph_oracle as O
     from diffsph_gb300 import scenes
-    cfg, st = scenes.dam_break(dx=1.0 / 64) if WORKLOADS[args.workload]["scene"] == "dam_break" else make_scene(args.workload)
+    sc = WORKLOADS[args.workload]["scene"]
+    if sc == "dam_break":
+        cfg, st = scenes.dam_break(dx=1.0 / 64)
+    elif sc == "batched":
+        cfg, st = scenes.batched_fourier(1, seed=0, n_min=4096, n_max=4096)[0]
+    else:
+        cfg, st = make_scene(args.workload)
     n = st["fluid"]["positions"].shape[0]
     s = copy.deepcopy(st)
     for _ in range(warm):
@@ -151,7 +165,7 @@ def run_reference(args):
         "impl": "reference", "metric": METRIC, "value": v, "unit": "particle-steps/s", "n_gpus": args.gpus,
         "steps": steps, "warmup": warm, "ms_per_step": 1e3 * dt / steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": args.workload, "sample": f"dam break dx=1/64, {n} fluid particles"},
+        "config": {"workload": args.workload, "sample": f"{sc} sample, {n} fluid particles"},
         "cpu_baseline": {"value": v, "unit": "particle-steps/s", "cores": 1, "kind": "port",
                          "sample": f"{n} fluid particles x {steps} steps"},
         "e2e": {"value": v, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -159,11 +173,49 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+def reduce_max(value, world):
+    """Max over ranks (the slowest rank defines the job time)."""
+    if world <= 1:
+        return value
+    import torch
+    dev = "cuda" if torch.cuda.is_available() and torch.distributed.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(value)], device=dev, dtype=torch.float64)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def build_solver(workload):
+    """Solver, fluid count, boundary count, scene (list of domains for batches)."""
+    import numpy as np
+    from diffsph_gb300 import scenes
+    from diffsph_gb300.neighborhood import exact_pairs
+    from diffsph_gb300.solver import BatchSolver, Solver
+    w = WORKLOADS[workload]
+    if w["scene"] == "batched":
+        doms = scenes.batched_fourier(w["domains"], seed=w.get("seed", 0))
+        sol = BatchSolver([c for c, _ in doms], [s["fluid"] for _, s in doms])
+        nF = sol.nF
+        # exact neighbors per particle, from the largest domain
+        cfg, st = max(doms, key=lambda d: d[1]["fluid"]["positions"].shape[0])
+        fl = st["fluid"]
+        _, off = exact_pairs(fl["positions"], fl["positions"], fl["supports"], cfg, count_only=True)
+        nbar = int(off[-1].item()) / fl["positions"].shape[0]
+        return sol, nF, 0, nbar, doms
+    cfg, st = make_scene(workload)
+    fl, bd = st["fluid"], st.get("boundary")
+    nF = fl["positions"].shape[0]
+    nB = bd["positions"].shape[0] if bd is not None else 0
+    sol = Solver(cfg, fl, bd)
+    allx = fl["positions"] if bd is None else np.concatenate([fl["positions"], bd["positions"]])
+    allh = fl["supports"] if bd is None else np.concatenate([fl["supports"], bd["supports"]])
+    _, off = exact_pairs(fl["positions"], allx, allh, cfg, count_only=True)
+    nbar = int(off[-1].item()) / nF
+    return sol, nF, nB, nbar, st
+
+
 def run_ours(args):
     import torch
     import __graft_entry__ as ge
-    from diffsph_gb300.neighborhood import exact_pairs
-    from diffsph_gb300.solver import Solver
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -172,115 +224,72 @@ def run_ours(args):
         torch.distributed.init_process_group("nccl")
     torch.cuda.set_device(local)
     ge.build()
-    cfg, st = make_scene(args.workload)
-    fl, bd = st["fluid"], st.get("boundary")
-    nF = fl["positions"].shape[0]
-    nB = bd["positions"].shape[0] if bd is not None else 0
-    sol = Solver(cfg, fl, bd)
-    # mean exact neighbors per fluid particle (fluid + boundary neighbors, incl. self)
-    allx = fl["positions"] if bd is None else __import__("numpy").concatenate([fl["positions"], bd["positions"]])
-    allh = fl["supports"] if bd is None else __import__("numpy").concatenate([fl["supports"], bd["supports"]])
-    _, offsets = exact_pairs(fl["positions"], allx, allh, cfg, count_only=True)
-    nbar = int(offsets[-1].item()) / nF
-    del offsets
-    stream = torch.cuda.current_stream()
-    shape, shape_ms = sol.autotune()
-    for _ in range(args.warmup):
-        sol.step(1)
-    sol.check()
+    batched = WORKLOADS[args.workload]["scene"] == "batched"
+    sol, nF, nB, nbar, scene = build_solver(args.workload)
+    stream = torch.cuda.Stream()
     torch.cuda.synchronize()
-    # timed region: device-resident state, CUDA events on the launching stream
-    sol.set_timing(["pass_b_rates", "pass_a_gradient", "shift", "cell_sort", "gather", "mdbc_ghosts"])
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    if world > 1:
-        torch.distributed.barrier()
-    torch.cuda.synchronize()
-    with ClockSampler(local) as clk:
-        e0.record(stream)
-        for _ in range(args.steps):
+    with torch.cuda.stream(stream):
+        shape, shape_ms = sol.autotune()
+        for _ in range(args.warmup):
             sol.step(1)
-        e1.record(stream)
+        sol.check()
+        steps = args.steps + (args.steps & 1 if batched else 0)
+        if batched:
+            sol.graph_step(2)  # capture
+            sol.check()
         torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1)
-    ktimes = sol.kernel_times()
-    sol.set_timing([])
-    sol.check()
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-        torch.distributed.barrier()
-    value = world * nF * args.steps / (ms / 1e3)
-
-    # end to end through the public API with host buffers: every step uploads the state
-    # from pinned host memory, advances one step, and reads the state back
-    hx = torch.from_numpy(fl["positions"]).pin_memory()
-    hu = torch.from_numpy(fl["velocities"]).pin_memory()
-    hr = torch.from_numpy(fl["densities"]).pin_memory()
-    bx = torch.from_numpy(bd["positions"]).pin_memory() if nB else None
-    bn = torch.from_numpy(bd["normals"]).pin_memory() if nB else None
-    bdd = torch.from_numpy(bd["distances"]).pin_memory() if nB else None
-    br = torch.from_numpy(bd["densities"]).pin_memory() if nB else None
-    ox, ou, orr = torch.empty_like(hx).pin_memory(), torch.empty_like(hu).pin_memory(), torch.empty_like(hr).pin_memory()
-    obr = torch.empty_like(br).pin_memory() if nB else None
-    dev = {k: torch.empty(v.shape, device="cuda") for k, v in
-           {"x": hx, "u": hu, "r": hr, **({"bx": bx, "bn": bn, "bd": bdd, "br": br} if nB else {})}.items()}
-    e_steps = max(1, min(args.steps, 10))
-
-    def e2e_step():
-        dev["x"].copy_(hx, non_blocking=True)
-        dev["u"].copy_(hu, non_blocking=True)
-        dev["r"].copy_(hr, non_blocking=True)
-        fluid = {"positions": dev["x"], "velocities": dev["u"], "densities": dev["r"]}
-        bnd = None
-        if nB:
-            for k, h in (("bx", bx), ("bn", bn), ("bd", bdd), ("br", br)):
-                dev[k].copy_(h, non_blocking=True)
-            bnd = {"positions": dev["bx"], "normals": dev["bn"], "distances": dev["bd"], "densities": dev["br"]}
-        sol.upload(fluid, bnd)
-        sol.step(1)
-        got = sol.download()
-        ox.copy_(got["positions"], non_blocking=True)
-        ou.copy_(got["velocities"], non_blocking=True)
-        orr.copy_(got["densities"], non_blocking=True)
-        if nB:
-            obr.copy_(got["boundary_densities"], non_blocking=True)
-
-    for _ in range(2):
-        e2e_step()
-    torch.cuda.synchronize()
-    e0.record(stream)
-    for _ in range(e_steps):
-        e2e_step()
-    e1.record(stream)
-    torch.cuda.synchronize()
-    ms_e2e = e0.elapsed_time(e1)
-    h2d = (hx.numel() + hu.numel() + hr.numel()) * 4 + ((bx.numel() + bn.numel() + bdd.numel() + br.numel()) * 4 if nB else 0)
-    d2h = (ox.numel() + ou.numel() + orr.numel()) * 4 + (obr.numel() * 4 if nB else 0)
-    e2e = {"value": world * nF * e_steps / (ms_e2e / 1e3), "unit": "particle-steps/s",
-           "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "steps": e_steps}
-
+        # timed region: device-resident state, CUDA events on the launching stream
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        if not batched:
+            sol.set_timing(["pass_b_rates", "pass_a_gradient", "shift", "cell_sort", "gather", "mdbc_ghosts"])
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        with ClockSampler(local) as clk:
+            e0.record(stream)
+            if batched:
+                for _ in range(steps // 2):
+                    sol.graph_step(2)
+            else:
+                for _ in range(steps):
+                    sol.step(1)
+            e1.record(stream)
+            torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        if batched:  # per-kernel times from a short event-timed loop of the same step
+            sol.set_timing(["pass_b_rates", "pass_a_gradient", "shift", "cell_sort", "gather", "mdbc_ghosts"])
+            for _ in range(4):
+                sol.step(1)
+        ktimes = sol.kernel_times()
+        sol.set_timing([])
+        sol.check()
+        ms = reduce_max(ms, world)
+        value = world * nF * steps / (ms / 1e3)
+        e2e = run_e2e(sol, scene, batched, nF, world, min(steps, 10), stream)
     pk, pk_kind = peaks()
     ab = algorithmic_bytes(nbar)
     pb_ms, pb_n = ktimes.get("pass_b_rates", (0.0, 0))
     pb_avg = pb_ms / max(pb_n, 1)
     achieved = ab["pass_b"] * nF / (pb_avg / 1e3) / 1e9 if pb_avg > 0 else None
-    step_achieved = ab["step"] * nF * args.steps / (ms / 1e3) / 1e9
-    launches = sol.launches_per_step() * args.steps
+    step_achieved = ab["step"] * nF * steps / (ms / 1e3) / 1e9
+    launches = sol.launches_per_step() * steps
     if rank != 0:
         return
     line = {
-        "metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": world, "steps": steps,
+        "warmup": args.warmup, "ms_per_step": ms / steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": args.workload, "fluid_particles": nF, "boundary_particles": nB,
-                   "mean_neighbors": round(nbar, 3), "l2": "state and lists (> 1 GB) exceed L2; no flush",
-                   "parallelism": "replicas" if world > 1 else "single",
+                   "mean_neighbors": round(nbar, 3), "l2": "state (> 160 MB) exceeds L2; no flush",
+                   "parallelism": "replicas" if world > 1 else "single", "graph": batched,
                    "launch_shape": shape, "shape_ms": [round(v, 4) for v in shape_ms]},
         "e2e": e2e,
         "roofline": {"bound": "hbm", "kernel": "pass_b_rates", "achieved": achieved, "peak": pk,
                      "peak_kind": pk_kind, "unit": "GB/s",
-                     "frac": (achieved / pk) if achieved else None, "traffic": None,
+                     "frac": (achieved / pk) if achieved else None,
+                     "traffic": PASS_B_DRAM_BYTES_PER_PARTICLE * nF,
+                     "traffic_note": "ncu dram bytes of k_pass_b on dambreak_dx512 (42.1 B/particle), "
+                                     "scaled by the particle count",
                      "alg_bytes_per_particle": ab["pass_b"], "avg_launch_ms": pb_avg,
                      "step_alg_bytes_per_particle": ab["step"], "step_achieved_gbs": step_achieved,
                      "step_frac": step_achieved / pk},
@@ -291,6 +300,54 @@ def run_ours(args):
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(args.workload, budget_s=args.cpu_budget)
     print(json.dumps(line))
+
+
+def run_e2e(sol, scene, batched, nF, world, e_steps, stream):
+    """Same metric through the public API with host buffers: every step uploads the state
+    from pinned host memory, advances one step and reads the state back."""
+    import torch
+    if batched:
+        fl = {k: torch.cat([torch.from_numpy(s["fluid"][k]) for _, s in scene]) for k in
+              ("positions", "velocities", "densities")}
+        bd = None
+    else:
+        fl = {k: torch.from_numpy(scene["fluid"][k]) for k in ("positions", "velocities", "densities")}
+        bd = ({k: torch.from_numpy(scene["boundary"][k]) for k in ("positions", "normals", "distances", "densities")}
+              if "boundary" in scene else None)
+    host_in = {("f", k): v.pin_memory() for k, v in fl.items()}
+    if bd is not None:
+        host_in.update({("b", k): v.pin_memory() for k, v in bd.items()})
+    dev_in = {k: torch.empty(v.shape, device="cuda") for k, v in host_in.items()}
+    host_out = {k: torch.empty(v.shape).pin_memory() for k, v in fl.items()}
+    if bd is not None:
+        host_out["boundary_densities"] = torch.empty(bd["densities"].shape).pin_memory()
+
+    def one():
+        for k, v in host_in.items():
+            dev_in[k].copy_(v, non_blocking=True)
+        f = {k: dev_in[("f", k)] for k in ("positions", "velocities", "densities")}
+        b = ({k: dev_in[("b", k)] for k in ("positions", "normals", "distances", "densities")}
+             if bd is not None else None)
+        sol.upload(f, b)
+        sol.step(1)
+        got = sol.download()
+        for k, v in host_out.items():
+            v.copy_(got[k], non_blocking=True)
+
+    for _ in range(2):
+        one()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(e_steps):
+        one()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = reduce_max(e0.elapsed_time(e1), world)
+    h2d = sum(v.numel() * 4 for v in host_in.values())
+    d2h = sum(v.numel() * 4 for v in host_out.values())
+    return {"value": world * nF * e_steps / (ms / 1e3), "unit": "particle-steps/s",
+            "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "steps": e_steps}
 
 
 def main():

@@ -53,7 +53,7 @@ EXPORTS = [
     "sph_solver_step", "sph_solver_integrate", "sph_solver_shift", "sph_solver_rhs", "sph_solver_download", "sph_solver_flags",
     "sph_solver_launches_per_step", "sph_solver_kernel_classes", "sph_solver_kernel_name",
     "sph_solver_set_timing", "sph_solver_kernel_times", "sph_solver_autotune", "sph_solver_shapes",
-    "sph_solver_set_shape",
+    "sph_solver_set_shape", "sph_batch_workspace_bytes", "sph_batch_create", "sph_solver_graph_step",
 ]
 
 _lib = None
@@ -96,6 +96,9 @@ def load(build_if_missing: bool = False):
         "sph_solver_autotune": ([P, ctypes.POINTER(I32), ctypes.POINTER(ctypes.c_float), P], ctypes.c_int),
         "sph_solver_shapes": ([], ctypes.c_int),
         "sph_solver_set_shape": ([P, I32], ctypes.c_int),
+        "sph_batch_workspace_bytes": ([PP, ctypes.POINTER(I64), I32, ctypes.POINTER(SZ)], ctypes.c_int),
+        "sph_batch_create": ([PP, ctypes.POINTER(I64), I32, P, SZ, ctypes.POINTER(P)], ctypes.c_int),
+        "sph_solver_graph_step": ([P, I32, P], ctypes.c_int),
         "sph_solver_kernel_times": ([P, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(I32), P], ctypes.c_int),
     }
     for name, (args, res) in sig.items():

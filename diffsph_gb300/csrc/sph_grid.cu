@@ -185,18 +185,25 @@ __global__ void k_cell_order(int64_t ncells, const int32_t* __restrict__ start, 
     }
 }
 
+cudaError_t cell_sort_counted(int64_t n, int64_t ncells, const int32_t* key, int32_t* perm, int32_t* count,
+                              int32_t* fill, int32_t* start, int32_t* scan_tmp, cudaStream_t s) {
+    cudaError_t e;
+    if ((e = cudaMemsetAsync(fill, 0, sizeof(int32_t) * ncells, s)) != cudaSuccess) return e;
+    if ((e = scan_exclusive(count, start, ncells, scan_tmp, s)) != cudaSuccess) return e;
+    unsigned gb = (unsigned)((n + kBlock - 1) / kBlock);
+    if (n > 0) k_cell_scatter<<<gb, kBlock, 0, s>>>(n, key, start, fill, perm);
+    k_cell_order<<<(unsigned)((ncells + kBlock - 1) / kBlock), kBlock, 0, s>>>(ncells, start, perm);
+    return cudaGetLastError();
+}
+
 cudaError_t cell_sort(const float* xy, int stride, int64_t n, const Grid& g, int64_t ncells,
                       int32_t* key, int32_t* perm, int32_t* count, int32_t* fill, int32_t* start,
                       int32_t* scan_tmp, cudaStream_t s) {
     cudaError_t e;
     if ((e = cudaMemsetAsync(count, 0, sizeof(int32_t) * ncells, s)) != cudaSuccess) return e;
-    if ((e = cudaMemsetAsync(fill, 0, sizeof(int32_t) * ncells, s)) != cudaSuccess) return e;
     unsigned gb = (unsigned)((n + kBlock - 1) / kBlock);
     if (n > 0) k_cell_keys<<<gb, kBlock, 0, s>>>(xy, stride, n, g, key, count);
-    if ((e = scan_exclusive(count, start, ncells, scan_tmp, s)) != cudaSuccess) return e;
-    if (n > 0) k_cell_scatter<<<gb, kBlock, 0, s>>>(n, key, start, fill, perm);
-    k_cell_order<<<(unsigned)((ncells + kBlock - 1) / kBlock), kBlock, 0, s>>>(ncells, start, perm);
-    return cudaGetLastError();
+    return cell_sort_counted(n, ncells, key, perm, count, fill, start, scan_tmp, s);
 }
 
 // ------------------------------------------------------------------------------------

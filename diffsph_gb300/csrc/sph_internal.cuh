@@ -79,6 +79,10 @@ cudaError_t cell_sort(const float* xy, int stride, int64_t n, const Grid& g, int
                       int32_t* key, int32_t* perm, int32_t* count, int32_t* fill, int32_t* start,
                       int32_t* scan_tmp, cudaStream_t s);
 
+// The same after the keys were computed and counted by the caller (count[key]++).
+cudaError_t cell_sort_counted(int64_t n, int64_t ncells, const int32_t* key, int32_t* perm, int32_t* count,
+                              int32_t* fill, int32_t* start, int32_t* scan_tmp, cudaStream_t s);
+
 inline size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
 
 // Sequential carve-out of a caller workspace.

@@ -84,17 +84,45 @@ struct RhsOut {
     int32_t* nn;    // [nF][2]: fluid and boundary neighbors (incl. self) per fluid particle
 };
 
+// One independent domain: its scheme constants, its cell grid and the offset of its cells in
+// the global cell table. A single simulation is a table of one; packed batches of domains
+// with different particle counts (and hence different dx, h, dt) share every kernel launch.
+struct Dom {
+    Phys P;
+    Grid g;
+    int32_t cell0;
+    int32_t pad;
+};
+
 __device__ __forceinline__ bool is_boundary(float rho_signed) { return __float_as_int(rho_signed) < 0; }
+
+__device__ __forceinline__ int dom_of(const int32_t* __restrict__ did, int64_t i, int64_t n) {
+    return (did && i < n) ? did[i] : 0;
+}
 
 // ------------------------------------------------------------------------------------
 // upload / download / gather
 // ------------------------------------------------------------------------------------
 __global__ void k_upload(int64_t nF, int64_t nB, const float* __restrict__ xf, const float* __restrict__ uf,
                          const float* __restrict__ rf, const float* __restrict__ xb, const float* __restrict__ nb,
-                         const float* __restrict__ db, const float* __restrict__ rb, Phys P, float2* Xr, float4* X4,
-                         float4* V4, int32_t* uid, float2* bnormal, float* bdist) {
+                         const float* __restrict__ db, const float* __restrict__ rb, const Dom* __restrict__ doms,
+                         const int64_t* __restrict__ dom_off, int nd, float2* Xr, float4* X4, float4* V4,
+                         int32_t* uid, int32_t* did, float2* bnormal, float* bdist) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nF + nB) return;
+    // domain of fluid particle i: dom_off[d] <= i < dom_off[d + 1]; boundaries belong to domain 0
+    int d = 0;
+    if (i < nF) {
+        int lo = 0, hi = nd - 1;
+        while (lo < hi) {
+            int mid = (lo + hi + 1) >> 1;
+            if (dom_off[mid] <= i) lo = mid;
+            else hi = mid - 1;
+        }
+        d = lo;
+    }
+    did[i] = d;
+    const Phys& P = doms[d].P;
     float2 x;
     float2 u = make_float2(0.f, 0.f);
     float rho, rho_s;
@@ -135,8 +163,9 @@ __global__ void k_download(int64_t n, int nF, const int32_t* __restrict__ uid, c
 
 __global__ void k_gather(int64_t n, int nF, const int32_t* __restrict__ perm, const float2* __restrict__ Xr_in,
                          const float4* __restrict__ X4_in, const float4* __restrict__ V4_in,
-                         const int32_t* __restrict__ uid_in, float2* __restrict__ Xr_out, float4* __restrict__ X4_out,
-                         float4* __restrict__ V4_out, int32_t* __restrict__ uid_out, int32_t* __restrict__ bidx,
+                         const int32_t* __restrict__ uid_in, const int32_t* __restrict__ did_in,
+                         float2* __restrict__ Xr_out, float4* __restrict__ X4_out, float4* __restrict__ V4_out,
+                         int32_t* __restrict__ uid_out, int32_t* __restrict__ did_out, int32_t* __restrict__ bidx,
                          uint32_t* __restrict__ words) {
     int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= n) return;
@@ -144,6 +173,7 @@ __global__ void k_gather(int64_t n, int nF, const int32_t* __restrict__ perm, co
     Xr_out[s] = Xr_in[o];
     X4_out[s] = X4_in[o];
     V4_out[s] = V4_in[o];
+    did_out[s] = did_in[o];
     int u = uid_in[o];
     uid_out[s] = u;
     if (u >= nF) bidx[atomicAdd(&words[2], 1u)] = (int32_t)s;
@@ -324,11 +354,16 @@ __global__ void k_mdbc(int nB, const int32_t* __restrict__ bidx, const int32_t* 
 //                                                 (densityDiffusion.py:7-46, deltaPlus.py:256-262)
 // The uniform mass m is factored out of the sums.
 // ------------------------------------------------------------------------------------
-template <bool PER, typename LT>
-__device__ __forceinline__ void pass_a_tile(int64_t i, int64_t n, const float4* __restrict__ X4,
-                                            float4* __restrict__ V4, const int32_t* __restrict__ start, const Grid& g,
-                                            const int32_t* __restrict__ uid, const Phys& P, const RhsOut& out,
+template <bool PER, bool BATCH, typename LT>
+__device__ __forceinline__ void pass_a_tile(const Dom& D0, int64_t i, int64_t n, const float4* __restrict__ X4,
+                                            float4* __restrict__ V4, const int32_t* __restrict__ start_all,
+                                            const Dom* __restrict__ doms, const int32_t* __restrict__ did,
+                                            const int32_t* __restrict__ uid, const RhsOut& out,
                                             LT* __restrict__ lst, uint32_t* __restrict__ words) {
+    const Dom& D = BATCH ? doms[dom_of(did, i, n)] : D0;
+    const Phys& P = D.P;
+    const Grid& g = D.g;
+    const int32_t* __restrict__ start = start_all + D.cell0;
     bool inb = i < n;
     float4 xi = inb ? X4[i] : make_float4(0.f, 0.f, -1.f, 0.f);
     bool active = inb && !is_boundary(xi.z);
@@ -384,15 +419,16 @@ __device__ __forceinline__ void pass_a_tile(int64_t i, int64_t n, const float4* 
 // One block handles 32 W consecutive slots: its warps sit in neighboring cells and share
 // most of their stencil data in L1.
 
-template <bool PER, typename LT, int W>
-__global__ void __launch_bounds__(32 * W) k_pass_a(int64_t n, const float4* __restrict__ X4,
-                                                         float4* __restrict__ V4, const int32_t* __restrict__ start,
-                                                         Grid g, const int32_t* __restrict__ uid, Phys P, RhsOut out,
-                                                         uint32_t* __restrict__ words) {
+template <bool PER, bool BATCH, typename LT, int W>
+__global__ void __launch_bounds__(32 * W) k_pass_a(const Dom D0, int64_t n, const float4* __restrict__ X4,
+                                                   float4* __restrict__ V4, const int32_t* __restrict__ start,
+                                                   const Dom* __restrict__ doms, const int32_t* __restrict__ did,
+                                                   const int32_t* __restrict__ uid, RhsOut out,
+                                                   uint32_t* __restrict__ words) {
     extern __shared__ __align__(16) unsigned char s_dyn[];
     LT* lst = reinterpret_cast<LT*>(s_dyn) + (threadIdx.x >> 5) * (kCap * 32);
-    pass_a_tile<PER, LT>((int64_t)blockIdx.x * (32 * W) + threadIdx.x, n, X4, V4, start, g, uid, P, out,
-                             lst, words);
+    pass_a_tile<PER, BATCH, LT>(D0, (int64_t)blockIdx.x * (32 * W) + threadIdx.x, n, X4, V4, start, doms, did, uid, out, lst,
+                         words);
 }
 
 // ------------------------------------------------------------------------------------
@@ -406,14 +442,20 @@ __global__ void __launch_bounds__(32 * W) k_pass_a(int64_t n, const float4* __re
 // MODE 0: write the rates (original order); 1: half step (integration.py:23-32);
 // MODE 2: final symplectic Euler update (integration.py:381-392, 439-513).
 // ------------------------------------------------------------------------------------
-template <bool PER, int MODE, typename LT>
-__device__ __forceinline__ void pass_b_tile(int64_t i, int64_t n, const float4* __restrict__ X4,
-                                            const float4* __restrict__ V4, const int32_t* __restrict__ start,
-                                            const Grid& g, const int32_t* __restrict__ uid, const Phys& P,
-                                            const RhsOut& out, float2* __restrict__ Xr,
-                                            const float4* __restrict__ X4n, const float4* __restrict__ V4n,
-                                            float4* __restrict__ X4o, float4* __restrict__ V4o,
-                                            uint32_t* __restrict__ words, LT* __restrict__ lst) {
+template <bool PER, bool BATCH, int MODE, typename LT>
+__device__ __forceinline__ void pass_b_tile(const Dom& D0, int64_t i, int64_t n, const float4* __restrict__ X4,
+                                            const float4* __restrict__ V4, const int32_t* __restrict__ start_all,
+                                            const Dom* __restrict__ doms, const int32_t* __restrict__ did,
+                                            const int32_t* __restrict__ uid, const RhsOut& out,
+                                            float2* __restrict__ Xr, const float4* __restrict__ X4n,
+                                            const float4* __restrict__ V4n, float4* __restrict__ X4o,
+                                            float4* __restrict__ V4o, uint32_t* __restrict__ words,
+                                            uint32_t* __restrict__ maxv, LT* __restrict__ lst) {
+    const int dom = BATCH ? dom_of(did, i, n) : 0;
+    const Dom& D = BATCH ? doms[dom] : D0;
+    const Phys& P = D.P;
+    const Grid& g = D.g;
+    const int32_t* __restrict__ start = start_all + D.cell0;
     bool inb = i < n;
     float4 xi = inb ? X4[i] : make_float4(0.f, 0.f, -1.f, 0.f);
     float4 vi = inb ? V4[i] : make_float4(0.f, 0.f, 0.f, 0.f);
@@ -506,7 +548,7 @@ __device__ __forceinline__ void pass_b_tile(int64_t i, int64_t n, const float4* 
         X4o[i] = make_float4(w.x, w.y, rnew, eos_p(rnew, P.eos));
         V4o[i] = make_float4(u0, u1, 0.f, 0.f);
         float sp = __fsqrt_rn(__fmaf_rn(u1, u1, __fmul_rn(u0, u0)));
-        atomicMax(&words[1], __float_as_uint(sp));
+        atomicMax(&maxv[dom], __float_as_uint(sp));
         if (!isfinite(u0) || !isfinite(u1) || !isfinite(rnew) || !isfinite(xp.x) || !isfinite(xp.y))
             atomicOr(&words[0], SPH_FLAG_NONFINITE);
         // the cells of this step's sort must still cover h + the displacement at the shift pass
@@ -516,32 +558,39 @@ __device__ __forceinline__ void pass_b_tile(int64_t i, int64_t n, const float4* 
     }
 }
 
-template <bool PER, int MODE, typename LT, int W>
-__global__ void __launch_bounds__(32 * W) k_pass_b(int64_t n, const float4* __restrict__ X4,
-                                                         const float4* __restrict__ V4,
-                                                         const int32_t* __restrict__ start, Grid g,
-                                                         const int32_t* __restrict__ uid, Phys P, RhsOut out,
-                                                         float2* __restrict__ Xr, const float4* __restrict__ X4n,
-                                                         const float4* __restrict__ V4n, float4* __restrict__ X4o,
-                                                         float4* __restrict__ V4o, uint32_t* __restrict__ words) {
+template <bool PER, bool BATCH, int MODE, typename LT, int W>
+__global__ void __launch_bounds__(32 * W) k_pass_b(const Dom D0, int64_t n, const float4* __restrict__ X4,
+                                                   const float4* __restrict__ V4, const int32_t* __restrict__ start,
+                                                   const Dom* __restrict__ doms, const int32_t* __restrict__ did,
+                                                   const int32_t* __restrict__ uid, RhsOut out,
+                                                   float2* __restrict__ Xr, const float4* __restrict__ X4n,
+                                                   const float4* __restrict__ V4n, float4* __restrict__ X4o,
+                                                   float4* __restrict__ V4o, uint32_t* __restrict__ words,
+                                                   uint32_t* __restrict__ maxv) {
     extern __shared__ __align__(16) unsigned char s_dyn[];
     LT* lst = reinterpret_cast<LT*>(s_dyn) + (threadIdx.x >> 5) * (kCap * 32);
-    pass_b_tile<PER, MODE, LT>((int64_t)blockIdx.x * (32 * W) + threadIdx.x, n, X4, V4, start, g, uid, P, out, Xr, X4n,
-                                   V4n, X4o, V4o, words, lst);
+    pass_b_tile<PER, BATCH, MODE, LT>(D0, (int64_t)blockIdx.x * (32 * W) + threadIdx.x, n, X4, V4, start, doms, did, uid, out,
+                               Xr, X4n, V4n, X4o, V4o, words, maxv, lst);
 }
 
 // ------------------------------------------------------------------------------------
 // delta+ shifting (shifting.py:119-147, applied as in solveShifting :990-1005)
 //   dx_i = clamp(-CFL Ma (2h/kappa)^2 sum (1 + R (W/W0)^n) m_j/(rho_i+rho_j) gradW, +-thr dx)
 // ------------------------------------------------------------------------------------
-template <bool PER, typename LT>
-__device__ __forceinline__ void shift_tile(int64_t i, int64_t n, const float4* __restrict__ X4,
-                                           const float4* __restrict__ V4, const int32_t* __restrict__ start,
-                                           const Grid& g, const Phys& P, float2* __restrict__ Xr,
-                                           float4* __restrict__ X4o, float4* __restrict__ V4o,
-                                           uint32_t* __restrict__ words, int enabled,
+template <bool PER, bool BATCH, typename LT>
+__device__ __forceinline__ void shift_tile(const Dom& D0, int64_t i, int64_t n, const float4* __restrict__ X4,
+                                           const float4* __restrict__ V4, const int32_t* __restrict__ start_all,
+                                           const Dom* __restrict__ doms, const int32_t* __restrict__ did,
+                                           float2* __restrict__ Xr, float4* __restrict__ X4o,
+                                           float4* __restrict__ V4o, uint32_t* __restrict__ words,
+                                           const uint32_t* __restrict__ maxv, int enabled,
                                            const int32_t* __restrict__ uid, float* __restrict__ dx_out,
                                            LT* __restrict__ lst) {
+    const int dom = BATCH ? dom_of(did, i, n) : 0;
+    const Dom& D = BATCH ? doms[dom] : D0;
+    const Phys& P = D.P;
+    const Grid& g = D.g;
+    const int32_t* __restrict__ start = start_all + D.cell0;
     bool inb = i < n;
     float4 xi = inb ? X4[i] : make_float4(0.f, 0.f, -1.f, 0.f);
     bool active = inb && !is_boundary(xi.z) && enabled;
@@ -573,7 +622,7 @@ __device__ __forceinline__ void shift_tile(int64_t i, int64_t n, const float4* _
         }
         return;
     }
-    float Ma = P.compute_mach ? __uint_as_float(words[1]) * P.inv_cs : 0.1f;
+    float Ma = P.compute_mach ? __uint_as_float(maxv[dom]) * P.inv_cs : 0.1f;
     float sc = P.sh_scale * Ma * P.m;
     // update = clamp(-(sc * s)); x_new = x - update; the reference then adds (x_new - x) to x
     float up0 = fminf(fmaxf(-(sc * s0), -P.sh_thr), P.sh_thr);
@@ -592,30 +641,42 @@ __device__ __forceinline__ void shift_tile(int64_t i, int64_t n, const float4* _
     }
 }
 
-template <bool PER, typename LT, int W>
-__global__ void __launch_bounds__(32 * W) k_shift(int64_t n, const float4* __restrict__ X4,
-                                                        const float4* __restrict__ V4,
-                                                        const int32_t* __restrict__ start, Grid g, Phys P,
-                                                        float2* __restrict__ Xr, float4* __restrict__ X4o,
-                                                        float4* __restrict__ V4o, uint32_t* __restrict__ words,
-                                                        int enabled, const int32_t* __restrict__ uid,
-                                                        float* __restrict__ dx_out) {
+template <bool PER, bool BATCH, typename LT, int W>
+__global__ void __launch_bounds__(32 * W) k_shift(const Dom D0, int64_t n, const float4* __restrict__ X4,
+                                                  const float4* __restrict__ V4, const int32_t* __restrict__ start,
+                                                  const Dom* __restrict__ doms, const int32_t* __restrict__ did,
+                                                  float2* __restrict__ Xr, float4* __restrict__ X4o,
+                                                  float4* __restrict__ V4o, uint32_t* __restrict__ words,
+                                                  const uint32_t* __restrict__ maxv, int enabled,
+                                                  const int32_t* __restrict__ uid, float* __restrict__ dx_out) {
     extern __shared__ __align__(16) unsigned char s_dyn[];
     LT* lst = reinterpret_cast<LT*>(s_dyn) + (threadIdx.x >> 5) * (kCap * 32);
-    shift_tile<PER, LT>((int64_t)blockIdx.x * (32 * W) + threadIdx.x, n, X4, V4, start, g, P, Xr, X4o, V4o, words, enabled,
-                            uid, dx_out, lst);
+    shift_tile<PER, BATCH, LT>(D0, (int64_t)blockIdx.x * (32 * W) + threadIdx.x, n, X4, V4, start, doms, did, Xr, X4o, V4o, words,
+                        maxv, enabled, uid, dx_out, lst);
 }
 
 // max |u| over all particles (the Mach number of shifting.py:139-142)
-__global__ void k_maxvel(int64_t n, const float4* __restrict__ V4, uint32_t* __restrict__ words) {
+__global__ void k_maxvel(int64_t n, const float4* __restrict__ V4, const int32_t* __restrict__ did,
+                         uint32_t* __restrict__ maxv) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    float sp = 0.f;
-    if (i < n) {
-        float4 v = V4[i];
-        sp = __fsqrt_rn(__fmaf_rn(v.y, v.y, __fmul_rn(v.x, v.x)));
-    }
-    for (int o = 16; o > 0; o >>= 1) sp = fmaxf(sp, __shfl_xor_sync(kFull, sp, o));
-    if ((threadIdx.x & 31) == 0) atomicMax(&words[1], __float_as_uint(sp));
+    if (i >= n) return;
+    float4 v = V4[i];
+    float sp = __fsqrt_rn(__fmaf_rn(v.y, v.y, __fmul_rn(v.x, v.x)));
+    atomicMax(&maxv[dom_of(did, i, n)], __float_as_uint(sp));
+}
+
+// global cell key = first cell of the particle's domain + its cell in the domain grid
+__global__ void k_dom_keys(int64_t n, const float4* __restrict__ X4, const int32_t* __restrict__ did,
+                           const Dom* __restrict__ doms, int32_t* __restrict__ key, int32_t* __restrict__ count) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const Dom& D = doms[dom_of(did, i, n)];
+    float4 x = X4[i];
+    int cx = cell_coord(x.x, D.g.mn[0], D.g.inv_cell[0], D.g.nc[0]);
+    int cy = cell_coord(x.y, D.g.mn[1], D.g.inv_cell[1], D.g.nc[1]);
+    int k = D.cell0 + cy * D.g.nc[0] + cx;
+    key[i] = k;
+    atomicAdd(&count[k], 1);
 }
 
 }  // namespace sph
@@ -623,28 +684,35 @@ __global__ void k_maxvel(int64_t n, const float4* __restrict__ V4, uint32_t* __r
 using namespace sph;
 
 // ------------------------------------------------------------------------------------
-// Solver handle
+// Solver handle (one domain, or a packed batch of independent fluid domains)
 // ------------------------------------------------------------------------------------
 struct sph_solver {
-    sph_params_t prm;
-    Phys P;
+    sph_params_t prm;            // parameters of domain 0 (mDBC, shifting switch)
+    int nd = 1;
+    std::vector<Dom> doms_host;
+    std::vector<int64_t> off_host;  // fluid particle offsets of the domains [nd + 1]
     int64_t nF, nB, n;
-    Grid grid;
     int64_t ncells;
     bool periodic;
     float2 *Xr, *Xr_t;
     float4 *Xc, *Xh, *Xf, *Xt;
     float4 *Vc, *Vh, *Vf, *Vt;
-    int32_t *uid, *uid_t;
+    int32_t *uid, *uid_t, *did, *did_t;
     int32_t *key, *perm, *count, *fill, *start, *scan32;
     int32_t* bidx;
-    uint32_t* words;  // [0] flags, [1] max |u| bits, [2] boundary count
-    unsigned long long* counters;  // tile counters of the passes (zeroed before each launch)
+    uint32_t* words;  // [0] flags, [2] boundary count
+    uint32_t* maxv;   // per-domain max |u| (float bits)
+    Dom* doms;
+    int64_t* dom_off;
     float2* bnormal;
     float* bdist;
-    bool list16;          // relative int16 list entries fit every stencil of the grid
-    int shape = 0;        // index into kShapes
+    bool list16 = false;
+    int shape = 0;
     bool attrs_set = false;
+    bool tables_uploaded = false;
+    // captured step graph
+    cudaGraphExec_t graph = nullptr;
+    int graph_steps = 0;
     // timing
     uint32_t timing_mask = 0;
     struct Ev {
@@ -660,11 +728,21 @@ struct sph_solver {
 constexpr int kSolverRad = 2;
 static double cell_size(const sph_params_t* p) { return p->support * p->skin * (1.0 + 1e-4) / kSolverRad; }
 
-static size_t solver_layout(const sph_params_t* p, int64_t nF, int64_t nB, void* ws, sph_solver* S) {
-    int64_t n = nF + nB;
+static Grid dom_grid(const sph_params_t* p, int64_t* ncells) {
     int per[2] = {p->domain.periodic[0], p->domain.periodic[1]};
-    int64_t ncells = 0;
-    Grid g = make_grid(p->domain.min, p->domain.max, per, cell_size(p), &ncells, kSolverRad);
+    return make_grid(p->domain.min, p->domain.max, per, cell_size(p), ncells, kSolverRad);
+}
+
+static size_t solver_layout(const sph_params_t* p, const int64_t* nF_d, int nd, int64_t nB, void* ws,
+                            sph_solver* S) {
+    int64_t nF = 0, ncells = 0;
+    for (int d = 0; d < nd; ++d) {
+        nF += nF_d[d];
+        int64_t nc = 0;
+        dom_grid(&p[d], &nc);
+        ncells += nc;
+    }
+    int64_t n = nF + nB;
     Carver c{(char*)ws};
     float2* Xr = c.take<float2>(n);
     float2* Xr_t = c.take<float2>(n);
@@ -674,6 +752,8 @@ static size_t solver_layout(const sph_params_t* p, int64_t nF, int64_t nB, void*
     for (int k = 0; k < 4; ++k) V[k] = c.take<float4>(n);
     int32_t* uid = c.take<int32_t>(n);
     int32_t* uid_t = c.take<int32_t>(n);
+    int32_t* did = c.take<int32_t>(n);
+    int32_t* did_t = c.take<int32_t>(n);
     int32_t* key = c.take<int32_t>(n);
     int32_t* perm = c.take<int32_t>(n);
     int32_t* count = c.take<int32_t>(ncells);
@@ -682,19 +762,22 @@ static size_t solver_layout(const sph_params_t* p, int64_t nF, int64_t nB, void*
     int32_t* scan32 = c.take<int32_t>(scan_tmp_elems(ncells));
     int32_t* bidx = c.take<int32_t>(nB);
     uint32_t* words = c.take<uint32_t>(8);
-    unsigned long long* counters = c.take<unsigned long long>(8);
+    uint32_t* maxv = c.take<uint32_t>(nd);
+    Dom* doms = c.take<Dom>(nd);
+    int64_t* dom_off = c.take<int64_t>(nd + 1);
     float2* bnormal = c.take<float2>(nB);
     float* bdist = c.take<float>(nB);
     if (S) {
         S->n = n;
-        S->grid = g;
+        S->nF = nF;
+        S->nB = nB;
         S->ncells = ncells;
         S->Xr = Xr; S->Xr_t = Xr_t;
         S->Xc = X[0]; S->Xh = X[1]; S->Xf = X[2]; S->Xt = X[3];
         S->Vc = V[0]; S->Vh = V[1]; S->Vf = V[2]; S->Vt = V[3];
-        S->uid = uid; S->uid_t = uid_t;
+        S->uid = uid; S->uid_t = uid_t; S->did = did; S->did_t = did_t;
         S->key = key; S->perm = perm; S->count = count; S->fill = fill; S->start = start; S->scan32 = scan32;
-        S->bidx = bidx; S->words = words; S->counters = counters;
+        S->bidx = bidx; S->words = words; S->maxv = maxv; S->doms = doms; S->dom_off = dom_off;
         S->bnormal = bnormal; S->bdist = bdist;
     }
     return c.off;
@@ -706,9 +789,8 @@ static int check_params(const sph_params_t* p, int64_t nF, int64_t nB) {
     if (!(p->skin >= 1.0) || !(p->kernel_scale > 0)) return SPH_ERR_ARGUMENT;
     for (int a = 0; a < 2; ++a)
         if (!(p->domain.max[a] > p->domain.min[a])) return SPH_ERR_ARGUMENT;
-    int per[2] = {p->domain.periodic[0], p->domain.periodic[1]};
     int64_t ncells = 0;
-    make_grid(p->domain.min, p->domain.max, per, cell_size(p), &ncells, kSolverRad);
+    dom_grid(p, &ncells);
     if (ncells > ((int64_t)1 << 28)) return SPH_ERR_ARGUMENT;
     return SPH_OK;
 }
@@ -781,43 +863,95 @@ static Phys make_phys(const sph_params_t* p, int64_t nF) {
     return P;
 }
 
+static int check_batch(const sph_params_t* params, const int64_t* n_fluid, int nd, int64_t nB) {
+    if (!params || !n_fluid || nd < 1) return SPH_ERR_ARGUMENT;
+    if (nd > 1 && nB != 0) return SPH_ERR_ARGUMENT;  // packed batches are fluid-only
+    int64_t tot = 0, cells = 0;
+    for (int d = 0; d < nd; ++d) {
+        int st = check_params(&params[d], n_fluid[d], d == 0 ? nB : 0);
+        if (st) return st;
+        tot += n_fluid[d];
+        int64_t nc = 0;
+        dom_grid(&params[d], &nc);
+        cells += nc;
+    }
+    if (tot + nB >= ((int64_t)1 << 31) - 1 || cells >= ((int64_t)1 << 30)) return SPH_ERR_ARGUMENT;
+    return SPH_OK;
+}
+
+static int create_impl(const sph_params_t* params, const int64_t* n_fluid, int nd, int64_t n_boundary,
+                       void* workspace, size_t workspace_bytes, sph_solver_t** out) {
+    int st = check_batch(params, n_fluid, nd, n_boundary);
+    if (st) return st;
+    if (!out) return SPH_ERR_ARGUMENT;
+    size_t need = solver_layout(params, n_fluid, nd, n_boundary, nullptr, nullptr);
+    if (!workspace || workspace_bytes < need) return SPH_ERR_WORKSPACE;
+    if (((uintptr_t)workspace & 255) != 0) return SPH_ERR_ARGUMENT;
+    sph_solver* S = new sph_solver();
+    S->prm = params[0];
+    S->nd = nd;
+    solver_layout(params, n_fluid, nd, n_boundary, workspace, S);
+    S->periodic = false;
+    S->doms_host.resize(nd);
+    S->off_host.resize(nd + 1);
+    int64_t off = 0, cell0 = 0;
+    double span_max = 0.0;
+    for (int d = 0; d < nd; ++d) {
+        Dom& D = S->doms_host[d];
+        memset(&D, 0, sizeof(Dom));
+        D.P = make_phys(&params[d], S->nF);
+        int64_t nc = 0;
+        D.g = dom_grid(&params[d], &nc);
+        D.cell0 = (int32_t)cell0;
+        cell0 += nc;
+        S->off_host[d] = off;
+        off += n_fluid[d];
+        S->periodic = S->periodic || params[d].domain.periodic[0] || params[d].domain.periodic[1];
+        // one-sided slot span of a stencil: rad rows of cells plus rad + 1 cells, at the rest
+        // density (cell/dx)^2 per cell with a 1.5x compression margin
+        double ppc = (cell_size(&params[d]) / params[d].dx) * (cell_size(&params[d]) / params[d].dx);
+        double span = ((double)kSolverRad * D.g.nc[0] + kSolverRad + 1) * ppc * 1.5;
+        // a periodic stencil wraps to the far end of the domain's slots
+        if (params[d].domain.periodic[0] || params[d].domain.periodic[1]) span = (double)n_fluid[d] + (d == 0 ? n_boundary : 0);
+        span_max = span > span_max ? span : span_max;
+    }
+    S->off_host[nd] = off;
+    S->list16 = span_max < 32767.0;
+    *out = S;
+    return SPH_OK;
+}
+
 extern "C" int sph_solver_workspace_bytes(const sph_params_t* params, int64_t n_fluid, int64_t n_boundary,
                                           size_t* bytes) {
-    int st = check_params(params, n_fluid, n_boundary);
+    int st = check_batch(params, &n_fluid, 1, n_boundary);
     if (st) return st;
     if (!bytes) return SPH_ERR_ARGUMENT;
-    *bytes = solver_layout(params, n_fluid, n_boundary, nullptr, nullptr);
+    *bytes = solver_layout(params, &n_fluid, 1, n_boundary, nullptr, nullptr);
     return SPH_OK;
 }
 
 extern "C" int sph_solver_create(const sph_params_t* params, int64_t n_fluid, int64_t n_boundary, void* workspace,
                                  size_t workspace_bytes, sph_solver_t** out) {
-    int st = check_params(params, n_fluid, n_boundary);
+    return create_impl(params, &n_fluid, 1, n_boundary, workspace, workspace_bytes, out);
+}
+
+extern "C" int sph_batch_workspace_bytes(const sph_params_t* params, const int64_t* n_fluid, int32_t n_domains,
+                                         size_t* bytes) {
+    int st = check_batch(params, n_fluid, n_domains, 0);
     if (st) return st;
-    if (!out) return SPH_ERR_ARGUMENT;
-    size_t need = solver_layout(params, n_fluid, n_boundary, nullptr, nullptr);
-    if (!workspace || workspace_bytes < need) return SPH_ERR_WORKSPACE;
-    if (((uintptr_t)workspace & 255) != 0) return SPH_ERR_ARGUMENT;
-    sph_solver* S = new sph_solver();
-    S->prm = *params;
-    S->nF = n_fluid;
-    S->nB = n_boundary;
-    solver_layout(params, n_fluid, n_boundary, workspace, S);
-    S->P = make_phys(params, n_fluid);
-    S->periodic = params->domain.periodic[0] || params->domain.periodic[1];
-    {
-        // one-sided slot span of a stencil: rad rows of cells plus rad + 1 cells, at the rest
-        // density (cell/dx)^2 per cell with a 1.5x compression margin
-        double ppc = (cell_size(params) / params->dx) * (cell_size(params) / params->dx);
-        double span = ((double)kSolverRad * S->grid.nc[0] + kSolverRad + 1) * ppc * 1.5;
-        S->list16 = span < 32767.0;
-    }
-    *out = S;
+    if (!bytes) return SPH_ERR_ARGUMENT;
+    *bytes = solver_layout(params, n_fluid, n_domains, 0, nullptr, nullptr);
     return SPH_OK;
+}
+
+extern "C" int sph_batch_create(const sph_params_t* params, const int64_t* n_fluid, int32_t n_domains,
+                                void* workspace, size_t workspace_bytes, sph_solver_t** out) {
+    return create_impl(params, n_fluid, n_domains, 0, workspace, workspace_bytes, out);
 }
 
 extern "C" void sph_solver_destroy(sph_solver_t* s) {
     if (!s) return;
+    if (s->graph) cudaGraphExecDestroy(s->graph);
     for (auto& e : s->pool) {
         cudaEventDestroy(e.a);
         cudaEventDestroy(e.b);
@@ -851,9 +985,18 @@ extern "C" int sph_solver_upload(sph_solver_t* S, const float* x_fluid, const fl
     if (!S || !x_fluid || !u_fluid || !rho_fluid) return SPH_ERR_ARGUMENT;
     if (S->nB > 0 && (!x_boundary || !normal_boundary || !dist_boundary)) return SPH_ERR_ARGUMENT;
     cudaStream_t st = (cudaStream_t)stream;
+    if (!S->tables_uploaded) {
+        if (cudaMemcpyAsync(S->doms, S->doms_host.data(), sizeof(Dom) * S->nd, cudaMemcpyHostToDevice, st) != cudaSuccess)
+            return SPH_ERR_CUDA;
+        if (cudaMemcpyAsync(S->dom_off, S->off_host.data(), sizeof(int64_t) * (S->nd + 1), cudaMemcpyHostToDevice,
+                            st) != cudaSuccess)
+            return SPH_ERR_CUDA;
+        if (cudaStreamSynchronize(st) != cudaSuccess) return SPH_ERR_CUDA;
+        S->tables_uploaded = true;
+    }
     k_upload<<<blocks_for(S->n), kBlock, 0, st>>>(S->nF, S->nB, x_fluid, u_fluid, rho_fluid, x_boundary,
-                                                    normal_boundary, dist_boundary, rho_boundary, S->P, S->Xr, S->Xc,
-                                                    S->Vc, S->uid, S->bnormal, S->bdist);
+                                                    normal_boundary, dist_boundary, rho_boundary, S->doms, S->dom_off,
+                                                    S->nd, S->Xr, S->Xc, S->Vc, S->uid, S->did, S->bnormal, S->bdist);
     if (cudaMemsetAsync(S->words, 0, sizeof(uint32_t) * 8, st) != cudaSuccess) return SPH_ERR_CUDA;
     return cudaGetLastError() == cudaSuccess ? SPH_OK : SPH_ERR_CUDA;
 }
@@ -861,50 +1004,60 @@ extern "C" int sph_solver_upload(sph_solver_t* S, const float* x_fluid, const fl
 // sort by cell and gather the state into the new order
 static int rebuild(sph_solver* S, cudaStream_t st) {
     tbeg(S, KC_SORT, st);
-    if (cell_sort((const float*)S->Xc, 4, S->n, S->grid, S->ncells, S->key, S->perm, S->count, S->fill, S->start,
-                  S->scan32, st) != cudaSuccess)
+    if (cudaMemsetAsync(S->count, 0, sizeof(int32_t) * S->ncells, st) != cudaSuccess) return SPH_ERR_CUDA;
+    k_dom_keys<<<blocks_for(S->n), kBlock, 0, st>>>(S->n, S->Xc, S->nd > 1 ? S->did : nullptr, S->doms, S->key,
+                                                      S->count);
+    if (cell_sort_counted(S->n, S->ncells, S->key, S->perm, S->count, S->fill, S->start, S->scan32, st) !=
+        cudaSuccess)
         return SPH_ERR_CUDA;
     tend(S, KC_SORT, st);
     if (cudaMemsetAsync(S->words + 2, 0, sizeof(uint32_t), st) != cudaSuccess) return SPH_ERR_CUDA;
     tbeg(S, KC_GATHER, st);
-    k_gather<<<blocks_for(S->n), kBlock, 0, st>>>(S->n, (int)S->nF, S->perm, S->Xr, S->Xc, S->Vc, S->uid, S->Xr_t,
-                                                    S->Xt, S->Vt, S->uid_t, S->bidx, S->words);
+    k_gather<<<blocks_for(S->n), kBlock, 0, st>>>(S->n, (int)S->nF, S->perm, S->Xr, S->Xc, S->Vc, S->uid, S->did,
+                                                    S->Xr_t, S->Xt, S->Vt, S->uid_t, S->did_t, S->bidx, S->words);
     tend(S, KC_GATHER, st);
     std::swap(S->Xr, S->Xr_t);
     std::swap(S->Xc, S->Xt);
     std::swap(S->Vc, S->Vt);
     std::swap(S->uid, S->uid_t);
+    std::swap(S->did, S->did_t);
     return cudaGetLastError() == cudaSuccess ? SPH_OK : SPH_ERR_CUDA;
 }
+
+static const int32_t* dids(sph_solver* S) { return S->nd > 1 ? S->did : nullptr; }
 
 static void launch_mdbc(sph_solver* S, float4* X4, float* rho_b_out, cudaStream_t st) {
     if (S->nB == 0) return;
     tbeg(S, KC_MDBC, st);
+    const Dom& D = S->doms_host[0];
     if (S->periodic)
         k_mdbc<true><<<blocks_for(S->nB), kBlock, 0, st>>>((int)S->nB, S->bidx, S->uid, S->Xr, X4, S->bnormal,
-                                                           S->bdist, S->start, S->grid, S->P, rho_b_out);
+                                                           S->bdist, S->start, D.g, D.P, rho_b_out);
     else
         k_mdbc<false><<<blocks_for(S->nB), kBlock, 0, st>>>((int)S->nB, S->bidx, S->uid, S->Xr, X4, S->bnormal,
-                                                            S->bdist, S->start, S->grid, S->P, rho_b_out);
+                                                            S->bdist, S->start, D.g, D.P, rho_b_out);
     tend(S, KC_MDBC, st);
 }
 
 template <typename LT, int W>
 static constexpr size_t list_bytes() { return (size_t)W * kCap * 32 * sizeof(LT); }
 
+template <bool PER, bool BATCH, typename LT, int W>
+static void allow_lists_k(int b) {
+    cudaFuncSetAttribute(k_pass_a<PER, BATCH, LT, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+    cudaFuncSetAttribute(k_pass_b<PER, BATCH, 0, LT, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+    cudaFuncSetAttribute(k_pass_b<PER, BATCH, 1, LT, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+    cudaFuncSetAttribute(k_pass_b<PER, BATCH, 2, LT, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+    cudaFuncSetAttribute(k_shift<PER, BATCH, LT, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+}
+
 template <typename LT, int W>
 static void allow_lists_s() {
     const int b = (int)list_bytes<LT, W>();
-    cudaFuncSetAttribute(k_pass_a<true, LT, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
-    cudaFuncSetAttribute(k_pass_a<false, LT, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
-    cudaFuncSetAttribute(k_pass_b<true, 0, LT, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
-    cudaFuncSetAttribute(k_pass_b<false, 0, LT, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
-    cudaFuncSetAttribute(k_pass_b<true, 1, LT, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
-    cudaFuncSetAttribute(k_pass_b<false, 1, LT, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
-    cudaFuncSetAttribute(k_pass_b<true, 2, LT, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
-    cudaFuncSetAttribute(k_pass_b<false, 2, LT, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
-    cudaFuncSetAttribute(k_shift<true, LT, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
-    cudaFuncSetAttribute(k_shift<false, LT, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+    allow_lists_k<true, false, LT, W>(b);
+    allow_lists_k<false, false, LT, W>(b);
+    allow_lists_k<true, true, LT, W>(b);
+    allow_lists_k<false, true, LT, W>(b);
 }
 
 static void set_attrs(sph_solver* S) {
@@ -925,15 +1078,22 @@ static void set_attrs(sph_solver* S) {
         default: CALL(int32_t, 4); break;             \
     }
 
+template <bool PER, bool BATCH, typename LT, int W>
+static void launch_a_k(sph_solver* S, float4* X4, float4* V4, RhsOut o, cudaStream_t st) {
+    unsigned gb = (unsigned)((S->n + 32 * W - 1) / (32 * W));
+    k_pass_a<PER, BATCH, LT, W><<<gb, 32 * W, list_bytes<LT, W>(), st>>>(S->doms_host[0], S->n, X4, V4, S->start,
+                                                                        S->doms, dids(S), S->uid, o, S->words);
+}
+
 template <typename LT, int W>
 static void launch_a_t(sph_solver* S, float4* X4, float4* V4, RhsOut o, cudaStream_t st) {
-    unsigned gb = (unsigned)((S->n + 32 * W - 1) / (32 * W));
-    if (S->periodic)
-        k_pass_a<true, LT, W><<<gb, 32 * W, list_bytes<LT, W>(), st>>>(S->n, X4, V4, S->start, S->grid, S->uid, S->P,
-                                                                      o, S->words);
-    else
-        k_pass_a<false, LT, W><<<gb, 32 * W, list_bytes<LT, W>(), st>>>(S->n, X4, V4, S->start, S->grid, S->uid,
-                                                                       S->P, o, S->words);
+    if (S->nd > 1) {
+        if (S->periodic) launch_a_k<true, true, LT, W>(S, X4, V4, o, st);
+        else launch_a_k<false, true, LT, W>(S, X4, V4, o, st);
+    } else {
+        if (S->periodic) launch_a_k<true, false, LT, W>(S, X4, V4, o, st);
+        else launch_a_k<false, false, LT, W>(S, X4, V4, o, st);
+    }
 }
 
 static void launch_a(sph_solver* S, float4* X4, float4* V4, RhsOut o, cudaStream_t st) {
@@ -945,15 +1105,23 @@ static void launch_a(sph_solver* S, float4* X4, float4* V4, RhsOut o, cudaStream
     tend(S, KC_PASS_A, st);
 }
 
+template <bool PER, bool BATCH, int MODE, typename LT, int W>
+static void launch_b_k(sph_solver* S, float4* X4, float4* V4, RhsOut o, float4* X4o, float4* V4o, cudaStream_t st) {
+    unsigned gb = (unsigned)((S->n + 32 * W - 1) / (32 * W));
+    k_pass_b<PER, BATCH, MODE, LT, W><<<gb, 32 * W, list_bytes<LT, W>(), st>>>(
+        S->doms_host[0], S->n, X4, V4, S->start, S->doms, dids(S), S->uid, o, S->Xr, S->Xc, S->Vc, X4o, V4o,
+        S->words, S->maxv);
+}
+
 template <int MODE, typename LT, int W>
 static void launch_b_t(sph_solver* S, float4* X4, float4* V4, RhsOut o, float4* X4o, float4* V4o, cudaStream_t st) {
-    unsigned gb = (unsigned)((S->n + 32 * W - 1) / (32 * W));
-    if (S->periodic)
-        k_pass_b<true, MODE, LT, W><<<gb, 32 * W, list_bytes<LT, W>(), st>>>(
-            S->n, X4, V4, S->start, S->grid, S->uid, S->P, o, S->Xr, S->Xc, S->Vc, X4o, V4o, S->words);
-    else
-        k_pass_b<false, MODE, LT, W><<<gb, 32 * W, list_bytes<LT, W>(), st>>>(
-            S->n, X4, V4, S->start, S->grid, S->uid, S->P, o, S->Xr, S->Xc, S->Vc, X4o, V4o, S->words);
+    if (S->nd > 1) {
+        if (S->periodic) launch_b_k<true, true, MODE, LT, W>(S, X4, V4, o, X4o, V4o, st);
+        else launch_b_k<false, true, MODE, LT, W>(S, X4, V4, o, X4o, V4o, st);
+    } else {
+        if (S->periodic) launch_b_k<true, false, MODE, LT, W>(S, X4, V4, o, X4o, V4o, st);
+        else launch_b_k<false, false, MODE, LT, W>(S, X4, V4, o, X4o, V4o, st);
+    }
 }
 
 template <int MODE>
@@ -977,23 +1145,30 @@ static int run_stages(sph_solver* S, cudaStream_t st) {
     // stage 2 at the half step; the epilogue also reduces max |u'| for the shifting Mach number
     launch_mdbc(S, S->Xh, nullptr, st);
     launch_a(S, S->Xh, S->Vh, none, st);
-    if (cudaMemsetAsync(S->words + 1, 0, sizeof(uint32_t), st) != cudaSuccess) return SPH_ERR_CUDA;
+    if (cudaMemsetAsync(S->maxv, 0, sizeof(uint32_t) * S->nd, st) != cudaSuccess) return SPH_ERR_CUDA;
     launch_b<2>(S, S->Xh, S->Vh, none, S->Xf, S->Vf, st);
     return cudaGetLastError() == cudaSuccess ? SPH_OK : SPH_ERR_CUDA;
+}
+
+template <bool PER, bool BATCH, typename LT, int W>
+static void launch_shift_k(sph_solver* S, float4* Xin, float4* Vin, float4* Xout, float4* Vout, float* dx_out,
+                           cudaStream_t st) {
+    unsigned gb = (unsigned)((S->n + 32 * W - 1) / (32 * W));
+    k_shift<PER, BATCH, LT, W><<<gb, 32 * W, list_bytes<LT, W>(), st>>>(S->doms_host[0], S->n, Xin, Vin, S->start,
+                                                                       S->doms, dids(S), S->Xr, Xout, Vout, S->words,
+                                                                       S->maxv, S->prm.shift_on, S->uid, dx_out);
 }
 
 template <typename LT, int W>
 static void launch_shift_t(sph_solver* S, float4* Xin, float4* Vin, float4* Xout, float4* Vout, float* dx_out,
                            cudaStream_t st) {
-    unsigned gb = (unsigned)((S->n + 32 * W - 1) / (32 * W));
-    if (S->periodic)
-        k_shift<true, LT, W><<<gb, 32 * W, list_bytes<LT, W>(), st>>>(S->n, Xin, Vin, S->start, S->grid, S->P, S->Xr,
-                                                                     Xout, Vout, S->words, S->prm.shift_on, S->uid,
-                                                                     dx_out);
-    else
-        k_shift<false, LT, W><<<gb, 32 * W, list_bytes<LT, W>(), st>>>(S->n, Xin, Vin, S->start, S->grid, S->P,
-                                                                      S->Xr, Xout, Vout, S->words, S->prm.shift_on,
-                                                                      S->uid, dx_out);
+    if (S->nd > 1) {
+        if (S->periodic) launch_shift_k<true, true, LT, W>(S, Xin, Vin, Xout, Vout, dx_out, st);
+        else launch_shift_k<false, true, LT, W>(S, Xin, Vin, Xout, Vout, dx_out, st);
+    } else {
+        if (S->periodic) launch_shift_k<true, false, LT, W>(S, Xin, Vin, Xout, Vout, dx_out, st);
+        else launch_shift_k<false, false, LT, W>(S, Xin, Vin, Xout, Vout, dx_out, st);
+    }
 }
 
 static void launch_shift(sph_solver* S, float4* Xin, float4* Vin, float4* Xout, float4* Vout, float* dx_out,
@@ -1006,9 +1181,7 @@ static void launch_shift(sph_solver* S, float4* Xin, float4* Vin, float4* Xout, 
     tend(S, KC_SHIFT, st);
 }
 
-extern "C" int sph_solver_step(sph_solver_t* S, int32_t n_steps, sph_stream_t stream) {
-    if (!S || n_steps < 0) return SPH_ERR_ARGUMENT;
-    cudaStream_t st = (cudaStream_t)stream;
+static int step_impl(sph_solver* S, int32_t n_steps, cudaStream_t st) {
     for (int it = 0; it < n_steps; ++it) {
         int rc = run_stages(S, st);
         if (rc) return rc;
@@ -1017,6 +1190,41 @@ extern "C" int sph_solver_step(sph_solver_t* S, int32_t n_steps, sph_stream_t st
         if (cudaGetLastError() != cudaSuccess) return SPH_ERR_CUDA;
     }
     return SPH_OK;
+}
+
+extern "C" int sph_solver_step(sph_solver_t* S, int32_t n_steps, sph_stream_t stream) {
+    if (!S || n_steps < 0) return SPH_ERR_ARGUMENT;
+    return step_impl(S, n_steps, (cudaStream_t)stream);
+}
+
+// The step sequence is static, so a fixed number of steps can be captured once into a CUDA
+// graph and replayed. Every step swaps the sorted/gather buffers, so an even number of steps
+// returns the handle to the buffer assignment it was captured with.
+extern "C" int sph_solver_graph_step(sph_solver_t* S, int32_t n_steps, sph_stream_t stream) {
+    if (!S || n_steps < 2 || (n_steps & 1)) return SPH_ERR_ARGUMENT;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (st == nullptr) return SPH_ERR_ARGUMENT;  // the legacy default stream cannot be captured
+    if (S->graph && S->graph_steps != n_steps) {
+        cudaGraphExecDestroy(S->graph);
+        S->graph = nullptr;
+    }
+    if (!S->graph) {
+        set_attrs(S);
+        uint32_t mask = S->timing_mask;
+        S->timing_mask = 0;
+        cudaGraph_t g = nullptr;
+        if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return SPH_ERR_CUDA;
+        int rc = step_impl(S, n_steps, st);
+        cudaError_t e = cudaStreamEndCapture(st, &g);
+        S->timing_mask = mask;
+        if (rc) return rc;
+        if (e != cudaSuccess || !g) return SPH_ERR_CUDA;
+        e = cudaGraphInstantiate(&S->graph, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) return SPH_ERR_CUDA;
+        S->graph_steps = n_steps;
+    }
+    return cudaGraphLaunch(S->graph, st) == cudaSuccess ? SPH_OK : SPH_ERR_CUDA;
 }
 
 extern "C" int sph_solver_integrate(sph_solver_t* S, sph_stream_t stream) {
@@ -1034,8 +1242,8 @@ extern "C" int sph_solver_shift(sph_solver_t* S, float* dx_out, sph_stream_t str
     cudaStream_t st = (cudaStream_t)stream;
     int rc = rebuild(S, st);
     if (rc) return rc;
-    if (cudaMemsetAsync(S->words + 1, 0, sizeof(uint32_t), st) != cudaSuccess) return SPH_ERR_CUDA;
-    k_maxvel<<<blocks_for(S->n), kBlock, 0, st>>>(S->n, S->Vc, S->words);
+    if (cudaMemsetAsync(S->maxv, 0, sizeof(uint32_t) * S->nd, st) != cudaSuccess) return SPH_ERR_CUDA;
+    k_maxvel<<<blocks_for(S->n), kBlock, 0, st>>>(S->n, S->Vc, dids(S), S->maxv);
     launch_shift(S, S->Xc, S->Vc, S->Xt, S->Vt, dx_out, st);
     std::swap(S->Xc, S->Xt);
     std::swap(S->Vc, S->Vt);
@@ -1076,6 +1284,10 @@ extern "C" int sph_solver_autotune(sph_solver_t* S, int32_t* shape_out, float* m
     cudaEventDestroy(b);
     S->shape = best_shape;
     S->timing_mask = saved_mask;
+    if (S->graph) {  // a captured graph holds the old shape's kernels
+        cudaGraphExecDestroy(S->graph);
+        S->graph = nullptr;
+    }
     if (shape_out) *shape_out = best_shape;
     return cudaGetLastError() == cudaSuccess ? SPH_OK : SPH_ERR_CUDA;
 }
@@ -1125,6 +1337,10 @@ extern "C" int sph_solver_set_shape(sph_solver_t* S, int32_t shape) {
     if (!S || shape < 0 || shape >= kNumShapes) return SPH_ERR_ARGUMENT;
     if (kShapes[shape].list16 && !S->list16) return SPH_ERR_ARGUMENT;
     S->shape = shape;
+    if (S->graph) {
+        cudaGraphExecDestroy(S->graph);
+        S->graph = nullptr;
+    }
     return SPH_OK;
 }
 

@@ -172,3 +172,19 @@ def fourier_periodic(nx: int = 128, seed: int = 0, jitter: float = 0.1, dtype=np
     st["fluid"]["velocities"] = u.astype(dtype)
     st["fluid"]["densities"] = np.full(x.shape[0], cfg["fluid"]["rho0"], dtype)
     return cfg, st
+
+
+def batched_fourier(n_domains: int = 256, seed: int = 0, n_min: int = 1024, n_max: int = 65536,
+                    jitter: float = 0.1, dtype=np.float32):
+    """Independent periodic domains on [-1,1]^2 for the batched solver: per domain the particle
+    count is drawn log-uniformly in [n_min, n_max] and rounded to a square lattice, positions
+    get uniform jitter of 0.1 dx, and the velocity is a random divergence-free Fourier-mode
+    field normalised to max speed 1; other parameters as in the Taylor-Green workload.
+    Returns a list of (config, state)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for d in range(n_domains):
+        n = float(np.exp(rng.uniform(np.log(n_min), np.log(n_max))))
+        nx = max(16, int(round(np.sqrt(n))))
+        out.append(fourier_periodic(nx, seed=int(rng.integers(0, 2**31 - 1)), jitter=jitter, dtype=dtype))
+    return out

@@ -195,6 +195,12 @@ class Solver:
     def step(self, n: int = 1):
         _lib.check("sph_solver_step", self.lib.sph_solver_step(self.handle, int(n), _stream()))
 
+    def graph_step(self, n: int = 2):
+        """n (even) steps replayed from a captured CUDA graph; needs a non-default stream."""
+        if torch.cuda.current_stream().cuda_stream == 0:
+            raise RuntimeError("graph_step needs a non-default CUDA stream (torch.cuda.stream(...))")
+        _lib.check("sph_solver_graph_step", self.lib.sph_solver_graph_step(self.handle, int(n), _stream()))
+
     def integrate(self):
         _lib.check("sph_solver_integrate", self.lib.sph_solver_integrate(self.handle, _stream()))
 
@@ -263,3 +269,47 @@ class Solver:
         _lib.check("sph_solver_kernel_times", self.lib.sph_solver_kernel_times(self.handle, ms, cnt, _stream()))
         names = self.kernel_classes()
         return {names[c]: (float(ms[c]), int(cnt[c])) for c in range(k)}
+
+
+class BatchSolver(Solver):
+    """Many independent periodic fluid domains packed into one set of arrays and stepped by
+    the same kernel launches (one solver handle for the whole batch)."""
+
+    def __init__(self, configs, fluids, skin: float = DEFAULT_SKIN, capacity: int | None = None):
+        if not torch.cuda.is_available():
+            raise RuntimeError("the sph103 solver needs a CUDA device")
+        if len(configs) != len(fluids) or not configs:
+            raise ValueError("one config per domain")
+        self.lib = _lib.load()
+        self.config = configs[0]
+        self.configs = configs
+        nd = len(configs)
+        counts = [int(torch.as_tensor(f["positions"]).shape[0]) for f in fluids]
+        self.counts = counts
+        self.nF = sum(counts)
+        self.nB = 0
+        P = (_lib.Params * nd)()
+        for d, (cfg, fl) in enumerate(zip(configs, fluids)):
+            if cfg.get("boundary", {}).get("active", False):
+                raise ValueError("batched domains are fluid-only")
+            P[d] = params_from_config(cfg, _uniform(fl["masses"], "mass"), skin, capacity)
+        self.params = P
+        n_arr = (ctypes.c_int64 * nd)(*counts)
+        nbytes = ctypes.c_size_t()
+        _lib.check("sph_batch_workspace_bytes", self.lib.sph_batch_workspace_bytes(P, n_arr, nd, ctypes.byref(nbytes)))
+        self.workspace = torch.empty(int(nbytes.value) + 256, dtype=torch.uint8, device="cuda")
+        self._ws_ptr = (self.workspace.data_ptr() + 255) & ~255
+        h = ctypes.c_void_p()
+        _lib.check("sph_batch_create", self.lib.sph_batch_create(
+            P, n_arr, nd, ctypes.c_void_p(self._ws_ptr), nbytes.value, ctypes.byref(h)))
+        self.handle = h
+        self.upload_domains(fluids)
+
+    def upload_domains(self, fluids):
+        cat = {k: torch.cat([torch.as_tensor(f[k]).reshape(torch.as_tensor(f[k]).shape[0], -1).float()
+                             for f in fluids]).squeeze(-1) for k in ("positions", "velocities", "densities")}
+        self.upload(cat, None)
+
+    def split(self, arr):
+        """Split a concatenated per-particle array into the domains."""
+        return list(torch.split(arr, self.counts))

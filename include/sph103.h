@@ -111,6 +111,16 @@ typedef struct sph_solver sph_solver_t;
 int sph_solver_workspace_bytes(const sph_params_t* params, int64_t n_fluid, int64_t n_boundary,
                                size_t* bytes);
 
+/* Packed batch of independent fluid-only domains (no walls): domain d has its own
+ * parameters (params[d]: extent, dx, support, dt, ...) and n_fluid[d] particles; the
+ * state arrays of sph_solver_upload / _download are the domains' arrays concatenated in
+ * domain order. Every kernel launch covers all domains (a per-particle domain id selects
+ * the constants and the cell grid); results equal those of one solver per domain. */
+int sph_batch_workspace_bytes(const sph_params_t* params, const int64_t* n_fluid, int32_t n_domains,
+                              size_t* bytes);
+int sph_batch_create(const sph_params_t* params, const int64_t* n_fluid, int32_t n_domains,
+                     void* workspace, size_t workspace_bytes, sph_solver_t** out);
+
 /* Creates a host-side handle over the caller's workspace (no device allocation). */
 int sph_solver_create(const sph_params_t* params, int64_t n_fluid, int64_t n_boundary,
                       void* workspace, size_t workspace_bytes, sph_solver_t** out);
@@ -124,6 +134,11 @@ int sph_solver_upload(sph_solver_t* s, const float* x_fluid, const float* u_flui
 
 /* Advances n_steps full time steps (integrate + shifting, fused). */
 int sph_solver_step(sph_solver_t* s, int32_t n_steps, sph_stream_t stream);
+
+/* Same as sph_solver_step, replayed from a CUDA graph captured on the first call (and
+ * re-captured when n_steps changes or the launch shape is changed). n_steps must be even
+ * and stream must not be the legacy default stream. */
+int sph_solver_graph_step(sph_solver_t* s, int32_t n_steps, sph_stream_t stream);
 
 /* The two halves of a step as the reference runner calls them: integrate (both
  * right-hand sides and the symplectic Euler update; integration.py:92-513) ... */
