@@ -15,6 +15,7 @@ STATUS = {
     0: "ok", 1: "invalid argument", 2: "workspace too small", 3: "neighbor list capacity exceeded",
     4: "CUDA launch or copy failed", 5: "particles moved farther than the neighbor-list skin allows",
     6: "non-finite value in the state",
+    7: "problem exceeds the fixed static scratch of sph_neighbor_count_static",
 }
 FLAG_CAPACITY, FLAG_VERLET, FLAG_NONFINITE = 1, 2, 4
 
@@ -54,6 +55,7 @@ EXPORTS = [
     "sph_solver_launches_per_step", "sph_solver_kernel_classes", "sph_solver_kernel_name",
     "sph_solver_set_timing", "sph_solver_kernel_times", "sph_solver_autotune", "sph_solver_shapes",
     "sph_solver_set_shape", "sph_batch_workspace_bytes", "sph_batch_create", "sph_solver_graph_step",
+    "sph_neighbor_count_static",
 ]
 
 _lib = None
@@ -79,6 +81,7 @@ def load(build_if_missing: bool = False):
         "sph_neighbor_count": ([P, I64, P, P, I64, DP, ctypes.c_double, P, SZ, P, P, P], ctypes.c_int),
         "sph_neighbor_fill": ([P, I64, P, P, I64, DP, ctypes.c_double, P, SZ, P, I64, P, P, P, P, P, P, P, P],
                               ctypes.c_int),
+        "sph_neighbor_count_static": ([P, I64, P, P, I64, DP, ctypes.c_double, P, P, P], ctypes.c_int),
         "sph_solver_workspace_bytes": ([PP, I64, I64, ctypes.POINTER(SZ)], ctypes.c_int),
         "sph_solver_create": ([PP, I64, I64, P, SZ, ctypes.POINTER(P)], ctypes.c_int),
         "sph_solver_destroy": ([P], None),

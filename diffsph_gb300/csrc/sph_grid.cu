@@ -2,6 +2,8 @@
 // exported for the neighborSearch drop-in (src/diffSPH/v2/modules/neighborhood.py:491-593).
 #include <math.h>
 
+#include <mutex>
+
 #include "../../include/sph103.h"
 #include "sph_internal.cuh"
 
@@ -410,4 +412,48 @@ extern "C" int sph_neighbor_fill(const float* x_query, int64_t n_query, const fl
         k_pair_kernels<<<(unsigned)((n_pairs + kBlock - 1) / kBlock), kBlock, 0, s>>>(n_pairs, q, xhat, h_pair,
                                                                                        kernels, gradients);
     return cudaGetLastError() == cudaSuccess ? SPH_OK : SPH_ERR_CUDA;
+}
+
+// ------------------------------------------------------------------------------------
+// Neighbor count without caller workspace. The scratch is one file-scope device array per
+// device (the module's global, created with the module); its device address is looked up
+// once per device and cached. Nothing here allocates. Of the scratch, only the per-cell
+// counters must start at zero, and cell_sort clears them (cudaMemsetAsync) on every call;
+// every other region is written before it is read.
+// ------------------------------------------------------------------------------------
+static __device__ __align__(256) unsigned char g_nb_static_scratch[SPH_NEIGHBOR_STATIC_SCRATCH_BYTES];
+
+namespace {
+constexpr int kStaticMaxDevices = 64;
+std::mutex g_static_mu;
+void* g_static_ptr[kStaticMaxDevices];  // device address of g_nb_static_scratch, per device
+
+int static_scratch(void** out) {
+    int dev = -1;
+    if (cudaGetDevice(&dev) != cudaSuccess) return SPH_ERR_CUDA;
+    if (dev < 0 || dev >= kStaticMaxDevices) return SPH_ERR_ARGUMENT;
+    std::lock_guard<std::mutex> lock(g_static_mu);
+    if (!g_static_ptr[dev]) {
+        void* p = nullptr;
+        if (cudaGetSymbolAddress(&p, g_nb_static_scratch) != cudaSuccess || !p) return SPH_ERR_CUDA;
+        g_static_ptr[dev] = p;
+    }
+    *out = g_static_ptr[dev];
+    return SPH_OK;
+}
+}  // namespace
+
+extern "C" int sph_neighbor_count_static(const float* x_query, int64_t n_query, const float* x_ref,
+                                         const float* h_ref, int64_t n_ref, const sph_domain_t* domain,
+                                         double max_support, int32_t* counts, int64_t* offsets,
+                                         sph_stream_t stream) {
+    NbWork w;
+    size_t need = 0;
+    int st = nb_layout(n_query, n_ref, domain, max_support, nullptr, &w, &need);
+    if (st) return st;
+    if (need > SPH_NEIGHBOR_STATIC_SCRATCH_BYTES) return SPH_ERR_STATIC_LIMIT;
+    void* scratch = nullptr;
+    if ((st = static_scratch(&scratch))) return st;
+    return sph_neighbor_count(x_query, n_query, x_ref, h_ref, n_ref, domain, max_support, scratch,
+                              SPH_NEIGHBOR_STATIC_SCRATCH_BYTES, counts, offsets, stream);
 }

@@ -29,7 +29,9 @@ enum sph_status {
     SPH_ERR_CAPACITY = 3,       /* a neighbor row exceeded the list capacity */
     SPH_ERR_CUDA = 4,           /* a CUDA launch or copy failed */
     SPH_ERR_VERLET = 5,         /* particles moved farther than the list skin allows */
-    SPH_ERR_NONFINITE = 6       /* a NaN / Inf appeared in the state */
+    SPH_ERR_NONFINITE = 6,      /* a NaN / Inf appeared in the state */
+    SPH_ERR_STATIC_LIMIT = 7    /* the problem needs more scratch than the fixed static
+                                   array of sph_neighbor_count_static holds */
 };
 
 /* Error flag bits accumulated on the device (sph_solver_flags). */
@@ -98,6 +100,23 @@ int sph_neighbor_fill(const float* x_query, int64_t n_query, const float* x_ref,
                       const int64_t* offsets, int64_t n_pairs, int64_t* pair_i, int64_t* pair_j,
                       float* q, float* xhat, float* h_pair, float* kernels, float* gradients,
                       sph_stream_t stream);
+
+/* Pass 1 without caller workspace; no counterpart in the reference (its neighborSearch
+ * allocates through torch). Same inputs, outputs and results as sph_neighbor_count, but the
+ * scratch is a file-scope device array of SPH_NEIGHBOR_STATIC_SCRATCH_BYTES per device, so
+ * the call allocates nothing. Returns SPH_ERR_STATIC_LIMIT, before any device work, when
+ * sph_neighbor_workspace_bytes for the same sizes exceeds that limit (about 400k particles
+ * in a square domain). The first call on a device, with that device current, looks up the
+ * array's device address (cudaGetSymbolAddress); make that first call before any stream
+ * capture. The per-cell counters that must start at zero are cleared on every call. All
+ * calls on one device share the one array: calls that overlap on the GPU (other streams, or
+ * another thread before the previous call's work has finished) race on it. Pass 2
+ * (sph_neighbor_fill) needs the caller workspace of sph_neighbor_count, not this call. */
+#define SPH_NEIGHBOR_STATIC_SCRATCH_BYTES ((size_t)16 << 20)
+int sph_neighbor_count_static(const float* x_query, int64_t n_query, const float* x_ref,
+                              const float* h_ref, int64_t n_ref, const sph_domain_t* domain,
+                              double max_support, int32_t* counts, int64_t* offsets,
+                              sph_stream_t stream);
 
 /* ------------------------------------------------------------------------------------
  * Fused solver: one time step of the reference runner (src/diffSPH/v2/runner.py:37-42):
