@@ -55,7 +55,7 @@ EXPORTS = [
     "sph_solver_launches_per_step", "sph_solver_kernel_classes", "sph_solver_kernel_name",
     "sph_solver_set_timing", "sph_solver_kernel_times", "sph_solver_autotune", "sph_solver_shapes",
     "sph_solver_set_shape", "sph_batch_workspace_bytes", "sph_batch_create", "sph_solver_graph_step",
-    "sph_neighbor_count_static",
+    "sph_neighbor_count_static", "sph_solver_vjp_rates", "sph_solver_vjp_gradient", "sph_solver_vjp_shift",
 ]
 
 _lib = None
@@ -81,6 +81,9 @@ def load(build_if_missing: bool = False):
         "sph_neighbor_count": ([P, I64, P, P, I64, DP, ctypes.c_double, P, SZ, P, P, P], ctypes.c_int),
         "sph_neighbor_fill": ([P, I64, P, P, I64, DP, ctypes.c_double, P, SZ, P, I64, P, P, P, P, P, P, P, P],
                               ctypes.c_int),
+        "sph_solver_vjp_rates": ([P, P, P, P, P, P, P, P, P], ctypes.c_int),
+        "sph_solver_vjp_gradient": ([P, P, P, P, P], ctypes.c_int),
+        "sph_solver_vjp_shift": ([P, P, P, P, P, P], ctypes.c_int),
         "sph_neighbor_count_static": ([P, I64, P, P, I64, DP, ctypes.c_double, P, P, P], ctypes.c_int),
         "sph_solver_workspace_bytes": ([PP, I64, I64, ctypes.POINTER(SZ)], ctypes.c_int),
         "sph_solver_create": ([PP, I64, I64, P, SZ, ctypes.POINTER(P)], ctypes.c_int),

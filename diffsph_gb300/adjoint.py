@@ -1,0 +1,248 @@
+"""Reverse-mode gradients of plain delta-SPH rollouts on the sm_103a VJP kernels.
+
+Scope: one periodic (or open) fluid-only domain with the viscid deltaSPH viscosity, the
+symplectic Euler step of the reference runner (integration.py:357-392, both density
+updates) followed by delta+ shifting (shifting.py:119-147, 882-1019). The reference has no
+adjoint of its own: it differentiates its torch operators with autograd step by step.
+
+One step z = (x, u, rho) -> z'' is, with rates (a, drho) = RHS(z) (simulationStep):
+
+    stage 1   x_h = x + dt/2 u,  u_h = u + dt/2 a(z),  rho_h = rho + dt/2 drho(z)
+    stage 2   u'  = u + dt a(z_h),  x' = x + dt (u + u')/2,
+              rho' = rho_h                                    (density update 'reference')
+              rho' = rho (2 - e)/(2 + e), e = -dt drho(z_h)/rho_h   ('rational')
+    shift     x'' = x' + clamp(dx(x', rho', Ma(u'))),  u'' = u',  rho'' = rho'
+
+The backward pass runs those three lines in reverse; the operator VJPs (shift, RHS pass B
+and the renormalised density gradient, pass A) are the CUDA kernels of libsph103.so,
+the elementwise integrator algebra is done here in torch. ``rollout`` checkpoints the
+state every ``checkpoint_every`` steps of the fused forward and recomputes a segment's
+stage states when its turn comes in the backward pass, so memory stays at
+O(n / checkpoint_every + checkpoint_every) states.
+"""
+from __future__ import annotations
+
+import copy
+
+import numpy as np
+import torch
+
+from .solver import Solver
+
+__all__ = ["rollout", "rollout_loss_and_grad", "step_stages", "step_vjp", "Rollout"]
+
+
+def _f32(v) -> float:
+    return float(np.float32(v))
+
+
+class _Consts:
+    def __init__(self, config):
+        dt = float(config["timestep"]["dt"])
+        self.dt = _f32(dt)
+        self.dth = _f32(dt / 2.0)
+        self.cs = float(config["fluid"]["cs"])
+        self.compute_mach = bool(config.get("shifting", {}).get("computeMach", True))
+        self.rational = config.get("integration", {}).get("densityUpdate", "reference") != "reference"
+
+
+def _check_scope(config):
+    diff = config.get("diffusion", {})
+    if diff.get("velocityScheme", "deltaSPH_inviscid") != "deltaSPH_viscid":
+        raise ValueError("the adjoint covers the deltaSPH_viscid viscosity")
+    if config.get("boundary", {}).get("active", False):
+        raise ValueError("the adjoint covers fluid-only domains")
+    if config.get("integration", {}).get("scheme", "symplecticEuler") != "symplecticEuler":
+        raise ValueError("the adjoint covers the symplecticEuler scheme")
+
+
+def _state(x, u, rho):
+    return {"positions": x, "velocities": u, "densities": rho}
+
+
+def step_stages(sol: Solver, C: _Consts, x, u, rho, shift: bool = True):
+    """Stage states of one step from (x, u, rho), evaluated operator by operator with the
+    fused step's operation order. Returns (z0, z_half, z_int, z_next, drho_half)."""
+    sol.upload(_state(x, u, rho))
+    r1 = sol.rhs()
+    xh = x + u * C.dth
+    uh = u + r1["dudt"] * C.dth
+    rh = rho + r1["drhodt"] * C.dth
+    sol.upload(_state(xh, uh, rh))
+    r2 = sol.rhs()
+    u1 = u + r2["dudt"] * C.dt
+    x1 = x + (0.5 * (u + u1)) * C.dt
+    if C.rational:
+        eps = (-C.dt * r2["drhodt"]) / rh
+        rho1 = rho * (2.0 - eps) / (2.0 + eps)
+    else:
+        rho1 = rh.clone()
+    if shift:
+        sol.upload(_state(x1, u1, rho1))
+        x2 = x1 + sol.shift()
+    else:
+        x2 = x1.clone()
+    return (x, u, rho), (xh, uh, rh), (x1, u1, rho1), (x2, u1.clone(), rho1.clone()), r2["drhodt"]
+
+
+def step_vjp(sol: Solver, C: _Consts, stages, xbar2, ubar2, rbar2, shift: bool = True):
+    """Adjoint of one step: from the adjoints of z'' to those of z (and of nu)."""
+    (x, u, rho), (xh, uh, rh), (x1, u1, rho1), _, drho_h = stages
+    n = x.shape[0]
+    dev = x.device
+    nu_part = torch.empty(n, device=dev)
+    nubar = torch.zeros((), dtype=torch.float64, device=dev)
+    # shift: x'' = x' + dx(x', rho', Ma(u'))
+    xbar1 = torch.zeros_like(x)
+    rbar1 = rbar2.clone()
+    ubar1 = ubar2.clone()
+    if shift:
+        sol.upload(_state(x1, u1, rho1))
+        mach = torch.empty(n, device=dev)
+        sol.vjp_shift(xbar2, xbar1, rbar1, mach)
+        if C.compute_mach:
+            sp = torch.linalg.vector_norm(u1, dim=1)
+            k = int(torch.argmax(sp))
+            if float(sp[k]) > 0:
+                ubar1[k] += mach.sum() / C.cs * u1[k] / sp[k]
+    else:
+        xbar1 += xbar2
+    # stage 2: u' = u + dt a(z_h); x' = x + dt (u + u')/2; rho' = rho_h or rational(rho, rho_h, drho(z_h))
+    ubar1_t = ubar1 + (0.5 * C.dt) * xbar1
+    xbar = xbar1.clone()
+    ubar = ubar1_t + (0.5 * C.dt) * xbar1
+    abar_h = C.dt * ubar1_t
+    rbar_h = torch.zeros_like(rho)
+    rbar = torch.zeros_like(rho)
+    drbar_h = None
+    if C.rational:
+        eps = (-C.dt * drho_h) / rh
+        R = (2.0 - eps) / (2.0 + eps)
+        rbar += rbar1 * R
+        ebar = rbar1 * rho * (-4.0 / (2.0 + eps) ** 2)
+        drbar_h = ebar * (-C.dt / rh)
+        rbar_h += ebar * (C.dt * drho_h / rh ** 2)
+    else:
+        rbar_h += rbar1
+    # pass B (and pass A when drho(z_h) has an adjoint) at z_h
+    sol.upload(_state(xh, uh, rh))
+    xbar_h = torch.zeros_like(x)
+    ubar_h = torch.zeros_like(u)
+    gbar_h = torch.zeros_like(x) if drbar_h is not None else None
+    sol.vjp_rates(abar_h, drbar_h, xbar_h, ubar_h, rbar_h, gbar_h, nu_part)
+    nubar += nu_part.double().sum()
+    if gbar_h is not None:
+        sol.vjp_gradient(gbar_h, xbar_h, rbar_h)
+    # stage 1: x_h = x + dt/2 u; u_h = u + dt/2 a(z); rho_h = rho + dt/2 drho(z)
+    xbar += xbar_h
+    ubar += C.dth * xbar_h + ubar_h
+    rbar += rbar_h
+    abar0 = C.dth * ubar_h
+    drbar0 = C.dth * rbar_h
+    sol.upload(_state(x, u, rho))
+    gbar0 = torch.zeros_like(x)
+    sol.vjp_rates(abar0, drbar0, xbar, ubar, rbar, gbar0, nu_part)
+    nubar += nu_part.double().sum()
+    sol.vjp_gradient(gbar0, xbar, rbar)
+    return xbar, ubar, rbar, nubar
+
+
+def _with_nu(config, nu):
+    cfg = copy.deepcopy(config)
+    cfg["diffusion"]["nu"] = float(nu)
+    return cfg
+
+
+def _forward(sol, x0, u0, rho0, n_steps, every, shift):
+    """Fused forward; returns the final state and the checkpoints {step: (x, u, rho)}."""
+    ckpt = {}
+    sol.upload(_state(x0, u0, rho0))
+    k = 0
+    while k < n_steps:
+        got = sol.download()
+        ckpt[k] = (got["positions"], got["velocities"], got["densities"])
+        m = min(every, n_steps - k)
+        if shift:
+            sol.step(m)
+        else:
+            for _ in range(m):
+                sol.integrate()
+        k += m
+    sol.check()
+    got = sol.download()
+    return (got["positions"], got["velocities"], got["densities"]), ckpt
+
+
+def _backward(sol, C, ckpt, n_steps, every, shift, xbar, ubar, rbar):
+    nubar = torch.zeros((), dtype=torch.float64, device=xbar.device)
+    for k0 in sorted(ckpt, reverse=True):
+        m = min(every, n_steps - k0)
+        x, u, rho = ckpt[k0]
+        tape = []
+        for _ in range(m):
+            st = step_stages(sol, C, x, u, rho, shift)
+            tape.append(st)
+            x, u, rho = st[3]
+        for st in reversed(tape):
+            xbar, ubar, rbar, nb = step_vjp(sol, C, st, xbar, ubar, rbar, shift)
+            nubar += nb
+    return xbar, ubar, rbar, nubar
+
+
+class Rollout(torch.autograd.Function):
+    """(x0, u0, rho0, nu) -> (x_n, u_n, rho_n) after n_steps full steps; differentiable in
+    all four inputs through the VJP kernels with segment checkpointing."""
+
+    @staticmethod
+    def forward(ctx, x0, u0, rho0, nu, config, n_steps, every, shift, fluid_extra):
+        _check_scope(config)
+        cfg = _with_nu(config, float(nu))
+        fluid = dict(fluid_extra)
+        fluid.update(_state(x0.detach(), u0.detach(), rho0.detach()))
+        sol = Solver(cfg, fluid)
+        (x, u, rho), ckpt = _forward(sol, x0.detach(), u0.detach(), rho0.detach(), n_steps, every, shift)
+        ctx.sol, ctx.ckpt, ctx.C = sol, ckpt, _Consts(cfg)
+        ctx.n_steps, ctx.every, ctx.shift = n_steps, every, shift
+        ctx.nu_dtype, ctx.nu_device = nu.dtype, nu.device
+        return x, u, rho
+
+    @staticmethod
+    def backward(ctx, gx, gu, gr):
+        n = ctx.sol.nF
+        dev = "cuda"
+        xbar = (gx if gx is not None else torch.zeros(n, 2, device=dev)).float().contiguous().clone()
+        ubar = (gu if gu is not None else torch.zeros(n, 2, device=dev)).float().contiguous().clone()
+        rbar = (gr if gr is not None else torch.zeros(n, device=dev)).float().contiguous().clone()
+        xbar, ubar, rbar, nubar = _backward(ctx.sol, ctx.C, ctx.ckpt, ctx.n_steps, ctx.every, ctx.shift,
+                                            xbar, ubar, rbar)
+        nub = nubar.to(device=ctx.nu_device, dtype=ctx.nu_dtype)
+        return xbar, ubar, rbar, nub, None, None, None, None, None
+
+
+def rollout(config, fluid, n_steps, nu=None, checkpoint_every=25, shift=True, x0=None, u0=None, rho0=None):
+    """Differentiable rollout of ``n_steps`` steps. Tensors x0 / u0 / rho0 / nu (defaults:
+    the fluid dict's fields and config['diffusion']['nu']) may require grad."""
+    _check_scope(config)
+    dev = "cuda"
+
+    def _t(v, ref):
+        return (v if v is not None else torch.as_tensor(ref)).to(device=dev, dtype=torch.float32).contiguous()
+
+    x0 = _t(x0, fluid["positions"])
+    u0 = _t(u0, fluid["velocities"])
+    rho0 = _t(rho0, fluid["densities"])
+    if nu is None:
+        nu = torch.tensor(float(config["diffusion"]["nu"]), dtype=torch.float64)
+    extra = {k: fluid[k] for k in ("masses", "supports") if k in fluid}
+    return Rollout.apply(x0, u0, rho0, nu, config, int(n_steps), int(checkpoint_every), bool(shift), extra)
+
+
+def rollout_loss_and_grad(config, fluid, target_u, n_steps, checkpoint_every=25, shift=True):
+    """Loss = mean((u_n - target)^2) over all velocity components; returns (loss, du0, dnu)."""
+    u0 = torch.as_tensor(fluid["velocities"]).to("cuda", torch.float32).clone().requires_grad_(True)
+    nu = torch.tensor(float(config["diffusion"]["nu"]), dtype=torch.float64, requires_grad=True)
+    _, u, _ = rollout(config, fluid, n_steps, nu=nu, checkpoint_every=checkpoint_every, shift=shift, u0=u0)
+    tgt = torch.as_tensor(target_u).to("cuda", torch.float32)
+    loss = torch.mean((u - tgt) ** 2)
+    loss.backward()
+    return float(loss), u0.grad.detach(), float(nu.grad)

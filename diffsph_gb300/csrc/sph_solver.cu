@@ -60,6 +60,7 @@ struct Phys {
     float diff_eps;     // 1e-6 * h
     float v_eps;        // eps * h^2
     float v_num;        // viscid 8 nu rho0 ; inviscid alpha h cs rho0   (divided by rho_i)
+    float dvnum_dnu;    // d v_num / d nu (viscid: 8 rho0; inviscid: 0)
     int bvisc;
     float bv_eps, bv_num;
     float gx, gy;
@@ -679,6 +680,409 @@ __global__ void k_dom_keys(int64_t n, const float4* __restrict__ X4, const int32
     atomicAdd(&count[k], 1);
 }
 
+
+// ======================================================================================
+// Adjoint of the fluid-only, viscid delta-SPH step: vector-Jacobian products of pass A,
+// pass B and the shift, in gather form. With a uniform support the exact neighbor relation
+// is symmetric, so particle k collects, over its neighbors j, the derivative of its own
+// pair terms T_kj (with its own multipliers) and of the neighbors' terms T_jk with respect
+// to k's variables (with the neighbors' multipliers): the transpose of the neighbor list
+// is walked without atomics. Derivatives are those of the exact expressions with
+// grad W_ij = f(r) x_ij, f = -20 C/h^4 (1-q)^3, f' = 60 C/h^5 (1-q)^2.
+// ======================================================================================
+struct KD {
+    float f, fp;
+};
+
+__device__ __forceinline__ KD kern_fd(float r, const Phys& P) {
+    float q = r * P.inv_h;
+    float om = fmaxf(1.f - q, 0.f);
+    float c4 = P.kc.cg * P.inv_h;
+    KD k;
+    k.f = -20.f * c4 * om * om * om;
+    k.fp = 60.f * c4 * P.inv_h * om * om;
+    return k;
+}
+
+__device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b); }
+__device__ __forceinline__ float dot2(float2 a, float2 b) { return a.x * b.x + a.y * b.y; }
+
+// gradients of lam . T_ij for the four pass-B pair terms (pressure, viscosity, continuity,
+// diffusion) with respect to the pair vector and the variables of i and j
+struct BVjp {
+    float2 gx, gui, guj, gGi, gGj;
+    float gri, grj, gpi, gpj;
+};
+
+__device__ __forceinline__ BVjp pairB_vjp(float2 x, float r, float2 ui, float2 uj, float ri, float rj, float pi,
+                                          float pj, float2 Gi, float2 Gj, float2 lP, float2 lV, float lC, float lD,
+                                          const Phys& P) {
+    BVjp o;
+    KD k = kern_fd(r, P);
+    float ir = 1.f / r, irj = 1.f / rj;
+    float2 xh = f2(x.x * ir, x.y * ir);
+    // pressure: (p_i + p_j)/rho_j f x
+    float lPx = dot2(lP, x);
+    float sP = (pi + pj) * irj;
+    o.gx = f2(sP * (k.f * lP.x + lPx * k.fp * xh.x), sP * (k.f * lP.y + lPx * k.fp * xh.y));
+    o.gpi = o.gpj = k.f * lPx * irj;
+    o.grj = -sP * k.f * lPx * irj;
+    // viscosity: (u_ij . x) phi f x / rho_j, phi = 1 / (r (r + eps h^2))
+    float2 uij = f2(ui.x - uj.x, ui.y - uj.y);
+    float ux = dot2(uij, x), lVx = dot2(lV, x);
+    float phi = 1.f / (r * (r + P.v_eps));
+    float phip = -(2.f * r + P.v_eps) * phi * phi;
+    float pf = phi * k.f, pfp = phip * k.f + phi * k.fp;
+    float cV = pf * irj;
+    o.gx.x += (uij.x * lVx + lV.x * ux) * cV + ux * lVx * irj * pfp * xh.x;
+    o.gx.y += (uij.y * lVx + lV.y * ux) * cV + ux * lVx * irj * pfp * xh.y;
+    o.gui = f2(x.x * lVx * cV, x.y * lVx * cV);
+    o.guj = f2(-o.gui.x, -o.gui.y);
+    o.grj += -(ux * lVx * cV) * irj;
+    // continuity: (u_j - u_i) . x f / rho_j
+    float cx = -ux;
+    o.gx.x += lC * irj * (-uij.x * k.f + cx * k.fp * xh.x);
+    o.gx.y += lC * irj * (-uij.y * k.f + cx * k.fp * xh.y);
+    float cC = lC * k.f * irj;
+    o.guj.x += cC * x.x;
+    o.guj.y += cC * x.y;
+    o.gui.x -= cC * x.x;
+    o.gui.y -= cC * x.y;
+    o.grj += -lC * cx * k.f * irj * irj;
+    // diffusion: [-2 (rho_j - rho_i) f psi + (G_i + G_j) . x f] / rho_j, psi = r / (r + 1e-6 h)
+    float psi = r / (r + P.diff_eps);
+    float psip = P.diff_eps / ((r + P.diff_eps) * (r + P.diff_eps));
+    float fpsi = k.f * psi, fpsip = k.fp * psi + k.f * psip;
+    float2 Gs = f2(Gi.x + Gj.x, Gi.y + Gj.y);
+    float Gx = dot2(Gs, x);
+    float dr = rj - ri;
+    float TD = (-2.f * dr * fpsi + Gx * k.f) * irj;
+    o.gx.x += lD * irj * (-2.f * dr * fpsip * xh.x + Gs.x * k.f + Gx * k.fp * xh.x);
+    o.gx.y += lD * irj * (-2.f * dr * fpsip * xh.y + Gs.y * k.f + Gx * k.fp * xh.y);
+    o.gri = lD * irj * 2.f * fpsi;
+    o.grj += lD * irj * (-2.f * fpsi) - lD * TD * irj;
+    o.gGi = o.gGj = f2(lD * k.f * x.x * irj, lD * k.f * x.y * irj);
+    return o;
+}
+
+// multipliers of pass B from the adjoints of the rates (original order in, sorted order out)
+__global__ void k_lam_rates(int64_t n, const float4* __restrict__ X4, const int32_t* __restrict__ uid, Dom D,
+                            const float* __restrict__ abar, const float* __restrict__ drbar,
+                            float4* __restrict__ L4, float4* __restrict__ L2) {
+    int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const Phys& P = D.P;
+    int o = uid[s];
+    float rho = X4[s].z;
+    float2 a = f2(abar[2 * o], abar[2 * o + 1]);
+    float dr = drbar ? drbar[o] : 0.f;
+    float mr = P.m / rho;
+    L4[s] = make_float4(-mr * a.x, -mr * a.y, P.v_num * mr * a.x, P.v_num * mr * a.y);
+    L2[s] = make_float4(-P.m * rho * dr, P.diff_coef * P.m * dr, 0.f, 0.f);
+}
+
+template <bool PER>
+__global__ void __launch_bounds__(128) k_vjp_rates(int64_t n, const float4* __restrict__ X4,
+                                                   const float4* __restrict__ V4, const int32_t* __restrict__ start,
+                                                   Dom D, const int32_t* __restrict__ uid,
+                                                   const float4* __restrict__ L4, const float4* __restrict__ L2,
+                                                   uint32_t* __restrict__ words, float* __restrict__ xbar,
+                                                   float* __restrict__ ubar, float* __restrict__ rbar,
+                                                   float* __restrict__ Gbar, float* __restrict__ nup) {
+    __shared__ int32_t s_list[4][kCap * 32];
+    const Phys& P = D.P;
+    const Grid& g = D.g;
+    int64_t k = (int64_t)blockIdx.x * 128 + threadIdx.x;
+    bool inb = k < n;
+    float4 xk = inb ? X4[k] : make_float4(0.f, 0.f, 1.f, 0.f);
+    float4 vk = inb ? V4[k] : make_float4(0.f, 0.f, 0.f, 0.f);
+    float4 lk4 = inb ? L4[k] : make_float4(0.f, 0.f, 0.f, 0.f);
+    float4 lk2 = inb ? L2[k] : make_float4(0.f, 0.f, 0.f, 0.f);
+    float2 pk = f2(xk.x, xk.y);
+    float2 gx = f2(0.f, 0.f), gu = f2(0.f, 0.f), gG = f2(0.f, 0.f);
+    float gr = 0.f, gp = 0.f;
+    float2 Ps = f2(0.f, 0.f), Vs = f2(0.f, 0.f);
+    float Cs = 0.f;
+    neighbor_loop<PER, int32_t>(inb, (int)k, pk, X4, start + D.cell0, g, P, s_list[threadIdx.x >> 5], words,
+                                [&](int j) {
+        if (j == (int)k) return;
+        float4 xj = __ldg(&X4[j]);
+        float4 vj = __ldg(&V4[j]);
+        float4 lj4 = __ldg(&L4[j]);
+        float4 lj2 = __ldg(&L2[j]);
+        float x0, x1;
+        pair_vec<PER>(pk, make_float2(xj.x, xj.y), P.geo, x0, x1);
+        float sq = sq_norm_ref(x0, x1);
+        float r = sqrtf(sq);
+        if (r <= 0.f) return;
+        float2 x = f2(x0, x1);
+        float2 uk = f2(vk.x, vk.y), uj = f2(vj.x, vj.y);
+        float2 Gk = f2(vk.z, vk.w), Gj = f2(vj.z, vj.w);
+        // k's own pair term T_kj
+        BVjp a = pairB_vjp(x, r, uk, uj, xk.z, xj.z, xk.w, xj.w, Gk, Gj, f2(lk4.x, lk4.y), f2(lk4.z, lk4.w), lk2.x,
+                           lk2.y, P);
+        // the neighbor's pair term T_jk (pair vector x_j - x_k = -x)
+        BVjp b = pairB_vjp(f2(-x0, -x1), r, uj, uk, xj.z, xk.z, xj.w, xk.w, Gj, Gk, f2(lj4.x, lj4.y),
+                           f2(lj4.z, lj4.w), lj2.x, lj2.y, P);
+        gx.x += a.gx.x - b.gx.x;
+        gx.y += a.gx.y - b.gx.y;
+        gu.x += a.gui.x + b.guj.x;
+        gu.y += a.gui.y + b.guj.y;
+        gr += a.gri + b.grj;
+        gp += a.gpi + b.gpj;
+        gG.x += a.gGi.x + b.gGj.x;
+        gG.y += a.gGi.y + b.gGj.y;
+        // forward sums of k (for the derivatives of the 1/rho_k and rho_k prefactors)
+        KD kd = kern_fd(r, P);
+        float irj = 1.f / xj.z;
+        float sP = (xk.w + xj.w) * irj * kd.f;
+        Ps.x += sP * x0;
+        Ps.y += sP * x1;
+        float ux = (uk.x - uj.x) * x0 + (uk.y - uj.y) * x1;
+        float sV = ux / (r * (r + P.v_eps)) * kd.f * irj;
+        Vs.x += sV * x0;
+        Vs.y += sV * x1;
+        Cs += -ux * kd.f * irj;
+    });
+    if (!inb) return;
+    int o = uid[k];
+    float rho = xk.z;
+    // p = B ((rho/rho0)^gamma - 1): dp/drho = B gamma (rho/rho0)^(gamma-1) / rho0
+    float dpdr = P.eos.B * P.eos.gamma * powf(rho / P.eos.rho0, P.eos.gamma - 1.f) / P.eos.rho0;
+    gr += gp * dpdr - (lk4.x * Ps.x + lk4.y * Ps.y) / rho - (lk4.z * Vs.x + lk4.w * Vs.y) / rho + lk2.x * Cs / rho;
+    xbar[2 * o] += gx.x;
+    xbar[2 * o + 1] += gx.y;
+    ubar[2 * o] += gu.x;
+    ubar[2 * o + 1] += gu.y;
+    rbar[o] += gr;
+    if (Gbar) {
+        Gbar[2 * o] += gG.x;
+        Gbar[2 * o + 1] += gG.y;
+    }
+    // d du_k / d nu = dvnum_dnu (m / rho_k) Vs, and (m / rho_k) abar_k = -lambda_P
+    if (nup) nup[o] = -P.dvnum_dnu * (lk4.x * Vs.x + lk4.y * Vs.y);
+}
+
+// pass A: per-particle multipliers of g = sum (rho_i - rho_j)/rho_j f x and of
+// M = -sum f/rho_j x x^T from the adjoint of gradRho^L = m L g, L = (m M)^-1
+template <bool PER>
+__global__ void __launch_bounds__(128) k_lam_grad(int64_t n, const float4* __restrict__ X4,
+                                                  const int32_t* __restrict__ start, Dom D,
+                                                  const int32_t* __restrict__ uid, const float* __restrict__ Gbar,
+                                                  uint32_t* __restrict__ words, float4* __restrict__ LM,
+                                                  float4* __restrict__ Lg) {
+    __shared__ int32_t s_list[4][kCap * 32];
+    const Phys& P = D.P;
+    int64_t k = (int64_t)blockIdx.x * 128 + threadIdx.x;
+    bool inb = k < n;
+    float4 xk = inb ? X4[k] : make_float4(0.f, 0.f, 1.f, 0.f);
+    float2 pk = f2(xk.x, xk.y);
+    float M00 = 0.f, M01 = 0.f, M10 = 0.f, M11 = 0.f, g0 = 0.f, g1 = 0.f;
+    int nf = 0;
+    neighbor_loop<PER, int32_t>(inb, (int)k, pk, X4, start + D.cell0, D.g, P, s_list[threadIdx.x >> 5], words,
+                                [&](int j) {
+        float4 xj = __ldg(&X4[j]);
+        float x0, x1;
+        pair_vec<PER>(pk, make_float2(xj.x, xj.y), P.geo, x0, x1);
+        ++nf;
+        if (j == (int)k) return;
+        float r = sqrtf(sq_norm_ref(x0, x1));
+        KD kd = kern_fd(r, P);
+        float w = kd.f / xj.z;
+        M00 -= w * x0 * x0;
+        M01 -= w * x0 * x1;
+        M10 -= w * x1 * x0;
+        M11 -= w * x1 * x1;
+        float c = (xk.z - xj.z) * w;
+        g0 += c * x0;
+        g1 += c * x1;
+    });
+    if (!inb) return;
+    int o = uid[k];
+    float m = P.m;
+    float G0 = Gbar[2 * o], G1 = Gbar[2 * o + 1];
+    M2 L;
+    if (nf < 4) {
+        L.a = 1.f; L.b = 0.f; L.c = 0.f; L.d = 1.f;
+    } else {
+        L = pinv2x2_ref(m * M00, m * M01, m * M10, m * M11);
+    }
+    // gbar = m L^T G; Lbar = m G g^T; Mbar = -L^T Lbar L^T (the multiplier of M carries m)
+    float gb0 = m * (L.a * G0 + L.c * G1), gb1 = m * (L.b * G0 + L.d * G1);
+    float mb00 = 0.f, mb01 = 0.f, mb10 = 0.f, mb11 = 0.f;
+    if (nf >= 4) {
+        float Lb00 = m * G0 * g0, Lb01 = m * G0 * g1, Lb10 = m * G1 * g0, Lb11 = m * G1 * g1;
+        // T = L^T Lbar
+        float t00 = L.a * Lb00 + L.c * Lb10, t01 = L.a * Lb01 + L.c * Lb11;
+        float t10 = L.b * Lb00 + L.d * Lb10, t11 = L.b * Lb01 + L.d * Lb11;
+        // Mbar = -T L^T
+        mb00 = -(t00 * L.a + t01 * L.b);
+        mb01 = -(t00 * L.c + t01 * L.d);
+        mb10 = -(t10 * L.a + t11 * L.b);
+        mb11 = -(t10 * L.c + t11 * L.d);
+    }
+    LM[k] = make_float4(m * mb00, m * mb01, m * mb10, m * mb11);
+    Lg[k] = make_float4(gb0, gb1, 0.f, 0.f);
+}
+
+__device__ __forceinline__ void pairA_vjp(float2 x, float r, float ri, float rj, float2 lg, float4 lM, const Phys& P,
+                                          float2& gx, float& gri, float& grj) {
+    KD k = kern_fd(r, P);
+    float irj = 1.f / rj;
+    float2 xh = f2(x.x / r, x.y / r);
+    // g term: (rho_i - rho_j)/rho_j f (lg . x)
+    float lgx = dot2(lg, x);
+    float c = (ri - rj) * irj;
+    gx = f2(c * (k.f * lg.x + lgx * k.fp * xh.x), c * (k.f * lg.y + lgx * k.fp * xh.y));
+    gri = irj * k.f * lgx;
+    grj = -k.f * lgx * ri * irj * irj;
+    // M term: -f/rho_j x^T Mbar x
+    float Mx0 = (lM.x + lM.x) * x.x + (lM.y + lM.z) * x.y;
+    float Mx1 = (lM.z + lM.y) * x.x + (lM.w + lM.w) * x.y;
+    float xMx = x.x * (lM.x * x.x + lM.y * x.y) + x.y * (lM.z * x.x + lM.w * x.y);
+    gx.x += -irj * (k.f * Mx0 + xMx * k.fp * xh.x);
+    gx.y += -irj * (k.f * Mx1 + xMx * k.fp * xh.y);
+    grj += k.f * irj * irj * xMx;
+}
+
+template <bool PER>
+__global__ void __launch_bounds__(128) k_vjp_grad(int64_t n, const float4* __restrict__ X4,
+                                                  const int32_t* __restrict__ start, Dom D,
+                                                  const int32_t* __restrict__ uid, const float4* __restrict__ LM,
+                                                  const float4* __restrict__ Lg, uint32_t* __restrict__ words,
+                                                  float* __restrict__ xbar, float* __restrict__ rbar) {
+    __shared__ int32_t s_list[4][kCap * 32];
+    const Phys& P = D.P;
+    int64_t k = (int64_t)blockIdx.x * 128 + threadIdx.x;
+    bool inb = k < n;
+    float4 xk = inb ? X4[k] : make_float4(0.f, 0.f, 1.f, 0.f);
+    float4 lMk = inb ? LM[k] : make_float4(0.f, 0.f, 0.f, 0.f);
+    float4 lgk = inb ? Lg[k] : make_float4(0.f, 0.f, 0.f, 0.f);
+    float2 pk = f2(xk.x, xk.y);
+    float2 gx = f2(0.f, 0.f);
+    float gr = 0.f;
+    neighbor_loop<PER, int32_t>(inb, (int)k, pk, X4, start + D.cell0, D.g, P, s_list[threadIdx.x >> 5], words,
+                                [&](int j) {
+        if (j == (int)k) return;
+        float4 xj = __ldg(&X4[j]);
+        float4 lMj = __ldg(&LM[j]);
+        float4 lgj = __ldg(&Lg[j]);
+        float x0, x1;
+        pair_vec<PER>(pk, make_float2(xj.x, xj.y), P.geo, x0, x1);
+        float r = sqrtf(sq_norm_ref(x0, x1));
+        if (r <= 0.f) return;
+        float2 ga, gb;
+        float ari, arj, bri, brj;
+        pairA_vjp(f2(x0, x1), r, xk.z, xj.z, f2(lgk.x, lgk.y), lMk, P, ga, ari, arj);
+        pairA_vjp(f2(-x0, -x1), r, xj.z, xk.z, f2(lgj.x, lgj.y), lMj, P, gb, bri, brj);
+        gx.x += ga.x - gb.x;
+        gx.y += ga.y - gb.y;
+        gr += ari + brj;
+    });
+    if (!inb) return;
+    int o = uid[k];
+    xbar[2 * o] += gx.x;
+    xbar[2 * o + 1] += gx.y;
+    rbar[o] += gr;
+}
+
+// shift: multipliers from the adjoint of the shifted positions (clamped components carry none)
+template <bool PER>
+__global__ void __launch_bounds__(128) k_lam_shift(int64_t n, const float4* __restrict__ X4,
+                                                   const int32_t* __restrict__ start, Dom D,
+                                                   const int32_t* __restrict__ uid, const uint32_t* __restrict__ maxv,
+                                                   const float* __restrict__ xbar_new, uint32_t* __restrict__ words,
+                                                   float4* __restrict__ LS, float* __restrict__ mapart) {
+    __shared__ int32_t s_list[4][kCap * 32];
+    const Phys& P = D.P;
+    int64_t k = (int64_t)blockIdx.x * 128 + threadIdx.x;
+    bool inb = k < n;
+    float4 xk = inb ? X4[k] : make_float4(0.f, 0.f, 1.f, 0.f);
+    float2 pk = f2(xk.x, xk.y);
+    float s0 = 0.f, s1 = 0.f;
+    neighbor_loop<PER, int32_t>(inb, (int)k, pk, X4, start + D.cell0, D.g, P, s_list[threadIdx.x >> 5], words,
+                                [&](int j) {
+        if (j == (int)k) return;
+        float4 xj = __ldg(&X4[j]);
+        float x0, x1;
+        pair_vec<PER>(pk, make_float2(xj.x, xj.y), P.geo, x0, x1);
+        float r = sqrtf(sq_norm_ref(x0, x1));
+        KD kd = kern_fd(r, P);
+        float W = wendland_w(r * P.inv_h, P.kc);
+        float kk = W * P.invW0;
+        float w = 1.f + P.shR * (kk * kk) * (kk * kk);
+        float c = w * kd.f / (xk.z + xj.z);
+        s0 += c * x0;
+        s1 += c * x1;
+    });
+    if (!inb) return;
+    int o = uid[k];
+    float Ma = P.compute_mach ? __uint_as_float(maxv[0]) * P.inv_cs : 0.1f;
+    float sc = P.sh_scale * P.m;
+    float d0 = sc * Ma * s0, d1 = sc * Ma * s1;
+    float a0 = fabsf(d0) < P.sh_thr ? 1.f : 0.f, a1 = fabsf(d1) < P.sh_thr ? 1.f : 0.f;
+    float xb0 = xbar_new[2 * o] * a0, xb1 = xbar_new[2 * o + 1] * a1;
+    LS[k] = make_float4(sc * Ma * xb0, sc * Ma * xb1, 0.f, 0.f);
+    mapart[o] = P.compute_mach ? sc * (xb0 * s0 + xb1 * s1) : 0.f;
+}
+
+__device__ __forceinline__ void pairS_vjp(float2 x, float r, float ri, float rj, float2 lS, const Phys& P, float2& gx,
+                                          float& gri, float& grj) {
+    KD k = kern_fd(r, P);
+    float W = wendland_w(r * P.inv_h, P.kc);
+    float kk = W * P.invW0;
+    float kk3 = kk * kk * kk;
+    float w = 1.f + P.shR * kk3 * kk;
+    float Wp = k.f * r;
+    float wp = 4.f * P.shR * kk3 * Wp * P.invW0;
+    float ir = 1.f / r, den = 1.f / (ri + rj);
+    float2 xh = f2(x.x * ir, x.y * ir);
+    float lx = dot2(lS, x);
+    float wf = w * k.f, wfp = wp * k.f + w * k.fp;
+    gx = f2(den * (wf * lS.x + lx * wfp * xh.x), den * (wf * lS.y + lx * wfp * xh.y));
+    gri = grj = -wf * lx * den * den;
+}
+
+template <bool PER>
+__global__ void __launch_bounds__(128) k_vjp_shift(int64_t n, const float4* __restrict__ X4,
+                                                   const int32_t* __restrict__ start, Dom D,
+                                                   const int32_t* __restrict__ uid, const float4* __restrict__ LS,
+                                                   const float* __restrict__ xbar_new, uint32_t* __restrict__ words,
+                                                   float* __restrict__ xbar, float* __restrict__ rbar) {
+    __shared__ int32_t s_list[4][kCap * 32];
+    const Phys& P = D.P;
+    int64_t k = (int64_t)blockIdx.x * 128 + threadIdx.x;
+    bool inb = k < n;
+    float4 xk = inb ? X4[k] : make_float4(0.f, 0.f, 1.f, 0.f);
+    float4 lk = inb ? LS[k] : make_float4(0.f, 0.f, 0.f, 0.f);
+    float2 pk = f2(xk.x, xk.y);
+    float2 gx = f2(0.f, 0.f);
+    float gr = 0.f;
+    neighbor_loop<PER, int32_t>(inb, (int)k, pk, X4, start + D.cell0, D.g, P, s_list[threadIdx.x >> 5], words,
+                                [&](int j) {
+        if (j == (int)k) return;
+        float4 xj = __ldg(&X4[j]);
+        float4 lj = __ldg(&LS[j]);
+        float x0, x1;
+        pair_vec<PER>(pk, make_float2(xj.x, xj.y), P.geo, x0, x1);
+        float r = sqrtf(sq_norm_ref(x0, x1));
+        if (r <= 0.f) return;
+        float2 ga, gb;
+        float ari, arj, bri, brj;
+        pairS_vjp(f2(x0, x1), r, xk.z, xj.z, f2(lk.x, lk.y), P, ga, ari, arj);
+        pairS_vjp(f2(-x0, -x1), r, xj.z, xk.z, f2(lj.x, lj.y), P, gb, bri, brj);
+        gx.x += ga.x - gb.x;
+        gx.y += ga.y - gb.y;
+        gr += ari + brj;
+    });
+    if (!inb) return;
+    int o = uid[k];
+    // x'' = x' + delta(x'): the identity part plus the shift's Jacobian
+    xbar[2 * o] += xbar_new[2 * o] + gx.x;
+    xbar[2 * o + 1] += xbar_new[2 * o + 1] + gx.y;
+    rbar[o] += gr;
+}
+
 }  // namespace sph
 
 using namespace sph;
@@ -832,6 +1236,7 @@ static Phys make_phys(const sph_params_t* p, int64_t nF) {
     P.v_eps = (float)p->eps * (float)(h * h);
     P.v_num = p->visc_scheme ? (float)((float)((float)p->alpha * (float)h) * (float)p->cs * (float)p->rho0)
                              : (float)(2.0 * (2 + 2) * p->nu * p->rho0);
+    P.dvnum_dnu = p->visc_scheme ? 0.f : (float)(2.0 * (2 + 2) * p->rho0);
     P.bvisc = p->bvisc_scheme;
     P.bv_eps = (float)p->b_eps * (float)(h * h);
     P.bv_num = p->bvisc_scheme ? (float)((float)((float)p->b_alpha * (float)h) * (float)p->cs * (float)p->rho0)
@@ -1289,6 +1694,82 @@ extern "C" int sph_solver_autotune(sph_solver_t* S, int32_t* shape_out, float* m
         S->graph = nullptr;
     }
     if (shape_out) *shape_out = best_shape;
+    return cudaGetLastError() == cudaSuccess ? SPH_OK : SPH_ERR_CUDA;
+}
+
+
+// ------------------------------------------------------------------------------------
+// Adjoint entry points (single fluid-only domain, viscid viscosity), evaluated at the
+// current state; gradients accumulate (+=) into the caller's arrays (original order).
+// ------------------------------------------------------------------------------------
+static int adjoint_ok(sph_solver* S) {
+    if (!S || S->nd != 1 || S->nB != 0 || S->prm.visc_scheme != 0) return SPH_ERR_ARGUMENT;
+    return SPH_OK;
+}
+
+extern "C" int sph_solver_vjp_rates(sph_solver_t* S, const float* abar, const float* drbar, float* xbar, float* ubar,
+                                    float* rbar, float* Gbar, float* nu_part, sph_stream_t stream) {
+    int rc = adjoint_ok(S);
+    if (rc) return rc;
+    if (!abar || !xbar || !ubar || !rbar) return SPH_ERR_ARGUMENT;
+    cudaStream_t st = (cudaStream_t)stream;
+    if ((rc = rebuild(S, st))) return rc;
+    RhsOut none = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    launch_a(S, S->Xc, S->Vc, none, st);  // gradRho^L of the current state (pass-B inputs)
+    const Dom& D = S->doms_host[0];
+    k_lam_rates<<<blocks_for(S->n), kBlock, 0, st>>>(S->n, S->Xc, S->uid, D, abar, drbar, S->Xh, S->Xf);
+    unsigned gb = blocks_for(S->n, 128);
+    if (S->periodic)
+        k_vjp_rates<true><<<gb, 128, 0, st>>>(S->n, S->Xc, S->Vc, S->start, D, S->uid, S->Xh, S->Xf, S->words, xbar,
+                                              ubar, rbar, Gbar, nu_part);
+    else
+        k_vjp_rates<false><<<gb, 128, 0, st>>>(S->n, S->Xc, S->Vc, S->start, D, S->uid, S->Xh, S->Xf, S->words, xbar,
+                                               ubar, rbar, Gbar, nu_part);
+    return cudaGetLastError() == cudaSuccess ? SPH_OK : SPH_ERR_CUDA;
+}
+
+extern "C" int sph_solver_vjp_gradient(sph_solver_t* S, const float* Gbar, float* xbar, float* rbar,
+                                       sph_stream_t stream) {
+    int rc = adjoint_ok(S);
+    if (rc) return rc;
+    if (!Gbar || !xbar || !rbar) return SPH_ERR_ARGUMENT;
+    cudaStream_t st = (cudaStream_t)stream;
+    if ((rc = rebuild(S, st))) return rc;
+    const Dom& D = S->doms_host[0];
+    unsigned gb = blocks_for(S->n, 128);
+    if (S->periodic) {
+        k_lam_grad<true><<<gb, 128, 0, st>>>(S->n, S->Xc, S->start, D, S->uid, Gbar, S->words, S->Xh, S->Xf);
+        k_vjp_grad<true><<<gb, 128, 0, st>>>(S->n, S->Xc, S->start, D, S->uid, S->Xh, S->Xf, S->words, xbar, rbar);
+    } else {
+        k_lam_grad<false><<<gb, 128, 0, st>>>(S->n, S->Xc, S->start, D, S->uid, Gbar, S->words, S->Xh, S->Xf);
+        k_vjp_grad<false><<<gb, 128, 0, st>>>(S->n, S->Xc, S->start, D, S->uid, S->Xh, S->Xf, S->words, xbar, rbar);
+    }
+    return cudaGetLastError() == cudaSuccess ? SPH_OK : SPH_ERR_CUDA;
+}
+
+extern "C" int sph_solver_vjp_shift(sph_solver_t* S, const float* xbar_new, float* xbar, float* rbar,
+                                    float* mach_part, sph_stream_t stream) {
+    int rc = adjoint_ok(S);
+    if (rc) return rc;
+    if (!xbar_new || !xbar || !rbar || !mach_part) return SPH_ERR_ARGUMENT;
+    if (!S->prm.shift_on) return SPH_ERR_ARGUMENT;
+    cudaStream_t st = (cudaStream_t)stream;
+    if ((rc = rebuild(S, st))) return rc;
+    if (cudaMemsetAsync(S->maxv, 0, sizeof(uint32_t), st) != cudaSuccess) return SPH_ERR_CUDA;
+    k_maxvel<<<blocks_for(S->n), kBlock, 0, st>>>(S->n, S->Vc, nullptr, S->maxv);
+    const Dom& D = S->doms_host[0];
+    unsigned gb = blocks_for(S->n, 128);
+    if (S->periodic) {
+        k_lam_shift<true><<<gb, 128, 0, st>>>(S->n, S->Xc, S->start, D, S->uid, S->maxv, xbar_new, S->words, S->Xh,
+                                              mach_part);
+        k_vjp_shift<true><<<gb, 128, 0, st>>>(S->n, S->Xc, S->start, D, S->uid, S->Xh, xbar_new, S->words, xbar,
+                                              rbar);
+    } else {
+        k_lam_shift<false><<<gb, 128, 0, st>>>(S->n, S->Xc, S->start, D, S->uid, S->maxv, xbar_new, S->words,
+                                               S->Xh, mach_part);
+        k_vjp_shift<false><<<gb, 128, 0, st>>>(S->n, S->Xc, S->start, D, S->uid, S->Xh, xbar_new, S->words, xbar,
+                                               rbar);
+    }
     return cudaGetLastError() == cudaSuccess ? SPH_OK : SPH_ERR_CUDA;
 }
 

@@ -222,6 +222,22 @@ class Solver:
             o["boundary_densities"] = rb
         return o
 
+    # -- adjoint (fluid-only, viscid) -------------------------------------------------------
+    def vjp_rates(self, abar, drbar, xbar, ubar, rbar, gbar=None, nu_part=None):
+        """Accumulates the pass-B vector-Jacobian product at the current state (see
+        sph_solver_vjp_rates); all arrays are CUDA float32 in the original order."""
+        _lib.check("sph_solver_vjp_rates", self.lib.sph_solver_vjp_rates(
+            self.handle, _ptr(abar), _ptr(drbar), _ptr(xbar), _ptr(ubar), _ptr(rbar), _ptr(gbar), _ptr(nu_part),
+            _stream()))
+
+    def vjp_gradient(self, gbar, xbar, rbar):
+        _lib.check("sph_solver_vjp_gradient", self.lib.sph_solver_vjp_gradient(
+            self.handle, _ptr(gbar), _ptr(xbar), _ptr(rbar), _stream()))
+
+    def vjp_shift(self, xbar_new, xbar, rbar, mach_part):
+        _lib.check("sph_solver_vjp_shift", self.lib.sph_solver_vjp_shift(
+            self.handle, _ptr(xbar_new), _ptr(xbar), _ptr(rbar), _ptr(mach_part), _stream()))
+
     def flags(self) -> int:
         f = ctypes.c_uint32()
         _lib.check("sph_solver_flags", self.lib.sph_solver_flags(self.handle, ctypes.byref(f), _stream()))

@@ -175,6 +175,39 @@ int sph_solver_shift(sph_solver_t* s, float* dx, sph_stream_t stream);
 int sph_solver_rhs(sph_solver_t* s, float* dudt, float* drhodt, float* grad_rho, float* L,
                    float* pressure, float* rho_boundary, int32_t* num_neighbors, sph_stream_t stream);
 
+/* ------------------------------------------------------------------------------------
+ * Adjoint (vector-Jacobian products) of the step's operators at the current state, for a
+ * single fluid-only domain with viscid viscosity (deltaSPH_viscid). No reference entry
+ * point has these: the reference differentiates its torch operators with autograd
+ * (simulationStep, deltaPlus.py:176-422, per step). Every VJP walks the exact neighbor
+ * lists in gather form (each particle collects its own pair terms and its neighbors' terms
+ * through the symmetric neighbor relation), so no atomics are used. Inputs and outputs
+ * are in the original particle order; gradients ACCUMULATE (+=) into xbar[nF][2],
+ * ubar[nF][2], rbar[nF], gbar[nF][2]. Positions are differentiated through the periodic
+ * wrap as the identity. Other configurations return SPH_ERR_ARGUMENT.
+ * ------------------------------------------------------------------------------------ */
+
+/* Right-hand side (pass B: continuity, delta-diffusion, pressure with the Tait EOS,
+ * viscosity): given the adjoints abar[nF][2] of dudt and drbar[nF] of drhodt (NULL = 0),
+ * accumulates the adjoints of positions, velocities, densities and of gradRho^L (gbar,
+ * NULL to drop), and writes per particle nu_part[nF] (NULL to skip) whose sum is the
+ * adjoint of diffusion.nu. gradRho^L is an input here; its own dependence on the state is
+ * sph_solver_vjp_gradient. */
+int sph_solver_vjp_rates(sph_solver_t* s, const float* abar, const float* drbar, float* xbar,
+                         float* ubar, float* rbar, float* gbar, float* nu_part, sph_stream_t stream);
+
+/* Renormalised density gradient (pass A: M, L = pinv(M), gradRho^L = m L g): given
+ * gbar[nF][2], accumulates the adjoints of positions and densities. */
+int sph_solver_vjp_gradient(sph_solver_t* s, const float* gbar, float* xbar, float* rbar,
+                            sph_stream_t stream);
+
+/* delta+ shift x'' = x' + clamp(dx(x', rho', Ma)): given xbar_new[nF][2] (the adjoint of
+ * x''), accumulates xbar (identity part included) and rbar, and writes mach_part[nF]
+ * whose sum is the adjoint of Ma = max|u| / cs (0 when shifting.computeMach is off).
+ * Clamped components carry no gradient. */
+int sph_solver_vjp_shift(sph_solver_t* s, const float* xbar_new, float* xbar, float* rbar,
+                         float* mach_part, sph_stream_t stream);
+
 /* Writes the current state back in the original order (NULL entries are skipped). */
 int sph_solver_download(sph_solver_t* s, float* x_fluid, float* u_fluid, float* rho_fluid,
                         float* rho_boundary, sph_stream_t stream);

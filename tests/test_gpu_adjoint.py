@@ -1,0 +1,233 @@
+"""Adjoint kernels against FP64 central finite differences of the oracle.
+
+Each operator VJP of libsph103.so (pass B rates with the pass-A density gradient, the
+delta+ shift) and the checkpointed rollout gradient are compared, along random
+directions, with central differences (eps = 1e-6) of the FP64 oracle run of the same
+scheme. Tolerance: 1e-3 relative to the finite-difference value, checked separately for
+the position, velocity, density and nu blocks so that a small block cannot hide behind a
+large one.
+"""
+import copy
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+from oracle import sph_oracle as O  # noqa: E402
+from diffsph_gb300 import scenes  # noqa: E402
+
+EPS = 1e-6
+RTOL = 1e-3
+
+
+def _gpu():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+
+
+def _np(t):
+    return t.detach().cpu().numpy()
+
+
+def _fluid64(fl):
+    return {k: np.asarray(v, np.float64).copy() for k, v in fl.items()}
+
+
+def _advanced_state(nx=32, seed=7, steps=5):
+    """A jittered periodic Fourier flow advanced a few steps on the GPU (non-uniform
+    densities and density gradients), returned as fp32 numpy arrays."""
+    from diffsph_gb300.solver import Solver
+    cfg, st = scenes.fourier_periodic(nx, seed=seed, jitter=0.2)
+    sol = Solver(cfg, st["fluid"])
+    sol.step(steps)
+    sol.check()
+    got = sol.download()
+    fl = dict(st["fluid"])
+    fl["positions"] = _np(got["positions"])
+    fl["velocities"] = _np(got["velocities"])
+    fl["densities"] = _np(got["densities"])
+    return cfg, fl
+
+
+def _dirs(cfg, fl, rng):
+    n = fl["positions"].shape[0]
+    dx = float(cfg["particle"]["dx"])
+    umax = float(np.abs(fl["velocities"]).max())
+    rvar = float(np.asarray(fl["densities"], np.float64).std()) + 1e-4
+    return {
+        "positions": rng.standard_normal((n, 2)) * dx,
+        "velocities": rng.standard_normal((n, 2)) * umax,
+        "densities": rng.standard_normal(n) * rvar,
+    }
+
+
+def _rel(pred, fd):
+    return abs(pred - fd) / abs(fd)
+
+
+@pytest.mark.gpu
+def test_rates_vjp_matches_fp64_finite_differences():
+    _gpu()
+    from diffsph_gb300.solver import Solver
+    cfg, fl = _advanced_state()
+    rng = np.random.default_rng(11)
+    n = fl["positions"].shape[0]
+    abar = rng.standard_normal((n, 2)).astype(np.float32)
+    drbar = rng.standard_normal(n).astype(np.float32)
+    sol = Solver(cfg, fl)
+    dev = "cuda"
+    xbar = torch.zeros(n, 2, device=dev)
+    ubar = torch.zeros(n, 2, device=dev)
+    rbar = torch.zeros(n, device=dev)
+    gbar = torch.zeros(n, 2, device=dev)
+    nup = torch.zeros(n, device=dev)
+    sol.vjp_rates(torch.as_tensor(abar, device=dev), torch.as_tensor(drbar, device=dev), xbar, ubar, rbar, gbar, nup)
+    sol.vjp_gradient(gbar, xbar, rbar)
+    grads = {"positions": _np(xbar), "velocities": _np(ubar), "densities": _np(rbar)}
+    f64 = _fluid64(fl)
+
+    def phi(state, c):
+        (_, dudt, drho), _ = O.simulation_step({"fluid": state}, c)
+        return float(np.sum(abar * dudt) + np.sum(drbar * drho))
+
+    d = _dirs(cfg, fl, rng)
+    for key in ("positions", "velocities", "densities"):
+        sp, sm = _fluid64(f64), _fluid64(f64)
+        sp[key] = sp[key] + EPS * d[key]
+        sm[key] = sm[key] - EPS * d[key]
+        fd = (phi(sp, cfg) - phi(sm, cfg)) / (2 * EPS)
+        pred = float(np.sum(grads[key].astype(np.float64) * d[key]))
+        assert _rel(pred, fd) < RTOL, (key, pred, fd)
+    nu = float(cfg["diffusion"]["nu"])
+    cp, cm = copy.deepcopy(cfg), copy.deepcopy(cfg)
+    cp["diffusion"]["nu"] = nu * (1 + EPS)
+    cm["diffusion"]["nu"] = nu * (1 - EPS)
+    fd = (phi(_fluid64(f64), cp) - phi(_fluid64(f64), cm)) / (2 * EPS * nu)
+    pred = float(nup.double().sum())
+    assert _rel(pred, fd) < RTOL, ("nu", pred, fd)
+
+
+@pytest.mark.gpu
+def test_shift_vjp_matches_fp64_finite_differences():
+    _gpu()
+    from diffsph_gb300.solver import Solver
+    cfg, fl = _advanced_state(seed=9)
+    rng = np.random.default_rng(12)
+    n = fl["positions"].shape[0]
+    xbn = rng.standard_normal((n, 2)).astype(np.float32)
+    sol = Solver(cfg, fl)
+    dev = "cuda"
+    xbar = torch.zeros(n, 2, device=dev)
+    rbar = torch.zeros(n, device=dev)
+    mach = torch.zeros(n, device=dev)
+    sol.vjp_shift(torch.as_tensor(xbn, device=dev), xbar, rbar, mach)
+    u = np.asarray(fl["velocities"], np.float64)
+    sp = np.linalg.norm(u, axis=1)
+    k = int(np.argmax(sp))
+    ubar = np.zeros((n, 2))
+    ubar[k] = float(mach.double().sum()) / float(cfg["fluid"]["cs"]) * u[k] / sp[k]
+    grads = {"positions": _np(xbar), "velocities": ubar, "densities": _np(rbar)}
+    f64 = _fluid64(fl)
+
+    def phi(state):
+        dx, _ = O.solve_shifting({"fluid": state}, cfg)
+        return float(np.sum(xbn * (state["positions"] + dx)))
+
+    d = _dirs(cfg, fl, rng)
+    for key in ("positions", "velocities", "densities"):
+        a, b = _fluid64(f64), _fluid64(f64)
+        a[key] = a[key] + EPS * d[key]
+        b[key] = b[key] - EPS * d[key]
+        fd = (phi(a) - phi(b)) / (2 * EPS)
+        pred = float(np.sum(np.asarray(grads[key], np.float64) * d[key]))
+        assert _rel(pred, fd) < RTOL, (key, pred, fd)
+
+
+def _oracle_rollout(cfg, fl64, n):
+    s = {"fluid": _fluid64(fl64)}
+    for _ in range(n):
+        s, _ = O.full_step(s, cfg)
+    return s["fluid"]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("density_update", ["reference", "rational"])
+def test_rollout_gradient_matches_fp64_finite_differences(density_update):
+    _gpu()
+    from diffsph_gb300.adjoint import rollout
+    cfg, st = scenes.fourier_periodic(24, seed=3, jitter=0.1)
+    cfg["integration"]["densityUpdate"] = density_update
+    fl = st["fluid"]
+    n = fl["positions"].shape[0]
+    steps = 12
+    rng = np.random.default_rng(5)
+    target = scenes.fourier_velocity(np.asarray(fl["positions"], np.float64), np.random.default_rng(99))
+    dev = "cuda"
+    u0 = torch.as_tensor(fl["velocities"], device=dev).clone().requires_grad_(True)
+    rho0 = torch.as_tensor(fl["densities"], device=dev).clone().requires_grad_(True)
+    x0 = torch.as_tensor(fl["positions"], device=dev).clone().requires_grad_(True)
+    nu = torch.tensor(float(cfg["diffusion"]["nu"]), dtype=torch.float64, requires_grad=True)
+    _, u, _ = rollout(cfg, fl, steps, nu=nu, checkpoint_every=5, x0=x0, u0=u0, rho0=rho0)
+    loss = torch.mean((u - torch.as_tensor(target, dtype=torch.float32, device=dev)) ** 2)
+    loss.backward()
+    f64 = _fluid64(fl)
+
+    def L(state, c):
+        out = _oracle_rollout(c, state, steps)
+        return float(np.mean((out["velocities"] - target) ** 2))
+
+    ref64 = L(f64, cfg)
+    assert abs(float(loss.detach()) - ref64) <= 1e-4 * ref64
+    grads = {"positions": _np(x0.grad), "velocities": _np(u0.grad), "densities": _np(rho0.grad)}
+    d = _dirs(cfg, fl, rng)
+    for key in ("velocities", "positions", "densities"):
+        a, b = _fluid64(f64), _fluid64(f64)
+        a[key] = a[key] + EPS * d[key]
+        b[key] = b[key] - EPS * d[key]
+        fd = (L(a, cfg) - L(b, cfg)) / (2 * EPS)
+        pred = float(np.sum(grads[key].astype(np.float64) * d[key]))
+        assert _rel(pred, fd) < RTOL, (key, pred, fd)
+    nuv = float(cfg["diffusion"]["nu"])
+    cp, cm = copy.deepcopy(cfg), copy.deepcopy(cfg)
+    cp["diffusion"]["nu"] = nuv * (1 + EPS)
+    cm["diffusion"]["nu"] = nuv * (1 - EPS)
+    fd = (L(f64, cp) - L(f64, cm)) / (2 * EPS * nuv)
+    assert _rel(float(nu.grad), fd) < RTOL, ("nu", float(nu.grad), fd)
+
+
+@pytest.mark.gpu
+def test_checkpoint_interval_does_not_change_the_gradient():
+    _gpu()
+    from diffsph_gb300.adjoint import rollout_loss_and_grad
+    cfg, st = scenes.fourier_periodic(32, seed=4, jitter=0.1)
+    target = scenes.fourier_velocity(np.asarray(st["fluid"]["positions"], np.float64), np.random.default_rng(1))
+    l1, g1, n1 = rollout_loss_and_grad(cfg, st["fluid"], target, 20, checkpoint_every=1)
+    l2, g2, n2 = rollout_loss_and_grad(cfg, st["fluid"], target, 20, checkpoint_every=25)
+    l3, g3, n3 = rollout_loss_and_grad(cfg, st["fluid"], target, 20, checkpoint_every=7)
+    assert l1 == l2 == l3
+    for g, nn in ((g2, n2), (g3, n3)):
+        assert float((g - g1).abs().max()) <= 1e-4 * float(g1.abs().max())
+        assert abs(nn - n1) <= 1e-4 * abs(n1)
+
+
+@pytest.mark.gpu
+def test_vjp_rejects_unsupported_configurations():
+    _gpu()
+    from diffsph_gb300 import _lib
+    from diffsph_gb300.solver import Solver
+    cfg, st = scenes.dam_break(1.0 / 32)
+    sol = Solver(cfg, st["fluid"], st["boundary"])
+    n = sol.nF
+    z2 = torch.zeros(n, 2, device="cuda")
+    z1 = torch.zeros(n, device="cuda")
+    with pytest.raises(_lib.SphError) as e:
+        sol.vjp_rates(z2, z1, z2, z2, z1)
+    assert e.value.code == 1
+
+
+def test_rollout_rejects_out_of_scope_configs():
+    from diffsph_gb300.adjoint import rollout
+    cfg, st = scenes.dam_break(1.0 / 32)
+    with pytest.raises(ValueError):
+        rollout(cfg, st["fluid"], 2)
