@@ -245,4 +245,4 @@ def rollout_loss_and_grad(config, fluid, target_u, n_steps, checkpoint_every=25,
     tgt = torch.as_tensor(target_u).to("cuda", torch.float32)
     loss = torch.mean((u - tgt) ** 2)
     loss.backward()
-    return float(loss), u0.grad.detach(), float(nu.grad)
+    return float(loss.detach()), u0.grad.detach(), float(nu.grad)

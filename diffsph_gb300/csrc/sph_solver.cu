@@ -1245,7 +1245,7 @@ static Phys make_phys(const sph_params_t* p, int64_t nF) {
     P.gy = p->gravity_on ? (float)p->gravity[1] : 0.f;
     P.nF = (int)nF;
     {  // W0 = W(dx/h, h) evaluated in fp32 like the reference (shifting.py:122)
-        float q0 = (float)p->dx / (float)h;
+        float q0 = (float)(p->dx / h);  // torch.tensor(dx / support): the double quotient, rounded
         float om = 1.f - q0;
         float hh = (float)h;
         float W0 = (om * om) * (om * om) * (1.f + 4.f * q0) * (float)(7.0 / M_PI) / (hh * hh);

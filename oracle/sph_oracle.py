@@ -514,7 +514,9 @@ def delta_plus_shifting(ps, nb, config):
     dt = ps["densities"].dtype.type
     h = _flt(config["particle"]["support"])
     dx = _flt(config["particle"]["dx"])
-    W0 = wendland_kernel(np.asarray([dt(dx) / dt(h)], dtype=ps["densities"].dtype), dt(h))[0]
+    # W_0 is built from torch.tensor(python float) arguments (shifting.py:121-122), i.e. in
+    # fp32 whatever the state's precision: q0 = fp32(dx / h), h = fp32(h)
+    W0 = wendland_kernel(np.asarray([np.float32(dx / h)], dtype=np.float32), np.float32(h))[0]
     i, j = nb["indices"]
     k = nb["kernels"] / W0
     R = dt(_flt(config["shifting"]["R"]))

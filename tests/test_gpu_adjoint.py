@@ -231,3 +231,82 @@ def test_rollout_rejects_out_of_scope_configs():
     cfg, st = scenes.dam_break(1.0 / 32)
     with pytest.raises(ValueError):
         rollout(cfg, st["fluid"], 2)
+
+
+def _adjoint_fixture():
+    import json
+    import os
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "adjoint_fourier24_100.npz")
+    z = np.load(path)
+    cfg = json.loads(bytes(z["config_json"]).decode())
+    fl = {k.split("/")[-1]: z[k] for k in z.files if k.startswith("in/fluid/")}
+    return z, cfg, fl
+
+
+def test_oracle_rollout_matches_reference_100_steps():
+    """The FP64 oracle's 100-step trajectory reproduces the reference's FP64 run (the
+    golden fixture made by torch autograd through the reference)."""
+    z, cfg, fl = _adjoint_fixture()
+    out = _oracle_rollout(cfg, fl, int(z["steps"]))
+    u = out["velocities"]
+    assert float(np.max(np.abs(u - z["f64/u_final"]))) <= 1e-9 * float(np.max(np.abs(z["f64/u_final"])))
+    loss = float(np.mean((u - z["target"]) ** 2))
+    assert abs(loss - float(z["f64/loss"])) <= 1e-10 * float(z["f64/loss"])
+
+
+def _rel_l2(a, b):
+    a, b = np.asarray(a, np.float64), np.asarray(b, np.float64)
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+@pytest.mark.gpu
+def test_rollout_gradient_matches_reference_autograd_100_steps():
+    """Gradients of the 100-step loss against the reference's own torch-autograd gradient
+    (FP64 run): relative L2 error <= 1e-3 for the velocity, position and density blocks
+    and relative error <= 1e-3 for nu. The reference's FP32 run is held to the same bar
+    as a statement of what FP32 rounding costs."""
+    _gpu()
+    from diffsph_gb300.adjoint import rollout
+    z, cfg, fl = _adjoint_fixture()
+    steps = int(z["steps"])
+    dev = "cuda"
+    x0 = torch.as_tensor(fl["positions"], device=dev).clone().requires_grad_(True)
+    u0 = torch.as_tensor(fl["velocities"], device=dev).clone().requires_grad_(True)
+    r0 = torch.as_tensor(fl["densities"], device=dev).clone().requires_grad_(True)
+    nu = torch.tensor(float(cfg["diffusion"]["nu"]), dtype=torch.float64, requires_grad=True)
+    _, u, _ = rollout(cfg, fl, steps, nu=nu, checkpoint_every=25, x0=x0, u0=u0, rho0=r0)
+    loss = torch.mean((u - torch.as_tensor(z["target"], dtype=torch.float32, device=dev)) ** 2)
+    loss.backward()
+    assert abs(float(loss.detach()) - float(z["f64/loss"])) <= 1e-5 * float(z["f64/loss"])
+    for name, g in (("u0", u0.grad), ("x0", x0.grad), ("rho0", r0.grad)):
+        assert _rel_l2(z[f"f32/{name}"], z[f"f64/{name}"]) < 1e-3
+        assert _rel_l2(_np(g), z[f"f64/{name}"]) < 1e-3, name
+    assert abs(float(nu.grad) - float(z["f64/nu"])) <= 1e-3 * abs(float(z["f64/nu"]))
+
+
+@pytest.mark.gpu
+def test_velocity_gradient_along_32_random_directions():
+    """d loss / d u0 along 32 random directions against FP64 central differences
+    (eps = 1e-6) of the oracle rollout: 24x24 periodic Fourier flow, 12 steps,
+    checkpoints every 25 steps (one segment)."""
+    _gpu()
+    from diffsph_gb300.adjoint import rollout_loss_and_grad
+    cfg, st = scenes.fourier_periodic(24, seed=8, jitter=0.1)
+    fl = st["fluid"]
+    steps = 12
+    target = scenes.fourier_velocity(np.asarray(fl["positions"], np.float64), np.random.default_rng(42))
+    loss, gu, _ = rollout_loss_and_grad(cfg, fl, target, steps)
+    g = _np(gu).astype(np.float64)
+    f64 = _fluid64(fl)
+    rng = np.random.default_rng(2024)
+    errs = []
+    for _ in range(32):
+        d = rng.standard_normal(f64["velocities"].shape)
+        a, b = _fluid64(f64), _fluid64(f64)
+        a["velocities"] += EPS * d
+        b["velocities"] -= EPS * d
+        la = np.mean((_oracle_rollout(cfg, a, steps)["velocities"] - target) ** 2)
+        lb = np.mean((_oracle_rollout(cfg, b, steps)["velocities"] - target) ** 2)
+        fd = (la - lb) / (2 * EPS)
+        errs.append(_rel(float(np.sum(g * d)), fd))
+    assert max(errs) < RTOL, max(errs)
