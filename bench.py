@@ -36,7 +36,10 @@ WORKLOADS = {
     "dambreak_dx512": dict(scene="dam_break", dx=1.0 / 512),
     "dambreak_dx256": dict(scene="dam_break", dx=1.0 / 256),
     "tgv_64": dict(scene="taylor_green", nx=64),
+    # gradient of a rollout loss: 128x128 periodic Fourier flow, 1000 steps, checkpoints every 25
+    "adjoint_fourier128": dict(scene="adjoint", nx=128, seed=0, target_seed=1, rollout=1000, every=25),
 }
+ADJOINT_METRIC = "adjoint particle-steps/s (forward + backward of a checkpointed rollout)"
 
 
 def make_scene(name):
@@ -143,6 +146,10 @@ def run_reference(args):
     if rank != 0:
         return
     steps, warm = args.steps, args.warmup
+    if WORKLOADS[args.workload]["scene"] == "adjoint":
+        print(json.dumps({"impl": "reference", "unavailable": "the reference has no adjoint; its gradients "
+                          "come from torch autograd through its own package, which is not installed here"}))
+        return
     from oracle import sph_oracle as O
     from diffsph_gb300 import scenes
     sc = WORKLOADS[args.workload]["scene"]
@@ -350,6 +357,81 @@ def run_e2e(sol, scene, batched, nF, world, e_steps, stream):
             "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "steps": e_steps}
 
 
+def run_adjoint(args):
+    """Gradient of mean((u_T - u_target)^2) w.r.t. the initial velocity and nu over a
+    1000-step rollout (forward with checkpoints, backward with segment recomputation).
+    value: state resident on the device; e2e: the same call from host arrays, gradient
+    copied back to pinned host memory."""
+    import numpy as np
+    import torch
+    import __graft_entry__ as ge
+    from diffsph_gb300 import scenes
+    from diffsph_gb300.adjoint import rollout
+
+    rank = int(os.environ.get("RANK", "0"))
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    ge.build()
+    w = WORKLOADS[args.workload]
+    cfg, st = scenes.fourier_periodic(w["nx"], seed=w["seed"], jitter=0.1)
+    fl = st["fluid"]
+    nF = fl["positions"].shape[0]
+    target = scenes.fourier_velocity(np.asarray(fl["positions"], np.float64), np.random.default_rng(w["target_seed"]))
+    T, every = w["rollout"], w["every"]
+    stream = torch.cuda.Stream()
+    tgt_d = torch.as_tensor(target, dtype=torch.float32, device="cuda")
+    dev = {k: torch.as_tensor(fl[k], device="cuda") for k in ("positions", "velocities", "densities")}
+    times = {}
+
+    def grad_run(n_steps, from_host=False, record=False):
+        if from_host:
+            u0 = torch.from_numpy(fl["velocities"]).pin_memory().to("cuda", non_blocking=True)
+            x0 = torch.from_numpy(fl["positions"]).pin_memory().to("cuda", non_blocking=True)
+            r0 = torch.from_numpy(fl["densities"]).pin_memory().to("cuda", non_blocking=True)
+            tg = torch.from_numpy(target.astype(np.float32)).pin_memory().to("cuda", non_blocking=True)
+        else:
+            u0, x0, r0, tg = dev["velocities"], dev["positions"], dev["densities"], tgt_d
+        u0 = u0.clone().requires_grad_(True)
+        nu = torch.tensor(float(cfg["diffusion"]["nu"]), dtype=torch.float64, requires_grad=True)
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        ev[0].record(stream)
+        _, u, _ = rollout(cfg, fl, n_steps, nu=nu, checkpoint_every=every, x0=x0, u0=u0, rho0=r0)
+        loss = torch.mean((u - tg) ** 2)
+        ev[1].record(stream)
+        loss.backward()
+        g = u0.grad
+        if from_host:
+            out = torch.empty(g.shape, pin_memory=True)
+            out.copy_(g, non_blocking=True)
+        ev[2].record(stream)
+        torch.cuda.synchronize()
+        if record:
+            times["forward_ms"] = ev[0].elapsed_time(ev[1])
+            times["backward_ms"] = ev[1].elapsed_time(ev[2])
+        return ev[0].elapsed_time(ev[2]), float(loss.detach()), float(nu.grad)
+
+    with torch.cuda.stream(stream):
+        for _ in range(max(args.warmup, 3)):
+            grad_run(10)
+        torch.cuda.synchronize()
+        with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
+            ms, loss, dnu = grad_run(T, record=True)
+        ms_e2e, _, _ = grad_run(T, from_host=True)
+    if rank != 0:
+        return
+    line = {
+        "metric": ADJOINT_METRIC, "value": nF * T / (ms / 1e3), "unit": "particle-steps/s", "n_gpus": 1,
+        "steps": T, "warmup": max(args.warmup, 3), "ms_per_step": ms / T, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": args.workload, "fluid_particles": nF, "rollout_steps": T, "checkpoint_every": every,
+                   "loss": loss, "dloss_dnu": dnu, "forward_ms": times["forward_ms"],
+                   "backward_ms": times["backward_ms"], "l2": "state below L2 size; no flush (latency-bound)"},
+        "e2e": {"value": nF * T / (ms_e2e / 1e3), "unit": "particle-steps/s",
+                "h2d_bytes_per_step": (nF * 5 + nF * 2) * 4 / T, "d2h_bytes_per_step": nF * 2 * 4 / T},
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -362,6 +444,8 @@ def main():
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
+    elif WORKLOADS[args.workload]["scene"] == "adjoint":
+        run_adjoint(args)
     else:
         run_ours(args)
 

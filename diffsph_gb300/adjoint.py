@@ -101,10 +101,11 @@ def step_vjp(sol: Solver, C: _Consts, stages, xbar2, ubar2, rbar2, shift: bool =
         mach = torch.empty(n, device=dev)
         sol.vjp_shift(xbar2, xbar1, rbar1, mach)
         if C.compute_mach:
+            # Ma = max|u'| / cs: the adjoint goes to the arg-max particle (no host sync)
             sp = torch.linalg.vector_norm(u1, dim=1)
-            k = int(torch.argmax(sp))
-            if float(sp[k]) > 0:
-                ubar1[k] += mach.sum() / C.cs * u1[k] / sp[k]
+            k = torch.argmax(sp).view(1)
+            scale = mach.sum() / C.cs / sp[k].clamp_min(1e-30)
+            ubar1.index_add_(0, k, scale[:, None] * u1[k])
     else:
         xbar1 += xbar2
     # stage 2: u' = u + dt a(z_h); x' = x + dt (u + u')/2; rho' = rho_h or rational(rho, rho_h, drho(z_h))
