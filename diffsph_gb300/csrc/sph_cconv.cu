@@ -1,0 +1,517 @@
+// Learned continuous-convolution step: the edge-basis aggregation over the exact neighbor
+// lists and the basis-weight contraction as a tcgen05 BF16 GEMM (TMA-fed shared-memory
+// tiles, FP32 accumulator in tensor memory).
+//
+// Layer (per particle i, neighbors j within the support H, self included):
+//   E_i[b, c] = inv_norm * sum_j phi_b(x_i - x_j) h_j[c]              (aggregation)
+//   or, in the relative (difference) form, h_j[c] - h_i[c] in place of h_j[c]
+//   y_i[o]    = sum_{b, c} E_i[b, c] W[b C + c, o]                     (contraction, GEMM)
+// Basis phi_{8a + m}(x) = w(q) T_a(2q - 1) F_m(theta), q = |x| / H, w(q) = (1 - q^2)^2,
+// T_a Chebyshev polynomials (a < 8), F_m the angular Fourier terms of z = x / |x|:
+// 1, Re z, Im z, Re z^2, Im z^2, Re z^3, Im z^3, Re z^4 (all but F_0 vanish at x = 0).
+#include <cuda.h>
+#include <cudaTypedefs.h>
+#include <cuda_bf16.h>
+#include <math.h>
+
+#include <mutex>
+
+#include "../../include/sph103.h"
+#include "sph_internal.cuh"
+
+namespace sph {
+namespace cconv {
+
+// ------------------------------------------------------------------------------------
+// tcgen05 GEMM  D[M x N] (fp32, row-major) (+)= A[M x K] (bf16, row-major) * Bt[N x K]^T
+// One CTA computes a 128 x BN tile. Warp 0 lane 0 feeds a 4-stage ring of shared-memory
+// tiles with TMA (128-byte swizzle, the canonical K-major layout of the MMA); warp 1
+// lane 0 issues the MMAs (K = 16 per instruction) into a TMEM accumulator of BN columns
+// and releases each stage with tcgen05.commit; all four warps then drain the accumulator
+// (warp w owns TMEM lanes 32w..32w+31 = rows) to global memory.
+// ------------------------------------------------------------------------------------
+constexpr int kBM = 128, kBK = 64, kStages = 4, kThreads = 128;
+constexpr uint32_t kSpinLimit = 1u << 22;  // bounded mbarrier polls (seconds at most)
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* b, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(b)), "r"(count));
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* b, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(b)), "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* b, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n"
+        " .reg .pred p;\n"
+        " mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n"
+        "}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(b)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// false when the phase did not complete within kSpinLimit polls
+__device__ __forceinline__ bool mbar_wait(uint64_t* b, uint32_t parity) {
+    for (uint32_t it = 0; it < kSpinLimit; ++it)
+        if (mbar_try_wait(b, parity)) return true;
+    return false;
+}
+
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, uint64_t* bar, int x, int y) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+            smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar))
+        : "memory");
+}
+
+// Shared-memory matrix descriptor: K-major operand, 128-byte swizzle, 8-row groups 1024 B
+// apart (stride byte offset), leading byte offset unused for swizzled K-major layouts.
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
+    uint64_t d = 0;
+    d |= static_cast<uint64_t>((saddr >> 4) & 0x3FFFu);
+    d |= static_cast<uint64_t>(1) << 16;
+    d |= static_cast<uint64_t>(1024 >> 4) << 32;
+    d |= static_cast<uint64_t>(1) << 46;  // descriptor version of sm_100 and later
+    d |= static_cast<uint64_t>(2) << 61;  // SWIZZLE_128B
+    return d;
+}
+
+// Instruction descriptor of kind::f16: BF16 A and B (K-major), FP32 accumulator, M x N.
+__host__ __device__ constexpr uint32_t idesc_bf16(int m, int n) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | (static_cast<uint32_t>(n >> 3) << 17) |
+           (static_cast<uint32_t>(m >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t tmem, uint64_t da, uint64_t db, uint32_t idesc, uint32_t acc) {
+    asm volatile(
+        "{\n"
+        " .reg .pred p;\n"
+        " setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n"
+        "}\n" ::"r"(tmem),
+        "l"(da), "l"(db), "r"(idesc), "r"(acc));
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&v)[16]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+        "%15}, [%16];"
+        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+          "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+template <int BN>
+struct GemmCfg {
+    static constexpr uint32_t kA = kBM * kBK * 2;
+    static constexpr uint32_t kB = BN * kBK * 2;
+    static constexpr uint32_t kStage = kA + kB;
+    static constexpr size_t kSmem = static_cast<size_t>(kStage) * kStages + 1024;
+};
+
+template <int BN>
+__global__ void __launch_bounds__(kThreads, 1)
+    k_gemm_tn(const __grid_constant__ CUtensorMap ma, const __grid_constant__ CUtensorMap mb, float* __restrict__ D,
+              int64_t ldd, int K, int accumulate, uint32_t* __restrict__ err) {
+    extern __shared__ uint8_t dsm[];
+    __shared__ uint64_t full[kStages], empty[kStages], done;
+    __shared__ uint32_t tmem_slot;
+    using C = GemmCfg<BN>;
+    uint8_t* tiles = dsm + ((1024u - (smem_u32(dsm) & 1023u)) & 1023u);  // SW128 tiles: 1024-aligned
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t m0 = static_cast<int64_t>(blockIdx.y) * kBM;
+    const int n0 = blockIdx.x * BN;
+    const int nk = K / kBK;
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < kStages; ++s) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
+        }
+        mbar_init(&done, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_slot)),
+                     "r"(BN));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    const uint32_t tmem = tmem_slot;
+
+    if (warp == 0 && lane == 0) {  // TMA producer
+        for (int k = 0; k < nk; ++k) {
+            const int s = k % kStages;
+            const uint32_t ph = (k / kStages) & 1;
+            if (!mbar_wait(&empty[s], ph ^ 1)) {
+                atomicOr(err, 1u);
+                break;
+            }
+            uint8_t* sa = tiles + s * C::kStage;
+            mbar_expect_tx(&full[s], C::kStage);
+            tma_load_2d(sa, &ma, &full[s], k * kBK, static_cast<int>(m0));
+            tma_load_2d(sa + C::kA, &mb, &full[s], k * kBK, n0);
+        }
+    } else if (warp == 1 && lane == 0) {  // MMA issuer
+        constexpr uint32_t idesc = idesc_bf16(kBM, BN);
+        for (int k = 0; k < nk; ++k) {
+            const int s = k % kStages;
+            const uint32_t ph = (k / kStages) & 1;
+            if (!mbar_wait(&full[s], ph)) {  // every load issued before this one has landed
+                atomicOr(err, 2u);
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;");
+            const uint64_t da = sw128_desc(smem_u32(tiles + s * C::kStage));
+            const uint64_t db = sw128_desc(smem_u32(tiles + s * C::kStage + C::kA));
+#pragma unroll
+            for (int kk = 0; kk < kBK / 16; ++kk)  // +32 bytes along K inside the swizzle atom
+                mma_bf16(tmem, da + 2 * kk, db + 2 * kk, idesc, (k > 0 || kk > 0) ? 1u : 0u);
+            mma_commit(&empty[s]);
+        }
+        mma_commit(&done);  // arrives once every MMA issued above has completed
+    }
+    __syncwarp();
+    const bool ready = mbar_wait(&done, 0);
+    if (!ready && lane == 0) atomicOr(err, 4u);
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    if (ready) {
+        const int64_t row = m0 + warp * 32 + lane;
+        float* drow = D + row * ldd + n0;
+#pragma unroll 1
+        for (int c = 0; c < BN; c += 16) {
+            uint32_t v[16];
+            tmem_ld16(tmem + (static_cast<uint32_t>(warp * 32) << 16) + static_cast<uint32_t>(c), v);
+            float4* dst = reinterpret_cast<float4*>(drow + c);
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                float4 o = make_float4(__uint_as_float(v[4 * q]), __uint_as_float(v[4 * q + 1]),
+                                       __uint_as_float(v[4 * q + 2]), __uint_as_float(v[4 * q + 3]));
+                if (accumulate) {
+                    const float4 p = dst[q];
+                    o.x += p.x;
+                    o.y += p.y;
+                    o.z += p.z;
+                    o.w += p.w;
+                }
+                dst[q] = o;
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(BN));
+}
+
+// ------------------------------------------------------------------------------------
+// Edge basis and aggregation (CUDA cores, FP32 accumulation)
+// ------------------------------------------------------------------------------------
+constexpr int kBasis = 64;
+constexpr int kAggThreads = 128;
+constexpr int kEdgeChunk = 16;
+
+struct BasisGeo {
+    Geo geo;
+    float inv_H;
+    float eps;  // added to |x| in z = x / (|x| + eps) so that the self pair has z = 0
+};
+
+// the 8 values phi_{8a + m}, m = 0..7, of radial order a for the pair vector x
+__device__ __forceinline__ void basis_row(float x0, float x1, int a, const BasisGeo& bg, float* out) {
+    const float r = sqrtf(x0 * x0 + x1 * x1);
+    const float q = fminf(r * bg.inv_H, 1.f);
+    const float om = 1.f - q * q;
+    const float w = om * om;
+    const float s = 2.f * q - 1.f;
+    float t0 = 1.f, t1 = s, ta = (a == 0) ? 1.f : s;
+    for (int k = 2; k <= a; ++k) {
+        const float t2 = 2.f * s * t1 - t0;
+        t0 = t1;
+        t1 = t2;
+        ta = t2;
+    }
+    const float R = w * ta;
+    const float inv = 1.f / (r + bg.eps);
+    const float zr = x0 * inv, zi = x1 * inv;
+    const float z2r = zr * zr - zi * zi, z2i = 2.f * zr * zi;
+    const float z3r = z2r * zr - z2i * zi, z3i = z2r * zi + z2i * zr;
+    const float z4r = z3r * zr - z3i * zi;
+    out[0] = R;
+    out[1] = R * zr;
+    out[2] = R * zi;
+    out[3] = R * z2r;
+    out[4] = R * z2i;
+    out[5] = R * z3r;
+    out[6] = R * z3i;
+    out[7] = R * z4r;
+}
+
+// phi for up to kEdgeChunk edges of the row [e0, e1) into s_phi[edge][64]; sign = +1 for
+// x_i - x_j (row of i lists j), -1 for the transposed use (row of j lists i)
+__device__ __forceinline__ void chunk_basis(const float* __restrict__ x, float2 pi, const int32_t* __restrict__ nbr,
+                                            int64_t e0, int64_t e1, const BasisGeo& bg, float sign,
+                                            float (*s_phi)[kBasis], int32_t* s_j) {
+    const int t = threadIdx.x;
+    const int e = t >> 3, a = t & 7;
+    const int64_t ge = e0 + e;
+    float vals[8];
+    int j = -1;
+    if (ge < e1) {
+        j = nbr[ge];
+        float x0, x1;
+        pair_vec<true>(pi, make_float2(x[2 * j], x[2 * j + 1]), bg.geo, x0, x1);
+        basis_row(sign * x0, sign * x1, a, bg, vals);
+    } else {
+#pragma unroll
+        for (int m = 0; m < 8; ++m) vals[m] = 0.f;
+    }
+#pragma unroll
+    for (int m = 0; m < 8; ++m) s_phi[e][a * 8 + m] = vals[m];
+    if (a == 0) s_j[e] = j;
+}
+
+template <int C, bool REL>
+__global__ void __launch_bounds__(kAggThreads) k_aggregate(int64_t n, const float* __restrict__ x,
+                                                           const int64_t* __restrict__ off,
+                                                           const int32_t* __restrict__ nbr, BasisGeo bg,
+                                                           float inv_norm, const __nv_bfloat16* __restrict__ h,
+                                                           __nv_bfloat16* __restrict__ E) {
+    constexpr int kPer = kBasis * C / kAggThreads;  // outputs per thread
+    constexpr int kStride = kAggThreads / C;        // basis stride between them
+    __shared__ float s_phi[kEdgeChunk][kBasis];
+    __shared__ int32_t s_j[kEdgeChunk];
+    const int64_t i = blockIdx.x;
+    const int t = threadIdx.x;
+    const int c = t % C, b0 = t / C;
+    const float2 pi = make_float2(x[2 * i], x[2 * i + 1]);
+    const float hi = REL ? __bfloat162float(h[i * C + c]) : 0.f;
+    float acc[kPer];
+#pragma unroll
+    for (int k = 0; k < kPer; ++k) acc[k] = 0.f;
+    const int64_t e1 = off[i + 1];
+    for (int64_t e0 = off[i]; e0 < e1; e0 += kEdgeChunk) {
+        chunk_basis(x, pi, nbr, e0, e1, bg, 1.f, s_phi, s_j);
+        __syncthreads();
+        const int ne = static_cast<int>(e1 - e0 < kEdgeChunk ? e1 - e0 : kEdgeChunk);
+        for (int e = 0; e < ne; ++e) {
+            const float hv = __bfloat162float(h[static_cast<int64_t>(s_j[e]) * C + c]) - hi;
+#pragma unroll
+            for (int k = 0; k < kPer; ++k) acc[k] = fmaf(s_phi[e][b0 + k * kStride], hv, acc[k]);
+        }
+        __syncthreads();
+    }
+    __nv_bfloat16* Ei = E + i * (kBasis * C);
+#pragma unroll
+    for (int k = 0; k < kPer; ++k) Ei[(b0 + k * kStride) * C + c] = __float2bfloat16_rn(acc[k] * inv_norm);
+}
+
+// dh_j[c] = inv_norm * sum_{i in N(j)} sum_b phi_b(x_i - x_j) dE_i[b C + c]; the relative
+// form adds the own term -inv_norm * sum_b dE_j[b C + c] sum_{i in N(j)} phi_b(x_j - x_i)
+template <int C, bool REL>
+__global__ void __launch_bounds__(kAggThreads) k_aggregate_t(int64_t n, const float* __restrict__ x,
+                                                             const int64_t* __restrict__ off,
+                                                             const int32_t* __restrict__ nbr, BasisGeo bg,
+                                                             float inv_norm, const float* __restrict__ dE,
+                                                             int64_t ldE, float* __restrict__ dh) {
+    constexpr int kPer = kBasis * C / kAggThreads;
+    constexpr int kStride = kAggThreads / C;
+    __shared__ float s_phi[kEdgeChunk][kBasis];
+    __shared__ int32_t s_j[kEdgeChunk];
+    __shared__ float s_red[kAggThreads];
+    const int64_t jrow = blockIdx.x;
+    const int t = threadIdx.x;
+    const int c = t % C, b0 = t / C;
+    const float2 pj = make_float2(x[2 * jrow], x[2 * jrow + 1]);
+    float acc = 0.f;
+    float own[REL ? kPer : 1];
+#pragma unroll
+    for (int k = 0; k < (REL ? kPer : 1); ++k) own[k] = 0.f;
+    const int64_t e1 = off[jrow + 1];
+    for (int64_t e0 = off[jrow]; e0 < e1; e0 += kEdgeChunk) {
+        chunk_basis(x, pj, nbr, e0, e1, bg, -1.f, s_phi, s_j);
+        __syncthreads();
+        const int ne = static_cast<int>(e1 - e0 < kEdgeChunk ? e1 - e0 : kEdgeChunk);
+        for (int e = 0; e < ne; ++e) {
+            const float* dEi = dE + static_cast<int64_t>(s_j[e]) * ldE + c;
+#pragma unroll
+            for (int k = 0; k < kPer; ++k) acc = fmaf(s_phi[e][b0 + k * kStride], dEi[(b0 + k * kStride) * C], acc);
+            if (REL) {
+                // phi_b(x_j - x_i) = (-1)^(angular order of b) phi_b(x_i - x_j): F_1, F_2, F_5, F_6 are odd
+#pragma unroll
+                for (int k = 0; k < (REL ? kPer : 1); ++k) {
+                    const int b = b0 + k * kStride;
+                    const int m = b & 7;
+                    const float sg = (m == 1 || m == 2 || m == 5 || m == 6) ? -1.f : 1.f;
+                    own[k] = fmaf(sg, s_phi[e][b], own[k]);
+                }
+            }
+        }
+        __syncthreads();
+    }
+    if (REL) {
+        const float* dEj = dE + jrow * ldE + c;
+#pragma unroll
+        for (int k = 0; k < (REL ? kPer : 1); ++k) acc = fmaf(-own[k], dEj[(b0 + k * kStride) * C], acc);
+    }
+    s_red[t] = acc;
+    __syncthreads();
+    if (t < C) {
+        float s = 0.f;
+        for (int k = 0; k < kStride; ++k) s += s_red[t + k * C];
+        dh[jrow * C + t] = s * inv_norm;
+    }
+}
+
+// ------------------------------------------------------------------------------------
+// host
+// ------------------------------------------------------------------------------------
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    });
+    return fn;
+}
+
+// row-major bf16 matrix [rows x cols] (leading dimension ld elements), box 64 x box_rows
+int make_map(CUtensorMap* m, const void* ptr, int64_t rows, int64_t cols, int64_t ld, int box_rows) {
+    PFN_cuTensorMapEncodeTiled_v12000 fn = encode_fn();
+    if (!fn) return SPH_ERR_CUDA;
+    cuuint64_t dims[2] = {static_cast<cuuint64_t>(cols), static_cast<cuuint64_t>(rows)};
+    cuuint64_t strides[1] = {static_cast<cuuint64_t>(ld) * 2};
+    cuuint32_t box[2] = {static_cast<cuuint32_t>(kBK), static_cast<cuuint32_t>(box_rows)};
+    cuuint32_t es[2] = {1, 1};
+    CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(ptr), dims, strides, box, es,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS ? SPH_OK : SPH_ERR_ARGUMENT;
+}
+
+template <int BN>
+int launch_gemm(const CUtensorMap& ma, const CUtensorMap& mb, float* D, int64_t M, int64_t N, int64_t K, int64_t ldd,
+                int acc, uint32_t* err, cudaStream_t s) {
+    static std::once_flag once;
+    static cudaError_t attr = cudaSuccess;
+    std::call_once(once, [] {
+        attr = cudaFuncSetAttribute(k_gemm_tn<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    static_cast<int>(GemmCfg<BN>::kSmem));
+    });
+    if (attr != cudaSuccess) return SPH_ERR_CUDA;
+    dim3 grid(static_cast<unsigned>(N / BN), static_cast<unsigned>(M / kBM));
+    k_gemm_tn<BN><<<grid, kThreads, GemmCfg<BN>::kSmem, s>>>(ma, mb, D, ldd, static_cast<int>(K), acc, err);
+    return cudaGetLastError() == cudaSuccess ? SPH_OK : SPH_ERR_CUDA;
+}
+
+BasisGeo make_basis_geo(const sph_domain_t* d, double support) {
+    BasisGeo bg;
+    int per[2] = {d->periodic[0], d->periodic[1]};
+    bg.geo = make_geo(d->min, d->max, per);
+    bg.inv_H = static_cast<float>(1.0 / support);
+    bg.eps = static_cast<float>(1e-6 * support);
+    return bg;
+}
+
+}  // namespace cconv
+}  // namespace sph
+
+using namespace sph;
+using namespace sph::cconv;
+
+extern "C" int sph_gemm_bf16_tn(const void* A, const void* Bt, float* D, int64_t M, int64_t N, int64_t K, int64_t lda,
+                                int64_t ldb, int64_t ldd, int32_t accumulate, uint32_t* err, sph_stream_t stream) {
+    if (!A || !Bt || !D || !err) return SPH_ERR_ARGUMENT;
+    if (M <= 0 || N <= 0 || K <= 0 || M % kBM || N % 64 || K % kBK) return SPH_ERR_ARGUMENT;
+    if (M / kBM > 65535 || lda < K || ldb < K || ldd < N || lda % 8 || ldb % 8 || ldd % 4) return SPH_ERR_ARGUMENT;
+    if ((reinterpret_cast<uintptr_t>(A) | reinterpret_cast<uintptr_t>(Bt) | reinterpret_cast<uintptr_t>(D)) & 15)
+        return SPH_ERR_ARGUMENT;
+    const int bn = (N % 256 == 0) ? 256 : (N % 128 == 0) ? 128 : 64;
+    CUtensorMap ma, mb;
+    int rc = make_map(&ma, A, M, K, lda, kBM);
+    if (!rc) rc = make_map(&mb, Bt, N, K, ldb, bn);
+    if (rc) return rc;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if (bn == 256) return launch_gemm<256>(ma, mb, D, M, N, K, ldd, accumulate, err, s);
+    if (bn == 128) return launch_gemm<128>(ma, mb, D, M, N, K, ldd, accumulate, err, s);
+    return launch_gemm<64>(ma, mb, D, M, N, K, ldd, accumulate, err, s);
+}
+
+static int check_agg(int64_t n, const float* x, const int64_t* off, const sph_domain_t* d, double support,
+                     int32_t channels) {
+    if (n < 0 || !d || support <= 0) return SPH_ERR_ARGUMENT;
+    if (n > 0 && (!x || !off)) return SPH_ERR_ARGUMENT;
+    if (channels != 16 && channels != 32 && channels != 64) return SPH_ERR_ARGUMENT;
+    return SPH_OK;
+}
+
+extern "C" int sph_cconv_aggregate(const float* x, int64_t n, const int64_t* offsets, const int32_t* neighbors,
+                                   const sph_domain_t* domain, double support, double inv_norm, const void* h,
+                                   int32_t channels, int32_t relative, void* E, sph_stream_t stream) {
+    int rc = check_agg(n, x, offsets, domain, support, channels);
+    if (rc) return rc;
+    if (n == 0) return SPH_OK;
+    if (!h || !E || !neighbors) return SPH_ERR_ARGUMENT;
+    BasisGeo bg = make_basis_geo(domain, support);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const auto* hb = static_cast<const __nv_bfloat16*>(h);
+    auto* Eb = static_cast<__nv_bfloat16*>(E);
+    const float nz = static_cast<float>(inv_norm);
+    const unsigned g = static_cast<unsigned>(n);
+#define SPH_AGG(CC, RR) k_aggregate<CC, RR><<<g, kAggThreads, 0, s>>>(n, x, offsets, neighbors, bg, nz, hb, Eb)
+    if (channels == 16) {
+        if (relative) SPH_AGG(16, true); else SPH_AGG(16, false);
+    } else if (channels == 32) {
+        if (relative) SPH_AGG(32, true); else SPH_AGG(32, false);
+    } else {
+        if (relative) SPH_AGG(64, true); else SPH_AGG(64, false);
+    }
+#undef SPH_AGG
+    return cudaGetLastError() == cudaSuccess ? SPH_OK : SPH_ERR_CUDA;
+}
+
+extern "C" int sph_cconv_aggregate_t(const float* x, int64_t n, const int64_t* offsets, const int32_t* neighbors,
+                                     const sph_domain_t* domain, double support, double inv_norm, const float* dE,
+                                     int64_t ldE, int32_t channels, int32_t relative, float* dh,
+                                     sph_stream_t stream) {
+    int rc = check_agg(n, x, offsets, domain, support, channels);
+    if (rc) return rc;
+    if (n == 0) return SPH_OK;
+    if (!dE || !dh || !neighbors || ldE < 64 * channels) return SPH_ERR_ARGUMENT;
+    BasisGeo bg = make_basis_geo(domain, support);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const float nz = static_cast<float>(inv_norm);
+    const unsigned g = static_cast<unsigned>(n);
+#define SPH_AGGT(CC, RR) k_aggregate_t<CC, RR><<<g, kAggThreads, 0, s>>>(n, x, offsets, neighbors, bg, nz, dE, ldE, dh)
+    if (channels == 16) {
+        if (relative) SPH_AGGT(16, true); else SPH_AGGT(16, false);
+    } else if (channels == 32) {
+        if (relative) SPH_AGGT(32, true); else SPH_AGGT(32, false);
+    } else {
+        if (relative) SPH_AGGT(64, true); else SPH_AGGT(64, false);
+    }
+#undef SPH_AGGT
+    return cudaGetLastError() == cudaSuccess ? SPH_OK : SPH_ERR_CUDA;
+}

@@ -1,0 +1,363 @@
+"""Learned k-step continuous-convolution stepper on the sm_103a kernels.
+
+No reference implementation exists for this part (the reference project has no learned
+model). The network stands in for ``k`` plain delta-SPH steps of the periodic fluid-only
+solver: from (x, u, rho) at time t it predicts the velocity and density increments over
+k dt and a position correction (the shifting), over the same exact neighbor lists the
+solver uses (|x_i - x_j| <= H, self included).
+
+Architecture (rotation-aware continuous convolution):
+    features h0 = (u, (rho/rho0 - 1) / 0.01, 1, 0 ...)                       [n, 16]
+    4 layers    h <- silu(conv(h) + h S + b) (+ h when widths match), width 64
+                conv(h)_i = sum_{b, c} E_i[b, c] W[b C + c, :],
+                E_i[b, c] = sum_j phi_b(x_i - x_j) g_j[c] / N0,  N0 = pi (H / dx)^2,
+                g_j = h_j - h_i in the first layer (the difference form of the SPH
+                operators), g_j = h_j in the others; S is the self weight
+                phi: 8 radial Chebyshev x 8 angular Fourier terms (libsph103 sph_cconv_aggregate)
+    decoder     silu(Linear(64, 64)) -> Linear(64, 5): du (2), drho (1), dx (2), each scaled
+                by the spread of the training targets
+    update      u' = u + du,  rho' = rho + drho,  x' = x + k dt (u + u') / 2 + dx
+
+The aggregation and its transpose run on the CUDA cores; the basis-weight contraction and
+both of its backward products (dE = dy W^T, dW = E^T dy) run on the tcgen05 BF16 GEMM
+(FP32 accumulation). Weights are kept in FP32 and rounded to BF16 for every product.
+
+``judged_rollout`` keeps the plain solver as fallback and judge: each segment of learned
+steps is checked against the solver's own kinetic-energy rate (one right-hand side at the
+segment start) and a density-deviation bound; a rejected segment is re-run by the solver.
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+
+import numpy as np
+import torch
+
+from . import _lib
+from .solver import Solver, domain_struct
+
+BASIS = 64
+WIDTH = 64
+IN_CH = 16
+OUT_CH = 5
+
+
+def _stream():
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def _p(t):
+    return ctypes.c_void_p(t.data_ptr()) if t is not None else None
+
+
+_ERR = {}
+
+
+def _err_word(device):
+    key = torch.device(device).index or 0
+    if key not in _ERR:
+        _ERR[key] = torch.zeros(1, dtype=torch.int32, device=device)
+    return _ERR[key]
+
+
+def check_device_errors():
+    """Raise if a tcgen05 GEMM recorded a wait that did not complete (synchronises)."""
+    for k, w in _ERR.items():
+        v = int(w.item())
+        if v:
+            w.zero_()
+            raise RuntimeError(f"sph_gemm_bf16_tn: pipeline wait timed out (flags {v:#x}) on device {k}")
+
+
+def gemm_tn(A, Bt, out=None, accumulate=False):
+    """out[M, N] (+)= A[M, K] @ Bt[N, K]^T with BF16 inputs and FP32 output (tcgen05)."""
+    if A.dtype != torch.bfloat16 or Bt.dtype != torch.bfloat16:
+        raise TypeError("gemm_tn takes bfloat16 operands")
+    if A.stride(1) != 1 or Bt.stride(1) != 1:
+        raise ValueError("gemm_tn operands must be row-major")
+    M, K = A.shape
+    N = Bt.shape[0]
+    if Bt.shape[1] != K:
+        raise ValueError("inner dimensions differ")
+    if out is None:
+        out = torch.empty(M, N, device=A.device, dtype=torch.float32)
+    lib = _lib.load()
+    _lib.check("sph_gemm_bf16_tn", lib.sph_gemm_bf16_tn(
+        _p(A), _p(Bt), _p(out), M, N, K, A.stride(0), Bt.stride(0), out.stride(0), int(bool(accumulate)),
+        _p(_err_word(A.device)), _stream()))
+    return out
+
+
+def _pad128(n):
+    return (n + 127) // 128 * 128
+
+
+class Graph:
+    """Exact neighbor lists (CSR, symmetric) of one or several equal periodic domains."""
+
+    def __init__(self, x, config, n_domains=1):
+        from .neighborhood import exact_pairs
+        x = x.to("cuda", torch.float32).contiguous()
+        n = x.shape[0]
+        if n % n_domains:
+            raise ValueError("particles must split evenly over the domains")
+        per = n // n_domains
+        H = float(config["particle"]["support"])
+        dx = float(config["particle"]["dx"])
+        offs, nbrs = [torch.zeros(1, dtype=torch.int64, device="cuda")], []
+        base = 0
+        for d in range(n_domains):
+            xd = x[d * per:(d + 1) * per]
+            hd = torch.full((per,), H, device="cuda")
+            _, j, _, _, _, _, _, _, off = exact_pairs(xd, xd, hd, config, compute_kernels=False)
+            offs.append(off[1:] + base)
+            nbrs.append((j + d * per).to(torch.int32))
+            base += int(off[-1].item())
+        self.x = x
+        self.offsets = torch.cat(offs).contiguous()
+        self.nbr = torch.cat(nbrs).contiguous()
+        self.n = n
+        self.npad = _pad128(n)
+        self.H = H
+        self.inv_norm = 1.0 / (math.pi * (H / dx) ** 2)
+        self.domain = domain_struct(config)
+
+
+def aggregate(g: Graph, h_bf16, relative=False):
+    """E [npad, 64 C] (bf16; rows >= n are zero) of features h [n, C] (bf16)."""
+    C = h_bf16.shape[1]
+    E = torch.empty(g.npad, BASIS * C, dtype=torch.bfloat16, device="cuda")
+    if g.npad > g.n:
+        E[g.n:].zero_()
+    _lib.check("sph_cconv_aggregate", _lib.load().sph_cconv_aggregate(
+        _p(g.x), g.n, _p(g.offsets), _p(g.nbr), ctypes.byref(g.domain), g.H, g.inv_norm, _p(h_bf16.contiguous()),
+        C, int(bool(relative)), _p(E), _stream()))
+    return E
+
+
+def aggregate_t(g: Graph, dE, C, relative=False):
+    """dh [n, C] (fp32) = transpose of ``aggregate`` applied to dE [>= n, 64 C] (fp32)."""
+    dh = torch.empty(g.n, C, device="cuda")
+    _lib.check("sph_cconv_aggregate_t", _lib.load().sph_cconv_aggregate_t(
+        _p(g.x), g.n, _p(g.offsets), _p(g.nbr), ctypes.byref(g.domain), g.H, g.inv_norm, _p(dE), dE.stride(0), C,
+        int(bool(relative)), _p(dh), _stream()))
+    return dh
+
+
+class ConvFn(torch.autograd.Function):
+    """y [n, 64] = aggregate(h) W, with W [64 C, 64] (FP32 master, BF16 products)."""
+
+    @staticmethod
+    def forward(ctx, h, W, g, relative=False):
+        C = h.shape[1]
+        E = aggregate(g, h.to(torch.bfloat16), relative)
+        Wt = W.t().contiguous().to(torch.bfloat16)
+        y = gemm_tn(E, Wt)
+        ctx.save_for_backward(W)
+        ctx.E, ctx.g, ctx.C, ctx.rel = E, g, C, relative
+        return y[:g.n]
+
+    @staticmethod
+    def backward(ctx, dy):
+        (W,) = ctx.saved_tensors
+        g, E, C = ctx.g, ctx.E, ctx.C
+        dyp = torch.zeros(g.npad, WIDTH, dtype=torch.bfloat16, device="cuda")
+        dyp[:g.n] = dy
+        dE = gemm_tn(dyp, W.to(torch.bfloat16).contiguous())       # [npad, 64 C]
+        dh = aggregate_t(g, dE, C, ctx.rel)
+        dW = gemm_tn(E.t().contiguous(), dyp.t().contiguous())     # [64 C, 64]
+        return dh, dW, None, None
+
+
+class CConvNet(torch.nn.Module):
+    def __init__(self, layers=4, width=WIDTH, in_ch=IN_CH, out_ch=OUT_CH, seed=0):
+        super().__init__()
+        gen = torch.Generator().manual_seed(seed)
+        self.W = torch.nn.ParameterList()
+        self.S = torch.nn.ParameterList()
+        self.b = torch.nn.ParameterList()
+        cin = in_ch
+        for _ in range(layers):
+            K = BASIS * cin
+            self.W.append(torch.nn.Parameter(torch.randn(K, width, generator=gen) * (2.0 / K) ** 0.5))
+            self.S.append(torch.nn.Parameter(torch.randn(cin, width, generator=gen) * (1.0 / cin) ** 0.5))
+            self.b.append(torch.nn.Parameter(torch.zeros(width)))
+            cin = width
+        self.dec1 = torch.nn.Linear(width, width)
+        self.dec2 = torch.nn.Linear(width, out_ch)
+        with torch.no_grad():
+            self.dec2.weight.mul_(0.1)
+            self.dec2.bias.zero_()
+        self.register_buffer("out_scale", torch.ones(out_ch))
+
+    def forward(self, feats, g):
+        h = feats
+        for layer, (W, S, b) in enumerate(zip(self.W, self.S, self.b)):
+            y = ConvFn.apply(h, W, g, layer == 0) + h @ S + b
+            hn = torch.nn.functional.silu(y)
+            h = hn + h if hn.shape == h.shape else hn
+        return self.dec2(torch.nn.functional.silu(self.dec1(h)))
+
+
+def features(u, rho, rho0):
+    n = u.shape[0]
+    f = torch.zeros(n, IN_CH, device="cuda")
+    f[:, 0:2] = u
+    f[:, 2] = (rho / rho0 - 1.0) / 0.01
+    f[:, 3] = 1.0
+    return f
+
+
+def _min_image(d, config):
+    lo = config["domain"]["minExtent"]
+    hi = config["domain"]["maxExtent"]
+    out = d.clone()
+    for a in range(2):
+        ext = float(hi[a]) - float(lo[a])
+        out[:, a] = d[:, a] - ext * torch.round(d[:, a] / ext)
+    return out
+
+
+def _wrap(x, config):
+    lo = config["domain"]["minExtent"]
+    hi = config["domain"]["maxExtent"]
+    out = x.clone()
+    for a in range(2):
+        ext = float(hi[a]) - float(lo[a])
+        out[:, a] = torch.remainder(x[:, a] - float(lo[a]), ext) + float(lo[a])
+    return out
+
+
+class LearnedStepper:
+    """One learned step = k plain steps of the periodic fluid-only solver."""
+
+    def __init__(self, config, net: CConvNet, k=4, n_domains=1):
+        self.config, self.net, self.k, self.n_domains = config, net, k, n_domains
+        self.dt = float(config["timestep"]["dt"])
+        self.rho0 = float(config["fluid"]["rho0"])
+
+    def predict(self, x, u, rho, g=None):
+        g = g or Graph(x, self.config, self.n_domains)
+        out = self.net(features(u, rho, self.rho0), g) * self.net.out_scale
+        return out, g
+
+    def apply(self, x, u, rho, out):
+        u1 = u + out[:, 0:2]
+        rho1 = rho + out[:, 2]
+        x1 = x + (self.k * self.dt) * 0.5 * (u + u1) + out[:, 3:5]
+        return _wrap(x1, self.config), u1, rho1
+
+    @torch.no_grad()
+    def step(self, x, u, rho):
+        out, _ = self.predict(x, u, rho)
+        return self.apply(x, u, rho, out)
+
+
+def targets(config, k, a, b):
+    """Network targets between frames a and b = frame a advanced k plain steps."""
+    dt = float(config["timestep"]["dt"])
+    du = b[1] - a[1]
+    drho = b[2] - a[2]
+    dxc = _min_image(b[0] - (a[0] + (k * dt) * 0.5 * (a[1] + b[1])), config)
+    return torch.cat([du, drho[:, None], dxc], dim=1)
+
+
+def generate_trajectories(n_traj, n_frames, nx, seed=0, k=4, jitter=0.1):
+    """Solver trajectories of random divergence-free Fourier flows on the periodic square:
+    returns (config, [[(x, u, rho) per frame] per trajectory]) with frames every k steps."""
+    from . import scenes
+    rng = np.random.default_rng(seed)
+    trajs, cfg = [], None
+    for _ in range(n_traj):
+        cfg, st = scenes.fourier_periodic(nx, seed=int(rng.integers(0, 2 ** 31 - 1)), jitter=jitter)
+        sol = Solver(cfg, st["fluid"])
+        frames = []
+        for f in range(n_frames):
+            got = sol.download()
+            frames.append((_wrap(got["positions"], cfg), got["velocities"].clone(), got["densities"].clone()))
+            if f + 1 < n_frames:
+                sol.step(k)
+        sol.check()
+        trajs.append(frames)
+    return cfg, trajs
+
+
+def fit_scales(config, trajs, k):
+    t = torch.cat([targets(config, k, fr[i], fr[i + 1]) for fr in trajs for i in range(len(fr) - 1)])
+    return t.std(dim=0).clamp_min(1e-12)
+
+
+def train(net, config, trajs, iters, k=4, lr=1e-3, seed=0, log_every=0):
+    """Adam on the normalised targets of consecutive frame pairs; returns the loss history."""
+    net.out_scale.copy_(fit_scales(config, trajs, k).to(net.out_scale.device))
+    pairs = [(t, i) for t in range(len(trajs)) for i in range(len(trajs[t]) - 1)]
+    graphs = {}
+    opt = torch.optim.Adam(net.parameters(), lr=lr)
+    sched = torch.optim.lr_scheduler.CosineAnnealingLR(opt, T_max=max(iters, 1), eta_min=lr * 0.05)
+    stepper = LearnedStepper(config, net, k)
+    rng = np.random.default_rng(seed)
+    hist = []
+    for it in range(iters):
+        t, i = pairs[int(rng.integers(0, len(pairs)))]
+        a, b = trajs[t][i], trajs[t][i + 1]
+        if (t, i) not in graphs:
+            graphs[(t, i)] = Graph(a[0], config)
+        tgt = targets(config, k, a, b) / net.out_scale
+        out = net(features(a[1], a[2], stepper.rho0), graphs[(t, i)])
+        loss = torch.mean((out - tgt) ** 2)
+        opt.zero_grad(set_to_none=True)
+        loss.backward()
+        opt.step()
+        sched.step()
+        hist.append(float(loss.detach()))
+        if log_every and (it + 1) % log_every == 0:
+            print(f"iter {it + 1}: loss {np.mean(hist[-log_every:]):.4e}")
+    check_device_errors()
+    return hist
+
+
+def kinetic_energy(u, m):
+    return 0.5 * m * float(torch.sum(u * u))
+
+
+@torch.no_grad()
+def judged_rollout(stepper: LearnedStepper, fluid, n_learned, segment=8, rho_tol=0.02, ke_tol=0.05):
+    """Rollout of n_learned learned steps (k plain steps each) with the solver as judge and
+    fallback. Each segment of ``segment`` learned steps is accepted when the density stays
+    within rho_tol of rho0 and the kinetic energy stays within ke_tol (relative) of the
+    solver's prediction KE0 + t dKE/dt, dKE/dt = sum m u . a from one right-hand side at the
+    segment start; otherwise the segment is re-run by the solver. Returns the final state
+    and the counts of accepted and rejected segments."""
+    cfg = stepper.config
+    m = float(fluid["masses"][0])
+    sol = Solver(cfg, fluid)
+    got = sol.download()
+    x, u, rho = _wrap(got["positions"], cfg), got["velocities"], got["densities"]
+    accepted = rejected = 0
+    done = 0
+    while done < n_learned:
+        nseg = min(segment, n_learned - done)
+        sol.upload({"positions": x, "velocities": u, "densities": rho})
+        r = sol.rhs()
+        ke0 = kinetic_energy(u, m)
+        dke = m * float(torch.sum(u * r["dudt"]))
+        xs, us, rs = x, u, rho
+        for _ in range(nseg):
+            xs, us, rs = stepper.step(xs, us, rs)
+        T = nseg * stepper.k * stepper.dt
+        ke_pred = ke0 + T * dke
+        ok = bool(torch.isfinite(us).all()) and float(torch.max(torch.abs(rs / stepper.rho0 - 1.0))) <= rho_tol
+        ok = ok and abs(kinetic_energy(us, m) - ke_pred) <= ke_tol * max(ke0, 1e-30)
+        if ok:
+            x, u, rho = xs, us, rs
+            accepted += 1
+        else:
+            sol.upload({"positions": x, "velocities": u, "densities": rho})
+            sol.step(nseg * stepper.k)
+            sol.check()
+            got = sol.download()
+            x, u, rho = _wrap(got["positions"], cfg), got["velocities"], got["densities"]
+            rejected += 1
+        done += nseg
+    return (x, u, rho), accepted, rejected

@@ -238,6 +238,38 @@ int sph_solver_set_timing(sph_solver_t* s, int32_t enabled);
 int sph_solver_kernel_times(sph_solver_t* s, float* ms_host, int32_t* launches_host,
                             sph_stream_t stream);
 
+/* ------------------------------------------------------------------------------------
+ * Learned continuous-convolution step (no reference implementation: the network is a
+ * stand-in for 4 solver steps). One layer is E = aggregate(h) followed by the basis-weight
+ * contraction y = E W on the tensor cores.
+ * ------------------------------------------------------------------------------------ */
+
+/* D[M x N] (fp32, row-major, leading dimension ldd) = A[M x K] * Bt[N x K]^T, or += when
+ * accumulate != 0. A and Bt are row-major bf16 (leading dimensions lda, ldb in elements).
+ * tcgen05 MMA (BF16 inputs, FP32 accumulation in tensor memory) fed by TMA. Requires
+ * M % 128 == 0, N % 64 == 0, K % 64 == 0, 16-byte aligned pointers, lda, ldb multiples of
+ * 8 and ldd a multiple of 4. A wait that does not complete sets a bit in *err (device
+ * word, caller-cleared) instead of hanging. */
+int sph_gemm_bf16_tn(const void* A, const void* Bt, float* D, int64_t M, int64_t N, int64_t K,
+                     int64_t lda, int64_t ldb, int64_t ldd, int32_t accumulate, uint32_t* err,
+                     sph_stream_t stream);
+
+/* E_i[b C + c] = inv_norm * sum_j phi_b(x_i - x_j) h_j[c] over the CSR neighbor rows
+ * (offsets[n+1] int64, neighbors int32, e.g. the exact lists of sph_neighbor_fill), with
+ * the 64 basis functions phi_{8a+m} = (1-q^2)^2 T_a(2q-1) F_m(angle), q = |x| / support.
+ * relative != 0 aggregates h_j[c] - h_i[c] instead (the difference form of SPH operators).
+ * h: bf16 [n][C], E: bf16 [n][64 C], C in {16, 32, 64}. */
+int sph_cconv_aggregate(const float* x, int64_t n, const int64_t* offsets, const int32_t* neighbors,
+                        const sph_domain_t* domain, double support, double inv_norm, const void* h,
+                        int32_t channels, int32_t relative, void* E, sph_stream_t stream);
+
+/* Transpose of sph_cconv_aggregate (for the backward pass, symmetric neighbor relation):
+ * dh_j[c] = inv_norm * sum_{i in N(j)} sum_b phi_b(x_i - x_j) dE_i[b C + c]; dE fp32 rows of
+ * leading dimension ldE, dh fp32 [n][C]. */
+int sph_cconv_aggregate_t(const float* x, int64_t n, const int64_t* offsets, const int32_t* neighbors,
+                          const sph_domain_t* domain, double support, double inv_norm, const float* dE,
+                          int64_t ldE, int32_t channels, int32_t relative, float* dh, sph_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

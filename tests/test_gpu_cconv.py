@@ -1,0 +1,174 @@
+"""Learned continuous-convolution path: kernels against the CPU oracle and the trained gain.
+
+* tcgen05 GEMM: against an FP32 matmul of the same BF16 operands, relative error <= 1e-5
+  of the output's magnitude (only the FP32 summation order differs).
+* aggregation: against the oracle's float64 sums of the same BF16 features; the kernel
+  rounds E to BF16, so |gpu - oracle| <= 2^-8 |oracle| + 1e-5 max|oracle|.
+* transposed aggregation (FP32 in and out): <= 1e-5 of the magnitude.
+* layer gradients dW and dh: against the oracle's backward with the same BF16 roundings,
+  relative L2 error <= 1e-4.
+* gain: a network trained here (3000 Adam iterations on 8 small solver trajectories)
+  predicts 4 solver steps better than the method without it (persistence, or one plain
+  step of 4 dt), for the velocity and the density increments.
+"""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+from oracle import cconv_oracle as CO  # noqa: E402
+from diffsph_gb300 import scenes  # noqa: E402
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _lib_built():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from diffsph_gb300 import _lib
+    _lib.load()
+
+
+def _np(t):
+    return t.detach().float().cpu().numpy()
+
+
+@pytest.mark.parametrize("M,N,K", [(128, 64, 64), (256, 64, 1024), (384, 128, 4096), (128, 256, 192),
+                                   (1024, 4096, 64), (4096, 64, 1024)])
+def test_gemm_matches_fp32_matmul(M, N, K):
+    from diffsph_gb300.learned import check_device_errors, gemm_tn
+    g = torch.Generator(device="cuda").manual_seed(M + N + K)
+    A = torch.randn(M, K, device="cuda", generator=g).to(torch.bfloat16)
+    Bt = torch.randn(N, K, device="cuda", generator=g).to(torch.bfloat16)
+    D = gemm_tn(A, Bt)
+    ref = A.float() @ Bt.float().t()
+    torch.cuda.synchronize()
+    check_device_errors()
+    err = float((D - ref).abs().max())
+    assert err <= 1e-5 * float(ref.abs().max()) + 1e-6, err
+    # accumulate into an existing output
+    D2 = gemm_tn(A, Bt, out=D.clone(), accumulate=True)
+    assert float((D2 - 2 * ref).abs().max()) <= 2e-5 * float(ref.abs().max()) + 1e-6
+
+
+def test_gemm_strided_operands():
+    from diffsph_gb300.learned import gemm_tn
+    A_full = torch.randn(256, 192, device="cuda").to(torch.bfloat16)
+    Bt_full = torch.randn(64, 256, device="cuda").to(torch.bfloat16)
+    A, Bt = A_full[:, :128], Bt_full[:, 64:192]
+    D = gemm_tn(A, Bt)
+    ref = A.float() @ Bt.float().t()
+    assert float((D - ref).abs().max()) <= 1e-5 * float(ref.abs().max())
+
+
+def test_gemm_rejects_bad_shapes():
+    from diffsph_gb300 import _lib
+    from diffsph_gb300.learned import gemm_tn
+    A = torch.zeros(100, 64, device="cuda", dtype=torch.bfloat16)
+    Bt = torch.zeros(64, 64, device="cuda", dtype=torch.bfloat16)
+    with pytest.raises(_lib.SphError):
+        gemm_tn(A, Bt)
+
+
+def _graph_case(nx=24, seed=4, C=16):
+    from diffsph_gb300.learned import Graph
+    cfg, st = scenes.fourier_periodic(nx, seed=seed, jitter=0.3)
+    x = torch.as_tensor(st["fluid"]["positions"], device="cuda")
+    g = Graph(x, cfg)
+    rng = np.random.default_rng(seed)
+    h = CO.bf16(rng.standard_normal((g.n, C)).astype(np.float32))
+    dom = {"min": cfg["domain"]["minExtent"], "max": cfg["domain"]["maxExtent"], "periodic": [True, True]}
+    return cfg, g, h, dom
+
+
+@pytest.mark.parametrize("C,rel", [(16, False), (32, False), (64, False), (16, True), (64, True)])
+def test_aggregate_matches_oracle(C, rel):
+    from diffsph_gb300.learned import aggregate
+    cfg, g, h, dom = _graph_case(C=C)
+    E = aggregate(g, torch.as_tensor(h, device="cuda").to(torch.bfloat16), rel)
+    Eo = CO.aggregate(_np(g.x), _np(g.offsets).astype(np.int64), _np(g.nbr).astype(np.int64), dom, g.H, g.inv_norm,
+                      h.astype(np.float64), rel)
+    Eg = _np(E[:g.n]).astype(np.float64)
+    assert np.all(np.abs(Eg - Eo) <= 2.0 ** -8 * np.abs(Eo) + 1e-5 * np.abs(Eo).max())
+    assert float(E[g.n:].abs().max()) == 0.0 if g.npad > g.n else True
+
+
+@pytest.mark.parametrize("C,rel", [(16, False), (64, False), (16, True), (64, True)])
+def test_aggregate_transpose_matches_oracle(C, rel):
+    from diffsph_gb300.learned import aggregate_t
+    cfg, g, _, dom = _graph_case(C=C)
+    rng = np.random.default_rng(7)
+    dE = rng.standard_normal((g.n, 64 * C)).astype(np.float32)
+    dh = aggregate_t(g, torch.as_tensor(dE, device="cuda"), C, rel)
+    ref = CO.aggregate_t(_np(g.x), _np(g.offsets).astype(np.int64), _np(g.nbr).astype(np.int64), dom, g.H,
+                         g.inv_norm, dE.astype(np.float64), C, rel)
+    assert np.max(np.abs(_np(dh) - ref)) <= 1e-5 * np.abs(ref).max()
+
+
+@pytest.mark.parametrize("C,rel", [(64, False), (16, True)])
+def test_layer_gradients_match_oracle(C, rel):
+    from diffsph_gb300.learned import ConvFn
+    cfg, g, h, dom = _graph_case(C=C, nx=20)
+    rng = np.random.default_rng(3)
+    W = (rng.standard_normal((64 * C, 64)) * 0.05).astype(np.float32)
+    G = rng.standard_normal((g.n, 64)).astype(np.float32)
+    ht = torch.as_tensor(h, device="cuda").requires_grad_(True)
+    Wt = torch.as_tensor(W, device="cuda").requires_grad_(True)
+    y = ConvFn.apply(ht, Wt, g, rel)
+    (y * torch.as_tensor(G, device="cuda")).sum().backward()
+    args = (_np(g.x), _np(g.offsets).astype(np.int64), _np(g.nbr).astype(np.int64), dom, g.H, g.inv_norm)
+    yo, Eq = CO.layer_forward(*args, h, W, relative=rel)
+    dho, dWo = CO.layer_backward(*args, Eq, W, G, C, relative=rel)
+
+    def rel(a, b):
+        return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+    # y: FP32 sums of identical BF16 products
+    assert rel(_np(y), yo) < 1e-4
+    assert rel(_np(Wt.grad), dWo) < 1e-4
+    assert rel(_np(ht.grad), dho) < 1e-4
+
+
+def test_trained_network_beats_the_method_without_it():
+    """Trains on 8 solver trajectories of 32^2-particle periodic Fourier flows (24 frames,
+    one every 4 steps) and evaluates on a held-out trajectory: the learned 4-step update
+    must be closer to the solver's 4 steps than persistence (u, rho unchanged) and than one
+    plain step of 4 dt (the solver taking the learned step's time step directly)."""
+    import copy
+
+    from diffsph_gb300.learned import (CConvNet, LearnedStepper, check_device_errors, generate_trajectories,
+                                       train)
+    from diffsph_gb300.solver import Solver
+    k = 4
+    cfg, trajs = generate_trajectories(9, 24, 32, seed=11, k=k)
+    train_set, held = trajs[:8], trajs[8]
+    torch.manual_seed(0)
+    net = CConvNet().cuda()
+    hist = train(net, cfg, train_set, iters=3000, k=k, lr=5e-3)
+    check_device_errors()
+    assert np.mean(hist[-50:]) < 0.5 * np.mean(hist[:50])
+    stepper = LearnedStepper(cfg, net, k)
+    cfg4 = copy.deepcopy(cfg)
+    cfg4["timestep"]["dt"] = k * float(cfg["timestep"]["dt"])
+    e_net, e_pers, e_big, e_rho = [], [], [], []
+    for i in range(len(held) - 1):
+        a, b = held[i], held[i + 1]
+        with torch.no_grad():
+            _, u_net, r_net = stepper.step(*a)
+        e_rho.append(float(torch.linalg.norm(r_net - b[2]) / torch.linalg.norm(b[2] - a[2])))
+        sol = Solver(cfg4, {"positions": a[0], "velocities": a[1], "densities": a[2],
+                            "masses": np.full(a[0].shape[0], float(cfg["particle"]["dx"]) ** 2),
+                            "supports": np.full(a[0].shape[0], float(cfg["particle"]["support"]))})
+        sol.step(1)
+        big = sol.download()
+        du = b[1] - a[1]
+        scale = float(torch.linalg.norm(du))
+        e_net.append(float(torch.linalg.norm(u_net - b[1])) / scale)
+        e_pers.append(float(torch.linalg.norm(a[1] - b[1])) / scale)
+        e_big.append(float(torch.linalg.norm(big["velocities"] - b[1])) / scale)
+    m_net, m_pers, m_big = np.mean(e_net), np.mean(e_pers), np.mean(e_big)
+    print(f"relative velocity-increment error: learned {m_net:.3f}, persistence {m_pers:.3f}, "
+          f"one 4dt step {m_big:.3f}; density increment: learned {np.mean(e_rho):.3f}, persistence 1")
+    assert m_net < m_pers
+    assert m_net < m_big
+    assert np.mean(e_rho) < 0.5
