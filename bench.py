@@ -38,7 +38,11 @@ WORKLOADS = {
     "tgv_64": dict(scene="taylor_green", nx=64),
     # gradient of a rollout loss: 128x128 periodic Fourier flow, 1000 steps, checkpoints every 25
     "adjoint_fourier128": dict(scene="adjoint", nx=128, seed=0, target_seed=1, rollout=1000, every=25),
+    # learned k=4 step: trained at 128x128 (dx = 1/64), evaluated on 32 domains of 256x256 (4x4 box)
+    "learned_fourier_b32": dict(scene="learned", nx_train=128, nx_eval=256, L_eval=4.0, batch=32, k=4, traj=8,
+                                frames=24, iters=3000, rollout=200),
 }
+LEARNED_METRIC = "particle-steps/s (learned k=4 step, counted in plain-step equivalents)"
 ADJOINT_METRIC = "adjoint particle-steps/s (forward + backward of a checkpointed rollout)"
 
 
@@ -149,6 +153,9 @@ def run_reference(args):
     if WORKLOADS[args.workload]["scene"] == "adjoint":
         print(json.dumps({"impl": "reference", "unavailable": "the reference has no adjoint; its gradients "
                           "come from torch autograd through its own package, which is not installed here"}))
+        return
+    if WORKLOADS[args.workload]["scene"] == "learned":
+        print(json.dumps({"impl": "reference", "unavailable": "the reference has no learned model"}))
         return
     from oracle import sph_oracle as O
     from diffsph_gb300 import scenes
@@ -432,6 +439,102 @@ def run_adjoint(args):
     print(json.dumps(line))
 
 
+def run_learned(args):
+    """Learned k=4 step against k plain steps on the same packed batch of periodic domains.
+    value: particles x k / learned-step time (the state resident on the device); the plain
+    batched solver's particle-steps/s on the same batch is reported beside it, with the
+    velocity error of a learned rollout against the plain rollout and the judge's counts."""
+    import numpy as np
+    import torch
+    import __graft_entry__ as ge
+    from diffsph_gb300 import scenes
+    from diffsph_gb300.learned import (CConvNet, LearnedStepper, check_device_errors, generate_trajectories,
+                                       judged_rollout, train)
+    from diffsph_gb300.solver import BatchSolver, Solver
+
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    if int(os.environ.get("RANK", "0")) != 0:
+        return
+    ge.build()
+    w = WORKLOADS[args.workload]
+    k = w["k"]
+    t0 = time.perf_counter()
+    cfg_t, trajs = generate_trajectories(w["traj"], w["frames"], w["nx_train"], seed=0, k=k)
+    torch.manual_seed(0)
+    net = CConvNet(seed=0).cuda()
+    hist = train(net, cfg_t, trajs, iters=w["iters"], k=k, lr=5e-3)
+    torch.cuda.synchronize()
+    t_train = time.perf_counter() - t0
+    net.eval()
+    doms = [scenes.fourier_periodic(w["nx_eval"], seed=1000 + d, jitter=0.1, L=w["L_eval"]) for d in range(w["batch"])]
+    cfg = doms[0][0]
+    fl = {key: torch.cat([torch.as_tensor(st["fluid"][key]) for _, st in doms]).cuda()
+          for key in ("positions", "velocities", "densities")}
+    n = fl["positions"].shape[0]
+    stepper = LearnedStepper(cfg, net, k, n_domains=w["batch"])
+    stream = torch.cuda.Stream()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    with torch.cuda.stream(stream):
+        x, u, r = fl["positions"], fl["velocities"], fl["densities"]
+        for _ in range(max(args.warmup, 3)):
+            x, u, r = stepper.step(x, u, r)
+        torch.cuda.synchronize()
+        with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
+            ev[0].record(stream)
+            for _ in range(args.steps):
+                x, u, r = stepper.step(x, u, r)
+            ev[1].record(stream)
+            torch.cuda.synchronize()
+        check_device_errors()
+        ms_learned = ev[0].elapsed_time(ev[1]) / args.steps
+        bsol = BatchSolver([c for c, _ in doms], [st["fluid"] for _, st in doms])
+        bsol.autotune()
+        for _ in range(max(args.warmup, 3)):
+            bsol.step(1)
+        bsol.graph_step(2)
+        torch.cuda.synchronize()
+        ev[2].record(stream)
+        nplain = 2 * args.steps * k // 2
+        for _ in range(nplain // 2):
+            bsol.graph_step(2)
+        ev[3].record(stream)
+        torch.cuda.synchronize()
+        bsol.check()
+        ms_plain = ev[2].elapsed_time(ev[3]) / nplain
+        # accuracy on one domain: learned rollout vs the plain rollout of the same length
+        c0, s0 = doms[0]
+        sol = Solver(c0, s0["fluid"])
+        sol.step(w["rollout"])
+        sol.check()
+        ref = sol.download()
+        one = LearnedStepper(c0, net, k)
+        xo = torch.as_tensor(s0["fluid"]["positions"]).cuda()
+        uo = torch.as_tensor(s0["fluid"]["velocities"]).cuda()
+        ro = torch.as_tensor(s0["fluid"]["densities"]).cuda()
+        for _ in range(w["rollout"] // k):
+            xo, uo, ro = one.step(xo, uo, ro)
+        err = float(torch.linalg.norm(uo - ref["velocities"]) / torch.linalg.norm(ref["velocities"]))
+        rho_dev = float(torch.max(torch.abs(ro - 1.0)))
+        (_, uj, _), acc, rej = judged_rollout(one, s0["fluid"], w["rollout"] // k, segment=5)
+        err_j = float(torch.linalg.norm(uj - ref["velocities"]) / torch.linalg.norm(ref["velocities"]))
+    line = {
+        "metric": LEARNED_METRIC, "value": n * k / (ms_learned / 1e3), "unit": "particle-steps/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": ms_learned, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "bf16 (fp32 accumulate)", "data": "synthetic",
+        "config": {"workload": args.workload, "particles": n, "domains": w["batch"], "k": k,
+                   "plain_ms_per_step": ms_plain, "plain_particle_steps_per_s": n / (ms_plain / 1e3),
+                   "learned_over_plain_simulated_time": (k * ms_plain) / ms_learned,
+                   "train": {"trajectories": w["traj"], "frames": w["frames"], "particles": w["nx_train"] ** 2,
+                             "iters": w["iters"], "seconds": round(t_train, 1),
+                             "loss_first100": float(np.mean(hist[:100])), "loss_last100": float(np.mean(hist[-100:]))},
+                   "rollout_steps": w["rollout"], "velocity_rel_l2_vs_plain": err, "max_density_dev": rho_dev,
+                   "judged": {"segments_accepted": acc, "segments_rejected": rej, "velocity_rel_l2_vs_plain": err_j},
+                   "l2": "inputs (2.1 M particles) exceed L2"},
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -446,6 +549,8 @@ def main():
         run_reference(args)
     elif WORKLOADS[args.workload]["scene"] == "adjoint":
         run_adjoint(args)
+    elif WORKLOADS[args.workload]["scene"] == "learned":
+        run_learned(args)
     else:
         run_ours(args)
 

@@ -160,14 +160,24 @@ def fourier_velocity(x, rng, modes: int = 16, kmax: int = 4, L: float = 2.0):
     return vel
 
 
-def fourier_periodic(nx: int = 128, seed: int = 0, jitter: float = 0.1, dtype=np.float32):
-    """Periodic domain with a random divergence-free Fourier-mode initial field."""
+def fourier_periodic(nx: int = 128, seed: int = 0, jitter: float = 0.1, dtype=np.float32, L: float = 2.0):
+    """Periodic square [-L/2, L/2]^2 of nx*nx particles (dx = L / nx) with a random
+    divergence-free Fourier-mode initial field; the Taylor-Green parameters otherwise."""
     cfg, st = taylor_green(nx, 0.0, seed, dtype)
     rng = np.random.default_rng(seed)
+    if L != 2.0:
+        dx = L / nx
+        cfg = _base_config(dx, 1.0, 10.0, (-L / 2, -L / 2), (L / 2, L / 2), True)
+        cfg["diffusion"] = {"velocityScheme": "deltaSPH_viscid", "nu": 0.01, "alpha": 0.01,
+                            "eps": 1e-6, "delta": 0.1, "densityScheme": "deltaSPH", "pi-switch": False}
+        cfg["boundaryDiffusion"] = dict(cfg["diffusion"])
+        n = nx * nx
+        st = {"fluid": {"masses": np.full(n, dx * dx, dtype), "supports": np.full(n, cfg["particle"]["support"], dtype),
+                        "areas": np.full(n, dx * dx, dtype)}}
     dx = cfg["particle"]["dx"]
-    x = _lattice(-1.0, 1.0, -1.0, 1.0, dx, np.float64)
+    x = _lattice(-L / 2, L / 2, -L / 2, L / 2, dx, np.float64)
     x = x + rng.uniform(-jitter * dx, jitter * dx, size=x.shape)
-    u = fourier_velocity(x, rng)
+    u = fourier_velocity(x, rng, L=L)
     st["fluid"]["positions"] = x.astype(dtype)
     st["fluid"]["velocities"] = u.astype(dtype)
     st["fluid"]["densities"] = np.full(x.shape[0], cfg["fluid"]["rho0"], dtype)

@@ -172,3 +172,29 @@ def test_trained_network_beats_the_method_without_it():
     assert m_net < m_pers
     assert m_net < m_big
     assert np.mean(e_rho) < 0.5
+
+
+@pytest.mark.parametrize("bad", ["density", "velocity"])
+def test_judge_rejects_a_bad_network_and_falls_back_to_the_solver(bad):
+    """A network whose output is biased breaks the density bound (+0.05 rho0 per learned
+    step) or the kinetic-energy bound (+0.2 on every velocity): every segment is rejected
+    and re-run by the solver, so the rollout equals the plain solver's (up to the summation
+    order of the re-sorted restarts)."""
+    from diffsph_gb300.learned import CConvNet, LearnedStepper, judged_rollout
+    from diffsph_gb300.solver import Solver
+    cfg, st = scenes.fourier_periodic(32, seed=21, jitter=0.1)
+    net = CConvNet(seed=5).cuda()
+    with torch.no_grad():
+        net.dec2.weight.zero_()
+        if bad == "density":
+            net.dec2.bias[2] = 0.05
+        else:
+            net.dec2.bias[0:2] = 0.2
+    stepper = LearnedStepper(cfg, net, 4)
+    (x, u, r), acc, rej = judged_rollout(stepper, st["fluid"], 6, segment=2)
+    assert acc == 0 and rej == 3
+    sol = Solver(cfg, st["fluid"])
+    sol.step(24)
+    ref = sol.download()
+    assert float(torch.linalg.norm(u - ref["velocities"]) / torch.linalg.norm(ref["velocities"])) < 1e-5
+    assert float(torch.max(torch.abs(r - ref["densities"]))) < 1e-5
