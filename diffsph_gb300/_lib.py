@@ -56,7 +56,8 @@ EXPORTS = [
     "sph_solver_set_timing", "sph_solver_kernel_times", "sph_solver_autotune", "sph_solver_shapes",
     "sph_solver_set_shape", "sph_batch_workspace_bytes", "sph_batch_create", "sph_solver_graph_step",
     "sph_neighbor_count_static", "sph_solver_vjp_rates", "sph_solver_vjp_gradient", "sph_solver_vjp_shift",
-    "sph_gemm_bf16_tn", "sph_cconv_aggregate", "sph_cconv_aggregate_t",
+    "sph_gemm_bf16_tn", "sph_cconv_aggregate", "sph_cconv_aggregate_t", "sph_cconv_aggregate_tc",
+    "sph_neighbor_fill_csr",
 ]
 
 _lib = None
@@ -88,8 +89,11 @@ def load(build_if_missing: bool = False):
         "sph_gemm_bf16_tn": ([P, P, P, I64, I64, I64, I64, I64, I64, I32, P, P], ctypes.c_int),
         "sph_cconv_aggregate": ([P, I64, P, P, DP, ctypes.c_double, ctypes.c_double, P, I32, I32, P, P],
                                 ctypes.c_int),
+        "sph_cconv_aggregate_tc": ([P, I64, P, P, DP, ctypes.c_double, ctypes.c_double, P, I32, I32, P, P, P],
+                                   ctypes.c_int),
         "sph_cconv_aggregate_t": ([P, I64, P, P, DP, ctypes.c_double, ctypes.c_double, P, I64, I32, I32, P, P],
                                   ctypes.c_int),
+        "sph_neighbor_fill_csr": ([P, I64, P, P, I64, DP, ctypes.c_double, P, SZ, P, P, P], ctypes.c_int),
         "sph_neighbor_count_static": ([P, I64, P, P, I64, DP, ctypes.c_double, P, P, P], ctypes.c_int),
         "sph_solver_workspace_bytes": ([PP, I64, I64, ctypes.POINTER(SZ)], ctypes.c_int),
         "sph_solver_create": ([PP, I64, I64, P, SZ, ctypes.POINTER(P)], ctypes.c_int),

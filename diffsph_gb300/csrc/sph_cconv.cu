@@ -190,7 +190,8 @@ __global__ void __launch_bounds__(kThreads, 1)
         mma_commit(&done);  // arrives once every MMA issued above has completed
     }
     __syncwarp();
-    const bool ready = mbar_wait(&done, 0);
+    // warp-uniform so that the .sync.aligned TMEM loads below run converged
+    const bool ready = __all_sync(0xffffffffu, mbar_wait(&done, 0));
     if (!ready && lane == 0) atomicOr(err, 4u);
     asm volatile("tcgen05.fence::after_thread_sync;");
     if (ready) {
@@ -321,6 +322,212 @@ __global__ void __launch_bounds__(kAggThreads) k_aggregate(int64_t n, const floa
     __nv_bfloat16* Ei = E + i * (kBasis * C);
 #pragma unroll
     for (int k = 0; k < kPer; ++k) Ei[(b0 + k * kStride) * C + c] = __float2bfloat16_rn(acc[k] * inv_norm);
+}
+
+// ------------------------------------------------------------------------------------
+// Aggregation on the tensor cores. Per particle, E_i = Phi_i^T G_i with Phi_i [edges x 64]
+// the basis values and G_i [edges x C] the neighbor features (or their differences to h_i in
+// the relative form), edges zero-padded to 64. Two particles share one M = 128 MMA group in
+// block-diagonal form: K atom 0 holds particle A (rows 0..63 of the A tile = Phi_A^T, rows
+// 64..127 zero) and K atom 1 particle B (rows 0..63 zero, rows 64..127 = Phi_B^T); the B
+// tile holds G_A^T and G_B^T in the two atoms. The accumulator rows 0..63 are then E_A and
+// rows 64..127 E_B, drained by warps 0-1 and 2-3. Operands are K-major with the 128-byte
+// swizzle; the zero quadrants are written once. One stage of 48 KB (C = 64) lets four CTAs
+// share an SM, which hides the gather latency of one another's operand builds.
+// ------------------------------------------------------------------------------------
+constexpr int kTcMaxEdges = 64;             // neighbors per particle (row), self included
+constexpr int kTcPairsPerCta = 32;          // 64 particles per CTA
+constexpr uint32_t kTcAtomA = 128u * 128u;  // 128 rows x 64 bf16
+
+template <int C>
+struct TcCfg {
+    static constexpr uint32_t kAtomB = C * 128u;
+    static constexpr uint32_t kTileA = 2 * kTcAtomA;
+    static constexpr uint32_t kTileB = 2 * kAtomB;
+    static constexpr size_t kSmem = static_cast<size_t>(kTileA + kTileB) + 1024;
+    static constexpr int kCols = C < 32 ? 32 : C;
+};
+
+// byte offset of element (row r, column k) in a K-major atom of 64 bf16 columns with the
+// 128-byte swizzle (16-byte chunk index XOR row mod 8), as TMA writes it
+__device__ __forceinline__ uint32_t sw128_off(int r, int k) {
+    return static_cast<uint32_t>(r) * 128u +
+           ((((static_cast<uint32_t>(k) >> 3) ^ (static_cast<uint32_t>(r) & 7u))) << 4) +
+           (static_cast<uint32_t>(k) & 7u) * 2u;
+}
+
+__device__ __forceinline__ uint32_t pack_bf16x2(float a, float b) {
+    __nv_bfloat162 v = __floats2bfloat162_rn(a, b);
+    return *reinterpret_cast<uint32_t*>(&v);
+}
+
+template <int C, bool REL>
+__global__ void __launch_bounds__(128, 4)
+    k_aggregate_tc(int64_t n, const float* __restrict__ x, const int64_t* __restrict__ off,
+                   const int32_t* __restrict__ nbr, BasisGeo bg, float inv_norm,
+                   const __nv_bfloat16* __restrict__ h, __nv_bfloat16* __restrict__ E, uint32_t* __restrict__ err) {
+    using Cf = TcCfg<C>;
+    extern __shared__ uint8_t dsm[];
+    __shared__ uint64_t mma_done;
+    __shared__ uint32_t tmem_slot;
+    uint8_t* tiles = dsm + ((1024u - (smem_u32(dsm) & 1023u)) & 1023u);
+    uint8_t* A = tiles;
+    uint8_t* B = tiles + Cf::kTileA;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int64_t q0 = static_cast<int64_t>(blockIdx.x) * (2 * kTcPairsPerCta);
+    for (uint32_t o = static_cast<uint32_t>(tid) * 16u; o < Cf::kTileA + Cf::kTileB; o += 128u * 16u)
+        *reinterpret_cast<uint4*>(tiles + o) = make_uint4(0u, 0u, 0u, 0u);
+    if (tid == 0) {
+        mbar_init(&mma_done, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_slot)),
+                     "r"(Cf::kCols));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    const uint32_t tmem = tmem_slot;
+    constexpr uint32_t idesc = idesc_bf16(128, C);
+    for (int it = 0; it < kTcPairsPerCta; ++it) {
+        const int64_t ia = q0 + 2 * it;
+        if (ia >= n) break;  // uniform across the CTA
+        // one thread per (particle p, edge e): the 64 basis values go to rows 64 p + b of A atom
+        // p and the neighbor's C features to rows c of B atom p, both at column e; lanes of a
+        // warp hold consecutive edges, so every store hits distinct banks
+        {
+            const int p = tid >> 6, e = tid & 63;
+            const int64_t i = ia + p;
+            int ne = 0;
+            int64_t e0 = 0;
+            if (i < n) {
+                e0 = off[i];
+                ne = static_cast<int>(off[i + 1] - e0);
+                if (ne > kTcMaxEdges) {
+                    if (e == 0) atomicOr(err, 8u);
+                    ne = kTcMaxEdges;
+                }
+            }
+            const bool valid = e < ne;
+            const int64_t j = valid ? static_cast<int64_t>(nbr[e0 + e]) : 0;
+            float x0 = 0.f, x1 = 0.f;
+            if (valid)
+                pair_vec<true>(make_float2(x[2 * i], x[2 * i + 1]), make_float2(x[2 * j], x[2 * j + 1]), bg.geo, x0,
+                               x1);
+            // basis: w(q) T_a(2q - 1) F_m(z), z = x / (|x| + eps)
+            const float r = sqrtf(x0 * x0 + x1 * x1);
+            const float q = fminf(r * bg.inv_H, 1.f);
+            const float om = 1.f - q * q;
+            const float w = valid ? om * om : 0.f;
+            const float sc = 2.f * q - 1.f;
+            const float inv = 1.f / (r + bg.eps);
+            const float zr = x0 * inv, zi = x1 * inv;
+            const float z2r = zr * zr - zi * zi, z2i = 2.f * zr * zi;
+            const float z3r = z2r * zr - z2i * zi, z3i = z2r * zi + z2i * zr;
+            const float z4r = z3r * zr - z3i * zi;
+            uint8_t* atomA = A + p * kTcAtomA;
+            float tm1 = 1.f, t0 = sc;
+#pragma unroll
+            for (int a = 0; a < 8; ++a) {
+                float ta;
+                if (a == 0) {
+                    ta = 1.f;
+                } else if (a == 1) {
+                    ta = sc;
+                } else {
+                    ta = 2.f * sc * t0 - tm1;
+                    tm1 = t0;
+                    t0 = ta;
+                }
+                const float R = w * ta;
+                const int row = 64 * p + 8 * a;
+                __nv_bfloat16* const bp = reinterpret_cast<__nv_bfloat16*>(atomA);
+                bp[sw128_off(row + 0, e) >> 1] = __float2bfloat16_rn(R);
+                bp[sw128_off(row + 1, e) >> 1] = __float2bfloat16_rn(R * zr);
+                bp[sw128_off(row + 2, e) >> 1] = __float2bfloat16_rn(R * zi);
+                bp[sw128_off(row + 3, e) >> 1] = __float2bfloat16_rn(R * z2r);
+                bp[sw128_off(row + 4, e) >> 1] = __float2bfloat16_rn(R * z2i);
+                bp[sw128_off(row + 5, e) >> 1] = __float2bfloat16_rn(R * z3r);
+                bp[sw128_off(row + 6, e) >> 1] = __float2bfloat16_rn(R * z3i);
+                bp[sw128_off(row + 7, e) >> 1] = __float2bfloat16_rn(R * z4r);
+            }
+            __nv_bfloat16* const bq = reinterpret_cast<__nv_bfloat16*>(B + p * Cf::kAtomB);
+            const uint4* hj = reinterpret_cast<const uint4*>(h + j * C);
+            const uint4* hi = reinterpret_cast<const uint4*>(h + (i < n ? i : 0) * C);
+#pragma unroll
+            for (int c8 = 0; c8 < C / 8; ++c8) {
+                uint4 vj = valid ? hj[c8] : make_uint4(0u, 0u, 0u, 0u);
+                const __nv_bfloat162* pj = reinterpret_cast<const __nv_bfloat162*>(&vj);
+                float f[8];
+#pragma unroll
+                for (int t = 0; t < 4; ++t) {
+                    const float2 g = __bfloat1622float2(pj[t]);
+                    f[2 * t] = g.x;
+                    f[2 * t + 1] = g.y;
+                }
+                if (REL && valid) {
+                    uint4 vi = hi[c8];
+                    const __nv_bfloat162* pi2 = reinterpret_cast<const __nv_bfloat162*>(&vi);
+#pragma unroll
+                    for (int t = 0; t < 4; ++t) {
+                        const float2 g = __bfloat1622float2(pi2[t]);
+                        f[2 * t] -= g.x;
+                        f[2 * t + 1] -= g.y;
+                    }
+                }
+#pragma unroll
+                for (int t = 0; t < 8; ++t) bq[sw128_off(8 * c8 + t, e) >> 1] = __float2bfloat16_rn(f[t]);
+            }
+        }
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // generic writes -> tensor core
+        __syncthreads();
+        if (tid == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;");
+#pragma unroll
+            for (int at = 0; at < 2; ++at) {
+                const uint64_t da = sw128_desc(smem_u32(A + at * kTcAtomA));
+                const uint64_t db = sw128_desc(smem_u32(B + at * Cf::kAtomB));
+#pragma unroll
+                for (int kk = 0; kk < 4; ++kk)
+                    mma_bf16(tmem, da + 2 * kk, db + 2 * kk, idesc, (at > 0 || kk > 0) ? 1u : 0u);
+            }
+            mma_commit(&mma_done);
+        }
+        __syncwarp();
+        const bool ok = __all_sync(0xffffffffu, mbar_wait(&mma_done, static_cast<uint32_t>(it) & 1u));
+        if (!ok && lane == 0) atomicOr(err, 16u);
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        const int p = warp >> 1;  // warps 0-1: particle A (rows 0..63), 2-3: particle B
+        const int64_t i = ia + p;
+        if (ok && i < n) {
+            const int b = (warp & 1) * 32 + lane;
+            __nv_bfloat16* dst = E + i * (64 * C) + b * C;
+#pragma unroll 1
+            for (int c = 0; c < C; c += 16) {
+                uint32_t v[16];
+                tmem_ld16(tmem + (static_cast<uint32_t>(warp * 32) << 16) + static_cast<uint32_t>(c), v);
+                uint4 o0, o1;
+                o0.x = pack_bf16x2(__uint_as_float(v[0]) * inv_norm, __uint_as_float(v[1]) * inv_norm);
+                o0.y = pack_bf16x2(__uint_as_float(v[2]) * inv_norm, __uint_as_float(v[3]) * inv_norm);
+                o0.z = pack_bf16x2(__uint_as_float(v[4]) * inv_norm, __uint_as_float(v[5]) * inv_norm);
+                o0.w = pack_bf16x2(__uint_as_float(v[6]) * inv_norm, __uint_as_float(v[7]) * inv_norm);
+                o1.x = pack_bf16x2(__uint_as_float(v[8]) * inv_norm, __uint_as_float(v[9]) * inv_norm);
+                o1.y = pack_bf16x2(__uint_as_float(v[10]) * inv_norm, __uint_as_float(v[11]) * inv_norm);
+                o1.z = pack_bf16x2(__uint_as_float(v[12]) * inv_norm, __uint_as_float(v[13]) * inv_norm);
+                o1.w = pack_bf16x2(__uint_as_float(v[14]) * inv_norm, __uint_as_float(v[15]) * inv_norm);
+                *reinterpret_cast<uint4*>(dst + c) = o0;
+                *reinterpret_cast<uint4*>(dst + c + 8) = o1;
+            }
+        }
+        asm volatile("tcgen05.fence::before_thread_sync;");
+        __syncthreads();
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(Cf::kCols));
 }
 
 // dh_j[c] = inv_norm * sum_{i in N(j)} sum_b phi_b(x_i - x_j) dE_i[b C + c]; the relative
@@ -514,4 +721,43 @@ extern "C" int sph_cconv_aggregate_t(const float* x, int64_t n, const int64_t* o
     }
 #undef SPH_AGGT
     return cudaGetLastError() == cudaSuccess ? SPH_OK : SPH_ERR_CUDA;
+}
+
+template <int C, bool REL>
+static int launch_agg_tc(int64_t n, const float* x, const int64_t* off, const int32_t* nbr, const BasisGeo& bg,
+                         float nz, const __nv_bfloat16* h, __nv_bfloat16* E, uint32_t* err, cudaStream_t s) {
+    static std::once_flag once;
+    static cudaError_t attr = cudaSuccess;
+    std::call_once(once, [] {
+        attr = cudaFuncSetAttribute(k_aggregate_tc<C, REL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    static_cast<int>(TcCfg<C>::kSmem));
+    });
+    if (attr != cudaSuccess) return SPH_ERR_CUDA;
+    const unsigned grid = static_cast<unsigned>((n + 2 * kTcPairsPerCta - 1) / (2 * kTcPairsPerCta));
+    k_aggregate_tc<C, REL><<<grid, 128, TcCfg<C>::kSmem, s>>>(n, x, off, nbr, bg, nz, h, E, err);
+    return cudaGetLastError() == cudaSuccess ? SPH_OK : SPH_ERR_CUDA;
+}
+
+extern "C" int sph_cconv_aggregate_tc(const float* x, int64_t n, const int64_t* offsets, const int32_t* neighbors,
+                                      const sph_domain_t* domain, double support, double inv_norm, const void* h,
+                                      int32_t channels, int32_t relative, void* E, uint32_t* err,
+                                      sph_stream_t stream) {
+    int rc = check_agg(n, x, offsets, domain, support, channels);
+    if (rc) return rc;
+    if (n == 0) return SPH_OK;
+    if (!h || !E || !neighbors || !err) return SPH_ERR_ARGUMENT;
+    if ((reinterpret_cast<uintptr_t>(E) | reinterpret_cast<uintptr_t>(h)) & 15) return SPH_ERR_ARGUMENT;
+    BasisGeo bg = make_basis_geo(domain, support);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const auto* hb = static_cast<const __nv_bfloat16*>(h);
+    auto* Eb = static_cast<__nv_bfloat16*>(E);
+    const float nz = static_cast<float>(inv_norm);
+    if (channels == 16)
+        return relative ? launch_agg_tc<16, true>(n, x, offsets, neighbors, bg, nz, hb, Eb, err, s)
+                        : launch_agg_tc<16, false>(n, x, offsets, neighbors, bg, nz, hb, Eb, err, s);
+    if (channels == 32)
+        return relative ? launch_agg_tc<32, true>(n, x, offsets, neighbors, bg, nz, hb, Eb, err, s)
+                        : launch_agg_tc<32, false>(n, x, offsets, neighbors, bg, nz, hb, Eb, err, s);
+    return relative ? launch_agg_tc<64, true>(n, x, offsets, neighbors, bg, nz, hb, Eb, err, s)
+                    : launch_agg_tc<64, false>(n, x, offsets, neighbors, bg, nz, hb, Eb, err, s);
 }

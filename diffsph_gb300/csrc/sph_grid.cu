@@ -329,6 +329,37 @@ __global__ void k_nb_query(int64_t nq, const float2* __restrict__ qxy, const flo
     }
 }
 
+// CSR only: original reference indices of each query's exact neighbors, in cell order
+__global__ void k_nb_csr(int64_t nq, const float2* __restrict__ qxy, const float2* __restrict__ rxy,
+                         const float* __restrict__ rh, const int32_t* __restrict__ ridx,
+                         const int32_t* __restrict__ start, Grid g, Geo geo, const int64_t* __restrict__ offsets,
+                         int32_t* __restrict__ nbr) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nq) return;
+    float2 p = qxy[i];
+    int cx = cell_coord(p.x, g.mn[0], g.inv_cell[0], g.nc[0]);
+    int cy = cell_coord(p.y, g.mn[1], g.inv_cell[1], g.nc[1]);
+    int rows[kMaxRows], lo[2], hi[2];
+    int nr = stencil_rows(cy, g, rows);
+    int ncr = stencil_cols(cx, g, lo, hi);
+    int64_t w = offsets[i];
+    const int64_t wend = offsets[i + 1];
+    for (int a = 0; a < nr; ++a) {
+        for (int b = 0; b < ncr; ++b) {
+            int c0 = rows[a] * g.nc[0] + lo[b], c1 = rows[a] * g.nc[0] + hi[b];
+            int s0 = start[c0], s1 = start[c1 + 1];
+            for (int s = s0; s < s1; ++s) {
+                float x0, x1;
+                pair_vec<true>(p, rxy[s], geo, x0, x1);
+                float r, q;
+                if (!exact_in(sq_norm_ref(x0, x1), rh[s], r, q)) continue;
+                if (w < wend) nbr[w] = ridx[s];
+                ++w;
+            }
+        }
+    }
+}
+
 __global__ void k_pair_kernels(int64_t np, const float* __restrict__ q, const float* __restrict__ xh,
                                const float* __restrict__ h, float* __restrict__ W, float* __restrict__ G) {
     int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -411,6 +442,23 @@ extern "C" int sph_neighbor_fill(const float* x_query, int64_t n_query, const fl
     if ((kernels || gradients) && n_pairs > 0)
         k_pair_kernels<<<(unsigned)((n_pairs + kBlock - 1) / kBlock), kBlock, 0, s>>>(n_pairs, q, xhat, h_pair,
                                                                                        kernels, gradients);
+    return cudaGetLastError() == cudaSuccess ? SPH_OK : SPH_ERR_CUDA;
+}
+
+extern "C" int sph_neighbor_fill_csr(const float* x_query, int64_t n_query, const float* x_ref, const float* h_ref,
+                                     int64_t n_ref, const sph_domain_t* domain, double max_support, void* workspace,
+                                     size_t workspace_bytes, const int64_t* offsets, int32_t* neighbors,
+                                     sph_stream_t stream) {
+    cudaStream_t s = (cudaStream_t)stream;
+    NbWork w;
+    size_t need;
+    int st = nb_layout(n_query, n_ref, domain, max_support, workspace, &w, &need);
+    if (st) return st;
+    if (!workspace || workspace_bytes < need) return SPH_ERR_WORKSPACE;
+    if (!offsets || (n_query > 0 && !neighbors)) return SPH_ERR_ARGUMENT;
+    if (n_query > 0)
+        k_nb_csr<<<(unsigned)((n_query + kBlock - 1) / kBlock), kBlock, 0, s>>>(
+            n_query, w.qry_xy, w.ref_xy, w.ref_h, w.ref_idx, w.start, w.grid, w.geo, offsets, neighbors);
     return cudaGetLastError() == cudaSuccess ? SPH_OK : SPH_ERR_CUDA;
 }
 

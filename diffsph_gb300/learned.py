@@ -18,9 +18,10 @@ Architecture (rotation-aware continuous convolution):
                 by the spread of the training targets
     update      u' = u + du,  rho' = rho + drho,  x' = x + k dt (u + u') / 2 + dx
 
-The aggregation and its transpose run on the CUDA cores; the basis-weight contraction and
-both of its backward products (dE = dy W^T, dW = E^T dy) run on the tcgen05 BF16 GEMM
-(FP32 accumulation). Weights are kept in FP32 and rounded to BF16 for every product.
+The aggregation runs on the tensor cores (per particle E_i = Phi_i^T G_i, a tcgen05 MMA);
+its transpose (backward) on the CUDA cores; the basis-weight contraction and both of its
+backward products (dE = dy W^T, dW = E^T dy) run on the tcgen05 BF16 GEMM (FP32
+accumulation). Weights are kept in FP32 and rounded to BF16 for every product.
 
 ``judged_rollout`` keeps the plain solver as fallback and judge: each segment of learned
 steps is checked against the solver's own kinetic-energy rate (one right-hand side at the
@@ -62,12 +63,13 @@ def _err_word(device):
 
 
 def check_device_errors():
-    """Raise if a tcgen05 GEMM recorded a wait that did not complete (synchronises)."""
+    """Raise if a tcgen05 kernel recorded a wait that did not complete or a neighbor row
+    longer than its capacity (synchronises)."""
     for k, w in _ERR.items():
         v = int(w.item())
         if v:
             w.zero_()
-            raise RuntimeError(f"sph_gemm_bf16_tn: pipeline wait timed out (flags {v:#x}) on device {k}")
+            raise RuntimeError(f"tcgen05 kernel error flags {v:#x} on device {k}")
 
 
 def gemm_tn(A, Bt, out=None, accumulate=False):
@@ -97,7 +99,6 @@ class Graph:
     """Exact neighbor lists (CSR, symmetric) of one or several equal periodic domains."""
 
     def __init__(self, x, config, n_domains=1):
-        from .neighborhood import exact_pairs
         x = x.to("cuda", torch.float32).contiguous()
         n = x.shape[0]
         if n % n_domains:
@@ -105,18 +106,39 @@ class Graph:
         per = n // n_domains
         H = float(config["particle"]["support"])
         dx = float(config["particle"]["dx"])
-        offs, nbrs = [torch.zeros(1, dtype=torch.int64, device="cuda")], []
-        base = 0
+        lib = _lib.load()
+        dom = domain_struct(config)
+        st = _stream()
+        hd = torch.full((per,), H, device="cuda")
+        nb = ctypes.c_size_t()
+        _lib.check("sph_neighbor_workspace_bytes",
+                   lib.sph_neighbor_workspace_bytes(per, per, ctypes.byref(dom), H, ctypes.byref(nb)))
+        wsb = (int(nb.value) + 255) // 256 * 256
+        ws = torch.empty(wsb * n_domains + 256, dtype=torch.uint8, device="cuda")
+        ws0 = (ws.data_ptr() + 255) & ~255
+        counts = torch.empty(n_domains, per, dtype=torch.int32, device="cuda")
+        offs = torch.empty(n_domains, per + 1, dtype=torch.int64, device="cuda")
+        # counts and row offsets of every domain, one host synchronisation, then the indices
         for d in range(n_domains):
             xd = x[d * per:(d + 1) * per]
-            hd = torch.full((per,), H, device="cuda")
-            _, j, _, _, _, _, _, _, off = exact_pairs(xd, xd, hd, config, compute_kernels=False)
-            offs.append(off[1:] + base)
-            nbrs.append((j + d * per).to(torch.int32))
-            base += int(off[-1].item())
+            _lib.check("sph_neighbor_count", lib.sph_neighbor_count(
+                _p(xd), per, _p(xd), _p(hd), per, ctypes.byref(dom), H, ctypes.c_void_p(ws0 + d * wsb), wsb,
+                _p(counts[d]), _p(offs[d]), st))
+        totals = offs[:, -1].cpu()
+        base = torch.zeros(n_domains + 1, dtype=torch.int64)
+        base[1:] = torch.cumsum(totals, 0)
+        self.nbr = torch.empty(int(base[-1]), dtype=torch.int32, device="cuda")
+        for d in range(n_domains):
+            xd = x[d * per:(d + 1) * per]
+            _lib.check("sph_neighbor_fill_csr", lib.sph_neighbor_fill_csr(
+                _p(xd), per, _p(xd), _p(hd), per, ctypes.byref(dom), H, ctypes.c_void_p(ws0 + d * wsb), wsb,
+                _p(offs[d]), _p(self.nbr[int(base[d]):]), st))
+        if n_domains > 1:  # global particle indices and row offsets
+            dom_of_pair = torch.repeat_interleave(torch.arange(n_domains, device="cuda"), totals.cuda())
+            self.nbr += (dom_of_pair * per).to(torch.int32)
+        rows = offs[:, :-1] + base[:-1].cuda()[:, None]
+        self.offsets = torch.cat([rows.reshape(-1), base[-1:].cuda()]).contiguous()
         self.x = x
-        self.offsets = torch.cat(offs).contiguous()
-        self.nbr = torch.cat(nbrs).contiguous()
         self.n = n
         self.npad = _pad128(n)
         self.H = H
@@ -124,15 +146,22 @@ class Graph:
         self.domain = domain_struct(config)
 
 
-def aggregate(g: Graph, h_bf16, relative=False):
-    """E [npad, 64 C] (bf16; rows >= n are zero) of features h [n, C] (bf16)."""
+def aggregate(g: Graph, h_bf16, relative=False, tensor_cores=True):
+    """E [npad, 64 C] (bf16; rows >= n are zero) of features h [n, C] (bf16). The tensor-core
+    kernel rounds the basis values to BF16; the CUDA-core kernel keeps them in FP32."""
     C = h_bf16.shape[1]
     E = torch.empty(g.npad, BASIS * C, dtype=torch.bfloat16, device="cuda")
     if g.npad > g.n:
         E[g.n:].zero_()
-    _lib.check("sph_cconv_aggregate", _lib.load().sph_cconv_aggregate(
-        _p(g.x), g.n, _p(g.offsets), _p(g.nbr), ctypes.byref(g.domain), g.H, g.inv_norm, _p(h_bf16.contiguous()),
-        C, int(bool(relative)), _p(E), _stream()))
+    lib = _lib.load()
+    if tensor_cores:
+        _lib.check("sph_cconv_aggregate_tc", lib.sph_cconv_aggregate_tc(
+            _p(g.x), g.n, _p(g.offsets), _p(g.nbr), ctypes.byref(g.domain), g.H, g.inv_norm,
+            _p(h_bf16.contiguous()), C, int(bool(relative)), _p(E), _p(_err_word(E.device)), _stream()))
+    else:
+        _lib.check("sph_cconv_aggregate", lib.sph_cconv_aggregate(
+            _p(g.x), g.n, _p(g.offsets), _p(g.nbr), ctypes.byref(g.domain), g.H, g.inv_norm,
+            _p(h_bf16.contiguous()), C, int(bool(relative)), _p(E), _stream()))
     return E
 
 

@@ -101,6 +101,15 @@ int sph_neighbor_fill(const float* x_query, int64_t n_query, const float* x_ref,
                       float* q, float* xhat, float* h_pair, float* kernels, float* gradients,
                       sph_stream_t stream);
 
+/* Pass 2, indices only (same workspace, after pass 1): the original reference index of each
+ * exact neighbor as int32, rows in the search's cell order rather than sorted by index.
+ * For callers that need the neighbor lists but not the pair fields (the learned step);
+ * no counterpart in the reference. */
+int sph_neighbor_fill_csr(const float* x_query, int64_t n_query, const float* x_ref,
+                          const float* h_ref, int64_t n_ref, const sph_domain_t* domain,
+                          double max_support, void* workspace, size_t workspace_bytes,
+                          const int64_t* offsets, int32_t* neighbors, sph_stream_t stream);
+
 /* Pass 1 without caller workspace; no counterpart in the reference (its neighborSearch
  * allocates through torch). Same inputs, outputs and results as sph_neighbor_count, but the
  * scratch is a file-scope device array of SPH_NEIGHBOR_STATIC_SCRATCH_BYTES per device, so
@@ -262,6 +271,15 @@ int sph_gemm_bf16_tn(const void* A, const void* Bt, float* D, int64_t M, int64_t
 int sph_cconv_aggregate(const float* x, int64_t n, const int64_t* offsets, const int32_t* neighbors,
                         const sph_domain_t* domain, double support, double inv_norm, const void* h,
                         int32_t channels, int32_t relative, void* E, sph_stream_t stream);
+
+/* sph_cconv_aggregate on the tensor cores: per particle E_i = Phi_i^T G_i as a tcgen05 MMA
+ * (BF16 basis values and features, FP32 accumulation in tensor memory), up to 128
+ * neighbors per row. Same layout and arguments; *err (device word, caller-cleared) gets
+ * bit 8 when a row had more than 128 neighbors (the rest are dropped) and bit 16 when a
+ * wait did not complete. */
+int sph_cconv_aggregate_tc(const float* x, int64_t n, const int64_t* offsets, const int32_t* neighbors,
+                           const sph_domain_t* domain, double support, double inv_norm, const void* h,
+                           int32_t channels, int32_t relative, void* E, uint32_t* err, sph_stream_t stream);
 
 /* Transpose of sph_cconv_aggregate (for the backward pass, symmetric neighbor relation):
  * dh_j[c] = inv_norm * sum_{i in N(j)} sum_b phi_b(x_i - x_j) dE_i[b C + c]; dE fp32 rows of

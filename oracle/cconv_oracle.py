@@ -72,13 +72,17 @@ def edges(x, offsets, nbr, domain, sign=1.0):
     return rows, cols, sign * d
 
 
-def aggregate(x, offsets, nbr, domain, H, inv_norm, h, relative=False):
-    """E [n, 64 C] from features h [n, C] (float64)."""
+def aggregate(x, offsets, nbr, domain, H, inv_norm, h, relative=False, round_operands=False):
+    """E [n, 64 C] from features h [n, C] (float64). round_operands rounds the basis values
+    and the (difference) features to bf16 first, as the tensor-core kernel does."""
     rows, cols, d = edges(x, offsets, nbr, domain)
     phi = basis(d, H)
     n, C = h.shape
     h = np.asarray(h, np.float64)
     hv = h[cols] - h[rows] if relative else h[cols]
+    if round_operands:
+        phi = bf16(phi).astype(np.float64)
+        hv = bf16(hv).astype(np.float64)
     E = np.zeros((n, BASIS, C))
     np.add.at(E, rows, phi[:, :, None] * hv[:, None, :])
     return (E * inv_norm).reshape(n, BASIS * C)
@@ -101,9 +105,11 @@ def aggregate_t(x, offsets, nbr, domain, H, inv_norm, dE, C, relative=False):
 
 
 def layer_forward(x, offsets, nbr, domain, H, inv_norm, h, W, round_like_gpu=True, relative=False):
-    """y = aggregate(h) W, rounding h, E and W to bf16 where the GPU path does."""
+    """y = aggregate(h) W, rounding h, the aggregation operands (tensor-core kernel), E and
+    W to bf16 where the GPU path does."""
     hq = bf16(h) if round_like_gpu else h
-    E = aggregate(x, offsets, nbr, domain, H, inv_norm, np.asarray(hq, np.float64), relative)
+    E = aggregate(x, offsets, nbr, domain, H, inv_norm, np.asarray(hq, np.float64), relative,
+                  round_operands=round_like_gpu)
     Eq = bf16(E).astype(np.float64) if round_like_gpu else E
     Wq = bf16(W).astype(np.float64) if round_like_gpu else np.asarray(W, np.float64)
     return Eq @ Wq, Eq

@@ -85,12 +85,39 @@ def _graph_case(nx=24, seed=4, C=16):
 def test_aggregate_matches_oracle(C, rel):
     from diffsph_gb300.learned import aggregate
     cfg, g, h, dom = _graph_case(C=C)
-    E = aggregate(g, torch.as_tensor(h, device="cuda").to(torch.bfloat16), rel)
+    E = aggregate(g, torch.as_tensor(h, device="cuda").to(torch.bfloat16), rel, tensor_cores=False)
     Eo = CO.aggregate(_np(g.x), _np(g.offsets).astype(np.int64), _np(g.nbr).astype(np.int64), dom, g.H, g.inv_norm,
                       h.astype(np.float64), rel)
     Eg = _np(E[:g.n]).astype(np.float64)
     assert np.all(np.abs(Eg - Eo) <= 2.0 ** -8 * np.abs(Eo) + 1e-5 * np.abs(Eo).max())
     assert float(E[g.n:].abs().max()) == 0.0 if g.npad > g.n else True
+
+
+@pytest.mark.parametrize("C,rel", [(16, False), (32, False), (64, False), (16, True), (64, True)])
+def test_tensor_core_aggregate_matches_oracle(C, rel):
+    """The tcgen05 aggregation against the oracle with the same BF16 operand roundings:
+    only the FP32 accumulation order and the final BF16 rounding differ."""
+    from diffsph_gb300.learned import aggregate, check_device_errors
+    cfg, g, h, dom = _graph_case(C=C)
+    E = aggregate(g, torch.as_tensor(h, device="cuda").to(torch.bfloat16), rel, tensor_cores=True)
+    torch.cuda.synchronize()
+    check_device_errors()
+    x, off, nbr = _np(g.x), _np(g.offsets).astype(np.int64), _np(g.nbr).astype(np.int64)
+    Eo = CO.aggregate(x, off, nbr, dom, g.H, g.inv_norm, h.astype(np.float64), rel, round_operands=True)
+    Eg = _np(E[:g.n]).astype(np.float64)
+    # the kernel rounds an fp32 basis value to bf16, the oracle an fp64 one: a term may land
+    # one bf16 ulp (2^-8 relative) apart, so the bound scales with the sum of |terms|
+    rows, cols, d = CO.edges(x, off, nbr, dom)
+    hh = h.astype(np.float64)
+    hv = np.abs(hh[cols] - hh[rows]) if rel else np.abs(hh[cols])
+    S = np.zeros((g.n, 64, C))
+    np.add.at(S, rows, np.abs(CO.basis(d, g.H))[:, :, None] * hv[:, None, :])
+    S = S.reshape(g.n, 64 * C) * g.inv_norm
+    assert np.all(np.abs(Eg - Eo) <= 2.0 ** -8 * np.abs(Eo) + 2.0 ** -7 * S + 1e-7)
+    assert np.linalg.norm(Eg - Eo) <= 2e-3 * np.linalg.norm(Eo)
+    # and against the exact (fp32-basis) CUDA-core kernel: BF16 basis rounding only
+    Ec = _np(aggregate(g, torch.as_tensor(h, device="cuda").to(torch.bfloat16), rel, tensor_cores=False)[:g.n])
+    assert np.linalg.norm(Eg - Ec) <= 5e-3 * np.linalg.norm(Ec)
 
 
 @pytest.mark.parametrize("C,rel", [(16, False), (64, False), (16, True), (64, True)])
@@ -198,3 +225,26 @@ def test_judge_rejects_a_bad_network_and_falls_back_to_the_solver(bad):
     ref = sol.download()
     assert float(torch.linalg.norm(u - ref["velocities"]) / torch.linalg.norm(ref["velocities"])) < 1e-5
     assert float(torch.max(torch.abs(r - ref["densities"]))) < 1e-5
+
+
+@pytest.mark.parametrize("n_domains", [1, 3])
+def test_graph_lists_equal_the_exact_neighbor_sets(n_domains):
+    """The CSR-only fill (cell order) holds exactly the pairs of the reference-format
+    search (sorted rows), domain by domain, with global indices for packed domains."""
+    from diffsph_gb300.learned import Graph
+    from diffsph_gb300.neighborhood import exact_pairs
+    doms = [scenes.fourier_periodic(24, seed=30 + d, jitter=0.3) for d in range(n_domains)]
+    cfg = doms[0][0]
+    x = torch.cat([torch.as_tensor(st["fluid"]["positions"]) for _, st in doms]).cuda()
+    g = Graph(x, cfg, n_domains)
+    per = x.shape[0] // n_domains
+    off = _np(g.offsets).astype(np.int64)
+    nbr = g.nbr.cpu().numpy().astype(np.int64)
+    for d in range(n_domains):
+        xd = x[d * per:(d + 1) * per]
+        _, j, _, _, _, _, _, _, o = exact_pairs(xd, xd, torch.full((per,), g.H, device="cuda"), cfg,
+                                                compute_kernels=False)
+        j, o = j.cpu().numpy(), o.cpu().numpy()
+        for i in range(per):
+            row = np.sort(nbr[off[d * per + i]:off[d * per + i + 1]]) - d * per
+            assert np.array_equal(row, j[o[i]:o[i + 1]]), (d, i)
