@@ -24,6 +24,8 @@ Grid make_grid(const double mn[2], const double mx[2], const int per[2], double 
                int64_t* ncells_out, int rad) {
     Grid g;
     g.rad = rad;
+    g.slot0 = 0;
+    g.nslots = 0;
     int64_t total = 1;
     for (int a = 0; a < 2; ++a) {
         double ext = mx[a] - mn[a];

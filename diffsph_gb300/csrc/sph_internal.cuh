@@ -20,6 +20,10 @@ struct Grid {
     int nc[2];
     int per[2];
     int rad;  // stencil radius in cells: (2 rad + 1)^2 cells cover the search radius
+    // sorted slot range of the domain; periodic neighbor-list offsets are stored modulo
+    // nslots so that neighbors across the wrap stay within a few cell rows of each other
+    int slot0;
+    int nslots;
 };
 
 __device__ __forceinline__ int cell_coord(float v, float mn, float inv, int nc) {

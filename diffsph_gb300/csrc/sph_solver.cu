@@ -219,6 +219,16 @@ __device__ __forceinline__ bool fits(int d) {
     return sizeof(LT) >= 4 || (d >= -32768 && d <= 32767);
 }
 
+template <bool PER>
+__device__ __forceinline__ int list_slot(int self, int d, const Grid& g) {
+    int j = self + d;
+    if (PER) {
+        if (j < g.slot0) j += g.nslots;
+        else if (j >= g.slot0 + g.nslots) j -= g.nslots;
+    }
+    return j;
+}
+
 template <bool PER, typename LT, class F>
 __device__ __forceinline__ void neighbor_loop(bool active, int self, float2 pi, const float4* __restrict__ X4,
                                               const int32_t* __restrict__ start, const Grid& g, const Phys& P,
@@ -244,6 +254,11 @@ __device__ __forceinline__ void neighbor_loop(bool active, int self, float2 pi, 
                     pair_vec<PER>(pi, make_float2(xj[u].x, xj[u].y), P.geo, x0, x1);
                     if (sq_norm_ref(x0, x1) <= P.T) {
                         int d = s + u - self;
+                        if (PER) {  // shortest offset modulo the domain's slots
+                            const int h2 = g.nslots >> 1;
+                            if (d > h2) d -= g.nslots;
+                            else if (d < -h2) d += g.nslots;
+                        }
                         if (fits<LT>(d)) lst[(cnt++) * 32 + lane] = (LT)d;
                         else overflow = true;
                     }
@@ -261,13 +276,13 @@ __device__ __forceinline__ void neighbor_loop(bool active, int self, float2 pi, 
         if (__any_sync(kFull, cnt > kCap - kUnroll)) {
             int mc = (int)__reduce_max_sync(kFull, (unsigned)cnt);
             for (int k = 0; k < mc; ++k)
-                if (k < cnt) f(self + (int)lst[k * 32 + lane]);
+                if (k < cnt) f(list_slot<PER>(self, (int)lst[k * 32 + lane], g));
             cnt = 0;
         }
     }
     int mc = (int)__reduce_max_sync(kFull, (unsigned)cnt);
     for (int k = 0; k < mc; ++k)
-        if (k < cnt) f(self + (int)lst[k * 32 + lane]);
+        if (k < cnt) f(list_slot<PER>(self, (int)lst[k * 32 + lane], g));
     if (overflow) atomicOr(&words[0], SPH_FLAG_CAPACITY);
 }
 
@@ -1307,6 +1322,8 @@ static int create_impl(const sph_params_t* params, const int64_t* n_fluid, int n
         D.P = make_phys(&params[d], S->nF);
         int64_t nc = 0;
         D.g = dom_grid(&params[d], &nc);
+        D.g.slot0 = (int)off;
+        D.g.nslots = (int)(n_fluid[d] + (nd == 1 ? n_boundary : 0));
         D.cell0 = (int32_t)cell0;
         cell0 += nc;
         S->off_host[d] = off;
@@ -1315,9 +1332,9 @@ static int create_impl(const sph_params_t* params, const int64_t* n_fluid, int n
         // one-sided slot span of a stencil: rad rows of cells plus rad + 1 cells, at the rest
         // density (cell/dx)^2 per cell with a 1.5x compression margin
         double ppc = (cell_size(&params[d]) / params[d].dx) * (cell_size(&params[d]) / params[d].dx);
+        // (periodic offsets are stored modulo the domain's slots: the same bound holds across
+        // the wrap)
         double span = ((double)kSolverRad * D.g.nc[0] + kSolverRad + 1) * ppc * 1.5;
-        // a periodic stencil wraps to the far end of the domain's slots
-        if (params[d].domain.periodic[0] || params[d].domain.periodic[1]) span = (double)n_fluid[d] + (d == 0 ? n_boundary : 0);
         span_max = span > span_max ? span : span_max;
     }
     S->off_host[nd] = off;
