@@ -187,25 +187,41 @@ __global__ void k_gather(int64_t n, int nF, const int32_t* __restrict__ perm, co
 // The cells are >= (h + largest displacement since the sort), so the stencil of the
 // particle's current cell holds every particle within h.
 // ------------------------------------------------------------------------------------
+// Bit k of *wrap marks range k as one whose pairs may cross the periodic boundary. Every
+// other range lies within rad cells of the particle's cell without wrapping and away from
+// the edge cells (where a particle may have crossed the boundary since the sort; the skin
+// check keeps that motion below one cell). On an axis of at least 2 (rad + 2) cells its
+// pairs then have |x_ij| < (rad + 2) cells <= half the extent, where the reference's minimum
+// image is the identity, so the scan may skip it there exactly.
 __device__ __forceinline__ int stencil_ranges(float2 p, const Grid& g, const int32_t* __restrict__ start,
-                                              int rs[kMaxRanges], int re[kMaxRanges]) {
+                                              int rs[kMaxRanges], int re[kMaxRanges], unsigned* wrap = nullptr) {
     int cx = cell_coord(p.x, g.mn[0], g.inv_cell[0], g.nc[0]);
     int cy = cell_coord(p.y, g.mn[1], g.inv_cell[1], g.nc[1]);
     int rows[kMaxRows], lo[2], hi[2];
     int nr = stencil_rows(cy, g, rows);
     int ncol = stencil_cols(cx, g, lo, hi);
+    const bool smallx = g.per[0] && g.nc[0] < 2 * g.rad + 4;
+    const bool smally = g.per[1] && g.nc[1] < 2 * g.rad + 4;
+    unsigned w = 0;
     int n = 0;
     for (int a = 0; a < nr; ++a) {
         int base = rows[a] * g.nc[0];
+        const int dy = rows[a] - cy;
+        const bool wy =
+            smally || (g.per[1] && (dy > g.rad || dy < -g.rad || rows[a] == 0 || rows[a] == g.nc[1] - 1));
         for (int b = 0; b < ncol; ++b) {
             int s0 = __ldg(&start[base + lo[b]]), s1 = __ldg(&start[base + hi[b] + 1]);
             if (s1 > s0) {
+                const bool wx = smallx || (g.per[0] && (lo[b] > cx + g.rad || hi[b] < cx - g.rad || lo[b] == 0 ||
+                                                        hi[b] == g.nc[0] - 1));
+                if (wx || wy) w |= 1u << n;
                 rs[n] = s0;
                 re[n] = s1;
                 ++n;
             }
         }
     }
+    if (wrap) *wrap = w;
     return n;
 }
 
@@ -235,7 +251,8 @@ __device__ __forceinline__ void neighbor_loop(bool active, int self, float2 pi, 
                                               LT* __restrict__ lst, uint32_t* __restrict__ words, F&& f) {
     const int lane = threadIdx.x & 31;
     int rs[kMaxRanges], re[kMaxRanges];
-    int nrng = active ? stencil_ranges(pi, g, start, rs, re) : 0;
+    unsigned wmask = 0;
+    int nrng = active ? stencil_ranges(pi, g, start, rs, re, PER ? &wmask : nullptr) : 0;
     int r = 0;
     int s = nrng > 0 ? rs[0] : 0, se = nrng > 0 ? re[0] : 0;
     int cnt = 0;
@@ -243,6 +260,7 @@ __device__ __forceinline__ void neighbor_loop(bool active, int self, float2 pi, 
     while (__any_sync(kFull, r < nrng)) {
         if (r < nrng) {
             int m = se - s < kUnroll ? se - s : kUnroll;
+            const bool wr = PER && ((wmask >> r) & 1u);
             float4 xj[kUnroll];
 #pragma unroll
             for (int u = 0; u < kUnroll; ++u)
@@ -251,7 +269,10 @@ __device__ __forceinline__ void neighbor_loop(bool active, int self, float2 pi, 
             for (int u = 0; u < kUnroll; ++u) {
                 if (u < m) {
                     float x0, x1;
-                    pair_vec<PER>(pi, make_float2(xj[u].x, xj[u].y), P.geo, x0, x1);
+                    if (wr)
+                        pair_vec<true>(pi, make_float2(xj[u].x, xj[u].y), P.geo, x0, x1);
+                    else
+                        pair_vec<false>(pi, make_float2(xj[u].x, xj[u].y), P.geo, x0, x1);
                     if (sq_norm_ref(x0, x1) <= P.T) {
                         int d = s + u - self;
                         if (PER) {  // shortest offset modulo the domain's slots
