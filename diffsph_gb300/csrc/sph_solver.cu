@@ -94,11 +94,36 @@ struct Dom {
     int32_t cell0;
     int32_t pad;
 };
+static_assert(sizeof(Dom) % 4 == 0, "Dom is copied as 32-bit words");
 
 __device__ __forceinline__ bool is_boundary(float rho_signed) { return __float_as_int(rho_signed) < 0; }
 
 __device__ __forceinline__ int dom_of(const int32_t* __restrict__ did, int64_t i, int64_t n) {
     return (did && i < n) ? did[i] : 0;
+}
+
+// Packed batches: a block of consecutive slots spans at most two domains when every domain
+// holds at least a block's worth of particles. Their constants are copied to shared memory
+// once per block; slots of any other domain read the global table.
+__device__ __forceinline__ void stage_doms(const Dom* __restrict__ doms, const int32_t* __restrict__ did,
+                                           int64_t first, int64_t last, int64_t n, Dom* s_dom, int* s_id) {
+    const int64_t a = first < n ? first : n - 1, b = last < n ? last : n - 1;
+    const int d0 = dom_of(did, a, n), d1 = dom_of(did, b, n);
+    constexpr int kWords = (int)(sizeof(Dom) / 4);
+    const uint32_t* src0 = reinterpret_cast<const uint32_t*>(doms + d0);
+    const uint32_t* src1 = reinterpret_cast<const uint32_t*>(doms + d1);
+    uint32_t* dst = reinterpret_cast<uint32_t*>(s_dom);
+    for (int k = threadIdx.x; k < 2 * kWords; k += blockDim.x) dst[k] = k < kWords ? src0[k] : src1[k - kWords];
+    if (threadIdx.x == 0) {
+        s_id[0] = d0;
+        s_id[1] = d1;
+    }
+    __syncthreads();
+}
+
+__device__ __forceinline__ const Dom& dom_ref(const Dom* __restrict__ doms, const Dom* s_dom, const int* s_id,
+                                              int d) {
+    return d == s_id[0] ? s_dom[0] : (d == s_id[1] ? s_dom[1] : doms[d]);
 }
 
 // ------------------------------------------------------------------------------------
@@ -394,10 +419,11 @@ __global__ void k_mdbc(int nB, const int32_t* __restrict__ bidx, const int32_t* 
 template <bool PER, bool BATCH, typename LT>
 __device__ __forceinline__ void pass_a_tile(const Dom& D0, int64_t i, int64_t n, const float4* __restrict__ X4,
                                             float4* __restrict__ V4, const int32_t* __restrict__ start_all,
-                                            const Dom* __restrict__ doms, const int32_t* __restrict__ did,
+                                            const Dom* __restrict__ doms, const Dom* s_dom, const int* s_id,
+                                            const int32_t* __restrict__ did,
                                             const int32_t* __restrict__ uid, const RhsOut& out,
                                             LT* __restrict__ lst, uint32_t* __restrict__ words) {
-    const Dom& D = BATCH ? doms[dom_of(did, i, n)] : D0;
+    const Dom& D = BATCH ? dom_ref(doms, s_dom, s_id, dom_of(did, i, n)) : D0;
     const Phys& P = D.P;
     const Grid& g = D.g;
     const int32_t* __restrict__ start = start_all + D.cell0;
@@ -463,9 +489,13 @@ __global__ void __launch_bounds__(32 * W) k_pass_a(const Dom D0, int64_t n, cons
                                                    const int32_t* __restrict__ uid, RhsOut out,
                                                    uint32_t* __restrict__ words) {
     extern __shared__ __align__(16) unsigned char s_dyn[];
+    __shared__ Dom s_dom[BATCH ? 2 : 1];
+    __shared__ int s_id[2];
     LT* lst = reinterpret_cast<LT*>(s_dyn) + (threadIdx.x >> 5) * (kCap * 32);
-    pass_a_tile<PER, BATCH, LT>(D0, (int64_t)blockIdx.x * (32 * W) + threadIdx.x, n, X4, V4, start, doms, did, uid, out, lst,
-                         words);
+    const int64_t first = (int64_t)blockIdx.x * (32 * W);
+    if (BATCH) stage_doms(doms, did, first, first + 32 * W - 1, n, s_dom, s_id);
+    pass_a_tile<PER, BATCH, LT>(D0, first + threadIdx.x, n, X4, V4, start, doms, s_dom, s_id, did, uid, out, lst,
+                                words);
 }
 
 // ------------------------------------------------------------------------------------
@@ -482,14 +512,15 @@ __global__ void __launch_bounds__(32 * W) k_pass_a(const Dom D0, int64_t n, cons
 template <bool PER, bool BATCH, int MODE, typename LT>
 __device__ __forceinline__ void pass_b_tile(const Dom& D0, int64_t i, int64_t n, const float4* __restrict__ X4,
                                             const float4* __restrict__ V4, const int32_t* __restrict__ start_all,
-                                            const Dom* __restrict__ doms, const int32_t* __restrict__ did,
+                                            const Dom* __restrict__ doms, const Dom* s_dom, const int* s_id,
+                                            const int32_t* __restrict__ did,
                                             const int32_t* __restrict__ uid, const RhsOut& out,
                                             float2* __restrict__ Xr, const float4* __restrict__ X4n,
                                             const float4* __restrict__ V4n, float4* __restrict__ X4o,
                                             float4* __restrict__ V4o, uint32_t* __restrict__ words,
                                             uint32_t* __restrict__ maxv, LT* __restrict__ lst) {
     const int dom = BATCH ? dom_of(did, i, n) : 0;
-    const Dom& D = BATCH ? doms[dom] : D0;
+    const Dom& D = BATCH ? dom_ref(doms, s_dom, s_id, dom) : D0;
     const Phys& P = D.P;
     const Grid& g = D.g;
     const int32_t* __restrict__ start = start_all + D.cell0;
@@ -585,7 +616,12 @@ __device__ __forceinline__ void pass_b_tile(const Dom& D0, int64_t i, int64_t n,
         X4o[i] = make_float4(w.x, w.y, rnew, eos_p(rnew, P.eos));
         V4o[i] = make_float4(u0, u1, 0.f, 0.f);
         float sp = __fsqrt_rn(__fmaf_rn(u1, u1, __fmul_rn(u0, u0)));
-        atomicMax(&maxv[dom], __float_as_uint(sp));
+        {  // one atomic per warp and domain (speeds are non-negative: their bits order as uints)
+            const unsigned act = __activemask();
+            const unsigned grp = BATCH ? __match_any_sync(act, dom) : act;
+            const unsigned vmax = __reduce_max_sync(grp, __float_as_uint(sp));
+            if ((int)(threadIdx.x & 31) == __ffs(grp) - 1) atomicMax(&maxv[dom], vmax);
+        }
         if (!isfinite(u0) || !isfinite(u1) || !isfinite(rnew) || !isfinite(xp.x) || !isfinite(xp.y))
             atomicOr(&words[0], SPH_FLAG_NONFINITE);
         // the cells of this step's sort must still cover h + the displacement at the shift pass
@@ -605,9 +641,13 @@ __global__ void __launch_bounds__(32 * W) k_pass_b(const Dom D0, int64_t n, cons
                                                    float4* __restrict__ V4o, uint32_t* __restrict__ words,
                                                    uint32_t* __restrict__ maxv) {
     extern __shared__ __align__(16) unsigned char s_dyn[];
+    __shared__ Dom s_dom[BATCH ? 2 : 1];
+    __shared__ int s_id[2];
     LT* lst = reinterpret_cast<LT*>(s_dyn) + (threadIdx.x >> 5) * (kCap * 32);
-    pass_b_tile<PER, BATCH, MODE, LT>(D0, (int64_t)blockIdx.x * (32 * W) + threadIdx.x, n, X4, V4, start, doms, did, uid, out,
-                               Xr, X4n, V4n, X4o, V4o, words, maxv, lst);
+    const int64_t first = (int64_t)blockIdx.x * (32 * W);
+    if (BATCH) stage_doms(doms, did, first, first + 32 * W - 1, n, s_dom, s_id);
+    pass_b_tile<PER, BATCH, MODE, LT>(D0, first + threadIdx.x, n, X4, V4, start, doms, s_dom, s_id, did, uid, out,
+                                      Xr, X4n, V4n, X4o, V4o, words, maxv, lst);
 }
 
 // ------------------------------------------------------------------------------------
@@ -617,14 +657,15 @@ __global__ void __launch_bounds__(32 * W) k_pass_b(const Dom D0, int64_t n, cons
 template <bool PER, bool BATCH, typename LT>
 __device__ __forceinline__ void shift_tile(const Dom& D0, int64_t i, int64_t n, const float4* __restrict__ X4,
                                            const float4* __restrict__ V4, const int32_t* __restrict__ start_all,
-                                           const Dom* __restrict__ doms, const int32_t* __restrict__ did,
+                                           const Dom* __restrict__ doms, const Dom* s_dom, const int* s_id,
+                                           const int32_t* __restrict__ did,
                                            float2* __restrict__ Xr, float4* __restrict__ X4o,
                                            float4* __restrict__ V4o, uint32_t* __restrict__ words,
                                            const uint32_t* __restrict__ maxv, int enabled,
                                            const int32_t* __restrict__ uid, float* __restrict__ dx_out,
                                            LT* __restrict__ lst) {
     const int dom = BATCH ? dom_of(did, i, n) : 0;
-    const Dom& D = BATCH ? doms[dom] : D0;
+    const Dom& D = BATCH ? dom_ref(doms, s_dom, s_id, dom) : D0;
     const Phys& P = D.P;
     const Grid& g = D.g;
     const int32_t* __restrict__ start = start_all + D.cell0;
@@ -687,9 +728,13 @@ __global__ void __launch_bounds__(32 * W) k_shift(const Dom D0, int64_t n, const
                                                   const uint32_t* __restrict__ maxv, int enabled,
                                                   const int32_t* __restrict__ uid, float* __restrict__ dx_out) {
     extern __shared__ __align__(16) unsigned char s_dyn[];
+    __shared__ Dom s_dom[BATCH ? 2 : 1];
+    __shared__ int s_id[2];
     LT* lst = reinterpret_cast<LT*>(s_dyn) + (threadIdx.x >> 5) * (kCap * 32);
-    shift_tile<PER, BATCH, LT>(D0, (int64_t)blockIdx.x * (32 * W) + threadIdx.x, n, X4, V4, start, doms, did, Xr, X4o, V4o, words,
-                        maxv, enabled, uid, dx_out, lst);
+    const int64_t first = (int64_t)blockIdx.x * (32 * W);
+    if (BATCH) stage_doms(doms, did, first, first + 32 * W - 1, n, s_dom, s_id);
+    shift_tile<PER, BATCH, LT>(D0, first + threadIdx.x, n, X4, V4, start, doms, s_dom, s_id, did, Xr, X4o, V4o,
+                               words, maxv, enabled, uid, dx_out, lst);
 }
 
 // max |u| over all particles (the Mach number of shifting.py:139-142)
