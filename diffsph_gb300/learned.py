@@ -133,9 +133,8 @@ class Graph:
             _lib.check("sph_neighbor_fill_csr", lib.sph_neighbor_fill_csr(
                 _p(xd), per, _p(xd), _p(hd), per, ctypes.byref(dom), H, ctypes.c_void_p(ws0 + d * wsb), wsb,
                 _p(offs[d]), _p(self.nbr[int(base[d]):]), st))
-        if n_domains > 1:  # global particle indices and row offsets
-            dom_of_pair = torch.repeat_interleave(torch.arange(n_domains, device="cuda"), totals.cuda())
-            self.nbr += (dom_of_pair * per).to(torch.int32)
+        for d in range(1, n_domains):  # global particle indices of the packed domains
+            self.nbr[int(base[d]):int(base[d + 1])] += d * per
         rows = offs[:, :-1] + base[:-1].cuda()[:, None]
         self.offsets = torch.cat([rows.reshape(-1), base[-1:].cuda()]).contiguous()
         self.x = x
