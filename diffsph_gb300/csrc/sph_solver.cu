@@ -255,6 +255,9 @@ __device__ __forceinline__ int stencil_ranges(float2 p, const Grid& g, const int
 // relative to the particle's own slot: int16_t halves the shared memory (leaving more of
 // the unified L1 for the neighbor data) and is used when the grid keeps every stencil
 // within +-32767 slots; an entry that does not fit raises SPH_FLAG_CAPACITY.
+// capacity of the neighbor list pass A stores for pass B (entries per particle)
+constexpr int kStoreCap = 64;
+
 template <typename LT>
 __device__ __forceinline__ bool fits(int d) {
     return sizeof(LT) >= 4 || (d >= -32768 && d <= 32767);
@@ -422,7 +425,8 @@ __device__ __forceinline__ void pass_a_tile(const Dom& D0, int64_t i, int64_t n,
                                             const Dom* __restrict__ doms, const Dom* s_dom, const int* s_id,
                                             const int32_t* __restrict__ did,
                                             const int32_t* __restrict__ uid, const RhsOut& out,
-                                            LT* __restrict__ lst, uint32_t* __restrict__ words) {
+                                            LT* __restrict__ lst, uint32_t* __restrict__ words,
+                                            int16_t* __restrict__ nl, int16_t* __restrict__ nlc) {
     const Dom& D = BATCH ? dom_ref(doms, s_dom, s_id, dom_of(did, i, n)) : D0;
     const Phys& P = D.P;
     const Grid& g = D.g;
@@ -435,7 +439,22 @@ __device__ __forceinline__ void pass_a_tile(const Dom& D0, int64_t i, int64_t n,
     float M00 = 0.f, M01 = 0.f, M10 = 0.f, M11 = 0.f;
     float gf0 = 0.f, gf1 = 0.f, gb0 = 0.f, gb1 = 0.f;
     int nf = 0, nbnd = 0;
+    int nstored = 0;
+    bool unstored = false;
     neighbor_loop<PER, LT>(active, (int)i, pi, X4, start, g, P, lst, words, [&](int j) {
+        {  // keep the exact list (scan order) for pass B at the same positions
+            int d = j - (int)i;
+            if (PER) {
+                const int h2 = g.nslots >> 1;
+                if (d > h2) d -= g.nslots;
+                else if (d < -h2) d += g.nslots;
+            }
+            if (nstored < kStoreCap && d >= -32768 && d <= 32767)
+                nl[(int64_t)nstored * n + i] = (int16_t)d;
+            else
+                unstored = true;
+            ++nstored;
+        }
         float4 xj = __ldg(&X4[j]);
         float x0, x1;
         pair_vec<PER>(pi, make_float2(xj.x, xj.y), P.geo, x0, x1);
@@ -460,6 +479,7 @@ __device__ __forceinline__ void pass_a_tile(const Dom& D0, int64_t i, int64_t n,
             ++nf;
         }
     });
+    if (inb) nlc[i] = active ? (unstored ? (int16_t)-1 : (int16_t)nstored) : (int16_t)0;
     if (!active) return;
     float m = P.m;
     if (nf < 4) {
@@ -487,7 +507,8 @@ __global__ void __launch_bounds__(32 * W) k_pass_a(const Dom D0, int64_t n, cons
                                                    float4* __restrict__ V4, const int32_t* __restrict__ start,
                                                    const Dom* __restrict__ doms, const int32_t* __restrict__ did,
                                                    const int32_t* __restrict__ uid, RhsOut out,
-                                                   uint32_t* __restrict__ words) {
+                                                   uint32_t* __restrict__ words, int16_t* __restrict__ nl,
+                                                   int16_t* __restrict__ nlc) {
     extern __shared__ __align__(16) unsigned char s_dyn[];
     __shared__ Dom s_dom[BATCH ? 2 : 1];
     __shared__ int s_id[2];
@@ -495,7 +516,7 @@ __global__ void __launch_bounds__(32 * W) k_pass_a(const Dom D0, int64_t n, cons
     const int64_t first = (int64_t)blockIdx.x * (32 * W);
     if (BATCH) stage_doms(doms, did, first, first + 32 * W - 1, n, s_dom, s_id);
     pass_a_tile<PER, BATCH, LT>(D0, first + threadIdx.x, n, X4, V4, start, doms, s_dom, s_id, did, uid, out, lst,
-                                words);
+                                words, nl, nlc);
 }
 
 // ------------------------------------------------------------------------------------
@@ -518,7 +539,8 @@ __device__ __forceinline__ void pass_b_tile(const Dom& D0, int64_t i, int64_t n,
                                             float2* __restrict__ Xr, const float4* __restrict__ X4n,
                                             const float4* __restrict__ V4n, float4* __restrict__ X4o,
                                             float4* __restrict__ V4o, uint32_t* __restrict__ words,
-                                            uint32_t* __restrict__ maxv, LT* __restrict__ lst) {
+                                            uint32_t* __restrict__ maxv, LT* __restrict__ lst,
+                                            const int16_t* __restrict__ nl, const int16_t* __restrict__ nlc) {
     const int dom = BATCH ? dom_of(did, i, n) : 0;
     const Dom& D = BATCH ? dom_ref(doms, s_dom, s_id, dom) : D0;
     const Phys& P = D.P;
@@ -531,7 +553,7 @@ __device__ __forceinline__ void pass_b_tile(const Dom& D0, int64_t i, int64_t n,
     float2 pi = make_float2(xi.x, xi.y);
     float rhoi = xi.z, pri = xi.w;
     float ac = 0.f, ad = 0.f, ap0 = 0.f, ap1 = 0.f, av0 = 0.f, av1 = 0.f, ab0 = 0.f, ab1 = 0.f;
-    neighbor_loop<PER, LT>(active, (int)i, pi, X4, start, g, P, lst, words, [&](int j) {
+    auto pair_b = [&](int j) {
         float4 xj = __ldg(&X4[j]);
         float4 vj = __ldg(&V4[j]);
         float x0, x1;
@@ -565,7 +587,24 @@ __device__ __forceinline__ void pass_b_tile(const Dom& D0, int64_t i, int64_t n,
             float psig = -rij * (pg.xh0 * g0 + pg.xh1 * g1) + (vi.z + vj.z) * g0 + (vi.w + vj.w) * g1;
             ad = fmaf(psig, irj, ad);
         }
-    });
+    };
+    // the exact list pass A stored at these positions (same scan order, so the same sums);
+    // a warp with a row that could not be stored scans the stencil itself
+    const int nst = active ? (int)nlc[i] : 0;
+    if (__any_sync(kFull, nst < 0)) {
+        neighbor_loop<PER, LT>(active, (int)i, pi, X4, start, g, P, lst, words, pair_b);
+    } else {
+        int k = 0;
+        for (; k + 4 <= nst; k += 4) {
+            const int d0 = nl[(int64_t)k * n + i], d1 = nl[(int64_t)(k + 1) * n + i];
+            const int d2 = nl[(int64_t)(k + 2) * n + i], d3 = nl[(int64_t)(k + 3) * n + i];
+            pair_b(list_slot<PER>((int)i, d0, g));
+            pair_b(list_slot<PER>((int)i, d1, g));
+            pair_b(list_slot<PER>((int)i, d2, g));
+            pair_b(list_slot<PER>((int)i, d3, g));
+        }
+        for (; k < nst; ++k) pair_b(list_slot<PER>((int)i, (int)nl[(int64_t)k * n + i], g));
+    }
     if (!inb) return;
     if (!active) {  // boundary rows: static, carried over to the next stage
         if (MODE != 0) {
@@ -639,7 +678,8 @@ __global__ void __launch_bounds__(32 * W) k_pass_b(const Dom D0, int64_t n, cons
                                                    float2* __restrict__ Xr, const float4* __restrict__ X4n,
                                                    const float4* __restrict__ V4n, float4* __restrict__ X4o,
                                                    float4* __restrict__ V4o, uint32_t* __restrict__ words,
-                                                   uint32_t* __restrict__ maxv) {
+                                                   uint32_t* __restrict__ maxv, const int16_t* __restrict__ nl,
+                                                   const int16_t* __restrict__ nlc) {
     extern __shared__ __align__(16) unsigned char s_dyn[];
     __shared__ Dom s_dom[BATCH ? 2 : 1];
     __shared__ int s_id[2];
@@ -647,7 +687,7 @@ __global__ void __launch_bounds__(32 * W) k_pass_b(const Dom D0, int64_t n, cons
     const int64_t first = (int64_t)blockIdx.x * (32 * W);
     if (BATCH) stage_doms(doms, did, first, first + 32 * W - 1, n, s_dom, s_id);
     pass_b_tile<PER, BATCH, MODE, LT>(D0, first + threadIdx.x, n, X4, V4, start, doms, s_dom, s_id, did, uid, out,
-                                      Xr, X4n, V4n, X4o, V4o, words, maxv, lst);
+                                      Xr, X4n, V4n, X4o, V4o, words, maxv, lst, nl, nlc);
 }
 
 // ------------------------------------------------------------------------------------
@@ -1186,6 +1226,8 @@ struct sph_solver {
     int32_t *key, *perm, *count, *fill, *start, *scan32;
     int32_t* bidx;
     uint32_t* words;  // [0] flags, [2] boundary count
+    int16_t* nl;      // exact neighbor list of the last pass A: slot offsets, [kStoreCap][n]
+    int16_t* nlc;     // its length per slot (-1: not stored)
     uint32_t* maxv;   // per-domain max |u| (float bits)
     Dom* doms;
     int64_t* dom_off;
@@ -1252,7 +1294,11 @@ static size_t solver_layout(const sph_params_t* p, const int64_t* nF_d, int nd, 
     int64_t* dom_off = c.take<int64_t>(nd + 1);
     float2* bnormal = c.take<float2>(nB);
     float* bdist = c.take<float>(nB);
+    int16_t* nl = c.take<int16_t>((int64_t)kStoreCap * n);
+    int16_t* nlc = c.take<int16_t>(n);
     if (S) {
+        S->nl = nl;
+        S->nlc = nlc;
         S->n = n;
         S->nF = nF;
         S->nB = nB;
@@ -1570,7 +1616,8 @@ template <bool PER, bool BATCH, typename LT, int W>
 static void launch_a_k(sph_solver* S, float4* X4, float4* V4, RhsOut o, cudaStream_t st) {
     unsigned gb = (unsigned)((S->n + 32 * W - 1) / (32 * W));
     k_pass_a<PER, BATCH, LT, W><<<gb, 32 * W, list_bytes<LT, W>(), st>>>(S->doms_host[0], S->n, X4, V4, S->start,
-                                                                        S->doms, dids(S), S->uid, o, S->words);
+                                                                        S->doms, dids(S), S->uid, o, S->words,
+                                                                        S->nl, S->nlc);
 }
 
 template <typename LT, int W>
@@ -1598,7 +1645,7 @@ static void launch_b_k(sph_solver* S, float4* X4, float4* V4, RhsOut o, float4* 
     unsigned gb = (unsigned)((S->n + 32 * W - 1) / (32 * W));
     k_pass_b<PER, BATCH, MODE, LT, W><<<gb, 32 * W, list_bytes<LT, W>(), st>>>(
         S->doms_host[0], S->n, X4, V4, S->start, S->doms, dids(S), S->uid, o, S->Xr, S->Xc, S->Vc, X4o, V4o,
-        S->words, S->maxv);
+        S->words, S->maxv, S->nl, S->nlc);
 }
 
 template <int MODE, typename LT, int W>
