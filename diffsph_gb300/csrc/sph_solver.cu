@@ -73,6 +73,8 @@ struct Phys {
     int compute_mach;
     int density_update;
     float verlet_lim;   // (skin - 1) * h: largest displacement since the sort
+    float T_skin;       // squared radius of the skin list (1.1 h, with a rounding margin)
+    float skin_lim;     // displacement since the sort up to which the skin list holds every pair
 };
 
 struct RhsOut {
@@ -257,6 +259,14 @@ __device__ __forceinline__ int stencil_ranges(float2 p, const Grid& g, const int
 // within +-32767 slots; an entry that does not fit raises SPH_FLAG_CAPACITY.
 // capacity of the neighbor list pass A stores for pass B (entries per particle)
 constexpr int kStoreCap = 64;
+// skin list: every candidate within (1 + kSkinFrac) h at the sort positions, kept by the
+// first pass A of a step; the second pass A and the shift filter it instead of the stencil
+constexpr double kSkinFrac = 0.1;
+constexpr int kSkinCap = 80;
+
+struct NoCand {
+    __device__ __forceinline__ void operator()(int, float) const {}
+};
 
 template <typename LT>
 __device__ __forceinline__ bool fits(int d) {
@@ -273,10 +283,11 @@ __device__ __forceinline__ int list_slot(int self, int d, const Grid& g) {
     return j;
 }
 
-template <bool PER, typename LT, class F>
+template <bool PER, typename LT, class F, class FC = NoCand>
 __device__ __forceinline__ void neighbor_loop(bool active, int self, float2 pi, const float4* __restrict__ X4,
                                               const int32_t* __restrict__ start, const Grid& g, const Phys& P,
-                                              LT* __restrict__ lst, uint32_t* __restrict__ words, F&& f) {
+                                              LT* __restrict__ lst, uint32_t* __restrict__ words, F&& f,
+                                              FC fc = FC()) {
     const int lane = threadIdx.x & 31;
     int rs[kMaxRanges], re[kMaxRanges];
     unsigned wmask = 0;
@@ -301,7 +312,9 @@ __device__ __forceinline__ void neighbor_loop(bool active, int self, float2 pi, 
                         pair_vec<true>(pi, make_float2(xj[u].x, xj[u].y), P.geo, x0, x1);
                     else
                         pair_vec<false>(pi, make_float2(xj[u].x, xj[u].y), P.geo, x0, x1);
-                    if (sq_norm_ref(x0, x1) <= P.T) {
+                    const float sqc = sq_norm_ref(x0, x1);
+                    fc(s + u, sqc);
+                    if (sqc <= P.T) {
                         int d = s + u - self;
                         if (PER) {  // shortest offset modulo the domain's slots
                             const int h2 = g.nslots >> 1;
@@ -333,6 +346,36 @@ __device__ __forceinline__ void neighbor_loop(bool active, int self, float2 pi, 
     for (int k = 0; k < mc; ++k)
         if (k < cnt) f(list_slot<PER>(self, (int)lst[k * 32 + lane], g));
     if (overflow) atomicOr(&words[0], SPH_FLAG_CAPACITY);
+}
+
+// The exact neighbors of the stored skin list (scan order of the first pass A of the step,
+// so the same order a scan at the same cells gives), filtered at the current positions.
+template <bool PER, class F>
+__device__ __forceinline__ void skin_loop(int self, float2 pi, const float4* __restrict__ X4, const Grid& g,
+                                          const Phys& P, const int16_t* __restrict__ sl, int cnt, int64_t n,
+                                          F&& f) {
+    int k = 0;
+    for (; k + 4 <= cnt; k += 4) {
+        int j[4];
+        float4 xj[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) j[u] = list_slot<PER>(self, (int)sl[(int64_t)(k + u) * n + self], g);
+#pragma unroll
+        for (int u = 0; u < 4; ++u) xj[u] = __ldg(&X4[j[u]]);
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            float x0, x1;
+            pair_vec<PER>(pi, make_float2(xj[u].x, xj[u].y), P.geo, x0, x1);
+            if (sq_norm_ref(x0, x1) <= P.T) f(j[u]);
+        }
+    }
+    for (; k < cnt; ++k) {
+        const int j = list_slot<PER>(self, (int)sl[(int64_t)k * n + self], g);
+        const float4 xj = __ldg(&X4[j]);
+        float x0, x1;
+        pair_vec<PER>(pi, make_float2(xj.x, xj.y), P.geo, x0, x1);
+        if (sq_norm_ref(x0, x1) <= P.T) f(j);
+    }
 }
 
 // ------------------------------------------------------------------------------------
@@ -419,14 +462,15 @@ __global__ void k_mdbc(int nB, const int32_t* __restrict__ bidx, const int32_t* 
 //                                                 (densityDiffusion.py:7-46, deltaPlus.py:256-262)
 // The uniform mass m is factored out of the sums.
 // ------------------------------------------------------------------------------------
-template <bool PER, bool BATCH, typename LT>
+template <bool PER, bool BATCH, typename LT, bool BUILD>
 __device__ __forceinline__ void pass_a_tile(const Dom& D0, int64_t i, int64_t n, const float4* __restrict__ X4,
                                             float4* __restrict__ V4, const int32_t* __restrict__ start_all,
                                             const Dom* __restrict__ doms, const Dom* s_dom, const int* s_id,
                                             const int32_t* __restrict__ did,
                                             const int32_t* __restrict__ uid, const RhsOut& out,
                                             LT* __restrict__ lst, uint32_t* __restrict__ words,
-                                            int16_t* __restrict__ nl, int16_t* __restrict__ nlc) {
+                                            int16_t* __restrict__ nl, int16_t* __restrict__ nlc,
+                                            int skin_mode, int16_t* __restrict__ sl, int16_t* __restrict__ slc) {
     const Dom& D = BATCH ? dom_ref(doms, s_dom, s_id, dom_of(did, i, n)) : D0;
     const Phys& P = D.P;
     const Grid& g = D.g;
@@ -441,7 +485,7 @@ __device__ __forceinline__ void pass_a_tile(const Dom& D0, int64_t i, int64_t n,
     int nf = 0, nbnd = 0;
     int nstored = 0;
     bool unstored = false;
-    neighbor_loop<PER, LT>(active, (int)i, pi, X4, start, g, P, lst, words, [&](int j) {
+    auto pair_a = [&](int j) {
         {  // keep the exact list (scan order) for pass B at the same positions
             int d = j - (int)i;
             if (PER) {
@@ -478,7 +522,40 @@ __device__ __forceinline__ void pass_a_tile(const Dom& D0, int64_t i, int64_t n,
             gf1 = fmaf(drho, k1, gf1);
             ++nf;
         }
-    });
+    };
+    // BUILD (first pass A after a sort): scan the stencil and keep every candidate within
+    // the skin radius. Otherwise skin_mode 1 filters the skin list when it is complete for
+    // every lane of the warp (no overflow, displacements within skin_lim) and skin_mode 2
+    // scans.
+    if (BUILD && !PER) {
+        int ns = 0;
+        bool sbad = false;
+        auto keep = [&](int slot, float sq) {
+            if (sq <= P.T_skin) {
+                int d = slot - (int)i;
+                if (PER) {
+                    const int h2 = g.nslots >> 1;
+                    if (d > h2) d -= g.nslots;
+                    else if (d < -h2) d += g.nslots;
+                }
+                if (ns < kSkinCap && d >= -32768 && d <= 32767)
+                    sl[(int64_t)ns * n + i] = (int16_t)d;
+                else
+                    sbad = true;
+                ++ns;
+            }
+        };
+        neighbor_loop<PER, LT>(active, (int)i, pi, X4, start, g, P, lst, words, pair_a, keep);
+        if (inb) slc[i] = active ? (sbad ? (int16_t)-1 : (int16_t)ns) : (int16_t)0;
+    } else {
+        // (periodic domains never use the skin list: the branch compiles away for them)
+        const int sk = (!PER && skin_mode == 1 && active) ? (int)slc[i] : 0;
+        const bool use_skin = !PER && skin_mode == 1 && __all_sync(kFull, sk >= 0) && words[3] == 0u;
+        if (use_skin)
+            skin_loop<PER>((int)i, pi, X4, g, P, sl, sk, n, pair_a);
+        else
+            neighbor_loop<PER, LT>(active, (int)i, pi, X4, start, g, P, lst, words, pair_a);
+    }
     if (inb) nlc[i] = active ? (unstored ? (int16_t)-1 : (int16_t)nstored) : (int16_t)0;
     if (!active) return;
     float m = P.m;
@@ -502,21 +579,22 @@ __device__ __forceinline__ void pass_a_tile(const Dom& D0, int64_t i, int64_t n,
 // One block handles 32 W consecutive slots: its warps sit in neighboring cells and share
 // most of their stencil data in L1.
 
-template <bool PER, bool BATCH, typename LT, int W>
+template <bool PER, bool BATCH, typename LT, int W, bool BUILD>
 __global__ void __launch_bounds__(32 * W) k_pass_a(const Dom D0, int64_t n, const float4* __restrict__ X4,
                                                    float4* __restrict__ V4, const int32_t* __restrict__ start,
                                                    const Dom* __restrict__ doms, const int32_t* __restrict__ did,
                                                    const int32_t* __restrict__ uid, RhsOut out,
                                                    uint32_t* __restrict__ words, int16_t* __restrict__ nl,
-                                                   int16_t* __restrict__ nlc) {
+                                                   int16_t* __restrict__ nlc, int skin_mode, int16_t* __restrict__ sl,
+                                                   int16_t* __restrict__ slc) {
     extern __shared__ __align__(16) unsigned char s_dyn[];
     __shared__ Dom s_dom[BATCH ? 2 : 1];
     __shared__ int s_id[2];
     LT* lst = reinterpret_cast<LT*>(s_dyn) + (threadIdx.x >> 5) * (kCap * 32);
     const int64_t first = (int64_t)blockIdx.x * (32 * W);
     if (BATCH) stage_doms(doms, did, first, first + 32 * W - 1, n, s_dom, s_id);
-    pass_a_tile<PER, BATCH, LT>(D0, first + threadIdx.x, n, X4, V4, start, doms, s_dom, s_id, did, uid, out, lst,
-                                words, nl, nlc);
+    pass_a_tile<PER, BATCH, LT, BUILD>(D0, first + threadIdx.x, n, X4, V4, start, doms, s_dom, s_id, did, uid, out,
+                                       lst, words, nl, nlc, skin_mode, sl, slc);
 }
 
 // ------------------------------------------------------------------------------------
@@ -635,6 +713,10 @@ __device__ __forceinline__ void pass_b_tile(const Dom& D0, int64_t i, int64_t n,
         float2 w = wrap_pos(xh, P.geo);
         X4o[i] = make_float4(w.x, w.y, rh, eos_p(rh, P.eos));
         V4o[i] = make_float4(u0, u1, 0.f, 0.f);
+        {  // the second pass A filters the skin list at these positions
+            const float e0 = xh.x - x.x, e1 = xh.y - x.y;
+            if (e0 * e0 + e1 * e1 > P.skin_lim * P.skin_lim) atomicOr(&words[3], 1u);
+        }
     } else {
         // v' = v + dudt dt; x' = x + 0.5 (v + v') dt; rho' per density_update
         float4 vn = V4n[i];
@@ -667,6 +749,8 @@ __device__ __forceinline__ void pass_b_tile(const Dom& D0, int64_t i, int64_t n,
         // (the shift clamp adds at most sqrt(2) thr dx, covered by the margin of verlet_lim)
         float e0 = xp.x - x.x, e1 = xp.y - x.y;
         if (sqrtf(e0 * e0 + e1 * e1) > P.verlet_lim) atomicOr(&words[0], SPH_FLAG_VERLET);
+        // the shift filters the skin list at these positions
+        if (e0 * e0 + e1 * e1 > P.skin_lim * P.skin_lim) atomicOr(&words[3], 1u);
     }
 }
 
@@ -703,7 +787,8 @@ __device__ __forceinline__ void shift_tile(const Dom& D0, int64_t i, int64_t n, 
                                            float4* __restrict__ V4o, uint32_t* __restrict__ words,
                                            const uint32_t* __restrict__ maxv, int enabled,
                                            const int32_t* __restrict__ uid, float* __restrict__ dx_out,
-                                           LT* __restrict__ lst) {
+                                           LT* __restrict__ lst, int use_skin, const int16_t* __restrict__ sl,
+                                           const int16_t* __restrict__ slc) {
     const int dom = BATCH ? dom_of(did, i, n) : 0;
     const Dom& D = BATCH ? dom_ref(doms, s_dom, s_id, dom) : D0;
     const Phys& P = D.P;
@@ -715,7 +800,7 @@ __device__ __forceinline__ void shift_tile(const Dom& D0, int64_t i, int64_t n, 
     float2 pi = make_float2(xi.x, xi.y);
     float rhoi = xi.z;
     float s0 = 0.f, s1 = 0.f;
-    neighbor_loop<PER, LT>(active, (int)i, pi, X4, start, g, P, lst, words, [&](int j) {
+    auto pair_s = [&](int j) {
         float4 xj = __ldg(&X4[j]);
         float x0, x1;
         pair_vec<PER>(pi, make_float2(xj.x, xj.y), P.geo, x0, x1);
@@ -727,7 +812,14 @@ __device__ __forceinline__ void shift_tile(const Dom& D0, int64_t i, int64_t n, 
         float c = (1.f + P.shR * kn) * __fdividef(1.0f, rhoi + fabsf(xj.z));
         s0 = fmaf(c, pg.xh0 * dW, s0);
         s1 = fmaf(c, pg.xh1 * dW, s1);
-    });
+    };
+    // the skin list of the step's first pass A holds every pair of the integrated positions
+    // unless a particle moved farther than skin_lim (flag set by the integrator)
+    const int sk = (!PER && use_skin && active) ? (int)slc[i] : 0;
+    if (!PER && use_skin && __all_sync(kFull, sk >= 0) && words[3] == 0u)
+        skin_loop<PER>((int)i, pi, X4, g, P, sl, sk, n, pair_s);
+    else
+        neighbor_loop<PER, LT>(active, (int)i, pi, X4, start, g, P, lst, words, pair_s);
     if (!inb) return;
     float4 vi = V4[i];
     if (!active) {
@@ -766,7 +858,9 @@ __global__ void __launch_bounds__(32 * W) k_shift(const Dom D0, int64_t n, const
                                                   float2* __restrict__ Xr, float4* __restrict__ X4o,
                                                   float4* __restrict__ V4o, uint32_t* __restrict__ words,
                                                   const uint32_t* __restrict__ maxv, int enabled,
-                                                  const int32_t* __restrict__ uid, float* __restrict__ dx_out) {
+                                                  const int32_t* __restrict__ uid, float* __restrict__ dx_out,
+                                                  int use_skin, const int16_t* __restrict__ sl,
+                                                  const int16_t* __restrict__ slc) {
     extern __shared__ __align__(16) unsigned char s_dyn[];
     __shared__ Dom s_dom[BATCH ? 2 : 1];
     __shared__ int s_id[2];
@@ -774,7 +868,7 @@ __global__ void __launch_bounds__(32 * W) k_shift(const Dom D0, int64_t n, const
     const int64_t first = (int64_t)blockIdx.x * (32 * W);
     if (BATCH) stage_doms(doms, did, first, first + 32 * W - 1, n, s_dom, s_id);
     shift_tile<PER, BATCH, LT>(D0, first + threadIdx.x, n, X4, V4, start, doms, s_dom, s_id, did, Xr, X4o, V4o,
-                               words, maxv, enabled, uid, dx_out, lst);
+                               words, maxv, enabled, uid, dx_out, lst, use_skin, sl, slc);
 }
 
 // max |u| over all particles (the Mach number of shifting.py:139-142)
@@ -1228,6 +1322,8 @@ struct sph_solver {
     uint32_t* words;  // [0] flags, [2] boundary count
     int16_t* nl;      // exact neighbor list of the last pass A: slot offsets, [kStoreCap][n]
     int16_t* nlc;     // its length per slot (-1: not stored)
+    int16_t* sl;      // skin list of the step's first pass A, [kSkinCap][n]
+    int16_t* slc;     // its length per slot (-1: not stored)
     uint32_t* maxv;   // per-domain max |u| (float bits)
     Dom* doms;
     int64_t* dom_off;
@@ -1296,9 +1392,13 @@ static size_t solver_layout(const sph_params_t* p, const int64_t* nF_d, int nd, 
     float* bdist = c.take<float>(nB);
     int16_t* nl = c.take<int16_t>((int64_t)kStoreCap * n);
     int16_t* nlc = c.take<int16_t>(n);
+    int16_t* sl = c.take<int16_t>((int64_t)kSkinCap * n);
+    int16_t* slc = c.take<int16_t>(n);
     if (S) {
         S->nl = nl;
         S->nlc = nlc;
+        S->sl = sl;
+        S->slc = slc;
         S->n = n;
         S->nF = nF;
         S->nB = nB;
@@ -1392,6 +1492,9 @@ static Phys make_phys(const sph_params_t* p, int64_t nF) {
     // displacement allowed between the sort and the last pass of the step; the shift clamp
     // (at most sqrt(2) threshold dx) is reserved out of the cell margin
     P.verlet_lim = (float)((p->skin - 1.0) * h - 1.5 * p->shift_threshold * p->dx);
+    // pairs within h later were within h + 2 D at the sort for displacements D <= skin_lim
+    P.T_skin = (float)((h * (1.0 + kSkinFrac)) * (h * (1.0 + kSkinFrac)) * (1.0 + 1e-4));
+    P.skin_lim = (float)(0.5 * kSkinFrac * h * 0.98);
     return P;
 }
 
@@ -1545,7 +1648,8 @@ static int rebuild(sph_solver* S, cudaStream_t st) {
         cudaSuccess)
         return SPH_ERR_CUDA;
     tend(S, KC_SORT, st);
-    if (cudaMemsetAsync(S->words + 2, 0, sizeof(uint32_t), st) != cudaSuccess) return SPH_ERR_CUDA;
+    // words[2]: boundary count of the gather; words[3]: skin-list validity of this sort
+    if (cudaMemsetAsync(S->words + 2, 0, 2 * sizeof(uint32_t), st) != cudaSuccess) return SPH_ERR_CUDA;
     tbeg(S, KC_GATHER, st);
     k_gather<<<blocks_for(S->n), kBlock, 0, st>>>(S->n, (int)S->nF, S->perm, S->Xr, S->Xc, S->Vc, S->uid, S->did,
                                                     S->Xr_t, S->Xt, S->Vt, S->uid_t, S->did_t, S->bidx, S->words);
@@ -1578,7 +1682,8 @@ static constexpr size_t list_bytes() { return (size_t)W * kCap * 32 * sizeof(LT)
 
 template <bool PER, bool BATCH, typename LT, int W>
 static void allow_lists_k(int b) {
-    cudaFuncSetAttribute(k_pass_a<PER, BATCH, LT, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+    cudaFuncSetAttribute(k_pass_a<PER, BATCH, LT, W, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+    cudaFuncSetAttribute(k_pass_a<PER, BATCH, LT, W, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
     cudaFuncSetAttribute(k_pass_b<PER, BATCH, 0, LT, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
     cudaFuncSetAttribute(k_pass_b<PER, BATCH, 1, LT, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
     cudaFuncSetAttribute(k_pass_b<PER, BATCH, 2, LT, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
@@ -1613,28 +1718,35 @@ static void set_attrs(sph_solver* S) {
     }
 
 template <bool PER, bool BATCH, typename LT, int W>
-static void launch_a_k(sph_solver* S, float4* X4, float4* V4, RhsOut o, cudaStream_t st) {
+static void launch_a_k(sph_solver* S, float4* X4, float4* V4, RhsOut o, int skin_mode, cudaStream_t st) {
     unsigned gb = (unsigned)((S->n + 32 * W - 1) / (32 * W));
-    k_pass_a<PER, BATCH, LT, W><<<gb, 32 * W, list_bytes<LT, W>(), st>>>(S->doms_host[0], S->n, X4, V4, S->start,
-                                                                        S->doms, dids(S), S->uid, o, S->words,
-                                                                        S->nl, S->nlc);
+    if (skin_mode == 0)
+        k_pass_a<PER, BATCH, LT, W, true><<<gb, 32 * W, list_bytes<LT, W>(), st>>>(
+            S->doms_host[0], S->n, X4, V4, S->start, S->doms, dids(S), S->uid, o, S->words, S->nl, S->nlc, skin_mode,
+            S->sl, S->slc);
+    else
+        k_pass_a<PER, BATCH, LT, W, false><<<gb, 32 * W, list_bytes<LT, W>(), st>>>(
+            S->doms_host[0], S->n, X4, V4, S->start, S->doms, dids(S), S->uid, o, S->words, S->nl, S->nlc, skin_mode,
+            S->sl, S->slc);
 }
 
 template <typename LT, int W>
-static void launch_a_t(sph_solver* S, float4* X4, float4* V4, RhsOut o, cudaStream_t st) {
+static void launch_a_t(sph_solver* S, float4* X4, float4* V4, RhsOut o, int skin_mode, cudaStream_t st) {
     if (S->nd > 1) {
-        if (S->periodic) launch_a_k<true, true, LT, W>(S, X4, V4, o, st);
-        else launch_a_k<false, true, LT, W>(S, X4, V4, o, st);
+        if (S->periodic) launch_a_k<true, true, LT, W>(S, X4, V4, o, skin_mode, st);
+        else launch_a_k<false, true, LT, W>(S, X4, V4, o, skin_mode, st);
     } else {
-        if (S->periodic) launch_a_k<true, false, LT, W>(S, X4, V4, o, st);
-        else launch_a_k<false, false, LT, W>(S, X4, V4, o, st);
+        if (S->periodic) launch_a_k<true, false, LT, W>(S, X4, V4, o, skin_mode, st);
+        else launch_a_k<false, false, LT, W>(S, X4, V4, o, skin_mode, st);
     }
 }
 
-static void launch_a(sph_solver* S, float4* X4, float4* V4, RhsOut o, cudaStream_t st) {
+// skin_mode: 0 keeps the skin list (first pass A after a sort), 1 filters it (second pass A
+// of the same step), 2 neither
+static void launch_a(sph_solver* S, float4* X4, float4* V4, RhsOut o, cudaStream_t st, int skin_mode = 2) {
     set_attrs(S);
     tbeg(S, KC_PASS_A, st);
-#define SPH_CALL_A(LT, W) launch_a_t<LT, W>(S, X4, V4, o, st)
+#define SPH_CALL_A(LT, W) launch_a_t<LT, W>(S, X4, V4, o, skin_mode, st)
     SPH_SHAPE_DISPATCH(S, SPH_CALL_A)
 #undef SPH_CALL_A
     tend(S, KC_PASS_A, st);
@@ -1675,11 +1787,14 @@ static int run_stages(sph_solver* S, cudaStream_t st) {
     if (rc) return rc;
     // stage 1 at t^n
     launch_mdbc(S, S->Xc, nullptr, st);
-    launch_a(S, S->Xc, S->Vc, none, st);
+    // skin list (non-periodic domains: there the stencil scan skips the minimum image on most
+    // ranges, which the skin filter cannot, and measured no faster)
+    const int skin = S->periodic ? 2 : 0;
+    launch_a(S, S->Xc, S->Vc, none, st, skin);
     launch_b<1>(S, S->Xc, S->Vc, none, S->Xh, S->Vh, st);
     // stage 2 at the half step; the epilogue also reduces max |u'| for the shifting Mach number
     launch_mdbc(S, S->Xh, nullptr, st);
-    launch_a(S, S->Xh, S->Vh, none, st);
+    launch_a(S, S->Xh, S->Vh, none, st, skin == 0 ? 1 : 2);
     if (cudaMemsetAsync(S->maxv, 0, sizeof(uint32_t) * S->nd, st) != cudaSuccess) return SPH_ERR_CUDA;
     launch_b<2>(S, S->Xh, S->Vh, none, S->Xf, S->Vf, st);
     return cudaGetLastError() == cudaSuccess ? SPH_OK : SPH_ERR_CUDA;
@@ -1687,30 +1802,32 @@ static int run_stages(sph_solver* S, cudaStream_t st) {
 
 template <bool PER, bool BATCH, typename LT, int W>
 static void launch_shift_k(sph_solver* S, float4* Xin, float4* Vin, float4* Xout, float4* Vout, float* dx_out,
-                           cudaStream_t st) {
+                           int use_skin, cudaStream_t st) {
     unsigned gb = (unsigned)((S->n + 32 * W - 1) / (32 * W));
     k_shift<PER, BATCH, LT, W><<<gb, 32 * W, list_bytes<LT, W>(), st>>>(S->doms_host[0], S->n, Xin, Vin, S->start,
                                                                        S->doms, dids(S), S->Xr, Xout, Vout, S->words,
-                                                                       S->maxv, S->prm.shift_on, S->uid, dx_out);
+                                                                       S->maxv, S->prm.shift_on, S->uid, dx_out,
+                                                                       use_skin, S->sl, S->slc);
 }
 
 template <typename LT, int W>
 static void launch_shift_t(sph_solver* S, float4* Xin, float4* Vin, float4* Xout, float4* Vout, float* dx_out,
-                           cudaStream_t st) {
+                           int use_skin, cudaStream_t st) {
     if (S->nd > 1) {
-        if (S->periodic) launch_shift_k<true, true, LT, W>(S, Xin, Vin, Xout, Vout, dx_out, st);
-        else launch_shift_k<false, true, LT, W>(S, Xin, Vin, Xout, Vout, dx_out, st);
+        if (S->periodic) launch_shift_k<true, true, LT, W>(S, Xin, Vin, Xout, Vout, dx_out, use_skin, st);
+        else launch_shift_k<false, true, LT, W>(S, Xin, Vin, Xout, Vout, dx_out, use_skin, st);
     } else {
-        if (S->periodic) launch_shift_k<true, false, LT, W>(S, Xin, Vin, Xout, Vout, dx_out, st);
-        else launch_shift_k<false, false, LT, W>(S, Xin, Vin, Xout, Vout, dx_out, st);
+        if (S->periodic) launch_shift_k<true, false, LT, W>(S, Xin, Vin, Xout, Vout, dx_out, use_skin, st);
+        else launch_shift_k<false, false, LT, W>(S, Xin, Vin, Xout, Vout, dx_out, use_skin, st);
     }
 }
 
+// use_skin: the skin list of this step's first pass A is valid for this sort (same step)
 static void launch_shift(sph_solver* S, float4* Xin, float4* Vin, float4* Xout, float4* Vout, float* dx_out,
-                         cudaStream_t st) {
+                         cudaStream_t st, int use_skin = 0) {
     set_attrs(S);
     tbeg(S, KC_SHIFT, st);
-#define SPH_CALL_S(LT, W) launch_shift_t<LT, W>(S, Xin, Vin, Xout, Vout, dx_out, st)
+#define SPH_CALL_S(LT, W) launch_shift_t<LT, W>(S, Xin, Vin, Xout, Vout, dx_out, use_skin, st)
     SPH_SHAPE_DISPATCH(S, SPH_CALL_S)
 #undef SPH_CALL_S
     tend(S, KC_SHIFT, st);
@@ -1720,8 +1837,8 @@ static int step_impl(sph_solver* S, int32_t n_steps, cudaStream_t st) {
     for (int it = 0; it < n_steps; ++it) {
         int rc = run_stages(S, st);
         if (rc) return rc;
-        // delta+ shifting at the integrated positions, on the same cell sort
-        launch_shift(S, S->Xf, S->Vf, S->Xc, S->Vc, nullptr, st);
+        // delta+ shifting at the integrated positions, on the same cell sort and skin list
+        launch_shift(S, S->Xf, S->Vf, S->Xc, S->Vc, nullptr, st, S->periodic ? 0 : 1);
         if (cudaGetLastError() != cudaSuccess) return SPH_ERR_CUDA;
     }
     return SPH_OK;
