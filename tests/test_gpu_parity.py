@@ -170,6 +170,31 @@ def test_full_step_matches_oracle(name, cfg, st):
                            r64["boundary"]["densities"], 1e-5, "boundary densities")
 
 
+@pytest.mark.parametrize("speed", [30.0, 45.0])
+def test_fast_flow_falls_back_from_the_skin_list(speed):
+    """Particles that move farther than the skin list allows (0.049 h since the sort) make
+    the passes that would filter it scan the stencil instead, inside the sort's 0.13 h bound:
+    at 30 m/s the step moves them about 0.07 h (the shift falls back), at 45 m/s the half step
+    already moves them 0.054 h (the second pass A falls back too). The step still matches
+    the oracle."""
+    cfg, st = scenes.dam_break(dx=1.0 / 32)
+    st = copy.deepcopy(st)
+    st["fluid"]["velocities"][:, 0] = np.float32(speed)
+    h = float(cfg["particle"]["support"])
+    assert 0.05 * h < speed * float(cfg["timestep"]["dt"]) < 0.125 * h
+    r32, _ = O.full_step(copy.deepcopy(st), _cfg32(cfg))
+    r64, _ = O.full_step(_as64(st), cfg)
+    sol = _solver(cfg, st)
+    sol.step(1)
+    sol.check()
+    got = sol.download()
+    a, b = r32["fluid"], r64["fluid"]
+    assert_fp32_parity(_np(got["velocities"]), a["velocities"], b["velocities"], 1e-4, "velocities")
+    assert_fp32_parity(_np(got["densities"]), a["densities"], b["densities"], 1e-5, "densities")
+    x0 = st["fluid"]["positions"]
+    assert_fp32_parity(_np(got["positions"]) - x0, a["positions"] - x0, b["positions"] - x0, 1e-4, "dx")
+
+
 def test_integrate_then_shift_equals_step():
     """The runner's two calls (integrate, solveShifting) give the fused step's result; the
     standalone shift re-sorts the particles, so sums differ only in summation order."""
