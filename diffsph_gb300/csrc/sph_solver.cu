@@ -264,9 +264,7 @@ constexpr int kStoreCap = 64;
 constexpr double kSkinFrac = 0.1;
 constexpr int kSkinCap = 80;
 
-struct NoCand {
-    __device__ __forceinline__ void operator()(int, float) const {}
-};
+
 
 template <typename LT>
 __device__ __forceinline__ bool fits(int d) {
@@ -283,11 +281,12 @@ __device__ __forceinline__ int list_slot(int self, int d, const Grid& g) {
     return j;
 }
 
-template <bool PER, typename LT, class F, class FC = NoCand>
+// SKIN: keep every candidate within the skin radius (T_skin) instead of the exact neighbors
+template <bool PER, typename LT, class F, bool SKIN = false>
 __device__ __forceinline__ void neighbor_loop(bool active, int self, float2 pi, const float4* __restrict__ X4,
                                               const int32_t* __restrict__ start, const Grid& g, const Phys& P,
-                                              LT* __restrict__ lst, uint32_t* __restrict__ words, F&& f,
-                                              FC fc = FC()) {
+                                              LT* __restrict__ lst, uint32_t* __restrict__ words, F&& f) {
+    const float thr = SKIN ? P.T_skin : P.T;
     const int lane = threadIdx.x & 31;
     int rs[kMaxRanges], re[kMaxRanges];
     unsigned wmask = 0;
@@ -312,9 +311,7 @@ __device__ __forceinline__ void neighbor_loop(bool active, int self, float2 pi, 
                         pair_vec<true>(pi, make_float2(xj[u].x, xj[u].y), P.geo, x0, x1);
                     else
                         pair_vec<false>(pi, make_float2(xj[u].x, xj[u].y), P.geo, x0, x1);
-                    const float sqc = sq_norm_ref(x0, x1);
-                    fc(s + u, sqc);
-                    if (sqc <= P.T) {
+                    if (sq_norm_ref(x0, x1) <= thr) {
                         int d = s + u - self;
                         if (PER) {  // shortest offset modulo the domain's slots
                             const int h2 = g.nslots >> 1;
@@ -381,62 +378,104 @@ __device__ __forceinline__ void skin_loop(int self, float2 pi, const float4* __r
 // ------------------------------------------------------------------------------------
 // mDBC boundary density (src/diffSPH/v2/modules/mDBC.py:9-36 ghosts, :50-163 density)
 // ------------------------------------------------------------------------------------
-template <bool PER>
-__global__ void k_mdbc(int nB, const int32_t* __restrict__ bidx, const int32_t* __restrict__ uid,
-                       const float2* __restrict__ Xr, float4* X4, const float2* __restrict__ bnormal,
-                       const float* __restrict__ bdist, const int32_t* __restrict__ start, Grid g, Phys P,
-                       float* __restrict__ rho_b_out) {
-    int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= nB) return;
-    int s = bidx[k];
-    int b = uid[s] - P.nF;
-    float2 xb = Xr[s];
-    float2 nrm = bnormal[b];
-    float d = bdist[b];
+// Two kernels: one warp per wall particle sums the 13 moments of its ghost, its lanes
+// striding over the candidates of all stencil ranges (a fixed shuffle tree combines them);
+// then one thread per wall particle solves the fp64 3x3 system, 32 wall particles per warp.
+constexpr int kMdbcSums = 16;  // 13 used: num, den, gs0, gs1, vg0, vg1, ps0, ps1, pm00, pm01, pm10, pm11, count
+
+__device__ __forceinline__ float2 mdbc_ghost(const Phys& P, float2 xb, float2 nrm, float d) {
     // mappingDistance = d + max(d, -h); ghost = x_b + mappingDistance * n
     float mapd = __fadd_rn(d, fmaxf(d, -P.h));
-    float2 gp = make_float2(__fadd_rn(xb.x, __fmul_rn(mapd, nrm.x)), __fadd_rn(xb.y, __fmul_rn(mapd, nrm.y)));
-    float2 gw = wrap_pos(gp, P.geo);
+    return make_float2(__fadd_rn(xb.x, __fmul_rn(mapd, nrm.x)), __fadd_rn(xb.y, __fmul_rn(mapd, nrm.y)));
+}
+
+template <bool PER>
+__global__ void __launch_bounds__(128) k_mdbc_sums(int nB, const int32_t* __restrict__ bidx,
+                                                   const int32_t* __restrict__ uid, const float2* __restrict__ Xr,
+                                                   const float4* __restrict__ X4, const float2* __restrict__ bnormal,
+                                                   const float* __restrict__ bdist,
+                                                   const int32_t* __restrict__ start, Grid g, Phys P,
+                                                   float* __restrict__ sums) {
+    const int lane = threadIdx.x & 31;
+    const int k = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (k >= nB) return;  // warp-uniform
+    const int s = bidx[k];
+    const int b = uid[s] - P.nF;
+    const float2 gp = mdbc_ghost(P, Xr[s], bnormal[b], bdist[b]);
+    const float2 gw = wrap_pos(gp, P.geo);
     int rs[kMaxRanges], re[kMaxRanges];
-    int nr = stencil_ranges(gw, g, start, rs, re);
-    float num = 0.f, den = 0.f, gs0 = 0.f, gs1 = 0.f, vg0 = 0.f, vg1 = 0.f, ps0 = 0.f, ps1 = 0.f;
-    float pm00 = 0.f, pm01 = 0.f, pm10 = 0.f, pm11 = 0.f;
-    int cnt = 0;
-    for (int a = 0; a < nr; ++a) {
-        for (int j = rs[a]; j < re[a]; ++j) {
-            float4 xj = __ldg(&X4[j]);
-            if (is_boundary(xj.z)) continue;
-            float x0, x1;
-            pair_vec<PER>(gw, make_float2(xj.x, xj.y), P.geo, x0, x1);
-            float sq = sq_norm_ref(x0, x1);
-            if (sq > P.T) continue;
-            PairG pg = pair_fast(x0, x1, sq, P.inv_h);
-            float W = wendland_w(pg.q, P.kc);
-            float dW = wendland_dw(pg.q, P.kc);
-            float g0 = pg.xh0 * dW, g1 = pg.xh1 * dW;
-            float V = P.m / xj.z;
-            num += P.m * W;
-            den += V * W;
-            float k0 = V * g0, k1 = V * g1;
-            gs0 += xj.z * k0;
-            gs1 += xj.z * k1;
-            vg0 += k0;
-            vg1 += k1;
-            float xr = -pg.q * P.h;
-            float xi0 = pg.xh0 * xr, xi1 = pg.xh1 * xr;
-            float vw = V * W;
-            ps0 += xi0 * vw;
-            ps1 += xi1 * vw;
-            pm00 += xi0 * k0;
-            pm01 += xi0 * k1;
-            pm10 += xi1 * k0;
-            pm11 += xi1 * k1;
-            ++cnt;
+    const int nr = stencil_ranges(gw, g, start, rs, re);
+    int total = 0;
+    for (int a = 0; a < nr; ++a) total += re[a] - rs[a];
+    float acc[13];
+#pragma unroll
+    for (int q = 0; q < 13; ++q) acc[q] = 0.f;
+    int r = 0, base = 0;  // range of the lane's current flat index and the flat start of that range
+    for (int t = lane; t < total; t += 32) {
+        while (t >= base + (re[r] - rs[r])) {
+            base += re[r] - rs[r];
+            ++r;
         }
+        const int j = rs[r] + (t - base);
+        const float4 xj = __ldg(&X4[j]);
+        if (is_boundary(xj.z)) continue;
+        float x0, x1;
+        pair_vec<PER>(gw, make_float2(xj.x, xj.y), P.geo, x0, x1);
+        const float sq = sq_norm_ref(x0, x1);
+        if (sq > P.T) continue;
+        const PairG pg = pair_fast(x0, x1, sq, P.inv_h);
+        const float W = wendland_w(pg.q, P.kc);
+        const float dW = wendland_dw(pg.q, P.kc);
+        const float g0 = pg.xh0 * dW, g1 = pg.xh1 * dW;
+        const float V = P.m / xj.z;
+        const float k0 = V * g0, k1 = V * g1;
+        const float xr = -pg.q * P.h;
+        const float xi0 = pg.xh0 * xr, xi1 = pg.xh1 * xr;
+        const float vw = V * W;
+        acc[0] += P.m * W;
+        acc[1] += vw;
+        acc[2] += xj.z * k0;
+        acc[3] += xj.z * k1;
+        acc[4] += k0;
+        acc[5] += k1;
+        acc[6] += xi0 * vw;
+        acc[7] += xi1 * vw;
+        acc[8] += xi0 * k0;
+        acc[9] += xi0 * k1;
+        acc[10] += xi1 * k0;
+        acc[11] += xi1 * k1;
+        acc[12] += 1.f;
     }
+#pragma unroll
+    for (int q = 0; q < 13; ++q) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) acc[q] += __shfl_xor_sync(kFull, acc[q], o);
+    }
+    if (lane < 13) {
+        float v = acc[0];
+#pragma unroll
+        for (int q = 1; q < 13; ++q)
+            if (lane == q) v = acc[q];
+        sums[(int64_t)k * kMdbcSums + lane] = v;
+    }
+}
+
+__global__ void k_mdbc_solve(int nB, const int32_t* __restrict__ bidx, const int32_t* __restrict__ uid,
+                             const float2* __restrict__ Xr, float4* X4, const float2* __restrict__ bnormal,
+                             const float* __restrict__ bdist, Phys P, const float* __restrict__ sums,
+                             float* __restrict__ rho_b_out) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nB) return;
+    const int s = bidx[k];
+    const int b = uid[s] - P.nF;
+    const float2 xb = Xr[s];
+    const float2 gp = mdbc_ghost(P, xb, bnormal[b], bdist[b]);
+    const float* a = sums + (int64_t)k * kMdbcSums;
+    const float num = a[0], den = a[1], gs0 = a[2], gs1 = a[3];
+    const int cnt = (int)a[12];
     float rho;
     if (cnt > 5) {
-        double A[9] = {den, ps0, ps1, vg0, pm00, pm01, vg1, pm10, pm11};
+        double A[9] = {den, a[6], a[7], a[4], a[8], a[9], a[5], a[10], a[11]};
         double Pi[9];
         pinv3_f64(A, Pi, 3.0 * 1.1920928955078125e-07);
         double r0 = Pi[0] * num + Pi[1] * gs0 + Pi[2] * gs1;
@@ -528,24 +567,25 @@ __device__ __forceinline__ void pass_a_tile(const Dom& D0, int64_t i, int64_t n,
     // every lane of the warp (no overflow, displacements within skin_lim) and skin_mode 2
     // scans.
     if (BUILD && !PER) {
+        // the scan's list holds the skin candidates; each flush stores them (lanes flush their
+        // k-th entries together, so the stores coalesce) and passes the exact ones on, in
+        // scan order
         int ns = 0;
         bool sbad = false;
-        auto keep = [&](int slot, float sq) {
-            if (sq <= P.T_skin) {
-                int d = slot - (int)i;
-                if (PER) {
-                    const int h2 = g.nslots >> 1;
-                    if (d > h2) d -= g.nslots;
-                    else if (d < -h2) d += g.nslots;
-                }
-                if (ns < kSkinCap && d >= -32768 && d <= 32767)
-                    sl[(int64_t)ns * n + i] = (int16_t)d;
-                else
-                    sbad = true;
-                ++ns;
-            }
+        auto skin_then_exact = [&](int j) {
+            const int d = j - (int)i;
+            if (ns < kSkinCap && d >= -32768 && d <= 32767)
+                sl[(int64_t)ns * n + i] = (int16_t)d;
+            else
+                sbad = true;
+            ++ns;
+            const float4 xj = __ldg(&X4[j]);
+            float x0, x1;
+            pair_vec<PER>(pi, make_float2(xj.x, xj.y), P.geo, x0, x1);
+            if (sq_norm_ref(x0, x1) <= P.T) pair_a(j);
         };
-        neighbor_loop<PER, LT>(active, (int)i, pi, X4, start, g, P, lst, words, pair_a, keep);
+        neighbor_loop<PER, LT, decltype(skin_then_exact)&, true>(active, (int)i, pi, X4, start, g, P, lst, words,
+                                                                 skin_then_exact);
         if (inb) slc[i] = active ? (sbad ? (int16_t)-1 : (int16_t)ns) : (int16_t)0;
     } else {
         // (periodic domains never use the skin list: the branch compiles away for them)
@@ -1324,6 +1364,7 @@ struct sph_solver {
     int16_t* nlc;     // its length per slot (-1: not stored)
     int16_t* sl;      // skin list of the step's first pass A, [kSkinCap][n]
     int16_t* slc;     // its length per slot (-1: not stored)
+    float* msums;     // mDBC ghost moments, [nB][kMdbcSums]
     uint32_t* maxv;   // per-domain max |u| (float bits)
     Dom* doms;
     int64_t* dom_off;
@@ -1394,7 +1435,9 @@ static size_t solver_layout(const sph_params_t* p, const int64_t* nF_d, int nd, 
     int16_t* nlc = c.take<int16_t>(n);
     int16_t* sl = c.take<int16_t>((int64_t)kSkinCap * n);
     int16_t* slc = c.take<int16_t>(n);
+    float* msums = c.take<float>(nB * kMdbcSums);
     if (S) {
+        S->msums = msums;
         S->nl = nl;
         S->nlc = nlc;
         S->sl = sl;
@@ -1668,12 +1711,15 @@ static void launch_mdbc(sph_solver* S, float4* X4, float* rho_b_out, cudaStream_
     if (S->nB == 0) return;
     tbeg(S, KC_MDBC, st);
     const Dom& D = S->doms_host[0];
+    const unsigned gw = (unsigned)((S->nB + 3) / 4);
     if (S->periodic)
-        k_mdbc<true><<<blocks_for(S->nB), kBlock, 0, st>>>((int)S->nB, S->bidx, S->uid, S->Xr, X4, S->bnormal,
-                                                           S->bdist, S->start, D.g, D.P, rho_b_out);
+        k_mdbc_sums<true><<<gw, 128, 0, st>>>((int)S->nB, S->bidx, S->uid, S->Xr, X4, S->bnormal, S->bdist, S->start,
+                                              D.g, D.P, S->msums);
     else
-        k_mdbc<false><<<blocks_for(S->nB), kBlock, 0, st>>>((int)S->nB, S->bidx, S->uid, S->Xr, X4, S->bnormal,
-                                                            S->bdist, S->start, D.g, D.P, rho_b_out);
+        k_mdbc_sums<false><<<gw, 128, 0, st>>>((int)S->nB, S->bidx, S->uid, S->Xr, X4, S->bnormal, S->bdist, S->start,
+                                               D.g, D.P, S->msums);
+    k_mdbc_solve<<<blocks_for(S->nB), kBlock, 0, st>>>((int)S->nB, S->bidx, S->uid, S->Xr, X4, S->bnormal, S->bdist,
+                                                       D.P, S->msums, rho_b_out);
     tend(S, KC_MDBC, st);
 }
 
@@ -2053,8 +2099,8 @@ extern "C" int sph_solver_flags(sph_solver_t* S, uint32_t* flags_host, sph_strea
 
 extern "C" int sph_solver_launches_per_step(const sph_solver_t* S) {
     if (!S) return -1;
-    // cell keys, scan (3), scatter, cell order, gather, 2 x (mdbc?, pass A, pass B), shift
-    return 7 + 2 * ((S->nB > 0 ? 1 : 0) + 2) + 1;
+    // cell keys, scan (3), scatter, cell order, gather, 2 x (mdbc moments and solve?, pass A, pass B), shift
+    return 7 + 2 * ((S->nB > 0 ? 2 : 0) + 2) + 1;
 }
 
 extern "C" int sph_solver_kernel_classes(void) { return KC_COUNT; }
