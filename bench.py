@@ -8,7 +8,8 @@ device-resident state larger than L2 (so no L2 flush between steps).
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload NAME]
 
 Prints one JSON line. ``--impl reference`` times the CPU restatement of the reference's
-step (the oracle) on the host cores on a bounded sample of the same workload.
+step (the oracle) on all host cores (one process per core) on a bounded sample of the same
+workload.
 """
 from __future__ import annotations
 
@@ -160,34 +161,68 @@ def run_reference(args):
     if WORKLOADS[args.workload]["scene"] == "learned":
         print(json.dumps({"impl": "reference", "unavailable": "the reference has no learned model"}))
         return
+    import multiprocessing as mp
     from oracle import sph_oracle as O
-    from diffsph_gb300 import scenes
+    O.build_oracle()  # once, before the workers load it
     sc = WORKLOADS[args.workload]["scene"]
-    if sc == "dam_break":
-        cfg, st = scenes.dam_break(dx=1.0 / 64)
-    elif sc == "batched":
-        cfg, st = scenes.batched_fourier(1, seed=0, n_min=4096, n_max=4096)[0]
-    else:
-        cfg, st = make_scene(args.workload)
-    n = st["fluid"]["positions"].shape[0]
-    s = copy.deepcopy(st)
-    for _ in range(warm):
-        s, _ = O.full_step(s, cfg)
-    t0 = time.perf_counter()
-    for _ in range(steps):
-        s, _ = O.full_step(s, cfg)
-    dt = time.perf_counter() - t0
-    v = n * steps / dt
+    # one single-threaded oracle process per host core, each on its own copy of the sample;
+    # they start their timed steps together (barrier) and the throughput is the particle-steps
+    # of all of them over the span from the first start to the last end
+    nproc = max(1, min(os.cpu_count() or 1, 64))
+    for var in ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS"):
+        os.environ[var] = "1"
+    ctx = mp.get_context("spawn")
+    barrier = ctx.Barrier(nproc)
+    queue = ctx.Queue()
+    procs = [ctx.Process(target=_reference_worker, args=(args.workload, steps, warm, barrier, queue))
+             for _ in range(nproc)]
+    for p in procs:
+        p.start()
+    res = [queue.get() for _ in procs]
+    for p in procs:
+        p.join()
+    n = res[0][0]
+    t_start = min(r[1] for r in res)
+    t_end = max(r[2] for r in res)
+    dt = t_end - t_start
+    v = nproc * n * steps / dt
     line = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": "particle-steps/s", "n_gpus": args.gpus,
         "steps": steps, "warmup": warm, "ms_per_step": 1e3 * dt / steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": args.workload, "sample": f"{sc} sample, {n} fluid particles"},
-        "cpu_baseline": {"value": v, "unit": "particle-steps/s", "cores": 1, "kind": "port",
-                         "sample": f"{n} fluid particles x {steps} steps"},
+        "config": {"workload": args.workload,
+                   "sample": f"{sc} sample, {n} fluid particles, one copy per host core"},
+        "cpu_baseline": {"value": v, "unit": "particle-steps/s", "cores": nproc, "kind": "port",
+                         "sample": f"{nproc} processes x {n} fluid particles x {steps} steps"},
         "e2e": {"value": v, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
+
+
+def _reference_sample(workload):
+    from diffsph_gb300 import scenes
+    sc = WORKLOADS[workload]["scene"]
+    if sc == "dam_break":
+        return scenes.dam_break(dx=1.0 / 64)
+    if sc == "batched":
+        return scenes.batched_fourier(1, seed=0, n_min=4096, n_max=4096)[0]
+    return make_scene(workload)
+
+
+def _reference_worker(workload, steps, warm, barrier, queue):
+    """One oracle process of the reference arm (spawned; no GPU use)."""
+    from oracle import sph_oracle as O
+    cfg, st = _reference_sample(workload)
+    n = st["fluid"]["positions"].shape[0]
+    s = copy.deepcopy(st)
+    for _ in range(warm):
+        s, _ = O.full_step(s, cfg)
+    barrier.wait()
+    t0 = time.monotonic()
+    for _ in range(steps):
+        s, _ = O.full_step(s, cfg)
+    t1 = time.monotonic()
+    queue.put((n, t0, t1))
 
 
 def reduce_max(value, world):
