@@ -154,8 +154,9 @@ def _with_nu(config, nu):
     return cfg
 
 
-def _forward(sol, x0, u0, rho0, n_steps, every, shift):
+def _forward(sol, x0, u0, rho0, n_steps, every, shift, use_graphs=False):
     """Fused forward; returns the final state and the checkpoints {step: (x, u, rho)}."""
+    graphed = use_graphs and shift and torch.cuda.current_stream().cuda_stream != 0
     ckpt = {}
     sol.upload(_state(x0, u0, rho0))
     k = 0
@@ -163,7 +164,11 @@ def _forward(sol, x0, u0, rho0, n_steps, every, shift):
         got = sol.download()
         ckpt[k] = (got["positions"], got["velocities"], got["densities"])
         m = min(every, n_steps - k)
-        if shift:
+        if graphed and m >= 2:
+            sol.graph_step(m - (m & 1))  # the graph replays an even number of steps
+            if m & 1:
+                sol.step(1)
+        elif shift:
             sol.step(m)
         else:
             for _ in range(m):
@@ -174,19 +179,101 @@ def _forward(sol, x0, u0, rho0, n_steps, every, shift):
     return (got["positions"], got["velocities"], got["densities"]), ckpt
 
 
-def _backward(sol, C, ckpt, n_steps, every, shift, xbar, ubar, rbar):
+def _flat(st):
+    (x, u, rho), (xh, uh, rh), (x1, u1, r1), (x2, u2, r2), dr = st
+    return [x, u, rho, xh, uh, rh, x1, u1, r1, x2, u2, r2, dr]
+
+
+def _unflat(t):
+    return (tuple(t[0:3]), tuple(t[3:6]), tuple(t[6:9]), tuple(t[9:12]), t[12])
+
+
+class _Replay:
+    """A CUDA graph of fn over static input tensors, which each call copies in first.
+
+    Every solver call inside fn re-sorts the particles and swaps the solver's buffer
+    pointers on the host; a graph bakes those pointers in, so fn must re-sort an even
+    number of times (the callers group steps accordingly)."""
+
+    def __init__(self, fn, inputs):
+        self.inputs = [t.clone() for t in inputs]
+        side = torch.cuda.Stream()
+        side.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(side):
+            fn(*self.inputs)  # first-call set-up (attributes, tables) outside the capture
+        torch.cuda.current_stream().wait_stream(side)
+        self.graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(self.graph):
+            self.outputs = fn(*self.inputs)
+
+    def __call__(self, *args):
+        for dst, src in zip(self.inputs, args):
+            dst.copy_(src)
+        self.graph.replay()
+        return self.outputs
+
+
+class _Graphs:
+    """Graphed recomputation of stage states (two steps per graph) and graphed step VJPs
+    (one step per graph when its re-sort count is even, else two)."""
+
+    def __init__(self, sol, C, shift):
+        self.sol, self.C, self.shift = sol, C, shift
+        self._rec = None
+        self._vjp = None
+        sorts = (1 if shift else 0) + 3 + (1 if C.rational else 0)
+        self.group = 1 if sorts % 2 == 0 else 2
+
+    def two_steps(self, x, u, rho):
+        if self._rec is None:
+            def fn(x, u, rho):
+                a = step_stages(self.sol, self.C, x, u, rho, self.shift)
+                b = step_stages(self.sol, self.C, *a[3], self.shift)
+                return _flat(a) + _flat(b)
+            self._rec = _Replay(fn, [x, u, rho])
+        out = [t.clone() for t in self._rec(x, u, rho)]
+        return _unflat(out[:13]), _unflat(out[13:])
+
+    def vjp(self, tapes, xbar, ubar, rbar):
+        if self._vjp is None:
+            G = self.group
+
+            def fn(*args):
+                xb, ub, rb = args[13 * G:]
+                nb = torch.zeros((), dtype=torch.float64, device=xb.device)
+                for g in reversed(range(G)):
+                    xb, ub, rb, n1 = step_vjp(self.sol, self.C, _unflat(args[13 * g:13 * (g + 1)]), xb, ub, rb,
+                                              self.shift)
+                    nb = nb + n1
+                return xb, ub, rb, nb
+            self._vjp = _Replay(fn, [t for st in tapes for t in _flat(st)] + [xbar, ubar, rbar])
+        out = self._vjp(*([t for st in tapes for t in _flat(st)] + [xbar, ubar, rbar]))
+        return tuple(t.clone() for t in out)
+
+
+def _backward(sol, C, ckpt, n_steps, every, shift, xbar, ubar, rbar, graphs=None):
     nubar = torch.zeros((), dtype=torch.float64, device=xbar.device)
     for k0 in sorted(ckpt, reverse=True):
         m = min(every, n_steps - k0)
         x, u, rho = ckpt[k0]
         tape = []
-        for _ in range(m):
+        while graphs is not None and m - len(tape) >= 2:
+            a, b = graphs.two_steps(x, u, rho)
+            tape += [a, b]
+            x, u, rho = b[3]
+        while len(tape) < m:
             st = step_stages(sol, C, x, u, rho, shift)
             tape.append(st)
             x, u, rho = st[3]
-        for st in reversed(tape):
-            xbar, ubar, rbar, nb = step_vjp(sol, C, st, xbar, ubar, rbar, shift)
+        i = len(tape)
+        while graphs is not None and i >= graphs.group:
+            xbar, ubar, rbar, nb = graphs.vjp(tape[i - graphs.group:i], xbar, ubar, rbar)
             nubar += nb
+            i -= graphs.group
+        while i > 0:
+            xbar, ubar, rbar, nb = step_vjp(sol, C, tape[i - 1], xbar, ubar, rbar, shift)
+            nubar += nb
+            i -= 1
     return xbar, ubar, rbar, nubar
 
 
@@ -195,15 +282,17 @@ class Rollout(torch.autograd.Function):
     all four inputs through the VJP kernels with segment checkpointing."""
 
     @staticmethod
-    def forward(ctx, x0, u0, rho0, nu, config, n_steps, every, shift, fluid_extra):
+    def forward(ctx, x0, u0, rho0, nu, config, n_steps, every, shift, fluid_extra, use_graphs=True):
         _check_scope(config)
         cfg = _with_nu(config, float(nu))
         fluid = dict(fluid_extra)
         fluid.update(_state(x0.detach(), u0.detach(), rho0.detach()))
         sol = Solver(cfg, fluid)
-        (x, u, rho), ckpt = _forward(sol, x0.detach(), u0.detach(), rho0.detach(), n_steps, every, shift)
+        (x, u, rho), ckpt = _forward(sol, x0.detach(), u0.detach(), rho0.detach(), n_steps, every, shift,
+                                     use_graphs)
         ctx.sol, ctx.ckpt, ctx.C = sol, ckpt, _Consts(cfg)
         ctx.n_steps, ctx.every, ctx.shift = n_steps, every, shift
+        ctx.use_graphs = use_graphs
         ctx.nu_dtype, ctx.nu_device = nu.dtype, nu.device
         return x, u, rho
 
@@ -214,15 +303,18 @@ class Rollout(torch.autograd.Function):
         xbar = (gx if gx is not None else torch.zeros(n, 2, device=dev)).float().contiguous().clone()
         ubar = (gu if gu is not None else torch.zeros(n, 2, device=dev)).float().contiguous().clone()
         rbar = (gr if gr is not None else torch.zeros(n, device=dev)).float().contiguous().clone()
+        graphs = _Graphs(ctx.sol, ctx.C, ctx.shift) if ctx.use_graphs else None
         xbar, ubar, rbar, nubar = _backward(ctx.sol, ctx.C, ctx.ckpt, ctx.n_steps, ctx.every, ctx.shift,
-                                            xbar, ubar, rbar)
+                                            xbar, ubar, rbar, graphs)
         nub = nubar.to(device=ctx.nu_device, dtype=ctx.nu_dtype)
-        return xbar, ubar, rbar, nub, None, None, None, None, None
+        return xbar, ubar, rbar, nub, None, None, None, None, None, None
 
 
-def rollout(config, fluid, n_steps, nu=None, checkpoint_every=25, shift=True, x0=None, u0=None, rho0=None):
+def rollout(config, fluid, n_steps, nu=None, checkpoint_every=25, shift=True, x0=None, u0=None, rho0=None,
+            use_graphs=True):
     """Differentiable rollout of ``n_steps`` steps. Tensors x0 / u0 / rho0 / nu (defaults:
-    the fluid dict's fields and config['diffusion']['nu']) may require grad."""
+    the fluid dict's fields and config['diffusion']['nu']) may require grad. use_graphs
+    replays the forward steps and the backward pass from CUDA graphs (same results)."""
     _check_scope(config)
     dev = "cuda"
 
@@ -235,14 +327,16 @@ def rollout(config, fluid, n_steps, nu=None, checkpoint_every=25, shift=True, x0
     if nu is None:
         nu = torch.tensor(float(config["diffusion"]["nu"]), dtype=torch.float64)
     extra = {k: fluid[k] for k in ("masses", "supports") if k in fluid}
-    return Rollout.apply(x0, u0, rho0, nu, config, int(n_steps), int(checkpoint_every), bool(shift), extra)
+    return Rollout.apply(x0, u0, rho0, nu, config, int(n_steps), int(checkpoint_every), bool(shift), extra,
+                         bool(use_graphs))
 
 
-def rollout_loss_and_grad(config, fluid, target_u, n_steps, checkpoint_every=25, shift=True):
+def rollout_loss_and_grad(config, fluid, target_u, n_steps, checkpoint_every=25, shift=True, use_graphs=True):
     """Loss = mean((u_n - target)^2) over all velocity components; returns (loss, du0, dnu)."""
     u0 = torch.as_tensor(fluid["velocities"]).to("cuda", torch.float32).clone().requires_grad_(True)
     nu = torch.tensor(float(config["diffusion"]["nu"]), dtype=torch.float64, requires_grad=True)
-    _, u, _ = rollout(config, fluid, n_steps, nu=nu, checkpoint_every=checkpoint_every, shift=shift, u0=u0)
+    _, u, _ = rollout(config, fluid, n_steps, nu=nu, checkpoint_every=checkpoint_every, shift=shift, u0=u0,
+                      use_graphs=use_graphs)
     tgt = torch.as_tensor(target_u).to("cuda", torch.float32)
     loss = torch.mean((u - tgt) ** 2)
     loss.backward()

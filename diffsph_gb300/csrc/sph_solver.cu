@@ -1375,8 +1375,13 @@ struct sph_solver {
     bool attrs_set = false;
     bool tables_uploaded = false;
     // captured step graph
-    cudaGraphExec_t graph = nullptr;
-    int graph_steps = 0;
+    // captured step graphs, keyed by step count and buffer assignment (two slots: eager
+    // steps between replays alternate the assignment)
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    int graph_n[2] = {0, 0};
+    const void* graph_key[2][14] = {};
+    int graph_next = 0;
+
     // timing
     uint32_t timing_mask = 0;
     struct Ev {
@@ -1631,7 +1636,8 @@ extern "C" int sph_batch_create(const sph_params_t* params, const int64_t* n_flu
 
 extern "C" void sph_solver_destroy(sph_solver_t* s) {
     if (!s) return;
-    if (s->graph) cudaGraphExecDestroy(s->graph);
+    for (int k = 0; k < 2; ++k)
+        if (s->graph[k]) cudaGraphExecDestroy(s->graph[k]);
     for (auto& e : s->pool) {
         cudaEventDestroy(e.a);
         cudaEventDestroy(e.b);
@@ -1902,27 +1908,35 @@ extern "C" int sph_solver_graph_step(sph_solver_t* S, int32_t n_steps, sph_strea
     if (!S || n_steps < 2 || (n_steps & 1)) return SPH_ERR_ARGUMENT;
     cudaStream_t st = (cudaStream_t)stream;
     if (st == nullptr) return SPH_ERR_ARGUMENT;  // the legacy default stream cannot be captured
-    if (S->graph && S->graph_steps != n_steps) {
-        cudaGraphExecDestroy(S->graph);
-        S->graph = nullptr;
+    // a graph bakes in which buffer holds the current state; eager steps, integrate and
+    // shift rotate the assignment, so graphs are keyed by it as well as by the step count
+    const void* bufs[14] = {S->Xr, S->Xr_t, S->Xc, S->Xh, S->Xf, S->Xt, S->Vc,
+                            S->Vh, S->Vf, S->Vt, S->uid, S->uid_t, S->did, S->did_t};
+    for (int k = 0; k < 2; ++k)
+        if (S->graph[k] && S->graph_n[k] == n_steps && memcmp(bufs, S->graph_key[k], sizeof(bufs)) == 0)
+            return cudaGraphLaunch(S->graph[k], st) == cudaSuccess ? SPH_OK : SPH_ERR_CUDA;
+    const int slot = S->graph_next;
+    if (S->graph[slot]) {
+        cudaGraphExecDestroy(S->graph[slot]);
+        S->graph[slot] = nullptr;
     }
-    if (!S->graph) {
-        set_attrs(S);
-        uint32_t mask = S->timing_mask;
-        S->timing_mask = 0;
-        cudaGraph_t g = nullptr;
-        if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return SPH_ERR_CUDA;
-        int rc = step_impl(S, n_steps, st);
-        cudaError_t e = cudaStreamEndCapture(st, &g);
-        S->timing_mask = mask;
-        if (rc) return rc;
-        if (e != cudaSuccess || !g) return SPH_ERR_CUDA;
-        e = cudaGraphInstantiate(&S->graph, g, 0);
-        cudaGraphDestroy(g);
-        if (e != cudaSuccess) return SPH_ERR_CUDA;
-        S->graph_steps = n_steps;
-    }
-    return cudaGraphLaunch(S->graph, st) == cudaSuccess ? SPH_OK : SPH_ERR_CUDA;
+    set_attrs(S);
+    uint32_t mask = S->timing_mask;
+    S->timing_mask = 0;
+    cudaGraph_t g = nullptr;
+    if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return SPH_ERR_CUDA;
+    int rc = step_impl(S, n_steps, st);
+    cudaError_t e = cudaStreamEndCapture(st, &g);
+    S->timing_mask = mask;
+    if (rc) return rc;
+    if (e != cudaSuccess || !g) return SPH_ERR_CUDA;
+    e = cudaGraphInstantiate(&S->graph[slot], g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return SPH_ERR_CUDA;
+    S->graph_n[slot] = n_steps;
+    memcpy(S->graph_key[slot], bufs, sizeof(bufs));
+    S->graph_next = 1 - slot;
+    return cudaGraphLaunch(S->graph[slot], st) == cudaSuccess ? SPH_OK : SPH_ERR_CUDA;
 }
 
 extern "C" int sph_solver_integrate(sph_solver_t* S, sph_stream_t stream) {
@@ -1982,9 +1996,9 @@ extern "C" int sph_solver_autotune(sph_solver_t* S, int32_t* shape_out, float* m
     cudaEventDestroy(b);
     S->shape = best_shape;
     S->timing_mask = saved_mask;
-    if (S->graph) {  // a captured graph holds the old shape's kernels
-        cudaGraphExecDestroy(S->graph);
-        S->graph = nullptr;
+    for (int k = 0; k < 2; ++k) {  // a captured graph holds the old shape's kernels
+        if (S->graph[k]) cudaGraphExecDestroy(S->graph[k]);
+        S->graph[k] = nullptr;
     }
     if (shape_out) *shape_out = best_shape;
     return cudaGetLastError() == cudaSuccess ? SPH_OK : SPH_ERR_CUDA;
@@ -2111,9 +2125,9 @@ extern "C" int sph_solver_set_shape(sph_solver_t* S, int32_t shape) {
     if (!S || shape < 0 || shape >= kNumShapes) return SPH_ERR_ARGUMENT;
     if (kShapes[shape].list16 && !S->list16) return SPH_ERR_ARGUMENT;
     S->shape = shape;
-    if (S->graph) {
-        cudaGraphExecDestroy(S->graph);
-        S->graph = nullptr;
+    for (int k = 0; k < 2; ++k) {
+        if (S->graph[k]) cudaGraphExecDestroy(S->graph[k]);
+        S->graph[k] = nullptr;
     }
     return SPH_OK;
 }

@@ -163,9 +163,10 @@ int sph_solver_upload(sph_solver_t* s, const float* x_fluid, const float* u_flui
 /* Advances n_steps full time steps (integrate + shifting, fused). */
 int sph_solver_step(sph_solver_t* s, int32_t n_steps, sph_stream_t stream);
 
-/* Same as sph_solver_step, replayed from a CUDA graph captured on the first call (and
- * re-captured when n_steps changes or the launch shape is changed). n_steps must be even
- * and stream must not be the legacy default stream. */
+/* Same as sph_solver_step, replayed from a CUDA graph captured on first use. The solver
+ * keeps two graphs, keyed by n_steps and by which internal buffers hold the current state
+ * (eager steps, integrate and shift rotate them); other calls capture again. n_steps must
+ * be even and stream must not be the legacy default stream. */
 int sph_solver_graph_step(sph_solver_t* s, int32_t n_steps, sph_stream_t stream);
 
 /* The two halves of a step as the reference runner calls them: integrate (both

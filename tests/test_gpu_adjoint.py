@@ -310,3 +310,24 @@ def test_velocity_gradient_along_32_random_directions():
         fd = (la - lb) / (2 * EPS)
         errs.append(_rel(float(np.sum(g * d)), fd))
     assert max(errs) < RTOL, max(errs)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("density_update", ["reference", "rational"])
+def test_graph_replay_gives_the_eager_gradient(density_update):
+    """The CUDA-graph replay of the recomputation and of the step VJPs (and of the fused
+    forward, on a side stream) gives the eager gradient: 23 steps, checkpoints every 9, so
+    that segments of odd length exercise the eager remainder too."""
+    _gpu()
+    from diffsph_gb300.adjoint import rollout_loss_and_grad
+    cfg, st = scenes.fourier_periodic(32, seed=6, jitter=0.1)
+    cfg["integration"]["densityUpdate"] = density_update
+    target = scenes.fourier_velocity(np.asarray(st["fluid"]["positions"], np.float64), np.random.default_rng(3))
+    side = torch.cuda.Stream()
+    with torch.cuda.stream(side):
+        lg, gg, ng = rollout_loss_and_grad(cfg, st["fluid"], target, 23, checkpoint_every=9, use_graphs=True)
+        le, ge, ne = rollout_loss_and_grad(cfg, st["fluid"], target, 23, checkpoint_every=9, use_graphs=False)
+    torch.cuda.synchronize()
+    assert abs(lg - le) <= 1e-6 * abs(le)
+    assert float((gg - ge).abs().max()) <= 1e-5 * float(ge.abs().max())
+    assert abs(ng - ne) <= 1e-5 * abs(ne)

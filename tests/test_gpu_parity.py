@@ -357,3 +357,25 @@ def test_graph_replay_equals_plain_steps():
     ga = a.download()
     for k in ("positions", "velocities", "densities"):
         assert torch.equal(ga[k], gb[k]), k
+
+
+@pytest.mark.parametrize("scene", ["fourier_periodic", "dam_break"])
+def test_graph_replay_interleaved_with_eager_steps(scene):
+    """Eager steps between replays rotate the solver's buffers; the replays must follow
+    (graphs are keyed by the buffer assignment): 1 + 2 + 1 + 2 + 2 steps equal 8 plain steps."""
+    cfg, st = scenes.fourier_periodic(48, seed=9) if scene == "fourier_periodic" else scenes.dam_break(dx=1.0 / 32)
+    a = _solver(cfg, st)
+    a.step(8)
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):
+        b = _solver(cfg, st)
+        b.step(1)
+        b.graph_step(2)
+        b.step(1)
+        b.graph_step(2)
+        b.graph_step(2)
+        gb = b.download()
+    s.synchronize()
+    ga = a.download()
+    for k in ("positions", "velocities", "densities"):
+        assert torch.equal(ga[k], gb[k]), k
