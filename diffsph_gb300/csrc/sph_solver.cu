@@ -30,9 +30,11 @@
 
 namespace sph {
 
-enum KernelClass { KC_SORT = 0, KC_GATHER, KC_MDBC, KC_PASS_A, KC_PASS_B, KC_SHIFT, KC_COUNT };
+// pass_a_gradient: pass A launches that filter the skin list; pass_a_scan: those that scan
+// the cell stencil (the first pass A after a sort, and every pass A of a periodic domain)
+enum KernelClass { KC_SORT = 0, KC_GATHER, KC_MDBC, KC_PASS_A, KC_PASS_B, KC_SHIFT, KC_PASS_A_SCAN, KC_COUNT };
 static const char* kClassNames[KC_COUNT] = {"cell_sort", "gather", "mdbc_ghosts", "pass_a_gradient",
-                                             "pass_b_rates", "shift"};
+                                             "pass_b_rates", "shift", "pass_a_scan"};
 
 // Launch shapes of the neighbor passes (warps per block, list entry width), picked per
 // problem by sph_solver_autotune; shape 0 is the default.
@@ -1797,11 +1799,12 @@ static void launch_a_t(sph_solver* S, float4* X4, float4* V4, RhsOut o, int skin
 // of the same step), 2 neither
 static void launch_a(sph_solver* S, float4* X4, float4* V4, RhsOut o, cudaStream_t st, int skin_mode = 2) {
     set_attrs(S);
-    tbeg(S, KC_PASS_A, st);
+    const int cls = skin_mode == 1 ? KC_PASS_A : KC_PASS_A_SCAN;
+    tbeg(S, cls, st);
 #define SPH_CALL_A(LT, W) launch_a_t<LT, W>(S, X4, V4, o, skin_mode, st)
     SPH_SHAPE_DISPATCH(S, SPH_CALL_A)
 #undef SPH_CALL_A
-    tend(S, KC_PASS_A, st);
+    tend(S, cls, st);
 }
 
 template <bool PER, bool BATCH, int MODE, typename LT, int W>
