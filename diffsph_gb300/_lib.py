@@ -48,6 +48,11 @@ class Params(ctypes.Structure):
     ]
 
 
+class IpsParams(ctypes.Structure):
+    """sph_ips_params_t (implicit particle shifting)."""
+    _fields_ = [("rtol", ctypes.c_double), ("max_iter", ctypes.c_int32), ("solver_threshold", ctypes.c_double)]
+
+
 EXPORTS = [
     "sph_neighbor_workspace_bytes", "sph_neighbor_count", "sph_neighbor_fill",
     "sph_solver_workspace_bytes", "sph_solver_create", "sph_solver_destroy", "sph_solver_upload",
@@ -57,7 +62,7 @@ EXPORTS = [
     "sph_solver_set_shape", "sph_batch_workspace_bytes", "sph_batch_create", "sph_solver_graph_step",
     "sph_neighbor_count_static", "sph_solver_vjp_rates", "sph_solver_vjp_gradient", "sph_solver_vjp_shift",
     "sph_gemm_bf16_tn", "sph_cconv_aggregate", "sph_cconv_aggregate_t", "sph_cconv_aggregate_tc",
-    "sph_neighbor_fill_csr",
+    "sph_neighbor_fill_csr", "sph_solver_ips_workspace_bytes", "sph_solver_set_ips", "sph_solver_ips_result",
 ]
 
 _lib = None
@@ -116,6 +121,9 @@ def load(build_if_missing: bool = False):
         "sph_batch_create": ([PP, ctypes.POINTER(I64), I32, P, SZ, ctypes.POINTER(P)], ctypes.c_int),
         "sph_solver_graph_step": ([P, I32, P], ctypes.c_int),
         "sph_solver_kernel_times": ([P, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(I32), P], ctypes.c_int),
+        "sph_solver_ips_workspace_bytes": ([P, ctypes.POINTER(SZ)], ctypes.c_int),
+        "sph_solver_set_ips": ([P, ctypes.POINTER(IpsParams), P, SZ], ctypes.c_int),
+        "sph_solver_ips_result": ([P, ctypes.POINTER(I32), ctypes.POINTER(I32), P], ctypes.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)

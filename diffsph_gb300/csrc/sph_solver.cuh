@@ -1,0 +1,374 @@
+// Solver internals shared by the step kernels (sph_solver.cu) and the implicit shifting
+// solve (sph_ips.cu): scheme constants, the domain table, the cell-stencil neighbor loops
+// and the solver handle.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <vector>
+
+#include "../../include/sph103.h"
+#include "sph_internal.cuh"
+
+namespace sph {
+
+// pass_a_gradient: pass A launches that filter the skin list; pass_a_scan: those that scan
+// the cell stencil (the first pass A after a sort, and every pass A of a periodic domain)
+enum KernelClass { KC_SORT = 0, KC_GATHER, KC_MDBC, KC_PASS_A, KC_PASS_B, KC_SHIFT, KC_PASS_A_SCAN, KC_COUNT };
+
+// Launch shapes of the neighbor passes (warps per block, list entry width), picked per
+// problem by sph_solver_autotune; shape 0 is the default.
+struct Shape {
+    int warps;
+    int list16;
+};
+constexpr int kNumShapes = 4;
+static const Shape kShapes[kNumShapes] = {{4, 0}, {4, 1}, {8, 1}, {16, 1}};
+constexpr int kCap = 64;  // exact neighbors held per lane before the pair terms are evaluated
+constexpr int kUnroll = 4;  // stencil candidates tested per lane per step of the scan
+constexpr unsigned kFull = 0xffffffffu;
+
+struct Phys {
+    Geo geo;
+    float h;            // support
+    float T;            // exact inclusion threshold: s <= T  <=>  fl(fl(sqrt(s)) / h) <= 1
+    float inv_h;
+    float m;            // particle mass
+    float dt, dth;      // dt, dt/2
+    KernelCoef kc;
+    Eos eos;
+    float rho0;
+    float diff_coef;    // delta * h / kappa * cs
+    float diff_eps;     // 1e-6 * h
+    float v_eps;        // eps * h^2
+    float v_num;        // viscid 8 nu rho0 ; inviscid alpha h cs rho0   (divided by rho_i)
+    float dvnum_dnu;    // d v_num / d nu (viscid: 8 rho0; inviscid: 0)
+    int bvisc;
+    float bv_eps, bv_num;
+    float gx, gy;
+    int nF;
+    float invW0;        // 1 / W(dx/h) for the shifting term
+    float shR, shN, sh_thr;
+    int shN4;           // n == 4
+    float sh_scale;     // -CFL * (h/kappa*2)^2 (times Ma)
+    float inv_cs;
+    int compute_mach;
+    int density_update;
+    float verlet_lim;   // (skin - 1) * h: largest displacement since the sort
+    float T_skin;       // squared radius of the skin list (1.1 h, with a rounding margin)
+    float skin_lim;     // displacement since the sort up to which the skin list holds every pair
+    float area;         // particle area dx^2 (the omega of the implicit shifting matrices)
+};
+
+struct RhsOut {
+    float* dudt;
+    float* drhodt;
+    float* grad;
+    float* L;
+    float* pressure;
+    float* rho_b;
+    int32_t* nn;    // [nF][2]: fluid and boundary neighbors (incl. self) per fluid particle
+};
+
+// One independent domain: its scheme constants, its cell grid and the offset of its cells in
+// the global cell table. A single simulation is a table of one; packed batches of domains
+// with different particle counts (and hence different dx, h, dt) share every kernel launch.
+struct Dom {
+    Phys P;
+    Grid g;
+    int32_t cell0;
+    int32_t pad;
+};
+static_assert(sizeof(Dom) % 4 == 0, "Dom is copied as 32-bit words");
+
+__device__ __forceinline__ bool is_boundary(float rho_signed) { return __float_as_int(rho_signed) < 0; }
+
+__device__ __forceinline__ int dom_of(const int32_t* __restrict__ did, int64_t i, int64_t n) {
+    return (did && i < n) ? did[i] : 0;
+}
+
+// Packed batches: a block of consecutive slots spans at most two domains when every domain
+// holds at least a block's worth of particles. Their constants are copied to shared memory
+// once per block; slots of any other domain read the global table.
+__device__ __forceinline__ void stage_doms(const Dom* __restrict__ doms, const int32_t* __restrict__ did,
+                                           int64_t first, int64_t last, int64_t n, Dom* s_dom, int* s_id) {
+    const int64_t a = first < n ? first : n - 1, b = last < n ? last : n - 1;
+    const int d0 = dom_of(did, a, n), d1 = dom_of(did, b, n);
+    constexpr int kWords = (int)(sizeof(Dom) / 4);
+    const uint32_t* src0 = reinterpret_cast<const uint32_t*>(doms + d0);
+    const uint32_t* src1 = reinterpret_cast<const uint32_t*>(doms + d1);
+    uint32_t* dst = reinterpret_cast<uint32_t*>(s_dom);
+    for (int k = threadIdx.x; k < 2 * kWords; k += blockDim.x) dst[k] = k < kWords ? src0[k] : src1[k - kWords];
+    if (threadIdx.x == 0) {
+        s_id[0] = d0;
+        s_id[1] = d1;
+    }
+    __syncthreads();
+}
+
+__device__ __forceinline__ const Dom& dom_ref(const Dom* __restrict__ doms, const Dom* s_dom, const int* s_id,
+                                              int d) {
+    return d == s_id[0] ? s_dom[0] : (d == s_id[1] ? s_dom[1] : doms[d]);
+}
+
+
+// ------------------------------------------------------------------------------------
+// Neighbor loop: candidates from the 3x3 cell stencil of the sort, exact filter, per-warp
+// shared-memory list of accepted slots, then f(j) for every exact neighbor j. Every lane of
+// the warp must call it (it votes); lanes with active == false contribute no pairs.
+// The cells are >= (h + largest displacement since the sort), so the stencil of the
+// particle's current cell holds every particle within h.
+// ------------------------------------------------------------------------------------
+// Bit k of *wrap marks range k as one whose pairs may cross the periodic boundary. Every
+// other range lies within rad cells of the particle's cell without wrapping and away from
+// the edge cells (where a particle may have crossed the boundary since the sort; the skin
+// check keeps that motion below one cell). On an axis of at least 2 (rad + 2) cells its
+// pairs then have |x_ij| < (rad + 2) cells <= half the extent, where the reference's minimum
+// image is the identity, so the scan may skip it there exactly.
+__device__ __forceinline__ int stencil_ranges(float2 p, const Grid& g, const int32_t* __restrict__ start,
+                                              int rs[kMaxRanges], int re[kMaxRanges], unsigned* wrap = nullptr) {
+    int cx = cell_coord(p.x, g.mn[0], g.inv_cell[0], g.nc[0]);
+    int cy = cell_coord(p.y, g.mn[1], g.inv_cell[1], g.nc[1]);
+    int rows[kMaxRows], lo[2], hi[2];
+    int nr = stencil_rows(cy, g, rows);
+    int ncol = stencil_cols(cx, g, lo, hi);
+    const bool smallx = g.per[0] && g.nc[0] < 2 * g.rad + 4;
+    const bool smally = g.per[1] && g.nc[1] < 2 * g.rad + 4;
+    unsigned w = 0;
+    int n = 0;
+    for (int a = 0; a < nr; ++a) {
+        int base = rows[a] * g.nc[0];
+        const int dy = rows[a] - cy;
+        const bool wy =
+            smally || (g.per[1] && (dy > g.rad || dy < -g.rad || rows[a] == 0 || rows[a] == g.nc[1] - 1));
+        for (int b = 0; b < ncol; ++b) {
+            int s0 = __ldg(&start[base + lo[b]]), s1 = __ldg(&start[base + hi[b] + 1]);
+            if (s1 > s0) {
+                const bool wx = smallx || (g.per[0] && (lo[b] > cx + g.rad || hi[b] < cx - g.rad || lo[b] == 0 ||
+                                                        hi[b] == g.nc[0] - 1));
+                if (wx || wy) w |= 1u << n;
+                rs[n] = s0;
+                re[n] = s1;
+                ++n;
+            }
+        }
+    }
+    if (wrap) *wrap = w;
+    return n;
+}
+
+// Each scan step takes up to kUnroll consecutive candidates of the lane's current range,
+// so that several independent loads are in flight per lane. List entries are slot offsets
+// relative to the particle's own slot: int16_t halves the shared memory (leaving more of
+// the unified L1 for the neighbor data) and is used when the grid keeps every stencil
+// within +-32767 slots; an entry that does not fit raises SPH_FLAG_CAPACITY.
+// capacity of the neighbor list pass A stores for pass B (entries per particle)
+constexpr int kStoreCap = 64;
+// skin list: every candidate within (1 + kSkinFrac) h at the sort positions, kept by the
+// first pass A of a step; the second pass A and the shift filter it instead of the stencil
+constexpr double kSkinFrac = 0.1;
+constexpr int kSkinCap = 80;
+
+
+
+template <typename LT>
+__device__ __forceinline__ bool fits(int d) {
+    return sizeof(LT) >= 4 || (d >= -32768 && d <= 32767);
+}
+
+template <bool PER>
+__device__ __forceinline__ int list_slot(int self, int d, const Grid& g) {
+    int j = self + d;
+    if (PER) {
+        if (j < g.slot0) j += g.nslots;
+        else if (j >= g.slot0 + g.nslots) j -= g.nslots;
+    }
+    return j;
+}
+
+// SKIN: keep every candidate within the skin radius (T_skin) instead of the exact neighbors
+template <bool PER, typename LT, class F, bool SKIN = false>
+__device__ __forceinline__ void neighbor_loop(bool active, int self, float2 pi, const float4* __restrict__ X4,
+                                              const int32_t* __restrict__ start, const Grid& g, const Phys& P,
+                                              LT* __restrict__ lst, uint32_t* __restrict__ words, F&& f) {
+    const float thr = SKIN ? P.T_skin : P.T;
+    const int lane = threadIdx.x & 31;
+    int rs[kMaxRanges], re[kMaxRanges];
+    unsigned wmask = 0;
+    int nrng = active ? stencil_ranges(pi, g, start, rs, re, PER ? &wmask : nullptr) : 0;
+    int r = 0;
+    int s = nrng > 0 ? rs[0] : 0, se = nrng > 0 ? re[0] : 0;
+    int cnt = 0;
+    bool overflow = false;
+    while (__any_sync(kFull, r < nrng)) {
+        if (r < nrng) {
+            int m = se - s < kUnroll ? se - s : kUnroll;
+            const bool wr = PER && ((wmask >> r) & 1u);
+            float4 xj[kUnroll];
+#pragma unroll
+            for (int u = 0; u < kUnroll; ++u)
+                if (u < m) xj[u] = __ldg(&X4[s + u]);
+#pragma unroll
+            for (int u = 0; u < kUnroll; ++u) {
+                if (u < m) {
+                    float x0, x1;
+                    if (wr)
+                        pair_vec<true>(pi, make_float2(xj[u].x, xj[u].y), P.geo, x0, x1);
+                    else
+                        pair_vec<false>(pi, make_float2(xj[u].x, xj[u].y), P.geo, x0, x1);
+                    if (sq_norm_ref(x0, x1) <= thr) {
+                        int d = s + u - self;
+                        if (PER) {  // shortest offset modulo the domain's slots
+                            const int h2 = g.nslots >> 1;
+                            if (d > h2) d -= g.nslots;
+                            else if (d < -h2) d += g.nslots;
+                        }
+                        if (fits<LT>(d)) lst[(cnt++) * 32 + lane] = (LT)d;
+                        else overflow = true;
+                    }
+                }
+            }
+            s += m;
+            if (s == se) {
+                ++r;
+                if (r < nrng) {
+                    s = rs[r];
+                    se = re[r];
+                }
+            }
+        }
+        if (__any_sync(kFull, cnt > kCap - kUnroll)) {
+            int mc = (int)__reduce_max_sync(kFull, (unsigned)cnt);
+            for (int k = 0; k < mc; ++k)
+                if (k < cnt) f(list_slot<PER>(self, (int)lst[k * 32 + lane], g));
+            cnt = 0;
+        }
+    }
+    int mc = (int)__reduce_max_sync(kFull, (unsigned)cnt);
+    for (int k = 0; k < mc; ++k)
+        if (k < cnt) f(list_slot<PER>(self, (int)lst[k * 32 + lane], g));
+    if (overflow) atomicOr(&words[0], SPH_FLAG_CAPACITY);
+}
+
+// The exact neighbors of the stored skin list (scan order of the first pass A of the step,
+// so the same order a scan at the same cells gives), filtered at the current positions.
+template <bool PER, class F>
+__device__ __forceinline__ void skin_loop(int self, float2 pi, const float4* __restrict__ X4, const Grid& g,
+                                          const Phys& P, const int16_t* __restrict__ sl, int cnt, int64_t n,
+                                          F&& f) {
+    int k = 0;
+    for (; k + 4 <= cnt; k += 4) {
+        int j[4];
+        float4 xj[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) j[u] = list_slot<PER>(self, (int)sl[(int64_t)(k + u) * n + self], g);
+#pragma unroll
+        for (int u = 0; u < 4; ++u) xj[u] = __ldg(&X4[j[u]]);
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            float x0, x1;
+            pair_vec<PER>(pi, make_float2(xj[u].x, xj[u].y), P.geo, x0, x1);
+            if (sq_norm_ref(x0, x1) <= P.T) f(j[u]);
+        }
+    }
+    for (; k < cnt; ++k) {
+        const int j = list_slot<PER>(self, (int)sl[(int64_t)k * n + self], g);
+        const float4 xj = __ldg(&X4[j]);
+        float x0, x1;
+        pair_vec<PER>(pi, make_float2(xj.x, xj.y), P.geo, x0, x1);
+        if (sq_norm_ref(x0, x1) <= P.T) f(j);
+    }
+}
+
+}  // namespace sph
+
+using namespace sph;
+
+// ------------------------------------------------------------------------------------
+// Solver handle (one domain, or a packed batch of independent fluid domains)
+// ------------------------------------------------------------------------------------
+struct sph_solver {
+    sph_params_t prm;            // parameters of domain 0 (mDBC, shifting switch)
+    int nd = 1;
+    std::vector<Dom> doms_host;
+    std::vector<int64_t> off_host;  // fluid particle offsets of the domains [nd + 1]
+    int64_t nF, nB, n;
+    int64_t ncells;
+    bool periodic;
+    float2 *Xr, *Xr_t;
+    float4 *Xc, *Xh, *Xf, *Xt;
+    float4 *Vc, *Vh, *Vf, *Vt;
+    int32_t *uid, *uid_t, *did, *did_t;
+    int32_t *key, *perm, *count, *fill, *start, *scan32;
+    int32_t* bidx;
+    uint32_t* words;  // [0] flags, [2] boundary count
+    int16_t* nl;      // exact neighbor list of the last pass A: slot offsets, [kStoreCap][n]
+    int16_t* nlc;     // its length per slot (-1: not stored)
+    int16_t* sl;      // skin list of the step's first pass A, [kSkinCap][n]
+    int16_t* slc;     // its length per slot (-1: not stored)
+    float* msums;     // mDBC ghost moments, [nB][kMdbcSums]
+    uint32_t* maxv;   // per-domain max |u| (float bits)
+    Dom* doms;
+    int64_t* dom_off;
+    float2* bnormal;
+    float* bdist;
+    bool list16 = false;
+    int shape = 0;
+    bool attrs_set = false;
+    bool tables_uploaded = false;
+    // captured step graph
+    // captured step graphs, keyed by step count and buffer assignment (two slots: eager
+    // steps between replays alternate the assignment)
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    int graph_n[2] = {0, 0};
+    const void* graph_key[2][14] = {};
+    int graph_next = 0;
+
+    // timing
+    uint32_t timing_mask = 0;
+    struct Ev {
+        cudaEvent_t a, b;
+        int cls;
+    };
+    std::vector<Ev> pool;
+    size_t used = 0;
+
+    // implicit particle shifting (shifting.scheme 'IPS'), replacing delta+ once configured
+    bool ips = false;
+    float ips_rtol = 1e-4f;
+    int ips_maxiter = 64;
+    float ips_thr = 0.f;             // per-particle |x| limit of the solve (solverThreshold)
+    float2* ips_vec = nullptr;       // x, r, r0, p, ap, s, as: [7][n] in the caller's workspace
+    double* ips_part = nullptr;      // per-block partial sums
+    void* ips_state = nullptr;       // scalars of the solve (device)
+};
+
+// The implicit shift on the sorted state Xin/Vin (integrated positions) into Xout/Vout, with
+// the fluid increments in the original order in dx_out when non-NULL (sph_ips.cu).
+int ips_shift(sph_solver* S, float4* Xin, float4* Vin, float4* Xout, float4* Vout, float* dx_out, int use_skin,
+              cudaStream_t st);
+size_t ips_workspace_bytes(int64_t n);
+
+inline unsigned blocks_for(int64_t n, int threads = kBlock) { return (unsigned)((n + threads - 1) / threads); }
+
+template <typename LT, int W>
+constexpr size_t list_bytes() { return (size_t)W * kCap * 32 * sizeof(LT); }
+
+// timing brackets (only for classes in the mask)
+inline void tbeg(sph_solver* S, int cls, cudaStream_t st) {
+    if (!(S->timing_mask & (1u << cls))) return;
+    if (S->used == S->pool.size()) {
+        sph_solver::Ev e;
+        cudaEventCreate(&e.a);
+        cudaEventCreate(&e.b);
+        S->pool.push_back(e);
+    }
+    S->pool[S->used].cls = cls;
+    cudaEventRecord(S->pool[S->used].a, st);
+}
+inline void tend(sph_solver* S, int cls, cudaStream_t st) {
+    if (!(S->timing_mask & (1u << cls))) return;
+    cudaEventRecord(S->pool[S->used].b, st);
+    S->used++;
+}

@@ -87,8 +87,13 @@ def integrate(simulationStep_, perennialState, config, previousStep=None):
 
 
 def solveShifting(simulationState, config):
-    """δ+ shifting; returns (dx, overallStates) like the reference (overallStates is empty:
-    it only collects IPS solver diagnostics)."""
+    """Shifting (δ+, or the implicit IPS scheme when config['shifting']['scheme'] is 'IPS');
+    returns (dx, overallStates) like the reference. overallStates collects the IPS solve's
+    diagnostics: one (convergence, code, residual) entry per shifting iteration, of which
+    only bicgstab_shifting's return code is kept here; it is empty for δ+."""
     sol = _solver_for(simulationState, config)
     dx = sol.shift()
-    return dx.to(simulationState["fluid"]["positions"].device), []
+    states = []
+    if config.get("shifting", {}).get("scheme", "deltaSPH") == "IPS":
+        states.append(([], sol.ips_result()[1], None))
+    return dx.to(simulationState["fluid"]["positions"].device), states

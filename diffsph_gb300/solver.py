@@ -110,8 +110,13 @@ def params_from_config(cfg, mass: float, skin: float = DEFAULT_SKIN, capacity: i
     p.gravity[0], p.gravity[1] = direction[0] * mag, direction[1] * mag
     p.dt = _f(cfg["timestep"]["dt"])
     sh = cfg.get("shifting", {})
-    if sh.get("scheme", "deltaSPH") != "deltaSPH" or sh.get("freeSurface", False) or int(sh.get("maxIterations", 1)) != 1:
-        raise ValueError("only delta+ shifting with one iteration and no free-surface handling is implemented")
+    if sh.get("scheme", "deltaSPH") not in ("deltaSPH", "IPS") or sh.get("freeSurface", False) \
+            or int(sh.get("maxIterations", 1)) != 1:
+        raise ValueError("only delta+ and implicit (IPS) shifting with one iteration and no free-surface "
+                         "handling are implemented")
+    if sh.get("scheme", "deltaSPH") == "IPS" and (sh.get("summationDensity", False)
+                                                  or sh.get("initialization", "zero") != "zero"):
+        raise ValueError("implicit shifting is implemented with summationDensity off and a zero initial guess")
     p.shift_on = int(bool(sh.get("active", True)))
     p.shift_R, p.shift_n = _f(sh.get("R", 0.25)), _f(sh.get("n", 4))
     p.shift_CFL, p.shift_threshold = _f(sh.get("CFL", 1.5)), _f(sh.get("threshold", 0.5))
@@ -164,6 +169,10 @@ class Solver:
             ctypes.byref(self.params), self.nF, self.nB, ctypes.c_void_p(self._ws_ptr), nbytes.value, ctypes.byref(h)))
         self.handle = h
         self.upload(fluid, boundary if self.nB else None)
+        sh = config.get("shifting", {})
+        if sh.get("scheme", "deltaSPH") == "IPS":
+            self.set_ips(rtol=float(sh.get("rtol", 1e-4)), max_iter=int(sh.get("maxSolveIter", 64)),
+                         solver_threshold=float(sh.get("solverThreshold", -0.5)))
 
     def __del__(self):
         h = getattr(self, "handle", None)
@@ -208,6 +217,33 @@ class Solver:
         dx = torch.empty(self.nF, 2, device="cuda")
         _lib.check("sph_solver_shift", self.lib.sph_solver_shift(self.handle, _ptr(dx), _stream()))
         return dx
+
+    def set_ips(self, rtol: float = 1e-4, max_iter: int = 64, solver_threshold: float = -0.5):
+        """Implicit particle shifting (shifting.scheme 'IPS', src/diffSPH/v2/modules/shifting.py:
+        780-880) in place of delta+; the defaults are the reference's (a negative solver
+        threshold means dx / 2, parameters.py:238). ``set_ips(None)`` returns to delta+."""
+        if rtol is None:
+            _lib.check("sph_solver_set_ips", self.lib.sph_solver_set_ips(self.handle, None, None, 0))
+            self._ips_ws = None
+            return
+        nbytes = ctypes.c_size_t()
+        _lib.check("sph_solver_ips_workspace_bytes",
+                   self.lib.sph_solver_ips_workspace_bytes(self.handle, ctypes.byref(nbytes)))
+        self._ips_ws = torch.empty(int(nbytes.value) + 256, dtype=torch.uint8, device="cuda")
+        ptr = (self._ips_ws.data_ptr() + 255) & ~255
+        dx = _f(self.config["particle"]["dx"])
+        thr = dx / 2 if solver_threshold < 0 else solver_threshold
+        p = _lib.IpsParams(float(rtol), int(max_iter), float(thr))
+        _lib.check("sph_solver_set_ips", self.lib.sph_solver_set_ips(self.handle, ctypes.byref(p),
+                                                                     ctypes.c_void_p(ptr), nbytes.value))
+
+    def ips_result(self):
+        """(iterations, code) of the last implicit shifting solve; code is bicgstab_shifting's
+        second return value."""
+        it, code = ctypes.c_int32(), ctypes.c_int32()
+        _lib.check("sph_solver_ips_result",
+                   self.lib.sph_solver_ips_result(self.handle, ctypes.byref(it), ctypes.byref(code), _stream()))
+        return int(it.value), int(code.value)
 
     def rhs(self):
         o = {"dudt": torch.empty(self.nF, 2, device="cuda"), "drhodt": torch.empty(self.nF, device="cuda"),

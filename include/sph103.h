@@ -218,6 +218,34 @@ int sph_solver_vjp_gradient(sph_solver_t* s, const float* gbar, float* xbar, flo
 int sph_solver_vjp_shift(sph_solver_t* s, const float* xbar_new, float* xbar, float* rbar,
                          float* mach_part, sph_stream_t stream);
 
+/* ------------------------------------------------------------------------------------
+ * Implicit particle shifting (shifting.scheme = 'IPS'): computeShifting,
+ * src/diffSPH/v2/modules/shifting.py:780-880, as solveShifting (:882-1019) calls it, with
+ * the system of getShiftingMatrices (:611-705; no free-surface handling, shifting.
+ * summationDensity off so omega = the particle area dx^2, initialization 'zero') solved by
+ * bicgstab_shifting (:322-493). Once set, it replaces the delta+ shift of sph_solver_step,
+ * sph_solver_graph_step and sph_solver_shift (single-domain solvers only). Outside a graph
+ * capture a solve synchronises the stream every 4 iterations to stop once it has returned;
+ * a captured step holds all max_iter iterations (those after the return do nothing).
+ * ------------------------------------------------------------------------------------ */
+typedef struct sph_ips_params {
+    double rtol;              /* shifting.rtol (reference default 1e-4) */
+    int32_t max_iter;         /* shifting.maxSolveIter (64) */
+    double solver_threshold;  /* shifting.solverThreshold as parsed: dx / 2 when negative
+                                 (parameters.py:238); the solve returns once any |x_i| exceeds it */
+} sph_ips_params_t;
+
+/* Bytes of the IPS workspace (7 float2 vectors per particle and the reduction scratch). */
+int sph_solver_ips_workspace_bytes(const sph_solver_t* s, size_t* bytes);
+/* Switches the solver to IPS (params != NULL; workspace 256-byte aligned, at least
+ * sph_solver_ips_workspace_bytes) or back to delta+ (params == NULL). Drops captured graphs. */
+int sph_solver_set_ips(sph_solver_t* s, const sph_ips_params_t* params, void* workspace,
+                       size_t workspace_bytes);
+/* Iteration count and bicgstab_shifting's second return value (the count when |r|
+ * converged, 0 when |s| converged, -10 / -11 breakdowns, -12 threshold, max_iter when the
+ * loop ran out) of the last solve. Synchronises the stream. */
+int sph_solver_ips_result(sph_solver_t* s, int32_t* iterations, int32_t* code, sph_stream_t stream);
+
 /* Writes the current state back in the original order (NULL entries are skipped). */
 int sph_solver_download(sph_solver_t* s, float* x_fluid, float* u_fluid, float* rho_fluid,
                         float* rho_boundary, sph_stream_t stream);

@@ -534,20 +534,147 @@ def delta_plus_shifting(ps, nb, config):
     return scale[:, None] * s
 
 
-def solve_shifting(state, config):
-    """solveShifting shifting.py:882-1019, delta+ branch with maxIterations = 1 and no
-    free-surface handling: returns the position increment of the fluid particles."""
+def _d2kdq2(q):
+    """Wendland C2 second q-derivative (2D), Wendland2.py:18-22: 20 (4q - 1) (1-q)_+^2."""
+    return 20 * (4 * q - 1) * _cpow(1 - q, 2)
+
+
+def wendland_hessian(q, xhat, h):
+    """Per-pair kernel Hessian, the reference's closed form with its regularisers
+    (KernelWrapper.Hessian2D, src/diffSPH/kernels.py:263-303). Returns [E, 2, 2]."""
+    dt = q.dtype.type
+    cd = dt(C_D_2D)
+    factor = cd / h ** 2
+    r = q * h
+    x = xhat * r[:, None]
+    k2 = _d2kdq2(q)
+    k1 = -20 * q * _cpow(1 - q, 3)
+    dA = h ** 2 * r ** 2 + dt(1e-5) * h
+    dB = h * r ** 3 + dt(1e-10) * h
+    self_term = np.where(q < dt(1e-5), _d2kdq2(np.zeros(1, dt))[0], dt(0))  # d2kdq2(0) at the particle itself
+    dxx = factor * (x[:, 0] ** 2 / dA * k2 + x[:, 1] ** 2 / dB * k1 + 1 / h ** 2 * self_term)
+    dyy = factor * (x[:, 1] ** 2 / dA * k2 + x[:, 0] ** 2 / dB * k1 + 1 / h ** 2 * self_term)
+    dxy = cd * h ** dt(-2) * np.where(q > dt(-1e-7), (x[:, 0] * x[:, 1]) / (h * r ** 2 + dt(1e-5) * h)
+                                      * (1 / h * k2 - 1 / (r + dt(1e-3) * h) * k1), dt(0))
+    H = np.zeros((q.shape[0], 2, 2), dtype=dt)
+    inside = q <= 1
+    H[:, 0, 0] = np.where(inside, dxx, 0)
+    H[:, 1, 1] = np.where(inside, dyy, 0)
+    H[:, 0, 1] = np.where(inside, dxy, 0)
+    H[:, 1, 0] = H[:, 0, 1]
+    return H
+
+
+def ips_matrices(ps, nb, marker):
+    """getShiftingMatrices shifting.py:611-705 without free-surface handling and with
+    shifting.summationDensity off (omega = areas), initialization 'zero': the 2x2 blocks
+    H_ij omega_j of the active rows (fluid i), the right-hand side J_i = sum grad W omega_j
+    (zero on wall rows) and x0 = 0."""
+    i, j = nb["indices"]
+    n = ps["positions"].shape[0]
+    omega = ps["areas"]
+    J = scatter_sum(nb["gradients"] * omega[j, None], i, n)
+    H = wendland_hessian(nb["distances"], nb["vectors"], nb["supports"]) * omega[j, None, None]
+    B = J.reshape(-1).copy()
+    B.reshape(-1, 2)[marker != 0] = 0
+    active = marker[i] == 0
+    return H[active], i[active], j[active], B
+
+
+def _spmv(H, i, j, x, n):
+    """multiplySparseShifting shifting.py:707-716: block rows summed per component."""
+    xv = x.reshape(-1, 2)
+    out = np.zeros_like(x)
+    out[0::2] = out[0::2] + scatter_sum(H[:, 0, 0] * xv[j, 0], i, n)
+    out[0::2] = out[0::2] + scatter_sum(H[:, 0, 1] * xv[j, 1], i, n)
+    out[1::2] = out[1::2] + scatter_sum(H[:, 1, 0] * xv[j, 0], i, n)
+    out[1::2] = out[1::2] + scatter_sum(H[:, 1, 1] * xv[j, 1], i, n)
+    return out
+
+
+def bicgstab_shifting(H, i, j, n, b, rtol, maxiter, threshold):
+    """bicgstab_shifting shifting.py:322-493 from x0 = 0: unpreconditioned BiCGStab (the
+    Jacobi matrix it is given is never applied) with the reference's stopping rules:
+    |r| < rtol |b| before an iteration, |s| < rtol |b| mid-iteration, rho / rv / omega
+    breakdowns, and any per-particle |x_i| > threshold. Returns (x, iterations, code) where
+    code is the reference's second return value: the iteration count when |r| converged
+    at the top of an iteration, 0 when |s| converged mid-iteration, -10 / -11 for the rho /
+    rv and omega breakdowns, -12 for the threshold, maxiter when the loop ran out."""
+    dt = b.dtype.type
+    norm = lambda v: dt(np.sqrt(np.dot(v, v)))
+    bnrm2 = norm(b)
+    atol = dt(max(0.0, float(rtol) * float(bnrm2)))
+    xk = np.zeros_like(b)
+    if bnrm2 == 0:
+        return b.copy(), 0, 0
+    rhotol = dt(float(np.finfo(dt).eps) ** 2)
+    rk = b.copy()
+    r0 = rk.copy()
+    pk = rk.copy()
+    for it in range(maxiter):
+        if norm(rk) < atol:
+            return xk, it, it
+        rho = dt(np.dot(rk, r0))
+        if abs(rho) < rhotol:
+            return xk, it, -10
+        apk = _spmv(H, i, j, pk, n)
+        rv = dt(np.dot(apk, r0))
+        if rv == 0:
+            return xk, it, -11
+        alpha = dt(rho / rv)
+        sk = rk - alpha * apk
+        if norm(sk) < atol:
+            return xk + alpha * pk, it + 1, 0
+        ask = _spmv(H, i, j, sk, n)
+        omega = dt(dt(np.dot(ask, sk)) / dt(np.dot(ask, ask)))
+        xk = xk + alpha * pk + omega * sk
+        rk = sk - omega * ask
+        beta = dt(dt(np.dot(rk, r0)) / rho) * dt(alpha / omega)
+        pk = rk + beta * (pk - omega * apk)
+        if it > 0 and abs(omega) < rhotol:
+            return xk, it + 1, -11
+        if np.any(np.sqrt(np.sum(xk.reshape(-1, 2) ** 2, axis=1)) > threshold):
+            return xk, it + 1, -12
+    return xk, maxiter, maxiter
+
+
+def ips_shift(ps, nb, marker, config):
+    """computeShifting shifting.py:780-880 (scheme 'IPS', solver 'BiCGStab_wJacobi'):
+    returns the update -x of the solve (before the clamp) and (iterations, code) as
+    ``bicgstab_shifting`` returns them."""
+    sh = config["shifting"]
+    dx = _flt(config["particle"]["dx"])
+    thr = sh.get("solverThreshold", -0.5)
+    thr = dx / 2 if thr < 0 else thr  # parameters.py:238
+    H, i, j, B = ips_matrices(ps, nb, marker)
+    n = ps["positions"].shape[0]
+    xk, iters, status = bicgstab_shifting(H, i, j, n, B, sh.get("rtol", 1e-4), int(sh.get("maxSolveIter", 64)),
+                                          thr)
+    return -xk.reshape(-1, 2), (iters, status)
+
+
+def solve_shifting(state, config, info=None):
+    """solveShifting shifting.py:882-1019 with maxIterations = 1 and no free-surface
+    handling, delta+ (deltaPlusShifting) or implicit (IPS) scheme: returns the position
+    increment of the fluid particles. ``info`` (a dict) receives the IPS solve's
+    iteration count, return code and right-hand side."""
     fl = state["fluid"]
     nF = fl["positions"].shape[0]
+    keys = ("positions", "velocities", "masses", "densities", "supports", "areas")
     if "boundary" in state:
         bd = state["boundary"]
-        ps = {k: np.concatenate([fl[k], bd[k]]) for k in ("positions", "velocities", "masses", "densities", "supports")}
+        ps = {k: np.concatenate([fl[k], bd[k]]) for k in keys}
         marker = np.concatenate([np.zeros(nF, np.int32), np.ones(bd["positions"].shape[0], np.int32)])
     else:
-        ps = {k: fl[k] for k in ("positions", "velocities", "masses", "densities", "supports")}
+        ps = {k: fl[k] for k in keys}
         marker = np.zeros(nF, np.int32)
     nb = neighbor_search(ps, ps, config)
-    update = -delta_plus_shifting(ps, nb, config)
+    if config["shifting"].get("scheme", "deltaSPH") == "IPS":
+        update, stats = ips_shift(ps, nb, marker, config)
+        if info is not None:
+            info["iterations"], info["code"] = stats
+    else:
+        update = -delta_plus_shifting(ps, nb, config)
     dt = fl["densities"].dtype.type
     thr = dt(_flt(config["shifting"]["threshold"]) * _flt(config["particle"]["dx"]))
     update = np.clip(update, -thr, thr)

@@ -91,3 +91,22 @@ def test_params_from_reference_config_keys():
     cfg["diffusion"]["velocityScheme"] = "Monaghan1992"
     with pytest.raises(ValueError):
         params_from_config(cfg, 1.0)
+
+
+def test_params_accept_the_implicit_shifting_scheme():
+    cfg, st = scenes.fourier_periodic(16, seed=1)
+    cfg["shifting"]["scheme"] = "IPS"
+    params_from_config(cfg, float(st["fluid"]["masses"][0]))
+    cfg["shifting"]["initialization"] = "deltaPlus"
+    with pytest.raises(ValueError):
+        params_from_config(cfg, 1.0)
+    cfg["shifting"]["initialization"] = "zero"
+    cfg["shifting"]["freeSurface"] = True
+    with pytest.raises(ValueError):
+        params_from_config(cfg, 1.0)
+
+
+def test_ips_params_struct_layout():
+    from diffsph_gb300 import _lib
+    assert ctypes.sizeof(_lib.IpsParams) == 24
+    assert _lib.IpsParams.solver_threshold.offset == 16

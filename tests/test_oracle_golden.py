@@ -127,3 +127,20 @@ def test_wendland_normalisation():
     W = O.wendland_kernel(q, np.float64(h))
     integral = np.trapezoid(W * 2 * np.pi * r, r)
     assert abs(integral - 1.0) < 1e-8
+
+
+IPS_CASES = ["tgv24_jitter", "fourier20", "dambreak16"]
+
+
+@pytest.mark.parametrize("case", IPS_CASES)
+def test_ips_shift_against_reference(case):
+    """Implicit particle shifting (shifting.scheme 'IPS'): the oracle's BiCGStab solve ends
+    the way the reference's does (same return code) with the same shift."""
+    z, cfg, st = load_case(f"ips_{case}")
+    info = {}
+    dx, _ = O.solve_shifting(copy.deepcopy(st), cfg, info)
+    assert info["code"] == int(z["ips/iterations"])
+    # the reference's right-hand side B = sum grad W omega_j (interleaved, wall rows zero)
+    ps_n = st["fluid"]["positions"].shape[0]
+    assert rel_max(dx, z["ips/shift"]) < 1e-4
+    assert dx.shape == z["ips/shift"].shape and ps_n == dx.shape[0]
