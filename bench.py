@@ -30,10 +30,14 @@ sys.path.insert(0, ROOT)
 
 METRIC = "particle-steps/s (plain delta-SPH step)"
 # dram__bytes_read + dram__bytes_write of one launch per fluid particle, from the ncu captures
-# summarised in profiles/pass_a_gradient_dambreak_dx512.md (12.33 + 9.99 MB / 524,288) and
+# summarised in profiles/pass_a_gradient_dambreak_dx512.md (the mean of the skin-building
+# launch, 20.30 + 80.22 MB, and the skin-filtering launch, 78.87 + 19.92 MB, / 524,288) and
 # profiles/pass_b_rates_dambreak_dx512.md (74.60 + 4.14 MB / 524,288)
-PASS_A_DRAM_BYTES_PER_PARTICLE = 42.6
+PASS_A_DRAM_BYTES_PER_PARTICLE = 190.1
 PASS_B_DRAM_BYTES_PER_PARTICLE = 150.2
+# the same for one product of the implicit shift (k_ips_spmv), profiles/ips_spmv_fourier512.md
+# ((192.06 + 3.65) MB and (189.98 + 3.62) MB / 262,144)
+IPS_SPMV_DRAM_BYTES_PER_PARTICLE = 742.0
 
 WORKLOADS = {
     "dambreak_dx1024": dict(scene="dam_break", dx=1.0 / 1024),
@@ -41,6 +45,9 @@ WORKLOADS = {
     "dambreak_dx512": dict(scene="dam_break", dx=1.0 / 512),
     "dambreak_dx256": dict(scene="dam_break", dx=1.0 / 256),
     "tgv_64": dict(scene="taylor_green", nx=64),
+    # implicit particle shifting (shifting.scheme 'IPS'): jittered periodic Fourier flow
+    "ips_fourier1024": dict(scene="fourier", nx=1024, seed=0, jitter=0.1, ips=True),
+    "ips_fourier512": dict(scene="fourier", nx=512, seed=0, jitter=0.1, ips=True),
     # gradient of a rollout loss: 128x128 periodic Fourier flow, 1000 steps, checkpoints every 25
     "adjoint_fourier128": dict(scene="adjoint", nx=128, seed=0, target_seed=1, rollout=1000, every=25),
     # learned k=4 step: trained at 128x128 (dx = 1/64), evaluated on 32 domains of 256x256 (4x4 box)
@@ -56,6 +63,11 @@ def make_scene(name):
     w = WORKLOADS[name]
     if w["scene"] == "dam_break":
         return scenes.dam_break(dx=w["dx"])
+    if w["scene"] == "fourier":
+        cfg, st = scenes.fourier_periodic(w["nx"], seed=w["seed"], jitter=w["jitter"])
+        if w.get("ips"):
+            cfg["shifting"]["scheme"] = "IPS"
+        return cfg, st
     return scenes.taylor_green(w["nx"])
 
 
@@ -120,7 +132,10 @@ def algorithmic_bytes(nbar):
     right-hand side reads the neighbor list (4 nbar + 4), x, rho (12) and writes gradRho (8);
     pass B reads the list and x, u, rho, gradRho (28) and writes the two rates (12); the whole
     plain step moves 24 nbar + 352."""
-    return {"pass_a": 4 * nbar + 24, "pass_b": 4 * nbar + 44, "step": 24 * nbar + 352}
+    return {"pass_a": 4 * nbar + 24, "pass_b": 4 * nbar + 44, "step": 24 * nbar + 352,
+            # one product y = A v of the implicit shift: the list (4 nbar + 4), x (8), v (8),
+            # the dot operand (8), y (8)
+            "ips_spmv": 4 * nbar + 36}
 
 
 def cpu_baseline(workload, budget_s=20.0):
@@ -134,6 +149,9 @@ def cpu_baseline(workload, budget_s=20.0):
     elif w["scene"] == "dam_break":
         cfg, st = scenes.dam_break(dx=1.0 / 64)
         sample = "dam break dx=1/64 (same scene and parameters, coarser lattice)"
+    elif w["scene"] == "fourier":
+        cfg, st = _reference_sample(workload)
+        sample = "the same flow generator at 64x64 (implicit shifting)"
     else:
         cfg, st = make_scene(workload)
         sample = workload
@@ -210,6 +228,12 @@ def _reference_sample(workload):
         return scenes.dam_break(dx=1.0 / 64)
     if sc == "batched":
         return scenes.batched_fourier(1, seed=0, n_min=4096, n_max=4096)[0]
+    if sc == "fourier":
+        w = WORKLOADS[workload]
+        cfg, st = scenes.fourier_periodic(64, seed=w["seed"], jitter=w["jitter"])
+        if w.get("ips"):
+            cfg["shifting"]["scheme"] = "IPS"
+        return cfg, st
     return make_scene(workload)
 
 
@@ -284,6 +308,7 @@ def run_ours(args):
     torch.cuda.set_device(local)
     ge.build()
     batched = WORKLOADS[args.workload]["scene"] == "batched"
+    ips = bool(WORKLOADS[args.workload].get("ips", False))
     sol, nF, nB, nbar, scene = build_solver(args.workload)
     stream = torch.cuda.Stream()
     torch.cuda.synchronize()
@@ -293,9 +318,12 @@ def run_ours(args):
             sol.step(1)
         sol.check()
         # the timed steps replay a captured CUDA graph of two steps (same kernels, no launch
-        # overhead); per-kernel times come from a short event-timed eager loop afterwards
+        # overhead); per-kernel times come from a short event-timed eager loop afterwards. An
+        # implicit shift runs eagerly: it stops launching once its solve has returned, where a
+        # graph would hold every one of its max_iter iterations
         steps = args.steps + (args.steps & 1)
-        sol.graph_step(2)  # capture
+        if not ips:
+            sol.graph_step(2)  # capture
         sol.check()
         torch.cuda.synchronize()
         # timed region: device-resident state, CUDA events on the launching stream
@@ -305,16 +333,23 @@ def run_ours(args):
         torch.cuda.synchronize()
         with ClockSampler(local) as clk:
             e0.record(stream)
-            for _ in range(steps // 2):
-                sol.graph_step(2)
+            if ips:
+                for _ in range(steps):
+                    sol.step(1)
+            else:
+                for _ in range(steps // 2):
+                    sol.graph_step(2)
             e1.record(stream)
             torch.cuda.synchronize()
         ms = e0.elapsed_time(e1)
         # per-kernel times from a short event-timed eager loop of the same step
         sol.set_timing(["pass_b_rates", "pass_a_gradient", "pass_a_scan", "shift", "cell_sort", "gather",
-                        "mdbc_ghosts"])
+                        "mdbc_ghosts", "ips_setup", "ips_spmv", "ips_vector"])
+        ips_iters = []
         for _ in range(4):
             sol.step(1)
+            if ips:
+                ips_iters.append(sol.ips_result())
         ktimes = sol.kernel_times()
         sol.set_timing([])
         sol.check()
@@ -334,31 +369,59 @@ def run_ours(args):
     achieved_b = ab["pass_b"] * nF / (pb_avg / 1e3) / 1e9 if pb_avg > 0 else None
     step_achieved = ab["step"] * nF * steps / (ms / 1e3) / 1e9
     launches = sol.launches_per_step() * steps
+    ips_info = None
+    if ips:
+        # the products of iterations the solve ran (launches after its return do nothing)
+        sp_ms, sp_n = ktimes.get("ips_spmv", (0.0, 0))
+        working = 2 * sum(it for it, _ in ips_iters)
+        sp_avg = sp_ms / max(working, 1)
+        achieved_s = ab["ips_spmv"] * nF / (sp_avg / 1e3) / 1e9 if sp_avg > 0 else None
+        ips_launches = sum(ktimes.get(k, (0.0, 0))[1] for k in ("ips_setup", "ips_spmv", "ips_vector")) / 4
+        # the delta+ shift launch is replaced by the implicit shift's
+        launches = int(round((sol.launches_per_step() - 1 + ips_launches) * steps))
+        ips_info = {"iterations_and_codes": ips_iters, "spmv_avg_ms": sp_avg, "spmv_achieved_gbs": achieved_s,
+                    "spmv_frac": (achieved_s / pk) if achieved_s else None,
+                    "spmv_alg_bytes_per_particle": ab["ips_spmv"],
+                    "spmv_traffic": (IPS_SPMV_DRAM_BYTES_PER_PARTICLE * nF
+                                     if IPS_SPMV_DRAM_BYTES_PER_PARTICLE else None)}
     if rank != 0:
         return
+    roofline = {"bound": "hbm", "kernel": "pass_a_gradient", "achieved": achieved, "peak": pk,
+                "peak_kind": pk_kind, "unit": "GB/s",
+                "frac": (achieved / pk) if achieved else None,
+                "traffic": PASS_A_DRAM_BYTES_PER_PARTICLE * nF,
+                "traffic_note": "ncu dram bytes of k_pass_a on dambreak_dx512 (190.1 B/particle, the "
+                                "mean of the skin-building and skin-filtering launches), scaled by "
+                                "the particle count",
+                "alg_bytes_per_particle": ab["pass_a"], "avg_launch_ms": pa_avg,
+                "pass_b": {"achieved": achieved_b, "frac": (achieved_b / pk) if achieved_b else None,
+                           "alg_bytes_per_particle": ab["pass_b"], "avg_launch_ms": pb_avg,
+                           "traffic": PASS_B_DRAM_BYTES_PER_PARTICLE * nF},
+                "step_alg_bytes_per_particle": ab["step"], "step_achieved_gbs": step_achieved,
+                "step_frac": step_achieved / pk}
+    if ips_info is not None and (sp_ms > pa_ms):
+        # the implicit shift's products dominate such a step
+        roofline.update({"kernel": "ips_spmv", "achieved": ips_info["spmv_achieved_gbs"],
+                         "frac": ips_info["spmv_frac"], "traffic": ips_info["spmv_traffic"],
+                         "traffic_note": "ncu dram bytes of k_ips_spmv on ips_fourier512, scaled by the "
+                                         "particle count",
+                         "alg_bytes_per_particle": ab["ips_spmv"], "avg_launch_ms": ips_info["spmv_avg_ms"],
+                         "pass_a": {"achieved": achieved, "frac": (achieved / pk) if achieved else None,
+                                    "alg_bytes_per_particle": ab["pass_a"], "avg_launch_ms": pa_avg}})
     line = {
         "metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": world, "steps": steps,
         "warmup": args.warmup, "ms_per_step": ms / steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": args.workload, "fluid_particles": nF, "boundary_particles": nB,
                    "mean_neighbors": round(nbar, 3), "l2": "state (> 160 MB) exceeds L2; no flush",
-                   "parallelism": "replicas" if world > 1 else "single", "graph": True,
+                   "parallelism": "replicas" if world > 1 else "single", "graph": not ips,
+                   "shifting": "IPS" if ips else "deltaPlus",
                    "launch_shape": shape, "shape_ms": [round(v, 4) for v in shape_ms]},
         "e2e": e2e,
-        "roofline": {"bound": "hbm", "kernel": "pass_a_gradient", "achieved": achieved, "peak": pk,
-                     "peak_kind": pk_kind, "unit": "GB/s",
-                     "frac": (achieved / pk) if achieved else None,
-                     "traffic": PASS_A_DRAM_BYTES_PER_PARTICLE * nF,
-                     "traffic_note": "ncu dram bytes of k_pass_a on dambreak_dx512 (42.6 B/particle), "
-                                     "scaled by the particle count",
-                     "alg_bytes_per_particle": ab["pass_a"], "avg_launch_ms": pa_avg,
-                     "pass_b": {"achieved": achieved_b, "frac": (achieved_b / pk) if achieved_b else None,
-                                "alg_bytes_per_particle": ab["pass_b"], "avg_launch_ms": pb_avg,
-                                "traffic": PASS_B_DRAM_BYTES_PER_PARTICLE * nF},
-                     "step_alg_bytes_per_particle": ab["step"], "step_achieved_gbs": step_achieved,
-                     "step_frac": step_achieved / pk},
+        "roofline": roofline,
         "kernel_ms": {k: {"total_ms": v[0], "launches": v[1]} for k, v in ktimes.items() if v[1]},
         "gpu_launches": launches,
+        **({"ips": ips_info} if ips_info is not None else {}),
         "clocks": clk.summary(),
     }
     if not args.no_cpu_baseline:

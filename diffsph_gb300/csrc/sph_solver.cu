@@ -33,7 +33,8 @@
 namespace sph {
 
 static const char* kClassNames[KC_COUNT] = {"cell_sort", "gather", "mdbc_ghosts", "pass_a_gradient",
-                                             "pass_b_rates", "shift", "pass_a_scan"};
+                                             "pass_b_rates", "shift", "pass_a_scan", "ips_setup",
+                                             "ips_spmv", "ips_vector"};
 
 // ------------------------------------------------------------------------------------
 // upload / download / gather

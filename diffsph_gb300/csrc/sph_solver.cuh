@@ -15,7 +15,12 @@ namespace sph {
 
 // pass_a_gradient: pass A launches that filter the skin list; pass_a_scan: those that scan
 // the cell stencil (the first pass A after a sort, and every pass A of a periodic domain)
-enum KernelClass { KC_SORT = 0, KC_GATHER, KC_MDBC, KC_PASS_A, KC_PASS_B, KC_SHIFT, KC_PASS_A_SCAN, KC_COUNT };
+// ips_setup / ips_spmv / ips_vector: the implicit shift's neighbor pass (b and its list), its
+// matrix products, and its vector updates (with the final position update)
+enum KernelClass {
+    KC_SORT = 0, KC_GATHER, KC_MDBC, KC_PASS_A, KC_PASS_B, KC_SHIFT, KC_PASS_A_SCAN,
+    KC_IPS_SETUP, KC_IPS_SPMV, KC_IPS_VECTOR, KC_COUNT
+};
 
 // Launch shapes of the neighbor passes (warps per block, list entry width), picked per
 // problem by sph_solver_autotune; shape 0 is the default.
@@ -340,6 +345,10 @@ struct sph_solver {
     int ips_maxiter = 64;
     float ips_thr = 0.f;             // per-particle |x| limit of the solve (solverThreshold)
     float2* ips_vec = nullptr;       // x, r, r0, p, ap, s, as: [7][n] in the caller's workspace
+    float* ips_H = nullptr;          // blocks of the stored exact list (warp-tile-major)
+    int16_t* ips_nl = nullptr;       // that list: slot offsets (warp-tile-major)
+    int16_t* ips_nlc = nullptr;      // its length per slot (-1: not stored)
+    int ips_sms = 0;                 // SM count of the device (grid caps)
     double* ips_part = nullptr;      // per-block partial sums
     void* ips_state = nullptr;       // scalars of the solve (device)
 };

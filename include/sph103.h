@@ -235,7 +235,8 @@ typedef struct sph_ips_params {
                                  (parameters.py:238); the solve returns once any |x_i| exceeds it */
 } sph_ips_params_t;
 
-/* Bytes of the IPS workspace (7 float2 vectors per particle and the reduction scratch). */
+/* Bytes of the IPS workspace: 7 float2 vectors and the stored 2x2 blocks of up to 64 exact
+ * neighbors (12 B each) per particle, and the reduction scratch. */
 int sph_solver_ips_workspace_bytes(const sph_solver_t* s, size_t* bytes);
 /* Switches the solver to IPS (params != NULL; workspace 256-byte aligned, at least
  * sph_solver_ips_workspace_bytes) or back to delta+ (params == NULL). Drops captured graphs. */
