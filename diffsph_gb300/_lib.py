@@ -48,6 +48,12 @@ class Params(ctypes.Structure):
     ]
 
 
+class FreeSurfaceParams(ctypes.Structure):
+    """sph_free_surface_params_t (free-surface handling of the shift)."""
+    _fields_ = [("barecasco_threshold", ctypes.c_double), ("expansion_iterations", ctypes.c_int32),
+                ("surface_scaling", ctypes.c_double)]
+
+
 class IpsParams(ctypes.Structure):
     """sph_ips_params_t (implicit particle shifting)."""
     _fields_ = [("rtol", ctypes.c_double), ("max_iter", ctypes.c_int32), ("solver_threshold", ctypes.c_double)]
@@ -63,6 +69,7 @@ EXPORTS = [
     "sph_neighbor_count_static", "sph_solver_vjp_rates", "sph_solver_vjp_gradient", "sph_solver_vjp_shift",
     "sph_gemm_bf16_tn", "sph_cconv_aggregate", "sph_cconv_aggregate_t", "sph_cconv_aggregate_tc",
     "sph_neighbor_fill_csr", "sph_solver_ips_workspace_bytes", "sph_solver_set_ips", "sph_solver_ips_result",
+    "sph_solver_free_surface_workspace_bytes", "sph_solver_set_free_surface", "sph_solver_free_surface_fields",
 ]
 
 _lib = None
@@ -124,6 +131,9 @@ def load(build_if_missing: bool = False):
         "sph_solver_ips_workspace_bytes": ([P, ctypes.POINTER(SZ)], ctypes.c_int),
         "sph_solver_set_ips": ([P, ctypes.POINTER(IpsParams), P, SZ], ctypes.c_int),
         "sph_solver_ips_result": ([P, ctypes.POINTER(I32), ctypes.POINTER(I32), P], ctypes.c_int),
+        "sph_solver_free_surface_workspace_bytes": ([P, ctypes.POINTER(SZ)], ctypes.c_int),
+        "sph_solver_set_free_surface": ([P, ctypes.POINTER(FreeSurfaceParams), P, SZ], ctypes.c_int),
+        "sph_solver_free_surface_fields": ([P, P, P, P, P, P], ctypes.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)

@@ -14,7 +14,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "libsph103.so")
 OBJ = os.path.join(HERE, "_build")
-SOURCES = ["sph_grid.cu", "sph_solver.cu", "sph_ips.cu", "sph_cconv.cu"]
+SOURCES = ["sph_grid.cu", "sph_solver.cu", "sph_ips.cu", "sph_surface.cu", "sph_cconv.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
 

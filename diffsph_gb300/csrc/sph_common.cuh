@@ -113,7 +113,8 @@ struct M2 {
     float a, b, c, d;
 };
 
-__device__ __forceinline__ M2 pinv2x2_ref(float a, float b, float c, float d) {
+__device__ __forceinline__ M2 pinv2x2_ref(float a, float b, float c, float d, float* sv1 = nullptr,
+                                          float* sv2 = nullptr) {
     float aa = a * a, bb = b * b, cc = c * c, dd = d * d;
     float theta = 0.5f * atan2f(2.0f * a * c + 2.0f * b * d, aa + bb - cc - dd);
     float ct, st;
@@ -124,6 +125,8 @@ __device__ __forceinline__ M2 pinv2x2_ref(float a, float b, float c, float d) {
     float S2 = sqrtf(t * t + 4.0f * u * u);
     float o1 = sqrtf((S1 + S2) * 0.5f);
     float o2 = sqrtf(fmaxf(S1 - S2 + 1e-7f, 1e-7f) * 0.5f);
+    if (sv1) *sv1 = o1;  // the singular values (math.py:53-54 orders them by magnitude)
+    if (sv2) *sv2 = o2;
     float phi = 0.5f * atan2f(2.0f * a * b + 2.0f * c * d, aa - bb + cc - dd);
     float cp, sp;
     sincosf(phi, &sp, &cp);

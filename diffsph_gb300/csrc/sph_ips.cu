@@ -190,7 +190,7 @@ __global__ void __launch_bounds__(32 * W)
     k_ips_setup(const Dom D, int64_t n, const float4* __restrict__ X4, const int32_t* __restrict__ start,
                 uint32_t* __restrict__ words, int use_skin, const int16_t* __restrict__ sl,
                 const int16_t* __restrict__ slc, IpsVec V, double* __restrict__ part, IpsState* st, float rtol,
-                int maxiter) {
+                int maxiter, const SurfaceView sv) {
     extern __shared__ __align__(16) unsigned char s_dyn[];
     LT* lst = reinterpret_cast<LT*>(s_dyn) + (threadIdx.x >> 5) * (kCap * 32);
     const Phys& P = D.P;
@@ -202,7 +202,8 @@ __global__ void __launch_bounds__(32 * W)
         const int64_t i = tile * (32 * W) + threadIdx.x;
         const bool inb = i < n;
         const float4 xi = inb ? X4[i] : make_float4(0.f, 0.f, -1.f, 0.f);
-        const bool active = inb && !is_boundary(xi.z);
+        // surface rows leave the system like wall rows (getShiftingMatrices :657-678)
+        const bool active = inb && !is_boundary(xi.z) && !(sv.fs && sv.fs[i]);
         const float2 pi = make_float2(xi.x, xi.y);
         float b0 = 0.f, b1 = 0.f;
         int nst = 0;
@@ -445,7 +446,7 @@ __global__ void __launch_bounds__(kIpsBlock) k_ips_p(int64_t n, IpsVec V, const 
 __global__ void __launch_bounds__(kIpsBlock)
     k_ips_apply(const Dom D, int64_t n, const float4* __restrict__ X4, const float4* __restrict__ V4,
                 float2* __restrict__ Xr, float4* __restrict__ X4o, float4* __restrict__ V4o, const float2* __restrict__ x,
-                int enabled, const int32_t* __restrict__ uid, float* __restrict__ dx_out) {
+                int enabled, const int32_t* __restrict__ uid, float* __restrict__ dx_out, const SurfaceView sv) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const Phys& P = D.P;
@@ -461,8 +462,10 @@ __global__ void __launch_bounds__(kIpsBlock)
         return;
     }
     const float2 s = x[i];
-    const float up0 = fminf(fmaxf(-s.x, -P.sh_thr), P.sh_thr);
-    const float up1 = fminf(fmaxf(-s.y, -P.sh_thr), P.sh_thr);
+    float u0 = -s.x, u1 = -s.y;
+    surface_project(sv, i, u0, u1);
+    const float up0 = fminf(fmaxf(u0, -P.sh_thr), P.sh_thr);
+    const float up1 = fminf(fmaxf(u1, -P.sh_thr), P.sh_thr);
     const float2 xr = Xr[i];
     const float y0 = __fsub_rn(xr.x, up0), y1 = __fsub_rn(xr.y, up1);
     const float2 xn = make_float2(__fadd_rn(xr.x, __fsub_rn(y0, xr.x)), __fadd_rn(xr.y, __fsub_rn(y1, xr.y)));
@@ -519,7 +522,8 @@ static void ips_launch(sph_solver* S, float4* Xin, float4* Vin, float4* Xout, fl
     cudaMemsetAsync(ist, 0, sizeof(IpsState), st);
     tbeg(S, KC_IPS_SETUP, st);
     k_ips_setup<PER, LT, kIpsW><<<gn, 32 * kIpsW, smem, st>>>(D, n, Xin, S->start, S->words, use_skin, S->sl, S->slc,
-                                                               V, S->ips_part, ist, S->ips_rtol, S->ips_maxiter);
+                                                               V, S->ips_part, ist, S->ips_rtol, S->ips_maxiter,
+                                                               surface_view(S));
     tend(S, KC_IPS_SETUP, st);
     cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
     cudaStreamIsCapturing(st, &cap);
@@ -549,7 +553,7 @@ static void ips_launch(sph_solver* S, float4* Xin, float4* Vin, float4* Xout, fl
     }
     tbeg(S, KC_IPS_VECTOR, st);
     k_ips_apply<<<blocks_for(n, kIpsBlock), kIpsBlock, 0, st>>>(D, n, Xin, Vin, S->Xr, Xout, Vout, V.x,
-                                                                S->prm.shift_on, S->uid, dx_out);
+                                                                S->prm.shift_on, S->uid, dx_out, surface_view(S));
     tend(S, KC_IPS_VECTOR, st);
 }
 

@@ -568,7 +568,7 @@ __device__ __forceinline__ void shift_tile(const Dom& D0, int64_t i, int64_t n, 
                                            const uint32_t* __restrict__ maxv, int enabled,
                                            const int32_t* __restrict__ uid, float* __restrict__ dx_out,
                                            LT* __restrict__ lst, int use_skin, const int16_t* __restrict__ sl,
-                                           const int16_t* __restrict__ slc) {
+                                           const int16_t* __restrict__ slc, const SurfaceView& sv) {
     const int dom = BATCH ? dom_of(did, i, n) : 0;
     const Dom& D = BATCH ? dom_ref(doms, s_dom, s_id, dom) : D0;
     const Phys& P = D.P;
@@ -614,9 +614,12 @@ __device__ __forceinline__ void shift_tile(const Dom& D0, int64_t i, int64_t n, 
     }
     float Ma = P.compute_mach ? __uint_as_float(maxv[dom]) * P.inv_cs : 0.1f;
     float sc = P.sh_scale * Ma * P.m;
-    // update = clamp(-(sc * s)); x_new = x - update; the reference then adds (x_new - x) to x
-    float up0 = fminf(fmaxf(-(sc * s0), -P.sh_thr), P.sh_thr);
-    float up1 = fminf(fmaxf(-(sc * s1), -P.sh_thr), P.sh_thr);
+    // update = clamp(-(sc * s)) (after the free-surface projection when that is on);
+    // x_new = x - update; the reference then adds (x_new - x) to x
+    float u0 = -(sc * s0), u1 = -(sc * s1);
+    surface_project(sv, i, u0, u1);
+    float up0 = fminf(fmaxf(u0, -P.sh_thr), P.sh_thr);
+    float up1 = fminf(fmaxf(u1, -P.sh_thr), P.sh_thr);
     float2 x = Xr[i];
     float y0 = __fsub_rn(x.x, up0), y1 = __fsub_rn(x.y, up1);
     float2 xn = make_float2(__fadd_rn(x.x, __fsub_rn(y0, x.x)), __fadd_rn(x.y, __fsub_rn(y1, x.y)));
@@ -640,7 +643,7 @@ __global__ void __launch_bounds__(32 * W) k_shift(const Dom D0, int64_t n, const
                                                   const uint32_t* __restrict__ maxv, int enabled,
                                                   const int32_t* __restrict__ uid, float* __restrict__ dx_out,
                                                   int use_skin, const int16_t* __restrict__ sl,
-                                                  const int16_t* __restrict__ slc) {
+                                                  const int16_t* __restrict__ slc, const SurfaceView sv) {
     extern __shared__ __align__(16) unsigned char s_dyn[];
     __shared__ Dom s_dom[BATCH ? 2 : 1];
     __shared__ int s_id[2];
@@ -648,7 +651,7 @@ __global__ void __launch_bounds__(32 * W) k_shift(const Dom D0, int64_t n, const
     const int64_t first = (int64_t)blockIdx.x * (32 * W);
     if (BATCH) stage_doms(doms, did, first, first + 32 * W - 1, n, s_dom, s_id);
     shift_tile<PER, BATCH, LT>(D0, first + threadIdx.x, n, X4, V4, start, doms, s_dom, s_id, did, Xr, X4o, V4o,
-                               words, maxv, enabled, uid, dx_out, lst, use_skin, sl, slc);
+                               words, maxv, enabled, uid, dx_out, lst, use_skin, sl, slc, sv);
 }
 
 // max |u| over all particles (the Mach number of shifting.py:139-142)
@@ -1532,7 +1535,7 @@ static void launch_shift_k(sph_solver* S, float4* Xin, float4* Vin, float4* Xout
     k_shift<PER, BATCH, LT, W><<<gb, 32 * W, list_bytes<LT, W>(), st>>>(S->doms_host[0], S->n, Xin, Vin, S->start,
                                                                        S->doms, dids(S), S->Xr, Xout, Vout, S->words,
                                                                        S->maxv, S->prm.shift_on, S->uid, dx_out,
-                                                                       use_skin, S->sl, S->slc);
+                                                                       use_skin, S->sl, S->slc, surface_view(S));
 }
 
 template <typename LT, int W>
@@ -1563,6 +1566,8 @@ static int step_impl(sph_solver* S, int32_t n_steps, cudaStream_t st) {
         int rc = run_stages(S, st);
         if (rc) return rc;
         // shifting at the integrated positions, on the same cell sort and skin list
+        rc = surface_detect(S, S->Xf, st);
+        if (rc) return rc;
         if (S->ips) {
             rc = ips_shift(S, S->Xf, S->Vf, S->Xc, S->Vc, nullptr, S->periodic ? 0 : 1, st);
             if (rc) return rc;
@@ -1634,6 +1639,8 @@ extern "C" int sph_solver_shift(sph_solver_t* S, float* dx_out, sph_stream_t str
     if (rc) return rc;
     if (cudaMemsetAsync(S->maxv, 0, sizeof(uint32_t) * S->nd, st) != cudaSuccess) return SPH_ERR_CUDA;
     k_maxvel<<<blocks_for(S->n), kBlock, 0, st>>>(S->n, S->Vc, dids(S), S->maxv);
+    rc = surface_detect(S, S->Xc, st);
+    if (rc) return rc;
     if (S->ips) {
         rc = ips_shift(S, S->Xc, S->Vc, S->Xt, S->Vt, dx_out, 0, st);
         if (rc) return rc;

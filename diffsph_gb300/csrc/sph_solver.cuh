@@ -286,6 +286,39 @@ __device__ __forceinline__ void skin_loop(int self, float2 pi, const float4* __r
     }
 }
 
+// Free-surface fields of the shift (solveShifting with shifting.freeSurface), per slot;
+// fs == nullptr when the handling is off.
+struct SurfaceView {
+    const uint8_t* fs;    // on the surface (detectFreeSurfaceBarecasco)
+    const uint8_t* fsm;   // expanded mask (expandFreeSurfaceMask)
+    const float* lam;     // Lambdas: the smaller singular value of the normalization matrix
+    const float2* nrm;    // normalised lambda gradient
+    float scaling;        // shifting.surfaceScaling
+};
+
+// The projection of solveShifting (shifting.py:972-982, projectionScheme 'mat') applied to
+// the update before its clamp: (I - n n^T) u on the expanded mask, zero where Lambdas < 0.4,
+// times surfaceScaling on the surface.
+__device__ __forceinline__ void surface_project(const SurfaceView& sv, int64_t i, float& u0, float& u1) {
+    if (!sv.fs) return;
+    if (sv.fsm[i]) {
+        const float2 nn = sv.nrm[i];
+        const float m00 = 1.f - nn.x * nn.x, m01 = 0.f - nn.x * nn.y;
+        const float m10 = 0.f - nn.y * nn.x, m11 = 1.f - nn.y * nn.y;
+        const float r0 = m00 * u0 + m01 * u1, r1 = m10 * u0 + m11 * u1;
+        u0 = r0;
+        u1 = r1;
+    }
+    if (sv.lam[i] < 0.4f) {
+        u0 = 0.f;
+        u1 = 0.f;
+    }
+    if (sv.fs[i]) {
+        u0 *= sv.scaling;
+        u1 *= sv.scaling;
+    }
+}
+
 }  // namespace sph
 
 using namespace sph;
@@ -349,6 +382,17 @@ struct sph_solver {
     int16_t* ips_nl = nullptr;       // that list: slot offsets (warp-tile-major)
     int16_t* ips_nlc = nullptr;      // its length per slot (-1: not stored)
     int ips_sms = 0;                 // SM count of the device (grid caps)
+
+    // free-surface handling of the shift (shifting.freeSurface), off unless set
+    bool fs_on = false;
+    float fs_half_angle = 0.f;       // surfaceDetection.BarecascoThreshold / 2
+    int fs_expand = 2;               // surfaceDetection.expansionIterations
+    float fs_scaling = 0.1f;         // shifting.surfaceScaling
+    uint8_t *fs = nullptr, *fsm = nullptr, *fsm_t = nullptr;
+    float* fs_lam = nullptr;
+    float4* fs_L = nullptr;
+    float2* fs_nrm = nullptr;
+    int16_t *fs_nl = nullptr, *fs_nlc = nullptr;
     double* ips_part = nullptr;      // per-block partial sums
     void* ips_state = nullptr;       // scalars of the solve (device)
 };
@@ -358,6 +402,10 @@ struct sph_solver {
 int ips_shift(sph_solver* S, float4* Xin, float4* Vin, float4* Xout, float4* Vout, float* dx_out, int use_skin,
               cudaStream_t st);
 size_t ips_workspace_bytes(int64_t n);
+// The free-surface fields at the sorted state X4 (sph_surface.cu); a view of them for the
+// shift kernels (fs == nullptr when the handling is off).
+int surface_detect(sph_solver* S, const float4* X4, cudaStream_t st);
+SurfaceView surface_view(const sph_solver* S);
 
 inline unsigned blocks_for(int64_t n, int threads = kBlock) { return (unsigned)((n + threads - 1) / threads); }
 

@@ -1,0 +1,323 @@
+// Free-surface handling of the shift (shifting.freeSurface = True) for sm_103a.
+//
+// solveShifting (src/diffSPH/v2/modules/shifting.py:882-1019) with the reference's defaults
+// for this branch (surfaceDetection 'Barcasco', normalScheme 'lambda', projectionScheme
+// 'mat', useExtendedMask off) works on the merged fluid + wall particle set:
+//   fs  = detectFreeSurfaceBarecasco   (src/diffSPH/v2/modules/surfaceDetection.py:95-107)
+//         no neighbor j != i within the cone of half-angle threshold / 2 around the
+//         normalised cover vector sum_j -xhat_ij (a vanishing cover vector: interior)
+//   fsm = expandFreeSurfaceMask        (surfaceDetection.py:54-63), OR over the neighbors,
+//         expansionIterations times
+//   L, Lambdas = pinv2x2 of the normalization matrix and its smaller singular value
+//         (normalizationMatrices.py:7-16, math.py:11-57, surfaceDetection.py:41-52)
+//   n   = normalize(sum_j V_j (Lambda_i - Lambda_j) L_i gradW_ij)   (computeLambdaGrad,
+//         shifting.py:151-171)
+// and the shift kernels then project their update (surface_project). For the implicit
+// scheme the surface rows leave the system like wall rows (getShiftingMatrices :657-678).
+//
+// Three kinds of pass over the sorted slots, one thread per slot, every slot a row (walls
+// included: their flags feed the mask expansion of the fluid):
+//   k_fs_detect  stencil scan: cover vector, normalization matrix -> L, Lambdas; keeps the
+//                exact list (int16 offsets, edge-major); then the cone test over that list
+//   k_fs_normals over the list: the lambda gradient -> n, and the first mask expansion
+//   k_fs_expand  over the list: each further expansion
+// The cone test uses the reference's unit vectors bit for bit (correctly rounded sqrt and
+// division); the cover vector's summation order differs from the reference's, so a flag
+// can differ only for a pair within rounding of the cone's edge.
+#include <math.h>
+#include <string.h>
+
+#include <utility>
+
+#include "sph_solver.cuh"
+
+namespace sph {
+
+constexpr int kFsW = 4;  // warps per block
+
+// the reference's unit vector x_ij / (|x_ij| + 1e-7) (neighborhood.py:433-460)
+__device__ __forceinline__ void unit_ref(float x0, float x1, float& u0, float& u1) {
+    const float r = __fsqrt_rn(sq_norm_ref(x0, x1));
+    const float d = __fadd_rn(r, 1e-7f);
+    u0 = __fdiv_rn(x0, d);
+    u1 = __fdiv_rn(x1, d);
+}
+
+// torch.nn.functional.normalize: v / max(|v|, 1e-12)
+__device__ __forceinline__ float2 normalize_ref(float v0, float v1) {
+    const float nrm = fmaxf(sqrtf(v0 * v0 + v1 * v1), 1e-12f);
+    return make_float2(v0 / nrm, v1 / nrm);
+}
+
+template <bool PER, typename LT, int W>
+__global__ void __launch_bounds__(32 * W)
+    k_fs_detect(const Dom D, int64_t n, const float4* __restrict__ X4, const int32_t* __restrict__ start,
+                uint32_t* __restrict__ words, int16_t* __restrict__ fnl, int16_t* __restrict__ fnlc,
+                uint8_t* __restrict__ fs, float* __restrict__ lam, float4* __restrict__ Lout, float half_angle) {
+    extern __shared__ __align__(16) unsigned char s_dyn[];
+    LT* lst = reinterpret_cast<LT*>(s_dyn) + (threadIdx.x >> 5) * (kCap * 32);
+    const Phys& P = D.P;
+    const Grid& g = D.g;
+    const int64_t i = (int64_t)blockIdx.x * (32 * W) + threadIdx.x;
+    const bool inb = i < n;
+    const float4 xi = inb ? X4[i] : make_float4(0.f, 0.f, 1.f, 0.f);
+    const float2 pi = make_float2(xi.x, xi.y);
+    float c0 = 0.f, c1 = 0.f;                          // cover vector
+    float M00 = 0.f, M01 = 0.f, M10 = 0.f, M11 = 0.f;  // normalization matrix
+    int nst = 0;
+    bool unstored = false;
+    auto pair_m = [&](int j) {
+        int d = j - (int)i;
+        if (PER) {
+            const int h2 = g.nslots >> 1;
+            if (d > h2) d -= g.nslots;
+            else if (d < -h2) d += g.nslots;
+        }
+        if (nst < kStoreCap && d >= -32768 && d <= 32767)
+            fnl[(int64_t)nst * n + i] = (int16_t)d;
+        else
+            unstored = true;
+        ++nst;
+        const float4 xj = __ldg(&X4[j]);
+        float x0, x1;
+        pair_vec<PER>(pi, make_float2(xj.x, xj.y), P.geo, x0, x1);
+        float u0, u1;
+        unit_ref(x0, x1, u0, u1);
+        c0 -= u0;
+        c1 -= u1;
+        const PairG pg = pair_fast(x0, x1, sq_norm_ref(x0, x1), P.inv_h);
+        const float dW = wendland_dw(pg.q, P.kc);
+        const float V = __fdividef(P.m, fabsf(xj.z));
+        const float k0 = pg.xh0 * dW * V, k1 = pg.xh1 * dW * V;
+        const float d0 = -pg.r * pg.xh0, d1 = -pg.r * pg.xh1;  // -(q h) xhat
+        M00 = fmaf(d0, k0, M00);
+        M01 = fmaf(d0, k1, M01);
+        M10 = fmaf(d1, k0, M10);
+        M11 = fmaf(d1, k1, M11);
+    };
+    neighbor_loop<PER, LT>(inb, (int)i, pi, X4, start, g, P, lst, words, pair_m);
+    if (inb) fnlc[i] = unstored ? (int16_t)-1 : (int16_t)nst;
+    // the cone test over the same neighbors (the stored list, or a second scan)
+    const float2 cn = normalize_ref(c0, c1);
+    const bool interior = sqrtf(cn.x * cn.x + cn.y * cn.y) <= 1e-5f;
+    bool inside = false;  // some neighbor within the cone
+    auto pair_c = [&](int j) {
+        if (j == (int)i) return;
+        const float4 xj = __ldg(&X4[j]);
+        float x0, x1;
+        pair_vec<PER>(pi, make_float2(xj.x, xj.y), P.geo, x0, x1);
+        float u0, u1;
+        unit_ref(x0, x1, u0, u1);
+        const float dot = __fadd_rn(__fmul_rn(u0, cn.x), __fmul_rn(u1, cn.y));
+        if (acosf(dot) <= half_angle) inside = true;
+    };
+    const int cnt = inb ? (int)fnlc[i] : 0;
+    if (__any_sync(kFull, cnt < 0)) {
+        neighbor_loop<PER, LT>(inb && !interior, (int)i, pi, X4, start, g, P, lst, words, pair_c);
+    } else if (!interior) {
+        for (int k = 0; k < cnt; ++k) pair_c(list_slot<PER>((int)i, (int)fnl[(int64_t)k * n + i], g));
+    }
+    if (!inb) return;
+    fs[i] = (uint8_t)(!interior && !inside);
+    float o1, o2;
+    const M2 L = pinv2x2_ref(M00, M01, M10, M11, &o1, &o2);
+    lam[i] = fminf(fabsf(o1), fabsf(o2));
+    Lout[i] = make_float4(L.a, L.b, L.c, L.d);
+}
+
+// first mask expansion and the normalised lambda gradient
+template <bool PER, typename LT, int W>
+__global__ void __launch_bounds__(32 * W)
+    k_fs_normals(const Dom D, int64_t n, const float4* __restrict__ X4, const int32_t* __restrict__ start,
+                 uint32_t* __restrict__ words, const int16_t* __restrict__ fnl, const int16_t* __restrict__ fnlc,
+                 const uint8_t* __restrict__ fs, const float* __restrict__ lam, const float4* __restrict__ Lin,
+                 uint8_t* __restrict__ fsm, float2* __restrict__ nrm) {
+    extern __shared__ __align__(16) unsigned char s_dyn[];
+    LT* lst = reinterpret_cast<LT*>(s_dyn) + (threadIdx.x >> 5) * (kCap * 32);
+    const Phys& P = D.P;
+    const Grid& g = D.g;
+    const int64_t i = (int64_t)blockIdx.x * (32 * W) + threadIdx.x;
+    const bool inb = i < n;
+    const float4 xi = inb ? X4[i] : make_float4(0.f, 0.f, 1.f, 0.f);
+    const float2 pi = make_float2(xi.x, xi.y);
+    const float4 L = inb ? Lin[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float li = inb ? lam[i] : 0.f;
+    bool any = false;
+    float g0 = 0.f, g1 = 0.f;
+    auto pair_n = [&](int j) {
+        any = any || fs[j];
+        const float4 xj = __ldg(&X4[j]);
+        float x0, x1;
+        pair_vec<PER>(pi, make_float2(xj.x, xj.y), P.geo, x0, x1);
+        const PairG pg = pair_fast(x0, x1, sq_norm_ref(x0, x1), P.inv_h);
+        const float dW = wendland_dw(pg.q, P.kc);
+        const float gw0 = pg.xh0 * dW, gw1 = pg.xh1 * dW;
+        const float ng0 = L.x * gw0 + L.y * gw1, ng1 = L.z * gw0 + L.w * gw1;  // L_i gradW
+        const float w = __fdividef(P.m, fabsf(xj.z)) * (li - lam[j]);
+        g0 = fmaf(w, ng0, g0);
+        g1 = fmaf(w, ng1, g1);
+    };
+    const int cnt = inb ? (int)fnlc[i] : 0;
+    if (__any_sync(kFull, cnt < 0)) {
+        neighbor_loop<PER, LT>(inb, (int)i, pi, X4, start, g, P, lst, words, pair_n);
+    } else {
+        for (int k = 0; k < cnt; ++k) pair_n(list_slot<PER>((int)i, (int)fnl[(int64_t)k * n + i], g));
+    }
+    if (!inb) return;
+    fsm[i] = (uint8_t)any;
+    nrm[i] = normalize_ref(g0, g1);
+}
+
+// a further mask expansion: out_i = OR over the neighbors of in_j
+template <bool PER, typename LT, int W>
+__global__ void __launch_bounds__(32 * W)
+    k_fs_expand(const Dom D, int64_t n, const float4* __restrict__ X4, const int32_t* __restrict__ start,
+                uint32_t* __restrict__ words, const int16_t* __restrict__ fnl, const int16_t* __restrict__ fnlc,
+                const uint8_t* __restrict__ in, uint8_t* __restrict__ out) {
+    extern __shared__ __align__(16) unsigned char s_dyn[];
+    LT* lst = reinterpret_cast<LT*>(s_dyn) + (threadIdx.x >> 5) * (kCap * 32);
+    const Phys& P = D.P;
+    const Grid& g = D.g;
+    const int64_t i = (int64_t)blockIdx.x * (32 * W) + threadIdx.x;
+    const bool inb = i < n;
+    const float4 xi = inb ? X4[i] : make_float4(0.f, 0.f, 1.f, 0.f);
+    const float2 pi = make_float2(xi.x, xi.y);
+    bool any = false;
+    auto pair_e = [&](int j) { any = any || in[j]; };
+    const int cnt = inb ? (int)fnlc[i] : 0;
+    if (__any_sync(kFull, cnt < 0)) {
+        neighbor_loop<PER, LT>(inb, (int)i, pi, X4, start, g, P, lst, words, pair_e);
+    } else {
+        for (int k = 0; k < cnt; ++k) pair_e(list_slot<PER>((int)i, (int)fnl[(int64_t)k * n + i], g));
+    }
+    if (inb) out[i] = (uint8_t)any;
+}
+
+// the fields in the original particle order (fluid first, then walls)
+__global__ void k_fs_download(int64_t n, const int32_t* __restrict__ uid, const uint8_t* __restrict__ fs,
+                              const uint8_t* __restrict__ fsm, const float* __restrict__ lam,
+                              const float2* __restrict__ nrm, uint8_t* fs_out, uint8_t* fsm_out, float* lam_out,
+                              float* nrm_out) {
+    const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const int o = uid[s];
+    if (fs_out) fs_out[o] = fs[s];
+    if (fsm_out) fsm_out[o] = fsm[s];
+    if (lam_out) lam_out[o] = lam[s];
+    if (nrm_out) {
+        nrm_out[2 * o] = nrm[s].x;
+        nrm_out[2 * o + 1] = nrm[s].y;
+    }
+}
+
+template <bool PER, typename LT>
+static void fs_launch(sph_solver* S, const float4* X4, cudaStream_t st) {
+    const int64_t n = S->n;
+    const Dom& D = S->doms_host[0];
+    const unsigned gb = (unsigned)((n + 32 * kFsW - 1) / (32 * kFsW));
+    const size_t smem = list_bytes<LT, kFsW>();
+    k_fs_detect<PER, LT, kFsW><<<gb, 32 * kFsW, smem, st>>>(D, n, X4, S->start, S->words, S->fs_nl, S->fs_nlc, S->fs,
+                                                            S->fs_lam, S->fs_L, S->fs_half_angle);
+    k_fs_normals<PER, LT, kFsW><<<gb, 32 * kFsW, smem, st>>>(D, n, X4, S->start, S->words, S->fs_nl, S->fs_nlc, S->fs,
+                                                             S->fs_lam, S->fs_L, S->fsm, S->fs_nrm);
+    for (int k = 1; k < S->fs_expand; ++k) {
+        k_fs_expand<PER, LT, kFsW><<<gb, 32 * kFsW, smem, st>>>(D, n, X4, S->start, S->words, S->fs_nl, S->fs_nlc,
+                                                                S->fsm, S->fsm_t);
+        std::swap(S->fsm, S->fsm_t);
+    }
+}
+
+}  // namespace sph
+
+int surface_detect(sph_solver* S, const float4* X4, cudaStream_t st) {
+    if (!S->fs_on || !S->prm.shift_on) return SPH_OK;
+    if (S->periodic) {
+        if (S->list16) fs_launch<true, int16_t>(S, X4, st);
+        else fs_launch<true, int32_t>(S, X4, st);
+    } else {
+        if (S->list16) fs_launch<false, int16_t>(S, X4, st);
+        else fs_launch<false, int32_t>(S, X4, st);
+    }
+    return cudaGetLastError() == cudaSuccess ? SPH_OK : SPH_ERR_CUDA;
+}
+
+SurfaceView surface_view(const sph_solver* S) {
+    SurfaceView v;
+    const bool on = S->fs_on && S->prm.shift_on;
+    v.fs = on ? S->fs : nullptr;
+    v.fsm = on ? S->fsm : nullptr;
+    v.lam = on ? S->fs_lam : nullptr;
+    v.nrm = on ? S->fs_nrm : nullptr;
+    v.scaling = S->fs_scaling;
+    return v;
+}
+
+// workspace: list [kStoreCap][n] + length [n] (int16), fs, fsm, fsm_t [n] (uint8), Lambdas [n],
+// L [n] (float4), normals [n] (float2)
+static size_t fs_layout(int64_t n, char* base, sph_solver* S) {
+    auto up = [](size_t b) { return (b + 255) & ~(size_t)255; };
+    const size_t N = (size_t)n;
+    const size_t sz[8] = {up((size_t)kStoreCap * N * sizeof(int16_t)), up(N * sizeof(int16_t)), up(N), up(N), up(N),
+                          up(N * sizeof(float)), up(N * sizeof(float4)), up(N * sizeof(float2))};
+    if (S && base) {
+        char* w = base;
+        S->fs_nl = reinterpret_cast<int16_t*>(w);
+        w += sz[0];
+        S->fs_nlc = reinterpret_cast<int16_t*>(w);
+        w += sz[1];
+        S->fs = reinterpret_cast<uint8_t*>(w);
+        w += sz[2];
+        S->fsm = reinterpret_cast<uint8_t*>(w);
+        w += sz[3];
+        S->fsm_t = reinterpret_cast<uint8_t*>(w);
+        w += sz[4];
+        S->fs_lam = reinterpret_cast<float*>(w);
+        w += sz[5];
+        S->fs_L = reinterpret_cast<float4*>(w);
+        w += sz[6];
+        S->fs_nrm = reinterpret_cast<float2*>(w);
+    }
+    size_t t = 0;
+    for (size_t b : sz) t += b;
+    return t;
+}
+
+extern "C" int sph_solver_free_surface_workspace_bytes(const sph_solver_t* S, size_t* bytes) {
+    if (!S || !bytes) return SPH_ERR_ARGUMENT;
+    *bytes = fs_layout(S->n, nullptr, nullptr);
+    return SPH_OK;
+}
+
+extern "C" int sph_solver_set_free_surface(sph_solver_t* S, const sph_free_surface_params_t* p, void* workspace,
+                                           size_t workspace_bytes) {
+    if (!S) return SPH_ERR_ARGUMENT;
+    for (int k = 0; k < 2; ++k)  // captured graphs hold the launches without the handling
+        if (S->graph[k]) {
+            cudaGraphExecDestroy(S->graph[k]);
+            S->graph[k] = nullptr;
+            S->graph_n[k] = 0;
+        }
+    if (!p) {
+        S->fs_on = false;
+        return SPH_OK;
+    }
+    if (S->nd != 1 || !workspace || p->expansion_iterations < 1 || !(p->barecasco_threshold >= 0.0))
+        return SPH_ERR_ARGUMENT;
+    if ((reinterpret_cast<uintptr_t>(workspace) & 255u) != 0) return SPH_ERR_ARGUMENT;
+    if (workspace_bytes < fs_layout(S->n, nullptr, nullptr)) return SPH_ERR_WORKSPACE;
+    fs_layout(S->n, static_cast<char*>(workspace), S);
+    S->fs_half_angle = (float)(p->barecasco_threshold / 2.0);
+    S->fs_expand = p->expansion_iterations;
+    S->fs_scaling = (float)p->surface_scaling;
+    S->fs_on = true;
+    return SPH_OK;
+}
+
+extern "C" int sph_solver_free_surface_fields(sph_solver_t* S, uint8_t* fs, uint8_t* fsm, float* lambdas,
+                                              float* normals, sph_stream_t stream) {
+    if (!S || !S->fs_on) return SPH_ERR_ARGUMENT;
+    cudaStream_t st = (cudaStream_t)stream;
+    k_fs_download<<<blocks_for(S->n), kBlock, 0, st>>>(S->n, S->uid, S->fs, S->fsm, S->fs_lam, S->fs_nrm, fs, fsm,
+                                                        lambdas, normals);
+    return cudaGetLastError() == cudaSuccess ? SPH_OK : SPH_ERR_CUDA;
+}

@@ -110,10 +110,14 @@ def params_from_config(cfg, mass: float, skin: float = DEFAULT_SKIN, capacity: i
     p.gravity[0], p.gravity[1] = direction[0] * mag, direction[1] * mag
     p.dt = _f(cfg["timestep"]["dt"])
     sh = cfg.get("shifting", {})
-    if sh.get("scheme", "deltaSPH") not in ("deltaSPH", "IPS") or sh.get("freeSurface", False) \
-            or int(sh.get("maxIterations", 1)) != 1:
-        raise ValueError("only delta+ and implicit (IPS) shifting with one iteration and no free-surface "
-                         "handling are implemented")
+    if sh.get("scheme", "deltaSPH") not in ("deltaSPH", "IPS") or int(sh.get("maxIterations", 1)) != 1:
+        raise ValueError("only delta+ and implicit (IPS) shifting with one iteration are implemented")
+    if sh.get("freeSurface", False) and (sh.get("surfaceDetection", "Barcasco") != "Barcasco"
+                                         or sh.get("normalScheme", "lambda") != "lambda"
+                                         or sh.get("projectionScheme", "mat") != "mat"
+                                         or sh.get("useExtendedMask", False)):
+        raise ValueError("free-surface shifting is implemented with surfaceDetection 'Barcasco', normalScheme "
+                         "'lambda', projectionScheme 'mat' and useExtendedMask off")
     if sh.get("scheme", "deltaSPH") == "IPS" and (sh.get("summationDensity", False)
                                                   or sh.get("initialization", "zero") != "zero"):
         raise ValueError("implicit shifting is implemented with summationDensity off and a zero initial guess")
@@ -173,6 +177,11 @@ class Solver:
         if sh.get("scheme", "deltaSPH") == "IPS":
             self.set_ips(rtol=float(sh.get("rtol", 1e-4)), max_iter=int(sh.get("maxSolveIter", 64)),
                          solver_threshold=float(sh.get("solverThreshold", -0.5)))
+        if sh.get("freeSurface", False):
+            sd = config.get("surfaceDetection", {})
+            self.set_free_surface(threshold=_f(sd.get("BarecascoThreshold", math.pi / 3)),
+                                  expansion=int(sd.get("expansionIterations", 2)),
+                                  scaling=_f(sh.get("surfaceScaling", 0.1)))
 
     def __del__(self):
         h = getattr(self, "handle", None)
@@ -236,6 +245,35 @@ class Solver:
         p = _lib.IpsParams(float(rtol), int(max_iter), float(thr))
         _lib.check("sph_solver_set_ips", self.lib.sph_solver_set_ips(self.handle, ctypes.byref(p),
                                                                      ctypes.c_void_p(ptr), nbytes.value))
+
+    def set_free_surface(self, threshold: float | None = math.pi / 3, expansion: int = 2, scaling: float = 0.1):
+        """Free-surface handling of the shift (shifting.freeSurface; Barecasco detection,
+        'lambda' normals, 'mat' projection; src/diffSPH/v2/modules/shifting.py:882-1019).
+        ``set_free_surface(None)`` switches it off."""
+        if threshold is None:
+            _lib.check("sph_solver_set_free_surface", self.lib.sph_solver_set_free_surface(self.handle, None, None, 0))
+            self._fs_ws = None
+            return
+        nbytes = ctypes.c_size_t()
+        _lib.check("sph_solver_free_surface_workspace_bytes",
+                   self.lib.sph_solver_free_surface_workspace_bytes(self.handle, ctypes.byref(nbytes)))
+        self._fs_ws = torch.empty(int(nbytes.value) + 256, dtype=torch.uint8, device="cuda")
+        ptr = (self._fs_ws.data_ptr() + 255) & ~255
+        p = _lib.FreeSurfaceParams(float(threshold), int(expansion), float(scaling))
+        _lib.check("sph_solver_set_free_surface", self.lib.sph_solver_set_free_surface(
+            self.handle, ctypes.byref(p), ctypes.c_void_p(ptr), nbytes.value))
+
+    def free_surface_fields(self):
+        """Surface flags, expanded mask, Lambdas and normals of the last shift's detection,
+        for the fluid particles followed by the walls (original order)."""
+        n = self.nF + self.nB
+        fs = torch.empty(n, dtype=torch.uint8, device="cuda")
+        fsm = torch.empty(n, dtype=torch.uint8, device="cuda")
+        lam = torch.empty(n, device="cuda")
+        nrm = torch.empty(n, 2, device="cuda")
+        _lib.check("sph_solver_free_surface_fields", self.lib.sph_solver_free_surface_fields(
+            self.handle, _ptr(fs), _ptr(fsm), _ptr(lam), _ptr(nrm), _stream()))
+        return {"freeSurface": fs.bool(), "freeSurfaceMask": fsm.bool(), "Lambdas": lam, "normals": nrm}
 
     def ips_result(self):
         """(iterations, code) of the last implicit shifting solve; code is bicgstab_shifting's

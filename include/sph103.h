@@ -247,6 +247,33 @@ int sph_solver_set_ips(sph_solver_t* s, const sph_ips_params_t* params, void* wo
  * loop ran out) of the last solve. Synchronises the stream. */
 int sph_solver_ips_result(sph_solver_t* s, int32_t* iterations, int32_t* code, sph_stream_t stream);
 
+/* ------------------------------------------------------------------------------------
+ * Free-surface handling of the shift (shifting.freeSurface = True): solveShifting
+ * (src/diffSPH/v2/modules/shifting.py:882-1019) with surface detection 'Barcasco'
+ * (detectFreeSurfaceBarecasco, surfaceDetection.py:95-107), the mask expansion
+ * (expandFreeSurfaceMask, :54-63), normals 'lambda' (computeNormalsMaronne :41-52 and
+ * computeLambdaGrad, shifting.py:151-171) and projection 'mat' (shifting.py:972-982), on the
+ * merged fluid and wall particles. Applies to the delta+ and the IPS shift (whose system
+ * then drops the surface rows, getShiftingMatrices :657-678). Single-domain solvers only.
+ * ------------------------------------------------------------------------------------ */
+typedef struct sph_free_surface_params {
+    double barecasco_threshold;    /* surfaceDetection.BarecascoThreshold (pi / 3) */
+    int32_t expansion_iterations;  /* surfaceDetection.expansionIterations (2) */
+    double surface_scaling;        /* shifting.surfaceScaling (0.1) */
+} sph_free_surface_params_t;
+
+/* Bytes of the free-surface workspace (about 160 B per particle, walls included). */
+int sph_solver_free_surface_workspace_bytes(const sph_solver_t* s, size_t* bytes);
+/* Switches the handling on (params != NULL; workspace 256-byte aligned) or off (NULL).
+ * Drops captured graphs. */
+int sph_solver_set_free_surface(sph_solver_t* s, const sph_free_surface_params_t* params,
+                                void* workspace, size_t workspace_bytes);
+/* The fields of the last shift's detection, in the original order of the merged set (fluid
+ * particles, then walls; NULL entries are skipped): surface flags fs[n] and expanded mask
+ * fsm[n] (uint8), Lambdas[n], normals[n][2]. */
+int sph_solver_free_surface_fields(sph_solver_t* s, uint8_t* fs, uint8_t* fsm, float* lambdas,
+                                   float* normals, sph_stream_t stream);
+
 /* Writes the current state back in the original order (NULL entries are skipped). */
 int sph_solver_download(sph_solver_t* s, float* x_fluid, float* u_fluid, float* rho_fluid,
                         float* rho_boundary, sph_stream_t stream);

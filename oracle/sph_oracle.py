@@ -181,8 +181,9 @@ def scatter_sum(src, index, n):
     return out
 
 
-def pinv2x2(M):
-    """Closed-form 2x2 pseudo-inverse via an SVD built from atan2/cos/sin, math.py:11-57."""
+def pinv2x2(M, eigenvalues=False):
+    """Closed-form 2x2 pseudo-inverse via an SVD built from atan2/cos/sin, math.py:11-57
+    (with its singular values, ordered by magnitude, when ``eigenvalues``)."""
     a, b, c, d = M[:, 0, 0], M[:, 0, 1], M[:, 1, 0], M[:, 1, 1]
     theta = 0.5 * np.arctan2(2 * a * c + 2 * b * d, a ** 2 + b ** 2 - c ** 2 - d ** 2)
     ct, st = np.cos(theta), np.sin(theta)
@@ -202,7 +203,14 @@ def pinv2x2(M):
     o2i = np.where(np.abs(o2) > 1e-5, 1 / np.where(o2 == 0, 1, o2), 0).astype(M.dtype)
     S = np.zeros_like(M)
     S[:, 0, 0], S[:, 1, 1] = o1i, o2i
-    return np.matmul(np.matmul(V, S), np.swapaxes(U, 1, 2))
+    L = np.matmul(np.matmul(V, S), np.swapaxes(U, 1, 2))
+    if not eigenvalues:
+        return L
+    # eigVals: (o1, o2), swapped where |o2| > |o1| (math.py:53-54)
+    ev = np.stack([o1, o2], axis=1)
+    sw = np.abs(ev[:, 1]) > np.abs(ev[:, 0])
+    ev[sw] = ev[sw][:, ::-1]
+    return L, ev
 
 
 # ----------------------------------------------------------------------------------------
@@ -653,11 +661,85 @@ def ips_shift(ps, nb, marker, config):
     return -xk.reshape(-1, 2), (iters, status)
 
 
+# ----------------------------------------------------------------------------------------
+# Free-surface handling of the shift (solveShifting with shifting.freeSurface)
+# ----------------------------------------------------------------------------------------
+def _normalize(v):
+    """torch.nn.functional.normalize: v / max(|v|, 1e-12) per row."""
+    nrm = np.sqrt(np.sum(v * v, axis=1))
+    return v / np.maximum(nrm, v.dtype.type(1e-12))[:, None]
+
+
+def _scatter_or(flags, index, n):
+    out = np.zeros(n, dtype=bool)
+    np.logical_or.at(out, index, flags)
+    return out
+
+
+def detect_free_surface_barecasco(ps, nb, config):
+    """detectFreeSurfaceBarecasco surfaceDetection.py:95-107: a particle is on the surface
+    when no neighbor lies within the cone of half-angle threshold / 2 around its normalised
+    cover vector sum_j -xhat_ij (a vanishing cover vector marks it interior)."""
+    i, j = nb["indices"]
+    n = ps["positions"].shape[0]
+    xij = nb["vectors"]
+    nrm = _normalize(scatter_sum(-xij, i, n))
+    with np.errstate(invalid="ignore"):
+        angle = np.arccos(np.einsum("ij,ij->i", xij, nrm[i]))
+    dt = xij.dtype.type
+    half = dt(_flt(config.get("surfaceDetection", {}).get("BarecascoThreshold", np.pi / 3)) / 2)
+    cond = ((angle <= half) & (i != j)) | (np.sqrt(np.sum(nrm * nrm, axis=1))[i] <= dt(1e-5))
+    return ~_scatter_or(cond, i, n)
+
+
+def expand_free_surface_mask(fs, nb, config):
+    """expandFreeSurfaceMask surfaceDetection.py:54-63: expansionIterations rounds of OR over
+    the neighbors."""
+    i, j = nb["indices"]
+    fsm = fs.copy()
+    for _ in range(int(config.get("surfaceDetection", {}).get("expansionIterations", 2))):
+        fsm = _scatter_or(fsm[j], i, fs.shape[0])
+    return fsm
+
+
+def normals_lambda(ps, nb, gradient=False):
+    """computeNormalizationMatrices normalizationMatrices.py:7-16 (L and its singular values),
+    computeNormalsMaronne surfaceDetection.py:41-52 (Lambdas = the smaller one) and the
+    normalised computeLambdaGrad shifting.py:151-171: sum_j V_j (Lambda_i - Lambda_j) L_i gradW.
+    Returns (normals, Lambdas, L), or the gradient before normalisation when ``gradient``."""
+    i, j = nb["indices"]
+    n = ps["positions"].shape[0]
+    M = compute_covariance(ps, ps, nb, None)
+    L, ev = pinv2x2(M, eigenvalues=True)
+    lam = np.min(np.abs(ev), axis=1)
+    ng = np.einsum("ijk,ik->ij", L[i], nb["gradients"])
+    k = _vol(ps, j)[:, None] * ng
+    grad = scatter_sum((lam[i] - lam[j])[:, None] * k, i, n)
+    if gradient:
+        return grad
+    return _normalize(grad), lam, L
+
+
+def free_surface_projection(update, fs, fsm, normals, lam, config):
+    """solveShifting shifting.py:972-982 (projectionScheme 'mat'): (I - n n^T) update on the
+    expanded mask, zero where Lambdas < 0.4, times surfaceScaling on the surface."""
+    dt = update.dtype.type
+    nmat = np.einsum("ij,ik->ikj", normals, normals)
+    Mp = np.eye(2, dtype=dt)[None] - nmat
+    res = np.einsum("nab,nb->na", Mp, update)
+    update = update.copy()
+    update[fsm] = res[fsm]
+    update[lam < dt(0.4)] = 0
+    update[fs] = update[fs] * dt(_flt(config["shifting"].get("surfaceScaling", 0.1)))
+    return update
+
+
 def solve_shifting(state, config, info=None):
-    """solveShifting shifting.py:882-1019 with maxIterations = 1 and no free-surface
-    handling, delta+ (deltaPlusShifting) or implicit (IPS) scheme: returns the position
-    increment of the fluid particles. ``info`` (a dict) receives the IPS solve's
-    iteration count, return code and right-hand side."""
+    """solveShifting shifting.py:882-1019 with maxIterations = 1, delta+ (deltaPlusShifting)
+    or implicit (IPS) scheme, with the free-surface handling of shifting.freeSurface
+    (Barecasco detection, 'lambda' normals, 'mat' projection): returns the position
+    increment of the fluid particles. ``info`` (a dict) receives the IPS solve's iteration
+    count and return code, and the free-surface fields of the merged particle set."""
     fl = state["fluid"]
     nF = fl["positions"].shape[0]
     keys = ("positions", "velocities", "masses", "densities", "supports", "areas")
@@ -669,12 +751,22 @@ def solve_shifting(state, config, info=None):
         ps = {k: fl[k] for k in keys}
         marker = np.zeros(nF, np.int32)
     nb = neighbor_search(ps, ps, config)
+    free = bool(config["shifting"].get("freeSurface", False))
+    if free:
+        fs = detect_free_surface_barecasco(ps, nb, config)
+        fsm = expand_free_surface_mask(fs, nb, config)
     if config["shifting"].get("scheme", "deltaSPH") == "IPS":
-        update, stats = ips_shift(ps, nb, marker, config)
+        # surface particles leave the system like wall rows (getShiftingMatrices :657-678)
+        update, stats = ips_shift(ps, nb, np.where(fs, 1, marker) if free else marker, config)
         if info is not None:
             info["iterations"], info["code"] = stats
     else:
         update = -delta_plus_shifting(ps, nb, config)
+    if free:
+        normals, lam, _ = normals_lambda(ps, nb)
+        update = free_surface_projection(update, fs, fsm, normals, lam, config)
+        if info is not None:
+            info.update(freeSurface=fs, freeSurfaceMask=fsm, normals=normals, Lambdas=lam)
     dt = fl["densities"].dtype.type
     thr = dt(_flt(config["shifting"]["threshold"]) * _flt(config["particle"]["dx"]))
     update = np.clip(update, -thr, thr)

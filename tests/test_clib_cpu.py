@@ -102,8 +102,16 @@ def test_params_accept_the_implicit_shifting_scheme():
         params_from_config(cfg, 1.0)
     cfg["shifting"]["initialization"] = "zero"
     cfg["shifting"]["freeSurface"] = True
+    params_from_config(cfg, 1.0)
+    cfg["shifting"]["surfaceDetection"] = "Maronne"
     with pytest.raises(ValueError):
         params_from_config(cfg, 1.0)
+
+
+def test_free_surface_params_struct_layout():
+    from diffsph_gb300 import _lib
+    assert ctypes.sizeof(_lib.FreeSurfaceParams) == 24
+    assert _lib.FreeSurfaceParams.surface_scaling.offset == 16
 
 
 def test_ips_params_struct_layout():

@@ -144,3 +144,25 @@ def test_ips_shift_against_reference(case):
     ps_n = st["fluid"]["positions"].shape[0]
     assert rel_max(dx, z["ips/shift"]) < 1e-4
     assert dx.shape == z["ips/shift"].shape and ps_n == dx.shape[0]
+
+
+FS_CASES = ["dambreak32_dplus", "dambreak32_ips", "dambreak24_jitter_dplus"]
+
+
+@pytest.mark.parametrize("case", FS_CASES)
+def test_free_surface_shift_against_reference(case):
+    """solveShifting with shifting.freeSurface: the oracle's surface flags and expanded mask
+    equal the reference's, its Lambdas and fluid normals agree to rounding, and so does the
+    shift (the IPS case ends with the reference's return code)."""
+    z, cfg, st = load_case(f"fs_{case}")
+    info = {}
+    dx, _ = O.solve_shifting(copy.deepcopy(st), cfg, info)
+    nF = st["fluid"]["positions"].shape[0]
+    assert np.array_equal(info["freeSurface"], z["fs/freeSurface"])
+    assert np.array_equal(info["freeSurfaceMask"], z["fs/freeSurfaceMask"])
+    assert rel_max(info["Lambdas"], z["fs/Lambdas"]) < 1e-5
+    # normals of vanishing lambda gradients (wall rows deep in the wall) are rounding noise
+    assert rel_max(info["normals"][:nF], z["fs/lambdaGrad"][:nF]) < 1e-3
+    assert rel_max(dx, z["fs/shift"]) < 1e-3
+    if "code" in info:
+        assert info["code"] == -12 or info["code"] >= 0
