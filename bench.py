@@ -43,6 +43,9 @@ WORKLOADS = {
     "dambreak_dx1024": dict(scene="dam_break", dx=1.0 / 1024),
     "batched_256": dict(scene="batched", domains=256, seed=0),
     "dambreak_dx512": dict(scene="dam_break", dx=1.0 / 512),
+    # the same dam break with the free-surface handling of the shift (shifting.freeSurface)
+    "dambreak_fs_dx1024": dict(scene="dam_break", dx=1.0 / 1024, free_surface=True),
+    "dambreak_fs_dx512": dict(scene="dam_break", dx=1.0 / 512, free_surface=True),
     "dambreak_dx256": dict(scene="dam_break", dx=1.0 / 256),
     "tgv_64": dict(scene="taylor_green", nx=64),
     # implicit particle shifting (shifting.scheme 'IPS'): jittered periodic Fourier flow
@@ -62,7 +65,10 @@ def make_scene(name):
     from diffsph_gb300 import scenes
     w = WORKLOADS[name]
     if w["scene"] == "dam_break":
-        return scenes.dam_break(dx=w["dx"])
+        cfg, st = scenes.dam_break(dx=w["dx"])
+        if w.get("free_surface"):
+            cfg["shifting"]["freeSurface"] = True
+        return cfg, st
     if w["scene"] == "fourier":
         cfg, st = scenes.fourier_periodic(w["nx"], seed=w["seed"], jitter=w["jitter"])
         if w.get("ips"):
@@ -147,7 +153,7 @@ def cpu_baseline(workload, budget_s=20.0):
         cfg, st = scenes.batched_fourier(1, seed=w.get("seed", 0), n_min=4096, n_max=4096)[0]
         sample = "one 64x64 domain of the batch generator"
     elif w["scene"] == "dam_break":
-        cfg, st = scenes.dam_break(dx=1.0 / 64)
+        cfg, st = _reference_sample(workload)
         sample = "dam break dx=1/64 (same scene and parameters, coarser lattice)"
     elif w["scene"] == "fourier":
         cfg, st = _reference_sample(workload)
@@ -225,7 +231,10 @@ def _reference_sample(workload):
     from diffsph_gb300 import scenes
     sc = WORKLOADS[workload]["scene"]
     if sc == "dam_break":
-        return scenes.dam_break(dx=1.0 / 64)
+        cfg, st = scenes.dam_break(dx=1.0 / 64)
+        if WORKLOADS[workload].get("free_surface"):
+            cfg["shifting"]["freeSurface"] = True
+        return cfg, st
     if sc == "batched":
         return scenes.batched_fourier(1, seed=0, n_min=4096, n_max=4096)[0]
     if sc == "fourier":
@@ -344,7 +353,7 @@ def run_ours(args):
         ms = e0.elapsed_time(e1)
         # per-kernel times from a short event-timed eager loop of the same step
         sol.set_timing(["pass_b_rates", "pass_a_gradient", "pass_a_scan", "shift", "cell_sort", "gather",
-                        "mdbc_ghosts", "ips_setup", "ips_spmv", "ips_vector"])
+                        "mdbc_ghosts", "ips_setup", "ips_spmv", "ips_vector", "free_surface"])
         ips_iters = []
         for _ in range(4):
             sol.step(1)
@@ -415,7 +424,8 @@ def run_ours(args):
         "config": {"workload": args.workload, "fluid_particles": nF, "boundary_particles": nB,
                    "mean_neighbors": round(nbar, 3), "l2": "state (> 160 MB) exceeds L2; no flush",
                    "parallelism": "replicas" if world > 1 else "single", "graph": not ips,
-                   "shifting": "IPS" if ips else "deltaPlus",
+                   "shifting": ("IPS" if ips else "deltaPlus") + (
+                       "+freeSurface" if WORKLOADS[args.workload].get("free_surface") else ""),
                    "launch_shape": shape, "shape_ms": [round(v, 4) for v in shape_ms]},
         "e2e": e2e,
         "roofline": roofline,

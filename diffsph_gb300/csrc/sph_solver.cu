@@ -34,7 +34,7 @@ namespace sph {
 
 static const char* kClassNames[KC_COUNT] = {"cell_sort", "gather", "mdbc_ghosts", "pass_a_gradient",
                                              "pass_b_rates", "shift", "pass_a_scan", "ips_setup",
-                                             "ips_spmv", "ips_vector"};
+                                             "ips_spmv", "ips_vector", "free_surface"};
 
 // ------------------------------------------------------------------------------------
 // upload / download / gather
@@ -1803,8 +1803,12 @@ extern "C" int sph_solver_flags(sph_solver_t* S, uint32_t* flags_host, sph_strea
 
 extern "C" int sph_solver_launches_per_step(const sph_solver_t* S) {
     if (!S) return -1;
-    // cell keys, scan (3), scatter, cell order, gather, 2 x (mdbc moments and solve?, pass A, pass B), shift
-    return 7 + 2 * ((S->nB > 0 ? 2 : 0) + 2) + 1;
+    // cell keys, scan (3), scatter, cell order, gather, 2 x (mdbc moments and solve?, pass A, pass B), shift;
+    // the free-surface passes (detection, normals, expansions) when on. An implicit shift adds
+    // its solve's launches (1 + 5 per iteration + 1 in place of the shift), which depend on
+    // how many iterations it runs.
+    const int fs = (S->fs_on && S->prm.shift_on) ? 2 + (S->fs_expand - 1) : 0;
+    return 7 + 2 * ((S->nB > 0 ? 2 : 0) + 2) + 1 + fs;
 }
 
 extern "C" int sph_solver_kernel_classes(void) { return KC_COUNT; }

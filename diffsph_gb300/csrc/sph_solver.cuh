@@ -16,10 +16,11 @@ namespace sph {
 // pass_a_gradient: pass A launches that filter the skin list; pass_a_scan: those that scan
 // the cell stencil (the first pass A after a sort, and every pass A of a periodic domain)
 // ips_setup / ips_spmv / ips_vector: the implicit shift's neighbor pass (b and its list), its
-// matrix products, and its vector updates (with the final position update)
+// matrix products, and its vector updates (with the final position update); free_surface:
+// the surface detection passes of the shift
 enum KernelClass {
     KC_SORT = 0, KC_GATHER, KC_MDBC, KC_PASS_A, KC_PASS_B, KC_SHIFT, KC_PASS_A_SCAN,
-    KC_IPS_SETUP, KC_IPS_SPMV, KC_IPS_VECTOR, KC_COUNT
+    KC_IPS_SETUP, KC_IPS_SPMV, KC_IPS_VECTOR, KC_SURFACE, KC_COUNT
 };
 
 // Launch shapes of the neighbor passes (warps per block, list entry width), picked per
@@ -385,7 +386,7 @@ struct sph_solver {
 
     // free-surface handling of the shift (shifting.freeSurface), off unless set
     bool fs_on = false;
-    float fs_half_angle = 0.f;       // surfaceDetection.BarecascoThreshold / 2
+    float fs_cos_half = 0.f;         // cos(surfaceDetection.BarecascoThreshold / 2)
     int fs_expand = 2;               // surfaceDetection.expansionIterations
     float fs_scaling = 0.1f;         // shifting.surfaceScaling
     uint8_t *fs = nullptr, *fsm = nullptr, *fsm_t = nullptr;

@@ -22,8 +22,9 @@
 //   k_fs_normals over the list: the lambda gradient -> n, and the first mask expansion
 //   k_fs_expand  over the list: each further expansion
 // The cone test uses the reference's unit vectors bit for bit (correctly rounded sqrt and
-// division); the cover vector's summation order differs from the reference's, so a flag
-// can differ only for a pair within rounding of the cone's edge.
+// division) and tests acos(d) <= threshold / 2 as d >= cos(threshold / 2); the cover vector's
+// summation order differs from the reference's, so a flag can differ only for a pair within
+// rounding of the cone's edge.
 #include <math.h>
 #include <string.h>
 
@@ -53,7 +54,7 @@ template <bool PER, typename LT, int W>
 __global__ void __launch_bounds__(32 * W)
     k_fs_detect(const Dom D, int64_t n, const float4* __restrict__ X4, const int32_t* __restrict__ start,
                 uint32_t* __restrict__ words, int16_t* __restrict__ fnl, int16_t* __restrict__ fnlc,
-                uint8_t* __restrict__ fs, float* __restrict__ lam, float4* __restrict__ Lout, float half_angle) {
+                uint8_t* __restrict__ fs, float* __restrict__ lam, float4* __restrict__ Lout, float cos_half) {
     extern __shared__ __align__(16) unsigned char s_dyn[];
     LT* lst = reinterpret_cast<LT*>(s_dyn) + (threadIdx.x >> 5) * (kCap * 32);
     const Phys& P = D.P;
@@ -81,11 +82,9 @@ __global__ void __launch_bounds__(32 * W)
         const float4 xj = __ldg(&X4[j]);
         float x0, x1;
         pair_vec<PER>(pi, make_float2(xj.x, xj.y), P.geo, x0, x1);
-        float u0, u1;
-        unit_ref(x0, x1, u0, u1);
-        c0 -= u0;
-        c1 -= u1;
         const PairG pg = pair_fast(x0, x1, sq_norm_ref(x0, x1), P.inv_h);
+        c0 -= pg.xh0;  // the cover vector only sets the cone's axis: its summation order already
+        c1 -= pg.xh1;  // differs from the reference's, so the unit vectors need no exact rounding
         const float dW = wendland_dw(pg.q, P.kc);
         const float V = __fdividef(P.m, fabsf(xj.z));
         const float k0 = pg.xh0 * dW * V, k1 = pg.xh1 * dW * V;
@@ -102,20 +101,22 @@ __global__ void __launch_bounds__(32 * W)
     const bool interior = sqrtf(cn.x * cn.x + cn.y * cn.y) <= 1e-5f;
     bool inside = false;  // some neighbor within the cone
     auto pair_c = [&](int j) {
-        if (j == (int)i) return;
+        if (j == (int)i || inside) return;
         const float4 xj = __ldg(&X4[j]);
         float x0, x1;
         pair_vec<PER>(pi, make_float2(xj.x, xj.y), P.geo, x0, x1);
         float u0, u1;
         unit_ref(x0, x1, u0, u1);
         const float dot = __fadd_rn(__fmul_rn(u0, cn.x), __fmul_rn(u1, cn.y));
-        if (acosf(dot) <= half_angle) inside = true;
+        // acos(dot) <= half_angle, tested as dot >= cos(half_angle) (acos is decreasing)
+        if (dot >= cos_half) inside = true;
     };
     const int cnt = inb ? (int)fnlc[i] : 0;
     if (__any_sync(kFull, cnt < 0)) {
         neighbor_loop<PER, LT>(inb && !interior, (int)i, pi, X4, start, g, P, lst, words, pair_c);
     } else if (!interior) {
-        for (int k = 0; k < cnt; ++k) pair_c(list_slot<PER>((int)i, (int)fnl[(int64_t)k * n + i], g));
+        // stops at the first neighbor inside the cone (most rows find one within a few)
+        for (int k = 0; k < cnt && !inside; ++k) pair_c(list_slot<PER>((int)i, (int)fnl[(int64_t)k * n + i], g));
     }
     if (!inb) return;
     fs[i] = (uint8_t)(!interior && !inside);
@@ -210,6 +211,32 @@ __global__ void k_fs_download(int64_t n, const int32_t* __restrict__ uid, const 
     }
 }
 
+// computePressureAccelSwitch (src/diffSPH/v2/modules/pressureForce.py:15-33) on a
+// neighborhood in the reference's format: rows sorted by the query index, one thread per row,
+// its pairs in the stored order, each fp32 step in the reference's order (so the sums are
+// the reference's bit for bit when the inputs are).
+__global__ void k_pressure_switch(int64_t n, const int32_t* __restrict__ off, const int32_t* __restrict__ cnt,
+                                  const int64_t* __restrict__ pj, const float* __restrict__ grad,
+                                  const float* __restrict__ pA, const float* __restrict__ rhoA,
+                                  const float* __restrict__ maskA, const float* __restrict__ pB,
+                                  const float* __restrict__ rhoB, const float* __restrict__ mB, float* __restrict__ out) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float p_i = pA[i], r_i = rhoA[i];
+    const bool sum = p_i >= 0.f || (maskA && maskA[i] > 0.5f);
+    float a0 = 0.f, a1 = 0.f;
+    const int64_t e0 = off[i], e1 = e0 + cnt[i];
+    for (int64_t e = e0; e < e1; ++e) {
+        const int64_t j = pj[e];
+        const float pij = sum ? __fadd_rn(pB[j], p_i) : __fsub_rn(pB[j], p_i);
+        const float k = __fdiv_rn(mB[j], __fmul_rn(r_i, rhoB[j]));
+        a0 = __fadd_rn(a0, __fmul_rn(pij, __fmul_rn(k, grad[2 * e])));
+        a1 = __fadd_rn(a1, __fmul_rn(pij, __fmul_rn(k, grad[2 * e + 1])));
+    }
+    out[2 * i] = -a0;
+    out[2 * i + 1] = -a1;
+}
+
 template <bool PER, typename LT>
 static void fs_launch(sph_solver* S, const float4* X4, cudaStream_t st) {
     const int64_t n = S->n;
@@ -217,7 +244,7 @@ static void fs_launch(sph_solver* S, const float4* X4, cudaStream_t st) {
     const unsigned gb = (unsigned)((n + 32 * kFsW - 1) / (32 * kFsW));
     const size_t smem = list_bytes<LT, kFsW>();
     k_fs_detect<PER, LT, kFsW><<<gb, 32 * kFsW, smem, st>>>(D, n, X4, S->start, S->words, S->fs_nl, S->fs_nlc, S->fs,
-                                                            S->fs_lam, S->fs_L, S->fs_half_angle);
+                                                            S->fs_lam, S->fs_L, S->fs_cos_half);
     k_fs_normals<PER, LT, kFsW><<<gb, 32 * kFsW, smem, st>>>(D, n, X4, S->start, S->words, S->fs_nl, S->fs_nlc, S->fs,
                                                              S->fs_lam, S->fs_L, S->fsm, S->fs_nrm);
     for (int k = 1; k < S->fs_expand; ++k) {
@@ -231,6 +258,7 @@ static void fs_launch(sph_solver* S, const float4* X4, cudaStream_t st) {
 
 int surface_detect(sph_solver* S, const float4* X4, cudaStream_t st) {
     if (!S->fs_on || !S->prm.shift_on) return SPH_OK;
+    tbeg(S, KC_SURFACE, st);
     if (S->periodic) {
         if (S->list16) fs_launch<true, int16_t>(S, X4, st);
         else fs_launch<true, int32_t>(S, X4, st);
@@ -238,6 +266,7 @@ int surface_detect(sph_solver* S, const float4* X4, cudaStream_t st) {
         if (S->list16) fs_launch<false, int16_t>(S, X4, st);
         else fs_launch<false, int32_t>(S, X4, st);
     }
+    tend(S, KC_SURFACE, st);
     return cudaGetLastError() == cudaSuccess ? SPH_OK : SPH_ERR_CUDA;
 }
 
@@ -306,7 +335,7 @@ extern "C" int sph_solver_set_free_surface(sph_solver_t* S, const sph_free_surfa
     if ((reinterpret_cast<uintptr_t>(workspace) & 255u) != 0) return SPH_ERR_ARGUMENT;
     if (workspace_bytes < fs_layout(S->n, nullptr, nullptr)) return SPH_ERR_WORKSPACE;
     fs_layout(S->n, static_cast<char*>(workspace), S);
-    S->fs_half_angle = (float)(p->barecasco_threshold / 2.0);
+    S->fs_cos_half = (float)cos((double)(float)(p->barecasco_threshold / 2.0));
     S->fs_expand = p->expansion_iterations;
     S->fs_scaling = (float)p->surface_scaling;
     S->fs_on = true;
@@ -319,5 +348,19 @@ extern "C" int sph_solver_free_surface_fields(sph_solver_t* S, uint8_t* fs, uint
     cudaStream_t st = (cudaStream_t)stream;
     k_fs_download<<<blocks_for(S->n), kBlock, 0, st>>>(S->n, S->uid, S->fs, S->fsm, S->fs_lam, S->fs_nrm, fs, fsm,
                                                         lambdas, normals);
+    return cudaGetLastError() == cudaSuccess ? SPH_OK : SPH_ERR_CUDA;
+}
+
+extern "C" int sph_pressure_switch(int64_t n_query, const int32_t* offsets, const int32_t* counts,
+                                   const int64_t* pair_j, const float* gradients, const float* p_query,
+                                   const float* rho_query, const float* surface_mask, const float* p_ref,
+                                   const float* rho_ref, const float* m_ref, float* accel, sph_stream_t stream) {
+    if (n_query < 0 || (n_query > 0 && (!offsets || !counts || !p_query || !rho_query || !p_ref || !rho_ref ||
+                                        !m_ref || !accel)))
+        return SPH_ERR_ARGUMENT;
+    if (n_query == 0) return SPH_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    k_pressure_switch<<<blocks_for(n_query), kBlock, 0, st>>>(n_query, offsets, counts, pair_j, gradients, p_query,
+                                                               rho_query, surface_mask, p_ref, rho_ref, m_ref, accel);
     return cudaGetLastError() == cudaSuccess ? SPH_OK : SPH_ERR_CUDA;
 }

@@ -7,6 +7,8 @@ Same signatures and return values as:
                                               src/diffSPH/v2/modules/integration.py:92-513
                                               (scheme 'symplecticEuler')
 * ``solveShifting(simulationState, config)``   src/diffSPH/v2/modules/shifting.py:882-1019
+* ``computePressureAccelSwitch(stateA, stateB, neighborhood, config)``
+                                                src/diffSPH/v2/modules/pressureForce.py:15-33
 
 State dicts hold torch tensors (any device). The solver keeps its own copy of the particle
 state on the GPU between calls of one state dict (cached under the key ``'sph103'``), so a
@@ -97,3 +99,34 @@ def solveShifting(simulationState, config):
     if config.get("shifting", {}).get("scheme", "deltaSPH") == "IPS":
         states.append(([], sol.ips_result()[1], None))
     return dx.to(simulationState["fluid"]["positions"].device), states
+
+
+def computePressureAccelSwitch(stateA, stateB, neighborhood, config):
+    """Pressure acceleration with Antuono's switch (pressureForce.py:15-33) on a neighborhood
+    in the reference's format (the drop-in ``neighborSearch`` returns one), on the GPU.
+    ``stateA['surfaceMask']`` (optional) marks the surface particles."""
+    import ctypes
+
+    from . import _lib
+
+    def dev(t, dtype=torch.float32):
+        return torch.as_tensor(t).to(device="cuda", dtype=dtype).contiguous()
+
+    def ptr(t):
+        return ctypes.c_void_p(t.data_ptr()) if t is not None else None
+
+    n = int(torch.as_tensor(stateA["pressures"]).shape[0])
+    i, j = neighborhood["indices"]
+    off = dev(neighborhood["neighborOffsets"], torch.int32)
+    cnt = dev(neighborhood["numNeighbors"], torch.int32)
+    pj = dev(j, torch.int64)
+    grad = dev(neighborhood["gradients"])
+    mask = dev(stateA["surfaceMask"]) if "surfaceMask" in stateA else None
+    args = [dev(stateA["pressures"]), dev(stateA["densities"]), mask, dev(stateB["pressures"]),
+            dev(stateB["densities"]), dev(stateB["masses"])]
+    out = torch.empty(n, 2, device="cuda")
+    lib = _lib.load()
+    _lib.check("sph_pressure_switch", lib.sph_pressure_switch(
+        n, ptr(off), ptr(cnt), ptr(pj), ptr(grad), *[ptr(a) for a in args], ptr(out),
+        ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)))
+    return out.to(torch.as_tensor(stateA["pressures"]).device)

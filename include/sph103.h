@@ -274,6 +274,17 @@ int sph_solver_set_free_surface(sph_solver_t* s, const sph_free_surface_params_t
 int sph_solver_free_surface_fields(sph_solver_t* s, uint8_t* fs, uint8_t* fsm, float* lambdas,
                                    float* normals, sph_stream_t stream);
 
+/* computePressureAccelSwitch (src/diffSPH/v2/modules/pressureForce.py:15-33), Antuono's
+ * switch: a_i = -sum_j m_j / (rho_i rho_j) p_ij gradW_ij with p_ij = p_j + p_i where p_i >= 0
+ * or surface_mask_i > 0.5, else p_j - p_i. Works on a neighborhood in the reference's format
+ * (neighborSearch, or sph_neighbor_fill): pairs sorted by query index, offsets[n_query] and
+ * counts[n_query] (neighborOffsets, numNeighbors), reference indices pair_j and gradients
+ * [pairs][2]. surface_mask may be NULL (no particle on the surface). Writes accel[n][2]. */
+int sph_pressure_switch(int64_t n_query, const int32_t* offsets, const int32_t* counts,
+                        const int64_t* pair_j, const float* gradients, const float* p_query,
+                        const float* rho_query, const float* surface_mask, const float* p_ref,
+                        const float* rho_ref, const float* m_ref, float* accel, sph_stream_t stream);
+
 /* Writes the current state back in the original order (NULL entries are skipped). */
 int sph_solver_download(sph_solver_t* s, float* x_fluid, float* u_fluid, float* rho_fluid,
                         float* rho_boundary, sph_stream_t stream);
@@ -291,7 +302,8 @@ int sph_solver_shapes(void);
  * list entries cannot address the grid's stencils. */
 int sph_solver_set_shape(sph_solver_t* s, int32_t shape);
 
-/* Number of kernel launches one sph_solver_step(s, 1, ...) issues. */
+/* Number of kernel launches one sph_solver_step(s, 1, ...) issues (with the delta+ shift;
+ * an implicit shift replaces its one launch by 2 + 5 per iteration of its solve). */
 int sph_solver_launches_per_step(const sph_solver_t* s);
 
 /* Kernel timing: when enabled, sph_solver_step brackets every launch with CUDA events on

@@ -294,6 +294,17 @@ def pressure_accel(sA, sB, nb, config):
     return -scatter_sum(q[:, None] * k, i, sA["positions"].shape[0]) / sA["densities"][:, None]
 
 
+def pressure_accel_switch(sA, sB, nb, config):
+    """computePressureAccelSwitch pressureForce.py:15-33 (Antuono's switch): p_ij = p_j + p_i
+    where p_i >= 0 or the particle is on the surface (surfaceMask > 0.5), else p_j - p_i;
+    a_i = -sum_j m_j / (rho_i rho_j) p_ij gradW_ij."""
+    i, j = nb["indices"]
+    p_i, p_j = sA["pressures"][i], sB["pressures"][j]
+    pij = np.where((p_i >= 0) | (sA["surfaceMask"][i] > 0.5), p_j + p_i, p_j - p_i)
+    k = (sB["masses"][j] / (sA["densities"][i] * sB["densities"][j]))[:, None] * nb["gradients"]
+    return -scatter_sum(pij[:, None] * k, i, sA["densities"].shape[0])
+
+
 def _pi_term(sA, sB, nb, eps):
     i, j = nb["indices"]
     h = nb["supports"]

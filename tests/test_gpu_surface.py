@@ -137,3 +137,27 @@ def test_free_surface_off_restores_the_plain_shift():
     # the handling changes the shift of surface particles
     c = _solver(cfg, st)
     assert not torch.equal(c.shift(), b.shift())
+
+
+def test_pressure_switch_matches_reference():
+    """computePressureAccelSwitch on the reference's state, neighborhoods and surface mask;
+    each fp32 step follows the reference's order, so the sums agree to rounding."""
+    import os
+    from golden_io import GOLDEN
+    from diffsph_gb300.scheme import computePressureAccelSwitch
+    z = np.load(os.path.join(GOLDEN, "switch_dambreak32.npz"))
+    fl = {k: torch.from_numpy(z[f"fluid/{k}"]) for k in ("densities", "masses", "pressures", "surfaceMask")}
+    bd = {k: torch.from_numpy(z[f"boundary/{k}"]) for k in ("densities", "masses", "pressures")}
+    for name, sB in (("ff", fl), ("fb", bd)):
+        nb = {"indices": (torch.from_numpy(z[f"{name}/i"]), torch.from_numpy(z[f"{name}/j"])),
+              "gradients": torch.from_numpy(z[f"{name}/gradients"]),
+              "numNeighbors": torch.from_numpy(z[f"{name}/numNeighbors"]),
+              "neighborOffsets": torch.from_numpy(z[f"{name}/neighborOffsets"])}
+        got = _np(computePressureAccelSwitch(fl, sB, nb, None))
+        assert rel_max(got, z[f"{name}/accel"]) < 1e-6, name
+        # without a surface mask every negative-pressure particle takes the difference form
+        fl0 = {k: v for k, v in fl.items() if k != "surfaceMask"}
+        ref0 = O.pressure_accel_switch({k: v.numpy() for k, v in fl.items()} | {"surfaceMask": np.zeros(
+            fl["pressures"].shape[0], np.float32)}, {k: v.numpy() for k, v in sB.items()},
+            {"indices": (z[f"{name}/i"], z[f"{name}/j"]), "gradients": z[f"{name}/gradients"]}, None)
+        assert rel_max(_np(computePressureAccelSwitch(fl0, sB, nb, None)), ref0) < 1e-6, name

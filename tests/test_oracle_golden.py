@@ -166,3 +166,17 @@ def test_free_surface_shift_against_reference(case):
     assert rel_max(dx, z["fs/shift"]) < 1e-3
     if "code" in info:
         assert info["code"] == -12 or info["code"] >= 0
+
+
+def test_pressure_switch_against_reference():
+    """computePressureAccelSwitch on the reference's own state, neighborhoods and surface mask."""
+    import os
+    from golden_io import GOLDEN
+    z = np.load(os.path.join(GOLDEN, "switch_dambreak32.npz"))
+    fl = {k: z[f"fluid/{k}"] for k in ("densities", "masses", "pressures", "surfaceMask")}
+    bd = {k: z[f"boundary/{k}"] for k in ("densities", "masses", "pressures")}
+    for name, sB in (("ff", fl), ("fb", bd)):
+        nb = {"indices": (z[f"{name}/i"], z[f"{name}/j"]), "gradients": z[f"{name}/gradients"]}
+        got = O.pressure_accel_switch(fl, sB, nb, None)
+        assert rel_max(got, z[f"{name}/accel"]) < 1e-6, name
+    assert np.any(fl["pressures"] < 0) and np.any(fl["surfaceMask"] > 0.5)
