@@ -1566,7 +1566,7 @@ static int step_impl(sph_solver* S, int32_t n_steps, cudaStream_t st) {
         int rc = run_stages(S, st);
         if (rc) return rc;
         // shifting at the integrated positions, on the same cell sort and skin list
-        rc = surface_detect(S, S->Xf, st);
+        rc = surface_detect(S, S->Xf, S->periodic ? 0 : 1, st);
         if (rc) return rc;
         if (S->ips) {
             rc = ips_shift(S, S->Xf, S->Vf, S->Xc, S->Vc, nullptr, S->periodic ? 0 : 1, st);
@@ -1639,7 +1639,7 @@ extern "C" int sph_solver_shift(sph_solver_t* S, float* dx_out, sph_stream_t str
     if (rc) return rc;
     if (cudaMemsetAsync(S->maxv, 0, sizeof(uint32_t) * S->nd, st) != cudaSuccess) return SPH_ERR_CUDA;
     k_maxvel<<<blocks_for(S->n), kBlock, 0, st>>>(S->n, S->Vc, dids(S), S->maxv);
-    rc = surface_detect(S, S->Xc, st);
+    rc = surface_detect(S, S->Xc, 0, st);
     if (rc) return rc;
     if (S->ips) {
         rc = ips_shift(S, S->Xc, S->Vc, S->Xt, S->Vt, dx_out, 0, st);
@@ -1807,7 +1807,7 @@ extern "C" int sph_solver_launches_per_step(const sph_solver_t* S) {
     // the free-surface passes (detection, normals, expansions) when on. An implicit shift adds
     // its solve's launches (1 + 5 per iteration + 1 in place of the shift), which depend on
     // how many iterations it runs.
-    const int fs = (S->fs_on && S->prm.shift_on) ? 2 + (S->fs_expand - 1) : 0;
+    const int fs = (S->fs_on && S->prm.shift_on) ? 2 + S->fs_expand : 0;
     return 7 + 2 * ((S->nB > 0 ? 2 : 0) + 2) + 1 + fs;
 }
 

@@ -405,7 +405,7 @@ int ips_shift(sph_solver* S, float4* Xin, float4* Vin, float4* Xout, float4* Vou
 size_t ips_workspace_bytes(int64_t n);
 // The free-surface fields at the sorted state X4 (sph_surface.cu); a view of them for the
 // shift kernels (fs == nullptr when the handling is off).
-int surface_detect(sph_solver* S, const float4* X4, cudaStream_t st);
+int surface_detect(sph_solver* S, const float4* X4, int use_skin, cudaStream_t st);
 SurfaceView surface_view(const sph_solver* S);
 
 inline unsigned blocks_for(int64_t n, int threads = kBlock) { return (unsigned)((n + threads - 1) / threads); }

@@ -17,18 +17,17 @@
 //
 // Three kinds of pass over the sorted slots, one thread per slot, every slot a row (walls
 // included: their flags feed the mask expansion of the fluid):
-//   k_fs_detect  stencil scan: cover vector, normalization matrix -> L, Lambdas; keeps the
-//                exact list (int16 offsets, edge-major); then the cone test over that list
-//   k_fs_normals over the list: the lambda gradient -> n, and the first mask expansion
-//   k_fs_expand  over the list: each further expansion
+//   k_fs_detect  the step's skin list (warps of fluid rows) or the stencil: cover vector,
+//                normalization matrix -> L, Lambdas; keeps the exact list (int16 offsets,
+//                edge-major); then the cone test over that list
+//   k_fs_scatter each mask expansion, written from the (sparse) flagged particles
+//   k_fs_normals the lambda gradient -> n, on the rows of the final mask
 // The cone test uses the reference's unit vectors bit for bit (correctly rounded sqrt and
 // division) and tests acos(d) <= threshold / 2 as d >= cos(threshold / 2); the cover vector's
 // summation order differs from the reference's, so a flag can differ only for a pair within
 // rounding of the cone's edge.
 #include <math.h>
 #include <string.h>
-
-#include <utility>
 
 #include "sph_solver.cuh"
 
@@ -54,7 +53,8 @@ template <bool PER, typename LT, int W>
 __global__ void __launch_bounds__(32 * W)
     k_fs_detect(const Dom D, int64_t n, const float4* __restrict__ X4, const int32_t* __restrict__ start,
                 uint32_t* __restrict__ words, int16_t* __restrict__ fnl, int16_t* __restrict__ fnlc,
-                uint8_t* __restrict__ fs, float* __restrict__ lam, float4* __restrict__ Lout, float cos_half) {
+                uint8_t* __restrict__ fs, float* __restrict__ lam, float4* __restrict__ Lout, float cos_half,
+                int use_skin, const int16_t* __restrict__ sl, const int16_t* __restrict__ slc) {
     extern __shared__ __align__(16) unsigned char s_dyn[];
     LT* lst = reinterpret_cast<LT*>(s_dyn) + (threadIdx.x >> 5) * (kCap * 32);
     const Phys& P = D.P;
@@ -63,6 +63,10 @@ __global__ void __launch_bounds__(32 * W)
     const bool inb = i < n;
     const float4 xi = inb ? X4[i] : make_float4(0.f, 0.f, 1.f, 0.f);
     const float2 pi = make_float2(xi.x, xi.y);
+    // fluid rows hold the step's skin list (wall rows do not): a warp of fluid rows with
+    // complete lists filters them, any other warp scans the stencil (same pairs, same order)
+    const int sk = (!PER && use_skin && inb && !is_boundary(xi.z)) ? (int)slc[i] : (inb ? -1 : 0);
+    const bool skin = !PER && use_skin && __all_sync(kFull, sk >= 0) && words[3] == 0u;
     float c0 = 0.f, c1 = 0.f;                          // cover vector
     float M00 = 0.f, M01 = 0.f, M10 = 0.f, M11 = 0.f;  // normalization matrix
     int nst = 0;
@@ -94,7 +98,10 @@ __global__ void __launch_bounds__(32 * W)
         M10 = fmaf(d1, k0, M10);
         M11 = fmaf(d1, k1, M11);
     };
-    neighbor_loop<PER, LT>(inb, (int)i, pi, X4, start, g, P, lst, words, pair_m);
+    if (skin)
+        skin_loop<PER>((int)i, pi, X4, g, P, sl, sk, n, pair_m);
+    else
+        neighbor_loop<PER, LT>(inb, (int)i, pi, X4, start, g, P, lst, words, pair_m);
     if (inb) fnlc[i] = unstored ? (int16_t)-1 : (int16_t)nst;
     // the cone test over the same neighbors (the stored list, or a second scan)
     const float2 cn = normalize_ref(c0, c1);
@@ -126,27 +133,26 @@ __global__ void __launch_bounds__(32 * W)
     Lout[i] = make_float4(L.a, L.b, L.c, L.d);
 }
 
-// first mask expansion and the normalised lambda gradient
+// the normalised lambda gradient, on the rows of the final mask (the only ones that use it)
 template <bool PER, typename LT, int W>
 __global__ void __launch_bounds__(32 * W)
     k_fs_normals(const Dom D, int64_t n, const float4* __restrict__ X4, const int32_t* __restrict__ start,
                  uint32_t* __restrict__ words, const int16_t* __restrict__ fnl, const int16_t* __restrict__ fnlc,
-                 const uint8_t* __restrict__ fs, const float* __restrict__ lam, const float4* __restrict__ Lin,
-                 uint8_t* __restrict__ fsm, float2* __restrict__ nrm) {
+                 const uint8_t* __restrict__ fsm, const float* __restrict__ lam, const float4* __restrict__ Lin,
+                 float2* __restrict__ nrm) {
     extern __shared__ __align__(16) unsigned char s_dyn[];
     LT* lst = reinterpret_cast<LT*>(s_dyn) + (threadIdx.x >> 5) * (kCap * 32);
     const Phys& P = D.P;
     const Grid& g = D.g;
     const int64_t i = (int64_t)blockIdx.x * (32 * W) + threadIdx.x;
-    const bool inb = i < n;
-    const float4 xi = inb ? X4[i] : make_float4(0.f, 0.f, 1.f, 0.f);
+    const bool row = i < n && fsm[i];
+    if (!__any_sync(kFull, row)) return;
+    const float4 xi = row ? X4[i] : make_float4(0.f, 0.f, 1.f, 0.f);
     const float2 pi = make_float2(xi.x, xi.y);
-    const float4 L = inb ? Lin[i] : make_float4(0.f, 0.f, 0.f, 0.f);
-    const float li = inb ? lam[i] : 0.f;
-    bool any = false;
+    const float4 L = row ? Lin[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float li = row ? lam[i] : 0.f;
     float g0 = 0.f, g1 = 0.f;
     auto pair_n = [&](int j) {
-        any = any || fs[j];
         const float4 xj = __ldg(&X4[j]);
         float x0, x1;
         pair_vec<PER>(pi, make_float2(xj.x, xj.y), P.geo, x0, x1);
@@ -158,40 +164,39 @@ __global__ void __launch_bounds__(32 * W)
         g0 = fmaf(w, ng0, g0);
         g1 = fmaf(w, ng1, g1);
     };
-    const int cnt = inb ? (int)fnlc[i] : 0;
+    const int cnt = row ? (int)fnlc[i] : 0;
     if (__any_sync(kFull, cnt < 0)) {
-        neighbor_loop<PER, LT>(inb, (int)i, pi, X4, start, g, P, lst, words, pair_n);
+        neighbor_loop<PER, LT>(row, (int)i, pi, X4, start, g, P, lst, words, pair_n);
     } else {
         for (int k = 0; k < cnt; ++k) pair_n(list_slot<PER>((int)i, (int)fnl[(int64_t)k * n + i], g));
     }
-    if (!inb) return;
-    fsm[i] = (uint8_t)any;
-    nrm[i] = normalize_ref(g0, g1);
+    if (row) nrm[i] = normalize_ref(g0, g1);
 }
 
-// a further mask expansion: out_i = OR over the neighbors of in_j
+// one mask expansion, out_k = OR over the neighbors j of k of in_j, written from the flagged
+// particles: every flagged j marks its neighbors (the neighbor relation is symmetric with one
+// support). The flags are sparse, and equal stores of 1 make the result independent of order.
 template <bool PER, typename LT, int W>
 __global__ void __launch_bounds__(32 * W)
-    k_fs_expand(const Dom D, int64_t n, const float4* __restrict__ X4, const int32_t* __restrict__ start,
-                uint32_t* __restrict__ words, const int16_t* __restrict__ fnl, const int16_t* __restrict__ fnlc,
-                const uint8_t* __restrict__ in, uint8_t* __restrict__ out) {
+    k_fs_scatter(const Dom D, int64_t n, const float4* __restrict__ X4, const int32_t* __restrict__ start,
+                 uint32_t* __restrict__ words, const int16_t* __restrict__ fnl, const int16_t* __restrict__ fnlc,
+                 const uint8_t* __restrict__ in, uint8_t* __restrict__ out) {
     extern __shared__ __align__(16) unsigned char s_dyn[];
     LT* lst = reinterpret_cast<LT*>(s_dyn) + (threadIdx.x >> 5) * (kCap * 32);
     const Phys& P = D.P;
     const Grid& g = D.g;
     const int64_t i = (int64_t)blockIdx.x * (32 * W) + threadIdx.x;
-    const bool inb = i < n;
-    const float4 xi = inb ? X4[i] : make_float4(0.f, 0.f, 1.f, 0.f);
+    const bool row = i < n && in[i];
+    if (!__any_sync(kFull, row)) return;
+    const float4 xi = row ? X4[i] : make_float4(0.f, 0.f, 1.f, 0.f);
     const float2 pi = make_float2(xi.x, xi.y);
-    bool any = false;
-    auto pair_e = [&](int j) { any = any || in[j]; };
-    const int cnt = inb ? (int)fnlc[i] : 0;
+    auto mark = [&](int j) { out[j] = 1; };
+    const int cnt = row ? (int)fnlc[i] : 0;
     if (__any_sync(kFull, cnt < 0)) {
-        neighbor_loop<PER, LT>(inb, (int)i, pi, X4, start, g, P, lst, words, pair_e);
+        neighbor_loop<PER, LT>(row, (int)i, pi, X4, start, g, P, lst, words, mark);
     } else {
-        for (int k = 0; k < cnt; ++k) pair_e(list_slot<PER>((int)i, (int)fnl[(int64_t)k * n + i], g));
+        for (int k = 0; k < cnt; ++k) mark(list_slot<PER>((int)i, (int)fnl[(int64_t)k * n + i], g));
     }
-    if (inb) out[i] = (uint8_t)any;
 }
 
 // the fields in the original particle order (fluid first, then walls)
@@ -238,33 +243,38 @@ __global__ void k_pressure_switch(int64_t n, const int32_t* __restrict__ off, co
 }
 
 template <bool PER, typename LT>
-static void fs_launch(sph_solver* S, const float4* X4, cudaStream_t st) {
+static void fs_launch(sph_solver* S, const float4* X4, int use_skin, cudaStream_t st) {
     const int64_t n = S->n;
     const Dom& D = S->doms_host[0];
     const unsigned gb = (unsigned)((n + 32 * kFsW - 1) / (32 * kFsW));
     const size_t smem = list_bytes<LT, kFsW>();
     k_fs_detect<PER, LT, kFsW><<<gb, 32 * kFsW, smem, st>>>(D, n, X4, S->start, S->words, S->fs_nl, S->fs_nlc, S->fs,
-                                                            S->fs_lam, S->fs_L, S->fs_cos_half);
-    k_fs_normals<PER, LT, kFsW><<<gb, 32 * kFsW, smem, st>>>(D, n, X4, S->start, S->words, S->fs_nl, S->fs_nlc, S->fs,
-                                                             S->fs_lam, S->fs_L, S->fsm, S->fs_nrm);
-    for (int k = 1; k < S->fs_expand; ++k) {
-        k_fs_expand<PER, LT, kFsW><<<gb, 32 * kFsW, smem, st>>>(D, n, X4, S->start, S->words, S->fs_nl, S->fs_nlc,
-                                                                S->fsm, S->fsm_t);
-        std::swap(S->fsm, S->fsm_t);
+                                                            S->fs_lam, S->fs_L, S->fs_cos_half, use_skin, S->sl,
+                                                            S->slc);
+    const uint8_t* in = S->fs;
+    for (int k = 0; k < S->fs_expand; ++k) {
+        uint8_t* out = ((S->fs_expand - 1 - k) & 1) ? S->fsm_t : S->fsm;  // the last one into fsm
+        cudaMemsetAsync(out, 0, (size_t)n, st);
+        k_fs_scatter<PER, LT, kFsW><<<gb, 32 * kFsW, smem, st>>>(D, n, X4, S->start, S->words, S->fs_nl, S->fs_nlc,
+                                                                 in, out);
+        in = out;
     }
+    cudaMemsetAsync(S->fs_nrm, 0, (size_t)n * sizeof(float2), st);  // zero off the mask
+    k_fs_normals<PER, LT, kFsW><<<gb, 32 * kFsW, smem, st>>>(D, n, X4, S->start, S->words, S->fs_nl, S->fs_nlc,
+                                                             S->fsm, S->fs_lam, S->fs_L, S->fs_nrm);
 }
 
 }  // namespace sph
 
-int surface_detect(sph_solver* S, const float4* X4, cudaStream_t st) {
+int surface_detect(sph_solver* S, const float4* X4, int use_skin, cudaStream_t st) {
     if (!S->fs_on || !S->prm.shift_on) return SPH_OK;
     tbeg(S, KC_SURFACE, st);
     if (S->periodic) {
-        if (S->list16) fs_launch<true, int16_t>(S, X4, st);
-        else fs_launch<true, int32_t>(S, X4, st);
+        if (S->list16) fs_launch<true, int16_t>(S, X4, 0, st);
+        else fs_launch<true, int32_t>(S, X4, 0, st);
     } else {
-        if (S->list16) fs_launch<false, int16_t>(S, X4, st);
-        else fs_launch<false, int32_t>(S, X4, st);
+        if (S->list16) fs_launch<false, int16_t>(S, X4, use_skin, st);
+        else fs_launch<false, int32_t>(S, X4, use_skin, st);
     }
     tend(S, KC_SURFACE, st);
     return cudaGetLastError() == cudaSuccess ? SPH_OK : SPH_ERR_CUDA;

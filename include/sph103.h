@@ -270,7 +270,8 @@ int sph_solver_set_free_surface(sph_solver_t* s, const sph_free_surface_params_t
                                 void* workspace, size_t workspace_bytes);
 /* The fields of the last shift's detection, in the original order of the merged set (fluid
  * particles, then walls; NULL entries are skipped): surface flags fs[n] and expanded mask
- * fsm[n] (uint8), Lambdas[n], normals[n][2]. */
+ * fsm[n] (uint8), Lambdas[n], normals[n][2] (computed on the rows of the expanded mask, the
+ * only ones the projection uses; zero elsewhere). */
 int sph_solver_free_surface_fields(sph_solver_t* s, uint8_t* fs, uint8_t* fsm, float* lambdas,
                                    float* normals, sph_stream_t stream);
 
