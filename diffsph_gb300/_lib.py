@@ -70,7 +70,7 @@ EXPORTS = [
     "sph_gemm_bf16_tn", "sph_cconv_aggregate", "sph_cconv_aggregate_t", "sph_cconv_aggregate_tc",
     "sph_neighbor_fill_csr", "sph_solver_ips_workspace_bytes", "sph_solver_set_ips", "sph_solver_ips_result",
     "sph_solver_free_surface_workspace_bytes", "sph_solver_set_free_surface", "sph_solver_free_surface_fields",
-    "sph_pressure_switch",
+    "sph_pressure_switch", "sph_liuliu_consistent",
 ]
 
 _lib = None
@@ -136,6 +136,7 @@ def load(build_if_missing: bool = False):
         "sph_solver_set_free_surface": ([P, ctypes.POINTER(FreeSurfaceParams), P, SZ], ctypes.c_int),
         "sph_solver_free_surface_fields": ([P, P, P, P, P, P], ctypes.c_int),
         "sph_pressure_switch": ([I64, P, P, P, P, P, P, P, P, P, P, P, P], ctypes.c_int),
+        "sph_liuliu_consistent": ([I64] + [P] * 15, ctypes.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)

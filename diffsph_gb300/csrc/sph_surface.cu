@@ -242,6 +242,62 @@ __global__ void k_pressure_switch(int64_t n, const int32_t* __restrict__ off, co
     out[2 * i + 1] = -a1;
 }
 
+// LiuLiuConsistent (src/diffSPH/v2/sphOps.py:313-341) on a neighborhood in the reference's
+// format: per query (ghost) row, the moment sums of b and M in the pair order with each fp32
+// step in the reference's order, then Cramer's rule in fp64 (the reference divides
+// determinants of fp32 LU factorisations; fp64 keeps the ill-conditioned rows accurate).
+__device__ __forceinline__ double det3(const double m[9]) {
+    return m[0] * (m[4] * m[8] - m[5] * m[7]) - m[1] * (m[3] * m[8] - m[5] * m[6]) +
+           m[2] * (m[3] * m[7] - m[4] * m[6]);
+}
+
+__global__ void k_liuliu(int64_t n, const int32_t* __restrict__ off, const int32_t* __restrict__ cnt,
+                         const int64_t* __restrict__ pj, const float* __restrict__ qd, const float* __restrict__ xh,
+                         const float* __restrict__ hp, const float* __restrict__ W, const float* __restrict__ G,
+                         const float* __restrict__ m, const float* __restrict__ rho, const float* __restrict__ q,
+                         float* __restrict__ sol, float* __restrict__ Mout, float* __restrict__ bout) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float b0 = 0.f, b1 = 0.f, b2 = 0.f;
+    float M0 = 0.f, Mg0 = 0.f, Mg1 = 0.f, Mx0 = 0.f, Mx1 = 0.f, Mxg00 = 0.f, Mxg01 = 0.f, Mxg10 = 0.f, Mxg11 = 0.f;
+    const int64_t e0 = off[i], e1 = e0 + cnt[i];
+    for (int64_t e = e0; e < e1; ++e) {
+        const int64_t j = pj[e];
+        const float V = __fdiv_rn(m[j], rho[j]);
+        const float vw = __fmul_rn(V, W[e]);
+        const float vg0 = __fmul_rn(V, G[2 * e]), vg1 = __fmul_rn(V, G[2 * e + 1]);
+        const float x0 = __fmul_rn(__fmul_rn(-xh[2 * e], qd[e]), hp[e]);
+        const float x1 = __fmul_rn(__fmul_rn(-xh[2 * e + 1], qd[e]), hp[e]);
+        const float qj = q[j];
+        b0 = __fadd_rn(b0, __fmul_rn(qj, vw));
+        b1 = __fadd_rn(b1, __fmul_rn(qj, vg0));
+        b2 = __fadd_rn(b2, __fmul_rn(qj, vg1));
+        M0 = __fadd_rn(M0, vw);
+        Mg0 = __fadd_rn(Mg0, vg0);
+        Mg1 = __fadd_rn(Mg1, vg1);
+        Mx0 = __fadd_rn(Mx0, __fmul_rn(x0, vw));
+        Mx1 = __fadd_rn(Mx1, __fmul_rn(x1, vw));
+        Mxg00 = __fadd_rn(Mxg00, __fmul_rn(x0, vg0));
+        Mxg01 = __fadd_rn(Mxg01, __fmul_rn(x0, vg1));
+        Mxg10 = __fadd_rn(Mxg10, __fmul_rn(x1, vg0));
+        Mxg11 = __fadd_rn(Mxg11, __fmul_rn(x1, vg1));
+    }
+    const float Mf[9] = {M0, Mx0, Mx1, Mg0, Mxg00, Mxg01, Mg1, Mxg10, Mxg11};
+    const float bf[3] = {b0, b1, b2};
+    double Md[9];
+    for (int k = 0; k < 9; ++k) Md[k] = Mf[k];
+    const double d0 = det3(Md) + 1e-7;
+    for (int c = 0; c < 3; ++c) {
+        double Mk[9];
+        for (int k = 0; k < 9; ++k) Mk[k] = (k % 3 == c) ? (double)bf[k / 3] : Md[k];
+        sol[3 * i + c] = (float)(det3(Mk) / d0);
+    }
+    if (Mout)
+        for (int k = 0; k < 9; ++k) Mout[9 * i + k] = Mf[k];
+    if (bout)
+        for (int k = 0; k < 3; ++k) bout[3 * i + k] = bf[k];
+}
+
 template <bool PER, typename LT>
 static void fs_launch(sph_solver* S, const float4* X4, int use_skin, cudaStream_t st) {
     const int64_t n = S->n;
@@ -372,5 +428,19 @@ extern "C" int sph_pressure_switch(int64_t n_query, const int32_t* offsets, cons
     cudaStream_t st = (cudaStream_t)stream;
     k_pressure_switch<<<blocks_for(n_query), kBlock, 0, st>>>(n_query, offsets, counts, pair_j, gradients, p_query,
                                                                rho_query, surface_mask, p_ref, rho_ref, m_ref, accel);
+    return cudaGetLastError() == cudaSuccess ? SPH_OK : SPH_ERR_CUDA;
+}
+
+extern "C" int sph_liuliu_consistent(int64_t n_query, const int32_t* offsets, const int32_t* counts,
+                                     const int64_t* pair_j, const float* distances, const float* vectors,
+                                     const float* supports, const float* kernels, const float* gradients,
+                                     const float* m_ref, const float* rho_ref, const float* quantity,
+                                     float* solution, float* M, float* b, sph_stream_t stream) {
+    if (n_query < 0 || (n_query > 0 && (!offsets || !counts || !m_ref || !rho_ref || !quantity || !solution)))
+        return SPH_ERR_ARGUMENT;
+    if (n_query == 0) return SPH_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    k_liuliu<<<blocks_for(n_query), kBlock, 0, st>>>(n_query, offsets, counts, pair_j, distances, vectors, supports,
+                                                      kernels, gradients, m_ref, rho_ref, quantity, solution, M, b);
     return cudaGetLastError() == cudaSuccess ? SPH_OK : SPH_ERR_CUDA;
 }

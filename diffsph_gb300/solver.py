@@ -109,6 +109,9 @@ def params_from_config(cfg, mass: float, skin: float = DEFAULT_SKIN, capacity: i
     mag = _f(g.get("magnitude", 9.81))
     p.gravity[0], p.gravity[1] = direction[0] * mag, direction[1] * mag
     p.dt = _f(cfg["timestep"]["dt"])
+    if cfg.get("regions"):
+        raise ValueError("the fused solver has a fixed particle count and no open-boundary regions; "
+                         "diffsph_gb300.regions serves the reference's step for them")
     sh = cfg.get("shifting", {})
     if sh.get("scheme", "deltaSPH") not in ("deltaSPH", "IPS") or int(sh.get("maxIterations", 1)) != 1:
         raise ValueError("only delta+ and implicit (IPS) shifting with one iteration are implemented")

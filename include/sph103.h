@@ -286,6 +286,18 @@ int sph_pressure_switch(int64_t n_query, const int32_t* offsets, const int32_t* 
                         const float* rho_query, const float* surface_mask, const float* p_ref,
                         const float* rho_ref, const float* m_ref, float* accel, sph_stream_t stream);
 
+/* LiuLiuConsistent (src/diffSPH/v2/sphOps.py:313-341), the first-order consistent
+ * interpolation the open-boundary (mirror outlet) ghosts use (deltaPlus.py:210-235): per
+ * query row of a neighborhood in the reference's format (offsets, counts, pair_j, and the pair
+ * distances q = r/h, unit vectors [pairs][2], supports, kernels, gradients [pairs][2]), the
+ * moments b[3] and M[3][3] of the fluid quantity (m_ref / rho_ref volumes) and the solution
+ * [value, d/dx, d/dy] by Cramer's rule. M and b may be NULL. */
+int sph_liuliu_consistent(int64_t n_query, const int32_t* offsets, const int32_t* counts,
+                          const int64_t* pair_j, const float* distances, const float* vectors,
+                          const float* supports, const float* kernels, const float* gradients,
+                          const float* m_ref, const float* rho_ref, const float* quantity,
+                          float* solution, float* M, float* b, sph_stream_t stream);
+
 /* Writes the current state back in the original order (NULL entries are skipped). */
 int sph_solver_download(sph_solver_t* s, float* x_fluid, float* u_fluid, float* rho_fluid,
                         float* rho_boundary, sph_stream_t stream);

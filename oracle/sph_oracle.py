@@ -305,6 +305,38 @@ def pressure_accel_switch(sA, sB, nb, config):
     return -scatter_sum(pij[:, None] * k, i, sA["densities"].shape[0])
 
 
+def liuliu_consistent(ghost, fluid, nb, q):
+    """LiuLiuConsistent sphOps.py:313-341: first-order consistent interpolation of the fluid
+    quantity q at the query (ghost) particles. With V_j = m_j / rho_j, x_ij = -xhat q h,
+        b = [sum V q_j W, sum V q_j gradW]
+        M = [[sum V W, sum V W x_ij^T], [sum V gradW_a, sum V x_ij,a gradW^T]  (a = 0, 1)]
+    and the solution by Cramer's rule, det(M with column k <- b) / (det M + 1e-7).
+    Returns (solution [n, 3], M [n, 3, 3], b [n, 3])."""
+    i, j = nb["indices"]
+    n = ghost["positions"].shape[0]
+    V = fluid["masses"][j] / fluid["densities"][j]
+    W, G = nb["kernels"], nb["gradients"]
+    dt = W.dtype.type
+    x = -nb["vectors"] * nb["distances"][:, None] * nb["supports"][:, None]
+    b = np.concatenate([scatter_sum(q[j] * (V * W), i, n)[:, None],
+                        scatter_sum(q[j][:, None] * (V[:, None] * G), i, n)], axis=1)
+    M0 = scatter_sum(V * W, i, n)
+    Mg = scatter_sum(V[:, None] * G, i, n)
+    Mx = scatter_sum(x * (V * W)[:, None], i, n)
+    Mxg = scatter_sum(np.einsum("na,nd->nad", x, V[:, None] * G), i, n)
+    M = np.zeros((n, 3, 3), dtype=dt)
+    M[:, 0, 0], M[:, 0, 1:] = M0, Mx
+    for a in range(2):
+        M[:, 1 + a, 0], M[:, 1 + a, 1:] = Mg[:, a], Mxg[:, a, :]
+    d0 = np.linalg.det(M)
+    sol = np.empty((n, 3), dtype=dt)
+    for k in range(3):
+        Mk = M.copy()
+        Mk[:, :, k] = b
+        sol[:, k] = np.linalg.det(Mk) / (d0 + dt(1e-7))
+    return sol, M, b
+
+
 def _pi_term(sA, sB, nb, eps):
     i, j = nb["indices"]
     h = nb["supports"]

@@ -118,3 +118,10 @@ def test_ips_params_struct_layout():
     from diffsph_gb300 import _lib
     assert ctypes.sizeof(_lib.IpsParams) == 24
     assert _lib.IpsParams.solver_threshold.offset == 16
+
+
+def test_params_reject_open_boundary_regions():
+    cfg, st = scenes.fourier_periodic(16, seed=1)
+    cfg["regions"] = [{"type": "outlet", "sdf": lambda p: p[:, 0]}]
+    with pytest.raises(ValueError):
+        params_from_config(cfg, 1.0)

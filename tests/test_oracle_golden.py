@@ -180,3 +180,20 @@ def test_pressure_switch_against_reference():
         got = O.pressure_accel_switch(fl, sB, nb, None)
         assert rel_max(got, z[f"{name}/accel"]) < 1e-6, name
     assert np.any(fl["pressures"] < 0) and np.any(fl["surfaceMask"] > 0.5)
+
+
+def test_liuliu_consistent_against_reference():
+    """LiuLiuConsistent on the reference's mirror-outlet ghosts (buildOutletGhostParticles)."""
+    import os
+    from golden_io import GOLDEN
+    z = np.load(os.path.join(GOLDEN, "regions_block32.npz"))
+    fluid = {k: z[f"in/fluid/{k}"] for k in ("positions", "velocities", "densities", "masses")}
+    ghost = {"positions": z["ghost/positions"]}
+    nb = {"indices": (z["ghost/i"], z["ghost/j"]), "distances": z["ghost/nb_distances"],
+          "vectors": z["ghost/nb_vectors"], "supports": z["ghost/nb_supports"], "kernels": z["ghost/nb_kernels"],
+          "gradients": z["ghost/nb_gradients"]}
+    for name, q in (("rho", fluid["densities"]), ("u", fluid["velocities"][:, 0]), ("v", fluid["velocities"][:, 1])):
+        sol, M, b = O.liuliu_consistent(ghost, fluid, nb, q)
+        assert rel_max(M, z[f"liuliu/{name}/M"]) < 1e-5, name
+        assert rel_max(b, z[f"liuliu/{name}/b"]) < 1e-5, name
+        assert rel_max(sol, z[f"liuliu/{name}/solution"]) < 1e-3, name
