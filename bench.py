@@ -51,6 +51,9 @@ WORKLOADS = {
     # implicit particle shifting (shifting.scheme 'IPS'): jittered periodic Fourier flow
     "ips_fourier1024": dict(scene="fourier", nx=1024, seed=0, jitter=0.1, ips=True),
     "ips_fourier512": dict(scene="fourier", nx=512, seed=0, jitter=0.1, ips=True),
+    # open-boundary mirror outlet: ghost construction + consistent interpolation of the density
+    # and both velocity components, fluid block of 1024 x 1024 with the outlet at x > 0.9
+    "outlet_mirror_1024": dict(scene="regions", nx=1024, mirror_x=0.9),
     # gradient of a rollout loss: 128x128 periodic Fourier flow, 1000 steps, checkpoints every 25
     "adjoint_fourier128": dict(scene="adjoint", nx=128, seed=0, target_seed=1, rollout=1000, every=25),
     # learned k=4 step: trained at 128x128 (dx = 1/64), evaluated on 32 domains of 256x256 (4x4 box)
@@ -188,6 +191,10 @@ def run_reference(args):
         return
     if WORKLOADS[args.workload]["scene"] == "learned":
         print(json.dumps({"impl": "reference", "unavailable": "the reference has no learned model"}))
+        return
+    if WORKLOADS[args.workload]["scene"] == "regions":
+        print(json.dumps({"impl": "reference", "unavailable": "the reference's region functions are torch code "
+                          "that is not installed on this machine; run_regions times the oracle port instead"}))
         return
     import multiprocessing as mp
     from oracle import sph_oracle as O
@@ -562,6 +569,95 @@ def run_adjoint(args):
     print(json.dumps(line))
 
 
+def run_regions(args):
+    """Mirror-outlet processing of the reference's step (deltaPlus.py:188-235) on a fluid block:
+    buildOutletGhostParticles (region distance function, mirrored ghosts, GPU neighbor search)
+    and LiuLiuConsistent (sm_103a kernel) for the density and both velocity components, then the
+    fluid update. Unit: ghost updates per second (one ghost, three quantities)."""
+    import numpy as np
+    import torch
+    import __graft_entry__ as ge
+    from diffsph_gb300 import regions, scenes
+
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    ge.build()
+    w = WORKLOADS[args.workload]
+    dx = 1.0 / w["nx"]
+    cfg, st = scenes.dam_break(dx=dx)
+    fl = st["fluid"]
+    keep = fl["positions"][:, 1] < 1.0
+    fl = {k: torch.from_numpy(v[keep].copy()).cuda() for k, v in fl.items()}
+    fl["numParticles"] = fl["positions"].shape[0]
+    rng = np.random.default_rng(3)
+    fl["velocities"] = torch.from_numpy(rng.uniform(-1, 1, tuple(fl["velocities"].shape)).astype(np.float32)).cuda()
+    cfg["boundary"]["active"] = False
+    cfg["particle"]["volume"] = dx * dx
+    mx = w["mirror_x"]
+    region = {"type": "mirror", "sdf": lambda p: mx - p[:, 0]}
+    state = {"fluid": fl}
+
+    def step():
+        g = regions.buildOutletGhostParticles([region], state, cfg)
+        cond = g["numNeighbors"] >= 10
+        shift = g["sdf_dist"][:, None] * g["sdf_grad"] * 2
+        for q, put in ((fl["densities"], None), (fl["velocities"][:, 0], 0), (fl["velocities"][:, 1], 1)):
+            sol, _, _ = regions.LiuLiuConsistent(g, fl, q)
+            val = torch.where(cond, sol[:, 0] + torch.einsum("nd,nd->n", shift, sol[:, 1:]), q[g["fluidIndex"]])
+            if put is None:
+                fl["densities"][g["fluidIndex"]] = val
+            else:
+                fl["velocities"][g["fluidIndex"], put] = val
+        return g["positions"].shape[0]
+
+    stream = torch.cuda.Stream()
+    with torch.cuda.stream(stream):
+        for _ in range(max(args.warmup, 3)):
+            ng = step()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
+            e0.record(stream)
+            for _ in range(args.steps):
+                ng = step()
+            e1.record(stream)
+            torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        # the kernel alone: one consistent interpolation over the ghost neighborhood
+        g = regions.buildOutletGhostParticles([region], state, cfg)
+        k0, k1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        k0.record(stream)
+        for _ in range(10):
+            regions.LiuLiuConsistent(g, fl, fl["densities"])
+        k1.record(stream)
+        torch.cuda.synchronize()
+        kernel_ms = k0.elapsed_time(k1) / 10
+    # the oracle's consistent interpolation on the host, on a 1/64 sample of the ghosts
+    from oracle import sph_oracle as O
+    nb = g["neighborhood"]
+    rows = max(ng // 64, 1)
+    sel = (nb["indices"][0] < rows).cpu().numpy()
+    nb_h = {"indices": (nb["indices"][0].cpu().numpy()[sel], nb["indices"][1].cpu().numpy()[sel])}
+    for k in ("distances", "vectors", "supports", "kernels", "gradients"):
+        nb_h[k] = nb[k].cpu().numpy()[sel]
+    fl_h = {k: fl[k].cpu().numpy() for k in ("masses", "densities")}
+    t0 = time.perf_counter()
+    O.liuliu_consistent({"positions": np.zeros((rows, 2), np.float32)}, fl_h, nb_h, fl_h["densities"])
+    t_cpu = time.perf_counter() - t0
+    print(json.dumps({
+        "metric": "ghost updates/s (mirror-outlet ghosts: construction, neighbor search and consistent "
+                  "interpolation of density and velocity)", "value": ng * args.steps / (ms / 1e3),
+        "unit": "ghost-updates/s", "n_gpus": 1, "steps": args.steps, "warmup": max(args.warmup, 3),
+        "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic",
+        "config": {"workload": args.workload, "fluid_particles": int(fl["numParticles"]), "ghosts": ng,
+                   "ghost_pairs": int(nb["indices"][0].shape[0]), "liuliu_kernel_ms": kernel_ms,
+                   "note": "the region's distance function and its gradient run in the caller's Python, "
+                           "the gradient on the host as in the reference"},
+        "cpu_baseline": {"value": rows / t_cpu, "unit": "ghost-interpolations/s", "cores": 1, "kind": "port",
+                         "sample": f"oracle consistent interpolation of {rows} ghosts (one quantity)"},
+        "clocks": clk.summary()}))
+
+
 def run_learned(args):
     """Learned k=4 step against k plain steps on the same packed batch of periodic domains.
     value: particles x k / learned-step time (the state resident on the device); the plain
@@ -687,6 +783,8 @@ def main():
         run_adjoint(args)
     elif WORKLOADS[args.workload]["scene"] == "learned":
         run_learned(args)
+    elif WORKLOADS[args.workload]["scene"] == "regions":
+        run_regions(args)
     else:
         run_ours(args)
 
