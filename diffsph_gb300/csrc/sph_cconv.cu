@@ -723,6 +723,238 @@ extern "C" int sph_cconv_aggregate_t(const float* x, int64_t n, const int64_t* o
     return cudaGetLastError() == cudaSuccess ? SPH_OK : SPH_ERR_CUDA;
 }
 
+// ------------------------------------------------------------------------------------
+// The same aggregation for C = 64 with both operands MN-major (128-byte swizzle): a K row
+// (one edge) of A is a particle's 64 basis values, of B the neighbor's 64 features, 128
+// contiguous bytes each. A thread per edge and operand (256 threads: the basis rows and the
+// feature rows are built by different halves of the CTA) therefore writes eight 16-byte
+// chunks, the features copied as they sit in global memory, instead of one 2-byte value per
+// basis row and feature; all eight warps then drain TMEM, two per lane quarter. A holds, per group of 8 K rows, the two particles' 64-row atoms
+// side by side (1 KB each; LBO 1 KB between them, SBO 2 KB between K groups); B holds one
+// 64-wide atom per K group (SBO 1 KB). Block-diagonal as above: K rows 0..63 are particle
+// A's edges (its atom), 64..127 particle B's; the other atom's rows stay zero.
+// ------------------------------------------------------------------------------------
+constexpr uint32_t kMnA = 16u * 2048u;  // 16 K groups x (2 atoms x 8 rows x 128 B)
+constexpr uint32_t kMnB = 16u * 1024u;  // 16 K groups x 8 rows x 128 B
+constexpr size_t kMnSmem = static_cast<size_t>(kMnA + kMnB) + 1024;
+
+__device__ __forceinline__ uint64_t mn128_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+    uint64_t d = 0;
+    d |= static_cast<uint64_t>((saddr >> 4) & 0x3FFFu);
+    d |= static_cast<uint64_t>((lbo >> 4) & 0x3FFFu) << 16;
+    d |= static_cast<uint64_t>((sbo >> 4) & 0x3FFFu) << 32;
+    d |= static_cast<uint64_t>(1) << 46;  // descriptor version of sm_100 and later
+    d |= static_cast<uint64_t>(2) << 61;  // SWIZZLE_128B
+    return d;
+}
+
+// kind::f16 instruction descriptor with A and B MN-major (bits 15 and 16)
+__host__ __device__ constexpr uint32_t idesc_bf16_mn(int m, int n) {
+    return idesc_bf16(m, n) | (1u << 15) | (1u << 16);
+}
+
+template <bool REL>
+__global__ void __launch_bounds__(256, 4)
+    k_aggregate_tc_mn(int64_t n, const float* __restrict__ x, const int64_t* __restrict__ off,
+                      const int32_t* __restrict__ nbr, BasisGeo bg, float inv_norm,
+                      const __nv_bfloat16* __restrict__ h, __nv_bfloat16* __restrict__ E, uint32_t* __restrict__ err) {
+    constexpr int C = 64;
+    extern __shared__ uint8_t dsm[];
+    __shared__ uint64_t mma_done;
+    __shared__ uint32_t tmem_slot;
+    uint8_t* tiles = dsm + ((1024u - (smem_u32(dsm) & 1023u)) & 1023u);
+    uint8_t* A = tiles;
+    uint8_t* B = tiles + kMnA;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int64_t q0 = static_cast<int64_t>(blockIdx.x) * (2 * kTcPairsPerCta);
+    for (uint32_t o = static_cast<uint32_t>(tid) * 16u; o < kMnA + kMnB; o += 256u * 16u)
+        *reinterpret_cast<uint4*>(tiles + o) = make_uint4(0u, 0u, 0u, 0u);
+    if (tid == 0) {
+        mbar_init(&mma_done, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_slot)),
+                     "r"(64));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    const uint32_t tmem = tmem_slot;
+    constexpr uint32_t idesc = idesc_bf16_mn(128, C);
+    // threads 0..127 build the basis rows (A), 128..255 the feature rows (B), one K row
+    // (edge e of particle p of the pair) each
+    const int role = tid >> 7, t = tid & 127;
+    const int p = t >> 6, e = t & 63;
+    const int k = 64 * p + e, grp = k >> 3, r = k & 7;
+    uint8_t* row = role == 0 ? A + grp * 2048 + p * 1024 + r * 128 : B + grp * 1024 + r * 128;
+    for (int it = 0; it < kTcPairsPerCta; ++it) {
+        const int64_t ia = q0 + 2 * it;
+        if (ia >= n) break;  // uniform across the CTA
+        {
+            const int64_t i = ia + p;
+            int ne = 0;
+            int64_t e0 = 0;
+            if (i < n) {
+                e0 = off[i];
+                ne = static_cast<int>(off[i + 1] - e0);
+                if (ne > kTcMaxEdges) {
+                    if (e == 0 && role == 0) atomicOr(err, 8u);
+                    ne = kTcMaxEdges;
+                }
+            }
+            const bool valid = e < ne;
+            const int64_t j = valid ? static_cast<int64_t>(nbr[e0 + e]) : 0;
+            if (role == 0) {
+                float x0 = 0.f, x1 = 0.f;
+                if (valid)
+                    pair_vec<true>(make_float2(x[2 * i], x[2 * i + 1]), make_float2(x[2 * j], x[2 * j + 1]), bg.geo,
+                                   x0, x1);
+                // basis: w(q) T_a(2q - 1) F_m(z); chunk a of the row holds phi_{8a..8a+7}
+                const float rr = sqrtf(x0 * x0 + x1 * x1);
+                const float q = fminf(rr * bg.inv_H, 1.f);
+                const float om = 1.f - q * q;
+                const float w = valid ? om * om : 0.f;
+                const float sc = 2.f * q - 1.f;
+                const float inv = 1.f / (rr + bg.eps);
+                const float zr = x0 * inv, zi = x1 * inv;
+                const float z2r = zr * zr - zi * zi, z2i = 2.f * zr * zi;
+                const float z3r = z2r * zr - z2i * zi, z3i = z2r * zi + z2i * zr;
+                const float z4r = z3r * zr - z3i * zi;
+                float tm1 = 1.f, t0 = sc;
+#pragma unroll
+                for (int a = 0; a < 8; ++a) {
+                    float ta;
+                    if (a == 0) {
+                        ta = 1.f;
+                    } else if (a == 1) {
+                        ta = sc;
+                    } else {
+                        ta = 2.f * sc * t0 - tm1;
+                        tm1 = t0;
+                        t0 = ta;
+                    }
+                    const float R = w * ta;
+                    uint4 v;
+                    v.x = pack_bf16x2(R, R * zr);
+                    v.y = pack_bf16x2(R * zi, R * z2r);
+                    v.z = pack_bf16x2(R * z2i, R * z3r);
+                    v.w = pack_bf16x2(R * z3i, R * z4r);
+                    *reinterpret_cast<uint4*>(row + ((a ^ r) << 4)) = v;
+                }
+            } else if (!REL) {
+                // the neighbor's feature row, copied global -> shared in eight asynchronous
+                // 16-byte pieces (zeros for a padding edge)
+                const __nv_bfloat16* hj = h + j * C;
+#pragma unroll
+                for (int c8 = 0; c8 < C / 8; ++c8) {
+                    uint8_t* dst = row + ((c8 ^ r) << 4);
+                    if (valid)
+                        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst)), "l"(hj + 8 * c8)
+                                     : "memory");
+                    else
+                        *reinterpret_cast<uint4*>(dst) = make_uint4(0u, 0u, 0u, 0u);
+                }
+                asm volatile("cp.async.wait_all;" ::: "memory");
+            } else {
+                // the differences of the neighbor's features to particle i's, 16 B per chunk
+                const uint4* hj = reinterpret_cast<const uint4*>(h + j * C);
+                const uint4* hi = reinterpret_cast<const uint4*>(h + (i < n ? i : 0) * C);
+                uint4 vj[C / 8];
+#pragma unroll
+                for (int c8 = 0; c8 < C / 8; ++c8) vj[c8] = valid ? hj[c8] : make_uint4(0u, 0u, 0u, 0u);
+#pragma unroll
+                for (int c8 = 0; c8 < C / 8; ++c8) {
+                    if (REL && valid) {
+                        const uint4 vi = hi[c8];
+                        __nv_bfloat162* pj = reinterpret_cast<__nv_bfloat162*>(&vj[c8]);
+                        const __nv_bfloat162* pi2 = reinterpret_cast<const __nv_bfloat162*>(&vi);
+#pragma unroll
+                        for (int u = 0; u < 4; ++u) {
+                            const float2 a2 = __bfloat1622float2(pj[u]), b2 = __bfloat1622float2(pi2[u]);
+                            pj[u] = __floats2bfloat162_rn(a2.x - b2.x, a2.y - b2.y);
+                        }
+                    }
+                    *reinterpret_cast<uint4*>(row + ((c8 ^ r) << 4)) = vj[c8];
+                }
+            }
+        }
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // generic writes -> tensor core
+        __syncthreads();
+        if (tid == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;");
+#pragma unroll
+            for (int kk = 0; kk < 8; ++kk)  // 16 K rows (2 groups) per MMA
+                mma_bf16(tmem, mn128_desc(smem_u32(A + kk * 4096), 1024u, 2048u),
+                         mn128_desc(smem_u32(B + kk * 2048), 1024u, 1024u), idesc, kk > 0 ? 1u : 0u);
+            mma_commit(&mma_done);
+        }
+        __syncwarp();
+        const bool ok_w = __all_sync(0xffffffffu, mbar_wait(&mma_done, static_cast<uint32_t>(it) & 1u));
+        if (!ok_w && lane == 0) atomicOr(err, 16u);
+        const bool ok = __syncthreads_and(ok_w) != 0;  // the staging below needs every warp's rows
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        // warp w drains TMEM lanes 32 (w % 4) .. + 31 (its quarter), columns 32 (w / 4) .. + 31,
+        // into the B tile (free once the MMA has completed) as the pair's E rows: row 64 p + b,
+        // 128 B, its 16-byte chunks XOR-swizzled by the row so that the lanes' stores spread
+        // over the banks. Then the CTA copies the two particles' E (16 KB, contiguous in
+        // global memory) out with coalesced 16-byte stores.
+        const int qd = warp & 3, half = warp >> 2;
+        if (ok) {
+            const int erow = qd * 32 + lane;  // = 64 pd + b
+#pragma unroll
+            for (int c = 32 * half; c < 32 * half + 32; c += 16) {
+                uint32_t v[16];
+                tmem_ld16(tmem + (static_cast<uint32_t>(qd * 32) << 16) + static_cast<uint32_t>(c), v);
+                uint4 o0, o1;
+                o0.x = pack_bf16x2(__uint_as_float(v[0]) * inv_norm, __uint_as_float(v[1]) * inv_norm);
+                o0.y = pack_bf16x2(__uint_as_float(v[2]) * inv_norm, __uint_as_float(v[3]) * inv_norm);
+                o0.z = pack_bf16x2(__uint_as_float(v[4]) * inv_norm, __uint_as_float(v[5]) * inv_norm);
+                o0.w = pack_bf16x2(__uint_as_float(v[6]) * inv_norm, __uint_as_float(v[7]) * inv_norm);
+                o1.x = pack_bf16x2(__uint_as_float(v[8]) * inv_norm, __uint_as_float(v[9]) * inv_norm);
+                o1.y = pack_bf16x2(__uint_as_float(v[10]) * inv_norm, __uint_as_float(v[11]) * inv_norm);
+                o1.z = pack_bf16x2(__uint_as_float(v[12]) * inv_norm, __uint_as_float(v[13]) * inv_norm);
+                o1.w = pack_bf16x2(__uint_as_float(v[14]) * inv_norm, __uint_as_float(v[15]) * inv_norm);
+                const int ch = c >> 3;  // 16-byte chunk of the row
+                *reinterpret_cast<uint4*>(B + erow * 128 + (((ch) ^ (erow & 7)) << 4)) = o0;
+                *reinterpret_cast<uint4*>(B + erow * 128 + (((ch + 1) ^ (erow & 7)) << 4)) = o1;
+            }
+        }
+        __syncthreads();
+        if (ok) {
+            const int64_t rows = (ia + 1 < n) ? 128 : 64;  // E rows of the pair that exist
+            uint4* dst = reinterpret_cast<uint4*>(E + ia * (64 * C));
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int idx = u * 256 + tid;  // 16-byte unit of the pair's E
+                const int erow = idx >> 3, ch = idx & 7;
+                if (erow < rows) dst[idx] = *reinterpret_cast<const uint4*>(B + erow * 128 + ((ch ^ (erow & 7)) << 4));
+            }
+        }
+        asm volatile("tcgen05.fence::before_thread_sync;");
+        __syncthreads();
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(64));
+}
+
+template <bool REL>
+static int launch_agg_tc_mn(int64_t n, const float* x, const int64_t* off, const int32_t* nbr, const BasisGeo& bg,
+                            float nz, const __nv_bfloat16* h, __nv_bfloat16* E, uint32_t* err, cudaStream_t s) {
+    static std::once_flag once;
+    static cudaError_t attr = cudaSuccess;
+    std::call_once(once, [] {
+        attr = cudaFuncSetAttribute(k_aggregate_tc_mn<REL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    static_cast<int>(kMnSmem));
+    });
+    if (attr != cudaSuccess) return SPH_ERR_CUDA;
+    const unsigned grid = static_cast<unsigned>((n + 2 * kTcPairsPerCta - 1) / (2 * kTcPairsPerCta));
+    k_aggregate_tc_mn<REL><<<grid, 256, kMnSmem, s>>>(n, x, off, nbr, bg, nz, h, E, err);
+    return cudaGetLastError() == cudaSuccess ? SPH_OK : SPH_ERR_CUDA;
+}
+
 template <int C, bool REL>
 static int launch_agg_tc(int64_t n, const float* x, const int64_t* off, const int32_t* nbr, const BasisGeo& bg,
                          float nz, const __nv_bfloat16* h, __nv_bfloat16* E, uint32_t* err, cudaStream_t s) {
@@ -758,6 +990,6 @@ extern "C" int sph_cconv_aggregate_tc(const float* x, int64_t n, const int64_t* 
     if (channels == 32)
         return relative ? launch_agg_tc<32, true>(n, x, offsets, neighbors, bg, nz, hb, Eb, err, s)
                         : launch_agg_tc<32, false>(n, x, offsets, neighbors, bg, nz, hb, Eb, err, s);
-    return relative ? launch_agg_tc<64, true>(n, x, offsets, neighbors, bg, nz, hb, Eb, err, s)
-                    : launch_agg_tc<64, false>(n, x, offsets, neighbors, bg, nz, hb, Eb, err, s);
+    return relative ? launch_agg_tc_mn<true>(n, x, offsets, neighbors, bg, nz, hb, Eb, err, s)
+                    : launch_agg_tc_mn<false>(n, x, offsets, neighbors, bg, nz, hb, Eb, err, s);
 }
