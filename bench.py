@@ -710,6 +710,38 @@ def run_learned(args):
             torch.cuda.synchronize()
         check_device_errors()
         ms_learned = ev[0].elapsed_time(ev[1]) / args.steps
+        # the dominant kernel alone: one 64-channel tensor-core aggregation on the live graph
+        from diffsph_gb300.learned import Graph, aggregate
+        g = Graph(x, cfg, w["batch"])
+        h64 = torch.randn(n, 64, device="cuda").to(torch.bfloat16)
+        aggregate(g, h64)
+        k0, k1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        k0.record(stream)
+        for _ in range(5):
+            aggregate(g, h64)
+        k1.record(stream)
+        torch.cuda.synchronize()
+        agg_ms = k0.elapsed_time(k1) / 5
+        pairs = int(g.offsets[-1].item())
+        # end to end: the state from pinned host memory, one learned step, the state back
+        xh, uh, rh = (t.detach().cpu().pin_memory() for t in (x, u, r))
+        outs = [torch.empty(t.shape, dtype=t.dtype).pin_memory() for t in (x, u, r)]
+        e2e_ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+        e_steps = max(args.steps // 2, 3)
+        e2e_ev[0].record(stream)
+        for _ in range(e_steps):
+            xd, ud, rd = (t.to("cuda", non_blocking=True) for t in (xh, uh, rh))
+            res = stepper.step(xd, ud, rd)
+            for o, t in zip(outs, res):
+                o.copy_(t, non_blocking=True)
+        e2e_ev[1].record(stream)
+        torch.cuda.synchronize()
+        ms_e2e = e2e_ev[0].elapsed_time(e2e_ev[1]) / e_steps
+        bytes_io = sum(t.numel() * t.element_size() for t in (xh, uh, rh))
+        # this library's kernels in one learned step: per domain the neighbor count (13: two
+        # position copies, cell keys, 3 scan kernels, scatter, cell order, gather, query, 3 scan
+        # kernels) and the index fill (1); per layer one aggregation and one contraction (4 + 4)
+        launches = 14 * w["batch"] + 8
         bsol = BatchSolver([c for c, _ in doms], [st["fluid"] for _, st in doms])
         bsol.autotune()
         for _ in range(max(args.warmup, 3)):
@@ -761,6 +793,24 @@ def run_learned(args):
                    "l2": f"inputs ({n} particles x 20 B) {'exceed' if n * 20 > 129e6 else 'fit in'} L2"},
         "clocks": clk.summary(),
     }
+    # algorithmic FLOPs of a 64-channel aggregation: 2 x 64 x 64 per exact pair
+    pk_tf = None
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            pk_tf, pk_kind = float(json.load(f)["bf16_tflops"]), "measured"
+    except Exception:
+        pk_tf, pk_kind = 1900.0, "fallback"
+    flops = 2.0 * 64 * 64 * pairs
+    achieved = flops / (agg_ms / 1e3) / 1e12
+    line["roofline"] = {"bound": "tensor", "kernel": "cconv_aggregate_tc (64 channels)", "achieved": achieved,
+                        "peak": pk_tf, "peak_kind": pk_kind, "unit": "TFLOP/s", "frac": achieved / pk_tf,
+                        "traffic": 4.233e9 / 524288 * n,
+                        "traffic_note": "ncu dram bytes (E write) of k_aggregate_tc_mn on 8 x 65,536 particles, "
+                                        "scaled by the particle count",
+                        "avg_launch_ms": agg_ms, "pairs": pairs, "flop_per_launch": flops}
+    line["e2e"] = {"value": n * k / (ms_e2e / 1e3), "unit": "particle-steps/s", "h2d_bytes_per_step": bytes_io,
+                   "d2h_bytes_per_step": bytes_io}
+    line["gpu_launches"] = launches * args.steps if launches is not None else None
     print(json.dumps(line))
 
 
