@@ -688,6 +688,75 @@ __global__ void k_dom_keys(int64_t n, const float4* __restrict__ X4, const int32
 // is walked without atomics. Derivatives are those of the exact expressions with
 // grad W_ij = f(r) x_ij, f = -20 C/h^4 (1-q)^3, f' = 60 C/h^5 (1-q)^2.
 // ======================================================================================
+// Each particle's pairs are spread over kAdjL lanes: lane sub of the group scans candidates
+// sub, sub + kAdjL, ... of every stencil range, and the group's partial sums are combined by a
+// butterfly of shuffles (a fixed order) before the group's first lane writes the results. At
+// the adjoint's sizes (tens of thousands of particles) one lane per particle leaves most of
+// the GPU idle, and each lane's pair chain is then a quarter as long.
+constexpr int kAdjL = 4;
+
+template <bool PER, class F>
+__device__ __forceinline__ void neighbor_loop_split(bool active, float2 pi, const float4* __restrict__ X4,
+                                                    const int32_t* __restrict__ start, const Grid& g, const Phys& P,
+                                                    int32_t* __restrict__ lst, F&& f) {
+    const int lane = threadIdx.x & 31, sub = lane % kAdjL;
+    int rs[kMaxRanges], re[kMaxRanges];
+    unsigned wmask = 0;
+    const int nrng = active ? stencil_ranges(pi, g, start, rs, re, PER ? &wmask : nullptr) : 0;
+    int r = 0;
+    int s = nrng > 0 ? rs[0] + sub : 0, se = nrng > 0 ? re[0] : 0;
+    auto advance = [&]() {  // to the next range this lane has a candidate in
+        while (r < nrng && s >= se) {
+            ++r;
+            if (r < nrng) {
+                s = rs[r] + sub;
+                se = re[r];
+            }
+        }
+    };
+    advance();
+    int cnt = 0;
+    while (__any_sync(kFull, r < nrng)) {
+        if (r < nrng) {
+            const int left = (se - s + kAdjL - 1) / kAdjL;
+            const int m = left < kUnroll ? left : kUnroll;
+            const bool wr = PER && ((wmask >> r) & 1u);
+            float4 xj[kUnroll];
+#pragma unroll
+            for (int u = 0; u < kUnroll; ++u)
+                if (u < m) xj[u] = __ldg(&X4[s + u * kAdjL]);
+#pragma unroll
+            for (int u = 0; u < kUnroll; ++u) {
+                if (u < m) {
+                    float x0, x1;
+                    if (wr)
+                        pair_vec<true>(pi, make_float2(xj[u].x, xj[u].y), P.geo, x0, x1);
+                    else
+                        pair_vec<false>(pi, make_float2(xj[u].x, xj[u].y), P.geo, x0, x1);
+                    if (sq_norm_ref(x0, x1) <= P.T) lst[(cnt++) * 32 + lane] = s + u * kAdjL;
+                }
+            }
+            s += m * kAdjL;
+            advance();
+        }
+        if (__any_sync(kFull, cnt > kCap - kUnroll)) {
+            const int mc = (int)__reduce_max_sync(kFull, (unsigned)cnt);
+            for (int k = 0; k < mc; ++k)
+                if (k < cnt) f(lst[k * 32 + lane]);
+            cnt = 0;
+        }
+    }
+    const int mc = (int)__reduce_max_sync(kFull, (unsigned)cnt);
+    for (int k = 0; k < mc; ++k)
+        if (k < cnt) f(lst[k * 32 + lane]);
+}
+
+__device__ __forceinline__ float group_sum(float v) {
+#pragma unroll
+    for (int o = kAdjL / 2; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
+    return v;
+}
+
 struct KD {
     float f, fp;
 };
@@ -790,7 +859,7 @@ __global__ void __launch_bounds__(128) k_vjp_rates(int64_t n, const float4* __re
     __shared__ int32_t s_list[4][kCap * 32];
     const Phys& P = D.P;
     const Grid& g = D.g;
-    int64_t k = (int64_t)blockIdx.x * 128 + threadIdx.x;
+    int64_t k = ((int64_t)blockIdx.x * 128 + threadIdx.x) / kAdjL;
     bool inb = k < n;
     float4 xk = inb ? X4[k] : make_float4(0.f, 0.f, 1.f, 0.f);
     float4 vk = inb ? V4[k] : make_float4(0.f, 0.f, 0.f, 0.f);
@@ -801,8 +870,7 @@ __global__ void __launch_bounds__(128) k_vjp_rates(int64_t n, const float4* __re
     float gr = 0.f, gp = 0.f;
     float2 Ps = f2(0.f, 0.f), Vs = f2(0.f, 0.f);
     float Cs = 0.f;
-    neighbor_loop<PER, int32_t>(inb, (int)k, pk, X4, start + D.cell0, g, P, s_list[threadIdx.x >> 5], words,
-                                [&](int j) {
+    neighbor_loop_split<PER>(inb, pk, X4, start + D.cell0, g, P, s_list[threadIdx.x >> 5], [&](int j) {
         if (j == (int)k) return;
         float4 xj = __ldg(&X4[j]);
         float4 vj = __ldg(&V4[j]);
@@ -842,7 +910,20 @@ __global__ void __launch_bounds__(128) k_vjp_rates(int64_t n, const float4* __re
         Vs.y += sV * x1;
         Cs += -ux * kd.f * irj;
     });
-    if (!inb) return;
+    gx.x = group_sum(gx.x);
+    gx.y = group_sum(gx.y);
+    gu.x = group_sum(gu.x);
+    gu.y = group_sum(gu.y);
+    gG.x = group_sum(gG.x);
+    gG.y = group_sum(gG.y);
+    gr = group_sum(gr);
+    gp = group_sum(gp);
+    Ps.x = group_sum(Ps.x);
+    Ps.y = group_sum(Ps.y);
+    Vs.x = group_sum(Vs.x);
+    Vs.y = group_sum(Vs.y);
+    Cs = group_sum(Cs);
+    if (!inb || (threadIdx.x & (kAdjL - 1)) != 0) return;
     int o = uid[k];
     float rho = xk.z;
     // p = B ((rho/rho0)^gamma - 1): dp/drho = B gamma (rho/rho0)^(gamma-1) / rho0
@@ -871,14 +952,13 @@ __global__ void __launch_bounds__(128) k_lam_grad(int64_t n, const float4* __res
                                                   float4* __restrict__ Lg) {
     __shared__ int32_t s_list[4][kCap * 32];
     const Phys& P = D.P;
-    int64_t k = (int64_t)blockIdx.x * 128 + threadIdx.x;
+    int64_t k = ((int64_t)blockIdx.x * 128 + threadIdx.x) / kAdjL;
     bool inb = k < n;
     float4 xk = inb ? X4[k] : make_float4(0.f, 0.f, 1.f, 0.f);
     float2 pk = f2(xk.x, xk.y);
     float M00 = 0.f, M01 = 0.f, M10 = 0.f, M11 = 0.f, g0 = 0.f, g1 = 0.f;
     int nf = 0;
-    neighbor_loop<PER, int32_t>(inb, (int)k, pk, X4, start + D.cell0, D.g, P, s_list[threadIdx.x >> 5], words,
-                                [&](int j) {
+    neighbor_loop_split<PER>(inb, pk, X4, start + D.cell0, D.g, P, s_list[threadIdx.x >> 5], [&](int j) {
         float4 xj = __ldg(&X4[j]);
         float x0, x1;
         pair_vec<PER>(pk, make_float2(xj.x, xj.y), P.geo, x0, x1);
@@ -895,7 +975,14 @@ __global__ void __launch_bounds__(128) k_lam_grad(int64_t n, const float4* __res
         g0 += c * x0;
         g1 += c * x1;
     });
-    if (!inb) return;
+    M00 = group_sum(M00);
+    M01 = group_sum(M01);
+    M10 = group_sum(M10);
+    M11 = group_sum(M11);
+    g0 = group_sum(g0);
+    g1 = group_sum(g1);
+    nf = (int)group_sum((float)nf);
+    if (!inb || (threadIdx.x & (kAdjL - 1)) != 0) return;
     int o = uid[k];
     float m = P.m;
     float G0 = Gbar[2 * o], G1 = Gbar[2 * o + 1];
@@ -951,7 +1038,7 @@ __global__ void __launch_bounds__(128) k_vjp_grad(int64_t n, const float4* __res
                                                   float* __restrict__ xbar, float* __restrict__ rbar) {
     __shared__ int32_t s_list[4][kCap * 32];
     const Phys& P = D.P;
-    int64_t k = (int64_t)blockIdx.x * 128 + threadIdx.x;
+    int64_t k = ((int64_t)blockIdx.x * 128 + threadIdx.x) / kAdjL;
     bool inb = k < n;
     float4 xk = inb ? X4[k] : make_float4(0.f, 0.f, 1.f, 0.f);
     float4 lMk = inb ? LM[k] : make_float4(0.f, 0.f, 0.f, 0.f);
@@ -959,8 +1046,7 @@ __global__ void __launch_bounds__(128) k_vjp_grad(int64_t n, const float4* __res
     float2 pk = f2(xk.x, xk.y);
     float2 gx = f2(0.f, 0.f);
     float gr = 0.f;
-    neighbor_loop<PER, int32_t>(inb, (int)k, pk, X4, start + D.cell0, D.g, P, s_list[threadIdx.x >> 5], words,
-                                [&](int j) {
+    neighbor_loop_split<PER>(inb, pk, X4, start + D.cell0, D.g, P, s_list[threadIdx.x >> 5], [&](int j) {
         if (j == (int)k) return;
         float4 xj = __ldg(&X4[j]);
         float4 lMj = __ldg(&LM[j]);
@@ -977,7 +1063,10 @@ __global__ void __launch_bounds__(128) k_vjp_grad(int64_t n, const float4* __res
         gx.y += ga.y - gb.y;
         gr += ari + brj;
     });
-    if (!inb) return;
+    gx.x = group_sum(gx.x);
+    gx.y = group_sum(gx.y);
+    gr = group_sum(gr);
+    if (!inb || (threadIdx.x & (kAdjL - 1)) != 0) return;
     int o = uid[k];
     xbar[2 * o] += gx.x;
     xbar[2 * o + 1] += gx.y;
@@ -993,13 +1082,12 @@ __global__ void __launch_bounds__(128) k_lam_shift(int64_t n, const float4* __re
                                                    float4* __restrict__ LS, float* __restrict__ mapart) {
     __shared__ int32_t s_list[4][kCap * 32];
     const Phys& P = D.P;
-    int64_t k = (int64_t)blockIdx.x * 128 + threadIdx.x;
+    int64_t k = ((int64_t)blockIdx.x * 128 + threadIdx.x) / kAdjL;
     bool inb = k < n;
     float4 xk = inb ? X4[k] : make_float4(0.f, 0.f, 1.f, 0.f);
     float2 pk = f2(xk.x, xk.y);
     float s0 = 0.f, s1 = 0.f;
-    neighbor_loop<PER, int32_t>(inb, (int)k, pk, X4, start + D.cell0, D.g, P, s_list[threadIdx.x >> 5], words,
-                                [&](int j) {
+    neighbor_loop_split<PER>(inb, pk, X4, start + D.cell0, D.g, P, s_list[threadIdx.x >> 5], [&](int j) {
         if (j == (int)k) return;
         float4 xj = __ldg(&X4[j]);
         float x0, x1;
@@ -1013,7 +1101,9 @@ __global__ void __launch_bounds__(128) k_lam_shift(int64_t n, const float4* __re
         s0 += c * x0;
         s1 += c * x1;
     });
-    if (!inb) return;
+    s0 = group_sum(s0);
+    s1 = group_sum(s1);
+    if (!inb || (threadIdx.x & (kAdjL - 1)) != 0) return;
     int o = uid[k];
     float Ma = P.compute_mach ? __uint_as_float(maxv[0]) * P.inv_cs : 0.1f;
     float sc = P.sh_scale * P.m;
@@ -1049,15 +1139,14 @@ __global__ void __launch_bounds__(128) k_vjp_shift(int64_t n, const float4* __re
                                                    float* __restrict__ xbar, float* __restrict__ rbar) {
     __shared__ int32_t s_list[4][kCap * 32];
     const Phys& P = D.P;
-    int64_t k = (int64_t)blockIdx.x * 128 + threadIdx.x;
+    int64_t k = ((int64_t)blockIdx.x * 128 + threadIdx.x) / kAdjL;
     bool inb = k < n;
     float4 xk = inb ? X4[k] : make_float4(0.f, 0.f, 1.f, 0.f);
     float4 lk = inb ? LS[k] : make_float4(0.f, 0.f, 0.f, 0.f);
     float2 pk = f2(xk.x, xk.y);
     float2 gx = f2(0.f, 0.f);
     float gr = 0.f;
-    neighbor_loop<PER, int32_t>(inb, (int)k, pk, X4, start + D.cell0, D.g, P, s_list[threadIdx.x >> 5], words,
-                                [&](int j) {
+    neighbor_loop_split<PER>(inb, pk, X4, start + D.cell0, D.g, P, s_list[threadIdx.x >> 5], [&](int j) {
         if (j == (int)k) return;
         float4 xj = __ldg(&X4[j]);
         float4 lj = __ldg(&LS[j]);
@@ -1073,7 +1162,10 @@ __global__ void __launch_bounds__(128) k_vjp_shift(int64_t n, const float4* __re
         gx.y += ga.y - gb.y;
         gr += ari + brj;
     });
-    if (!inb) return;
+    gx.x = group_sum(gx.x);
+    gx.y = group_sum(gx.y);
+    gr = group_sum(gr);
+    if (!inb || (threadIdx.x & (kAdjL - 1)) != 0) return;
     int o = uid[k];
     // x'' = x' + delta(x'): the identity part plus the shift's Jacobian
     xbar[2 * o] += xbar_new[2 * o] + gx.x;
@@ -1715,7 +1807,7 @@ extern "C" int sph_solver_vjp_rates(sph_solver_t* S, const float* abar, const fl
     launch_a(S, S->Xc, S->Vc, none, st);  // gradRho^L of the current state (pass-B inputs)
     const Dom& D = S->doms_host[0];
     k_lam_rates<<<blocks_for(S->n), kBlock, 0, st>>>(S->n, S->Xc, S->uid, D, abar, drbar, S->Xh, S->Xf);
-    unsigned gb = blocks_for(S->n, 128);
+    unsigned gb = blocks_for(S->n * kAdjL, 128);  // kAdjL lanes per particle
     if (S->periodic)
         k_vjp_rates<true><<<gb, 128, 0, st>>>(S->n, S->Xc, S->Vc, S->start, D, S->uid, S->Xh, S->Xf, S->words, xbar,
                                               ubar, rbar, Gbar, nu_part);
@@ -1733,7 +1825,7 @@ extern "C" int sph_solver_vjp_gradient(sph_solver_t* S, const float* Gbar, float
     cudaStream_t st = (cudaStream_t)stream;
     if ((rc = rebuild(S, st))) return rc;
     const Dom& D = S->doms_host[0];
-    unsigned gb = blocks_for(S->n, 128);
+    unsigned gb = blocks_for(S->n * kAdjL, 128);  // kAdjL lanes per particle
     if (S->periodic) {
         k_lam_grad<true><<<gb, 128, 0, st>>>(S->n, S->Xc, S->start, D, S->uid, Gbar, S->words, S->Xh, S->Xf);
         k_vjp_grad<true><<<gb, 128, 0, st>>>(S->n, S->Xc, S->start, D, S->uid, S->Xh, S->Xf, S->words, xbar, rbar);
@@ -1755,7 +1847,7 @@ extern "C" int sph_solver_vjp_shift(sph_solver_t* S, const float* xbar_new, floa
     if (cudaMemsetAsync(S->maxv, 0, sizeof(uint32_t), st) != cudaSuccess) return SPH_ERR_CUDA;
     k_maxvel<<<blocks_for(S->n), kBlock, 0, st>>>(S->n, S->Vc, nullptr, S->maxv);
     const Dom& D = S->doms_host[0];
-    unsigned gb = blocks_for(S->n, 128);
+    unsigned gb = blocks_for(S->n * kAdjL, 128);  // kAdjL lanes per particle
     if (S->periodic) {
         k_lam_shift<true><<<gb, 128, 0, st>>>(S->n, S->Xc, S->start, D, S->uid, S->maxv, xbar_new, S->words, S->Xh,
                                               mach_part);
