@@ -70,7 +70,7 @@ EXPORTS = [
     "sph_gemm_bf16_tn", "sph_cconv_aggregate", "sph_cconv_aggregate_t", "sph_cconv_aggregate_tc",
     "sph_neighbor_fill_csr", "sph_solver_ips_workspace_bytes", "sph_solver_set_ips", "sph_solver_ips_result",
     "sph_solver_free_surface_workspace_bytes", "sph_solver_set_free_surface", "sph_solver_free_surface_fields",
-    "sph_pressure_switch", "sph_liuliu_consistent",
+    "sph_pressure_switch", "sph_liuliu_consistent", "sph_solver_set_verlet_reuse", "sph_solver_sort_count",
 ]
 
 _lib = None
@@ -125,6 +125,8 @@ def load(build_if_missing: bool = False):
         "sph_solver_autotune": ([P, ctypes.POINTER(I32), ctypes.POINTER(ctypes.c_float), P], ctypes.c_int),
         "sph_solver_shapes": ([], ctypes.c_int),
         "sph_solver_set_shape": ([P, I32], ctypes.c_int),
+        "sph_solver_set_verlet_reuse": ([P, I32], ctypes.c_int),
+        "sph_solver_sort_count": ([P, ctypes.POINTER(ctypes.c_uint32), P], ctypes.c_int),
         "sph_batch_workspace_bytes": ([PP, ctypes.POINTER(I64), I32, ctypes.POINTER(SZ)], ctypes.c_int),
         "sph_batch_create": ([PP, ctypes.POINTER(I64), I32, P, SZ, ctypes.POINTER(P)], ctypes.c_int),
         "sph_solver_graph_step": ([P, I32, P], ctypes.c_int),

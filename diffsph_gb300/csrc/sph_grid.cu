@@ -87,8 +87,14 @@ __device__ __forceinline__ O block_exclusive(O v, O* total) {
     return res;
 }
 
+// gate: a device word read at entry; when it is given and zero the launch does nothing
+// (the solver skips the cell sort of a step that reuses the previous one)
+__device__ __forceinline__ bool gated_off(const uint32_t* gate) { return gate && *gate == 0u; }
+
 template <typename I, typename O>
-__global__ void k_scan_local(const I* __restrict__ in, O* __restrict__ out, O* __restrict__ sums, int64_t n) {
+__global__ void k_scan_local(const I* __restrict__ in, O* __restrict__ out, O* __restrict__ sums, int64_t n,
+                             const uint32_t* gate) {
+    if (gated_off(gate)) return;
     int64_t base = (int64_t)blockIdx.x * kScanTile + (int64_t)threadIdx.x * kScanItems;
     O v[kScanItems];
     O t = 0;
@@ -110,7 +116,8 @@ __global__ void k_scan_local(const I* __restrict__ in, O* __restrict__ out, O* _
 }
 
 template <typename O>
-__global__ void k_scan_sums(O* sums, int64_t nb) {
+__global__ void k_scan_sums(O* sums, int64_t nb, const uint32_t* gate) {
+    if (gated_off(gate)) return;
     O carry = 0;
     for (int64_t c0 = 0; c0 < nb; c0 += kBlock) {
         int64_t i = c0 + threadIdx.x;
@@ -124,29 +131,33 @@ __global__ void k_scan_sums(O* sums, int64_t nb) {
 }
 
 template <typename O>
-__global__ void k_scan_add(O* __restrict__ out, const O* __restrict__ sums, int64_t n, int64_t nb) {
+__global__ void k_scan_add(O* __restrict__ out, const O* __restrict__ sums, int64_t n, int64_t nb,
+                           const uint32_t* gate) {
+    if (gated_off(gate)) return;
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) out[i] += sums[i / kScanTile];
     if (i == 0) out[n] = sums[nb];
 }
 
 template <typename I, typename O>
-static cudaError_t scan_impl(const I* in, O* out, int64_t n, O* tmp, cudaStream_t s) {
+static cudaError_t scan_impl(const I* in, O* out, int64_t n, O* tmp, cudaStream_t s, const uint32_t* gate) {
     int64_t nb = (n + kScanTile - 1) / kScanTile;
     if (nb == 0) {
         return cudaMemsetAsync(out, 0, sizeof(O), s);
     }
-    k_scan_local<I, O><<<(unsigned)nb, kBlock, 0, s>>>(in, out, tmp, n);
-    k_scan_sums<O><<<1, kBlock, 0, s>>>(tmp, nb);
-    k_scan_add<O><<<(unsigned)((n + kBlock - 1) / kBlock), kBlock, 0, s>>>(out, tmp, n, nb);
+    k_scan_local<I, O><<<(unsigned)nb, kBlock, 0, s>>>(in, out, tmp, n, gate);
+    k_scan_sums<O><<<1, kBlock, 0, s>>>(tmp, nb, gate);
+    k_scan_add<O><<<(unsigned)((n + kBlock - 1) / kBlock), kBlock, 0, s>>>(out, tmp, n, nb, gate);
     return cudaGetLastError();
 }
 
-cudaError_t scan_exclusive(const int32_t* in, int32_t* out, int64_t n, int32_t* tmp, cudaStream_t s) {
-    return scan_impl<int32_t, int32_t>(in, out, n, tmp, s);
+cudaError_t scan_exclusive(const int32_t* in, int32_t* out, int64_t n, int32_t* tmp, cudaStream_t s,
+                           const uint32_t* gate) {
+    return scan_impl<int32_t, int32_t>(in, out, n, tmp, s, gate);
 }
-cudaError_t scan_exclusive(const int32_t* in, int64_t* out, int64_t n, int64_t* tmp, cudaStream_t s) {
-    return scan_impl<int32_t, int64_t>(in, out, n, tmp, s);
+cudaError_t scan_exclusive(const int32_t* in, int64_t* out, int64_t n, int64_t* tmp, cudaStream_t s,
+                           const uint32_t* gate) {
+    return scan_impl<int32_t, int64_t>(in, out, n, tmp, s, gate);
 }
 
 // ------------------------------------------------------------------------------------
@@ -165,7 +176,8 @@ __global__ void k_cell_keys(const float* __restrict__ xy, int stride, int64_t n,
 }
 
 __global__ void k_cell_scatter(int64_t n, const int32_t* __restrict__ key, const int32_t* __restrict__ start,
-                               int32_t* __restrict__ fill, int32_t* __restrict__ perm) {
+                               int32_t* __restrict__ fill, int32_t* __restrict__ perm, const uint32_t* gate) {
+    if (gated_off(gate)) return;
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     int k = key[i];
@@ -174,7 +186,9 @@ __global__ void k_cell_scatter(int64_t n, const int32_t* __restrict__ key, const
 }
 
 // Cells hold a few tens of particles: one thread sorts its cell's slots by input index.
-__global__ void k_cell_order(int64_t ncells, const int32_t* __restrict__ start, int32_t* __restrict__ perm) {
+__global__ void k_cell_order(int64_t ncells, const int32_t* __restrict__ start, int32_t* __restrict__ perm,
+                             const uint32_t* gate) {
+    if (gated_off(gate)) return;
     int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= ncells) return;
     int b = start[c], e = start[c + 1];
@@ -190,13 +204,14 @@ __global__ void k_cell_order(int64_t ncells, const int32_t* __restrict__ start, 
 }
 
 cudaError_t cell_sort_counted(int64_t n, int64_t ncells, const int32_t* key, int32_t* perm, int32_t* count,
-                              int32_t* fill, int32_t* start, int32_t* scan_tmp, cudaStream_t s) {
+                              int32_t* fill, int32_t* start, int32_t* scan_tmp, cudaStream_t s,
+                              const uint32_t* gate) {
     cudaError_t e;
     if ((e = cudaMemsetAsync(fill, 0, sizeof(int32_t) * ncells, s)) != cudaSuccess) return e;
-    if ((e = scan_exclusive(count, start, ncells, scan_tmp, s)) != cudaSuccess) return e;
+    if ((e = scan_exclusive(count, start, ncells, scan_tmp, s, gate)) != cudaSuccess) return e;
     unsigned gb = (unsigned)((n + kBlock - 1) / kBlock);
-    if (n > 0) k_cell_scatter<<<gb, kBlock, 0, s>>>(n, key, start, fill, perm);
-    k_cell_order<<<(unsigned)((ncells + kBlock - 1) / kBlock), kBlock, 0, s>>>(ncells, start, perm);
+    if (n > 0) k_cell_scatter<<<gb, kBlock, 0, s>>>(n, key, start, fill, perm, gate);
+    k_cell_order<<<(unsigned)((ncells + kBlock - 1) / kBlock), kBlock, 0, s>>>(ncells, start, perm, gate);
     return cudaGetLastError();
 }
 

@@ -73,8 +73,11 @@ Geo make_geo(const double mn[2], const double mx[2], const int per[2]);
 
 // Device-wide exclusive scans: out[0..n] with out[n] = total. tmp holds scan_tmp_elems(n).
 int64_t scan_tmp_elems(int64_t n);
-cudaError_t scan_exclusive(const int32_t* in, int32_t* out, int64_t n, int32_t* tmp, cudaStream_t s);
-cudaError_t scan_exclusive(const int32_t* in, int64_t* out, int64_t n, int64_t* tmp, cudaStream_t s);
+// With a gate (a device word), every launch returns at once when the word reads zero.
+cudaError_t scan_exclusive(const int32_t* in, int32_t* out, int64_t n, int32_t* tmp, cudaStream_t s,
+                           const uint32_t* gate = nullptr);
+cudaError_t scan_exclusive(const int32_t* in, int64_t* out, int64_t n, int64_t* tmp, cudaStream_t s,
+                           const uint32_t* gate = nullptr);
 
 // Counting sort of points (xy of a float2 or float4 array given by stride in floats) by
 // cell, with ascending input index inside each cell (deterministic order).
@@ -83,9 +86,11 @@ cudaError_t cell_sort(const float* xy, int stride, int64_t n, const Grid& g, int
                       int32_t* key, int32_t* perm, int32_t* count, int32_t* fill, int32_t* start,
                       int32_t* scan_tmp, cudaStream_t s);
 
-// The same after the keys were computed and counted by the caller (count[key]++).
+// The same after the keys were computed and counted by the caller (count[key]++); with a
+// gate, its kernels do nothing when the word reads zero (start and perm keep their values).
 cudaError_t cell_sort_counted(int64_t n, int64_t ncells, const int32_t* key, int32_t* perm, int32_t* count,
-                              int32_t* fill, int32_t* start, int32_t* scan_tmp, cudaStream_t s);
+                              int32_t* fill, int32_t* start, int32_t* scan_tmp, cudaStream_t s,
+                              const uint32_t* gate = nullptr);
 
 inline size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
 

@@ -102,17 +102,63 @@ __global__ void k_gather(int64_t n, int nF, const int32_t* __restrict__ perm, co
                          const int32_t* __restrict__ uid_in, const int32_t* __restrict__ did_in,
                          float2* __restrict__ Xr_out, float4* __restrict__ X4_out, float4* __restrict__ V4_out,
                          int32_t* __restrict__ uid_out, int32_t* __restrict__ did_out, int32_t* __restrict__ bidx,
-                         uint32_t* __restrict__ words) {
+                         uint32_t* __restrict__ words, float2* __restrict__ Xs, const uint32_t* __restrict__ gate) {
+    if (gate && *gate == 0u) return;
     int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= n) return;
     int o = perm[s];
-    Xr_out[s] = Xr_in[o];
+    const float2 xo = Xr_in[o];
+    Xr_out[s] = xo;
+    Xs[s] = xo;
     X4_out[s] = X4_in[o];
     V4_out[s] = V4_in[o];
     did_out[s] = did_in[o];
     int u = uid_in[o];
     uid_out[s] = u;
     if (u >= nF) bidx[atomicAdd(&words[2], 1u)] = (int32_t)s;
+}
+
+// Verlet reuse: the gathered state goes back into the current buffers (the assignment of
+// buffers stays fixed, so steps that keep the sort need no copy at all)
+__global__ void k_copy_back(int64_t n, const float2* __restrict__ Xr_t, const float4* __restrict__ Xt,
+                            const float4* __restrict__ Vt, const int32_t* __restrict__ uid_t,
+                            const int32_t* __restrict__ did_t, float2* __restrict__ Xr, float4* __restrict__ Xc,
+                            float4* __restrict__ Vc, int32_t* __restrict__ uid, int32_t* __restrict__ did,
+                            const uint32_t* __restrict__ gate) {
+    if (*gate == 0u) return;
+    int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    Xr[s] = Xr_t[s];
+    Xc[s] = Xt[s];
+    Vc[s] = Vt[s];
+    uid[s] = uid_t[s];
+    did[s] = did_t[s];
+}
+
+// Verlet reuse: words[4] (sort this step) is set when a particle moved farther than lim since
+// the last sort, or when the skin list of that sort went invalid (words[3])
+__global__ void k_verlet_check(int64_t n, const float2* __restrict__ Xr, const float2* __restrict__ Xs,
+                               uint32_t* __restrict__ words, float lim2) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    bool far = false;
+    if (i < n) {
+        const float2 a = Xr[i], b = Xs[i];
+        const float e0 = a.x - b.x, e1 = a.y - b.y;
+        far = e0 * e0 + e1 * e1 > lim2;
+    }
+    if (i == 0 && words[3] != 0u) far = true;
+    if (__any_sync(0xffffffffu, far) && (threadIdx.x & 31) == 0) atomicOr(&words[4], 1u);
+}
+
+// start of a sort: reset the gather's boundary count, count the sort, and mark the skin list
+// valid when the caller's first pass A rebuilds it for this sort (invalid otherwise: it
+// belongs to an earlier order)
+__global__ void k_sort_begin(uint32_t* words, int skin_rebuilt) {
+    if (threadIdx.x == 0 && words[4] != 0u) {
+        words[2] = 0u;
+        words[3] = skin_rebuilt ? 0u : 1u;
+        words[5] += 1u;
+    }
 }
 
 // ------------------------------------------------------------------------------------
@@ -367,6 +413,12 @@ __global__ void __launch_bounds__(32 * W) k_pass_a(const Dom D0, int64_t n, cons
                                                    uint32_t* __restrict__ words, int16_t* __restrict__ nl,
                                                    int16_t* __restrict__ nlc, int skin_mode, int16_t* __restrict__ sl,
                                                    int16_t* __restrict__ slc) {
+    // skin_mode 3 / 4: the first pass A of a step under Verlet reuse, launched both ways; 3
+    // runs (as 0: scan, keep the skin list) after a sort, 4 (as 1: filter it) otherwise
+    if (skin_mode >= 3) {
+        if ((words[4] != 0u) != (skin_mode == 3)) return;
+        skin_mode -= 3;
+    }
     extern __shared__ __align__(16) unsigned char s_dyn[];
     __shared__ Dom s_dom[BATCH ? 2 : 1];
     __shared__ int s_id[2];
@@ -398,7 +450,8 @@ __device__ __forceinline__ void pass_b_tile(const Dom& D0, int64_t i, int64_t n,
                                             const float4* __restrict__ V4n, float4* __restrict__ X4o,
                                             float4* __restrict__ V4o, uint32_t* __restrict__ words,
                                             uint32_t* __restrict__ maxv, LT* __restrict__ lst,
-                                            const int16_t* __restrict__ nl, const int16_t* __restrict__ nlc) {
+                                            const int16_t* __restrict__ nl, const int16_t* __restrict__ nlc,
+                                            const float2* __restrict__ Xs) {
     const int dom = BATCH ? dom_of(did, i, n) : 0;
     const Dom& D = BATCH ? dom_ref(doms, s_dom, s_id, dom) : D0;
     const Phys& P = D.P;
@@ -494,7 +547,8 @@ __device__ __forceinline__ void pass_b_tile(const Dom& D0, int64_t i, int64_t n,
         X4o[i] = make_float4(w.x, w.y, rh, eos_p(rh, P.eos));
         V4o[i] = make_float4(u0, u1, 0.f, 0.f);
         {  // the second pass A filters the skin list at these positions
-            const float e0 = xh.x - x.x, e1 = xh.y - x.y;
+            const float2 xs = Xs[i];
+            const float e0 = xh.x - xs.x, e1 = xh.y - xs.y;
             if (e0 * e0 + e1 * e1 > P.skin_lim * P.skin_lim) atomicOr(&words[3], 1u);
         }
     } else {
@@ -525,9 +579,10 @@ __device__ __forceinline__ void pass_b_tile(const Dom& D0, int64_t i, int64_t n,
         }
         if (!isfinite(u0) || !isfinite(u1) || !isfinite(rnew) || !isfinite(xp.x) || !isfinite(xp.y))
             atomicOr(&words[0], SPH_FLAG_NONFINITE);
-        // the cells of this step's sort must still cover h + the displacement at the shift pass
+        // the cells of the last sort must still cover h + the displacement at the shift pass
         // (the shift clamp adds at most sqrt(2) thr dx, covered by the margin of verlet_lim)
-        float e0 = xp.x - x.x, e1 = xp.y - x.y;
+        const float2 xs = Xs[i];
+        float e0 = xp.x - xs.x, e1 = xp.y - xs.y;
         if (sqrtf(e0 * e0 + e1 * e1) > P.verlet_lim) atomicOr(&words[0], SPH_FLAG_VERLET);
         // the shift filters the skin list at these positions
         if (e0 * e0 + e1 * e1 > P.skin_lim * P.skin_lim) atomicOr(&words[3], 1u);
@@ -543,7 +598,7 @@ __global__ void __launch_bounds__(32 * W) k_pass_b(const Dom D0, int64_t n, cons
                                                    const float4* __restrict__ V4n, float4* __restrict__ X4o,
                                                    float4* __restrict__ V4o, uint32_t* __restrict__ words,
                                                    uint32_t* __restrict__ maxv, const int16_t* __restrict__ nl,
-                                                   const int16_t* __restrict__ nlc) {
+                                                   const int16_t* __restrict__ nlc, const float2* __restrict__ Xs) {
     extern __shared__ __align__(16) unsigned char s_dyn[];
     __shared__ Dom s_dom[BATCH ? 2 : 1];
     __shared__ int s_id[2];
@@ -551,7 +606,7 @@ __global__ void __launch_bounds__(32 * W) k_pass_b(const Dom D0, int64_t n, cons
     const int64_t first = (int64_t)blockIdx.x * (32 * W);
     if (BATCH) stage_doms(doms, did, first, first + 32 * W - 1, n, s_dom, s_id);
     pass_b_tile<PER, BATCH, MODE, LT>(D0, first + threadIdx.x, n, X4, V4, start, doms, s_dom, s_id, did, uid, out,
-                                      Xr, X4n, V4n, X4o, V4o, words, maxv, lst, nl, nlc);
+                                      Xr, X4n, V4n, X4o, V4o, words, maxv, lst, nl, nlc, Xs);
 }
 
 // ------------------------------------------------------------------------------------
@@ -666,7 +721,9 @@ __global__ void k_maxvel(int64_t n, const float4* __restrict__ V4, const int32_t
 
 // global cell key = first cell of the particle's domain + its cell in the domain grid
 __global__ void k_dom_keys(int64_t n, const float4* __restrict__ X4, const int32_t* __restrict__ did,
-                           const Dom* __restrict__ doms, int32_t* __restrict__ key, int32_t* __restrict__ count) {
+                           const Dom* __restrict__ doms, int32_t* __restrict__ key, int32_t* __restrict__ count,
+                           const uint32_t* __restrict__ gate) {
+    if (gate && *gate == 0u) return;
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const Dom& D = doms[dom_of(did, i, n)];
@@ -1201,6 +1258,7 @@ static size_t solver_layout(const sph_params_t* p, const int64_t* nF_d, int nd, 
     Carver c{(char*)ws};
     float2* Xr = c.take<float2>(n);
     float2* Xr_t = c.take<float2>(n);
+    float2* Xs = c.take<float2>(n);
     float4* X[4];
     float4* V[4];
     for (int k = 0; k < 4; ++k) X[k] = c.take<float4>(n);
@@ -1237,7 +1295,7 @@ static size_t solver_layout(const sph_params_t* p, const int64_t* nF_d, int nd, 
         S->nF = nF;
         S->nB = nB;
         S->ncells = ncells;
-        S->Xr = Xr; S->Xr_t = Xr_t;
+        S->Xr = Xr; S->Xr_t = Xr_t; S->Xs = Xs;
         S->Xc = X[0]; S->Xh = X[1]; S->Xf = X[2]; S->Xt = X[3];
         S->Vc = V[0]; S->Vh = V[1]; S->Vf = V[2]; S->Vt = V[3];
         S->uid = uid; S->uid_t = uid_t; S->did = did; S->did_t = did_t;
@@ -1453,30 +1511,49 @@ extern "C" int sph_solver_upload(sph_solver_t* S, const float* x_fluid, const fl
                                                     normal_boundary, dist_boundary, rho_boundary, S->doms, S->dom_off,
                                                     S->nd, S->Xr, S->Xc, S->Vc, S->uid, S->did, S->bnormal, S->bdist);
     if (cudaMemsetAsync(S->words, 0, sizeof(uint32_t) * 8, st) != cudaSuccess) return SPH_ERR_CUDA;
+    // a new state is always sorted first
+    if (cudaMemsetAsync(S->words + 4, 1, sizeof(uint32_t), st) != cudaSuccess) return SPH_ERR_CUDA;
     return cudaGetLastError() == cudaSuccess ? SPH_OK : SPH_ERR_CUDA;
 }
 
 // sort by cell and gather the state into the new order
-static int rebuild(sph_solver* S, cudaStream_t st) {
+// With Verlet reuse the sort runs only when k_verlet_check asks for it (words[4]); its kernels
+// are launched every step and return at once otherwise, so a captured graph covers both
+// cases. in_step: the caller is a step, whose first pass A branches on words[4] too (it is
+// left set) and rebuilds the skin list after a sort.
+static int rebuild(sph_solver* S, cudaStream_t st, bool in_step = false) {
+    const uint32_t* gate = S->reuse ? S->words + 4 : nullptr;
+    if (S->reuse)
+        k_verlet_check<<<blocks_for(S->n), kBlock, 0, st>>>(S->n, S->Xr, S->Xs, S->words,
+                                                            S->reuse_lim * S->reuse_lim);
+    else if (cudaMemsetAsync(S->words + 4, 1, sizeof(uint32_t), st) != cudaSuccess)
+        return SPH_ERR_CUDA;
+    k_sort_begin<<<1, 32, 0, st>>>(S->words, in_step ? 1 : 0);
     tbeg(S, KC_SORT, st);
     if (cudaMemsetAsync(S->count, 0, sizeof(int32_t) * S->ncells, st) != cudaSuccess) return SPH_ERR_CUDA;
     k_dom_keys<<<blocks_for(S->n), kBlock, 0, st>>>(S->n, S->Xc, S->nd > 1 ? S->did : nullptr, S->doms, S->key,
-                                                      S->count);
-    if (cell_sort_counted(S->n, S->ncells, S->key, S->perm, S->count, S->fill, S->start, S->scan32, st) !=
+                                                      S->count, gate);
+    if (cell_sort_counted(S->n, S->ncells, S->key, S->perm, S->count, S->fill, S->start, S->scan32, st, gate) !=
         cudaSuccess)
         return SPH_ERR_CUDA;
     tend(S, KC_SORT, st);
-    // words[2]: boundary count of the gather; words[3]: skin-list validity of this sort
-    if (cudaMemsetAsync(S->words + 2, 0, 2 * sizeof(uint32_t), st) != cudaSuccess) return SPH_ERR_CUDA;
     tbeg(S, KC_GATHER, st);
     k_gather<<<blocks_for(S->n), kBlock, 0, st>>>(S->n, (int)S->nF, S->perm, S->Xr, S->Xc, S->Vc, S->uid, S->did,
-                                                    S->Xr_t, S->Xt, S->Vt, S->uid_t, S->did_t, S->bidx, S->words);
+                                                    S->Xr_t, S->Xt, S->Vt, S->uid_t, S->did_t, S->bidx, S->words,
+                                                    S->Xs, gate);
+    if (S->reuse)
+        k_copy_back<<<blocks_for(S->n), kBlock, 0, st>>>(S->n, S->Xr_t, S->Xt, S->Vt, S->uid_t, S->did_t, S->Xr,
+                                                          S->Xc, S->Vc, S->uid, S->did, gate);
     tend(S, KC_GATHER, st);
-    std::swap(S->Xr, S->Xr_t);
-    std::swap(S->Xc, S->Xt);
-    std::swap(S->Vc, S->Vt);
-    std::swap(S->uid, S->uid_t);
-    std::swap(S->did, S->did_t);
+    if (!S->reuse) {
+        std::swap(S->Xr, S->Xr_t);
+        std::swap(S->Xc, S->Xt);
+        std::swap(S->Vc, S->Vt);
+        std::swap(S->uid, S->uid_t);
+        std::swap(S->did, S->did_t);
+    } else if (!in_step && cudaMemsetAsync(S->words + 4, 0, sizeof(uint32_t), st) != cudaSuccess) {
+        return SPH_ERR_CUDA;
+    }
     return cudaGetLastError() == cudaSuccess ? SPH_OK : SPH_ERR_CUDA;
 }
 
@@ -1539,7 +1616,7 @@ static void set_attrs(sph_solver* S) {
 template <bool PER, bool BATCH, typename LT, int W>
 static void launch_a_k(sph_solver* S, float4* X4, float4* V4, RhsOut o, int skin_mode, cudaStream_t st) {
     unsigned gb = (unsigned)((S->n + 32 * W - 1) / (32 * W));
-    if (skin_mode == 0)
+    if (skin_mode == 0 || skin_mode == 3)
         k_pass_a<PER, BATCH, LT, W, true><<<gb, 32 * W, list_bytes<LT, W>(), st>>>(
             S->doms_host[0], S->n, X4, V4, S->start, S->doms, dids(S), S->uid, o, S->words, S->nl, S->nlc, skin_mode,
             S->sl, S->slc);
@@ -1561,10 +1638,10 @@ static void launch_a_t(sph_solver* S, float4* X4, float4* V4, RhsOut o, int skin
 }
 
 // skin_mode: 0 keeps the skin list (first pass A after a sort), 1 filters it (second pass A
-// of the same step), 2 neither
+// of the same step), 2 neither; 3 and 4 are 0 and 1 decided on the device by words[4]
 static void launch_a(sph_solver* S, float4* X4, float4* V4, RhsOut o, cudaStream_t st, int skin_mode = 2) {
     set_attrs(S);
-    const int cls = skin_mode == 1 ? KC_PASS_A : KC_PASS_A_SCAN;
+    const int cls = (skin_mode == 1 || skin_mode == 4) ? KC_PASS_A : KC_PASS_A_SCAN;
     tbeg(S, cls, st);
 #define SPH_CALL_A(LT, W) launch_a_t<LT, W>(S, X4, V4, o, skin_mode, st)
     SPH_SHAPE_DISPATCH(S, SPH_CALL_A)
@@ -1577,7 +1654,7 @@ static void launch_b_k(sph_solver* S, float4* X4, float4* V4, RhsOut o, float4* 
     unsigned gb = (unsigned)((S->n + 32 * W - 1) / (32 * W));
     k_pass_b<PER, BATCH, MODE, LT, W><<<gb, 32 * W, list_bytes<LT, W>(), st>>>(
         S->doms_host[0], S->n, X4, V4, S->start, S->doms, dids(S), S->uid, o, S->Xr, S->Xc, S->Vc, X4o, V4o,
-        S->words, S->maxv, S->nl, S->nlc);
+        S->words, S->maxv, S->nl, S->nlc, S->Xs);
 }
 
 template <int MODE, typename LT, int W>
@@ -1603,14 +1680,21 @@ static void launch_b(sph_solver* S, float4* X4, float4* V4, RhsOut o, float4* X4
 
 static int run_stages(sph_solver* S, cudaStream_t st) {
     RhsOut none = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
-    int rc = rebuild(S, st);
+    int rc = rebuild(S, st, true);
     if (rc) return rc;
     // stage 1 at t^n
     launch_mdbc(S, S->Xc, nullptr, st);
     // skin list (non-periodic domains: there the stencil scan skips the minimum image on most
     // ranges, which the skin filter cannot, and measured no faster)
     const int skin = S->periodic ? 2 : 0;
-    launch_a(S, S->Xc, S->Vc, none, st, skin);
+    if (S->reuse) {
+        // after a sort: scan and keep the skin list; otherwise filter the one kept
+        launch_a(S, S->Xc, S->Vc, none, st, 3);
+        launch_a(S, S->Xc, S->Vc, none, st, 4);
+        if (cudaMemsetAsync(S->words + 4, 0, sizeof(uint32_t), st) != cudaSuccess) return SPH_ERR_CUDA;
+    } else {
+        launch_a(S, S->Xc, S->Vc, none, st, skin);
+    }
     launch_b<1>(S, S->Xc, S->Vc, none, S->Xh, S->Vh, st);
     // stage 2 at the half step; the epilogue also reduces max |u'| for the shifting Mach number
     launch_mdbc(S, S->Xh, nullptr, st);
@@ -1899,8 +1983,36 @@ extern "C" int sph_solver_launches_per_step(const sph_solver_t* S) {
     // the free-surface passes (detection, normals, expansions) when on. An implicit shift adds
     // its solve's launches (1 + 5 per iteration + 1 in place of the shift), which depend on
     // how many iterations it runs.
+    // Verlet reuse launches the displacement check, the copy back of a sort and the first
+    // pass A both ways (one returns at once), every step
     const int fs = (S->fs_on && S->prm.shift_on) ? 2 + S->fs_expand : 0;
-    return 7 + 2 * ((S->nB > 0 ? 2 : 0) + 2) + 1 + fs;
+    return 8 + 2 * ((S->nB > 0 ? 2 : 0) + 2) + 1 + fs + (S->reuse ? 3 : 0);
+}
+
+extern "C" int sph_solver_set_verlet_reuse(sph_solver_t* S, int32_t on) {
+    if (!S || on < 0 || on > 1) return SPH_ERR_ARGUMENT;
+    if (on && (S->periodic || S->nd > 1)) return SPH_ERR_ARGUMENT;
+    if (S->reuse != (on == 1)) {
+        // the captured sequences differ (and so does the buffer rotation of a sort)
+        for (int k = 0; k < 2; ++k) {
+            if (S->graph[k]) cudaGraphExecDestroy(S->graph[k]);
+            S->graph[k] = nullptr;
+        }
+    }
+    S->reuse = on == 1;
+    // a sort ahead of the skin list's limit (0.049 h): a step moves particles up to about
+    // 0.013 h in the first steps of a dam break, so the list keeps holding every pair through
+    // the step that crosses 0.034 h
+    S->reuse_lim = 0.7f * S->doms_host[0].P.skin_lim;
+    return SPH_OK;
+}
+
+extern "C" int sph_solver_sort_count(sph_solver_t* S, uint32_t* sorts, sph_stream_t stream) {
+    if (!S || !sorts) return SPH_ERR_ARGUMENT;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (cudaMemcpyAsync(sorts, S->words + 5, sizeof(uint32_t), cudaMemcpyDeviceToHost, st) != cudaSuccess)
+        return SPH_ERR_CUDA;
+    return cudaStreamSynchronize(st) == cudaSuccess ? SPH_OK : SPH_ERR_CUDA;
 }
 
 extern "C" int sph_solver_kernel_classes(void) { return KC_COUNT; }

@@ -336,12 +336,14 @@ struct sph_solver {
     int64_t ncells;
     bool periodic;
     float2 *Xr, *Xr_t;
+    float2* Xs;                  // raw positions at the last cell sort (displacement checks)
     float4 *Xc, *Xh, *Xf, *Xt;
     float4 *Vc, *Vh, *Vf, *Vt;
     int32_t *uid, *uid_t, *did, *did_t;
     int32_t *key, *perm, *count, *fill, *start, *scan32;
     int32_t* bidx;
-    uint32_t* words;  // [0] flags, [2] boundary count
+    // [0] flags, [2] boundary count, [3] skin list invalid, [4] sort this step, [5] sorts done
+    uint32_t* words;
     int16_t* nl;      // exact neighbor list of the last pass A: slot offsets, [kStoreCap][n]
     int16_t* nlc;     // its length per slot (-1: not stored)
     int16_t* sl;      // skin list of the step's first pass A, [kSkinCap][n]
@@ -356,6 +358,11 @@ struct sph_solver {
     int shape = 0;
     bool attrs_set = false;
     bool tables_uploaded = false;
+    // Verlet reuse of the cell sort and the skin list across steps (single non-periodic
+    // domain): a step sorts again only when a particle moved farther than reuse_lim since
+    // the last sort, or the skin list of that sort went invalid
+    bool reuse = false;
+    float reuse_lim = 0.f;
     // captured step graph
     // captured step graphs, keyed by step count and buffer assignment (two slots: eager
     // steps between replays alternate the assignment)

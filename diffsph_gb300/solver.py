@@ -185,6 +185,13 @@ class Solver:
             self.set_free_surface(threshold=_f(sd.get("BarecascoThreshold", math.pi / 3)),
                                   expansion=int(sd.get("expansionIterations", 2)),
                                   scaling=_f(sh.get("surfaceScaling", 0.1)))
+        # Verlet reuse of the cell sort and skin list, as the reference reuses its neighbor
+        # structure for neighborhood.verletScale > 1 (default 1.5); single non-periodic domains
+        dom = self.params.domain
+        self.verlet_reuse = False
+        if not (dom.periodic[0] or dom.periodic[1]) and \
+                _f(config.get("neighborhood", {}).get("verletScale", 1.5)) > 1.0:
+            self.set_verlet_reuse(True)
 
     def __del__(self):
         h = getattr(self, "handle", None)
@@ -340,6 +347,18 @@ class Solver:
 
     def set_shape(self, shape: int):
         _lib.check("sph_solver_set_shape", self.lib.sph_solver_set_shape(self.handle, int(shape)))
+
+    def set_verlet_reuse(self, on: bool):
+        """Keep the cell sort and the skin list across steps until a particle moved 0.034 h
+        (single non-periodic domains; see sph_solver_set_verlet_reuse)."""
+        _lib.check("sph_solver_set_verlet_reuse", self.lib.sph_solver_set_verlet_reuse(self.handle, int(bool(on))))
+        self.verlet_reuse = bool(on)
+
+    def sort_count(self) -> int:
+        """Cell sorts since the last upload."""
+        c = ctypes.c_uint32()
+        _lib.check("sph_solver_sort_count", self.lib.sph_solver_sort_count(self.handle, ctypes.byref(c), _stream()))
+        return int(c.value)
 
     def launches_per_step(self) -> int:
         return int(self.lib.sph_solver_launches_per_step(self.handle))

@@ -68,7 +68,8 @@ typedef struct sph_params {
     int32_t compute_mach;    /* shifting.computeMach */
     int32_t density_update;  /* 0: the reference's observable update (half-step density),
                                 1: rational symplectic update rho (2-eps)/(2+eps) */
-    double skin;             /* candidate list radius factor (>= 1); lists are rebuilt every step */
+    double skin;             /* cell margin factor (>= 1): the displacement since the last sort
+                                that the cells still cover is (skin - 1) h, less the shift clamp */
     int32_t capacity;        /* candidate slots per particle */
 } sph_params_t;
 
@@ -304,6 +305,19 @@ int sph_solver_download(sph_solver_t* s, float* x_fluid, float* u_fluid, float* 
 
 /* Copies the device error flags (SPH_FLAG_*) to *flags_host; synchronises the stream. */
 int sph_solver_flags(sph_solver_t* s, uint32_t* flags_host, sph_stream_t stream);
+
+/* Verlet reuse of the neighbor structure across steps, as the reference's neighborSearch
+ * does with neighborhood.verletScale > 1 (src/diffSPH/v2/modules/neighborhood.py:505-518,
+ * the default scale 1.5 at :603): a step sorts the particles by cell again, and rebuilds the
+ * skin list of candidates within 1.1 h, only when a particle moved farther than 0.034 h
+ * since the last sort (or the list went invalid); otherwise it keeps that order and filters
+ * the kept list. Single non-periodic domains only (SPH_ERR_ARGUMENT otherwise); off after
+ * sph_solver_create. The decision is taken on the device, so captured step graphs replay
+ * both cases. Results differ from the sort-every-step ones only in the order of each
+ * particle's pair sums. */
+int sph_solver_set_verlet_reuse(sph_solver_t* s, int32_t on);
+/* Number of cell sorts since the last upload (device counter); synchronises the stream. */
+int sph_solver_sort_count(sph_solver_t* s, uint32_t* sorts, sph_stream_t stream);
 
 /* Autotuner: times the neighbor passes under each launch shape (warps per block, width
  * of the per-warp neighbor list) on the current state and keeps the fastest for all

@@ -402,3 +402,64 @@ def test_taylor_green_decays_at_the_viscous_rate():
     assert abs(t - 0.9375) < 1e-9
     nu = float(cfg["diffusion"]["nu"])
     assert abs(amp / np.exp(-2 * np.pi ** 2 * nu * t) - 1) < 5e-3, amp
+
+
+def test_verlet_reuse_skips_sorts_and_matches_sorting_every_step():
+    """Verlet reuse (on by default for one non-periodic domain, as the reference reuses its
+    neighbor structure at neighborhood.verletScale = 1.5): in the dam break's first steps the
+    column's foot moves 0.002-0.013 h per step, so only some steps sort (about one in three).
+    The state equals that of a solver sorting every step up to the order of each particle's
+    pair sums; a graph replay equals the eager steps bit for bit."""
+    cfg, st = scenes.dam_break(dx=1.0 / 32)
+    a = _solver(cfg, st)
+    assert a.verlet_reuse
+    b = _solver(cfg, st)
+    b.set_verlet_reuse(False)
+    a.step(12)
+    b.step(12)
+    a.check()
+    b.check()
+    assert b.sort_count() == 12
+    assert 2 <= a.sort_count() < 12
+    ga, gb = a.download(), b.download()
+    assert rel_max(_np(ga["velocities"]), _np(gb["velocities"])) < 1e-4
+    assert rel_max(_np(ga["densities"]), _np(gb["densities"])) < 1e-5
+    assert float((ga["positions"] - gb["positions"]).abs().max()) < 1e-6
+    c = _solver(cfg, st)
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):
+        for _ in range(6):
+            c.graph_step(2)
+        gc = c.download()
+    s.synchronize()
+    assert c.sort_count() == a.sort_count()
+    for k in ("positions", "velocities", "densities", "boundary_densities"):
+        assert torch.equal(ga[k], gc[k]), k
+
+
+def test_verlet_reuse_sorts_every_step_of_a_fast_flow():
+    """At 20 m/s a step moves every particle 0.048 h, past the 0.034 h reuse limit: each step
+    sorts, and the result equals sorting every step bit for bit."""
+    cfg, st = scenes.dam_break(dx=1.0 / 32)
+    st = copy.deepcopy(st)
+    st["fluid"]["velocities"][:, 0] = np.float32(20.0)
+    a = _solver(cfg, st)
+    b = _solver(cfg, st)
+    b.set_verlet_reuse(False)
+    a.step(3)
+    b.step(3)
+    a.check()
+    b.check()
+    assert a.sort_count() == 3
+    ga, gb = a.download(), b.download()
+    for k in ("positions", "velocities", "densities", "boundary_densities"):
+        assert torch.equal(ga[k], gb[k]), k
+
+
+def test_verlet_reuse_is_rejected_on_periodic_domains():
+    from diffsph_gb300._lib import SphError
+    cfg, st = scenes.taylor_green(16)
+    sol = _solver(cfg, st)
+    assert not getattr(sol, "verlet_reuse", False)
+    with pytest.raises(SphError):
+        sol.set_verlet_reuse(True)
