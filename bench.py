@@ -29,14 +29,14 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "particle-steps/s (plain delta-SPH step)"
-# dram__bytes_read + dram__bytes_write of one launch per fluid particle, from the ncu captures
-# summarised in profiles/pass_a_gradient_dambreak_dx512.md (the mean of the skin-building
-# launch, 20.30 + 80.22 MB, and the skin-filtering launch, 78.87 + 19.92 MB, / 524,288) and
-# profiles/pass_b_rates_dambreak_dx512.md (74.60 + 4.14 MB / 524,288)
-PASS_A_DRAM_BYTES_PER_PARTICLE = 190.1
+# dram__bytes_read + dram__bytes_write of one launch per fluid particle, from ncu captures of
+# the dam break at dx = 1/512 (524,288 fluid particles): pass A is the mean of the four
+# working launches of two steps under Verlet reuse (19.05 + 78.72, 78.89 + 18.56,
+# 79.05 + 18.85 and 78.91 + 18.46 MB), pass B one launch (74.60 + 4.14 MB)
+PASS_A_DRAM_BYTES_PER_PARTICLE = 186.2
 PASS_B_DRAM_BYTES_PER_PARTICLE = 150.2
-# the same for one product of the implicit shift (k_ips_spmv), profiles/ips_spmv_fourier512.md
-# ((192.06 + 3.65) MB and (189.98 + 3.62) MB / 262,144)
+# the same for one product of the implicit shift (k_ips_spmv) on the jittered periodic flow
+# of 512^2 particles ((192.06 + 3.65) MB and (189.98 + 3.62) MB / 262,144)
 IPS_SPMV_DRAM_BYTES_PER_PARTICLE = 742.0
 
 WORKLOADS = {
@@ -410,9 +410,9 @@ def run_ours(args):
                 "peak_kind": pk_kind, "unit": "GB/s",
                 "frac": (achieved / pk) if achieved else None,
                 "traffic": PASS_A_DRAM_BYTES_PER_PARTICLE * nF,
-                "traffic_note": "ncu dram bytes of k_pass_a on dambreak_dx512 (190.1 B/particle, the "
-                                "mean of the skin-building and skin-filtering launches), scaled by "
-                                "the particle count",
+                "traffic_note": "ncu dram bytes of k_pass_a on dambreak_dx512 (186.2 B/particle, the "
+                                "mean of the skin-building and skin-filtering launches of two "
+                                "steps under Verlet reuse), scaled by the particle count",
                 "alg_bytes_per_particle": ab["pass_a"], "avg_launch_ms": pa_avg,
                 "pass_b": {"achieved": achieved_b, "frac": (achieved_b / pk) if achieved_b else None,
                            "alg_bytes_per_particle": ab["pass_b"], "avg_launch_ms": pb_avg,
