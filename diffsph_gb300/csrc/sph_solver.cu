@@ -4,17 +4,19 @@
 //   integrate(simulationStep) with scheme symplecticEuler (modules/integration.py:357-392),
 //   then solveShifting (modules/shifting.py:882-1019, delta+ branch, one iteration).
 //
-// Data layout (structure of arrays, particles in cell-sorted order, re-sorted every step):
+// Data layout (structure of arrays, particles in cell-sorted order, re-sorted every step or,
+// under Verlet reuse, when a particle moved 0.034 h since the last sort):
 //   Xr[n]  float2  raw positions (never wrapped, like the reference state)
+//   Xs[n]  float2  raw positions at the last sort
 //   X4[n]  float4  (wrapped x, wrapped y, rho, p); rho carries the sign bit for boundary
 //                  particles (-rho), so a neighbor's kind costs no extra load
 //   V4[n]  float4  (u, v, gradRho^L x, gradRho^L y)
 // Neighbor passes walk the 5x5 half-cell stencil of every particle over the sorted arrays,
 // keep the exact neighbors (the reference's fp32 test) in a per-warp shared-memory list and
 // evaluate the pair terms over it. The first pass A after a sort also stores the skin list
-// (candidates within 1.1 h) that the second pass A and the shift filter, and every pass A
-// stores its exact list for the pass B that follows. Per step:
-//   sort by cell -> gather
+// (candidates within 1.1 h) that the later passes filter until the next sort, and every
+// pass A stores its exact list for the pass B that follows. Per step:
+//   displacement check -> sort by cell -> gather (the last two only when sorting)
 //   stage 1: mDBC ghosts -> pass A -> pass B (+ half-step update)
 //   stage 2: mDBC ghosts -> pass A -> pass B (+ final update, max |u|)
 //   shift pass (+ position update)
