@@ -90,7 +90,10 @@ def peaks():
 
 
 class ClockSampler:
-    """nvidia-smi clock / throttle sampling during the timed region."""
+    """nvidia-smi clock / throttle sampling during the timed region: the sampler is live (its
+    first sample has arrived) before the region starts, samples every 20 ms, and keeps the
+    samples whose arrival falls inside the region; a region shorter than the sampling interval
+    gets the first sample after it instead (and says so in `window`)."""
 
     Q = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
@@ -99,26 +102,35 @@ class ClockSampler:
         self.index = index
         self.samples = []
         self.proc = None
+        self.t0 = self.t1 = None
+        self.first = threading.Event()
 
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
-                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", "20"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
+            self.first.wait(timeout=5.0)
         except Exception:
             self.proc = None
+        self.t0 = time.monotonic()
         return self
 
     def _read(self):
         for line in self.proc.stdout:
             parts = [p.strip() for p in line.split(",")]
             if len(parts) == 6:
-                self.samples.append(parts)
+                self.samples.append((time.monotonic(), parts))
+                self.first.set()
 
     def __exit__(self, *a):
+        self.t1 = time.monotonic()
         if self.proc is not None:
+            deadline = self.t1 + 0.5
+            while not any(t >= self.t0 for t, _ in self.samples) and time.monotonic() < deadline:
+                time.sleep(0.005)
             self.proc.terminate()
             try:
                 self.proc.wait(timeout=5)
@@ -126,14 +138,18 @@ class ClockSampler:
                 self.proc.kill()
 
     def summary(self):
-        if not self.samples:
+        inside = [p for t, p in self.samples if self.t0 is not None and self.t0 <= t <= self.t1]
+        after = [p for t, p in self.samples if self.t1 is not None and t > self.t1][:1]
+        used, window = (inside, "timed region") if inside else (after, "first sample after the timed region")
+        if not used:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
-        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
-        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        sm = [float(s[0]) for s in used if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in used if s[1].replace(".", "").isdigit()]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[k] for s in self.samples for k in range(4) if s[2 + k].lower() == "active"})
+        reasons = sorted({names[k] for s in used for k in range(4) if s[2 + k].lower() == "active"})
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": reasons, "samples": len(self.samples)}
+                "reasons": reasons, "samples": len(used), "window": window,
+                "region_s": round(self.t1 - self.t0, 4)}
 
 
 def algorithmic_bytes(nbar):
@@ -822,7 +838,7 @@ def run_learned(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="dambreak_dx1024", choices=list(WORKLOADS))
