@@ -1,0 +1,65 @@
+"""Host-side pieces of bench.py, on the CPU.
+
+The clock sampler's window logic is checked against a stand-in nvidia-smi that prints one
+sample every 20 ms. The algorithmic bytes per particle are checked against their
+definition: 4 n̄ + 24 for pass A, 4 n̄ + 44 for pass B and 24 n̄ + 352 for the step.
+"""
+import os
+import time
+
+import pytest
+
+import bench
+
+IDLE = "2070, 2070, Not Active, Not Active, Not Active, Not Active"
+
+
+def _fake_smi(tmp_path, line, delay=0.2):
+    p = tmp_path / "nvidia-smi"
+    p.write_text(f'#!/bin/bash\nsleep {delay}\nwhile true; do echo "{line}"; sleep 0.02; done\n')
+    p.chmod(0o755)
+    return str(tmp_path) + os.pathsep + os.environ.get("PATH", "")
+
+
+def test_clock_sampler_keeps_the_samples_of_the_region(tmp_path, monkeypatch):
+    monkeypatch.setenv("PATH", _fake_smi(tmp_path, IDLE))
+    with bench.ClockSampler(0) as c:
+        time.sleep(0.25)
+    s = c.summary()
+    assert s["window"] == "timed region"
+    assert s["samples"] >= 3
+    assert s["sm_mhz"] == 2070.0 and s["sm_max_mhz"] == 2070.0
+    assert s["reasons"] == []
+
+
+def test_clock_sampler_reports_throttle_reasons(tmp_path, monkeypatch):
+    monkeypatch.setenv("PATH", _fake_smi(tmp_path, "1500, 2070, Not Active, Active, Not Active, Active"))
+    with bench.ClockSampler(0) as c:
+        time.sleep(0.1)
+    s = c.summary()
+    assert s["sm_mhz"] == 1500.0
+    assert s["reasons"] == ["hw_thermal_slowdown", "sw_power_cap"]
+
+
+def test_short_region_takes_the_next_sample(tmp_path, monkeypatch):
+    monkeypatch.setenv("PATH", _fake_smi(tmp_path, IDLE))
+    with bench.ClockSampler(0) as c:
+        pass
+    s = c.summary()
+    assert s["samples"] == 1
+    assert s["window"] in ("timed region", "first sample after the timed region")
+
+
+def test_no_nvidia_smi_means_unsampled(tmp_path, monkeypatch):
+    monkeypatch.setenv("PATH", str(tmp_path))
+    with bench.ClockSampler(0) as c:
+        pass
+    assert c.summary()["reasons"] == ["unsampled"]
+
+
+@pytest.mark.parametrize("nbar", [1.0, 48.94, 60.0])
+def test_algorithmic_bytes(nbar):
+    ab = bench.algorithmic_bytes(nbar)
+    assert ab["pass_a"] == pytest.approx(4 * nbar + 24)
+    assert ab["pass_b"] == pytest.approx(4 * nbar + 44)
+    assert ab["step"] == pytest.approx(24 * nbar + 352)
