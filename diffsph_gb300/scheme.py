@@ -10,11 +10,13 @@ Same signatures and return values as:
 * ``computePressureAccelSwitch(stateA, stateB, neighborhood, config)``
                                                 src/diffSPH/v2/modules/pressureForce.py:15-33
 
-State dicts hold torch tensors (any device). The solver keeps its own copy of the particle
-state on the GPU between calls of one state dict (cached under the key ``'sph103'``), so a
-runner loop ``integrate -> solveShifting -> positions += dx`` re-uploads only what the
-caller changed. ``simulationStep`` writes the intermediates the reference leaves in the
-state (``L``, ``gradRho^L``, ``pressures``, wall densities, ``numNeighbors``).
+State dicts hold torch tensors (any device). One solver (its workspace, captured graphs
+and tuned launch shape) is cached per state dict under the key ``'sph103'`` and reused
+while the particle counts and the config object stay the same. Each call uploads the
+state's current positions, velocities and densities, since the runner may have changed
+them (``positions += dx`` after ``solveShifting``), and an upload always sorts.
+``simulationStep`` writes the intermediates the reference leaves in the state (``L``,
+``gradRho^L``, ``pressures``, wall densities, ``numNeighbors``).
 """
 from __future__ import annotations
 
