@@ -390,7 +390,9 @@ def run_ours(args):
         sol.check()
         ms = reduce_max(ms, world)
         value = world * nF * steps / (ms / 1e3)
-        e2e = run_e2e(sol, scene, batched, nF, world, min(steps, 10), stream)
+        # a one-step graph where the buffers never rotate (Verlet reuse); eager steps otherwise
+        one_step_graph = bool(getattr(sol, "verlet_reuse", False)) and not ips
+        e2e = run_e2e(sol, scene, batched, nF, world, min(steps, 10), stream, one_step_graph)
     pk, pk_kind = peaks()
     ab = algorithmic_bytes(nbar)
     # the dominant kernel of a step (largest share of its device time): pass A
@@ -467,9 +469,10 @@ def run_ours(args):
     print(json.dumps(line))
 
 
-def run_e2e(sol, scene, batched, nF, world, e_steps, stream):
+def run_e2e(sol, scene, batched, nF, world, e_steps, stream, one_step_graph=False):
     """Same metric through the public API with host buffers: every step uploads the state
-    from pinned host memory, advances one step and reads the state back."""
+    from pinned host memory, advances one step (a replayed one-step graph when
+    one_step_graph) and reads the state back."""
     import torch
     if batched:
         fl = {k: torch.cat([torch.from_numpy(s["fluid"][k]) for _, s in scene]) for k in
@@ -494,7 +497,10 @@ def run_e2e(sol, scene, batched, nF, world, e_steps, stream):
         b = ({k: dev_in[("b", k)] for k in ("positions", "normals", "distances", "densities")}
              if bd is not None else None)
         sol.upload(f, b)
-        sol.step(1)
+        if one_step_graph:
+            sol.graph_step(1)
+        else:
+            sol.step(1)
         got = sol.download()
         for k, v in host_out.items():
             v.copy_(got[k], non_blocking=True)
@@ -512,7 +518,8 @@ def run_e2e(sol, scene, batched, nF, world, e_steps, stream):
     h2d = sum(v.numel() * 4 for v in host_in.values())
     d2h = sum(v.numel() * 4 for v in host_out.values())
     return {"value": world * nF * e_steps / (ms / 1e3), "unit": "particle-steps/s",
-            "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "steps": e_steps}
+            "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "steps": e_steps,
+            "one_step_graph": bool(one_step_graph)}
 
 
 def run_adjoint(args):

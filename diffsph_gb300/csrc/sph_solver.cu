@@ -1764,9 +1764,10 @@ extern "C" int sph_solver_step(sph_solver_t* S, int32_t n_steps, sph_stream_t st
 
 // The step sequence is static, so a fixed number of steps can be captured once into a CUDA
 // graph and replayed. Every step swaps the sorted/gather buffers, so an even number of steps
-// returns the handle to the buffer assignment it was captured with.
+// returns the handle to the buffer assignment it was captured with; under Verlet reuse the
+// assignment never changes and any number of steps can be captured.
 extern "C" int sph_solver_graph_step(sph_solver_t* S, int32_t n_steps, sph_stream_t stream) {
-    if (!S || n_steps < 2 || (n_steps & 1)) return SPH_ERR_ARGUMENT;
+    if (!S || n_steps < 1 || (!S->reuse && (n_steps & 1))) return SPH_ERR_ARGUMENT;
     cudaStream_t st = (cudaStream_t)stream;
     if (st == nullptr) return SPH_ERR_ARGUMENT;  // the legacy default stream cannot be captured
     // a graph bakes in which buffer holds the current state; eager steps, integrate and

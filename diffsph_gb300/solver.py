@@ -224,7 +224,8 @@ class Solver:
         _lib.check("sph_solver_step", self.lib.sph_solver_step(self.handle, int(n), _stream()))
 
     def graph_step(self, n: int = 2):
-        """n (even) steps replayed from a captured CUDA graph; needs a non-default stream."""
+        """n steps replayed from a captured CUDA graph (n even, or any n >= 1 under Verlet
+        reuse); needs a non-default stream."""
         if torch.cuda.current_stream().cuda_stream == 0:
             raise RuntimeError("graph_step needs a non-default CUDA stream (torch.cuda.stream(...))")
         _lib.check("sph_solver_graph_step", self.lib.sph_solver_graph_step(self.handle, int(n), _stream()))

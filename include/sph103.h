@@ -167,7 +167,8 @@ int sph_solver_step(sph_solver_t* s, int32_t n_steps, sph_stream_t stream);
 /* Same as sph_solver_step, replayed from a CUDA graph captured on first use. The solver
  * keeps two graphs, keyed by n_steps and by which internal buffers hold the current state
  * (eager steps, integrate and shift rotate them); other calls capture again. n_steps must
- * be even and stream must not be the legacy default stream. */
+ * be even, or at least 1 under Verlet reuse (whose sorts copy back and never rotate the
+ * buffers), and stream must not be the legacy default stream. */
 int sph_solver_graph_step(sph_solver_t* s, int32_t n_steps, sph_stream_t stream);
 
 /* The two halves of a step as the reference runner calls them: integrate (both

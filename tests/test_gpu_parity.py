@@ -435,6 +435,15 @@ def test_verlet_reuse_skips_sorts_and_matches_sorting_every_step():
     assert c.sort_count() == a.sort_count()
     for k in ("positions", "velocities", "densities", "boundary_densities"):
         assert torch.equal(ga[k], gc[k]), k
+    # the buffers never rotate under reuse, so one-step graphs replay too
+    d = _solver(cfg, st)
+    with torch.cuda.stream(s):
+        for _ in range(12):
+            d.graph_step(1)
+        gd = d.download()
+    s.synchronize()
+    for k in ("positions", "velocities", "densities", "boundary_densities"):
+        assert torch.equal(ga[k], gd[k]), k
 
 
 def test_verlet_reuse_sorts_every_step_of_a_fast_flow():
@@ -463,3 +472,9 @@ def test_verlet_reuse_is_rejected_on_periodic_domains():
     assert not getattr(sol, "verlet_reuse", False)
     with pytest.raises(SphError):
         sol.set_verlet_reuse(True)
+    # without reuse every step rotates the buffers: graphs hold an even number of steps
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):
+        with pytest.raises(SphError):
+            sol.graph_step(1)
+    s.synchronize()
