@@ -197,3 +197,28 @@ def test_liuliu_consistent_against_reference():
         assert rel_max(M, z[f"liuliu/{name}/M"]) < 1e-5, name
         assert rel_max(b, z[f"liuliu/{name}/b"]) < 1e-5, name
         assert rel_max(sol, z[f"liuliu/{name}/solution"]) < 1e-3, name
+
+
+def test_pinv2x2_edge_cases_against_reference():
+    """The reference's closed-form pinv2x2 (math.py:11-57) on 183 fp32 matrices
+    (tests/golden/make_pinv_golden.py): general, zero, near-singular (condition up to 1e5,
+    where the 1e-7 floor replaces the smaller singular value), negative-determinant, diagonal,
+    symmetric, rotation and normalisation-like matrices agree within 1e-6 of each result's
+    magnitude, and the singular values of all of them within 1e-6. The 32 rank-1 matrices are
+    compared by their singular values only: there S1 - S2 cancels to rounding noise and the
+    sign s22 of a cancelling sum picks the direction of the floored value, so L is noise in
+    any fp32 evaluation, the reference's included."""
+    import os
+    z = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "pinv2x2_cases.npz"))
+    M, L, ev = z["M"], z["L"], z["eigVals"]
+    Lo, evo = O.pinv2x2(M.copy(), eigenvalues=True)
+    n = M.shape[0]
+    rank1 = np.zeros(n, bool)
+    rank1[64:96] = True
+    assert np.linalg.matrix_rank(M[rank1].astype(np.float64), tol=1e-5).max() == 1
+    err = np.abs(Lo - L).reshape(n, -1).max(1) / np.maximum(np.abs(L).reshape(n, -1).max(1), 1e-30)
+    assert err[~rank1].max() < 1e-6
+    assert np.array_equal(L[96:100], np.zeros_like(L[96:100]))  # the zero matrix maps to zero
+    assert np.array_equal(Lo[96:100], L[96:100])
+    ev_err = np.abs(evo - ev).max(1) / np.abs(ev).max(1)
+    assert ev_err.max() < 1e-6
