@@ -125,3 +125,14 @@ def test_params_reject_open_boundary_regions():
     cfg["regions"] = [{"type": "outlet", "sdf": lambda p: p[:, 0]}]
     with pytest.raises(ValueError):
         params_from_config(cfg, 1.0)
+
+
+def test_handle_entry_points_reject_null_handles(lib):
+    """Host-side argument checks of the handle-based entry points, before any device work."""
+    u32 = ctypes.c_uint32()
+    assert lib.sph_solver_set_verlet_reuse(None, 1) == 1
+    assert lib.sph_solver_sort_count(None, ctypes.byref(u32), None) == 1
+    assert lib.sph_solver_flags(None, ctypes.byref(u32), None) == 1
+    assert lib.sph_solver_graph_step(None, 2, None) == 1
+    assert lib.sph_solver_step(None, 1, None) == 1
+    assert lib.sph_solver_launches_per_step(None) == -1
