@@ -80,3 +80,22 @@ def test_tait_equation_of_state_round_trip():
     back = O.stiff_tait_eos({"densities": rho}, cfg)
     assert np.max(np.abs(back - p)) < 1e-12 * rho0 * cs ** 2
     assert O.stiff_tait_eos({"densities": np.array([rho0])}, cfg)[0] == 0.0
+
+
+@pytest.mark.parametrize("nx", [16, 64])
+def test_lattice_density_is_the_kernel_lattice_sum(nx):
+    """Density summation (density.py:6-15) on a uniform periodic lattice with h = 4 dx is
+    the same at every particle: rho0 sum_{|k| <= 4} W(|k| / 4) dx^2 over the integer offsets
+    k, 1.0012058 rho0 for the Wendland C2 kernel, whatever the resolution."""
+    from diffsph_gb300 import scenes
+    cfg, st = scenes.taylor_green(nx)
+    fl = _as64(st)["fluid"]
+    nb = O.neighbor_search(fl, fl, cfg)
+    rho = O.compute_density(fl, fl, nb, cfg)
+    k = np.arange(-4, 5)
+    I, J = np.meshgrid(k, k)
+    q = np.sqrt(I ** 2 + J ** 2) / 4.0
+    lattice = np.sum(np.where(q <= 1, (1 - q) ** 4 * (1 + 4 * q), 0.0)) * 7 / np.pi / 16
+    rho0 = float(cfg["fluid"]["rho0"])
+    assert abs(lattice - 1.0012058) < 1e-7
+    assert np.max(np.abs(rho - lattice * rho0)) < 1e-12 * rho0
