@@ -10,6 +10,7 @@ the oracle in fp64.
   isotropic, so L = c I, with c within 1e-3 of 1 at h = 4 dx.
 - The Tait equation of state (pressureEOS.py:5-11) inverts in closed form:
   rho = rho0 (1 + gamma p / (rho0 c0^2))^(1 / gamma).
+- Density summation on a uniform lattice is the kernel's lattice sum.
 """
 import copy
 
