@@ -63,3 +63,27 @@ def test_algorithmic_bytes(nbar):
     assert ab["pass_a"] == pytest.approx(4 * nbar + 24)
     assert ab["pass_b"] == pytest.approx(4 * nbar + 44)
     assert ab["step"] == pytest.approx(24 * nbar + 352)
+
+
+def _args(**kw):
+    import argparse
+    a = dict(gpus=2, steps=1, warmup=0, impl="reference", workload="dambreak_dx1024", no_cpu_baseline=True)
+    a.update(kw)
+    return argparse.Namespace(**a)
+
+
+def test_reference_arm_prints_only_on_rank_zero(monkeypatch, capsys):
+    """Under torchrun the reference arm runs on rank 0 alone; the other ranks exit without
+    work and print nothing."""
+    monkeypatch.setenv("RANK", "1")
+    bench.run_reference(_args())
+    assert capsys.readouterr().out == ""
+
+
+@pytest.mark.parametrize("workload", ["learned_fourier_b32", "adjoint_fourier128", "outlet_mirror_1024"])
+def test_reference_arm_without_a_reference_path_says_why(monkeypatch, capsys, workload):
+    import json
+    monkeypatch.setenv("RANK", "0")
+    bench.run_reference(_args(workload=workload))
+    line = json.loads(capsys.readouterr().out.strip())
+    assert line["impl"] == "reference" and line["unavailable"]
