@@ -66,10 +66,10 @@ def simulationStep(state, config):
     return (u, dudt, drhodt), (torch.as_tensor(bd["velocities"]).clone(), None, torch.zeros_like(bd["densities"]))
 
 
-def integrate(simulationStep_, perennialState, config, previousStep=None):
+def integrate(simulationStep, perennialState, config, previousStep=None):
     """symplecticEuler step of the reference (both right-hand sides fused on the GPU).
 
-    ``simulationStep_`` is accepted for signature compatibility; the fused kernels
+    ``simulationStep`` is accepted for signature compatibility; the fused kernels
     evaluate the δ-SPH right-hand side themselves. Returns
     (perennialState, tempState, dxdt, dudt, drhodt) like the reference; the rates of
     the fused step are not materialised, so the last three are None."""
