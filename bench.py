@@ -353,9 +353,14 @@ def run_ours(args):
         # overhead); per-kernel times come from a short event-timed eager loop afterwards. An
         # implicit shift runs eagerly: it stops launching once its solve has returned, where a
         # graph would hold every one of its max_iter iterations
-        steps = args.steps + (args.steps & 1)
+        # exactly K steps: pairs from the two-step graph, an odd last step from a one-step
+        # graph under Verlet reuse (its buffers never rotate) or else eagerly
+        steps = args.steps
+        one_graph = bool(getattr(sol, "verlet_reuse", False))
         if not ips:
             sol.graph_step(2)  # capture
+            if steps & 1 and one_graph:
+                sol.graph_step(1)  # capture
         sol.check()
         sorts0 = sol.sort_count()
         torch.cuda.synchronize()
@@ -372,6 +377,11 @@ def run_ours(args):
             else:
                 for _ in range(steps // 2):
                     sol.graph_step(2)
+                if steps & 1:
+                    if one_graph:
+                        sol.graph_step(1)
+                    else:
+                        sol.step(1)
             e1.record(stream)
             torch.cuda.synchronize()
         ms = e0.elapsed_time(e1)
