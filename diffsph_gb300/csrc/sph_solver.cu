@@ -34,9 +34,6 @@
 
 namespace sph {
 
-static const char* kClassNames[KC_COUNT] = {"cell_sort", "gather", "mdbc_ghosts", "pass_a_gradient",
-                                             "pass_b_rates", "shift", "pass_a_scan", "ips_setup",
-                                             "ips_spmv", "ips_vector", "free_surface"};
 
 // ------------------------------------------------------------------------------------
 // upload / download / gather
@@ -2034,7 +2031,7 @@ extern "C" int sph_solver_set_shape(sph_solver_t* S, int32_t shape) {
 }
 
 extern "C" const char* sph_solver_kernel_name(int cls) {
-    return (cls >= 0 && cls < KC_COUNT) ? kClassNames[cls] : nullptr;
+    return kernel_class_name(cls);
 }
 
 extern "C" int sph_solver_set_timing(sph_solver_t* S, int32_t enabled) {

@@ -4,6 +4,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 #include <stdint.h>
 
 #include <vector>
@@ -22,6 +23,14 @@ enum KernelClass {
     KC_SORT = 0, KC_GATHER, KC_MDBC, KC_PASS_A, KC_PASS_B, KC_SHIFT, KC_PASS_A_SCAN,
     KC_IPS_SETUP, KC_IPS_SPMV, KC_IPS_VECTOR, KC_SURFACE, KC_COUNT
 };
+
+// The classes' names: sph_solver_kernel_name and the NVTX ranges around their launches
+inline const char* kernel_class_name(int cls) {
+    static const char* const names[KC_COUNT] = {"cell_sort", "gather", "mdbc_ghosts", "pass_a_gradient",
+                                                 "pass_b_rates", "shift", "pass_a_scan", "ips_setup",
+                                                 "ips_spmv", "ips_vector", "free_surface"};
+    return (cls >= 0 && cls < KC_COUNT) ? names[cls] : nullptr;
+}
 
 // Launch shapes of the neighbor passes (warps per block, list entry width), picked per
 // problem by sph_solver_autotune; shape 0 is the default.
@@ -420,8 +429,11 @@ inline unsigned blocks_for(int64_t n, int threads = kBlock) { return (unsigned)(
 template <typename LT, int W>
 constexpr size_t list_bytes() { return (size_t)W * kCap * 32 * sizeof(LT); }
 
-// timing brackets (only for classes in the mask)
+// brackets of each launch group: an NVTX range named after its class (host-side, so a
+// profiler can select the group's kernels by range), and CUDA events for the classes in the
+// timing mask
 inline void tbeg(sph_solver* S, int cls, cudaStream_t st) {
+    nvtxRangePushA(kernel_class_name(cls));
     if (!(S->timing_mask & (1u << cls))) return;
     if (S->used == S->pool.size()) {
         sph_solver::Ev e;
@@ -433,6 +445,7 @@ inline void tbeg(sph_solver* S, int cls, cudaStream_t st) {
     cudaEventRecord(S->pool[S->used].a, st);
 }
 inline void tend(sph_solver* S, int cls, cudaStream_t st) {
+    nvtxRangePop();
     if (!(S->timing_mask & (1u << cls))) return;
     cudaEventRecord(S->pool[S->used].b, st);
     S->used++;
