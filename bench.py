@@ -29,6 +29,10 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "particle-steps/s (plain delta-SPH step)"
+REGIONS_METRIC = ("ghost updates/s (mirror-outlet ghosts: construction, neighbor search and consistent "
+                  "interpolation of density and velocity)")
+# lattice of the host sample of the mirror-outlet workload (reference arm, CPU baseline)
+REGIONS_SAMPLE_NX = 128
 # dram__bytes_read + dram__bytes_write of one launch per fluid particle, from ncu captures of
 # the dam break at dx = 1/512 (524,288 fluid particles): pass A is the mean of the four
 # working launches of two steps under Verlet reuse (19.05 + 78.72, 78.89 + 18.56,
@@ -208,10 +212,6 @@ def run_reference(args):
     if WORKLOADS[args.workload]["scene"] == "learned":
         print(json.dumps({"impl": "reference", "unavailable": "the reference has no learned model"}))
         return
-    if WORKLOADS[args.workload]["scene"] == "regions":
-        print(json.dumps({"impl": "reference", "unavailable": "the reference's region functions are torch code "
-                          "that is not installed on this machine; run_regions times the oracle port instead"}))
-        return
     import multiprocessing as mp
     from oracle import sph_oracle as O
     O.build_oracle()  # once, before the workers load it
@@ -237,6 +237,17 @@ def run_reference(args):
     t_end = max(r[2] for r in res)
     dt = t_end - t_start
     v = nproc * n * steps / dt
+    if sc == "regions":
+        print(json.dumps({
+            "impl": "reference", "metric": REGIONS_METRIC, "value": v, "unit": "ghost-updates/s",
+            "n_gpus": args.gpus, "steps": steps, "warmup": warm, "ms_per_step": 1e3 * dt / steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": args.workload,
+                       "sample": f"mirror outlet on a {REGIONS_SAMPLE_NX}^2 block, {n} ghosts, one copy per host core"},
+            "cpu_baseline": {"value": v, "unit": "ghost-updates/s", "cores": nproc, "kind": "port",
+                             "sample": f"{nproc} processes x {n} ghosts x {steps} steps"},
+            "e2e": {"value": v, "unit": "ghost-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
+        return
     line = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": "particle-steps/s", "n_gpus": args.gpus,
         "steps": steps, "warmup": warm, "ms_per_step": 1e3 * dt / steps, "higher_is_better": True,
@@ -269,12 +280,79 @@ def _reference_sample(workload):
     return make_scene(workload)
 
 
+def _regions_block(nx, mirror_x):
+    """The mirror-outlet scene of run_regions on an nx x nx lattice (numpy): the lower unit
+    square of the dam break's fluid, random velocities, no walls; the region is x > mirror_x."""
+    from diffsph_gb300 import scenes
+    dx = 1.0 / nx
+    cfg, st = scenes.dam_break(dx=dx)
+    fl = st["fluid"]
+    keep = fl["positions"][:, 1] < 1.0
+    fl = {k: v[keep].copy() for k, v in fl.items()}
+    rng = np.random.default_rng(3)
+    fl["velocities"] = rng.uniform(-1, 1, fl["velocities"].shape).astype(np.float32)
+    cfg["boundary"]["active"] = False
+    cfg["particle"]["volume"] = dx * dx
+    return fl, cfg
+
+
+def regions_oracle_step(fl, cfg, mx):
+    """One mirror-outlet update with the oracle on the host, the same steps as run_regions'
+    GPU step (deltaPlus.py:188-235 with inletOutlet.py:67-147 and sphOps.py:313-341). The
+    fluid inside the region x > mx gets ghosts mirrored across x = mx: the distance is
+    mx - x, its gradient a central difference over 0.01 h (weights -1/2, 0, 1/2),
+    normalised. The ghosts' neighbors are found among the fluid. The consistent
+    interpolation of the density, then of both velocity components, is written back where a
+    ghost has at least 10 neighbors. Returns the ghost count."""
+    from oracle import sph_oracle as O
+    H = float(cfg["particle"]["support"])
+    x = fl["positions"]
+    inside = np.nonzero(mx - x[:, 0] < 0)[0]
+    p = x[inside]
+    dist = mx - p[:, 0]
+    # fp32 throughout, in the order of the GPU path's host-side gradient
+    step = H * 0.01
+    wts = np.array([-0.5, 0.0, 0.5], np.float32)
+    grad = np.zeros_like(p)
+    for a in range(2):
+        off = np.zeros((3, 2), np.float32)
+        off[:, a] = wts
+        probe = p[:, None, :] + off[None] * np.float32(step)
+        grad[:, a] = np.sum(wts * (mx - probe[..., 0]), axis=-1) / np.float32(step)
+    grad = grad / (np.linalg.norm(grad, axis=1, keepdims=True) + np.float32(1e-7))
+    ghost = {"positions": (p - 2 * dist[:, None] * grad).astype(np.float32),
+             "supports": np.full(len(p), H, np.float32)}
+    nb = O.neighbor_search(ghost, fl, cfg)
+    ok = nb["numNeighbors"] >= 10
+    shift = dist[:, None] * grad * 2
+    for key, col in (("densities", None), ("velocities", 0), ("velocities", 1)):
+        q = fl[key] if col is None else fl[key][:, col]
+        sol = O.liuliu_consistent(ghost, fl, nb, q)[0]
+        val = np.where(ok, sol[:, 0] + np.einsum("nd,nd->n", shift, sol[:, 1:]), q[inside])
+        if col is None:
+            fl[key][inside] = val
+        else:
+            fl[key][inside, col] = val
+    return len(p)
+
+
 def _reference_worker(workload, steps, warm, barrier, queue):
     """One oracle process of the reference arm (spawned; no GPU use)."""
     from oracle import sph_oracle as O
     # (wall ghosts whose moment system is singular get density 0, as in the reference; the
     # shift's wall-wall pairs then divide by zero in rows that are discarded)
     np.seterr(divide="ignore", invalid="ignore")
+    if WORKLOADS[workload]["scene"] == "regions":
+        fl, cfg = _regions_block(REGIONS_SAMPLE_NX, WORKLOADS[workload]["mirror_x"])
+        for _ in range(warm):
+            regions_oracle_step(fl, cfg, WORKLOADS[workload]["mirror_x"])
+        barrier.wait()
+        t0 = time.monotonic()
+        for _ in range(steps):
+            ng = regions_oracle_step(fl, cfg, WORKLOADS[workload]["mirror_x"])
+        t1 = time.monotonic()
+        queue.put((ng if steps else 0, t0, t1))
+        return
     cfg, st = _reference_sample(workload)
     n = st["fluid"]["positions"].shape[0]
     s = copy.deepcopy(st)
@@ -612,25 +690,17 @@ def run_regions(args):
     buildOutletGhostParticles (region distance function, mirrored ghosts, GPU neighbor search)
     and LiuLiuConsistent (sm_103a kernel) for the density and both velocity components, then the
     fluid update. Unit: ghost updates per second (one ghost, three quantities)."""
-    import numpy as np
     import torch
     import __graft_entry__ as ge
-    from diffsph_gb300 import regions, scenes
+    from diffsph_gb300 import regions
 
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
     ge.build()
     w = WORKLOADS[args.workload]
-    dx = 1.0 / w["nx"]
-    cfg, st = scenes.dam_break(dx=dx)
-    fl = st["fluid"]
-    keep = fl["positions"][:, 1] < 1.0
-    fl = {k: torch.from_numpy(v[keep].copy()).cuda() for k, v in fl.items()}
-    fl["numParticles"] = fl["positions"].shape[0]
-    rng = np.random.default_rng(3)
-    fl["velocities"] = torch.from_numpy(rng.uniform(-1, 1, tuple(fl["velocities"].shape)).astype(np.float32)).cuda()
-    cfg["boundary"]["active"] = False
-    cfg["particle"]["volume"] = dx * dx
     mx = w["mirror_x"]
+    fl_np, cfg = _regions_block(w["nx"], mx)
+    fl = {k: torch.from_numpy(v).cuda() for k, v in fl_np.items()}
+    fl["numParticles"] = fl["positions"].shape[0]
     region = {"type": "mirror", "sdf": lambda p: mx - p[:, 0]}
     state = {"fluid": fl}
 
@@ -669,21 +739,17 @@ def run_regions(args):
         k1.record(stream)
         torch.cuda.synchronize()
         kernel_ms = k0.elapsed_time(k1) / 10
-    # the oracle's consistent interpolation on the host, on a 1/64 sample of the ghosts
-    from oracle import sph_oracle as O
     nb = g["neighborhood"]
-    rows = max(ng // 64, 1)
-    sel = (nb["indices"][0] < rows).cpu().numpy()
-    nb_h = {"indices": (nb["indices"][0].cpu().numpy()[sel], nb["indices"][1].cpu().numpy()[sel])}
-    for k in ("distances", "vectors", "supports", "kernels", "gradients"):
-        nb_h[k] = nb[k].cpu().numpy()[sel]
-    fl_h = {k: fl[k].cpu().numpy() for k in ("masses", "densities")}
-    t0 = time.perf_counter()
-    O.liuliu_consistent({"positions": np.zeros((rows, 2), np.float32)}, fl_h, nb_h, fl_h["densities"])
+    # the same step with the oracle on one host core, on the 128^2 sample of the block
+    fl_h, cfg_h = _regions_block(REGIONS_SAMPLE_NX, mx)
+    regions_oracle_step(fl_h, cfg_h, mx)
+    reps, ng_h, t0 = 0, 0, time.perf_counter()
+    while reps < 3 or time.perf_counter() - t0 < 2.0:
+        ng_h = regions_oracle_step(fl_h, cfg_h, mx)
+        reps += 1
     t_cpu = time.perf_counter() - t0
     print(json.dumps({
-        "metric": "ghost updates/s (mirror-outlet ghosts: construction, neighbor search and consistent "
-                  "interpolation of density and velocity)", "value": ng * args.steps / (ms / 1e3),
+        "metric": REGIONS_METRIC, "value": ng * args.steps / (ms / 1e3),
         "unit": "ghost-updates/s", "n_gpus": 1, "steps": args.steps, "warmup": max(args.warmup, 3),
         "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic",
@@ -691,8 +757,8 @@ def run_regions(args):
                    "ghost_pairs": int(nb["indices"][0].shape[0]), "liuliu_kernel_ms": kernel_ms,
                    "note": "the region's distance function and its gradient run in the caller's Python, "
                            "the gradient on the host as in the reference"},
-        "cpu_baseline": {"value": rows / t_cpu, "unit": "ghost-interpolations/s", "cores": 1, "kind": "port",
-                         "sample": f"oracle consistent interpolation of {rows} ghosts (one quantity)"},
+        "cpu_baseline": {"value": ng_h * reps / t_cpu, "unit": "ghost-updates/s", "cores": 1, "kind": "port",
+                         "sample": f"the oracle's step on the {REGIONS_SAMPLE_NX}^2 block ({ng_h} ghosts) x {reps}"},
         "clocks": clk.summary()}))
 
 

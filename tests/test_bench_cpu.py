@@ -80,10 +80,38 @@ def test_reference_arm_prints_only_on_rank_zero(monkeypatch, capsys):
     assert capsys.readouterr().out == ""
 
 
-@pytest.mark.parametrize("workload", ["learned_fourier_b32", "adjoint_fourier128", "outlet_mirror_1024"])
+@pytest.mark.parametrize("workload", ["learned_fourier_b32", "adjoint_fourier128"])
 def test_reference_arm_without_a_reference_path_says_why(monkeypatch, capsys, workload):
     import json
     monkeypatch.setenv("RANK", "0")
     bench.run_reference(_args(workload=workload))
     line = json.loads(capsys.readouterr().out.strip())
     assert line["impl"] == "reference" and line["unavailable"]
+
+
+def test_reference_arm_outlet_step_matches_the_reference():
+    """The host step that the mirror-outlet workload's reference arm and CPU baseline time
+    (bench.regions_oracle_step) against the reference's own outlet update on the same block
+    (tests/golden/make_outlet_step_golden.py): same ghosts, densities and velocities within
+    1e-6 of their magnitudes (the consistent interpolation's rounding)."""
+    import numpy as np
+    from golden_io import GOLDEN, rel_max
+    z = np.load(os.path.join(GOLDEN, "outlet_step_block32.npz"))
+    fl = {k.split("/")[-1]: z[k].copy() for k in z.files if k.startswith("in/fluid/")}
+    _, cfg = bench._regions_block(32, 0.9)
+    assert bench.regions_oracle_step(fl, cfg, 0.9) == int(z["out/ghosts"])
+    assert rel_max(fl["densities"], z["out/densities"]) < 1e-6
+    assert rel_max(fl["velocities"], z["out/velocities"]) < 1e-6
+    assert not np.array_equal(z["out/densities"], z["in/fluid/densities"])
+
+
+def test_reference_arm_of_the_mirror_outlet(monkeypatch, capsys):
+    """The mirror-outlet workload's reference arm: one oracle process per host core on the
+    128^2 sample, in the workload's own unit."""
+    import json
+    monkeypatch.setenv("RANK", "0")
+    bench.run_reference(_args(workload="outlet_mirror_1024", steps=1, warmup=0))
+    line = json.loads(capsys.readouterr().out.strip().splitlines()[-1])
+    assert line["impl"] == "reference" and line["unit"] == "ghost-updates/s"
+    assert line["value"] > 0 and line["cpu_baseline"]["kind"] == "port"
+    assert line["metric"] == bench.REGIONS_METRIC
