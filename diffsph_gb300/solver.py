@@ -70,6 +70,16 @@ def _uniform(arr, name):
     return float(v[0]) if v.numel() else 0.0
 
 
+def wants_verlet_reuse(cfg, params: _lib.Params) -> bool:
+    """Verlet reuse of the cell sort and skin list, as the reference reuses its neighbor
+    structure while neighborhood.verletScale > 1 (default 1.5, neighborhood.py:505-518,603):
+    on for single non-periodic domains."""
+    dom = params.domain
+    if dom.periodic[0] or dom.periodic[1]:
+        return False
+    return _f(cfg.get("neighborhood", {}).get("verletScale", 1.5)) > 1.0
+
+
 def params_from_config(cfg, mass: float, skin: float = DEFAULT_SKIN, capacity: int | None = None) -> _lib.Params:
     p = _lib.Params()
     p.domain = domain_struct(cfg)
@@ -185,12 +195,8 @@ class Solver:
             self.set_free_surface(threshold=_f(sd.get("BarecascoThreshold", math.pi / 3)),
                                   expansion=int(sd.get("expansionIterations", 2)),
                                   scaling=_f(sh.get("surfaceScaling", 0.1)))
-        # Verlet reuse of the cell sort and skin list, as the reference reuses its neighbor
-        # structure for neighborhood.verletScale > 1 (default 1.5); single non-periodic domains
-        dom = self.params.domain
         self.verlet_reuse = False
-        if not (dom.periodic[0] or dom.periodic[1]) and \
-                _f(config.get("neighborhood", {}).get("verletScale", 1.5)) > 1.0:
+        if wants_verlet_reuse(config, self.params):
             self.set_verlet_reuse(True)
 
     def __del__(self):

@@ -136,3 +136,17 @@ def test_handle_entry_points_reject_null_handles(lib):
     assert lib.sph_solver_graph_step(None, 2, None) == 1
     assert lib.sph_solver_step(None, 1, None) == 1
     assert lib.sph_solver_launches_per_step(None) == -1
+
+
+def test_verlet_reuse_follows_the_reference_verlet_scale():
+    from diffsph_gb300.solver import wants_verlet_reuse
+    cfg, st = scenes.dam_break(dx=1.0 / 32)
+    p = params_from_config(cfg, float(st["fluid"]["masses"][0]))
+    assert wants_verlet_reuse(cfg, p)                  # verletScale 1.5, walls
+    cfg["neighborhood"]["verletScale"] = 1.0
+    assert not wants_verlet_reuse(cfg, p)              # the reference rebuilds every step
+    del cfg["neighborhood"]
+    assert wants_verlet_reuse(cfg, p)                  # the reference's default, 1.5
+    cfg, st = scenes.taylor_green(16)
+    p = params_from_config(cfg, float(st["fluid"]["masses"][0]))
+    assert not wants_verlet_reuse(cfg, p)              # periodic: sorted every step
