@@ -100,3 +100,22 @@ def test_lattice_density_is_the_kernel_lattice_sum(nx):
     rho0 = float(cfg["fluid"]["rho0"])
     assert abs(lattice - 1.0012058) < 1e-7
     assert np.max(np.abs(rho - lattice * rho0)) < 1e-12 * rho0
+
+
+def test_workload_time_steps_are_the_acoustic_limit():
+    """The workloads step at the acoustic limit of computeTimestep (timestep.py:18),
+    dt = CFL h / (c0 kappa) with CFL 0.3, h = 4 dx, kappa = 2: 0.6 dx / c0. For the
+    Taylor-Green vortex c0 = 10 (10 max|u|), dt = 1.875e-3 at 64^2; for the dam break
+    c0 = 10 sqrt(2 g H) with a 2 m column, dt = 3.74e-5 at dx = 1/256 and 9.35e-6 at 1/1024."""
+    import math
+    from diffsph_gb300 import scenes
+    cfg, _ = scenes.taylor_green(64)
+    assert cfg["timestep"]["dt"] == pytest.approx(1.875e-3, rel=1e-12)
+    assert cfg["timestep"]["dt"] == pytest.approx(O.acoustic_timestep(cfg, 0.3), rel=1e-12)
+    c0 = 10 * math.sqrt(2 * 9.81 * 2.0)
+    for dx, dt in ((1 / 256, 3.7415e-5), (1 / 1024, 9.3538e-6)):
+        cfg, _ = scenes.dam_break(dx=dx)
+        assert cfg["fluid"]["cs"] == pytest.approx(c0, rel=1e-12)
+        assert cfg["timestep"]["dt"] == pytest.approx(0.6 * dx / c0, rel=1e-12)
+        assert cfg["timestep"]["dt"] == pytest.approx(dt, rel=1e-4)
+        assert cfg["timestep"]["dt"] == pytest.approx(O.acoustic_timestep(cfg, 0.3), rel=1e-12)
