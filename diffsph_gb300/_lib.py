@@ -44,7 +44,7 @@ class Params(ctypes.Structure):
         ("shift_on", ctypes.c_int32), ("shift_R", ctypes.c_double), ("shift_n", ctypes.c_double),
         ("shift_CFL", ctypes.c_double), ("shift_threshold", ctypes.c_double),
         ("compute_mach", ctypes.c_int32), ("density_update", ctypes.c_int32),
-        ("skin", ctypes.c_double), ("capacity", ctypes.c_int32),
+        ("skin", ctypes.c_double), ("capacity", ctypes.c_int32), ("density_scheme", ctypes.c_int32),
     ]
 
 
@@ -71,6 +71,7 @@ EXPORTS = [
     "sph_neighbor_fill_csr", "sph_solver_ips_workspace_bytes", "sph_solver_set_ips", "sph_solver_ips_result",
     "sph_solver_free_surface_workspace_bytes", "sph_solver_set_free_surface", "sph_solver_free_surface_fields",
     "sph_pressure_switch", "sph_liuliu_consistent", "sph_solver_set_verlet_reuse", "sph_solver_sort_count",
+    "sph_solver_rhs_walls",
 ]
 
 _lib = None
@@ -116,6 +117,7 @@ def load(build_if_missing: bool = False):
         "sph_solver_integrate": ([P, P], ctypes.c_int),
         "sph_solver_shift": ([P, P, P], ctypes.c_int),
         "sph_solver_rhs": ([P, P, P, P, P, P, P, P, P], ctypes.c_int),
+        "sph_solver_rhs_walls": ([P, P, P, P, P, P, P, P, P], ctypes.c_int),
         "sph_solver_download": ([P, P, P, P, P, P], ctypes.c_int),
         "sph_solver_flags": ([P, ctypes.POINTER(ctypes.c_uint32), P], ctypes.c_int),
         "sph_solver_launches_per_step": ([P], ctypes.c_int),

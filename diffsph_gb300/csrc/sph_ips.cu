@@ -237,7 +237,7 @@ __global__ void __launch_bounds__(32 * W)
         };
         const int sk = (!PER && use_skin && active) ? (int)slc[i] : 0;
         if (!PER && use_skin && __all_sync(kFull, sk >= 0) && words[3] == 0u)
-            skin_loop<PER>((int)i, pi, X4, g, P, sl, sk, n, pair_j);
+            skin_loop<PER>((int)i, pi, X4, g, P, sl, sk, pair_j);
         else
             neighbor_loop<PER, LT>(active, (int)i, pi, X4, start, g, P, lst, words, pair_j);
         const float2 b = make_float2(b0, b1);  // zero on wall rows

@@ -304,11 +304,13 @@ __device__ __forceinline__ void pass_a_tile(const Dom& D0, int64_t i, int64_t n,
     bool active = inb && !is_boundary(xi.z);
     float2 pi = make_float2(xi.x, xi.y);
     float rhoi = xi.z;
-    float M00 = 0.f, M01 = 0.f, M10 = 0.f, M11 = 0.f;
+    float M00 = 0.f, M01 = 0.f, M11 = 0.f;
     float gf0 = 0.f, gf1 = 0.f, gb0 = 0.f, gb1 = 0.f;
     int nf = 0, nbnd = 0;
     int nstored = 0;
     bool unstored = false;
+    const float cg20 = -20.0f * P.kc.cg;
+    int16_t* __restrict__ nrow = nl + tile_row(i, kStoreCap);
     auto pair_a = [&](int j) {
         {  // keep the exact list (scan order) for pass B at the same positions
             int d = j - (int)i;
@@ -318,32 +320,33 @@ __device__ __forceinline__ void pass_a_tile(const Dom& D0, int64_t i, int64_t n,
                 else if (d < -h2) d += g.nslots;
             }
             if (nstored < kStoreCap && d >= -32768 && d <= 32767)
-                nl[(int64_t)nstored * n + i] = (int16_t)d;
+                nrow[nstored * 32] = (int16_t)d;
             else
                 unstored = true;
             ++nstored;
         }
-        float4 xj = __ldg(&X4[j]);
+        const float4 xj = __ldg(&X4[j]);
         float x0, x1;
         pair_vec<PER>(pi, make_float2(xj.x, xj.y), P.geo, x0, x1);
-        PairG pg = pair_fast(x0, x1, sq_norm_ref(x0, x1), P.inv_h);
-        float dW = wendland_dw(pg.q, P.kc);
-        float rj = fabsf(xj.z);
-        float w = dW * __fdividef(1.0f, rj);
-        float k0 = pg.xh0 * w, k1 = pg.xh1 * w;
-        float d0 = -pg.r * pg.xh0, d1 = -pg.r * pg.xh1;
-        M00 = fmaf(d0, k0, M00);
-        M01 = fmaf(d0, k1, M01);
-        M10 = fmaf(d1, k0, M10);
-        M11 = fmaf(d1, k1, M11);
-        float drho = rhoi - rj;
+        const PairR pr = pair_r(x0, x1, P.inv_h);
+        const float om = fmaxf(1.0f - pr.q, 0.0f);
+        const float rj = fabsf(xj.z);
+        // gradW / rho_j = x w
+        const float w = wendland_gf(pr, om, cg20) * __fdividef(1.0f, rj);
+        // (-r xhat) (x) (gradW / rho_j) = c x x^T: the matrix is symmetric
+        const float c = -(pr.r * pr.inv) * w;
+        const float t0 = c * x0;
+        M00 = fmaf(t0, x0, M00);
+        M01 = fmaf(t0, x1, M01);
+        M11 = fmaf(c * x1, x1, M11);
+        const float dw = (rhoi - rj) * w;
         if (is_boundary(xj.z)) {
-            gb0 = fmaf(drho, k0, gb0);
-            gb1 = fmaf(drho, k1, gb1);
+            gb0 = fmaf(dw, x0, gb0);
+            gb1 = fmaf(dw, x1, gb1);
             ++nbnd;
         } else {
-            gf0 = fmaf(drho, k0, gf0);
-            gf1 = fmaf(drho, k1, gf1);
+            gf0 = fmaf(dw, x0, gf0);
+            gf1 = fmaf(dw, x1, gf1);
             ++nf;
         }
     };
@@ -357,16 +360,16 @@ __device__ __forceinline__ void pass_a_tile(const Dom& D0, int64_t i, int64_t n,
         // scan order
         int ns = 0;
         bool sbad = false;
+        int16_t* __restrict__ srow = sl + tile_row(i, kSkinCap);
         auto skin_then_exact = [&](int j) {
             const int d = j - (int)i;
             if (ns < kSkinCap && d >= -32768 && d <= 32767)
-                sl[(int64_t)ns * n + i] = (int16_t)d;
+                srow[ns * 32] = (int16_t)d;
             else
                 sbad = true;
             ++ns;
-            const float4 xj = __ldg(&X4[j]);
             float x0, x1;
-            pair_vec<PER>(pi, make_float2(xj.x, xj.y), P.geo, x0, x1);
+            pair_vec<PER>(pi, ldg_xy(X4, j), P.geo, x0, x1);
             if (sq_norm_ref(x0, x1) <= P.T) pair_a(j);
         };
         neighbor_loop<PER, LT, decltype(skin_then_exact)&, true>(active, (int)i, pi, X4, start, g, P, lst, words,
@@ -377,7 +380,7 @@ __device__ __forceinline__ void pass_a_tile(const Dom& D0, int64_t i, int64_t n,
         const int sk = (!PER && skin_mode == 1 && active) ? (int)slc[i] : 0;
         const bool use_skin = !PER && skin_mode == 1 && __all_sync(kFull, sk >= 0) && words[3] == 0u;
         if (use_skin)
-            skin_loop<PER>((int)i, pi, X4, g, P, sl, sk, n, pair_a);
+            skin_list_loop<PER, LT>((int)i, pi, X4, g, P, sl, sk, lst, pair_a);
         else
             neighbor_loop<PER, LT>(active, (int)i, pi, X4, start, g, P, lst, words, pair_a);
     }
@@ -385,11 +388,11 @@ __device__ __forceinline__ void pass_a_tile(const Dom& D0, int64_t i, int64_t n,
     if (!active) return;
     float m = P.m;
     if (nf < 4) {
-        M00 = 1.f; M01 = 0.f; M10 = 0.f; M11 = 1.f;
+        M00 = 1.f; M01 = 0.f; M11 = 1.f;
     } else {
-        M00 *= m; M01 *= m; M10 *= m; M11 *= m;
+        M00 *= m; M01 *= m; M11 *= m;
     }
-    M2 L = pinv2x2_ref(M00, M01, M10, M11);
+    M2 L = pinv2x2_ref(M00, M01, M01, M11);
     float g0 = m * (L.a * gf0 + L.b * gf1 + gb0);
     float g1 = m * (L.c * gf0 + L.d * gf1 + gb1);
     *reinterpret_cast<float2*>(&V4[i].z) = make_float2(g0, g1);
@@ -463,39 +466,42 @@ __device__ __forceinline__ void pass_b_tile(const Dom& D0, int64_t i, int64_t n,
     float2 pi = make_float2(xi.x, xi.y);
     float rhoi = xi.z, pri = xi.w;
     float ac = 0.f, ad = 0.f, ap0 = 0.f, ap1 = 0.f, av0 = 0.f, av1 = 0.f, ab0 = 0.f, ab1 = 0.f;
+    const float cg20 = -20.0f * P.kc.cg;
+    // gradW = gf x_ij with gf = dW/dr / (r + 1e-7) (wendland_gf); xhat = x_ij inv
     auto pair_b = [&](int j) {
-        float4 xj = __ldg(&X4[j]);
-        float4 vj = __ldg(&V4[j]);
+        const float4 xj = __ldg(&X4[j]);
+        const float4 vj = __ldg(&V4[j]);
         float x0, x1;
         pair_vec<PER>(pi, make_float2(xj.x, xj.y), P.geo, x0, x1);
-        PairG pg = pair_fast(x0, x1, sq_norm_ref(x0, x1), P.inv_h);
-        float dW = wendland_dw(pg.q, P.kc);
-        float g0 = pg.xh0 * dW, g1 = pg.xh1 * dW;
-        float rj = fabsf(xj.z);
-        float irj = __fdividef(1.0f, rj);
+        const PairR pr = pair_r(x0, x1, P.inv_h);
+        const float om = fmaxf(1.0f - pr.q, 0.0f);
+        const float gf = wendland_gf(pr, om, cg20);
+        const float rj = fabsf(xj.z);
+        const float irj = __fdividef(1.0f, rj);
+        // (u_j - u_i) . x_ij
+        const float dux = fmaf(vj.y - vi.y, x1, (vj.x - vi.x) * x0);
         // continuity: sum (u_j - u_i).gradW / rho_j          (x -m rho_i below)
-        float dug = (vj.x - vi.x) * g0 + (vj.y - vi.y) * g1;
-        ac = fmaf(dug, irj, ac);
+        ac = fmaf(gf * dux, irj, ac);
         // pressure: sum (p_i + p_j) / rho_j gradW            (x -m / rho_i below)
-        float pp = (pri + xj.w) * irj;
-        ap0 = fmaf(pp, g0, ap0);
-        ap1 = fmaf(pp, g1, ap1);
-        // viscosity: pi_ij = (u_i - u_j).xhat / (r + eps h^2)
-        float vr = (vi.x - vj.x) * pg.xh0 + (vi.y - vj.y) * pg.xh1;
+        const float pp = (pri + xj.w) * irj * gf;
+        ap0 = fmaf(pp, x0, ap0);
+        ap1 = fmaf(pp, x1, ap1);
+        // viscosity: pi_ij = (u_i - u_j).xhat / (r + eps h^2) = -dux inv / (r + eps h^2)
+        const float vr = -dux * pr.inv;
         if (is_boundary(xj.z)) {
-            float piv = __fdividef(vr, pg.r + P.bv_eps);
-            float w = P.bvisc ? __fdividef(piv, rhoi + rj) : piv * irj;
-            ab0 = fmaf(w, g0, ab0);
-            ab1 = fmaf(w, g1, ab1);
+            const float piv = __fdividef(vr, pr.r + P.bv_eps);
+            const float w = (P.bvisc ? __fdividef(piv, rhoi + rj) : piv * irj) * gf;
+            ab0 = fmaf(w, x0, ab0);
+            ab1 = fmaf(w, x1, ab1);
         } else {
-            float piv = __fdividef(vr, pg.r + P.v_eps);
-            float w = piv * irj;
-            av0 = fmaf(w, g0, av0);
-            av1 = fmaf(w, g1, av1);
-            // delta-SPH density diffusion: psi = -2 (rho_j - rho_i)/(r + 1e-6 h) xhat + (gradRho_i + gradRho_j)
-            float rij = __fdividef(2.f * (rj - rhoi), pg.r + P.diff_eps);
-            float psig = -rij * (pg.xh0 * g0 + pg.xh1 * g1) + (vi.z + vj.z) * g0 + (vi.w + vj.w) * g1;
-            ad = fmaf(psig, irj, ad);
+            const float w = __fdividef(vr, pr.r + P.v_eps) * irj * gf;
+            av0 = fmaf(w, x0, av0);
+            av1 = fmaf(w, x1, av1);
+            // delta-SPH density diffusion: psi = -2 (rho_j - rho_i)/(r + 1e-6 h) xhat + (gradRho_i + gradRho_j);
+            // psi . gradW = gf (-2 (rho_j - rho_i)/(r + 1e-6 h) inv sq + (G_i + G_j) . x_ij)
+            const float rij = __fdividef(2.f * (rj - rhoi), pr.r + P.diff_eps);
+            const float gx = fmaf(vi.w + vj.w, x1, (vi.z + vj.z) * x0);
+            ad = fmaf(gf * fmaf(-rij * pr.inv, pr.sq, gx), irj, ad);
         }
     };
     // the exact list pass A stored at these positions (same scan order, so the same sums);
@@ -504,16 +510,16 @@ __device__ __forceinline__ void pass_b_tile(const Dom& D0, int64_t i, int64_t n,
     if (__any_sync(kFull, nst < 0)) {
         neighbor_loop<PER, LT>(active, (int)i, pi, X4, start, g, P, lst, words, pair_b);
     } else {
+        const int16_t* __restrict__ row = nl + tile_row(i, kStoreCap);
         int k = 0;
         for (; k + 4 <= nst; k += 4) {
-            const int d0 = nl[(int64_t)k * n + i], d1 = nl[(int64_t)(k + 1) * n + i];
-            const int d2 = nl[(int64_t)(k + 2) * n + i], d3 = nl[(int64_t)(k + 3) * n + i];
+            const int d0 = row[k * 32], d1 = row[(k + 1) * 32], d2 = row[(k + 2) * 32], d3 = row[(k + 3) * 32];
             pair_b(list_slot<PER>((int)i, d0, g));
             pair_b(list_slot<PER>((int)i, d1, g));
             pair_b(list_slot<PER>((int)i, d2, g));
             pair_b(list_slot<PER>((int)i, d3, g));
         }
-        for (; k < nst; ++k) pair_b(list_slot<PER>((int)i, (int)nl[(int64_t)k * n + i], g));
+        for (; k < nst; ++k) pair_b(list_slot<PER>((int)i, (int)row[k * 32], g));
     }
     if (!inb) return;
     if (!active) {  // boundary rows: static, carried over to the next stage
@@ -634,24 +640,27 @@ __device__ __forceinline__ void shift_tile(const Dom& D0, int64_t i, int64_t n, 
     float2 pi = make_float2(xi.x, xi.y);
     float rhoi = xi.z;
     float s0 = 0.f, s1 = 0.f;
+    const float cg20 = -20.0f * P.kc.cg;
     auto pair_s = [&](int j) {
-        float4 xj = __ldg(&X4[j]);
+        const float4 xj = __ldg(&X4[j]);
         float x0, x1;
         pair_vec<PER>(pi, make_float2(xj.x, xj.y), P.geo, x0, x1);
-        PairG pg = pair_fast(x0, x1, sq_norm_ref(x0, x1), P.inv_h);
-        float W = wendland_w(pg.q, P.kc);
-        float dW = wendland_dw(pg.q, P.kc);
-        float kk = W * P.invW0;
-        float kn = P.shN4 ? (kk * kk) * (kk * kk) : powf(kk, P.shN);
-        float c = (1.f + P.shR * kn) * __fdividef(1.0f, rhoi + fabsf(xj.z));
-        s0 = fmaf(c, pg.xh0 * dW, s0);
-        s1 = fmaf(c, pg.xh1 * dW, s1);
+        const PairR pr = pair_r(x0, x1, P.inv_h);
+        const float om = fmaxf(1.0f - pr.q, 0.0f);
+        const float om2 = om * om;
+        const float W = om2 * om2 * (1.0f + 4.0f * pr.q) * P.kc.cw;
+        const float kk = W * P.invW0;
+        const float kn = P.shN4 ? (kk * kk) * (kk * kk) : powf(kk, P.shN);
+        // (1 + R (W/W0)^n) m_j/(rho_i + rho_j) gradW without m (applied below), gradW = gf x_ij
+        const float c = (1.f + P.shR * kn) * __fdividef(1.0f, rhoi + fabsf(xj.z)) * wendland_gf(pr, om, cg20);
+        s0 = fmaf(c, x0, s0);
+        s1 = fmaf(c, x1, s1);
     };
     // the skin list of the step's first pass A holds every pair of the integrated positions
     // unless a particle moved farther than skin_lim (flag set by the integrator)
     const int sk = (!PER && use_skin && active) ? (int)slc[i] : 0;
     if (!PER && use_skin && __all_sync(kFull, sk >= 0) && words[3] == 0u)
-        skin_loop<PER>((int)i, pi, X4, g, P, sl, sk, n, pair_s);
+        skin_list_loop<PER, LT>((int)i, pi, X4, g, P, sl, sk, lst, pair_s);
     else
         neighbor_loop<PER, LT>(active, (int)i, pi, X4, start, g, P, lst, words, pair_s);
     if (!inb) return;
@@ -706,6 +715,76 @@ __global__ void __launch_bounds__(32 * W) k_shift(const Dom D0, int64_t n, const
     if (BATCH) stage_doms(doms, did, first, first + 32 * W - 1, n, s_dom, s_id);
     shift_tile<PER, BATCH, LT>(D0, first + threadIdx.x, n, X4, V4, start, doms, s_dom, s_id, did, Xr, X4o, V4o,
                                words, maxv, enabled, uid, dx_out, lst, use_skin, sl, slc, sv);
+}
+
+// ------------------------------------------------------------------------------------
+// Summation density (simulation.densityScheme 'summation', deltaPlus.py:193-198):
+//   rho_i = sum_fluid m_j W_ij + sum_walls m_j W_ij   (computeDensity, density.py:6-15 ->
+//   sphDensityInterpolation, sphOps.py:20-29; direction 'all': ftf + btf for the fluid rows)
+// It runs first in every right-hand side, before the mDBC extrapolation that reads the
+// fluid densities. The state is written out of place (X4 -> X4o, walls copied), so no
+// thread reads a density another thread of the launch writes. The wall rows' own
+// summation is not kept: the mDBC extrapolation replaces it (deltaPlus.py:200-202).
+// ------------------------------------------------------------------------------------
+template <bool PER, bool BATCH, typename LT, int W>
+__global__ void __launch_bounds__(32 * W) k_density_sum(const Dom D0, int64_t n, const float4* __restrict__ X4,
+                                                        float4* __restrict__ X4o, const int32_t* __restrict__ start_all,
+                                                        const Dom* __restrict__ doms, const int32_t* __restrict__ did,
+                                                        uint32_t* __restrict__ words, int skin_mode,
+                                                        const int16_t* __restrict__ sl,
+                                                        const int16_t* __restrict__ slc) {
+    extern __shared__ __align__(16) unsigned char s_dyn[];
+    __shared__ Dom s_dom[BATCH ? 2 : 1];
+    __shared__ int s_id[2];
+    LT* lst = reinterpret_cast<LT*>(s_dyn) + (threadIdx.x >> 5) * (kCap * 32);
+    const int64_t first = (int64_t)blockIdx.x * (32 * W);
+    if (BATCH) stage_doms(doms, did, first, first + 32 * W - 1, n, s_dom, s_id);
+    const int64_t i = first + threadIdx.x;
+    const Dom& D = BATCH ? dom_ref(doms, s_dom, s_id, dom_of(did, i, n)) : D0;
+    const Phys& P = D.P;
+    const Grid& g = D.g;
+    const int32_t* __restrict__ start = start_all + D.cell0;
+    const bool inb = i < n;
+    const float4 xi = inb ? X4[i] : make_float4(0.f, 0.f, -1.f, 0.f);
+    const bool active = inb && !is_boundary(xi.z);
+    const float2 pi = make_float2(xi.x, xi.y);
+    float sf = 0.f, sb = 0.f;
+    auto pair_d = [&](int j) {
+        const float4 xj = __ldg(&X4[j]);
+        float x0, x1;
+        pair_vec<PER>(pi, make_float2(xj.x, xj.y), P.geo, x0, x1);
+        const PairG pg = pair_fast(x0, x1, sq_norm_ref(x0, x1), P.inv_h);
+        const float w = P.m * wendland_w(pg.q, P.kc);
+        if (is_boundary(xj.z)) sb += w;
+        else sf += w;
+    };
+    // skin_mode 1 filters the skin list (complete for every lane of the warp, still valid);
+    // 4 does the same when this step kept its sort (words[4] == 0) and scans otherwise; 2 scans
+    const bool try_skin = !PER && (skin_mode == 1 || (skin_mode == 4 && words[4] == 0u));
+    const int sk = (try_skin && active) ? (int)slc[i] : 0;
+    if (!PER && try_skin && __all_sync(kFull, sk >= 0) && words[3] == 0u)
+        skin_list_loop<PER, LT>((int)i, pi, X4, g, P, sl, sk, lst, pair_d);
+    else
+        neighbor_loop<PER, LT>(active, (int)i, pi, X4, start, g, P, lst, words, pair_d);
+    if (!inb) return;
+    float4 o = xi;
+    if (active) {
+        o.z = sf + sb;
+        o.w = eos_p(o.z, P.eos);
+    }
+    X4o[i] = o;
+}
+
+// Caller-given wall densities (sph_solver_rhs_walls): rho_b[b] in the original order of the
+// walls, its EOS pressure; the sign bit of the stored density marks the wall
+__global__ void k_set_walls(int nB, const int32_t* __restrict__ bidx, const int32_t* __restrict__ uid,
+                            float4* __restrict__ X4, Phys P, const float* __restrict__ rho_b) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nB) return;
+    const int s = bidx[k];
+    const float rho = rho_b[uid[s] - P.nF];
+    X4[s].z = -rho;
+    X4[s].w = eos_p(rho, P.eos);
 }
 
 // max |u| over all particles (the Mach number of shifting.py:139-142)
@@ -1279,9 +1358,9 @@ static size_t solver_layout(const sph_params_t* p, const int64_t* nF_d, int nd, 
     int64_t* dom_off = c.take<int64_t>(nd + 1);
     float2* bnormal = c.take<float2>(nB);
     float* bdist = c.take<float>(nB);
-    int16_t* nl = c.take<int16_t>((int64_t)kStoreCap * n);
+    int16_t* nl = c.take<int16_t>(tile_elems(n, kStoreCap));
     int16_t* nlc = c.take<int16_t>(n);
-    int16_t* sl = c.take<int16_t>((int64_t)kSkinCap * n);
+    int16_t* sl = c.take<int16_t>(tile_elems(n, kSkinCap));
     int16_t* slc = c.take<int16_t>(n);
     float* msums = c.take<float>(nB * kMdbcSums);
     if (S) {
@@ -1309,6 +1388,10 @@ static int check_params(const sph_params_t* p, int64_t nF, int64_t nB) {
     if (!p || nF < 1 || nB < 0 || nF + nB >= ((int64_t)1 << 31) - 1) return SPH_ERR_ARGUMENT;
     if (!(p->support > 0) || !(p->dx > 0) || !(p->mass > 0) || !(p->rho0 > 0) || !(p->cs > 0)) return SPH_ERR_ARGUMENT;
     if (!(p->skin >= 1.0) || !(p->kernel_scale > 0)) return SPH_ERR_ARGUMENT;
+    // the summation density replaces the integrated one: the rational density update (an
+    // option of this library, not the reference's observable update) does not apply to it
+    if (p->density_scheme < 0 || p->density_scheme > 1 || (p->density_scheme == 1 && p->density_update != 0))
+        return SPH_ERR_ARGUMENT;
     for (int a = 0; a < 2; ++a)
         if (!(p->domain.max[a] > p->domain.min[a])) return SPH_ERR_ARGUMENT;
     int64_t ncells = 0;
@@ -1397,6 +1480,7 @@ static int check_batch(const sph_params_t* params, const int64_t* n_fluid, int n
     for (int d = 0; d < nd; ++d) {
         int st = check_params(&params[d], n_fluid[d], d == 0 ? nB : 0);
         if (st) return st;
+        if (params[d].density_scheme != params[0].density_scheme) return SPH_ERR_ARGUMENT;
         tot += n_fluid[d];
         int64_t nc = 0;
         dom_grid(&params[d], &nc);
@@ -1583,6 +1667,7 @@ static void allow_lists_k(int b) {
     cudaFuncSetAttribute(k_pass_b<PER, BATCH, 1, LT, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
     cudaFuncSetAttribute(k_pass_b<PER, BATCH, 2, LT, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
     cudaFuncSetAttribute(k_shift<PER, BATCH, LT, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+    cudaFuncSetAttribute(k_density_sum<PER, BATCH, LT, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
 }
 
 template <typename LT, int W>
@@ -1677,29 +1762,73 @@ static void launch_b(sph_solver* S, float4* X4, float4* V4, RhsOut o, float4* X4
     tend(S, KC_PASS_B, st);
 }
 
+template <bool PER, bool BATCH, typename LT, int W>
+static void launch_dsum_k(sph_solver* S, const float4* Xin, float4* Xout, int skin_mode, cudaStream_t st) {
+    unsigned gb = (unsigned)((S->n + 32 * W - 1) / (32 * W));
+    k_density_sum<PER, BATCH, LT, W><<<gb, 32 * W, list_bytes<LT, W>(), st>>>(
+        S->doms_host[0], S->n, Xin, Xout, S->start, S->doms, dids(S), S->words, skin_mode, S->sl, S->slc);
+}
+
+template <typename LT, int W>
+static void launch_dsum_t(sph_solver* S, const float4* Xin, float4* Xout, int skin_mode, cudaStream_t st) {
+    if (S->nd > 1) {
+        if (S->periodic) launch_dsum_k<true, true, LT, W>(S, Xin, Xout, skin_mode, st);
+        else launch_dsum_k<false, true, LT, W>(S, Xin, Xout, skin_mode, st);
+    } else {
+        if (S->periodic) launch_dsum_k<true, false, LT, W>(S, Xin, Xout, skin_mode, st);
+        else launch_dsum_k<false, false, LT, W>(S, Xin, Xout, skin_mode, st);
+    }
+}
+
+// Summation density of the state Xin into Xout (skin_mode as k_density_sum)
+static void launch_dsum(sph_solver* S, const float4* Xin, float4* Xout, cudaStream_t st, int skin_mode) {
+    set_attrs(S);
+    tbeg(S, KC_DENSITY, st);
+#define SPH_CALL_D(LT, W) launch_dsum_t<LT, W>(S, Xin, Xout, skin_mode, st)
+    SPH_SHAPE_DISPATCH(S, SPH_CALL_D)
+#undef SPH_CALL_D
+    tend(S, KC_DENSITY, st);
+}
+
+static bool summation(const sph_solver* S) { return S->prm.density_scheme == 1; }
+
 static int run_stages(sph_solver* S, cudaStream_t st) {
     RhsOut none = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     int rc = rebuild(S, st, true);
     if (rc) return rc;
-    // stage 1 at t^n
-    launch_mdbc(S, S->Xc, nullptr, st);
     // skin list (non-periodic domains: there the stencil scan skips the minimum image on most
     // ranges, which the skin filter cannot, and measured no faster)
     const int skin = S->periodic ? 2 : 0;
+    // stage 1 at t^n. With the summation density the stage reads the state with the summed
+    // densities from the spare buffer Xt (free between the sort and the next step)
+    float4* X1 = S->Xc;
+    if (summation(S)) {
+        launch_dsum(S, S->Xc, S->Xt, st, S->periodic ? 2 : (S->reuse ? 4 : 2));
+        X1 = S->Xt;
+    }
+    launch_mdbc(S, X1, nullptr, st);
     if (S->reuse) {
         // after a sort: scan and keep the skin list; otherwise filter the one kept
-        launch_a(S, S->Xc, S->Vc, none, st, 3);
-        launch_a(S, S->Xc, S->Vc, none, st, 4);
+        launch_a(S, X1, S->Vc, none, st, 3);
+        launch_a(S, X1, S->Vc, none, st, 4);
         if (cudaMemsetAsync(S->words + 4, 0, sizeof(uint32_t), st) != cudaSuccess) return SPH_ERR_CUDA;
     } else {
-        launch_a(S, S->Xc, S->Vc, none, st, skin);
+        launch_a(S, X1, S->Vc, none, st, skin);
     }
-    launch_b<1>(S, S->Xc, S->Vc, none, S->Xh, S->Vh, st);
-    // stage 2 at the half step; the epilogue also reduces max |u'| for the shifting Mach number
-    launch_mdbc(S, S->Xh, nullptr, st);
-    launch_a(S, S->Xh, S->Vh, none, st, skin == 0 ? 1 : 2);
+    launch_b<1>(S, X1, S->Vc, none, S->Xh, S->Vh, st);
+    // stage 2 at the half step; the epilogue also reduces max |u'| for the shifting Mach number.
+    // With the summation density the half-step densities are replaced by the sums at the
+    // half-step positions, which the final update keeps (the reference's state sync,
+    // integration.py:439-513, takes the temporary state's densities)
+    float4* X2 = S->Xh;
+    if (summation(S)) {
+        launch_dsum(S, S->Xh, S->Xt, st, skin == 0 ? 1 : 2);
+        X2 = S->Xt;
+    }
+    launch_mdbc(S, X2, nullptr, st);
+    launch_a(S, X2, S->Vh, none, st, skin == 0 ? 1 : 2);
     if (cudaMemsetAsync(S->maxv, 0, sizeof(uint32_t) * S->nd, st) != cudaSuccess) return SPH_ERR_CUDA;
-    launch_b<2>(S, S->Xh, S->Vh, none, S->Xf, S->Vf, st);
+    launch_b<2>(S, X2, S->Vh, none, S->Xf, S->Vf, st);
     return cudaGetLastError() == cudaSuccess ? SPH_OK : SPH_ERR_CUDA;
 }
 
@@ -1876,7 +2005,7 @@ extern "C" int sph_solver_autotune(sph_solver_t* S, int32_t* shape_out, float* m
 // current state; gradients accumulate (+=) into the caller's arrays (original order).
 // ------------------------------------------------------------------------------------
 static int adjoint_ok(sph_solver* S) {
-    if (!S || S->nd != 1 || S->nB != 0 || S->prm.visc_scheme != 0) return SPH_ERR_ARGUMENT;
+    if (!S || S->nd != 1 || S->nB != 0 || S->prm.visc_scheme != 0 || summation(S)) return SPH_ERR_ARGUMENT;
     return SPH_OK;
 }
 
@@ -1946,17 +2075,43 @@ extern "C" int sph_solver_vjp_shift(sph_solver_t* S, const float* xbar_new, floa
     return cudaGetLastError() == cudaSuccess ? SPH_OK : SPH_ERR_CUDA;
 }
 
-extern "C" int sph_solver_rhs(sph_solver_t* S, float* dudt, float* drhodt, float* grad_rho, float* L, float* pressure,
-                              float* rho_boundary, int32_t* num_neighbors, sph_stream_t stream) {
-    if (!S || !dudt || !drhodt) return SPH_ERR_ARGUMENT;
-    cudaStream_t st = (cudaStream_t)stream;
+// One right-hand side at the current state: the summation density (when configured), the
+// wall densities (mDBC, or the caller's rho_b_in), pass A and pass B with the rates written
+static int rhs_impl(sph_solver* S, const float* rho_b_in, float* dudt, float* drhodt, float* grad_rho, float* L,
+                    float* pressure, float* rho_boundary, int32_t* num_neighbors, cudaStream_t st) {
     int rc = rebuild(S, st);
     if (rc) return rc;
     RhsOut o = {dudt, drhodt, grad_rho, L, pressure, rho_boundary, num_neighbors};
-    launch_mdbc(S, S->Xc, rho_boundary, st);
-    launch_a(S, S->Xc, S->Vc, o, st);
-    launch_b<0>(S, S->Xc, S->Vc, o, nullptr, nullptr, st);
+    float4* X = S->Xc;
+    if (summation(S)) {
+        launch_dsum(S, S->Xc, S->Xt, st, 2);
+        X = S->Xt;
+    }
+    if (rho_b_in) {
+        if (S->nB > 0)
+            k_set_walls<<<blocks_for(S->nB), kBlock, 0, st>>>((int)S->nB, S->bidx, S->uid, X, S->doms_host[0].P,
+                                                              rho_b_in);
+    } else {
+        launch_mdbc(S, X, rho_boundary, st);
+    }
+    launch_a(S, X, S->Vc, o, st);
+    launch_b<0>(S, X, S->Vc, o, nullptr, nullptr, st);
     return cudaGetLastError() == cudaSuccess ? SPH_OK : SPH_ERR_CUDA;
+}
+
+extern "C" int sph_solver_rhs(sph_solver_t* S, float* dudt, float* drhodt, float* grad_rho, float* L, float* pressure,
+                              float* rho_boundary, int32_t* num_neighbors, sph_stream_t stream) {
+    if (!S || !dudt || !drhodt) return SPH_ERR_ARGUMENT;
+    return rhs_impl(S, nullptr, dudt, drhodt, grad_rho, L, pressure, rho_boundary, num_neighbors,
+                    (cudaStream_t)stream);
+}
+
+extern "C" int sph_solver_rhs_walls(sph_solver_t* S, const float* rho_boundary_in, float* dudt, float* drhodt,
+                                    float* grad_rho, float* L, float* pressure, int32_t* num_neighbors,
+                                    sph_stream_t stream) {
+    if (!S || !dudt || !drhodt || (S->nB > 0 && !rho_boundary_in)) return SPH_ERR_ARGUMENT;
+    return rhs_impl(S, rho_boundary_in, dudt, drhodt, grad_rho, L, pressure, nullptr, num_neighbors,
+                    (cudaStream_t)stream);
 }
 
 extern "C" int sph_solver_download(sph_solver_t* S, float* x_fluid, float* u_fluid, float* rho_fluid,
@@ -1985,8 +2140,9 @@ extern "C" int sph_solver_launches_per_step(const sph_solver_t* S) {
     // how many iterations it runs.
     // Verlet reuse launches the displacement check, the copy back of a sort and the first
     // pass A both ways (one returns at once), every step
+    // The summation density adds one launch per right-hand side.
     const int fs = (S->fs_on && S->prm.shift_on) ? 2 + S->fs_expand : 0;
-    return 8 + 2 * ((S->nB > 0 ? 2 : 0) + 2) + 1 + fs + (S->reuse ? 3 : 0);
+    return 8 + 2 * ((S->nB > 0 ? 2 : 0) + 2 + (summation(S) ? 1 : 0)) + 1 + fs + (S->reuse ? 3 : 0);
 }
 
 extern "C" int sph_solver_set_verlet_reuse(sph_solver_t* S, int32_t on) {

@@ -19,16 +19,17 @@ namespace sph {
 // ips_setup / ips_spmv / ips_vector: the implicit shift's neighbor pass (b and its list), its
 // matrix products, and its vector updates (with the final position update); free_surface:
 // the surface detection passes of the shift
+// density_sum: the summation density of simulation.densityScheme 'summation'
 enum KernelClass {
     KC_SORT = 0, KC_GATHER, KC_MDBC, KC_PASS_A, KC_PASS_B, KC_SHIFT, KC_PASS_A_SCAN,
-    KC_IPS_SETUP, KC_IPS_SPMV, KC_IPS_VECTOR, KC_SURFACE, KC_COUNT
+    KC_IPS_SETUP, KC_IPS_SPMV, KC_IPS_VECTOR, KC_SURFACE, KC_DENSITY, KC_COUNT
 };
 
 // The classes' names: sph_solver_kernel_name and the NVTX ranges around their launches
 inline const char* kernel_class_name(int cls) {
     static const char* const names[KC_COUNT] = {"cell_sort", "gather", "mdbc_ghosts", "pass_a_gradient",
                                                  "pass_b_rates", "shift", "pass_a_scan", "ips_setup",
-                                                 "ips_spmv", "ips_vector", "free_surface"};
+                                                 "ips_spmv", "ips_vector", "free_surface", "density_sum"};
     return (cls >= 0 && cls < KC_COUNT) ? names[cls] : nullptr;
 }
 
@@ -266,34 +267,112 @@ __device__ __forceinline__ void neighbor_loop(bool active, int self, float2 pi, 
     if (overflow) atomicOr(&words[0], SPH_FLAG_CAPACITY);
 }
 
+// The stored lists (skin list, exact list) are warp-tile-major: the cap entries of the 32
+// slots of a warp form one block, entry k of every lane contiguous, so a lane walks its row
+// at a fixed 64-byte stride (no index arithmetic per entry) and the warp's k-th loads
+// coalesce. Row of slot i: list + tile_row(i, cap), entry k at [k * 32].
+__host__ __device__ __forceinline__ int64_t tile_row(int64_t i, int cap) {
+    return (i >> 5) * (int64_t)(cap * 32) + (i & 31);
+}
+// elements of a list of cap entries per slot for n slots (rounded up to whole warps)
+inline int64_t tile_elems(int64_t n, int cap) { return ((n + 31) & ~(int64_t)31) * cap; }
+
+// The xy of a stored state entry (an 8-byte load of the float4)
+__device__ __forceinline__ float2 ldg_xy(const float4* __restrict__ X4, int j) {
+    return __ldg(reinterpret_cast<const float2*>(X4) + 2 * (int64_t)j);
+}
+
 // The exact neighbors of the stored skin list (scan order of the first pass A of the step,
 // so the same order a scan at the same cells gives), filtered at the current positions.
 template <bool PER, class F>
 __device__ __forceinline__ void skin_loop(int self, float2 pi, const float4* __restrict__ X4, const Grid& g,
-                                          const Phys& P, const int16_t* __restrict__ sl, int cnt, int64_t n,
-                                          F&& f) {
+                                          const Phys& P, const int16_t* __restrict__ sl, int cnt, F&& f) {
+    const int16_t* __restrict__ row = sl + tile_row(self, kSkinCap);
     int k = 0;
     for (; k + 4 <= cnt; k += 4) {
         int j[4];
-        float4 xj[4];
+        float2 xj[4];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) j[u] = list_slot<PER>(self, (int)sl[(int64_t)(k + u) * n + self], g);
+        for (int u = 0; u < 4; ++u) j[u] = list_slot<PER>(self, (int)row[(k + u) * 32], g);
 #pragma unroll
-        for (int u = 0; u < 4; ++u) xj[u] = __ldg(&X4[j[u]]);
+        for (int u = 0; u < 4; ++u) xj[u] = ldg_xy(X4, j[u]);
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
             float x0, x1;
-            pair_vec<PER>(pi, make_float2(xj[u].x, xj[u].y), P.geo, x0, x1);
+            pair_vec<PER>(pi, xj[u], P.geo, x0, x1);
             if (sq_norm_ref(x0, x1) <= P.T) f(j[u]);
         }
     }
     for (; k < cnt; ++k) {
-        const int j = list_slot<PER>(self, (int)sl[(int64_t)k * n + self], g);
-        const float4 xj = __ldg(&X4[j]);
+        const int j = list_slot<PER>(self, (int)row[k * 32], g);
         float x0, x1;
-        pair_vec<PER>(pi, make_float2(xj.x, xj.y), P.geo, x0, x1);
+        pair_vec<PER>(pi, ldg_xy(X4, j), P.geo, x0, x1);
         if (sq_norm_ref(x0, x1) <= P.T) f(j);
     }
+}
+
+// The same neighbors in two steps, for pair terms that cost more than the test: the filter
+// (list entry, neighbor position, the reference's exact test) fills the warp's shared-memory
+// list lst, then f(j) runs over the accepted entries with every lane busy, in the skin
+// list's order. Every lane of the warp must call it (it votes); lanes with cnt = 0 add no
+// pairs.
+template <bool PER, typename LT, class F>
+__device__ __forceinline__ void skin_list_loop(int self, float2 pi, const float4* __restrict__ X4, const Grid& g,
+                                               const Phys& P, const int16_t* __restrict__ sl, int cnt,
+                                               LT* __restrict__ lst, F&& f) {
+    const int lane = threadIdx.x & 31;
+    const int kmax = (int)__reduce_max_sync(kFull, (unsigned)cnt);
+    const int16_t* __restrict__ row = sl + tile_row(self, kSkinCap);
+    int m = 0;
+    for (int k = 0; k < kmax; k += 4) {
+        int d[4];
+        float2 xj[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) d[u] = (k + u < cnt) ? (int)row[(k + u) * 32] : 0;
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+            if (k + u < cnt) xj[u] = ldg_xy(X4, list_slot<PER>(self, d[u], g));
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            if (k + u < cnt) {
+                float x0, x1;
+                pair_vec<PER>(pi, xj[u], P.geo, x0, x1);
+                if (sq_norm_ref(x0, x1) <= P.T) lst[(m++) * 32 + lane] = (LT)d[u];
+            }
+        }
+        if (__any_sync(kFull, m > kCap - 4)) {
+            const int mc = (int)__reduce_max_sync(kFull, (unsigned)m);
+            for (int q = 0; q < mc; ++q)
+                if (q < m) f(list_slot<PER>(self, (int)lst[q * 32 + lane], g));
+            m = 0;
+        }
+    }
+    const int mc = (int)__reduce_max_sync(kFull, (unsigned)m);
+    for (int q = 0; q < mc; ++q)
+        if (q < m) f(list_slot<PER>(self, (int)lst[q * 32 + lane], g));
+}
+
+// Geometry of a pair that already passed the exact test: r, q = r / h and the reference's
+// unit-vector factor inv = 1 / (r + 1e-7) (tolerance-checked sums: fast reciprocal square
+// root and reciprocal). 1e-30 enters the squared norm so that the self pair (sq = 0) gives
+// r = 0 rather than 0 * inf; it changes no realistic sq.
+struct PairR {
+    float sq, r, q, inv;
+};
+
+__device__ __forceinline__ PairR pair_r(float x0, float x1, float inv_h) {
+    PairR p;
+    p.sq = fmaf(x1, x1, fmaf(x0, x0, 1e-30f));
+    p.r = p.sq * rsqrtf(p.sq);
+    p.q = p.r * inv_h;
+    p.inv = __fdividef(1.0f, p.r + 1e-7f);
+    return p;
+}
+
+// The Wendland C2 gradient as gradW = x_ij * wendland_gf(...): with om = (1 - q)_+,
+// dW/dr = -20 q om^3 C_d/h^3 and xhat = x_ij inv, so the factor is q om^3 (-20 C_d/h^3) inv.
+__device__ __forceinline__ float wendland_gf(const PairR& p, float om, float cg20) {
+    return (p.q * (om * om * om)) * cg20 * p.inv;
 }
 
 // Free-surface fields of the shift (solveShifting with shifting.freeSurface), per slot;

@@ -99,7 +99,7 @@ __global__ void __launch_bounds__(32 * W)
         M11 = fmaf(d1, k1, M11);
     };
     if (skin)
-        skin_loop<PER>((int)i, pi, X4, g, P, sl, sk, n, pair_m);
+        skin_loop<PER>((int)i, pi, X4, g, P, sl, sk, pair_m);
     else
         neighbor_loop<PER, LT>(inb, (int)i, pi, X4, start, g, P, lst, words, pair_m);
     if (inb) fnlc[i] = unstored ? (int16_t)-1 : (int16_t)nst;

@@ -15,6 +15,10 @@ import torch
 from . import _lib
 
 VISC_SCHEMES = {"deltaSPH_viscid": 0, "deltaSPH_inviscid": 1}
+# simulation.densityScheme (parameters.py:24, deltaPlus.py:193-198)
+DENSITY_SCHEMES = {"continuity": 0, "summation": 1}
+# kernel.name (parameters.py:37): the kernels evaluate the Wendland C2 kernel only
+KERNELS = ("Wendland2",)
 DEFAULT_SKIN = 1.15
 
 
@@ -93,6 +97,13 @@ def params_from_config(cfg, mass: float, skin: float = DEFAULT_SKIN, capacity: i
         raise ValueError(f"EOS {eos.get('type')} is not implemented by the fused solver (stiffTait is)")
     p.gamma = _f(eos.get("polytropicExponent", 7.0))
     p.kernel_scale = _f(cfg["kernel"]["kernelScale"])
+    kname = cfg["kernel"].get("name", "Wendland2")
+    if kname not in KERNELS:
+        raise ValueError(f"kernel {kname} is not implemented by the fused solver (Wendland2 is)")
+    ds = cfg.get("simulation", {}).get("densityScheme", "continuity")
+    if ds not in DENSITY_SCHEMES:
+        raise ValueError(f"density scheme {ds} is not implemented (continuity, summation are)")
+    p.density_scheme = DENSITY_SCHEMES[ds]
     diff = cfg["diffusion"]
     if diff.get("densityScheme", "deltaSPH") != "deltaSPH":
         raise ValueError("only the deltaSPH density diffusion scheme is implemented")
@@ -139,6 +150,8 @@ def params_from_config(cfg, mass: float, skin: float = DEFAULT_SKIN, capacity: i
     p.shift_CFL, p.shift_threshold = _f(sh.get("CFL", 1.5)), _f(sh.get("threshold", 0.5))
     p.compute_mach = int(bool(sh.get("computeMach", True)))
     p.density_update = 0 if cfg.get("integration", {}).get("densityUpdate", "reference") == "reference" else 1
+    if p.density_scheme == 1 and p.density_update != 0:
+        raise ValueError("the summation density replaces the integrated one: densityUpdate must be 'reference'")
     p.skin = skin
     p.capacity = capacity or default_capacity(skin, p.support, p.dx)
     return p
@@ -300,11 +313,23 @@ class Solver:
                    self.lib.sph_solver_ips_result(self.handle, ctypes.byref(it), ctypes.byref(code), _stream()))
         return int(it.value), int(code.value)
 
-    def rhs(self):
+    def rhs(self, boundary_densities=None):
+        """One right-hand side at the current state. ``boundary_densities`` (walls, original
+        order) replaces the mDBC extrapolation when given (sph_solver_rhs_walls)."""
         o = {"dudt": torch.empty(self.nF, 2, device="cuda"), "drhodt": torch.empty(self.nF, device="cuda"),
              "gradRho^L": torch.empty(self.nF, 2, device="cuda"), "L": torch.empty(self.nF, 2, 2, device="cuda"),
              "pressures": torch.empty(self.nF, device="cuda"),
              "numNeighbors": torch.empty(self.nF, 2, dtype=torch.int32, device="cuda")}
+        if boundary_densities is not None:
+            rb = _dev(boundary_densities) if self.nB else None
+            if rb is not None and rb.numel() != self.nB:
+                raise ValueError("one density per wall particle")
+            _lib.check("sph_solver_rhs_walls", self.lib.sph_solver_rhs_walls(
+                self.handle, _ptr(rb), _ptr(o["dudt"]), _ptr(o["drhodt"]), _ptr(o["gradRho^L"]), _ptr(o["L"]),
+                _ptr(o["pressures"]), _ptr(o["numNeighbors"]), _stream()))
+            if self.nB:
+                o["boundary_densities"] = rb
+            return o
         rb = torch.empty(self.nB, device="cuda") if self.nB else None
         _lib.check("sph_solver_rhs", self.lib.sph_solver_rhs(
             self.handle, _ptr(o["dudt"]), _ptr(o["drhodt"]), _ptr(o["gradRho^L"]), _ptr(o["L"]), _ptr(o["pressures"]),

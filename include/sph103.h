@@ -71,6 +71,11 @@ typedef struct sph_params {
     double skin;             /* cell margin factor (>= 1): the displacement since the last sort
                                 that the cells still cover is (skin - 1) h, less the shift clamp */
     int32_t capacity;        /* candidate slots per particle */
+    int32_t density_scheme;  /* simulation.densityScheme: 0 'continuity' (the density is
+                                integrated), 1 'summation' (deltaPlus.py:193-198: every
+                                right-hand side first sets the fluid densities to
+                                sum_j m_j W_ij over fluid and wall neighbors; needs
+                                density_update 0) */
 } sph_params_t;
 
 /* ------------------------------------------------------------------------------------
@@ -186,6 +191,15 @@ int sph_solver_shift(sph_solver_t* s, float* dx, sph_stream_t stream);
  * of fluid and of boundary neighbors (self included) of every fluid particle nn[nF][2]. */
 int sph_solver_rhs(sph_solver_t* s, float* dudt, float* drhodt, float* grad_rho, float* L,
                    float* pressure, float* rho_boundary, int32_t* num_neighbors, sph_stream_t stream);
+
+/* sph_solver_rhs with the wall densities rho_boundary_in[nB] (original order) given by the
+ * caller in place of the mDBC extrapolation: the rest of simulationStep (deltaPlus.py:240-422)
+ * after its mDBCDensity call (deltaPlus.py:200-202), e.g. for a caller that keeps the
+ * reference's own wall model. The walls' pressures are the EOS of the given densities.
+ * Outputs as sph_solver_rhs. */
+int sph_solver_rhs_walls(sph_solver_t* s, const float* rho_boundary_in, float* dudt, float* drhodt,
+                         float* grad_rho, float* L, float* pressure, int32_t* num_neighbors,
+                         sph_stream_t stream);
 
 /* ------------------------------------------------------------------------------------
  * Adjoint (vector-Jacobian products) of the step's operators at the current state, for a

@@ -474,13 +474,15 @@ def simulation_step(state, config):
     if bnd:
         bd = state["boundary"]
         state["boundaryToFluidNeighborhood"] = neighbor_search(fl, bd, config)
+    # summation density (deltaPlus.py:193-198, direction 'all': ftf + btf for the fluid rows),
+    # before the mDBC extrapolation, which reads the fluid densities
+    if config.get("simulation", {}).get("densityScheme", "continuity") == "summation":
+        ftf = compute_density(fl, fl, fl["neighborhood"], config)
+        fl["densities"] = ftf + compute_density(fl, bd, state["boundaryToFluidNeighborhood"], config) if bnd else ftf
+    if bnd:
         # mDBC boundary density (deltaPlus.py:200-202)
         bd["densities"], shep, gnb = mdbc_density(bd, fl, config)
         state["boundaryGhost"] = {"densities": shep, "neighborhood": gnb}
-    if config.get("simulation", {}).get("densityScheme", "continuity") == "summation":
-        fl["densities"] = compute_density(fl, fl, fl["neighborhood"], config)
-        if bnd:
-            fl["densities"] = fl["densities"] + compute_density(fl, bd, state["boundaryToFluidNeighborhood"], config)
     nbf = fl["neighborhood"]
     # normalisation matrices (deltaPlus.py:240-252), direction 'fluidwBoundary'
     M = compute_covariance(fl, fl, nbf, config)

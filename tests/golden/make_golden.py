@@ -55,6 +55,7 @@ def reference_config(R, cfg):
         "gravity": {"active": cfg["gravity"]["active"]},
         "boundary": {"active": cfg["boundary"]["active"]},
         "export": {"active": False},
+        "simulation": {"densityScheme": cfg.get("simulation", {}).get("densityScheme", "continuity")},
     }
     if raw["particle"]["dx"] > 0:
         raw["particle"]["dx"] = float(cfg["particle"]["dx"])
@@ -76,7 +77,7 @@ def npy(t):
     return t.detach().cpu().numpy() if isinstance(t, torch.Tensor) else np.asarray(t)
 
 
-def run_case(R, name, cfg, st):
+def run_case(R, name, cfg, st, store_pairs=True):
     rc = reference_config(R, cfg)
     derived = {
         "support": float(rc["particle"]["support"]), "dx": float(rc["particle"]["dx"]),
@@ -94,9 +95,11 @@ def run_case(R, name, cfg, st):
     state = {p: to_torch_state(v) for p, v in st.items()}
     # 1) fluid-fluid neighbor search
     _, nb = R.neighborhood.neighborSearch(state["fluid"], state["fluid"], rc, True, None, None, False)
-    for k in ("distances", "vectors", "supports", "kernels", "gradients", "numNeighbors", "neighborOffsets"):
-        out[f"nb/{k}"] = npy(nb[k])
-    out["nb/i"], out["nb/j"] = npy(nb["indices"][0]), npy(nb["indices"][1])
+    out["nb/numNeighbors"] = npy(nb["numNeighbors"])
+    if store_pairs:
+        for k in ("distances", "vectors", "supports", "kernels", "gradients", "neighborOffsets"):
+            out[f"nb/{k}"] = npy(nb[k])
+        out["nb/i"], out["nb/j"] = npy(nb["indices"][0]), npy(nb["indices"][1])
 
     # 2) one right-hand-side evaluation with its intermediates
     s1 = copy.deepcopy(state)
@@ -105,13 +108,16 @@ def run_case(R, name, cfg, st):
     for k in ("covarianceMatrix", "L", "gradRho^L", "densityDiffusion", "velocityDiffusion",
               "momentumEquation", "pressures", "pressureAccel", "gravityAccel"):
         out[f"rhs/{k}"] = npy(s1["fluid"][k])
+    out["rhs/densities"] = npy(s1["fluid"]["densities"])
     if "boundary" in s1:
         out["rhs/boundary_densities"] = npy(s1["boundary"]["densities"])
         out["rhs/ghost_shepard"] = npy(s1["boundaryGhost"]["densities"])
         out["rhs/ghost_numNeighbors"] = npy(s1["boundaryGhost"]["numNeighbors"])
         out["rhs/ghost_positions"] = npy(s1["boundaryGhost"]["positions"])
         btf = s1["boundaryToFluidNeighborhood"]
-        out["rhs/btf_i"], out["rhs/btf_j"] = npy(btf["indices"][0]), npy(btf["indices"][1])
+        out["rhs/btf_numNeighbors"] = npy(btf["numNeighbors"])
+        if store_pairs:
+            out["rhs/btf_i"], out["rhs/btf_j"] = npy(btf["indices"][0]), npy(btf["indices"][1])
 
     # 3) one full time step: integrate (symplectic Euler) + delta+ shifting
     s2 = copy.deepcopy(state)
@@ -130,11 +136,22 @@ def run_case(R, name, cfg, st):
     out["step/positions"] = npy(perennial["fluid"]["positions"])
     path = os.path.join(HERE, f"{name}.npz")
     np.savez_compressed(path, **out)
-    print(f"{name}: fluid {st['fluid']['positions'].shape[0]}, pairs {out['nb/i'].shape[0]} -> {path}")
+    print(f"{name}: fluid {st['fluid']['positions'].shape[0]}, pairs {int(out['nb/numNeighbors'].sum())} -> {path}")
 
 
-def main():
+def summation(cfg_st):
+    """The same scene with simulation.densityScheme 'summation' (deltaPlus.py:193-198)."""
+    cfg, st = cfg_st
+    cfg = copy.deepcopy(cfg)
+    cfg.setdefault("simulation", {})["densityScheme"] = "summation"
+    return cfg, st
+
+
+def main(only=None):
     R = load_reference()
+    if only == "extra":
+        extra(R)
+        return
     # lattice TGV (many pairs exactly at r = H)
     cfg, st = scenes.taylor_green(16)
     run_case(R, "tgv16_lattice", cfg, st)
@@ -152,7 +169,19 @@ def main():
     # dam break with mDBC walls (coarse: dx = 1/16)
     cfg, st = scenes.dam_break(dx=1.0 / 16)
     run_case(R, "dambreak16", cfg, st)
+    extra(R)
+
+
+def extra(R):
+    # summation density: a jittered periodic flow and the coarse dam break
+    cfg, st = summation(scenes.taylor_green(24, jitter=0.1, seed=7))
+    run_case(R, "tgv24_summation", cfg, st, store_pairs=False)
+    cfg, st = summation(scenes.dam_break(dx=1.0 / 16))
+    run_case(R, "dambreak16_summation", cfg, st, store_pairs=False)
+    # the dam break at dx = 1/32 (outputs only: its pair list would be several MB)
+    cfg, st = scenes.dam_break(dx=1.0 / 32)
+    run_case(R, "dambreak32", cfg, st, store_pairs=False)
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1] if len(sys.argv) > 1 else None)

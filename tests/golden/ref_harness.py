@@ -31,7 +31,10 @@ import types
 import numpy as np
 import torch
 
-REF_SRC = os.environ.get("DIFFSPH_REF_SRC", "/root/reference/src")
+# The reference's ``src`` directory (the one holding the ``diffSPH`` package). The fixture
+# generators take it from this variable, e.g.
+#     DIFFSPH_REF_SRC=<reference checkout>/src python tests/golden/make_golden.py
+REF_SRC = os.environ.get("DIFFSPH_REF_SRC")
 
 
 class _Stub(types.ModuleType):
@@ -145,8 +148,14 @@ def load_reference():
     global _LOADED
     if _LOADED is not None:
         return _LOADED
+    if not REF_SRC or not os.path.isdir(os.path.join(REF_SRC, "diffSPH")):
+        raise RuntimeError("set DIFFSPH_REF_SRC to the reference's src directory (the one holding diffSPH/)")
     _install_stubs()
     _install_compact_radius_shim()
+    if not torch.cuda.is_available():
+        # the summation-density branch synchronises the CUDA device (deltaPlus.py:198); on a
+        # host without one that call is a no-op here
+        torch.cuda.synchronize = lambda *a, **k: None
     if REF_SRC not in sys.path:
         sys.path.insert(0, REF_SRC)
     import diffSPH.v2.compiler as comp

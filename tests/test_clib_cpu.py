@@ -3,6 +3,7 @@
 Runs without a GPU: only host-side queries (workspace sizes, parameter validation) are
 called here; compute calls are covered by the gpu-marked tests.
 """
+import copy
 import ctypes
 import os
 import re
@@ -150,3 +151,41 @@ def test_verlet_reuse_follows_the_reference_verlet_scale():
     cfg, st = scenes.taylor_green(16)
     p = params_from_config(cfg, float(st["fluid"]["masses"][0]))
     assert not wants_verlet_reuse(cfg, p)              # periodic: sorted every step
+
+
+def test_params_reject_what_the_kernels_do_not_implement():
+    """The fused solver raises instead of silently stepping another scheme: kernel.name
+    (parameters.py:37) other than Wendland2, simulation.densityScheme (parameters.py:24) other
+    than continuity / summation, and the summation density with the rational density update."""
+    cfg, st = scenes.dam_break(dx=1.0 / 64)
+    m = float(st["fluid"]["masses"][0])
+    assert params_from_config(cfg, m).density_scheme == 0
+    c = copy.deepcopy(cfg)
+    c["kernel"]["name"] = "CubicSpline"
+    with pytest.raises(ValueError):
+        params_from_config(c, m)
+    c = copy.deepcopy(cfg)
+    c["simulation"]["densityScheme"] = "shepard"
+    with pytest.raises(ValueError):
+        params_from_config(c, m)
+    c = copy.deepcopy(cfg)
+    c["simulation"]["densityScheme"] = "summation"
+    assert params_from_config(c, m).density_scheme == 1
+    c.setdefault("integration", {})["densityUpdate"] = "rational"
+    with pytest.raises(ValueError):
+        params_from_config(c, m)
+
+
+def test_solver_rejects_summation_with_rational_update(lib):
+    """The C ABI's own check (sph_solver_workspace_bytes validates the parameters)."""
+    cfg, st = scenes.dam_break(dx=1.0 / 64)
+    p = params_from_config(cfg, float(st["fluid"]["masses"][0]))
+    nbytes = ctypes.c_size_t()
+    nF, nB = st["fluid"]["positions"].shape[0], st["boundary"]["positions"].shape[0]
+    assert lib.sph_solver_workspace_bytes(ctypes.byref(p), nF, nB, ctypes.byref(nbytes)) == 0
+    p.density_scheme = 1
+    assert lib.sph_solver_workspace_bytes(ctypes.byref(p), nF, nB, ctypes.byref(nbytes)) == 0
+    p.density_update = 1
+    assert lib.sph_solver_workspace_bytes(ctypes.byref(p), nF, nB, ctypes.byref(nbytes)) == 1
+    p.density_update, p.density_scheme = 0, 2
+    assert lib.sph_solver_workspace_bytes(ctypes.byref(p), nF, nB, ctypes.byref(nbytes)) == 1

@@ -1,7 +1,7 @@
 """The drop-in installer (diffsph_gb300.dropin) against the reference package itself.
 
-The reference is imported from its source tree through tests/golden/ref_harness.py, which
-exists in the development container only: elsewhere these tests skip. Nothing is called on
+The reference is imported from its source tree through tests/golden/ref_harness.py, from the
+directory the DIFFSPH_REF_SRC environment variable names; without it these tests skip. Nothing is called on
 a GPU: the checks are that every copy of every replaced name points at the drop-in after
 ``install``, that ``uninstall`` restores the reference's functions, and that each drop-in
 keeps the reference function's parameter names.
@@ -20,8 +20,8 @@ GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 def reference():
     sys.path.insert(0, GOLDEN)
     import ref_harness
-    if not os.path.isdir(ref_harness.REF_SRC):
-        pytest.skip("the reference source tree is not on this machine")
+    if not ref_harness.REF_SRC or not os.path.isdir(ref_harness.REF_SRC):
+        pytest.skip("DIFFSPH_REF_SRC does not name the reference's src directory")
     return ref_harness.load_reference()
 
 
