@@ -54,6 +54,20 @@ class FreeSurfaceParams(ctypes.Structure):
                 ("surface_scaling", ctypes.c_double)]
 
 
+class Pairs(ctypes.Structure):
+    """sph_pairs_t: a neighborhood in the reference's format (device pointers)."""
+    _fields_ = [("n_query", ctypes.c_int64), ("offsets", ctypes.c_void_p), ("counts", ctypes.c_void_p),
+                ("pair_j", ctypes.c_void_p), ("distances", ctypes.c_void_p), ("vectors", ctypes.c_void_p),
+                ("supports", ctypes.c_void_p), ("kernels", ctypes.c_void_p), ("gradients", ctypes.c_void_p)]
+
+
+class ViscosityParams(ctypes.Structure):
+    """sph_viscosity_params_t (the deltaSPH viscosity schemes)."""
+    _fields_ = [("scheme", ctypes.c_int32), ("wall_volume", ctypes.c_int32), ("pi_switch", ctypes.c_int32),
+                ("nu", ctypes.c_double), ("alpha", ctypes.c_double), ("eps", ctypes.c_double),
+                ("cs", ctypes.c_double), ("rho0", ctypes.c_double)]
+
+
 class IpsParams(ctypes.Structure):
     """sph_ips_params_t (implicit particle shifting)."""
     _fields_ = [("rtol", ctypes.c_double), ("max_iter", ctypes.c_int32), ("solver_threshold", ctypes.c_double)]
@@ -71,7 +85,8 @@ EXPORTS = [
     "sph_neighbor_fill_csr", "sph_solver_ips_workspace_bytes", "sph_solver_set_ips", "sph_solver_ips_result",
     "sph_solver_free_surface_workspace_bytes", "sph_solver_set_free_surface", "sph_solver_free_surface_fields",
     "sph_pressure_switch", "sph_liuliu_consistent", "sph_solver_set_verlet_reuse", "sph_solver_sort_count",
-    "sph_solver_rhs_walls",
+    "sph_solver_rhs_walls", "sph_operation", "sph_covariance", "sph_density_gradient", "sph_delta_term",
+    "sph_momentum", "sph_pressure_accel", "sph_viscosity", "sph_mdbc_density",
 ]
 
 _lib = None
@@ -141,6 +156,15 @@ def load(build_if_missing: bool = False):
         "sph_solver_free_surface_fields": ([P, P, P, P, P, P], ctypes.c_int),
         "sph_pressure_switch": ([I64, P, P, P, P, P, P, P, P, P, P, P, P], ctypes.c_int),
         "sph_liuliu_consistent": ([I64] + [P] * 15, ctypes.c_int),
+        "sph_operation": ([ctypes.POINTER(Pairs), I32, I32, I32, I32] + [P] * 8, ctypes.c_int),
+        "sph_covariance": ([ctypes.POINTER(Pairs), P, P, P, P], ctypes.c_int),
+        "sph_density_gradient": ([ctypes.POINTER(Pairs), P, P, P, P, P, P], ctypes.c_int),
+        "sph_delta_term": ([ctypes.POINTER(Pairs)] + [P] * 6 + [ctypes.c_double] * 3 + [P, P], ctypes.c_int),
+        "sph_momentum": ([ctypes.POINTER(Pairs)] + [P] * 7, ctypes.c_int),
+        "sph_pressure_accel": ([ctypes.POINTER(Pairs)] + [P] * 7, ctypes.c_int),
+        "sph_viscosity": ([ctypes.POINTER(Pairs)] + [P] * 6 + [ctypes.POINTER(ViscosityParams), P, P], ctypes.c_int),
+        "sph_mdbc_density": ([ctypes.POINTER(Pairs), P, P, P, P, ctypes.c_double, ctypes.c_double, P, P, P],
+                             ctypes.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)

@@ -314,6 +314,119 @@ int sph_liuliu_consistent(int64_t n_query, const int32_t* offsets, const int32_t
                           const float* m_ref, const float* rho_ref, const float* quantity,
                           float* solution, float* M, float* b, sph_stream_t stream);
 
+/* ------------------------------------------------------------------------------------
+ * Pair-sum operators on a neighborhood in the reference's format (what neighborSearch,
+ * src/diffSPH/v2/modules/neighborhood.py:491-593, or sph_neighbor_fill returns), for callers
+ * that keep the reference's own simulationStep. Each query row i sums its pairs
+ * [offsets[i], offsets[i] + counts[i]) in their stored order, with the reference's fp32
+ * operation order per pair, as its scatter_sum (src/diffSPH/v2/math.py:77-93) adds them on
+ * the CPU. Per-pair arrays: pair_j (int64), distances (q = r / h_j), vectors (unit x_ij,
+ * [P][2]), supports (h_j), kernels (W), gradients (grad W, [P][2]); an operator that does
+ * not read one of them accepts NULL there. "a" arrays are per query particle, "b" arrays
+ * per reference particle; vectors are [n][2], 2x2 matrices [n][4] row-major.
+ * ------------------------------------------------------------------------------------ */
+typedef struct sph_pairs {
+    int64_t n_query;
+    const int32_t* offsets;   /* neighborOffsets [n_query] */
+    const int32_t* counts;    /* numNeighbors [n_query] */
+    const int64_t* pair_j;    /* indices[1] [P] */
+    const float* distances;
+    const float* vectors;
+    const float* supports;
+    const float* kernels;
+    const float* gradients;
+} sph_pairs_t;
+
+/* sphOperation / sphOperationStates (src/diffSPH/v2/sphOps.py:243-303) */
+enum sph_operation_kind {
+    SPH_OP_DENSITY = 0,       /* sphDensityInterpolation (:20-29): sum m_j W */
+    SPH_OP_INTERPOLATE = 1,   /* sphInterpolation (:6-18): sum (m_j / rho_j) W q */
+    SPH_OP_GRADIENT = 2,      /* sphGradient (:32-60): sum q (x) (m_j / rho_j) grad W */
+    SPH_OP_DIVERGENCE = 3,    /* sphDivergence (:63-98): sum q . (m_j / rho_j) grad W */
+    SPH_OP_CURL = 4,          /* sphCurl (:139-171), 2D */
+    SPH_OP_LAPLACIAN = 5      /* sphLaplacian (:174-240), every type but 'naive' */
+};
+/* gradientMode (and the laplacian's type): the pair quantity q_j (naive), q_i - q_j
+ * (gradient 'difference'; q_j - q_i for divergence and curl), q_i + q_j (summation), or the
+ * symmetric form rho_i sum m_j (q_i / rho_i^2 + q_j / rho_j^2) grad W; the laplacian types
+ * 'conserving', 'divergenceFree', 'dot' and its default formula (any other value) */
+enum sph_operation_mode {
+    SPH_MODE_NAIVE = 0,
+    SPH_MODE_DIFFERENCE = 1,
+    SPH_MODE_SUMMATION = 2,
+    SPH_MODE_SYMMETRIC = 3,
+    SPH_MODE_CONSERVING = 4,
+    SPH_MODE_DIVERGENCE_FREE = 5,
+    SPH_MODE_DOT = 6
+};
+
+/* One sphOperation over quantities with `components` values per particle (1 scalar, 2
+ * vector, 4 2x2 matrix): per particle as the tuple (q_a, q_b), or per pair (q_pair != NULL,
+ * the reference's non-tuple argument, used as is in every mode). divergence_mode 0 is 'div'
+ * (the last index contracted), 1 'dot' (the first). Output per query row: 1 value (density,
+ * curl, divergence of a vector), components (interpolate, laplacian), 2 components
+ * (gradient: q_c grad W_d at [c][d]), 2 (divergence of a matrix). */
+int sph_operation(const sph_pairs_t* nb, int32_t operation, int32_t mode, int32_t divergence_mode,
+                  int32_t components, const float* m_b, const float* rho_a, const float* rho_b,
+                  const float* q_a, const float* q_b, const float* q_pair, float* out,
+                  sph_stream_t stream);
+
+/* computeCovarianceMatrices (src/diffSPH/v2/modules/normalizationMatrices.py:18-23):
+ * out[n][4] = sum (-(q h) xhat) (x) (m_j / rho_j) grad W. */
+int sph_covariance(const sph_pairs_t* nb, const float* m_b, const float* rho_b, float* out,
+                   sph_stream_t stream);
+
+/* renormalizedDensityGradient (src/diffSPH/v2/modules/densityDiffusion.py:7-26) with L[n][4]
+ * (the normalised kernel gradient L_i grad W), or densityGradient (:28-46) with L == NULL:
+ * out[n][2] = sum (rho_i - rho_j) (m_j / rho_j) grad W. */
+int sph_density_gradient(const sph_pairs_t* nb, const float* m_b, const float* rho_a, const float* rho_b,
+                         const float* L, float* out, sph_stream_t stream);
+
+/* computeDensityDeltaTerm (densityDiffusion.py:49-73), scheme 'deltaSPH': out[n] =
+ * delta h_i / kappa cs sum psi_ij . (m_j / rho_j) grad W with psi_ij = -2 (rho_j - rho_i) /
+ * (r_ij + 1e-6 h) xhat + (gradRho^L_i + gradRho^L_j); h_a are the query supports. */
+int sph_delta_term(const sph_pairs_t* nb, const float* m_b, const float* rho_a, const float* rho_b,
+                   const float* grad_a, const float* grad_b, const float* h_a, double delta, double kappa,
+                   double cs, float* out, sph_stream_t stream);
+
+/* computeMomentumEquation (src/diffSPH/v2/modules/momentumEquation.py:6-39): out[n] =
+ * -sum ((u_j - u_i) m_j) . grad W rho_i / rho_j. */
+int sph_momentum(const sph_pairs_t* nb, const float* m_b, const float* rho_a, const float* rho_b,
+                 const float* u_a, const float* u_b, float* out, sph_stream_t stream);
+
+/* computePressureAccel (src/diffSPH/v2/modules/pressureForce.py:10-12): out[n][2] =
+ * -(sum (p_i + p_j) (m_j / rho_j) grad W) / rho_i. */
+int sph_pressure_accel(const sph_pairs_t* nb, const float* m_b, const float* rho_a, const float* rho_b,
+                       const float* p_a, const float* p_b, float* out, sph_stream_t stream);
+
+/* computeViscosity (src/diffSPH/v2/modules/viscosity.py:222-241) for the deltaSPH schemes
+ * (:123-170 inviscid, :200-218 viscid) and computeViscosity_Boundary
+ * (boundaryViscosity.py:123-173, 199-219; wall_volume = 1 gives the inviscid wall scheme's
+ * m_j / (rho_i + rho_j)). The values are the config section's (diffusion or
+ * boundaryDiffusion). h_a (query supports) is read by the inviscid scheme. */
+typedef struct sph_viscosity_params {
+    int32_t scheme;        /* 0 deltaSPH_viscid, 1 deltaSPH_inviscid */
+    int32_t wall_volume;   /* inviscid wall scheme: V_j = m_j / (rho_i + rho_j) */
+    int32_t pi_switch;     /* pi-switch: only approaching pairs ((u_i - u_j).xhat < 0) */
+    double nu, alpha, eps;
+    double cs, rho0;       /* fluid.cs, fluid.rho0 */
+} sph_viscosity_params_t;
+int sph_viscosity(const sph_pairs_t* nb, const float* m_b, const float* rho_a, const float* rho_b,
+                  const float* u_a, const float* u_b, const float* h_a, const sph_viscosity_params_t* params,
+                  float* out, sph_stream_t stream);
+
+/* mDBCDensity (src/diffSPH/v2/modules/mDBC.py:50-163) on the ghost -> fluid neighborhood
+ * (query = the wall particles' ghosts, x_ghost[n][2]; reference = the fluid): the Shepard
+ * density, the 3x3 moment system solved where a ghost has more than five neighbors and the
+ * first-order extrapolation to the wall particle x_wall[n][2]; the rest density rho0 where a
+ * ghost has none. The sums follow the reference's order; the pseudo-inverse is fp64 with
+ * torch.linalg.pinv's truncation rule (the reference's fp32 solve carries ~1e-4 relative
+ * rounding on the ill-conditioned matrices near free edges). support is particle.support.
+ * Writes rho_out[n] and, when non-NULL, shepard_out[n]. */
+int sph_mdbc_density(const sph_pairs_t* nb, const float* m_f, const float* rho_f, const float* x_wall,
+                     const float* x_ghost, double support, double rho0, float* rho_out, float* shepard_out,
+                     sph_stream_t stream);
+
 /* Writes the current state back in the original order (NULL entries are skipped). */
 int sph_solver_download(sph_solver_t* s, float* x_fluid, float* u_fluid, float* rho_fluid,
                         float* rho_boundary, sph_stream_t stream);

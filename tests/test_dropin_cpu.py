@@ -25,7 +25,10 @@ def reference():
     return ref_harness.load_reference()
 
 
-@pytest.mark.parametrize("mode", ["fused", "regions"])
+MODES = ["fused", "regions", "operators"]
+
+
+@pytest.mark.parametrize("mode", MODES)
 def test_install_replaces_every_copy_and_uninstall_restores(reference, mode):
     from diffsph_gb300 import dropin
     before = {(m, a): getattr(importlib.import_module(m), a) for m, a, _ in dropin.targets(mode)}
@@ -41,7 +44,7 @@ def test_install_replaces_every_copy_and_uninstall_restores(reference, mode):
 
 def test_dropins_keep_the_reference_signatures(reference):
     from diffsph_gb300 import dropin
-    for mode in ("fused", "regions"):
+    for mode in MODES:
         for m, a, new in dropin.targets(mode):
             ref = getattr(importlib.import_module(m), a)
             assert list(inspect.signature(new).parameters) == list(inspect.signature(ref).parameters), (m, a)
@@ -51,3 +54,22 @@ def test_unknown_mode_is_rejected():
     from diffsph_gb300 import dropin
     with pytest.raises(ValueError):
         dropin.targets("unknown")
+
+
+@pytest.mark.parametrize("mode", MODES)
+def test_every_by_name_copy_is_covered(reference, mode):
+    """Every loaded reference module that holds (under the same name) a function the mode
+    replaces is itself a target, so no call site of the step keeps the reference's version;
+    the modules off the step (dropin.LEFT_ALONE, each with its reason) are skipped."""
+    from diffsph_gb300 import dropin
+    tg = dropin.targets(mode)
+    covered = {(m, a) for m, a, _ in tg}
+    originals = {a: getattr(importlib.import_module(m), a) for m, a, _ in tg}
+    missed = []
+    for name, mod in list(sys.modules.items()):
+        if not name.startswith("diffSPH") or mod is None or name in dropin.LEFT_ALONE:
+            continue
+        for a, f in originals.items():
+            if getattr(mod, a, None) is f and (name, a) not in covered:
+                missed.append((name, a))
+    assert not missed, missed
