@@ -64,6 +64,10 @@ WORKLOADS = {
     "learned_fourier_b32": dict(scene="learned", nx_train=128, nx_eval=256, L_eval=4.0, batch=32, k=4, traj=8,
                                 frames=24, iters=3000, rollout=200),
 }
+# the drop-in neighbor search (neighborSearch's reference-format output) on the fluid of the
+# 2.1M-particle dam break, query = reference set
+WORKLOADS["neighbors_dx1024"] = dict(scene="neighbors", dx=1.0 / 1024)
+NEIGHBOR_METRIC = "neighbor pairs/s (exact scatter-mode search, reference-format pair list)"
 LEARNED_METRIC = "particle-steps/s (learned k=4 step, counted in plain-step equivalents)"
 ADJOINT_METRIC = "adjoint particle-steps/s (forward + backward of a checkpointed rollout)"
 
@@ -168,10 +172,19 @@ def algorithmic_bytes(nbar):
 
 
 def cpu_baseline(workload, budget_s=20.0):
-    """The oracle (numpy restatement of the reference step) on a bounded sample."""
+    """The oracle (numpy restatement of the reference step) on a bounded sample of the
+    workload, on every host core (port_parallel); workloads without a dam-break / flow sample
+    run it on one core."""
     from oracle import sph_oracle as O
     from diffsph_gb300 import scenes
     w = WORKLOADS[workload]
+    if w["scene"] in ("dam_break", "fourier"):
+        steps = 8 if w.get("ips") else 12
+        v, nproc, n, dt = port_parallel(workload, steps, 1)
+        return {"value": v, "unit": "particle-steps/s", "cores": nproc, "kind": "port",
+                "sample": f"{nproc} processes x {n} fluid particles x {steps} steps in {dt:.1f} s "
+                          f"({'dam break dx=1/64' if w['scene'] == 'dam_break' else 'the same flow at 64x64'}, "
+                          "same scene and parameters, coarser lattice)"}
     if w["scene"] == "batched":
         cfg, st = scenes.batched_fourier(1, seed=w.get("seed", 0), n_min=4096, n_max=4096)[0]
         sample = "one 64x64 domain of the batch generator"
@@ -212,31 +225,19 @@ def run_reference(args):
     if WORKLOADS[args.workload]["scene"] == "learned":
         print(json.dumps({"impl": "reference", "unavailable": "the reference has no learned model"}))
         return
-    import multiprocessing as mp
-    from oracle import sph_oracle as O
-    O.build_oracle()  # once, before the workers load it
     sc = WORKLOADS[args.workload]["scene"]
-    # one single-threaded oracle process per host core, each on its own copy of the sample;
-    # they start their timed steps together (barrier) and the throughput is the particle-steps
-    # of all of them over the span from the first start to the last end
-    nproc = max(1, min(os.cpu_count() or 1, 64))
-    for var in ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS"):
-        os.environ[var] = "1"
-    ctx = mp.get_context("spawn")
-    barrier = ctx.Barrier(nproc)
-    queue = ctx.Queue()
-    procs = [ctx.Process(target=_reference_worker, args=(args.workload, steps, warm, barrier, queue))
-             for _ in range(nproc)]
-    for p in procs:
-        p.start()
-    res = [queue.get() for _ in procs]
-    for p in procs:
-        p.join()
-    n = res[0][0]
-    t_start = min(r[1] for r in res)
-    t_end = max(r[2] for r in res)
-    dt = t_end - t_start
-    v = nproc * n * steps / dt
+    v, nproc, n, dt = port_parallel(args.workload, steps, warm)
+    if sc == "neighbors":
+        print(json.dumps({
+            "impl": "reference", "metric": NEIGHBOR_METRIC, "value": v, "unit": "pairs/s", "n_gpus": args.gpus,
+            "steps": steps, "warmup": warm, "ms_per_step": 1e3 * dt / steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 (int64 indices)", "data": "synthetic",
+            "config": {"workload": args.workload,
+                       "sample": f"the dam break's fluid at dx = 1/64, {n} pairs, one copy per host core"},
+            "cpu_baseline": {"value": v, "unit": "pairs/s", "cores": nproc, "kind": "port",
+                             "sample": f"{nproc} processes x {n} pairs x {steps} searches"},
+            "e2e": {"value": v, "unit": "pairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
+        return
     if sc == "regions":
         print(json.dumps({
             "impl": "reference", "metric": REGIONS_METRIC, "value": v, "unit": "ghost-updates/s",
@@ -259,6 +260,32 @@ def run_reference(args):
         "e2e": {"value": v, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
+
+
+def port_parallel(workload, steps, warm):
+    """The oracle's port of the step on every host core: one single-threaded process per core
+    (spawned), each on its own copy of the workload's sample; they start their timed steps
+    together (barrier) and the throughput is the units of all of them over the span from the
+    first start to the last end. Returns (units/s, processes, units per step, seconds)."""
+    import multiprocessing as mp
+    from oracle import sph_oracle as O
+    O.build_oracle()  # once, before the workers load it
+    nproc = max(1, min(os.cpu_count() or 1, 64))
+    for var in ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS"):
+        os.environ[var] = "1"
+    ctx = mp.get_context("spawn")
+    barrier = ctx.Barrier(nproc)
+    queue = ctx.Queue()
+    procs = [ctx.Process(target=_reference_worker, args=(workload, steps, warm, barrier, queue))
+             for _ in range(nproc)]
+    for p in procs:
+        p.start()
+    res = [queue.get() for _ in procs]
+    for p in procs:
+        p.join()
+    n = res[0][0]
+    dt = max(r[2] for r in res) - min(r[1] for r in res)
+    return nproc * n * steps / dt, nproc, n, dt
 
 
 def _reference_sample(workload):
@@ -342,6 +369,20 @@ def _reference_worker(workload, steps, warm, barrier, queue):
     # (wall ghosts whose moment system is singular get density 0, as in the reference; the
     # shift's wall-wall pairs then divide by zero in rows that are discarded)
     np.seterr(divide="ignore", invalid="ignore")
+    if WORKLOADS[workload]["scene"] == "neighbors":
+        from diffsph_gb300 import scenes
+        cfg, st = scenes.dam_break(dx=1.0 / 64)
+        fl = st["fluid"]
+        for _ in range(warm):
+            O.neighbor_search(fl, fl, cfg)
+        barrier.wait()
+        t0 = time.monotonic()
+        pairs = 0
+        for _ in range(steps):
+            pairs = int(O.neighbor_search(fl, fl, cfg)["indices"][0].shape[0])
+        t1 = time.monotonic()
+        queue.put((pairs, t0, t1))
+        return
     if WORKLOADS[workload]["scene"] == "regions":
         fl, cfg = _regions_block(REGIONS_SAMPLE_NX, WORKLOADS[workload]["mirror_x"])
         for _ in range(warm):
@@ -762,6 +803,135 @@ def run_regions(args):
         "clocks": clk.summary()}))
 
 
+def neighbor_bytes(nq, nr, pairs):
+    """Algorithmic bytes of one search (fixed definition): the positions and supports read by
+    the sort and the query (8 + 4 per reference particle, twice; 8 per query particle), the
+    per-query counts and offsets written (4 + 8), and the pair list written in the reference's
+    format: i, j (int64), q, h_j, W (fp32), xhat, gradW (2 x fp32) = 44 B per pair."""
+    return 2 * 12 * nr + 8 * nq + 12 * nq + 44 * pairs
+
+
+def run_neighbors(args):
+    """The drop-in search alone (sph_neighbor_count + sph_neighbor_fill, with kernels and
+    gradients): value with every buffer resident on the device; e2e from pinned host
+    positions and supports to the whole pair list back in pinned host memory."""
+    import ctypes
+    import torch
+    import __graft_entry__ as ge
+    from diffsph_gb300 import _lib, scenes
+    from diffsph_gb300.solver import domain_struct
+
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    if int(os.environ.get("RANK", "0")) != 0:
+        return
+    ge.build()
+    lib = _lib.load()
+    cfg, st = scenes.dam_break(dx=WORKLOADS[args.workload]["dx"])
+    fl = st["fluid"]
+    n = fl["positions"].shape[0]
+    x = torch.from_numpy(fl["positions"]).cuda()
+    h = torch.from_numpy(fl["supports"]).cuda()
+    dom = domain_struct(cfg)
+    hmax = float(fl["supports"].max())
+    nbytes = ctypes.c_size_t()
+    _lib.check("sph_neighbor_workspace_bytes",
+               lib.sph_neighbor_workspace_bytes(n, n, ctypes.byref(dom), hmax, ctypes.byref(nbytes)))
+    ws = torch.empty(int(nbytes.value) + 256, dtype=torch.uint8, device="cuda")
+    wsp = ctypes.c_void_p((ws.data_ptr() + 255) & ~255)
+    counts = torch.empty(n, dtype=torch.int32, device="cuda")
+    offsets = torch.empty(n + 1, dtype=torch.int64, device="cuda")
+    stream = torch.cuda.Stream()
+    P = ctypes.c_void_p
+
+    def count(xd, hd, st_):
+        _lib.check("sph_neighbor_count", lib.sph_neighbor_count(
+            P(xd.data_ptr()), n, P(xd.data_ptr()), P(hd.data_ptr()), n, ctypes.byref(dom), hmax, wsp,
+            nbytes.value, P(counts.data_ptr()), P(offsets.data_ptr()), st_))
+
+    with torch.cuda.stream(stream):
+        st_ = ctypes.c_void_p(stream.cuda_stream)
+        count(x, h, st_)
+        torch.cuda.synchronize()
+        npairs = int(offsets[-1].item())
+        out = {"i": torch.empty(npairs, dtype=torch.int64, device="cuda"),
+               "j": torch.empty(npairs, dtype=torch.int64, device="cuda"),
+               "q": torch.empty(npairs, device="cuda"), "xhat": torch.empty(npairs, 2, device="cuda"),
+               "h": torch.empty(npairs, device="cuda"), "W": torch.empty(npairs, device="cuda"),
+               "gradW": torch.empty(npairs, 2, device="cuda")}
+
+        def fill(xd, hd, st_):
+            _lib.check("sph_neighbor_fill", lib.sph_neighbor_fill(
+                P(xd.data_ptr()), n, P(xd.data_ptr()), P(hd.data_ptr()), n, ctypes.byref(dom), hmax, wsp,
+                nbytes.value, P(offsets.data_ptr()), npairs, *[P(out[k].data_ptr()) for k in
+                                                                ("i", "j", "q", "xhat", "h", "W", "gradW")], st_))
+
+        for _ in range(max(args.warmup, 3)):
+            count(x, h, st_)
+            fill(x, h, st_)
+        torch.cuda.synchronize()
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+        with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
+            ev[0].record(stream)
+            for _ in range(args.steps):
+                count(x, h, st_)
+                fill(x, h, st_)
+            ev[1].record(stream)
+            torch.cuda.synchronize()
+        ms = ev[0].elapsed_time(ev[1]) / args.steps
+        # the fill alone (the dominant launch: it writes the pair list)
+        ev[2].record(stream)
+        for _ in range(args.steps):
+            fill(x, h, st_)
+        ev[3].record(stream)
+        torch.cuda.synchronize()
+        fill_ms = ev[2].elapsed_time(ev[3]) / args.steps
+        # end to end: host arrays in, the pair count read back to size the list, the list out
+        xh, hh = torch.from_numpy(fl["positions"]).pin_memory(), torch.from_numpy(fl["supports"]).pin_memory()
+        host = {k: torch.empty(v.shape, dtype=v.dtype).pin_memory() for k, v in out.items()}
+        cnt_h = torch.empty(1, dtype=torch.int64).pin_memory()
+        e_steps = max(min(args.steps, 5), 2)
+        t0 = time.perf_counter()
+        for _ in range(e_steps):
+            xd, hd = xh.to("cuda", non_blocking=True), hh.to("cuda", non_blocking=True)
+            count(xd, hd, st_)
+            cnt_h.copy_(offsets[-1:], non_blocking=True)
+            stream.synchronize()
+            assert int(cnt_h.item()) == npairs
+            fill(xd, hd, st_)
+            for k, v in host.items():
+                v.copy_(out[k], non_blocking=True)
+        stream.synchronize()
+        e2e_s = (time.perf_counter() - t0) / e_steps
+    alg = neighbor_bytes(n, n, npairs)
+    pk, pk_kind = peaks()
+    fill_alg = 44 * npairs + 12 * n
+    line = {
+        "metric": NEIGHBOR_METRIC, "value": npairs / (ms / 1e3), "unit": "pairs/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 (int64 indices)", "data": "synthetic",
+        "config": {"workload": args.workload, "query_particles": n, "reference_particles": n, "pairs": npairs,
+                   "mean_neighbors": round(npairs / n, 3), "kernels": True,
+                   "l2": f"pair list ({44 * npairs / 1e9:.2f} GB) exceeds L2; no flush"},
+        "e2e": {"value": npairs / e2e_s, "unit": "pairs/s", "h2d_bytes_per_step": 12 * n,
+                "d2h_bytes_per_step": 44 * npairs + 8, "steps": e_steps,
+                "note": "host clock around upload, count, pair-count read-back, fill and the list's copy back"},
+        "roofline": {"bound": "hbm", "kernel": "neighbor_fill", "achieved": fill_alg / (fill_ms / 1e3) / 1e9,
+                     "peak": pk, "peak_kind": pk_kind, "unit": "GB/s",
+                     "frac": fill_alg / (fill_ms / 1e3) / 1e9 / pk, "traffic": None,
+                     "alg_bytes_per_launch": fill_alg, "avg_launch_ms": fill_ms,
+                     "search_alg_bytes": alg, "search_achieved_gbs": alg / (ms / 1e3) / 1e9,
+                     "search_frac": alg / (ms / 1e3) / 1e9 / pk},
+        "gpu_launches": None,
+        "clocks": clk.summary(),
+    }
+    if not args.no_cpu_baseline:
+        v, nproc, pairs_h, dt = port_parallel(args.workload, 10, 1)
+        line["cpu_baseline"] = {"value": v, "unit": "pairs/s", "cores": nproc, "kind": "port",
+                                "sample": f"{nproc} processes x the oracle's search on the dam break's fluid at "
+                                          f"dx = 1/64 ({pairs_h} pairs) x 10 in {dt:.1f} s"}
+    print(json.dumps(line))
+
+
 def run_learned(args):
     """Learned k=4 step against k plain steps on the same packed batch of periodic domains.
     value: particles x k / learned-step time (the state resident on the device); the plain
@@ -939,6 +1109,8 @@ def main():
         run_learned(args)
     elif WORKLOADS[args.workload]["scene"] == "regions":
         run_regions(args)
+    elif WORKLOADS[args.workload]["scene"] == "neighbors":
+        run_neighbors(args)
     else:
         run_ours(args)
 

@@ -86,7 +86,8 @@ EXPORTS = [
     "sph_solver_free_surface_workspace_bytes", "sph_solver_set_free_surface", "sph_solver_free_surface_fields",
     "sph_pressure_switch", "sph_liuliu_consistent", "sph_solver_set_verlet_reuse", "sph_solver_sort_count",
     "sph_solver_rhs_walls", "sph_operation", "sph_covariance", "sph_density_gradient", "sph_delta_term",
-    "sph_momentum", "sph_pressure_accel", "sph_viscosity", "sph_mdbc_density",
+    "sph_momentum", "sph_pressure_accel", "sph_viscosity", "sph_mdbc_density", "sph_set_gemm_wait_limit",
+    "sph_solver_set_verlet_scale",
 ]
 
 _lib = None
@@ -143,6 +144,7 @@ def load(build_if_missing: bool = False):
         "sph_solver_shapes": ([], ctypes.c_int),
         "sph_solver_set_shape": ([P, I32], ctypes.c_int),
         "sph_solver_set_verlet_reuse": ([P, I32], ctypes.c_int),
+        "sph_solver_set_verlet_scale": ([P, ctypes.c_double], ctypes.c_int),
         "sph_solver_sort_count": ([P, ctypes.POINTER(ctypes.c_uint32), P], ctypes.c_int),
         "sph_batch_workspace_bytes": ([PP, ctypes.POINTER(I64), I32, ctypes.POINTER(SZ)], ctypes.c_int),
         "sph_batch_create": ([PP, ctypes.POINTER(I64), I32, P, SZ, ctypes.POINTER(P)], ctypes.c_int),
@@ -165,6 +167,7 @@ def load(build_if_missing: bool = False):
         "sph_viscosity": ([ctypes.POINTER(Pairs)] + [P] * 6 + [ctypes.POINTER(ViscosityParams), P, P], ctypes.c_int),
         "sph_mdbc_density": ([ctypes.POINTER(Pairs), P, P, P, P, ctypes.c_double, ctypes.c_double, P, P, P],
                              ctypes.c_int),
+        "sph_set_gemm_wait_limit": ([ctypes.c_uint32, ctypes.POINTER(ctypes.c_uint32)], ctypes.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)

@@ -32,6 +32,8 @@ namespace cconv {
 // ------------------------------------------------------------------------------------
 constexpr int kBM = 128, kBK = 64, kStages = 4, kThreads = 128;
 constexpr uint32_t kSpinLimit = 1u << 22;  // bounded mbarrier polls (seconds at most)
+// the poll limit of the GEMM's waits (sph_set_gemm_wait_limit); read at each launch
+static uint32_t g_gemm_polls = kSpinLimit;
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
     return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -39,6 +41,10 @@ __device__ __forceinline__ uint32_t smem_u32(const void* p) {
 
 __device__ __forceinline__ void mbar_init(uint64_t* b, uint32_t count) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(b)), "r"(count));
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* b) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(b)) : "memory");
 }
 
 __device__ __forceinline__ void mbar_expect_tx(uint64_t* b, uint32_t bytes) {
@@ -60,9 +66,9 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* b, uint32_t parity) {
     return ok != 0;
 }
 
-// false when the phase did not complete within kSpinLimit polls
-__device__ __forceinline__ bool mbar_wait(uint64_t* b, uint32_t parity) {
-    for (uint32_t it = 0; it < kSpinLimit; ++it)
+// false when the phase did not complete within `polls` polls (kSpinLimit by default)
+__device__ __forceinline__ bool mbar_wait(uint64_t* b, uint32_t parity, uint32_t polls = kSpinLimit) {
+    for (uint32_t it = 0; it < polls; ++it)
         if (mbar_try_wait(b, parity)) return true;
     return false;
 }
@@ -126,10 +132,17 @@ struct GemmCfg {
     static constexpr size_t kSmem = static_cast<size_t>(kStage) * kStages + 1024;
 };
 
+// Every mbarrier wait polls at most `polls` times. A wait that runs out sets a bit of *err:
+// 1 the producer's wait for a free stage (it then issues no further load), 2 the MMA
+// issuer's wait for a loaded stage (it issues no further MMA), 4 the wait for the MMAs to
+// complete (the accumulator is then not read), 32 the final wait for loads still in flight.
+// Before the TMEM is released the producer waits (bounded) for the last loads it issued, so
+// no bulk copy lands in the shared memory of an exited CTA. polls = 0 makes every wait fail
+// at once: no load and no MMA is issued.
 template <int BN>
 __global__ void __launch_bounds__(kThreads, 1)
     k_gemm_tn(const __grid_constant__ CUtensorMap ma, const __grid_constant__ CUtensorMap mb, float* __restrict__ D,
-              int64_t ldd, int K, int accumulate, uint32_t* __restrict__ err) {
+              int64_t ldd, int K, int accumulate, uint32_t* __restrict__ err, uint32_t polls) {
     extern __shared__ uint8_t dsm[];
     __shared__ uint64_t full[kStages], empty[kStages], done;
     __shared__ uint32_t tmem_slot;
@@ -157,11 +170,12 @@ __global__ void __launch_bounds__(kThreads, 1)
     asm volatile("tcgen05.fence::after_thread_sync;");
     const uint32_t tmem = tmem_slot;
 
+    int issued = 0;  // loads issued by the producer (its lane only)
     if (warp == 0 && lane == 0) {  // TMA producer
         for (int k = 0; k < nk; ++k) {
             const int s = k % kStages;
             const uint32_t ph = (k / kStages) & 1;
-            if (!mbar_wait(&empty[s], ph ^ 1)) {
+            if (!mbar_wait(&empty[s], ph ^ 1, polls)) {
                 atomicOr(err, 1u);
                 break;
             }
@@ -169,16 +183,19 @@ __global__ void __launch_bounds__(kThreads, 1)
             mbar_expect_tx(&full[s], C::kStage);
             tma_load_2d(sa, &ma, &full[s], k * kBK, static_cast<int>(m0));
             tma_load_2d(sa + C::kA, &mb, &full[s], k * kBK, n0);
+            issued = k + 1;
         }
     } else if (warp == 1 && lane == 0) {  // MMA issuer
         constexpr uint32_t idesc = idesc_bf16(kBM, BN);
+        int mmas = 0;
         for (int k = 0; k < nk; ++k) {
             const int s = k % kStages;
             const uint32_t ph = (k / kStages) & 1;
-            if (!mbar_wait(&full[s], ph)) {  // every load issued before this one has landed
+            if (!mbar_wait(&full[s], ph, polls)) {  // every load issued before this one has landed
                 atomicOr(err, 2u);
                 break;
             }
+            ++mmas;
             asm volatile("tcgen05.fence::after_thread_sync;");
             const uint64_t da = sw128_desc(smem_u32(tiles + s * C::kStage));
             const uint64_t db = sw128_desc(smem_u32(tiles + s * C::kStage + C::kA));
@@ -187,12 +204,21 @@ __global__ void __launch_bounds__(kThreads, 1)
                 mma_bf16(tmem, da + 2 * kk, db + 2 * kk, idesc, (k > 0 || kk > 0) ? 1u : 0u);
             mma_commit(&empty[s]);
         }
-        mma_commit(&done);  // arrives once every MMA issued above has completed
+        // arrives once every MMA issued above has completed; with none issued (a timed-out
+        // first wait) a plain arrive, so that no asynchronous arrive outlives the CTA
+        if (mmas > 0) mma_commit(&done);
+        else mbar_arrive(&done);
     }
     __syncwarp();
     // warp-uniform so that the .sync.aligned TMEM loads below run converged
-    const bool ready = __all_sync(0xffffffffu, mbar_wait(&done, 0));
+    const bool ready = __all_sync(0xffffffffu, mbar_wait(&done, 0, polls));
     if (!ready && lane == 0) atomicOr(err, 4u);
+    if (warp == 0 && lane == 0) {
+        // the last loads issued (one per stage at most) have landed, whether or not the MMA
+        // issuer consumed them: each stage's full barrier has at most that one phase pending
+        for (int k = issued > kStages ? issued - kStages : 0; k < issued; ++k)
+            if (!mbar_wait(&full[k % kStages], (k / kStages) & 1, polls)) atomicOr(err, 32u);
+    }
     asm volatile("tcgen05.fence::after_thread_sync;");
     if (ready) {
         const int64_t row = m0 + warp * 32 + lane;
@@ -629,7 +655,8 @@ int launch_gemm(const CUtensorMap& ma, const CUtensorMap& mb, float* D, int64_t 
     });
     if (attr != cudaSuccess) return SPH_ERR_CUDA;
     dim3 grid(static_cast<unsigned>(N / BN), static_cast<unsigned>(M / kBM));
-    k_gemm_tn<BN><<<grid, kThreads, GemmCfg<BN>::kSmem, s>>>(ma, mb, D, ldd, static_cast<int>(K), acc, err);
+    k_gemm_tn<BN><<<grid, kThreads, GemmCfg<BN>::kSmem, s>>>(ma, mb, D, ldd, static_cast<int>(K), acc, err,
+                                                              g_gemm_polls);
     return cudaGetLastError() == cudaSuccess ? SPH_OK : SPH_ERR_CUDA;
 }
 
@@ -647,6 +674,12 @@ BasisGeo make_basis_geo(const sph_domain_t* d, double support) {
 
 using namespace sph;
 using namespace sph::cconv;
+
+extern "C" int sph_set_gemm_wait_limit(uint32_t polls, uint32_t* previous) {
+    if (previous) *previous = g_gemm_polls;
+    g_gemm_polls = polls;
+    return SPH_OK;
+}
 
 extern "C" int sph_gemm_bf16_tn(const void* A, const void* Bt, float* D, int64_t M, int64_t N, int64_t K, int64_t lda,
                                 int64_t ldb, int64_t ldd, int32_t accumulate, uint32_t* err, sph_stream_t stream) {

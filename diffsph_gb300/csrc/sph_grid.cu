@@ -1,5 +1,7 @@
 // Cell grid, device-wide scans, counting sort by cell, and the exact neighbor search
 // exported for the neighborSearch drop-in (src/diffSPH/v2/modules/neighborhood.py:491-593).
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <math.h>
 
 #include <mutex>
@@ -481,27 +483,54 @@ extern "C" int sph_neighbor_fill_csr(const float* x_query, int64_t n_query, cons
 
 // ------------------------------------------------------------------------------------
 // Neighbor count without caller workspace. The scratch is one file-scope device array per
-// device (the module's global, created with the module); its device address is looked up
-// once per device and cached. Nothing here allocates. Of the scratch, only the per-cell
-// counters must start at zero, and cell_sort clears them (cudaMemsetAsync) on every call;
-// every other region is written before it is read.
+// device (the module's global, created with the module in each context); its device address
+// is looked up once per device and context and cached: a new context on the device (after a
+// cudaDeviceReset, the module loaded again) is noticed and the address looked up again.
+// Nothing here allocates. Of the scratch, only the per-cell counters must start at zero, and
+// cell_sort clears them (cudaMemsetAsync) on every call; every other region is written before
+// it is read.
 // ------------------------------------------------------------------------------------
 static __device__ __align__(256) unsigned char g_nb_static_scratch[SPH_NEIGHBOR_STATIC_SCRATCH_BYTES];
 
 namespace {
 constexpr int kStaticMaxDevices = 64;
 std::mutex g_static_mu;
-void* g_static_ptr[kStaticMaxDevices];  // device address of g_nb_static_scratch, per device
+void* g_static_ptr[kStaticMaxDevices];      // device address of g_nb_static_scratch, per device
+CUcontext g_static_ctx[kStaticMaxDevices];  // the context that address belongs to
+
+PFN_cuCtxGetCurrent_v4000 ctx_get_current() {
+    static PFN_cuCtxGetCurrent_v4000 fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 4000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuCtxGetCurrent_v4000>(p);
+    });
+    return fn;
+}
 
 int static_scratch(void** out) {
     int dev = -1;
     if (cudaGetDevice(&dev) != cudaSuccess) return SPH_ERR_CUDA;
     if (dev < 0 || dev >= kStaticMaxDevices) return SPH_ERR_ARGUMENT;
+    PFN_cuCtxGetCurrent_v4000 get = ctx_get_current();
+    if (!get) return SPH_ERR_CUDA;
+    CUcontext ctx = nullptr;
+    void* fresh = nullptr;
+    if (get(&ctx) != CUDA_SUCCESS) return SPH_ERR_CUDA;
+    if (!ctx) {
+        // no context current on this thread yet: the lookup binds the device's primary context
+        if (cudaGetSymbolAddress(&fresh, g_nb_static_scratch) != cudaSuccess || !fresh) return SPH_ERR_CUDA;
+        if (get(&ctx) != CUDA_SUCCESS || !ctx) return SPH_ERR_CUDA;
+    }
     std::lock_guard<std::mutex> lock(g_static_mu);
-    if (!g_static_ptr[dev]) {
-        void* p = nullptr;
-        if (cudaGetSymbolAddress(&p, g_nb_static_scratch) != cudaSuccess || !p) return SPH_ERR_CUDA;
+    if (!g_static_ptr[dev] || g_static_ctx[dev] != ctx) {
+        void* p = fresh;
+        if (!p && (cudaGetSymbolAddress(&p, g_nb_static_scratch) != cudaSuccess || !p)) return SPH_ERR_CUDA;
         g_static_ptr[dev] = p;
+        g_static_ctx[dev] = ctx;
     }
     *out = g_static_ptr[dev];
     return SPH_OK;

@@ -1916,8 +1916,10 @@ extern "C" int sph_solver_graph_step(sph_solver_t* S, int32_t n_steps, sph_strea
     int rc = step_impl(S, n_steps, st);
     cudaError_t e = cudaStreamEndCapture(st, &g);
     S->timing_mask = mask;
-    if (rc) return rc;
-    if (e != cudaSuccess || !g) return SPH_ERR_CUDA;
+    if (rc || e != cudaSuccess || !g) {  // the capture is invalid: drop what it recorded
+        if (g) cudaGraphDestroy(g);
+        return rc ? rc : SPH_ERR_CUDA;
+    }
     e = cudaGraphInstantiate(&S->graph[slot], g, 0);
     cudaGraphDestroy(g);
     if (e != cudaSuccess) return SPH_ERR_CUDA;
@@ -2160,6 +2162,17 @@ extern "C" int sph_solver_set_verlet_reuse(sph_solver_t* S, int32_t on) {
     // 0.013 h in the first steps of a dam break, so the list keeps holding every pair through
     // the step that crosses 0.034 h
     S->reuse_lim = 0.7f * S->doms_host[0].P.skin_lim;
+    return SPH_OK;
+}
+
+extern "C" int sph_solver_set_verlet_scale(sph_solver_t* S, double verlet_scale) {
+    if (!S || !(verlet_scale > 1.0)) return SPH_ERR_ARGUMENT;
+    // the reference rebuilds once 2 max|dx| > (verletScale - 1) h; the skin list of this solver
+    // holds every pair up to 0.049 h of displacement, and sorting at 0.7 of that keeps it
+    // complete through the step that crosses the limit: the stricter of the two applies
+    const float ref_lim = (float)((verlet_scale - 1.0) * S->doms_host[0].P.h * 0.5);
+    const float own_lim = 0.7f * S->doms_host[0].P.skin_lim;
+    S->reuse_lim = ref_lim < own_lim ? ref_lim : own_lim;
     return SPH_OK;
 }
 

@@ -141,15 +141,26 @@ def dam_break(dx: float = 1.0 / 256, layers: int = 3, hydrostatic: bool = True, 
     return cfg, {"fluid": fluid, "boundary": boundary}
 
 
-def fourier_velocity(x, rng, modes: int = 16, kmax: int = 4, L: float = 2.0):
-    """Divergence-free velocity from psi = sum |k|^-2 sin(k.x + phi), max speed 1."""
-    ks = []
-    while len(ks) < modes:
-        k = rng.integers(-kmax, kmax + 1, size=2)
-        if 0 < np.hypot(*k) <= kmax:
-            ks.append(k)
-    ks = np.asarray(ks, np.float64) * (2 * np.pi / L)
+def fourier_modes(rng, modes: int = 16, kmax: int = 4):
+    """`modes` distinct integer wave vectors with 0 < |k| <= kmax, drawn without replacement;
+    k and -k are one mode (sin(-k.x + phi) = -sin(k.x - phi)), so each is drawn as the
+    representative with kx > 0, or kx = 0 and ky > 0. Returns (k [modes, 2] int, phases)."""
+    cand = [(a, b) for a in range(0, kmax + 1) for b in range(-kmax, kmax + 1)
+            if (a > 0 or b > 0) and a * a + b * b <= kmax * kmax]
+    if modes > len(cand):
+        raise ValueError(f"only {len(cand)} distinct modes have 0 < |k| <= {kmax}")
+    pick = rng.choice(len(cand), size=modes, replace=False)
+    ks = np.asarray([cand[p] for p in pick], np.int64)
     ph = rng.uniform(0, 2 * np.pi, size=modes)
+    return ks, ph
+
+
+def fourier_velocity(x, rng, modes: int = 16, kmax: int = 4, L: float = 2.0):
+    """Divergence-free velocity from the stream function psi = sum |k|^-2 sin(k.x + phi)
+    over `modes` distinct modes (fourier_modes): u = d psi / dy, v = -d psi / dx, scaled to a
+    maximum speed of 1 over the sampled points."""
+    kint, ph = fourier_modes(rng, modes, kmax)
+    ks = kint.astype(np.float64) * (2 * np.pi / L)
     amp = 1.0 / np.sum(ks ** 2, axis=1)
     arg = x @ ks.T + ph
     c = np.cos(arg) * amp

@@ -74,14 +74,26 @@ def _uniform(arr, name):
     return float(v[0]) if v.numel() else 0.0
 
 
+def verlet_scale(cfg) -> float:
+    """neighborhood.verletScale (default 1.5, neighborhood.py:603)."""
+    return _f(cfg.get("neighborhood", {}).get("verletScale", 1.5))
+
+
 def wants_verlet_reuse(cfg, params: _lib.Params) -> bool:
     """Verlet reuse of the cell sort and skin list, as the reference reuses its neighbor
-    structure while neighborhood.verletScale > 1 (default 1.5, neighborhood.py:505-518,603):
-    on for single non-periodic domains."""
+    structure while neighborhood.verletScale > 1 (neighborhood.py:505-518): on for single
+    non-periodic domains."""
     dom = params.domain
     if dom.periodic[0] or dom.periodic[1]:
         return False
-    return _f(cfg.get("neighborhood", {}).get("verletScale", 1.5)) > 1.0
+    return verlet_scale(cfg) > 1.0
+
+
+def verlet_sort_limit(scale: float, support: float, skin_lim: float) -> float:
+    """The displacement since the last sort past which a step sorts again under Verlet
+    reuse: the stricter of the reference's rule (a rebuild once 2 max|dx| > (verletScale - 1) h,
+    neighborhood.py:509-513) and 0.7 of the skin list's limit (sph_solver_set_verlet_scale)."""
+    return min((scale - 1.0) * support / 2.0, 0.7 * skin_lim)
 
 
 def params_from_config(cfg, mass: float, skin: float = DEFAULT_SKIN, capacity: int | None = None) -> _lib.Params:
@@ -211,6 +223,8 @@ class Solver:
         self.verlet_reuse = False
         if wants_verlet_reuse(config, self.params):
             self.set_verlet_reuse(True)
+            _lib.check("sph_solver_set_verlet_scale",
+                       self.lib.sph_solver_set_verlet_scale(self.handle, verlet_scale(config)))
 
     def __del__(self):
         h = getattr(self, "handle", None)

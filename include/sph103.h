@@ -123,7 +123,8 @@ int sph_neighbor_fill_csr(const float* x_query, int64_t n_query, const float* x_
  * sph_neighbor_workspace_bytes for the same sizes exceeds that limit (about 400k particles
  * in a square domain). The first call on a device, with that device current, looks up the
  * array's device address (cudaGetSymbolAddress); make that first call before any stream
- * capture. The per-cell counters that must start at zero are cleared on every call. All
+ * capture. The address is cached per device and CUDA context: after a cudaDeviceReset the
+ * next call (again outside any capture) looks it up in the new context. The per-cell counters that must start at zero are cleared on every call. All
  * calls on one device share the one array: calls that overlap on the GPU (other streams, or
  * another thread before the previous call's work has finished) race on it. Pass 2
  * (sph_neighbor_fill) needs the caller workspace of sph_neighbor_count, not this call. */
@@ -444,6 +445,11 @@ int sph_solver_flags(sph_solver_t* s, uint32_t* flags_host, sph_stream_t stream)
  * both cases. Results differ from the sort-every-step ones only in the order of each
  * particle's pair sums. */
 int sph_solver_set_verlet_reuse(sph_solver_t* s, int32_t on);
+/* The reference's rebuild rule for that reuse (neighborhood.py:509-513): a rebuild once
+ * 2 max |x - x_sort| > (verletScale - 1) h. The solver sorts at the stricter of
+ * (verletScale - 1) h / 2 and its own 0.034 h (the skin list's limit with a margin);
+ * verlet_scale must exceed 1. With the default verletScale 1.5 the solver's limit applies. */
+int sph_solver_set_verlet_scale(sph_solver_t* s, double verlet_scale);
 /* Number of cell sorts since the last upload (device counter); synchronises the stream. */
 int sph_solver_sort_count(sph_solver_t* s, uint32_t* sorts, sph_stream_t stream);
 
@@ -486,6 +492,15 @@ int sph_solver_kernel_times(sph_solver_t* s, float* ms_host, int32_t* launches_h
 int sph_gemm_bf16_tn(const void* A, const void* Bt, float* D, int64_t M, int64_t N, int64_t K,
                      int64_t lda, int64_t ldb, int64_t ldd, int32_t accumulate, uint32_t* err,
                      sph_stream_t stream);
+
+/* The poll limit of sph_gemm_bf16_tn's mbarrier waits (default 2^22 polls, about a
+ * second): a wait that runs out sets a bit of *err (1: a free stage, 2: a loaded stage,
+ * 4: the MMAs' completion, 32: loads still in flight at the end) and the CTA stops issuing
+ * work, waits (bounded) for the loads it issued and releases its tensor memory. 0 makes every
+ * wait fail at once, so that no load or MMA is issued: the error path can be exercised without
+ * a stuck wait. Applies to launches after the call (process-wide); *previous (when non-NULL)
+ * gets the old limit. */
+int sph_set_gemm_wait_limit(uint32_t polls, uint32_t* previous);
 
 /* E_i[b C + c] = inv_norm * sum_j phi_b(x_i - x_j) h_j[c] over the CSR neighbor rows
  * (offsets[n+1] int64, neighbors int32, e.g. the exact lists of sph_neighbor_fill), with

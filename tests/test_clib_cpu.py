@@ -137,6 +137,7 @@ def test_handle_entry_points_reject_null_handles(lib):
     assert lib.sph_solver_graph_step(None, 2, None) == 1
     assert lib.sph_solver_step(None, 1, None) == 1
     assert lib.sph_solver_launches_per_step(None) == -1
+    assert lib.sph_solver_set_verlet_scale(None, 1.5) == 1
 
 
 def test_verlet_reuse_follows_the_reference_verlet_scale():
@@ -189,3 +190,15 @@ def test_solver_rejects_summation_with_rational_update(lib):
     assert lib.sph_solver_workspace_bytes(ctypes.byref(p), nF, nB, ctypes.byref(nbytes)) == 1
     p.density_update, p.density_scheme = 0, 2
     assert lib.sph_solver_workspace_bytes(ctypes.byref(p), nF, nB, ctypes.byref(nbytes)) == 1
+
+
+def test_verlet_sort_limit_is_the_stricter_of_the_reference_rule_and_the_skin_limit():
+    """The reference rebuilds once 2 max|dx| > (verletScale - 1) h (neighborhood.py:509-513);
+    the solver keeps its skin list complete only up to 0.049 h, so it sorts at the smaller of
+    (verletScale - 1) h / 2 and 0.7 x 0.049 h."""
+    from diffsph_gb300.solver import verlet_sort_limit
+    h = 4.0 / 1024
+    skin_lim = 0.5 * 0.1 * h * 0.98
+    assert verlet_sort_limit(1.5, h, skin_lim) == 0.7 * skin_lim        # default scale: the skin limit
+    assert abs(verlet_sort_limit(1.02, h, skin_lim) - 0.02 * h / 2) < 1e-15  # a tight scale: the reference's rule
+    assert verlet_sort_limit(1.0686, h, skin_lim) < 0.7 * skin_lim + 1e-12

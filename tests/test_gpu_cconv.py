@@ -61,6 +61,37 @@ def test_gemm_strided_operands():
     assert float((D - ref).abs().max()) <= 1e-5 * float(ref.abs().max())
 
 
+def test_gemm_wait_timeout_sets_the_error_word_and_the_context_stays_usable():
+    """Every mbarrier wait of the tensor-core GEMM is bounded. With the poll limit at 0 every
+    wait fails at once (no load and no MMA is issued): the kernel sets its error bits (free
+    stage 1, loaded stage 2, completion 4), releases its tensor memory and returns, and
+    check_device_errors raises. The limit restored, the next GEMM in the same context is
+    correct."""
+    import ctypes
+
+    from diffsph_gb300 import _lib
+    from diffsph_gb300.learned import check_device_errors, gemm_tn
+    lib = _lib.load()
+    A = torch.randn(256, 128, device="cuda").to(torch.bfloat16)
+    Bt = torch.randn(64, 128, device="cuda").to(torch.bfloat16)
+    check_device_errors()
+    prev = ctypes.c_uint32()
+    _lib.check("sph_set_gemm_wait_limit", lib.sph_set_gemm_wait_limit(0, ctypes.byref(prev)))
+    try:
+        gemm_tn(A, Bt)
+        torch.cuda.synchronize()
+    finally:
+        lib.sph_set_gemm_wait_limit(prev.value, None)
+    assert prev.value > 0
+    with pytest.raises(RuntimeError, match="0x7"):
+        check_device_errors()
+    D = gemm_tn(A, Bt)
+    ref = A.float() @ Bt.float().t()
+    torch.cuda.synchronize()
+    check_device_errors()
+    assert float((D - ref).abs().max()) <= 1e-5 * float(ref.abs().max()) + 1e-6
+
+
 def test_gemm_rejects_bad_shapes():
     from diffsph_gb300 import _lib
     from diffsph_gb300.learned import gemm_tn
