@@ -284,14 +284,15 @@ __global__ void k_ref_gather(int64_t n, const int32_t* __restrict__ perm, const 
     sidx[s] = o;
 }
 
+// One query row by one thread: the count (FILL = false), or the row's pairs written and then
+// put in the reference's column order by an insertion sort in place (FILL = true; the fill of
+// rows longer than the warp fill's shared buffer).
 template <bool FILL>
-__global__ void k_nb_query(int64_t nq, const float2* __restrict__ qxy, const float2* __restrict__ rxy,
-                           const float* __restrict__ rh, const int32_t* __restrict__ ridx,
-                           const int32_t* __restrict__ start, Grid g, Geo geo, int32_t* __restrict__ counts,
-                           const int64_t* __restrict__ offsets, int64_t* __restrict__ pi, int64_t* __restrict__ pj,
-                           float* __restrict__ pq, float* __restrict__ px, float* __restrict__ ph) {
-    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= nq) return;
+__device__ void nb_row(int64_t i, const float2* __restrict__ qxy, const float2* __restrict__ rxy,
+                       const float* __restrict__ rh, const int32_t* __restrict__ ridx,
+                       const int32_t* __restrict__ start, const Grid& g, const Geo& geo, int32_t* __restrict__ counts,
+                       const int64_t* __restrict__ offsets, int64_t* __restrict__ pi, int64_t* __restrict__ pj,
+                       float* __restrict__ pq, float* __restrict__ px, float* __restrict__ ph) {
     float2 p = qxy[i];
     int cx = cell_coord(p.x, g.mn[0], g.inv_cell[0], g.nc[0]);
     int cy = cell_coord(p.y, g.mn[1], g.inv_cell[1], g.nc[1]);
@@ -348,6 +349,140 @@ __global__ void k_nb_query(int64_t nq, const float2* __restrict__ qxy, const flo
     }
 }
 
+template <bool FILL>
+__global__ void k_nb_query(int64_t nq, const float2* __restrict__ qxy, const float2* __restrict__ rxy,
+                           const float* __restrict__ rh, const int32_t* __restrict__ ridx,
+                           const int32_t* __restrict__ start, Grid g, Geo geo, int32_t* __restrict__ counts,
+                           const int64_t* __restrict__ offsets, int64_t* __restrict__ pi, int64_t* __restrict__ pj,
+                           float* __restrict__ pq, float* __restrict__ px, float* __restrict__ ph) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nq) return;
+    nb_row<FILL>(i, qxy, rxy, rh, ridx, start, g, geo, counts, offsets, pi, pj, pq, px, ph);
+}
+
+// The Wendland C2 kernel and gradient of one pair from its stored q, unit vector and support
+__device__ __forceinline__ void pair_kernel(float qq, float x0h, float x1h, float hh, float* W, float* G,
+                                            int64_t k) {
+    KernelCoef kc;
+    kc.cw = kCd / (hh * hh);
+    kc.cg = kCd / (hh * hh * hh);
+    if (W) W[k] = wendland_w(qq, kc);
+    if (G) {
+        const float d = wendland_dw(qq, kc);
+        G[2 * k] = x0h * d;
+        G[2 * k + 1] = x1h * d;
+    }
+}
+
+// The pair list by one warp per query row. The lanes test the row's stencil candidates 32 at
+// a time (the exact test of the count pass, so the same pairs), the accepted ones are packed
+// into the warp's shared buffer in candidate order (ballot + prefix count), each entry's rank
+// among the row's reference indices gives its slot (the reference's column order, ascending
+// reference index; indices are distinct within a row), and the row leaves with stores that
+// cover its contiguous range of every output array, the kernel values fused in. Rows with
+// more than kFillCap pairs take the one-thread path (nb_row) instead.
+constexpr int kFillWarps = 8;
+constexpr int kFillCap = 128;
+
+__global__ void __launch_bounds__(32 * kFillWarps)
+    k_nb_fill_warp(int64_t nq, const float2* __restrict__ qxy, const float2* __restrict__ rxy,
+                   const float* __restrict__ rh, const int32_t* __restrict__ ridx, const int32_t* __restrict__ start,
+                   Grid g, Geo geo, const int64_t* __restrict__ offsets, int64_t* __restrict__ pi,
+                   int64_t* __restrict__ pj, float* __restrict__ pq, float* __restrict__ px, float* __restrict__ ph,
+                   float* __restrict__ W, float* __restrict__ G) {
+    __shared__ int32_t s_j[kFillWarps][kFillCap];
+    __shared__ float s_q[kFillWarps][kFillCap], s_x0[kFillWarps][kFillCap], s_x1[kFillWarps][kFillCap],
+        s_h[kFillWarps][kFillCap];
+    const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t i = (int64_t)blockIdx.x * kFillWarps + wid;
+    if (i >= nq) return;  // warp-uniform
+    const int64_t w0 = offsets[i];
+    const int cnt_row = (int)(offsets[i + 1] - w0);
+    if (cnt_row > kFillCap) {
+        if (lane == 0) nb_row<true>(i, qxy, rxy, rh, ridx, start, g, geo, nullptr, offsets, pi, pj, pq, px, ph);
+        __syncwarp();
+        if (W || G)
+            for (int e = lane; e < cnt_row; e += 32) {
+                const int64_t o = w0 + e;
+                pair_kernel(pq[o], px[2 * o], px[2 * o + 1], ph[o], W, G, o);
+            }
+        return;
+    }
+    const float2 p = qxy[i];
+    const int cx = cell_coord(p.x, g.mn[0], g.inv_cell[0], g.nc[0]);
+    const int cy = cell_coord(p.y, g.mn[1], g.inv_cell[1], g.nc[1]);
+    int rows[kMaxRows], lo[2], hi[2];
+    const int nr = stencil_rows(cy, g, rows);
+    const int ncr = stencil_cols(cx, g, lo, hi);
+    int rs[kMaxRanges], len[kMaxRanges];
+    int nrg = 0, total = 0;
+    for (int a = 0; a < nr; ++a)
+        for (int b = 0; b < ncr; ++b) {
+            const int s0 = start[rows[a] * g.nc[0] + lo[b]], s1 = start[rows[a] * g.nc[0] + hi[b] + 1];
+            if (s1 > s0) {
+                rs[nrg] = s0;
+                len[nrg] = s1 - s0;
+                total += s1 - s0;
+                ++nrg;
+            }
+        }
+    int base = 0;
+    for (int t0 = 0; t0 < total; t0 += 32) {
+        const int t = t0 + lane;
+        bool acc = false;
+        int jo = 0;
+        float q = 0.f, x0h = 0.f, x1h = 0.f, hh = 0.f;
+        if (t < total) {
+            int r = 0, off = t;
+            while (off >= len[r]) {
+                off -= len[r];
+                ++r;
+            }
+            const int sl = rs[r] + off;
+            float x0, x1;
+            pair_vec<true>(p, rxy[sl], geo, x0, x1);
+            float rr, qq;
+            hh = rh[sl];
+            if (exact_in(sq_norm_ref(x0, x1), hh, rr, qq)) {
+                acc = true;
+                jo = ridx[sl];
+                q = qq;
+                const float den = __fadd_rn(rr, 1e-7f);
+                x0h = __fdiv_rn(x0, den);
+                x1h = __fdiv_rn(x1, den);
+            }
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, acc);
+        const int pos = base + __popc(m & ((1u << lane) - 1u));
+        if (acc && pos < kFillCap) {
+            s_j[wid][pos] = jo;
+            s_q[wid][pos] = q;
+            s_x0[wid][pos] = x0h;
+            s_x1[wid][pos] = x1h;
+            s_h[wid][pos] = hh;
+        }
+        base += __popc(m);
+    }
+    __syncwarp();
+    // the count pass found the same pairs (same candidates, same test); the bound only
+    // keeps an inconsistent row inside its own range
+    const int n_e = base < cnt_row ? base : cnt_row;
+    for (int e = lane; e < n_e; e += 32) {
+        const int je = s_j[wid][e];
+        int rank = 0;
+        for (int k = 0; k < n_e; ++k) rank += s_j[wid][k] < je ? 1 : 0;
+        const int64_t o = w0 + rank;
+        const float q = s_q[wid][e], x0h = s_x0[wid][e], x1h = s_x1[wid][e], hh = s_h[wid][e];
+        pi[o] = i;
+        pj[o] = je;
+        pq[o] = q;
+        px[2 * o] = x0h;
+        px[2 * o + 1] = x1h;
+        ph[o] = hh;
+        if (W || G) pair_kernel(q, x0h, x1h, hh, W, G, o);
+    }
+}
+
 // CSR only: original reference indices of each query's exact neighbors, in cell order
 __global__ void k_nb_csr(int64_t nq, const float2* __restrict__ qxy, const float2* __restrict__ rxy,
                          const float* __restrict__ rh, const int32_t* __restrict__ ridx,
@@ -376,23 +511,6 @@ __global__ void k_nb_csr(int64_t nq, const float2* __restrict__ qxy, const float
                 ++w;
             }
         }
-    }
-}
-
-__global__ void k_pair_kernels(int64_t np, const float* __restrict__ q, const float* __restrict__ xh,
-                               const float* __restrict__ h, float* __restrict__ W, float* __restrict__ G) {
-    int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= np) return;
-    float hh = h[k];
-    KernelCoef kc;
-    kc.cw = kCd / (hh * hh);
-    kc.cg = kCd / (hh * hh * hh);
-    float qq = q[k];
-    if (W) W[k] = wendland_w(qq, kc);
-    if (G) {
-        float d = wendland_dw(qq, kc);
-        G[2 * k] = xh[2 * k] * d;
-        G[2 * k + 1] = xh[2 * k + 1] * d;
     }
 }
 
@@ -455,12 +573,9 @@ extern "C" int sph_neighbor_fill(const float* x_query, int64_t n_query, const fl
     if (!offsets || (n_pairs > 0 && (!pair_i || !pair_j || !q || !xhat || !h_pair))) return SPH_ERR_ARGUMENT;
     // the sorted reference set from sph_neighbor_count is still in the workspace
     if (n_query > 0)
-        k_nb_query<true><<<(unsigned)((n_query + kBlock - 1) / kBlock), kBlock, 0, s>>>(
-            n_query, w.qry_xy, w.ref_xy, w.ref_h, w.ref_idx, w.start, w.grid, w.geo, nullptr, offsets, pair_i,
-            pair_j, q, xhat, h_pair);
-    if ((kernels || gradients) && n_pairs > 0)
-        k_pair_kernels<<<(unsigned)((n_pairs + kBlock - 1) / kBlock), kBlock, 0, s>>>(n_pairs, q, xhat, h_pair,
-                                                                                       kernels, gradients);
+        k_nb_fill_warp<<<(unsigned)((n_query + kFillWarps - 1) / kFillWarps), 32 * kFillWarps, 0, s>>>(
+            n_query, w.qry_xy, w.ref_xy, w.ref_h, w.ref_idx, w.start, w.grid, w.geo, offsets, pair_i, pair_j, q, xhat,
+            h_pair, kernels, gradients);
     return cudaGetLastError() == cudaSuccess ? SPH_OK : SPH_ERR_CUDA;
 }
 
