@@ -39,6 +39,18 @@ REGIONS_SAMPLE_NX = 128
 # 79.05 + 18.85 and 78.91 + 18.46 MB), pass B one launch (74.60 + 4.14 MB)
 PASS_A_DRAM_BYTES_PER_PARTICLE = 186.2
 PASS_B_DRAM_BYTES_PER_PARTICLE = 150.2
+# measured DRAM bytes per particle of pass A / pass B by scene, with where they come from;
+# a scene without a capture of its own reports no traffic
+DRAM_BYTES = {
+    "dam_break": (PASS_A_DRAM_BYTES_PER_PARTICLE, PASS_B_DRAM_BYTES_PER_PARTICLE,
+                  "ncu dram bytes of k_pass_a on dambreak_dx512 (186.2 B/particle, the mean of the "
+                  "skin-building and skin-filtering launches of two steps under Verlet reuse), scaled by "
+                  "the particle count"),
+    "batched": (109.2, 181.8,
+                "ncu dram bytes of k_pass_a (stencil scan, 16 launches) and k_pass_b (8 half-step + 8 final "
+                "launches) on batched_64 (1,162,235 particles in 64 periodic domains), scaled by the "
+                "particle count"),
+}
 # the same for one product of the implicit shift (k_ips_spmv) on the jittered periodic flow
 # of 512^2 particles ((192.06 + 3.65) MB and (189.98 + 3.62) MB / 262,144)
 IPS_SPMV_DRAM_BYTES_PER_PARTICLE = 742.0
@@ -46,6 +58,8 @@ IPS_SPMV_DRAM_BYTES_PER_PARTICLE = 742.0
 WORKLOADS = {
     "dambreak_dx1024": dict(scene="dam_break", dx=1.0 / 1024),
     "batched_256": dict(scene="batched", domains=256, seed=0),
+    # the first 64 domains of the same draw: the case the batch's DRAM traffic is captured on
+    "batched_64": dict(scene="batched", domains=64, seed=0),
     "dambreak_dx512": dict(scene="dam_break", dx=1.0 / 512),
     # the same dam break with the free-surface handling of the shift (shifting.freeSurface)
     "dambreak_fs_dx1024": dict(scene="dam_break", dx=1.0 / 1024, free_surface=True),
@@ -553,17 +567,17 @@ def run_ours(args):
                                      if IPS_SPMV_DRAM_BYTES_PER_PARTICLE else None)}
     if rank != 0:
         return
+    dram_a, dram_b, dram_note = DRAM_BYTES.get(WORKLOADS[args.workload]["scene"],
+                                               (None, None, "no ncu capture of this scene's passes"))
     roofline = {"bound": "hbm", "kernel": "pass_a_gradient", "achieved": achieved, "peak": pk,
                 "peak_kind": pk_kind, "unit": "GB/s",
                 "frac": (achieved / pk) if achieved else None,
-                "traffic": PASS_A_DRAM_BYTES_PER_PARTICLE * nF,
-                "traffic_note": "ncu dram bytes of k_pass_a on dambreak_dx512 (186.2 B/particle, the "
-                                "mean of the skin-building and skin-filtering launches of two "
-                                "steps under Verlet reuse), scaled by the particle count",
+                "traffic": dram_a * nF if dram_a else None,
+                "traffic_note": dram_note,
                 "alg_bytes_per_particle": ab["pass_a"], "avg_launch_ms": pa_avg,
                 "pass_b": {"achieved": achieved_b, "frac": (achieved_b / pk) if achieved_b else None,
                            "alg_bytes_per_particle": ab["pass_b"], "avg_launch_ms": pb_avg,
-                           "traffic": PASS_B_DRAM_BYTES_PER_PARTICLE * nF},
+                           "traffic": dram_b * nF if dram_b else None},
                 "step_alg_bytes_per_particle": ab["step"], "step_achieved_gbs": step_achieved,
                 "step_frac": step_achieved / pk}
     if ips_info is not None and (sp_ms > pa_ms):
@@ -584,7 +598,8 @@ def run_ours(args):
                    "parallelism": "replicas" if world > 1 else "single", "graph": not ips,
                    "shifting": ("IPS" if ips else "deltaPlus") + (
                        "+freeSurface" if WORKLOADS[args.workload].get("free_surface") else ""),
-                   "launch_shape": shape, "shape_ms": [round(v, 4) for v in shape_ms],
+                   "launch_shapes": shape,
+                   "shape_ms": {k: [round(v, 4) for v in ms] for k, ms in shape_ms.items() if max(ms) > 0},
                    "verlet_reuse": bool(getattr(sol, "verlet_reuse", False)), "sorts_in_timed_steps": sorts},
         "e2e": e2e,
         "roofline": roofline,

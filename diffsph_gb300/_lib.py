@@ -79,7 +79,8 @@ EXPORTS = [
     "sph_solver_step", "sph_solver_integrate", "sph_solver_shift", "sph_solver_rhs", "sph_solver_download", "sph_solver_flags",
     "sph_solver_launches_per_step", "sph_solver_kernel_classes", "sph_solver_kernel_name",
     "sph_solver_set_timing", "sph_solver_kernel_times", "sph_solver_autotune", "sph_solver_shapes",
-    "sph_solver_set_shape", "sph_batch_workspace_bytes", "sph_batch_create", "sph_solver_graph_step",
+    "sph_solver_set_shape", "sph_solver_tuned_passes", "sph_solver_set_pass_shape", "sph_solver_pass_shapes",
+    "sph_batch_workspace_bytes", "sph_batch_create", "sph_solver_graph_step",
     "sph_neighbor_count_static", "sph_solver_vjp_rates", "sph_solver_vjp_gradient", "sph_solver_vjp_shift",
     "sph_gemm_bf16_tn", "sph_cconv_aggregate", "sph_cconv_aggregate_t", "sph_cconv_aggregate_tc",
     "sph_neighbor_fill_csr", "sph_solver_ips_workspace_bytes", "sph_solver_set_ips", "sph_solver_ips_result",
@@ -143,6 +144,9 @@ def load(build_if_missing: bool = False):
         "sph_solver_autotune": ([P, ctypes.POINTER(I32), ctypes.POINTER(ctypes.c_float), P], ctypes.c_int),
         "sph_solver_shapes": ([], ctypes.c_int),
         "sph_solver_set_shape": ([P, I32], ctypes.c_int),
+        "sph_solver_tuned_passes": ([], ctypes.c_int),
+        "sph_solver_set_pass_shape": ([P, I32, I32], ctypes.c_int),
+        "sph_solver_pass_shapes": ([P, ctypes.POINTER(I32)], ctypes.c_int),
         "sph_solver_set_verlet_reuse": ([P, I32], ctypes.c_int),
         "sph_solver_set_verlet_scale": ([P, ctypes.c_double], ctypes.c_int),
         "sph_solver_sort_count": ([P, ctypes.POINTER(ctypes.c_uint32), P], ctypes.c_int),

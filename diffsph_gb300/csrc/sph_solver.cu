@@ -407,7 +407,7 @@ __device__ __forceinline__ void pass_a_tile(const Dom& D0, int64_t i, int64_t n,
 // One block handles 32 W consecutive slots: its warps sit in neighboring cells and share
 // most of their stencil data in L1.
 
-template <bool PER, bool BATCH, typename LT, int W, bool BUILD>
+template <bool PER, bool BATCH, typename LT, int W, bool BUILD, bool PERSIST>
 __global__ void __launch_bounds__(32 * W) k_pass_a(const Dom D0, int64_t n, const float4* __restrict__ X4,
                                                    float4* __restrict__ V4, const int32_t* __restrict__ start,
                                                    const Dom* __restrict__ doms, const int32_t* __restrict__ did,
@@ -425,10 +425,10 @@ __global__ void __launch_bounds__(32 * W) k_pass_a(const Dom D0, int64_t n, cons
     __shared__ Dom s_dom[BATCH ? 2 : 1];
     __shared__ int s_id[2];
     LT* lst = reinterpret_cast<LT*>(s_dyn) + (threadIdx.x >> 5) * (kCap * 32);
-    const int64_t first = (int64_t)blockIdx.x * (32 * W);
-    if (BATCH) stage_doms(doms, did, first, first + 32 * W - 1, n, s_dom, s_id);
-    pass_a_tile<PER, BATCH, LT, BUILD>(D0, first + threadIdx.x, n, X4, V4, start, doms, s_dom, s_id, did, uid, out,
-                                       lst, words, nl, nlc, skin_mode, sl, slc);
+    run_tiles<BATCH, W, PERSIST>(n, doms, did, s_dom, s_id, [&](int64_t first) {
+        pass_a_tile<PER, BATCH, LT, BUILD>(D0, first + threadIdx.x, n, X4, V4, start, doms, s_dom, s_id, did, uid,
+                                           out, lst, words, nl, nlc, skin_mode, sl, slc);
+    });
 }
 
 // ------------------------------------------------------------------------------------
@@ -594,7 +594,7 @@ __device__ __forceinline__ void pass_b_tile(const Dom& D0, int64_t i, int64_t n,
     }
 }
 
-template <bool PER, bool BATCH, int MODE, typename LT, int W>
+template <bool PER, bool BATCH, int MODE, typename LT, int W, bool PERSIST>
 __global__ void __launch_bounds__(32 * W) k_pass_b(const Dom D0, int64_t n, const float4* __restrict__ X4,
                                                    const float4* __restrict__ V4, const int32_t* __restrict__ start,
                                                    const Dom* __restrict__ doms, const int32_t* __restrict__ did,
@@ -608,10 +608,10 @@ __global__ void __launch_bounds__(32 * W) k_pass_b(const Dom D0, int64_t n, cons
     __shared__ Dom s_dom[BATCH ? 2 : 1];
     __shared__ int s_id[2];
     LT* lst = reinterpret_cast<LT*>(s_dyn) + (threadIdx.x >> 5) * (kCap * 32);
-    const int64_t first = (int64_t)blockIdx.x * (32 * W);
-    if (BATCH) stage_doms(doms, did, first, first + 32 * W - 1, n, s_dom, s_id);
-    pass_b_tile<PER, BATCH, MODE, LT>(D0, first + threadIdx.x, n, X4, V4, start, doms, s_dom, s_id, did, uid, out,
-                                      Xr, X4n, V4n, X4o, V4o, words, maxv, lst, nl, nlc, Xs);
+    run_tiles<BATCH, W, PERSIST>(n, doms, did, s_dom, s_id, [&](int64_t first) {
+        pass_b_tile<PER, BATCH, MODE, LT>(D0, first + threadIdx.x, n, X4, V4, start, doms, s_dom, s_id, did, uid,
+                                          out, Xr, X4n, V4n, X4o, V4o, words, maxv, lst, nl, nlc, Xs);
+    });
 }
 
 // ------------------------------------------------------------------------------------
@@ -697,7 +697,7 @@ __device__ __forceinline__ void shift_tile(const Dom& D0, int64_t i, int64_t n, 
     }
 }
 
-template <bool PER, bool BATCH, typename LT, int W>
+template <bool PER, bool BATCH, typename LT, int W, bool PERSIST>
 __global__ void __launch_bounds__(32 * W) k_shift(const Dom D0, int64_t n, const float4* __restrict__ X4,
                                                   const float4* __restrict__ V4, const int32_t* __restrict__ start,
                                                   const Dom* __restrict__ doms, const int32_t* __restrict__ did,
@@ -711,10 +711,10 @@ __global__ void __launch_bounds__(32 * W) k_shift(const Dom D0, int64_t n, const
     __shared__ Dom s_dom[BATCH ? 2 : 1];
     __shared__ int s_id[2];
     LT* lst = reinterpret_cast<LT*>(s_dyn) + (threadIdx.x >> 5) * (kCap * 32);
-    const int64_t first = (int64_t)blockIdx.x * (32 * W);
-    if (BATCH) stage_doms(doms, did, first, first + 32 * W - 1, n, s_dom, s_id);
-    shift_tile<PER, BATCH, LT>(D0, first + threadIdx.x, n, X4, V4, start, doms, s_dom, s_id, did, Xr, X4o, V4o,
-                               words, maxv, enabled, uid, dx_out, lst, use_skin, sl, slc, sv);
+    run_tiles<BATCH, W, PERSIST>(n, doms, did, s_dom, s_id, [&](int64_t first) {
+        shift_tile<PER, BATCH, LT>(D0, first + threadIdx.x, n, X4, V4, start, doms, s_dom, s_id, did, Xr, X4o, V4o,
+                                   words, maxv, enabled, uid, dx_out, lst, use_skin, sl, slc, sv);
+    });
 }
 
 // ------------------------------------------------------------------------------------
@@ -726,20 +726,13 @@ __global__ void __launch_bounds__(32 * W) k_shift(const Dom D0, int64_t n, const
 // thread reads a density another thread of the launch writes. The wall rows' own
 // summation is not kept: the mDBC extrapolation replaces it (deltaPlus.py:200-202).
 // ------------------------------------------------------------------------------------
-template <bool PER, bool BATCH, typename LT, int W>
-__global__ void __launch_bounds__(32 * W) k_density_sum(const Dom D0, int64_t n, const float4* __restrict__ X4,
-                                                        float4* __restrict__ X4o, const int32_t* __restrict__ start_all,
-                                                        const Dom* __restrict__ doms, const int32_t* __restrict__ did,
-                                                        uint32_t* __restrict__ words, int skin_mode,
-                                                        const int16_t* __restrict__ sl,
-                                                        const int16_t* __restrict__ slc) {
-    extern __shared__ __align__(16) unsigned char s_dyn[];
-    __shared__ Dom s_dom[BATCH ? 2 : 1];
-    __shared__ int s_id[2];
-    LT* lst = reinterpret_cast<LT*>(s_dyn) + (threadIdx.x >> 5) * (kCap * 32);
-    const int64_t first = (int64_t)blockIdx.x * (32 * W);
-    if (BATCH) stage_doms(doms, did, first, first + 32 * W - 1, n, s_dom, s_id);
-    const int64_t i = first + threadIdx.x;
+template <bool PER, bool BATCH, typename LT>
+__device__ __forceinline__ void density_sum_tile(const Dom& D0, int64_t i, int64_t n, const float4* __restrict__ X4,
+                                                 float4* __restrict__ X4o, const int32_t* __restrict__ start_all,
+                                                 const Dom* __restrict__ doms, const Dom* s_dom, const int* s_id,
+                                                 const int32_t* __restrict__ did, uint32_t* __restrict__ words,
+                                                 int skin_mode, const int16_t* __restrict__ sl,
+                                                 const int16_t* __restrict__ slc, LT* __restrict__ lst) {
     const Dom& D = BATCH ? dom_ref(doms, s_dom, s_id, dom_of(did, i, n)) : D0;
     const Phys& P = D.P;
     const Grid& g = D.g;
@@ -773,6 +766,23 @@ __global__ void __launch_bounds__(32 * W) k_density_sum(const Dom D0, int64_t n,
         o.w = eos_p(o.z, P.eos);
     }
     X4o[i] = o;
+}
+
+template <bool PER, bool BATCH, typename LT, int W, bool PERSIST>
+__global__ void __launch_bounds__(32 * W) k_density_sum(const Dom D0, int64_t n, const float4* __restrict__ X4,
+                                                        float4* __restrict__ X4o, const int32_t* __restrict__ start_all,
+                                                        const Dom* __restrict__ doms, const int32_t* __restrict__ did,
+                                                        uint32_t* __restrict__ words, int skin_mode,
+                                                        const int16_t* __restrict__ sl,
+                                                        const int16_t* __restrict__ slc) {
+    extern __shared__ __align__(16) unsigned char s_dyn[];
+    __shared__ Dom s_dom[BATCH ? 2 : 1];
+    __shared__ int s_id[2];
+    LT* lst = reinterpret_cast<LT*>(s_dyn) + (threadIdx.x >> 5) * (kCap * 32);
+    run_tiles<BATCH, W, PERSIST>(n, doms, did, s_dom, s_id, [&](int64_t first) {
+        density_sum_tile<PER, BATCH, LT>(D0, first + threadIdx.x, n, X4, X4o, start_all, doms, s_dom, s_id, did,
+                                         words, skin_mode, sl, slc, lst);
+    });
 }
 
 // Caller-given wall densities (sph_solver_rhs_walls): rho_b[b] in the original order of the
@@ -1659,96 +1669,105 @@ static void launch_mdbc(sph_solver* S, float4* X4, float* rho_b_out, cudaStream_
 }
 
 
-template <bool PER, bool BATCH, typename LT, int W>
+template <bool PER, bool BATCH, typename LT, int W, bool PS>
 static void allow_lists_k(int b) {
-    cudaFuncSetAttribute(k_pass_a<PER, BATCH, LT, W, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
-    cudaFuncSetAttribute(k_pass_a<PER, BATCH, LT, W, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
-    cudaFuncSetAttribute(k_pass_b<PER, BATCH, 0, LT, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
-    cudaFuncSetAttribute(k_pass_b<PER, BATCH, 1, LT, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
-    cudaFuncSetAttribute(k_pass_b<PER, BATCH, 2, LT, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
-    cudaFuncSetAttribute(k_shift<PER, BATCH, LT, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
-    cudaFuncSetAttribute(k_density_sum<PER, BATCH, LT, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+    cudaFuncSetAttribute(k_pass_a<PER, BATCH, LT, W, false, PS>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+    cudaFuncSetAttribute(k_pass_a<PER, BATCH, LT, W, true, PS>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+    cudaFuncSetAttribute(k_pass_b<PER, BATCH, 0, LT, W, PS>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+    cudaFuncSetAttribute(k_pass_b<PER, BATCH, 1, LT, W, PS>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+    cudaFuncSetAttribute(k_pass_b<PER, BATCH, 2, LT, W, PS>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+    cudaFuncSetAttribute(k_shift<PER, BATCH, LT, W, PS>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+    cudaFuncSetAttribute(k_density_sum<PER, BATCH, LT, W, PS>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
 }
 
-template <typename LT, int W>
+template <typename LT, int W, bool PS>
 static void allow_lists_s() {
     const int b = (int)list_bytes<LT, W>();
-    allow_lists_k<true, false, LT, W>(b);
-    allow_lists_k<false, false, LT, W>(b);
-    allow_lists_k<true, true, LT, W>(b);
-    allow_lists_k<false, true, LT, W>(b);
+    allow_lists_k<true, false, LT, W, PS>(b);
+    allow_lists_k<false, false, LT, W, PS>(b);
+    allow_lists_k<true, true, LT, W, PS>(b);
+    allow_lists_k<false, true, LT, W, PS>(b);
 }
 
 static void set_attrs(sph_solver* S) {
     if (S->attrs_set) return;
-    allow_lists_s<int32_t, 4>();
-    allow_lists_s<int16_t, 4>();
-    allow_lists_s<int16_t, 8>();
-    allow_lists_s<int16_t, 16>();
+    allow_lists_s<int32_t, 4, false>();
+    allow_lists_s<int16_t, 4, false>();
+    allow_lists_s<int16_t, 8, false>();
+    allow_lists_s<int16_t, 16, false>();
+    allow_lists_s<int16_t, 8, true>();
     S->attrs_set = true;
 }
 
 // dispatch a launcher template over the shape table
-#define SPH_SHAPE_DISPATCH(S, CALL)                   \
-    switch ((S)->shape) {                             \
-        case 1: CALL(int16_t, 4); break;              \
-        case 2: CALL(int16_t, 8); break;              \
-        case 3: CALL(int16_t, 16); break;             \
-        default: CALL(int32_t, 4); break;             \
+#define SPH_SHAPE_DISPATCH(SH, CALL)                  \
+    switch (SH) {                                     \
+        case 1: CALL(int16_t, 4, false); break;       \
+        case 2: CALL(int16_t, 8, false); break;       \
+        case 3: CALL(int16_t, 16, false); break;      \
+        case 4: CALL(int16_t, 8, true); break;        \
+        default: CALL(int32_t, 4, false); break;      \
     }
-
-template <bool PER, bool BATCH, typename LT, int W>
-static void launch_a_k(sph_solver* S, float4* X4, float4* V4, RhsOut o, int skin_mode, cudaStream_t st) {
-    unsigned gb = (unsigned)((S->n + 32 * W - 1) / (32 * W));
-    if (skin_mode == 0 || skin_mode == 3)
-        k_pass_a<PER, BATCH, LT, W, true><<<gb, 32 * W, list_bytes<LT, W>(), st>>>(
-            S->doms_host[0], S->n, X4, V4, S->start, S->doms, dids(S), S->uid, o, S->words, S->nl, S->nlc, skin_mode,
-            S->sl, S->slc);
-    else
-        k_pass_a<PER, BATCH, LT, W, false><<<gb, 32 * W, list_bytes<LT, W>(), st>>>(
-            S->doms_host[0], S->n, X4, V4, S->start, S->doms, dids(S), S->uid, o, S->words, S->nl, S->nlc, skin_mode,
-            S->sl, S->slc);
-}
-
-template <typename LT, int W>
-static void launch_a_t(sph_solver* S, float4* X4, float4* V4, RhsOut o, int skin_mode, cudaStream_t st) {
-    if (S->nd > 1) {
-        if (S->periodic) launch_a_k<true, true, LT, W>(S, X4, V4, o, skin_mode, st);
-        else launch_a_k<false, true, LT, W>(S, X4, V4, o, skin_mode, st);
-    } else {
-        if (S->periodic) launch_a_k<true, false, LT, W>(S, X4, V4, o, skin_mode, st);
-        else launch_a_k<false, false, LT, W>(S, X4, V4, o, skin_mode, st);
-    }
-}
 
 // skin_mode: 0 keeps the skin list (first pass A after a sort), 1 filters it (second pass A
 // of the same step), 2 neither; 3 and 4 are 0 and 1 decided on the device by words[4]
+static int pass_a_tuned(int skin_mode) { return (skin_mode == 1 || skin_mode == 4) ? TP_A_FILTER : TP_A_SCAN; }
+
+template <bool PER, bool BATCH, typename LT, int W, bool PS>
+static void launch_a_k(sph_solver* S, float4* X4, float4* V4, RhsOut o, int skin_mode, cudaStream_t st) {
+    const int tp = pass_a_tuned(skin_mode), sh = S->shape_of[tp];
+    const size_t sm = list_bytes<LT, W>();
+    if (skin_mode == 0 || skin_mode == 3) {
+        auto kern = k_pass_a<PER, BATCH, LT, W, true, PS>;
+        kern<<<pass_grid(S, tp, sh, kern, 32 * W, sm), 32 * W, sm, st>>>(
+            S->doms_host[0], S->n, X4, V4, S->start, S->doms, dids(S), S->uid, o, S->words, S->nl, S->nlc, skin_mode,
+            S->sl, S->slc);
+    } else {
+        auto kern = k_pass_a<PER, BATCH, LT, W, false, PS>;
+        kern<<<pass_grid(S, tp, sh, kern, 32 * W, sm), 32 * W, sm, st>>>(
+            S->doms_host[0], S->n, X4, V4, S->start, S->doms, dids(S), S->uid, o, S->words, S->nl, S->nlc, skin_mode,
+            S->sl, S->slc);
+    }
+}
+
+template <typename LT, int W, bool PS>
+static void launch_a_t(sph_solver* S, float4* X4, float4* V4, RhsOut o, int skin_mode, cudaStream_t st) {
+    if (S->nd > 1) {
+        if (S->periodic) launch_a_k<true, true, LT, W, PS>(S, X4, V4, o, skin_mode, st);
+        else launch_a_k<false, true, LT, W, PS>(S, X4, V4, o, skin_mode, st);
+    } else {
+        if (S->periodic) launch_a_k<true, false, LT, W, PS>(S, X4, V4, o, skin_mode, st);
+        else launch_a_k<false, false, LT, W, PS>(S, X4, V4, o, skin_mode, st);
+    }
+}
+
 static void launch_a(sph_solver* S, float4* X4, float4* V4, RhsOut o, cudaStream_t st, int skin_mode = 2) {
     set_attrs(S);
     const int cls = (skin_mode == 1 || skin_mode == 4) ? KC_PASS_A : KC_PASS_A_SCAN;
     tbeg(S, cls, st);
-#define SPH_CALL_A(LT, W) launch_a_t<LT, W>(S, X4, V4, o, skin_mode, st)
-    SPH_SHAPE_DISPATCH(S, SPH_CALL_A)
+#define SPH_CALL_A(LT, W, PS) launch_a_t<LT, W, PS>(S, X4, V4, o, skin_mode, st)
+    SPH_SHAPE_DISPATCH(S->shape_of[pass_a_tuned(skin_mode)], SPH_CALL_A)
 #undef SPH_CALL_A
     tend(S, cls, st);
 }
 
-template <bool PER, bool BATCH, int MODE, typename LT, int W>
+template <bool PER, bool BATCH, int MODE, typename LT, int W, bool PS>
 static void launch_b_k(sph_solver* S, float4* X4, float4* V4, RhsOut o, float4* X4o, float4* V4o, cudaStream_t st) {
-    unsigned gb = (unsigned)((S->n + 32 * W - 1) / (32 * W));
-    k_pass_b<PER, BATCH, MODE, LT, W><<<gb, 32 * W, list_bytes<LT, W>(), st>>>(
+    const size_t sm = list_bytes<LT, W>();
+    auto kern = k_pass_b<PER, BATCH, MODE, LT, W, PS>;
+    kern<<<pass_grid(S, TP_B, S->shape_of[TP_B], kern, 32 * W, sm), 32 * W, sm, st>>>(
         S->doms_host[0], S->n, X4, V4, S->start, S->doms, dids(S), S->uid, o, S->Xr, S->Xc, S->Vc, X4o, V4o,
         S->words, S->maxv, S->nl, S->nlc, S->Xs);
 }
 
-template <int MODE, typename LT, int W>
+template <int MODE, typename LT, int W, bool PS>
 static void launch_b_t(sph_solver* S, float4* X4, float4* V4, RhsOut o, float4* X4o, float4* V4o, cudaStream_t st) {
     if (S->nd > 1) {
-        if (S->periodic) launch_b_k<true, true, MODE, LT, W>(S, X4, V4, o, X4o, V4o, st);
-        else launch_b_k<false, true, MODE, LT, W>(S, X4, V4, o, X4o, V4o, st);
+        if (S->periodic) launch_b_k<true, true, MODE, LT, W, PS>(S, X4, V4, o, X4o, V4o, st);
+        else launch_b_k<false, true, MODE, LT, W, PS>(S, X4, V4, o, X4o, V4o, st);
     } else {
-        if (S->periodic) launch_b_k<true, false, MODE, LT, W>(S, X4, V4, o, X4o, V4o, st);
-        else launch_b_k<false, false, MODE, LT, W>(S, X4, V4, o, X4o, V4o, st);
+        if (S->periodic) launch_b_k<true, false, MODE, LT, W, PS>(S, X4, V4, o, X4o, V4o, st);
+        else launch_b_k<false, false, MODE, LT, W, PS>(S, X4, V4, o, X4o, V4o, st);
     }
 }
 
@@ -1756,27 +1775,28 @@ template <int MODE>
 static void launch_b(sph_solver* S, float4* X4, float4* V4, RhsOut o, float4* X4o, float4* V4o, cudaStream_t st) {
     set_attrs(S);
     tbeg(S, KC_PASS_B, st);
-#define SPH_CALL_B(LT, W) launch_b_t<MODE, LT, W>(S, X4, V4, o, X4o, V4o, st)
-    SPH_SHAPE_DISPATCH(S, SPH_CALL_B)
+#define SPH_CALL_B(LT, W, PS) launch_b_t<MODE, LT, W, PS>(S, X4, V4, o, X4o, V4o, st)
+    SPH_SHAPE_DISPATCH(S->shape_of[TP_B], SPH_CALL_B)
 #undef SPH_CALL_B
     tend(S, KC_PASS_B, st);
 }
 
-template <bool PER, bool BATCH, typename LT, int W>
+template <bool PER, bool BATCH, typename LT, int W, bool PS>
 static void launch_dsum_k(sph_solver* S, const float4* Xin, float4* Xout, int skin_mode, cudaStream_t st) {
-    unsigned gb = (unsigned)((S->n + 32 * W - 1) / (32 * W));
-    k_density_sum<PER, BATCH, LT, W><<<gb, 32 * W, list_bytes<LT, W>(), st>>>(
+    const size_t sm = list_bytes<LT, W>();
+    auto kern = k_density_sum<PER, BATCH, LT, W, PS>;
+    kern<<<pass_grid(S, TP_DENSITY, S->shape_of[TP_DENSITY], kern, 32 * W, sm), 32 * W, sm, st>>>(
         S->doms_host[0], S->n, Xin, Xout, S->start, S->doms, dids(S), S->words, skin_mode, S->sl, S->slc);
 }
 
-template <typename LT, int W>
+template <typename LT, int W, bool PS>
 static void launch_dsum_t(sph_solver* S, const float4* Xin, float4* Xout, int skin_mode, cudaStream_t st) {
     if (S->nd > 1) {
-        if (S->periodic) launch_dsum_k<true, true, LT, W>(S, Xin, Xout, skin_mode, st);
-        else launch_dsum_k<false, true, LT, W>(S, Xin, Xout, skin_mode, st);
+        if (S->periodic) launch_dsum_k<true, true, LT, W, PS>(S, Xin, Xout, skin_mode, st);
+        else launch_dsum_k<false, true, LT, W, PS>(S, Xin, Xout, skin_mode, st);
     } else {
-        if (S->periodic) launch_dsum_k<true, false, LT, W>(S, Xin, Xout, skin_mode, st);
-        else launch_dsum_k<false, false, LT, W>(S, Xin, Xout, skin_mode, st);
+        if (S->periodic) launch_dsum_k<true, false, LT, W, PS>(S, Xin, Xout, skin_mode, st);
+        else launch_dsum_k<false, false, LT, W, PS>(S, Xin, Xout, skin_mode, st);
     }
 }
 
@@ -1784,8 +1804,8 @@ static void launch_dsum_t(sph_solver* S, const float4* Xin, float4* Xout, int sk
 static void launch_dsum(sph_solver* S, const float4* Xin, float4* Xout, cudaStream_t st, int skin_mode) {
     set_attrs(S);
     tbeg(S, KC_DENSITY, st);
-#define SPH_CALL_D(LT, W) launch_dsum_t<LT, W>(S, Xin, Xout, skin_mode, st)
-    SPH_SHAPE_DISPATCH(S, SPH_CALL_D)
+#define SPH_CALL_D(LT, W, PS) launch_dsum_t<LT, W, PS>(S, Xin, Xout, skin_mode, st)
+    SPH_SHAPE_DISPATCH(S->shape_of[TP_DENSITY], SPH_CALL_D)
 #undef SPH_CALL_D
     tend(S, KC_DENSITY, st);
 }
@@ -1832,25 +1852,25 @@ static int run_stages(sph_solver* S, cudaStream_t st) {
     return cudaGetLastError() == cudaSuccess ? SPH_OK : SPH_ERR_CUDA;
 }
 
-template <bool PER, bool BATCH, typename LT, int W>
+template <bool PER, bool BATCH, typename LT, int W, bool PS>
 static void launch_shift_k(sph_solver* S, float4* Xin, float4* Vin, float4* Xout, float4* Vout, float* dx_out,
                            int use_skin, cudaStream_t st) {
-    unsigned gb = (unsigned)((S->n + 32 * W - 1) / (32 * W));
-    k_shift<PER, BATCH, LT, W><<<gb, 32 * W, list_bytes<LT, W>(), st>>>(S->doms_host[0], S->n, Xin, Vin, S->start,
-                                                                       S->doms, dids(S), S->Xr, Xout, Vout, S->words,
-                                                                       S->maxv, S->prm.shift_on, S->uid, dx_out,
-                                                                       use_skin, S->sl, S->slc, surface_view(S));
+    const size_t sm = list_bytes<LT, W>();
+    auto kern = k_shift<PER, BATCH, LT, W, PS>;
+    kern<<<pass_grid(S, TP_SHIFT, S->shape_of[TP_SHIFT], kern, 32 * W, sm), 32 * W, sm, st>>>(
+        S->doms_host[0], S->n, Xin, Vin, S->start, S->doms, dids(S), S->Xr, Xout, Vout, S->words, S->maxv,
+        S->prm.shift_on, S->uid, dx_out, use_skin, S->sl, S->slc, surface_view(S));
 }
 
-template <typename LT, int W>
+template <typename LT, int W, bool PS>
 static void launch_shift_t(sph_solver* S, float4* Xin, float4* Vin, float4* Xout, float4* Vout, float* dx_out,
                            int use_skin, cudaStream_t st) {
     if (S->nd > 1) {
-        if (S->periodic) launch_shift_k<true, true, LT, W>(S, Xin, Vin, Xout, Vout, dx_out, use_skin, st);
-        else launch_shift_k<false, true, LT, W>(S, Xin, Vin, Xout, Vout, dx_out, use_skin, st);
+        if (S->periodic) launch_shift_k<true, true, LT, W, PS>(S, Xin, Vin, Xout, Vout, dx_out, use_skin, st);
+        else launch_shift_k<false, true, LT, W, PS>(S, Xin, Vin, Xout, Vout, dx_out, use_skin, st);
     } else {
-        if (S->periodic) launch_shift_k<true, false, LT, W>(S, Xin, Vin, Xout, Vout, dx_out, use_skin, st);
-        else launch_shift_k<false, false, LT, W>(S, Xin, Vin, Xout, Vout, dx_out, use_skin, st);
+        if (S->periodic) launch_shift_k<true, false, LT, W, PS>(S, Xin, Vin, Xout, Vout, dx_out, use_skin, st);
+        else launch_shift_k<false, false, LT, W, PS>(S, Xin, Vin, Xout, Vout, dx_out, use_skin, st);
     }
 }
 
@@ -1859,8 +1879,8 @@ static void launch_shift(sph_solver* S, float4* Xin, float4* Vin, float4* Xout, 
                          cudaStream_t st, int use_skin = 0) {
     set_attrs(S);
     tbeg(S, KC_SHIFT, st);
-#define SPH_CALL_S(LT, W) launch_shift_t<LT, W>(S, Xin, Vin, Xout, Vout, dx_out, use_skin, st)
-    SPH_SHAPE_DISPATCH(S, SPH_CALL_S)
+#define SPH_CALL_S(LT, W, PS) launch_shift_t<LT, W, PS>(S, Xin, Vin, Xout, Vout, dx_out, use_skin, st)
+    SPH_SHAPE_DISPATCH(S->shape_of[TP_SHIFT], SPH_CALL_S)
 #undef SPH_CALL_S
     tend(S, KC_SHIFT, st);
 }
@@ -1959,45 +1979,96 @@ extern "C" int sph_solver_shift(sph_solver_t* S, float* dx_out, sph_stream_t str
     return cudaGetLastError() == cudaSuccess ? SPH_OK : SPH_ERR_CUDA;
 }
 
-extern "C" int sph_solver_autotune(sph_solver_t* S, int32_t* shape_out, float* ms_out, sph_stream_t stream) {
+// The autotuner times every pass it shapes separately, on the current state, under each
+// shape: a fresh sort at the current positions first (so that the skin list the timed
+// scanning pass A keeps belongs to it), then pass A scanning, pass A filtering that list,
+// the shift (into the spare buffers, with the raw positions it moves saved and restored),
+// the summation density and pass B (half-step update into the spare stage buffers). The
+// skin list is marked invalid at the end, so a Verlet-reuse step sorts again first.
+extern "C" int sph_solver_autotune(sph_solver_t* S, int32_t* shapes_out, float* ms_out, sph_stream_t stream) {
     if (!S) return SPH_ERR_ARGUMENT;
     cudaStream_t st = (cudaStream_t)stream;
+    if (cudaMemsetAsync(S->words + 3, 1, sizeof(uint32_t), st) != cudaSuccess) return SPH_ERR_CUDA;
     int rc = rebuild(S, st);
     if (rc) return rc;
+    set_attrs(S);
     RhsOut none = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     cudaEvent_t a, b;
-    if (cudaEventCreate(&a) != cudaSuccess || cudaEventCreate(&b) != cudaSuccess) return SPH_ERR_CUDA;
-    uint32_t saved_mask = S->timing_mask;
+    if (cudaEventCreate(&a) != cudaSuccess) return SPH_ERR_CUDA;
+    if (cudaEventCreate(&b) != cudaSuccess) {
+        cudaEventDestroy(a);
+        return SPH_ERR_CUDA;
+    }
+    const uint32_t saved_mask = S->timing_mask;
+    const bool saved_fs = S->fs_on;
     S->timing_mask = 0;
-    float best = 1e30f;
-    int best_shape = 0;
-    for (int k = 0; k < kNumShapes; ++k) {
-        float ms = -1.f;
-        if (!kShapes[k].list16 || S->list16) {
-            S->shape = k;
-            launch_a(S, S->Xc, S->Vc, none, st);  // warm-up
-            cudaEventRecord(a, st);
-            for (int r = 0; r < 3; ++r) launch_a(S, S->Xc, S->Vc, none, st);
-            cudaEventRecord(b, st);
-            if (cudaEventSynchronize(b) != cudaSuccess) return SPH_ERR_CUDA;
-            cudaEventElapsedTime(&ms, a, b);
-            ms /= 3.f;
-            if (ms < best) {
-                best = ms;
-                best_shape = k;
+    S->fs_on = false;
+    const int skin_scan = S->periodic ? 2 : 0;
+    const int order[TP_COUNT] = {TP_A_SCAN, TP_A_FILTER, TP_SHIFT, TP_DENSITY, TP_B};
+    rc = SPH_OK;
+    for (int oi = 0; oi < TP_COUNT && rc == SPH_OK; ++oi) {
+        const int tp = order[oi];
+        const bool applies = tp == TP_A_SCAN || tp == TP_B || (tp == TP_A_FILTER && !S->periodic) ||
+                             (tp == TP_SHIFT && !S->ips) || (tp == TP_DENSITY && summation(S));
+        auto run = [&]() {
+            switch (tp) {
+                case TP_A_SCAN: launch_a(S, S->Xc, S->Vc, none, st, skin_scan); break;
+                case TP_A_FILTER: launch_a(S, S->Xc, S->Vc, none, st, 1); break;
+                case TP_B: launch_b<1>(S, S->Xc, S->Vc, none, S->Xh, S->Vh, st); break;
+                case TP_SHIFT: launch_shift(S, S->Xc, S->Vc, S->Xt, S->Vt, nullptr, st, S->periodic ? 0 : 1); break;
+                default: launch_dsum(S, S->Xc, S->Xt, st, S->periodic ? 2 : 1); break;
             }
+        };
+        if (tp == TP_SHIFT && applies &&
+            cudaMemcpyAsync(S->Xr_t, S->Xr, sizeof(float2) * S->n, cudaMemcpyDeviceToDevice, st) != cudaSuccess) {
+            rc = SPH_ERR_CUDA;
+            break;
         }
-        if (ms_out) ms_out[k] = ms;
+        float best = 1e30f;
+        int best_shape = 0;
+        for (int k = 0; k < kNumShapes; ++k) {
+            float ms = -1.f;
+            if (applies && (!kShapes[k].list16 || S->list16)) {
+                S->shape_of[tp] = k;
+                run();  // warm-up
+                cudaEventRecord(a, st);
+                for (int r = 0; r < 3; ++r) run();
+                cudaEventRecord(b, st);
+                if (cudaEventSynchronize(b) != cudaSuccess) {
+                    rc = SPH_ERR_CUDA;
+                    break;
+                }
+                cudaEventElapsedTime(&ms, a, b);
+                ms /= 3.f;
+                if (ms < best) {
+                    best = ms;
+                    best_shape = k;
+                }
+            }
+            if (ms_out) ms_out[tp * kNumShapes + k] = ms;
+        }
+        S->shape_of[tp] = best_shape;
+        // the scanning pass A kept the skin list at the sort positions: valid for the filters
+        if (tp == TP_A_SCAN && !S->periodic &&
+            cudaMemsetAsync(S->words + 3, 0, sizeof(uint32_t), st) != cudaSuccess)
+            rc = SPH_ERR_CUDA;
+        if (tp == TP_SHIFT && applies &&
+            cudaMemcpyAsync(S->Xr, S->Xr_t, sizeof(float2) * S->n, cudaMemcpyDeviceToDevice, st) != cudaSuccess)
+            rc = SPH_ERR_CUDA;
     }
     cudaEventDestroy(a);
     cudaEventDestroy(b);
-    S->shape = best_shape;
     S->timing_mask = saved_mask;
-    for (int k = 0; k < 2; ++k) {  // a captured graph holds the old shape's kernels
+    S->fs_on = saved_fs;
+    if (cudaMemsetAsync(S->words + 3, 1, sizeof(uint32_t), st) != cudaSuccess) rc = rc ? rc : SPH_ERR_CUDA;
+    for (int k = 0; k < 2; ++k) {  // a captured graph holds the old shapes' kernels
         if (S->graph[k]) cudaGraphExecDestroy(S->graph[k]);
         S->graph[k] = nullptr;
     }
-    if (shape_out) *shape_out = best_shape;
+    if (shapes_out)
+        for (int p = 0; p < TP_COUNT; ++p) shapes_out[p] = S->shape_of[p];
+    if (rc) return rc;
+    if (cudaStreamSynchronize(st) != cudaSuccess) return SPH_ERR_CUDA;
     return cudaGetLastError() == cudaSuccess ? SPH_OK : SPH_ERR_CUDA;
 }
 
@@ -2187,15 +2258,25 @@ extern "C" int sph_solver_sort_count(sph_solver_t* S, uint32_t* sorts, sph_strea
 extern "C" int sph_solver_kernel_classes(void) { return KC_COUNT; }
 
 extern "C" int sph_solver_shapes(void) { return kNumShapes; }
+extern "C" int sph_solver_tuned_passes(void) { return TP_COUNT; }
 
-extern "C" int sph_solver_set_shape(sph_solver_t* S, int32_t shape) {
-    if (!S || shape < 0 || shape >= kNumShapes) return SPH_ERR_ARGUMENT;
+extern "C" int sph_solver_set_pass_shape(sph_solver_t* S, int32_t pass, int32_t shape) {
+    if (!S || shape < 0 || shape >= kNumShapes || pass < -1 || pass >= TP_COUNT) return SPH_ERR_ARGUMENT;
     if (kShapes[shape].list16 && !S->list16) return SPH_ERR_ARGUMENT;
-    S->shape = shape;
-    for (int k = 0; k < 2; ++k) {
+    for (int p = 0; p < TP_COUNT; ++p)
+        if (pass < 0 || p == pass) S->shape_of[p] = shape;
+    for (int k = 0; k < 2; ++k) {  // a captured graph holds the old shapes' kernels
         if (S->graph[k]) cudaGraphExecDestroy(S->graph[k]);
         S->graph[k] = nullptr;
     }
+    return SPH_OK;
+}
+
+extern "C" int sph_solver_set_shape(sph_solver_t* S, int32_t shape) { return sph_solver_set_pass_shape(S, -1, shape); }
+
+extern "C" int sph_solver_pass_shapes(const sph_solver_t* S, int32_t* shapes_out) {
+    if (!S || !shapes_out) return SPH_ERR_ARGUMENT;
+    for (int p = 0; p < TP_COUNT; ++p) shapes_out[p] = S->shape_of[p];
     return SPH_OK;
 }
 

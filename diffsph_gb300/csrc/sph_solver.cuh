@@ -33,14 +33,23 @@ inline const char* kernel_class_name(int cls) {
     return (cls >= 0 && cls < KC_COUNT) ? names[cls] : nullptr;
 }
 
-// Launch shapes of the neighbor passes (warps per block, list entry width), picked per
-// problem by sph_solver_autotune; shape 0 is the default.
+// Launch shapes of the neighbor passes (warps per block, list entry width, grid), picked per
+// pass and problem by sph_solver_autotune; shape 0 is the default. Shapes 0-3 launch one
+// block per tile of 32 W slots. Shape 4 is persistent: as many blocks as the SMs hold at
+// once, each looping over the tiles blockIdx.x, blockIdx.x + gridDim.x, ... (for a packed
+// batch, the tiles of all domains in the offset-indexed slot order). The loop is a
+// separate kernel instance: it costs the passes 6-15 registers per thread, which the
+// one-tile kernels do not pay.
 struct Shape {
     int warps;
     int list16;
+    int persist;
 };
-constexpr int kNumShapes = 4;
-static const Shape kShapes[kNumShapes] = {{4, 0}, {4, 1}, {8, 1}, {16, 1}};
+constexpr int kNumShapes = 5;
+static const Shape kShapes[kNumShapes] = {{4, 0, 0}, {4, 1, 0}, {8, 1, 0}, {16, 1, 0}, {8, 1, 1}};
+// The passes the autotuner shapes separately: pass A scanning the stencil (and keeping the
+// skin list), pass A filtering the skin list, pass B, the delta+ shift, the summation density
+enum TunedPass { TP_A_SCAN = 0, TP_A_FILTER, TP_B, TP_SHIFT, TP_DENSITY, TP_COUNT };
 constexpr int kCap = 64;  // exact neighbors held per lane before the pair terms are evaluated
 constexpr int kUnroll = 4;  // stencil candidates tested per lane per step of the scan
 constexpr unsigned kFull = 0xffffffffu;
@@ -443,7 +452,8 @@ struct sph_solver {
     float2* bnormal;
     float* bdist;
     bool list16 = false;
-    int shape = 0;
+    int shape_of[TP_COUNT] = {0, 0, 0, 0, 0};  // launch shape per tuned pass
+    int grid_cap[TP_COUNT][kNumShapes] = {};   // persistent grid per pass and shape (0: not yet known)
     bool attrs_set = false;
     bool tables_uploaded = false;
     // Verlet reuse of the cell sort and the skin list across steps (single non-periodic
@@ -504,6 +514,48 @@ int surface_detect(sph_solver* S, const float4* X4, int use_skin, cudaStream_t s
 SurfaceView surface_view(const sph_solver* S);
 
 inline unsigned blocks_for(int64_t n, int threads = kBlock) { return (unsigned)((n + threads - 1) / threads); }
+
+// Blocks of a neighbor-pass launch: one per tile of 32 W slots, or for a persistent shape
+// the blocks the SMs hold at once (capped by the tiles). kern is the kernel instance,
+// smem its dynamic shared memory; the occupancy query runs once per pass and shape.
+template <class K>
+inline unsigned pass_grid(sph_solver* S, int pass, int shape, K kern, int threads, size_t smem) {
+    const unsigned tiles = blocks_for(S->n, threads);
+    if (!kShapes[shape].persist) return tiles;
+    int& cap = S->grid_cap[pass][shape];
+    if (cap == 0) {
+        int dev = 0, sms = 0, per_sm = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem);
+        cap = (sms > 0 ? sms : 1) * (per_sm > 0 ? per_sm : 1);
+    }
+    return tiles < (unsigned)cap ? tiles : (unsigned)cap;
+}
+
+// The tiles of a neighbor-pass block: body(first) for the first slot of each tile the block
+// owns, one tile (PERSIST false) or every gridDim.x-th tile from blockIdx.x on. For packed
+// batches the domain constants of the tile are staged in shared memory first (after a
+// barrier between tiles, so no warp still reads the previous tile's).
+template <bool BATCH, int W, bool PERSIST, class F>
+__device__ __forceinline__ void run_tiles(int64_t n, const Dom* __restrict__ doms, const int32_t* __restrict__ did,
+                                          Dom* s_dom, int* s_id, F&& body) {
+    const int64_t first0 = (int64_t)blockIdx.x * (32 * W);
+    if (!PERSIST) {
+        if (BATCH) stage_doms(doms, did, first0, first0 + 32 * W - 1, n, s_dom, s_id);
+        body(first0);
+        return;
+    }
+    const int64_t step = (int64_t)gridDim.x * (32 * W);
+#pragma unroll 1
+    for (int64_t first = first0; first < n; first += step) {
+        if (BATCH) {
+            if (first != first0) __syncthreads();
+            stage_doms(doms, did, first, first + 32 * W - 1, n, s_dom, s_id);
+        }
+        body(first);
+    }
+}
 
 template <typename LT, int W>
 constexpr size_t list_bytes() { return (size_t)W * kCap * 32 * sizeof(LT); }

@@ -291,23 +291,37 @@ def targets(config, k, a, b):
     return torch.cat([du, drho[:, None], dxc], dim=1)
 
 
-def generate_trajectories(n_traj, n_frames, nx, seed=0, k=4, jitter=0.1):
+def generate_trajectories(n_traj, n_frames, nx, seed=0, k=4, jitter=0.1, chunk=256):
     """Solver trajectories of random divergence-free Fourier flows on the periodic square:
-    returns (config, [[(x, u, rho) per frame] per trajectory]) with frames every k steps."""
+    returns (config, [[(x, u, rho) per frame] per trajectory]) with frames every k steps.
+    The trajectories are stepped together, up to `chunk` domains packed into one batched
+    solver (same kernel launches for all of them, k steps per captured graph replay); the
+    batch steps every domain exactly as a solver of its own would."""
     from . import scenes
+    from .solver import BatchSolver
     rng = np.random.default_rng(seed)
+    seeds = [int(rng.integers(0, 2 ** 31 - 1)) for _ in range(n_traj)]
     trajs, cfg = [], None
-    for _ in range(n_traj):
-        cfg, st = scenes.fourier_periodic(nx, seed=int(rng.integers(0, 2 ** 31 - 1)), jitter=jitter)
-        sol = Solver(cfg, st["fluid"])
-        frames = []
-        for f in range(n_frames):
-            got = sol.download()
-            frames.append((_wrap(got["positions"], cfg), got["velocities"].clone(), got["densities"].clone()))
-            if f + 1 < n_frames:
-                sol.step(k)
-        sol.check()
-        trajs.append(frames)
+    stream = torch.cuda.Stream()  # graph replays need a stream of their own
+    with torch.cuda.stream(stream):
+        for c0 in range(0, n_traj, chunk):
+            doms = [scenes.fourier_periodic(nx, seed=s, jitter=jitter) for s in seeds[c0:c0 + chunk]]
+            cfg = doms[0][0]
+            sol = BatchSolver([c for c, _ in doms], [st["fluid"] for _, st in doms])
+            frames = [[] for _ in doms]
+            for f in range(n_frames):
+                got = sol.download()
+                xs, us, rs = (sol.split(got[q]) for q in ("positions", "velocities", "densities"))
+                for d in range(len(doms)):
+                    frames[d].append((_wrap(xs[d], cfg), us[d].clone(), rs[d].clone()))
+                if f + 1 < n_frames:
+                    if k % 2 == 0:
+                        sol.graph_step(k)
+                    else:
+                        sol.step(k)
+            sol.check()
+            trajs.extend(frames)
+    torch.cuda.current_stream().wait_stream(stream)
     return cfg, trajs
 
 

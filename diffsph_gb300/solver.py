@@ -19,6 +19,8 @@ VISC_SCHEMES = {"deltaSPH_viscid": 0, "deltaSPH_inviscid": 1}
 DENSITY_SCHEMES = {"continuity": 0, "summation": 1}
 # kernel.name (parameters.py:37): the kernels evaluate the Wendland C2 kernel only
 KERNELS = ("Wendland2",)
+# the neighbor passes the autotuner shapes separately, in the C interface's order
+TUNED_PASSES = ("pass_a_scan", "pass_a_filter", "pass_b", "shift", "density_sum")
 DEFAULT_SKIN = 1.15
 
 
@@ -384,15 +386,31 @@ class Solver:
             raise _lib.SphError("sph_solver_step", 6)
 
     def autotune(self):
-        """Pick the fastest launch shape of the neighbor passes for this problem."""
+        """Pick the fastest launch shape of each neighbor pass for this problem. Returns
+        ({pass: shape}, {pass: [ms per shape, -1 where it does not apply]}) with the passes
+        named as in TUNED_PASSES."""
         k = self.lib.sph_solver_shapes()
-        ms = (ctypes.c_float * k)()
-        shape = ctypes.c_int32()
-        _lib.check("sph_solver_autotune", self.lib.sph_solver_autotune(self.handle, ctypes.byref(shape), ms, _stream()))
-        return int(shape.value), [float(v) for v in ms]
+        npass = self.lib.sph_solver_tuned_passes()
+        ms = (ctypes.c_float * (k * npass))()
+        shapes = (ctypes.c_int32 * npass)()
+        _lib.check("sph_solver_autotune", self.lib.sph_solver_autotune(self.handle, shapes, ms, _stream()))
+        names = TUNED_PASSES[:npass]
+        return ({n: int(shapes[p]) for p, n in enumerate(names)},
+                {n: [float(ms[p * k + s]) for s in range(k)] for p, n in enumerate(names)})
 
-    def set_shape(self, shape: int):
-        _lib.check("sph_solver_set_shape", self.lib.sph_solver_set_shape(self.handle, int(shape)))
+    def set_shape(self, shape: int, tuned_pass: str | None = None):
+        """Force a launch shape on every neighbor pass, or on one (a name of TUNED_PASSES)."""
+        if tuned_pass is None:
+            _lib.check("sph_solver_set_shape", self.lib.sph_solver_set_shape(self.handle, int(shape)))
+        else:
+            p = TUNED_PASSES.index(tuned_pass)
+            _lib.check("sph_solver_set_pass_shape", self.lib.sph_solver_set_pass_shape(self.handle, p, int(shape)))
+
+    def shapes(self):
+        npass = self.lib.sph_solver_tuned_passes()
+        out = (ctypes.c_int32 * npass)()
+        _lib.check("sph_solver_pass_shapes", self.lib.sph_solver_pass_shapes(self.handle, out))
+        return {n: int(out[p]) for p, n in enumerate(TUNED_PASSES[:npass])}
 
     def set_verlet_reuse(self, on: bool):
         """Keep the cell sort and the skin list across steps until a particle moved 0.034 h

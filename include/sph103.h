@@ -453,15 +453,30 @@ int sph_solver_set_verlet_scale(sph_solver_t* s, double verlet_scale);
 /* Number of cell sorts since the last upload (device counter); synchronises the stream. */
 int sph_solver_sort_count(sph_solver_t* s, uint32_t* sorts, sph_stream_t stream);
 
-/* Autotuner: times the neighbor passes under each launch shape (warps per block, width
- * of the per-warp neighbor list) on the current state and keeps the fastest for all
- * later launches. Writes the chosen shape and the time of each (ms; -1 when a shape does
- * not apply) to ms_out[sph_solver_shapes()] when non-NULL. Synchronises the stream. */
-int sph_solver_autotune(sph_solver_t* s, int32_t* shape_out, float* ms_out, sph_stream_t stream);
+/* Launch shapes of the neighbor passes: warps per block, width of the per-warp neighbor
+ * list and grid. Shapes 0-3 launch one block per tile of 32 x warps slots (0: 4 warps with
+ * 32-bit entries; 1, 2, 3: 4, 8, 16 warps with 16-bit entries); shape 4 is shape 2 under a
+ * persistent grid (as many blocks as the SMs hold at once, each looping over the tiles, for
+ * a packed batch over the tiles of every domain). Each of the sph_solver_tuned_passes() passes has its own shape, in this
+ * order: 0 pass A scanning the cell stencil (and keeping the skin list), 1 pass A filtering
+ * the skin list, 2 pass B, 3 the delta+ shift, 4 the summation density. No shape changes a
+ * result: every shape evaluates the same pairs in the same order.
+ *
+ * Autotuner: times every pass under every shape on the current state (after a cell sort
+ * at the current positions; the state itself is left unchanged) and keeps the fastest per
+ * pass. Writes the chosen shapes to shapes_out[sph_solver_tuned_passes()] and the time of
+ * each pass and shape (ms; -1 when the shape or the pass does not apply) to
+ * ms_out[pass * sph_solver_shapes() + shape] when non-NULL. Synchronises the stream. */
+int sph_solver_autotune(sph_solver_t* s, int32_t* shapes_out, float* ms_out, sph_stream_t stream);
 int sph_solver_shapes(void);
-/* Forces a launch shape (0 <= shape < sph_solver_shapes()); rejects shapes whose 16-bit
- * list entries cannot address the grid's stencils. */
+int sph_solver_tuned_passes(void);
+/* Forces a launch shape (0 <= shape < sph_solver_shapes()) on every pass, or on one
+ * (0 <= pass < sph_solver_tuned_passes(); -1: all); rejects shapes whose 16-bit list
+ * entries cannot address the grid's stencils. */
 int sph_solver_set_shape(sph_solver_t* s, int32_t shape);
+int sph_solver_set_pass_shape(sph_solver_t* s, int32_t pass, int32_t shape);
+/* The shape of each pass, shapes_out[sph_solver_tuned_passes()]. */
+int sph_solver_pass_shapes(const sph_solver_t* s, int32_t* shapes_out);
 
 /* Number of kernel launches one sph_solver_step(s, 1, ...) issues (with the delta+ shift;
  * an implicit shift replaces its one launch by 2 + 5 per iteration of its solve). */

@@ -187,6 +187,27 @@ def test_layer_gradients_match_oracle(C, rel):
     assert rel(_np(ht.grad), dho) < 1e-4
 
 
+def test_training_data_comes_from_the_batched_solver():
+    """generate_trajectories packs its trajectories into one batched solver (graph replays of
+    k steps); every frame equals a single-domain solver's run of the same initial condition,
+    bit for bit."""
+    from diffsph_gb300 import scenes
+    from diffsph_gb300.learned import _wrap, generate_trajectories
+    from diffsph_gb300.solver import Solver
+    cfg, trajs = generate_trajectories(3, 3, 24, seed=5, k=4, chunk=2)
+    rng = np.random.default_rng(5)
+    assert len(trajs) == 3 and all(len(t) == 3 for t in trajs)
+    for t in range(3):
+        c, st = scenes.fourier_periodic(24, seed=int(rng.integers(0, 2 ** 31 - 1)), jitter=0.1)
+        sol = Solver(c, st["fluid"])
+        for f in range(3):
+            got = sol.download()
+            assert torch.equal(_wrap(got["positions"], c), trajs[t][f][0]), (t, f)
+            assert torch.equal(got["velocities"], trajs[t][f][1]), (t, f)
+            assert torch.equal(got["densities"], trajs[t][f][2]), (t, f)
+            sol.step(4)
+
+
 def test_trained_network_beats_the_method_without_it():
     """Trains on 8 solver trajectories of 32^2-particle periodic Fourier flows (24 frames,
     one every 4 steps) and evaluates on a held-out trajectory: the learned 4-step update

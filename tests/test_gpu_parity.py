@@ -254,9 +254,10 @@ def test_ten_steps_track_oracle():
     assert rel_max(_np(got["densities"]) - 1.0, s["fluid"]["densities"] - 1.0) < 1e-3
 
 
-@pytest.mark.parametrize("shape", [0, 1, 2, 3])
+@pytest.mark.parametrize("shape", list(range(5)))
 def test_every_launch_shape_gives_the_same_step(shape):
-    """All launch shapes of the autotuner evaluate the same pairs in the same order."""
+    """All launch shapes of the autotuner (4, 8, 16 warps; 32- or 16-bit lists; one block
+    per tile or a persistent grid) evaluate the same pairs in the same order."""
     cfg, st = scenes.dam_break(dx=1.0 / 32)
     a = _solver(cfg, st)
     a.step(2)
@@ -272,13 +273,63 @@ def test_every_launch_shape_gives_the_same_step(shape):
 def test_autotune_picks_a_shape_and_keeps_parity():
     cfg, st = scenes.fourier_periodic(64, seed=4)
     a = _solver(cfg, st)
-    shape, ms = a.autotune()
-    assert 0 <= shape < len(ms) and ms[shape] > 0
+    shapes, ms = a.autotune()
+    assert shapes == a.shapes()
+    for p in ("pass_a_scan", "pass_b", "shift"):
+        assert 0 <= shapes[p] < len(ms[p]) and ms[p][shapes[p]] > 0
+        assert ms[p][shapes[p]] == min(v for v in ms[p] if v > 0)
+    # a periodic domain never filters a skin list; the continuity scheme sums no densities
+    assert max(ms["pass_a_filter"]) < 0 and max(ms["density_sum"]) < 0
     a.step(1)
     b = _solver(cfg, st)
     b.step(1)
     ga, gb = a.download(), b.download()
     assert torch.equal(ga["velocities"], gb["velocities"])
+
+
+def test_autotune_per_pass_on_the_dam_break_leaves_the_state_and_the_steps_unchanged():
+    """The tuner runs every pass (the shift too) on the current state without moving it, and
+    a Verlet-reuse solver steps on like an untuned one (up to the order of the pair sums:
+    the tuner sorts at the current positions, the untuned solver keeps its older order)."""
+    cfg, st = scenes.dam_break(dx=1.0 / 64)
+    a = _solver(cfg, st)
+    a.set_verlet_reuse(True)
+    a.step(2)
+    before = a.download()
+    shapes, ms = a.autotune()
+    after = a.download()
+    for k in ("positions", "velocities", "densities"):
+        assert torch.equal(before[k], after[k]), k
+    assert max(ms["pass_a_filter"]) > 0 and max(ms["shift"]) > 0
+    a.step(3)
+    a.check()
+    b = _solver(cfg, st)
+    b.set_verlet_reuse(True)
+    b.step(5)
+    ga, gb = a.download(), b.download()
+    d = float(cfg["particle"]["dx"])
+    assert float((ga["positions"] - gb["positions"]).abs().max()) < 1e-5 * d
+    assert rel_max(_np(ga["velocities"]), _np(gb["velocities"])) < 1e-5
+    assert rel_max(_np(ga["densities"]), _np(gb["densities"])) < 1e-6
+
+
+def test_per_pass_shapes_mix_in_one_batched_step():
+    """Different shapes per pass (persistent and one-block-per-tile grids mixed) on a packed
+    batch give the same state as the default shape."""
+    from diffsph_gb300.solver import BatchSolver
+    doms = [scenes.fourier_periodic(nx, seed=20 + nx, jitter=0.1) for nx in (24, 40, 33)]
+    a = BatchSolver([c for c, _ in doms], [s["fluid"] for _, s in doms])
+    b = BatchSolver([c for c, _ in doms], [s["fluid"] for _, s in doms])
+    b.set_shape(4, "pass_a_scan")
+    b.set_shape(3, "pass_b")
+    b.set_shape(4, "shift")
+    assert b.shapes()["pass_b"] == 3 and b.shapes()["shift"] == 4
+    a.step(3)
+    b.step(3)
+    b.check()
+    ga, gb = a.download(), b.download()
+    for k in ("positions", "velocities", "densities"):
+        assert torch.equal(ga[k], gb[k]), k
 
 
 def test_reference_runner_loop_with_dropins():
