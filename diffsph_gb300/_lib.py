@@ -82,6 +82,7 @@ EXPORTS = [
     "sph_solver_set_shape", "sph_solver_tuned_passes", "sph_solver_set_pass_shape", "sph_solver_pass_shapes",
     "sph_batch_workspace_bytes", "sph_batch_create", "sph_solver_graph_step",
     "sph_neighbor_count_static", "sph_solver_vjp_rates", "sph_solver_vjp_gradient", "sph_solver_vjp_shift",
+    "sph_solver_vjp_walls",
     "sph_gemm_bf16_tn", "sph_cconv_aggregate", "sph_cconv_aggregate_t", "sph_cconv_aggregate_tc",
     "sph_neighbor_fill_csr", "sph_solver_ips_workspace_bytes", "sph_solver_set_ips", "sph_solver_ips_result",
     "sph_solver_free_surface_workspace_bytes", "sph_solver_set_free_surface", "sph_solver_free_surface_fields",
@@ -114,9 +115,10 @@ def load(build_if_missing: bool = False):
         "sph_neighbor_count": ([P, I64, P, P, I64, DP, ctypes.c_double, P, SZ, P, P, P], ctypes.c_int),
         "sph_neighbor_fill": ([P, I64, P, P, I64, DP, ctypes.c_double, P, SZ, P, I64, P, P, P, P, P, P, P, P],
                               ctypes.c_int),
-        "sph_solver_vjp_rates": ([P, P, P, P, P, P, P, P, P], ctypes.c_int),
-        "sph_solver_vjp_gradient": ([P, P, P, P, P], ctypes.c_int),
-        "sph_solver_vjp_shift": ([P, P, P, P, P, P], ctypes.c_int),
+        "sph_solver_vjp_rates": ([P, P, P, P, P, P, P, P, P, P], ctypes.c_int),
+        "sph_solver_vjp_gradient": ([P, P, P, P, P, P], ctypes.c_int),
+        "sph_solver_vjp_shift": ([P, P, P, P, P, P, P], ctypes.c_int),
+        "sph_solver_vjp_walls": ([P, P, P, P, P], ctypes.c_int),
         "sph_gemm_bf16_tn": ([P, P, P, I64, I64, I64, I64, I64, I64, I32, P, P], ctypes.c_int),
         "sph_cconv_aggregate": ([P, I64, P, P, DP, ctypes.c_double, ctypes.c_double, P, I32, I32, P, P],
                                 ctypes.c_int),

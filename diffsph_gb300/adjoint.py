@@ -1,24 +1,27 @@
 """Reverse-mode gradients of plain delta-SPH rollouts on the sm_103a VJP kernels.
 
-Scope: one periodic (or open) fluid-only domain with the viscid deltaSPH viscosity, the
-symplectic Euler step of the reference runner (integration.py:357-392, both density
-updates) followed by delta+ shifting (shifting.py:119-147, 882-1019). The reference has no
+Scope: one periodic or walled (mDBC) domain with either deltaSPH viscosity (and the
+boundary viscosity), gravity, the symplectic Euler step of the reference runner
+(integration.py:357-392, both density updates) followed by delta+ shifting
+(shifting.py:119-147, 882-1019) without the free-surface handling. The reference has no
 adjoint of its own: it differentiates its torch operators with autograd step by step.
 
-One step z = (x, u, rho) -> z'' is, with rates (a, drho) = RHS(z) (simulationStep):
+One step z = (x, u, rho) -> z'' is, with rates (a, drho) = RHS(z, rho_b(z)) (simulationStep;
+rho_b(z) the mDBC wall densities extrapolated from the fluid state z):
 
     stage 1   x_h = x + dt/2 u,  u_h = u + dt/2 a(z),  rho_h = rho + dt/2 drho(z)
     stage 2   u'  = u + dt a(z_h),  x' = x + dt (u + u')/2,
               rho' = rho_h                                    (density update 'reference')
               rho' = rho (2 - e)/(2 + e), e = -dt drho(z_h)/rho_h   ('rational')
-    shift     x'' = x' + clamp(dx(x', rho', Ma(u'))),  u'' = u',  rho'' = rho'
+    shift     x'' = x' + clamp(dx(x', rho', rho_b(z_h), Ma(u'))),  u'' = u',  rho'' = rho'
 
-The backward pass runs those three lines in reverse; the operator VJPs (shift, RHS pass B
-and the renormalised density gradient, pass A) are the CUDA kernels of libsph103.so,
-the elementwise integrator algebra is done here in torch. ``rollout`` checkpoints the
-state every ``checkpoint_every`` steps of the fused forward and recomputes a segment's
-stage states when its turn comes in the backward pass, so memory stays at
-O(n / checkpoint_every + checkpoint_every) states.
+The backward pass runs those three lines in reverse; the operator VJPs (shift, RHS pass B,
+the renormalised density gradient of pass A and the mDBC extrapolation) are the CUDA
+kernels of libsph103.so, the elementwise integrator algebra is done here in torch. The wall
+densities' adjoint of the shift and of stage 2 meets at z_h, where one mDBC VJP returns it
+to the fluid. ``rollout`` checkpoints the state every ``checkpoint_every`` steps of the
+fused forward and recomputes a segment's stage states when its turn comes in the backward
+pass, so memory stays at O(n / checkpoint_every + checkpoint_every) states.
 """
 from __future__ import annotations
 
@@ -48,28 +51,46 @@ class _Consts:
 
 def _check_scope(config):
     diff = config.get("diffusion", {})
-    if diff.get("velocityScheme", "deltaSPH_inviscid") != "deltaSPH_viscid":
-        raise ValueError("the adjoint covers the deltaSPH_viscid viscosity")
-    if config.get("boundary", {}).get("active", False):
-        raise ValueError("the adjoint covers fluid-only domains")
+    if diff.get("velocityScheme", "deltaSPH_inviscid") not in ("deltaSPH_viscid", "deltaSPH_inviscid"):
+        raise ValueError("the adjoint covers the deltaSPH_viscid and deltaSPH_inviscid viscosities")
     if config.get("integration", {}).get("scheme", "symplecticEuler") != "symplecticEuler":
         raise ValueError("the adjoint covers the symplecticEuler scheme")
+    if config.get("simulation", {}).get("densityScheme", "continuity") != "continuity":
+        raise ValueError("the adjoint covers the continuity density")
+    sh = config.get("shifting", {})
+    if sh.get("scheme", "deltaSPH") != "deltaSPH" or sh.get("freeSurface", False):
+        raise ValueError("the adjoint covers the delta+ shift without the free-surface handling")
+    if config.get("regions"):
+        raise ValueError("the adjoint covers domains without inlet/outlet regions")
 
 
 def _state(x, u, rho):
     return {"positions": x, "velocities": u, "densities": rho}
 
 
+def _walls(sol: Solver, densities=None):
+    """The solver's wall particles for an upload (None for a fluid-only domain)."""
+    if not sol.nB:
+        return None
+    b = dict(sol.boundary)
+    if densities is not None:
+        b["densities"] = densities
+    return b
+
+
 def step_stages(sol: Solver, C: _Consts, x, u, rho, shift: bool = True):
     """Stage states of one step from (x, u, rho), evaluated operator by operator with the
-    fused step's operation order. Returns (z0, z_half, z_int, z_next, drho_half)."""
-    sol.upload(_state(x, u, rho))
+    fused step's operation order. Returns (z0, z_half, z_int, z_next, drho_half, rho_b_half)
+    with rho_b_half the wall densities of stage 2 (which the shift reads; empty without
+    walls)."""
+    sol.upload(_state(x, u, rho), _walls(sol))
     r1 = sol.rhs()
     xh = x + u * C.dth
     uh = u + r1["dudt"] * C.dth
     rh = rho + r1["drhodt"] * C.dth
-    sol.upload(_state(xh, uh, rh))
+    sol.upload(_state(xh, uh, rh), _walls(sol))
     r2 = sol.rhs()
+    rbh = r2["boundary_densities"] if sol.nB else torch.zeros(0, device=x.device)
     u1 = u + r2["dudt"] * C.dt
     x1 = x + (0.5 * (u + u1)) * C.dt
     if C.rational:
@@ -78,28 +99,32 @@ def step_stages(sol: Solver, C: _Consts, x, u, rho, shift: bool = True):
     else:
         rho1 = rh.clone()
     if shift:
-        sol.upload(_state(x1, u1, rho1))
+        sol.upload(_state(x1, u1, rho1), _walls(sol, rbh))
         x2 = x1 + sol.shift()
     else:
         x2 = x1.clone()
-    return (x, u, rho), (xh, uh, rh), (x1, u1, rho1), (x2, u1.clone(), rho1.clone()), r2["drhodt"]
+    return (x, u, rho), (xh, uh, rh), (x1, u1, rho1), (x2, u1.clone(), rho1.clone()), r2["drhodt"], rbh
 
 
 def step_vjp(sol: Solver, C: _Consts, stages, xbar2, ubar2, rbar2, shift: bool = True):
     """Adjoint of one step: from the adjoints of z'' to those of z (and of nu)."""
-    (x, u, rho), (xh, uh, rh), (x1, u1, rho1), _, drho_h = stages
+    (x, u, rho), (xh, uh, rh), (x1, u1, rho1), _, drho_h, rbh = stages
     n = x.shape[0]
     dev = x.device
     nu_part = torch.empty(n, device=dev)
     nubar = torch.zeros((), dtype=torch.float64, device=dev)
-    # shift: x'' = x' + dx(x', rho', Ma(u'))
+    walls = sol.nB > 0
+    # adjoints of the wall densities of stage 2 (read by the shift too) and of stage 1
+    wbar_h = torch.zeros(sol.nB, device=dev) if walls else None
+    wbar_0 = torch.zeros(sol.nB, device=dev) if walls else None
+    # shift: x'' = x' + dx(x', rho', rho_b(z_h), Ma(u'))
     xbar1 = torch.zeros_like(x)
     rbar1 = rbar2.clone()
     ubar1 = ubar2.clone()
     if shift:
-        sol.upload(_state(x1, u1, rho1))
+        sol.upload(_state(x1, u1, rho1), _walls(sol, rbh))
         mach = torch.empty(n, device=dev)
-        sol.vjp_shift(xbar2, xbar1, rbar1, mach)
+        sol.vjp_shift(xbar2, xbar1, rbar1, mach, wbar_h)
         if C.compute_mach:
             # Ma = max|u'| / cs: the adjoint goes to the arg-max particle (no host sync)
             sp = torch.linalg.vector_norm(u1, dim=1)
@@ -125,26 +150,30 @@ def step_vjp(sol: Solver, C: _Consts, stages, xbar2, ubar2, rbar2, shift: bool =
         rbar_h += ebar * (C.dt * drho_h / rh ** 2)
     else:
         rbar_h += rbar1
-    # pass B (and pass A when drho(z_h) has an adjoint) at z_h
-    sol.upload(_state(xh, uh, rh))
+    # pass B (and pass A when drho(z_h) has an adjoint) at z_h, then the wall densities of z_h
+    sol.upload(_state(xh, uh, rh), _walls(sol))
     xbar_h = torch.zeros_like(x)
     ubar_h = torch.zeros_like(u)
     gbar_h = torch.zeros_like(x) if drbar_h is not None else None
-    sol.vjp_rates(abar_h, drbar_h, xbar_h, ubar_h, rbar_h, gbar_h, nu_part)
+    sol.vjp_rates(abar_h, drbar_h, xbar_h, ubar_h, rbar_h, gbar_h, nu_part, wbar_h)
     nubar += nu_part.double().sum()
     if gbar_h is not None:
-        sol.vjp_gradient(gbar_h, xbar_h, rbar_h)
+        sol.vjp_gradient(gbar_h, xbar_h, rbar_h, wbar_h)
+    if walls:
+        sol.vjp_walls(wbar_h, xbar_h, rbar_h)
     # stage 1: x_h = x + dt/2 u; u_h = u + dt/2 a(z); rho_h = rho + dt/2 drho(z)
     xbar += xbar_h
     ubar += C.dth * xbar_h + ubar_h
     rbar += rbar_h
     abar0 = C.dth * ubar_h
     drbar0 = C.dth * rbar_h
-    sol.upload(_state(x, u, rho))
+    sol.upload(_state(x, u, rho), _walls(sol))
     gbar0 = torch.zeros_like(x)
-    sol.vjp_rates(abar0, drbar0, xbar, ubar, rbar, gbar0, nu_part)
+    sol.vjp_rates(abar0, drbar0, xbar, ubar, rbar, gbar0, nu_part, wbar_0)
     nubar += nu_part.double().sum()
-    sol.vjp_gradient(gbar0, xbar, rbar)
+    sol.vjp_gradient(gbar0, xbar, rbar, wbar_0)
+    if walls:
+        sol.vjp_walls(wbar_0, xbar, rbar)
     return xbar, ubar, rbar, nubar
 
 
@@ -158,7 +187,7 @@ def _forward(sol, x0, u0, rho0, n_steps, every, shift, use_graphs=False):
     """Fused forward; returns the final state and the checkpoints {step: (x, u, rho)}."""
     graphed = use_graphs and shift and torch.cuda.current_stream().cuda_stream != 0
     ckpt = {}
-    sol.upload(_state(x0, u0, rho0))
+    sol.upload(_state(x0, u0, rho0), _walls(sol))
     k = 0
     while k < n_steps:
         got = sol.download()
@@ -180,12 +209,15 @@ def _forward(sol, x0, u0, rho0, n_steps, every, shift, use_graphs=False):
 
 
 def _flat(st):
-    (x, u, rho), (xh, uh, rh), (x1, u1, r1), (x2, u2, r2), dr = st
-    return [x, u, rho, xh, uh, rh, x1, u1, r1, x2, u2, r2, dr]
+    (x, u, rho), (xh, uh, rh), (x1, u1, r1), (x2, u2, r2), dr, rbh = st
+    return [x, u, rho, xh, uh, rh, x1, u1, r1, x2, u2, r2, dr, rbh]
+
+
+_TAPE = 14  # tensors per step in a flat tape
 
 
 def _unflat(t):
-    return (tuple(t[0:3]), tuple(t[3:6]), tuple(t[6:9]), tuple(t[9:12]), t[12])
+    return (tuple(t[0:3]), tuple(t[3:6]), tuple(t[6:9]), tuple(t[9:12]), t[12], t[13])
 
 
 class _Replay:
@@ -221,7 +253,7 @@ class _Graphs:
         self.sol, self.C, self.shift = sol, C, shift
         self._rec = None
         self._vjp = None
-        sorts = (1 if shift else 0) + 3 + (1 if C.rational else 0)
+        sorts = (1 if shift else 0) + 3 + (1 if C.rational else 0) + (2 if sol.nB else 0)
         self.group = 1 if sorts % 2 == 0 else 2
 
     def two_steps(self, x, u, rho):
@@ -232,17 +264,17 @@ class _Graphs:
                 return _flat(a) + _flat(b)
             self._rec = _Replay(fn, [x, u, rho])
         out = [t.clone() for t in self._rec(x, u, rho)]
-        return _unflat(out[:13]), _unflat(out[13:])
+        return _unflat(out[:_TAPE]), _unflat(out[_TAPE:])
 
     def vjp(self, tapes, xbar, ubar, rbar):
         if self._vjp is None:
             G = self.group
 
             def fn(*args):
-                xb, ub, rb = args[13 * G:]
+                xb, ub, rb = args[_TAPE * G:]
                 nb = torch.zeros((), dtype=torch.float64, device=xb.device)
                 for g in reversed(range(G)):
-                    xb, ub, rb, n1 = step_vjp(self.sol, self.C, _unflat(args[13 * g:13 * (g + 1)]), xb, ub, rb,
+                    xb, ub, rb, n1 = step_vjp(self.sol, self.C, _unflat(args[_TAPE * g:_TAPE * (g + 1)]), xb, ub, rb,
                                               self.shift)
                     nb = nb + n1
                 return xb, ub, rb, nb
@@ -285,9 +317,12 @@ class Rollout(torch.autograd.Function):
     def forward(ctx, x0, u0, rho0, nu, config, n_steps, every, shift, fluid_extra, use_graphs=True):
         _check_scope(config)
         cfg = _with_nu(config, float(nu))
-        fluid = dict(fluid_extra)
+        fluid = {k: v for k, v in fluid_extra.items() if k != "boundary"}
         fluid.update(_state(x0.detach(), u0.detach(), rho0.detach()))
-        sol = Solver(cfg, fluid)
+        sol = Solver(cfg, fluid, fluid_extra.get("boundary"))
+        # sort every step, as the stage replay of the backward pass does (same pair order)
+        if sol.verlet_reuse:
+            sol.set_verlet_reuse(False)
         (x, u, rho), ckpt = _forward(sol, x0.detach(), u0.detach(), rho0.detach(), n_steps, every, shift,
                                      use_graphs)
         ctx.sol, ctx.ckpt, ctx.C = sol, ckpt, _Consts(cfg)
@@ -311,10 +346,12 @@ class Rollout(torch.autograd.Function):
 
 
 def rollout(config, fluid, n_steps, nu=None, checkpoint_every=25, shift=True, x0=None, u0=None, rho0=None,
-            use_graphs=True):
+            use_graphs=True, boundary=None):
     """Differentiable rollout of ``n_steps`` steps. Tensors x0 / u0 / rho0 / nu (defaults:
-    the fluid dict's fields and config['diffusion']['nu']) may require grad. use_graphs
-    replays the forward steps and the backward pass from CUDA graphs (same results)."""
+    the fluid dict's fields and config['diffusion']['nu']) may require grad. ``boundary``:
+    the static mDBC wall particles of a walled domain (positions, normals, distances,
+    masses, supports). use_graphs replays the forward steps and the backward pass from CUDA
+    graphs (same results)."""
     _check_scope(config)
     dev = "cuda"
 
@@ -327,16 +364,19 @@ def rollout(config, fluid, n_steps, nu=None, checkpoint_every=25, shift=True, x0
     if nu is None:
         nu = torch.tensor(float(config["diffusion"]["nu"]), dtype=torch.float64)
     extra = {k: fluid[k] for k in ("masses", "supports") if k in fluid}
+    if boundary is not None and config.get("boundary", {}).get("active", True):
+        extra["boundary"] = boundary
     return Rollout.apply(x0, u0, rho0, nu, config, int(n_steps), int(checkpoint_every), bool(shift), extra,
                          bool(use_graphs))
 
 
-def rollout_loss_and_grad(config, fluid, target_u, n_steps, checkpoint_every=25, shift=True, use_graphs=True):
+def rollout_loss_and_grad(config, fluid, target_u, n_steps, checkpoint_every=25, shift=True, use_graphs=True,
+                          boundary=None):
     """Loss = mean((u_n - target)^2) over all velocity components; returns (loss, du0, dnu)."""
     u0 = torch.as_tensor(fluid["velocities"]).to("cuda", torch.float32).clone().requires_grad_(True)
     nu = torch.tensor(float(config["diffusion"]["nu"]), dtype=torch.float64, requires_grad=True)
     _, u, _ = rollout(config, fluid, n_steps, nu=nu, checkpoint_every=checkpoint_every, shift=shift, u0=u0,
-                      use_graphs=use_graphs)
+                      use_graphs=use_graphs, boundary=boundary)
     tgt = torch.as_tensor(target_u).to("cuda", torch.float32)
     loss = torch.mean((u - tgt) ** 2)
     loss.backward()

@@ -174,25 +174,14 @@ __device__ __forceinline__ float2 mdbc_ghost(const Phys& P, float2 xb, float2 nr
     return make_float2(__fadd_rn(xb.x, __fmul_rn(mapd, nrm.x)), __fadd_rn(xb.y, __fmul_rn(mapd, nrm.y)));
 }
 
+// The 13 moments of one ghost over the fluid candidates of its cell stencil, lane-strided
+// over the flat candidate index with a fixed xor-shuffle tree: every lane of the warp ends
+// with the totals (k_mdbc_sums and its adjoint k_mdbc_vjp sum in exactly this order).
 template <bool PER>
-__global__ void __launch_bounds__(128) k_mdbc_sums(int nB, const int32_t* __restrict__ bidx,
-                                                   const int32_t* __restrict__ uid, const float2* __restrict__ Xr,
-                                                   const float4* __restrict__ X4, const float2* __restrict__ bnormal,
-                                                   const float* __restrict__ bdist,
-                                                   const int32_t* __restrict__ start, Grid g, Phys P,
-                                                   float* __restrict__ sums) {
-    const int lane = threadIdx.x & 31;
-    const int k = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-    if (k >= nB) return;  // warp-uniform
-    const int s = bidx[k];
-    const int b = uid[s] - P.nF;
-    const float2 gp = mdbc_ghost(P, Xr[s], bnormal[b], bdist[b]);
-    const float2 gw = wrap_pos(gp, P.geo);
-    int rs[kMaxRanges], re[kMaxRanges];
-    const int nr = stencil_ranges(gw, g, start, rs, re);
+__device__ __forceinline__ void mdbc_moments(const Phys& P, float2 gw, const int* rs, const int* re, int nr,
+                                             const float4* __restrict__ X4, int lane, float acc[13]) {
     int total = 0;
     for (int a = 0; a < nr; ++a) total += re[a] - rs[a];
-    float acc[13];
 #pragma unroll
     for (int q = 0; q < 13; ++q) acc[q] = 0.f;
     int r = 0, base = 0;  // range of the lane's current flat index and the flat start of that range
@@ -236,6 +225,26 @@ __global__ void __launch_bounds__(128) k_mdbc_sums(int nB, const int32_t* __rest
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) acc[q] += __shfl_xor_sync(kFull, acc[q], o);
     }
+}
+
+template <bool PER>
+__global__ void __launch_bounds__(128) k_mdbc_sums(int nB, const int32_t* __restrict__ bidx,
+                                                   const int32_t* __restrict__ uid, const float2* __restrict__ Xr,
+                                                   const float4* __restrict__ X4, const float2* __restrict__ bnormal,
+                                                   const float* __restrict__ bdist,
+                                                   const int32_t* __restrict__ start, Grid g, Phys P,
+                                                   float* __restrict__ sums) {
+    const int lane = threadIdx.x & 31;
+    const int k = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (k >= nB) return;  // warp-uniform
+    const int s = bidx[k];
+    const int b = uid[s] - P.nF;
+    const float2 gp = mdbc_ghost(P, Xr[s], bnormal[b], bdist[b]);
+    const float2 gw = wrap_pos(gp, P.geo);
+    int rs[kMaxRanges], re[kMaxRanges];
+    const int nr = stencil_ranges(gw, g, start, rs, re);
+    float acc[13];
+    mdbc_moments<PER>(P, gw, rs, re, nr, X4, lane, acc);
     if (lane < 13) {
         float v = acc[0];
 #pragma unroll
@@ -825,12 +834,15 @@ __global__ void k_dom_keys(int64_t n, const float4* __restrict__ X4, const int32
 
 
 // ======================================================================================
-// Adjoint of the fluid-only, viscid delta-SPH step: vector-Jacobian products of pass A,
-// pass B and the shift, in gather form. With a uniform support the exact neighbor relation
-// is symmetric, so particle k collects, over its neighbors j, the derivative of its own
-// pair terms T_kj (with its own multipliers) and of the neighbors' terms T_jk with respect
-// to k's variables (with the neighbors' multipliers): the transpose of the neighbor list
-// is walked without atomics. Derivatives are those of the exact expressions with
+// Adjoint of the delta-SPH step: vector-Jacobian products of pass A, pass B and the shift,
+// in gather form. With a uniform support the exact neighbor relation is symmetric, so
+// particle k collects, over its neighbors j, the derivative of its own pair terms T_kj
+// (with its own multipliers) and of the neighbors' terms T_jk with respect to k's
+// variables (with the neighbors' multipliers): the transpose of the neighbor list is walked
+// without atomics. Wall particles (mDBC) have no terms of their own; they collect the
+// derivatives of their fluid neighbors' terms with respect to the wall density and
+// pressure, which k_mdbc_vjp then pulls back to the fluid state the densities were
+// extrapolated from. Derivatives are those of the exact expressions with
 // grad W_ij = f(r) x_ij, f = -20 C/h^4 (1-q)^3, f' = 60 C/h^5 (1-q)^2.
 // ======================================================================================
 // Each particle's pairs are spread over kAdjL lanes: lane sub of the group scans candidates
@@ -977,22 +989,81 @@ __device__ __forceinline__ BVjp pairB_vjp(float2 x, float r, float2 ui, float2 u
     return o;
 }
 
-// multipliers of pass B from the adjoints of the rates (original order in, sorted order out)
+// gradients of lam . T_ib for the pair terms of fluid particle i with wall particle b (wall
+// velocity 0): pressure, continuity and the boundary viscosity (no density diffusion)
+struct BWVjp {
+    float2 gx, gui;
+    float gri, grb, gpi, gpb;
+};
+
+__device__ __forceinline__ BWVjp pairBW_vjp(float2 x, float r, float2 ui, float ri, float rb, float pi, float pb,
+                                            float2 lP, float2 lB, float lC, const Phys& P) {
+    BWVjp o;
+    KD k = kern_fd(r, P);
+    float ir = 1.f / r, irb = 1.f / rb;
+    float2 xh = f2(x.x * ir, x.y * ir);
+    // pressure: (p_i + p_b)/rho_b f x
+    float lPx = dot2(lP, x);
+    float sP = (pi + pb) * irb;
+    o.gx = f2(sP * (k.f * lP.x + lPx * k.fp * xh.x), sP * (k.f * lP.y + lPx * k.fp * xh.y));
+    o.gpi = o.gpb = k.f * lPx * irb;
+    o.grb = -sP * k.f * lPx * irb;
+    o.gri = 0.f;
+    // continuity: (u_b - u_i) . x f / rho_b = -(u_i . x) f / rho_b
+    float ux = dot2(ui, x);
+    o.gx.x += lC * irb * (-ui.x * k.f - ux * k.fp * xh.x);
+    o.gx.y += lC * irb * (-ui.y * k.f - ux * k.fp * xh.y);
+    o.gui = f2(-lC * k.f * irb * x.x, -lC * k.f * irb * x.y);
+    o.grb += lC * ux * k.f * irb * irb;
+    // boundary viscosity: (u_i . x) phi f D x, phi = 1 / (r (r + eps_b h^2)),
+    // D = 1 / (rho_i + rho_b) (boundaryViscosity) or 1 / rho_b
+    float D = P.bvisc ? 1.f / (ri + rb) : irb;
+    float lBx = dot2(lB, x);
+    float phi = 1.f / (r * (r + P.bv_eps));
+    float phip = -(2.f * r + P.bv_eps) * phi * phi;
+    float pf = phi * k.f, pfp = phip * k.f + phi * k.fp;
+    float cB = pf * D;
+    o.gx.x += (ui.x * lBx + lB.x * ux) * cB + ux * lBx * D * pfp * xh.x;
+    o.gx.y += (ui.y * lBx + lB.y * ux) * cB + ux * lBx * D * pfp * xh.y;
+    o.gui.x += x.x * lBx * cB;
+    o.gui.y += x.y * lBx * cB;
+    float EB = ux * lBx * cB;
+    o.grb -= EB * D;
+    if (P.bvisc) o.gri -= EB * D;
+    return o;
+}
+
+__device__ __forceinline__ float eos_dpdr(float rho, const Phys& P) {
+    // p = B ((rho/rho0)^gamma - 1): dp/drho = B gamma (rho/rho0)^(gamma-1) / rho0
+    return P.eos.B * P.eos.gamma * powf(rho / P.eos.rho0, P.eos.gamma - 1.f) / P.eos.rho0;
+}
+
+// multipliers of pass B from the adjoints of the rates (original order in, sorted order out);
+// wall particles have no rates and carry none
 __global__ void k_lam_rates(int64_t n, const float4* __restrict__ X4, const int32_t* __restrict__ uid, Dom D,
                             const float* __restrict__ abar, const float* __restrict__ drbar,
                             float4* __restrict__ L4, float4* __restrict__ L2) {
     int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= n) return;
     const Phys& P = D.P;
-    int o = uid[s];
     float rho = X4[s].z;
+    if (is_boundary(rho)) {
+        L4[s] = make_float4(0.f, 0.f, 0.f, 0.f);
+        L2[s] = make_float4(0.f, 0.f, 0.f, 0.f);
+        return;
+    }
+    int o = uid[s];
     float2 a = f2(abar[2 * o], abar[2 * o + 1]);
     float dr = drbar ? drbar[o] : 0.f;
     float mr = P.m / rho;
     L4[s] = make_float4(-mr * a.x, -mr * a.y, P.v_num * mr * a.x, P.v_num * mr * a.y);
-    L2[s] = make_float4(-P.m * rho * dr, P.diff_coef * P.m * dr, 0.f, 0.f);
+    L2[s] = make_float4(-P.m * rho * dr, P.diff_coef * P.m * dr, P.bv_num * mr * a.x, P.bv_num * mr * a.y);
 }
 
+// Fluid particle k: its own pair terms and its fluid neighbors' terms, as for a fluid-only
+// domain, plus its own terms with wall neighbors. Wall particle k: the derivatives of its
+// fluid neighbors' terms with respect to its density and pressure, folded into the wall
+// density's adjoint rbbar (original wall order).
 template <bool PER>
 __global__ void __launch_bounds__(128) k_vjp_rates(int64_t n, const float4* __restrict__ X4,
                                                    const float4* __restrict__ V4, const int32_t* __restrict__ start,
@@ -1000,7 +1071,8 @@ __global__ void __launch_bounds__(128) k_vjp_rates(int64_t n, const float4* __re
                                                    const float4* __restrict__ L4, const float4* __restrict__ L2,
                                                    uint32_t* __restrict__ words, float* __restrict__ xbar,
                                                    float* __restrict__ ubar, float* __restrict__ rbar,
-                                                   float* __restrict__ Gbar, float* __restrict__ nup) {
+                                                   float* __restrict__ Gbar, float* __restrict__ nup,
+                                                   float* __restrict__ rbbar) {
     __shared__ int32_t s_list[4][kCap * 32];
     const Phys& P = D.P;
     const Grid& g = D.g;
@@ -1010,50 +1082,84 @@ __global__ void __launch_bounds__(128) k_vjp_rates(int64_t n, const float4* __re
     float4 vk = inb ? V4[k] : make_float4(0.f, 0.f, 0.f, 0.f);
     float4 lk4 = inb ? L4[k] : make_float4(0.f, 0.f, 0.f, 0.f);
     float4 lk2 = inb ? L2[k] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const bool kb = is_boundary(xk.z);
+    const float rk = fabsf(xk.z);
     float2 pk = f2(xk.x, xk.y);
     float2 gx = f2(0.f, 0.f), gu = f2(0.f, 0.f), gG = f2(0.f, 0.f);
     float gr = 0.f, gp = 0.f;
-    float2 Ps = f2(0.f, 0.f), Vs = f2(0.f, 0.f);
+    float2 Ps = f2(0.f, 0.f), Vs = f2(0.f, 0.f), Bs = f2(0.f, 0.f);
     float Cs = 0.f;
     neighbor_loop_split<PER>(inb, pk, X4, start + D.cell0, g, P, s_list[threadIdx.x >> 5], [&](int j) {
         if (j == (int)k) return;
         float4 xj = __ldg(&X4[j]);
-        float4 vj = __ldg(&V4[j]);
-        float4 lj4 = __ldg(&L4[j]);
-        float4 lj2 = __ldg(&L2[j]);
+        const bool jb = is_boundary(xj.z);
+        if (kb && jb) return;
         float x0, x1;
         pair_vec<PER>(pk, make_float2(xj.x, xj.y), P.geo, x0, x1);
         float sq = sq_norm_ref(x0, x1);
         float r = sqrtf(sq);
         if (r <= 0.f) return;
+        const float rj = fabsf(xj.z);
         float2 x = f2(x0, x1);
-        float2 uk = f2(vk.x, vk.y), uj = f2(vj.x, vj.y);
-        float2 Gk = f2(vk.z, vk.w), Gj = f2(vj.z, vj.w);
-        // k's own pair term T_kj
-        BVjp a = pairB_vjp(x, r, uk, uj, xk.z, xj.z, xk.w, xj.w, Gk, Gj, f2(lk4.x, lk4.y), f2(lk4.z, lk4.w), lk2.x,
-                           lk2.y, P);
-        // the neighbor's pair term T_jk (pair vector x_j - x_k = -x)
-        BVjp b = pairB_vjp(f2(-x0, -x1), r, uj, uk, xj.z, xk.z, xj.w, xk.w, Gj, Gk, f2(lj4.x, lj4.y),
-                           f2(lj4.z, lj4.w), lj2.x, lj2.y, P);
-        gx.x += a.gx.x - b.gx.x;
-        gx.y += a.gx.y - b.gx.y;
-        gu.x += a.gui.x + b.guj.x;
-        gu.y += a.gui.y + b.guj.y;
-        gr += a.gri + b.grj;
-        gp += a.gpi + b.gpj;
-        gG.x += a.gGi.x + b.gGj.x;
-        gG.y += a.gGi.y + b.gGj.y;
-        // forward sums of k (for the derivatives of the 1/rho_k and rho_k prefactors)
-        KD kd = kern_fd(r, P);
-        float irj = 1.f / xj.z;
-        float sP = (xk.w + xj.w) * irj * kd.f;
-        Ps.x += sP * x0;
-        Ps.y += sP * x1;
-        float ux = (uk.x - uj.x) * x0 + (uk.y - uj.y) * x1;
-        float sV = ux / (r * (r + P.v_eps)) * kd.f * irj;
-        Vs.x += sV * x0;
-        Vs.y += sV * x1;
-        Cs += -ux * kd.f * irj;
+        float2 uk = f2(vk.x, vk.y);
+        if (!kb && !jb) {
+            float4 vj = __ldg(&V4[j]);
+            float4 lj4 = __ldg(&L4[j]);
+            float4 lj2 = __ldg(&L2[j]);
+            float2 uj = f2(vj.x, vj.y);
+            float2 Gk = f2(vk.z, vk.w), Gj = f2(vj.z, vj.w);
+            // k's own pair term T_kj
+            BVjp a = pairB_vjp(x, r, uk, uj, rk, rj, xk.w, xj.w, Gk, Gj, f2(lk4.x, lk4.y), f2(lk4.z, lk4.w), lk2.x,
+                               lk2.y, P);
+            // the neighbor's pair term T_jk (pair vector x_j - x_k = -x)
+            BVjp b = pairB_vjp(f2(-x0, -x1), r, uj, uk, rj, rk, xj.w, xk.w, Gj, Gk, f2(lj4.x, lj4.y),
+                               f2(lj4.z, lj4.w), lj2.x, lj2.y, P);
+            gx.x += a.gx.x - b.gx.x;
+            gx.y += a.gx.y - b.gx.y;
+            gu.x += a.gui.x + b.guj.x;
+            gu.y += a.gui.y + b.guj.y;
+            gr += a.gri + b.grj;
+            gp += a.gpi + b.gpj;
+            gG.x += a.gGi.x + b.gGj.x;
+            gG.y += a.gGi.y + b.gGj.y;
+            // forward sums of k (for the derivatives of the 1/rho_k and rho_k prefactors)
+            KD kd = kern_fd(r, P);
+            float irj = 1.f / rj;
+            float sP = (xk.w + xj.w) * irj * kd.f;
+            Ps.x += sP * x0;
+            Ps.y += sP * x1;
+            float ux = (uk.x - uj.x) * x0 + (uk.y - uj.y) * x1;
+            float sV = ux / (r * (r + P.v_eps)) * kd.f * irj;
+            Vs.x += sV * x0;
+            Vs.y += sV * x1;
+            Cs += -ux * kd.f * irj;
+        } else if (!kb) {  // fluid k, wall j: k's own term
+            BWVjp a = pairBW_vjp(x, r, uk, rk, rj, xk.w, xj.w, f2(lk4.x, lk4.y), f2(lk2.z, lk2.w), lk2.x, P);
+            gx.x += a.gx.x;
+            gx.y += a.gx.y;
+            gu.x += a.gui.x;
+            gu.y += a.gui.y;
+            gr += a.gri;
+            gp += a.gpi;
+            KD kd = kern_fd(r, P);
+            float irj = 1.f / rj;
+            float sP = (xk.w + xj.w) * irj * kd.f;
+            Ps.x += sP * x0;
+            Ps.y += sP * x1;
+            float ux = uk.x * x0 + uk.y * x1;
+            Cs += -ux * kd.f * irj;
+            float sB = ux / (r * (r + P.bv_eps)) * kd.f * (P.bvisc ? 1.f / (rk + rj) : irj);
+            Bs.x += sB * x0;
+            Bs.y += sB * x1;
+        } else {  // wall k, fluid j: j's term with respect to the wall's density and pressure
+            float4 vj = __ldg(&V4[j]);
+            float4 lj4 = __ldg(&L4[j]);
+            float4 lj2 = __ldg(&L2[j]);
+            BWVjp b = pairBW_vjp(f2(-x0, -x1), r, f2(vj.x, vj.y), rj, rk, xj.w, xk.w, f2(lj4.x, lj4.y),
+                                 f2(lj2.z, lj2.w), lj2.x, P);
+            gr += b.grb;
+            gp += b.gpb;
+        }
     });
     gx.x = group_sum(gx.x);
     gx.y = group_sum(gx.y);
@@ -1067,13 +1173,18 @@ __global__ void __launch_bounds__(128) k_vjp_rates(int64_t n, const float4* __re
     Ps.y = group_sum(Ps.y);
     Vs.x = group_sum(Vs.x);
     Vs.y = group_sum(Vs.y);
+    Bs.x = group_sum(Bs.x);
+    Bs.y = group_sum(Bs.y);
     Cs = group_sum(Cs);
     if (!inb || (threadIdx.x & (kAdjL - 1)) != 0) return;
     int o = uid[k];
-    float rho = xk.z;
-    // p = B ((rho/rho0)^gamma - 1): dp/drho = B gamma (rho/rho0)^(gamma-1) / rho0
-    float dpdr = P.eos.B * P.eos.gamma * powf(rho / P.eos.rho0, P.eos.gamma - 1.f) / P.eos.rho0;
-    gr += gp * dpdr - (lk4.x * Ps.x + lk4.y * Ps.y) / rho - (lk4.z * Vs.x + lk4.w * Vs.y) / rho + lk2.x * Cs / rho;
+    if (kb) {
+        if (rbbar) rbbar[o - P.nF] += gr + gp * eos_dpdr(rk, P);
+        return;
+    }
+    float rho = rk;
+    gr += gp * eos_dpdr(rho, P) - (lk4.x * Ps.x + lk4.y * Ps.y) / rho - (lk4.z * Vs.x + lk4.w * Vs.y) / rho -
+          (lk2.z * Bs.x + lk2.w * Bs.y) / rho + lk2.x * Cs / rho;
     xbar[2 * o] += gx.x;
     xbar[2 * o + 1] += gx.y;
     ubar[2 * o] += gu.x;
@@ -1087,8 +1198,10 @@ __global__ void __launch_bounds__(128) k_vjp_rates(int64_t n, const float4* __re
     if (nup) nup[o] = -P.dvnum_dnu * (lk4.x * Vs.x + lk4.y * Vs.y);
 }
 
-// pass A: per-particle multipliers of g = sum (rho_i - rho_j)/rho_j f x and of
-// M = -sum f/rho_j x x^T from the adjoint of gradRho^L = m L g, L = (m M)^-1
+// pass A: per-particle multipliers of g_f = sum_fluid (rho_i - rho_j)/rho_j f x, of
+// g_b = sum_walls (rho_i - rho_b)/rho_b f x and of M = -sum_all f/rho_j x x^T from the
+// adjoint of gradRho^L = m (L g_f + g_b), L = (m M)^-1: Lg.xy = m L^T G (fluid pairs),
+// Lg.zw = m G (wall pairs); walls carry none
 template <bool PER>
 __global__ void __launch_bounds__(128) k_lam_grad(int64_t n, const float4* __restrict__ X4,
                                                   const int32_t* __restrict__ start, Dom D,
@@ -1100,25 +1213,30 @@ __global__ void __launch_bounds__(128) k_lam_grad(int64_t n, const float4* __res
     int64_t k = ((int64_t)blockIdx.x * 128 + threadIdx.x) / kAdjL;
     bool inb = k < n;
     float4 xk = inb ? X4[k] : make_float4(0.f, 0.f, 1.f, 0.f);
+    const bool kb = is_boundary(xk.z);
     float2 pk = f2(xk.x, xk.y);
     float M00 = 0.f, M01 = 0.f, M10 = 0.f, M11 = 0.f, g0 = 0.f, g1 = 0.f;
     int nf = 0;
-    neighbor_loop_split<PER>(inb, pk, X4, start + D.cell0, D.g, P, s_list[threadIdx.x >> 5], [&](int j) {
+    neighbor_loop_split<PER>(inb && !kb, pk, X4, start + D.cell0, D.g, P, s_list[threadIdx.x >> 5], [&](int j) {
         float4 xj = __ldg(&X4[j]);
+        const bool jb = is_boundary(xj.z);
         float x0, x1;
         pair_vec<PER>(pk, make_float2(xj.x, xj.y), P.geo, x0, x1);
-        ++nf;
+        if (!jb) ++nf;
         if (j == (int)k) return;
         float r = sqrtf(sq_norm_ref(x0, x1));
         KD kd = kern_fd(r, P);
-        float w = kd.f / xj.z;
+        const float rj = fabsf(xj.z);
+        float w = kd.f / rj;
         M00 -= w * x0 * x0;
         M01 -= w * x0 * x1;
         M10 -= w * x1 * x0;
         M11 -= w * x1 * x1;
-        float c = (xk.z - xj.z) * w;
-        g0 += c * x0;
-        g1 += c * x1;
+        if (!jb) {
+            float c = (xk.z - rj) * w;
+            g0 += c * x0;
+            g1 += c * x1;
+        }
     });
     M00 = group_sum(M00);
     M01 = group_sum(M01);
@@ -1128,6 +1246,11 @@ __global__ void __launch_bounds__(128) k_lam_grad(int64_t n, const float4* __res
     g1 = group_sum(g1);
     nf = (int)group_sum((float)nf);
     if (!inb || (threadIdx.x & (kAdjL - 1)) != 0) return;
+    if (kb) {
+        LM[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+        Lg[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+        return;
+    }
     int o = uid[k];
     float m = P.m;
     float G0 = Gbar[2 * o], G1 = Gbar[2 * o + 1];
@@ -1152,7 +1275,7 @@ __global__ void __launch_bounds__(128) k_lam_grad(int64_t n, const float4* __res
         mb11 = -(t10 * L.c + t11 * L.d);
     }
     LM[k] = make_float4(m * mb00, m * mb01, m * mb10, m * mb11);
-    Lg[k] = make_float4(gb0, gb1, 0.f, 0.f);
+    Lg[k] = make_float4(gb0, gb1, m * G0, m * G1);
 }
 
 __device__ __forceinline__ void pairA_vjp(float2 x, float r, float ri, float rj, float2 lg, float4 lM, const Phys& P,
@@ -1180,7 +1303,8 @@ __global__ void __launch_bounds__(128) k_vjp_grad(int64_t n, const float4* __res
                                                   const int32_t* __restrict__ start, Dom D,
                                                   const int32_t* __restrict__ uid, const float4* __restrict__ LM,
                                                   const float4* __restrict__ Lg, uint32_t* __restrict__ words,
-                                                  float* __restrict__ xbar, float* __restrict__ rbar) {
+                                                  float* __restrict__ xbar, float* __restrict__ rbar,
+                                                  float* __restrict__ rbbar) {
     __shared__ int32_t s_list[4][kCap * 32];
     const Phys& P = D.P;
     int64_t k = ((int64_t)blockIdx.x * 128 + threadIdx.x) / kAdjL;
@@ -1188,37 +1312,59 @@ __global__ void __launch_bounds__(128) k_vjp_grad(int64_t n, const float4* __res
     float4 xk = inb ? X4[k] : make_float4(0.f, 0.f, 1.f, 0.f);
     float4 lMk = inb ? LM[k] : make_float4(0.f, 0.f, 0.f, 0.f);
     float4 lgk = inb ? Lg[k] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const bool kb = is_boundary(xk.z);
+    const float rk = fabsf(xk.z);
     float2 pk = f2(xk.x, xk.y);
     float2 gx = f2(0.f, 0.f);
     float gr = 0.f;
     neighbor_loop_split<PER>(inb, pk, X4, start + D.cell0, D.g, P, s_list[threadIdx.x >> 5], [&](int j) {
         if (j == (int)k) return;
         float4 xj = __ldg(&X4[j]);
-        float4 lMj = __ldg(&LM[j]);
-        float4 lgj = __ldg(&Lg[j]);
+        const bool jb = is_boundary(xj.z);
+        if (kb && jb) return;
         float x0, x1;
         pair_vec<PER>(pk, make_float2(xj.x, xj.y), P.geo, x0, x1);
         float r = sqrtf(sq_norm_ref(x0, x1));
         if (r <= 0.f) return;
+        const float rj = fabsf(xj.z);
         float2 ga, gb;
         float ari, arj, bri, brj;
-        pairA_vjp(f2(x0, x1), r, xk.z, xj.z, f2(lgk.x, lgk.y), lMk, P, ga, ari, arj);
-        pairA_vjp(f2(-x0, -x1), r, xj.z, xk.z, f2(lgj.x, lgj.y), lMj, P, gb, bri, brj);
-        gx.x += ga.x - gb.x;
-        gx.y += ga.y - gb.y;
-        gr += ari + brj;
+        if (!kb && !jb) {
+            float4 lMj = __ldg(&LM[j]);
+            float4 lgj = __ldg(&Lg[j]);
+            pairA_vjp(f2(x0, x1), r, rk, rj, f2(lgk.x, lgk.y), lMk, P, ga, ari, arj);
+            pairA_vjp(f2(-x0, -x1), r, rj, rk, f2(lgj.x, lgj.y), lMj, P, gb, bri, brj);
+            gx.x += ga.x - gb.x;
+            gx.y += ga.y - gb.y;
+            gr += ari + brj;
+        } else if (!kb) {  // fluid k, wall j: k's own term (the boundary part of the gradient)
+            pairA_vjp(f2(x0, x1), r, rk, rj, f2(lgk.z, lgk.w), lMk, P, ga, ari, arj);
+            gx.x += ga.x;
+            gx.y += ga.y;
+            gr += ari;
+        } else {  // wall k, fluid j: j's term with respect to the wall's density
+            float4 lMj = __ldg(&LM[j]);
+            float4 lgj = __ldg(&Lg[j]);
+            pairA_vjp(f2(-x0, -x1), r, rj, rk, f2(lgj.z, lgj.w), lMj, P, gb, bri, brj);
+            gr += brj;
+        }
     });
     gx.x = group_sum(gx.x);
     gx.y = group_sum(gx.y);
     gr = group_sum(gr);
     if (!inb || (threadIdx.x & (kAdjL - 1)) != 0) return;
     int o = uid[k];
+    if (kb) {
+        if (rbbar) rbbar[o - P.nF] += gr;
+        return;
+    }
     xbar[2 * o] += gx.x;
     xbar[2 * o + 1] += gx.y;
     rbar[o] += gr;
 }
 
-// shift: multipliers from the adjoint of the shifted positions (clamped components carry none)
+// shift: multipliers from the adjoint of the shifted positions (clamped components carry
+// none); walls are not shifted and carry none
 template <bool PER>
 __global__ void __launch_bounds__(128) k_lam_shift(int64_t n, const float4* __restrict__ X4,
                                                    const int32_t* __restrict__ start, Dom D,
@@ -1230,9 +1376,10 @@ __global__ void __launch_bounds__(128) k_lam_shift(int64_t n, const float4* __re
     int64_t k = ((int64_t)blockIdx.x * 128 + threadIdx.x) / kAdjL;
     bool inb = k < n;
     float4 xk = inb ? X4[k] : make_float4(0.f, 0.f, 1.f, 0.f);
+    const bool kb = is_boundary(xk.z);
     float2 pk = f2(xk.x, xk.y);
     float s0 = 0.f, s1 = 0.f;
-    neighbor_loop_split<PER>(inb, pk, X4, start + D.cell0, D.g, P, s_list[threadIdx.x >> 5], [&](int j) {
+    neighbor_loop_split<PER>(inb && !kb, pk, X4, start + D.cell0, D.g, P, s_list[threadIdx.x >> 5], [&](int j) {
         if (j == (int)k) return;
         float4 xj = __ldg(&X4[j]);
         float x0, x1;
@@ -1242,13 +1389,17 @@ __global__ void __launch_bounds__(128) k_lam_shift(int64_t n, const float4* __re
         float W = wendland_w(r * P.inv_h, P.kc);
         float kk = W * P.invW0;
         float w = 1.f + P.shR * (kk * kk) * (kk * kk);
-        float c = w * kd.f / (xk.z + xj.z);
+        float c = w * kd.f / (xk.z + fabsf(xj.z));
         s0 += c * x0;
         s1 += c * x1;
     });
     s0 = group_sum(s0);
     s1 = group_sum(s1);
     if (!inb || (threadIdx.x & (kAdjL - 1)) != 0) return;
+    if (kb) {
+        LS[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+        return;
+    }
     int o = uid[k];
     float Ma = P.compute_mach ? __uint_as_float(maxv[0]) * P.inv_cs : 0.1f;
     float sc = P.sh_scale * P.m;
@@ -1281,41 +1432,230 @@ __global__ void __launch_bounds__(128) k_vjp_shift(int64_t n, const float4* __re
                                                    const int32_t* __restrict__ start, Dom D,
                                                    const int32_t* __restrict__ uid, const float4* __restrict__ LS,
                                                    const float* __restrict__ xbar_new, uint32_t* __restrict__ words,
-                                                   float* __restrict__ xbar, float* __restrict__ rbar) {
+                                                   float* __restrict__ xbar, float* __restrict__ rbar,
+                                                   float* __restrict__ rbbar) {
     __shared__ int32_t s_list[4][kCap * 32];
     const Phys& P = D.P;
     int64_t k = ((int64_t)blockIdx.x * 128 + threadIdx.x) / kAdjL;
     bool inb = k < n;
     float4 xk = inb ? X4[k] : make_float4(0.f, 0.f, 1.f, 0.f);
     float4 lk = inb ? LS[k] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const bool kb = is_boundary(xk.z);
+    const float rk = fabsf(xk.z);
     float2 pk = f2(xk.x, xk.y);
     float2 gx = f2(0.f, 0.f);
     float gr = 0.f;
     neighbor_loop_split<PER>(inb, pk, X4, start + D.cell0, D.g, P, s_list[threadIdx.x >> 5], [&](int j) {
         if (j == (int)k) return;
         float4 xj = __ldg(&X4[j]);
-        float4 lj = __ldg(&LS[j]);
+        const bool jb = is_boundary(xj.z);
+        if (kb && jb) return;
         float x0, x1;
         pair_vec<PER>(pk, make_float2(xj.x, xj.y), P.geo, x0, x1);
         float r = sqrtf(sq_norm_ref(x0, x1));
         if (r <= 0.f) return;
+        const float rj = fabsf(xj.z);
         float2 ga, gb;
         float ari, arj, bri, brj;
-        pairS_vjp(f2(x0, x1), r, xk.z, xj.z, f2(lk.x, lk.y), P, ga, ari, arj);
-        pairS_vjp(f2(-x0, -x1), r, xj.z, xk.z, f2(lj.x, lj.y), P, gb, bri, brj);
-        gx.x += ga.x - gb.x;
-        gx.y += ga.y - gb.y;
-        gr += ari + brj;
+        if (!kb) {
+            pairS_vjp(f2(x0, x1), r, rk, rj, f2(lk.x, lk.y), P, ga, ari, arj);
+            gx.x += ga.x;
+            gx.y += ga.y;
+            gr += ari;
+        }
+        if (!jb) {  // the fluid neighbor's term
+            float4 lj = __ldg(&LS[j]);
+            pairS_vjp(f2(-x0, -x1), r, rj, rk, f2(lj.x, lj.y), P, gb, bri, brj);
+            if (!kb) {
+                gx.x -= gb.x;
+                gx.y -= gb.y;
+            }
+            gr += brj;
+        }
     });
     gx.x = group_sum(gx.x);
     gx.y = group_sum(gx.y);
     gr = group_sum(gr);
     if (!inb || (threadIdx.x & (kAdjL - 1)) != 0) return;
     int o = uid[k];
+    if (kb) {
+        if (rbbar) rbbar[o - P.nF] += gr;
+        return;
+    }
     // x'' = x' + delta(x'): the identity part plus the shift's Jacobian
     xbar[2 * o] += xbar_new[2 * o] + gx.x;
     xbar[2 * o + 1] += xbar_new[2 * o + 1] + gx.y;
     rbar[o] += gr;
+}
+
+// The 13 ghost moments of mdbc_moments in fp64 (the adjoint's solve: near free edges the
+// moment matrix reaches condition numbers of ~1e4, where fp32 moments would cost the
+// derivative ~1e-3 of its accuracy)
+template <bool PER>
+__device__ __forceinline__ void mdbc_moments_f64(const Phys& P, float2 gw, const int* rs, const int* re, int nr,
+                                                 const float4* __restrict__ X4, int lane, double acc[13]) {
+    int total = 0;
+    for (int a = 0; a < nr; ++a) total += re[a] - rs[a];
+#pragma unroll
+    for (int q = 0; q < 13; ++q) acc[q] = 0.0;
+    int r = 0, base = 0;
+    for (int t = lane; t < total; t += 32) {
+        while (t >= base + (re[r] - rs[r])) {
+            base += re[r] - rs[r];
+            ++r;
+        }
+        const int j = rs[r] + (t - base);
+        const float4 xj = __ldg(&X4[j]);
+        if (is_boundary(xj.z)) continue;
+        float x0, x1;
+        pair_vec<PER>(gw, make_float2(xj.x, xj.y), P.geo, x0, x1);
+        const float sq = sq_norm_ref(x0, x1);
+        if (sq > P.T) continue;
+        const double dr = sqrt((double)sq);
+        const double q = dr * P.inv_h;
+        const double om = 1.0 - q;
+        const double W = om * om * om * om * (1.0 + 4.0 * q) * P.kc.cw;
+        const double W1 = -20.0 * q * om * om * om * P.kc.cg;
+        const double e0 = dr > 0.0 ? x0 / dr : 0.0, e1 = dr > 0.0 ? x1 / dr : 0.0;
+        const double g0 = W1 * e0, g1 = W1 * e1;
+        const double V = (double)P.m / xj.z;
+        const double xi0 = -(double)x0, xi1 = -(double)x1;
+        acc[0] += P.m * W;
+        acc[1] += V * W;
+        acc[2] += P.m * g0;
+        acc[3] += P.m * g1;
+        acc[4] += V * g0;
+        acc[5] += V * g1;
+        acc[6] += xi0 * V * W;
+        acc[7] += xi1 * V * W;
+        acc[8] += xi0 * V * g0;
+        acc[9] += xi0 * V * g1;
+        acc[10] += xi1 * V * g0;
+        acc[11] += xi1 * V * g1;
+        acc[12] += 1.0;
+    }
+#pragma unroll
+    for (int q = 0; q < 13; ++q) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) acc[q] += __shfl_xor_sync(kFull, acc[q], o);
+    }
+}
+
+// mDBC adjoint: the wall densities' adjoint rbbar (original wall order) pulled back to the
+// fluid positions and densities the ghost moments read (mDBC.py:50-163 as k_mdbc_sums /
+// k_mdbc_solve evaluate it). One warp per wall particle recomputes its ghost's moments (in
+// fp64); every lane then forms the adjoints of the 13 moments from the fp64 solve
+// (y = A^+ b, rho_b = c . y with c = (1, x_b - x_ghost): bbar = A^+T c rhobar,
+// Abar = -bbar y^T; the Shepard branch rho_b = num / (den + 1e-7)) and adds its fluid
+// candidates' derivatives into fp64 accumulators by slot (the sums are rounded to fp32
+// once, by k_wall_adjoint_fin). With d = x_ghost - x_j, V = m / rho_j, g = W'(r) d/r and
+// xi = -d, the moments of one fluid particle are m W, V W, m g, V g, xi V W and xi (x) V g.
+template <bool PER>
+__global__ void __launch_bounds__(128) k_mdbc_vjp(int nB, const int32_t* __restrict__ bidx,
+                                                  const int32_t* __restrict__ uid, const float2* __restrict__ Xr,
+                                                  const float4* __restrict__ X4, const float2* __restrict__ bnormal,
+                                                  const float* __restrict__ bdist, const int32_t* __restrict__ start,
+                                                  Grid g, Phys P, const float* __restrict__ rbbar,
+                                                  double* __restrict__ xacc, double* __restrict__ racc) {
+    const int lane = threadIdx.x & 31;
+    const int k = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (k >= nB) return;  // warp-uniform
+    const int s = bidx[k];
+    const int b = uid[s] - P.nF;
+    const float rhobar = rbbar[b];
+    if (rhobar == 0.f) return;  // warp-uniform
+    const float2 xb = Xr[s];
+    const float2 gp = mdbc_ghost(P, xb, bnormal[b], bdist[b]);
+    const float2 gw = wrap_pos(gp, P.geo);
+    int rs[kMaxRanges], re[kMaxRanges];
+    const int nr = stencil_ranges(gw, g, start, rs, re);
+    double a[13];
+    mdbc_moments_f64<PER>(P, gw, rs, re, nr, X4, lane, a);
+    const int cnt = (int)a[12];
+    double sb[12];
+#pragma unroll
+    for (int q = 0; q < 12; ++q) sb[q] = 0.0;
+    if (cnt > 5) {
+        double A[9] = {a[1], a[6], a[7], a[4], a[8], a[9], a[5], a[10], a[11]};
+        double Pi[9];
+        pinv3_f64(A, Pi, 3.0 * 1.1920928955078125e-07);
+        const double bv[3] = {a[0], a[2], a[3]};
+        double y[3];
+        for (int r = 0; r < 3; ++r) y[r] = Pi[3 * r] * bv[0] + Pi[3 * r + 1] * bv[1] + Pi[3 * r + 2] * bv[2];
+        const float rel0 = __fsub_rn(xb.x, gp.x), rel1 = __fsub_rn(xb.y, gp.y);
+        const double yb[3] = {(double)rhobar, (double)rel0 * rhobar, (double)rel1 * rhobar};
+        double bb[3];
+        for (int c = 0; c < 3; ++c) bb[c] = Pi[c] * yb[0] + Pi[3 + c] * yb[1] + Pi[6 + c] * yb[2];
+        sb[0] = bb[0];
+        sb[2] = bb[1];
+        sb[3] = bb[2];
+        // A's entries and the moments they hold: (den, xi0 VW, xi1 VW; V g0, xi0 V g0, xi0 V g1;
+        // V g1, xi1 V g0, xi1 V g1)
+        const int mom[9] = {1, 6, 7, 4, 8, 9, 5, 10, 11};
+        for (int r = 0; r < 3; ++r)
+            for (int c = 0; c < 3; ++c) sb[mom[3 * r + c]] = -bb[r] * y[c];
+    } else if (cnt > 0) {
+        const double dd = a[1] + 1e-7;
+        sb[0] = rhobar / dd;
+        sb[1] = -rhobar * a[0] / (dd * dd);
+    } else {
+        return;
+    }
+    int total = 0;
+    for (int q = 0; q < nr; ++q) total += re[q] - rs[q];
+    const float cg20 = -20.f * P.kc.cg * P.inv_h;
+    int r = 0, base = 0;
+    for (int t = lane; t < total; t += 32) {
+        while (t >= base + (re[r] - rs[r])) {
+            base += re[r] - rs[r];
+            ++r;
+        }
+        const int j = rs[r] + (t - base);
+        const float4 xj = __ldg(&X4[j]);
+        if (is_boundary(xj.z)) continue;
+        float d0, d1;
+        pair_vec<PER>(gw, make_float2(xj.x, xj.y), P.geo, d0, d1);
+        const float sq = sq_norm_ref(d0, d1);
+        if (sq > P.T) continue;
+        const double dr = sqrt((double)sq);
+        const double q = dr * P.inv_h;
+        const double om = 1.0 - q;
+        const double Wv = om * om * om * om * (1.0 + 4.0 * q) * P.kc.cw;
+        const double W1 = -20.0 * q * om * om * om * P.kc.cg;   // dW/dr
+        const double Wr = (double)cg20 * om * om * om;           // W'/r
+        const double W2 = (double)cg20 * om * om * (1.0 - 4.0 * q);  // d2W/dr2
+        const double e0 = dr > 0.0 ? d0 / dr : 0.0, e1 = dr > 0.0 ? d1 / dr : 0.0;
+        const double g0 = W1 * e0, g1 = W1 * e1;
+        const double V = (double)P.m / xj.z;
+        const double xi0 = -(double)d0, xi1 = -(double)d1;
+        // E = cW W + cg . g (+ the xi dependence below)
+        const double cW = sb[0] * P.m + sb[1] * V + V * (sb[6] * xi0 + sb[7] * xi1);
+        const double cg0 = sb[2] * P.m + sb[4] * V + V * (sb[8] * xi0 + sb[10] * xi1);
+        const double cg1 = sb[3] * P.m + sb[5] * V + V * (sb[9] * xi0 + sb[11] * xi1);
+        // Jg cg, Jg = W2 e e^T + Wr (I - e e^T)
+        const double ec = e0 * cg0 + e1 * cg1;
+        const double J0 = W2 * ec * e0 + Wr * (cg0 - ec * e0), J1 = W2 * ec * e1 + Wr * (cg1 - ec * e1);
+        const double Gd0 = cW * W1 * e0 + J0 - V * Wv * sb[6] - V * (sb[8] * g0 + sb[9] * g1);
+        const double Gd1 = cW * W1 * e1 + J1 - V * Wv * sb[7] - V * (sb[10] * g0 + sb[11] * g1);
+        // the V-proportional moments, for d/d rho_j (V = m / rho_j)
+        const double VE = V * (sb[1] * Wv + sb[4] * g0 + sb[5] * g1 + Wv * (sb[6] * xi0 + sb[7] * xi1) +
+                               sb[8] * xi0 * g0 + sb[9] * xi0 * g1 + sb[10] * xi1 * g0 + sb[11] * xi1 * g1);
+        atomicAdd(&xacc[2 * (int64_t)j], -Gd0);
+        atomicAdd(&xacc[2 * (int64_t)j + 1], -Gd1);
+        atomicAdd(&racc[j], -VE / xj.z);
+    }
+}
+
+__global__ void k_wall_adjoint_fin(int64_t n, int nF, const int32_t* __restrict__ uid,
+                                   const double* __restrict__ xacc, const double* __restrict__ racc,
+                                   float* __restrict__ xbar, float* __restrict__ rbar) {
+    const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const int o = uid[s];
+    if (o >= nF) return;
+    xbar[2 * o] += (float)xacc[2 * s];
+    xbar[2 * o + 1] += (float)xacc[2 * s + 1];
+    rbar[o] += (float)racc[s];
 }
 
 }  // namespace sph
@@ -2074,59 +2414,65 @@ extern "C" int sph_solver_autotune(sph_solver_t* S, int32_t* shapes_out, float* 
 
 
 // ------------------------------------------------------------------------------------
-// Adjoint entry points (single fluid-only domain, viscid viscosity), evaluated at the
-// current state; gradients accumulate (+=) into the caller's arrays (original order).
+// Adjoint entry points (single domain, delta+ shift without the free-surface handling,
+// continuity density), evaluated at the current state; gradients accumulate (+=) into the
+// caller's arrays (original order). With walls the wall-density adjoint accumulates into
+// rhob_bar (original wall order), which sph_solver_vjp_walls pulls back to the fluid.
 // ------------------------------------------------------------------------------------
 static int adjoint_ok(sph_solver* S) {
-    if (!S || S->nd != 1 || S->nB != 0 || S->prm.visc_scheme != 0 || summation(S)) return SPH_ERR_ARGUMENT;
+    if (!S || S->nd != 1 || summation(S) || S->ips || S->fs_on) return SPH_ERR_ARGUMENT;
     return SPH_OK;
 }
 
 extern "C" int sph_solver_vjp_rates(sph_solver_t* S, const float* abar, const float* drbar, float* xbar, float* ubar,
-                                    float* rbar, float* Gbar, float* nu_part, sph_stream_t stream) {
+                                    float* rbar, float* Gbar, float* nu_part, float* rhob_bar, sph_stream_t stream) {
     int rc = adjoint_ok(S);
     if (rc) return rc;
-    if (!abar || !xbar || !ubar || !rbar) return SPH_ERR_ARGUMENT;
+    if (!abar || !xbar || !ubar || !rbar || (S->nB > 0 && !rhob_bar)) return SPH_ERR_ARGUMENT;
     cudaStream_t st = (cudaStream_t)stream;
     if ((rc = rebuild(S, st))) return rc;
     RhsOut none = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    launch_mdbc(S, S->Xc, nullptr, st);   // the wall densities of the current state
     launch_a(S, S->Xc, S->Vc, none, st);  // gradRho^L of the current state (pass-B inputs)
     const Dom& D = S->doms_host[0];
     k_lam_rates<<<blocks_for(S->n), kBlock, 0, st>>>(S->n, S->Xc, S->uid, D, abar, drbar, S->Xh, S->Xf);
     unsigned gb = blocks_for(S->n * kAdjL, 128);  // kAdjL lanes per particle
     if (S->periodic)
         k_vjp_rates<true><<<gb, 128, 0, st>>>(S->n, S->Xc, S->Vc, S->start, D, S->uid, S->Xh, S->Xf, S->words, xbar,
-                                              ubar, rbar, Gbar, nu_part);
+                                              ubar, rbar, Gbar, nu_part, rhob_bar);
     else
         k_vjp_rates<false><<<gb, 128, 0, st>>>(S->n, S->Xc, S->Vc, S->start, D, S->uid, S->Xh, S->Xf, S->words, xbar,
-                                               ubar, rbar, Gbar, nu_part);
+                                               ubar, rbar, Gbar, nu_part, rhob_bar);
     return cudaGetLastError() == cudaSuccess ? SPH_OK : SPH_ERR_CUDA;
 }
 
-extern "C" int sph_solver_vjp_gradient(sph_solver_t* S, const float* Gbar, float* xbar, float* rbar,
+extern "C" int sph_solver_vjp_gradient(sph_solver_t* S, const float* Gbar, float* xbar, float* rbar, float* rhob_bar,
                                        sph_stream_t stream) {
     int rc = adjoint_ok(S);
     if (rc) return rc;
-    if (!Gbar || !xbar || !rbar) return SPH_ERR_ARGUMENT;
+    if (!Gbar || !xbar || !rbar || (S->nB > 0 && !rhob_bar)) return SPH_ERR_ARGUMENT;
     cudaStream_t st = (cudaStream_t)stream;
     if ((rc = rebuild(S, st))) return rc;
+    launch_mdbc(S, S->Xc, nullptr, st);  // the wall densities of the current state
     const Dom& D = S->doms_host[0];
     unsigned gb = blocks_for(S->n * kAdjL, 128);  // kAdjL lanes per particle
     if (S->periodic) {
         k_lam_grad<true><<<gb, 128, 0, st>>>(S->n, S->Xc, S->start, D, S->uid, Gbar, S->words, S->Xh, S->Xf);
-        k_vjp_grad<true><<<gb, 128, 0, st>>>(S->n, S->Xc, S->start, D, S->uid, S->Xh, S->Xf, S->words, xbar, rbar);
+        k_vjp_grad<true><<<gb, 128, 0, st>>>(S->n, S->Xc, S->start, D, S->uid, S->Xh, S->Xf, S->words, xbar, rbar,
+                                             rhob_bar);
     } else {
         k_lam_grad<false><<<gb, 128, 0, st>>>(S->n, S->Xc, S->start, D, S->uid, Gbar, S->words, S->Xh, S->Xf);
-        k_vjp_grad<false><<<gb, 128, 0, st>>>(S->n, S->Xc, S->start, D, S->uid, S->Xh, S->Xf, S->words, xbar, rbar);
+        k_vjp_grad<false><<<gb, 128, 0, st>>>(S->n, S->Xc, S->start, D, S->uid, S->Xh, S->Xf, S->words, xbar, rbar,
+                                              rhob_bar);
     }
     return cudaGetLastError() == cudaSuccess ? SPH_OK : SPH_ERR_CUDA;
 }
 
 extern "C" int sph_solver_vjp_shift(sph_solver_t* S, const float* xbar_new, float* xbar, float* rbar,
-                                    float* mach_part, sph_stream_t stream) {
+                                    float* mach_part, float* rhob_bar, sph_stream_t stream) {
     int rc = adjoint_ok(S);
     if (rc) return rc;
-    if (!xbar_new || !xbar || !rbar || !mach_part) return SPH_ERR_ARGUMENT;
+    if (!xbar_new || !xbar || !rbar || !mach_part || (S->nB > 0 && !rhob_bar)) return SPH_ERR_ARGUMENT;
     if (!S->prm.shift_on) return SPH_ERR_ARGUMENT;
     cudaStream_t st = (cudaStream_t)stream;
     if ((rc = rebuild(S, st))) return rc;
@@ -2138,13 +2484,38 @@ extern "C" int sph_solver_vjp_shift(sph_solver_t* S, const float* xbar_new, floa
         k_lam_shift<true><<<gb, 128, 0, st>>>(S->n, S->Xc, S->start, D, S->uid, S->maxv, xbar_new, S->words, S->Xh,
                                               mach_part);
         k_vjp_shift<true><<<gb, 128, 0, st>>>(S->n, S->Xc, S->start, D, S->uid, S->Xh, xbar_new, S->words, xbar,
-                                              rbar);
+                                              rbar, rhob_bar);
     } else {
         k_lam_shift<false><<<gb, 128, 0, st>>>(S->n, S->Xc, S->start, D, S->uid, S->maxv, xbar_new, S->words,
                                                S->Xh, mach_part);
         k_vjp_shift<false><<<gb, 128, 0, st>>>(S->n, S->Xc, S->start, D, S->uid, S->Xh, xbar_new, S->words, xbar,
-                                               rbar);
+                                               rbar, rhob_bar);
     }
+    return cudaGetLastError() == cudaSuccess ? SPH_OK : SPH_ERR_CUDA;
+}
+
+extern "C" int sph_solver_vjp_walls(sph_solver_t* S, const float* rhob_bar, float* xbar, float* rbar,
+                                    sph_stream_t stream) {
+    int rc = adjoint_ok(S);
+    if (rc) return rc;
+    if (S->nB == 0) return SPH_OK;
+    if (!rhob_bar || !xbar || !rbar) return SPH_ERR_ARGUMENT;
+    cudaStream_t st = (cudaStream_t)stream;
+    if ((rc = rebuild(S, st))) return rc;
+    // fp64 accumulators by slot in the spare state buffers (free between a sort and a step)
+    double* xacc = reinterpret_cast<double*>(S->Xt);
+    double* racc = reinterpret_cast<double*>(S->Vt);
+    if (cudaMemsetAsync(xacc, 0, sizeof(double) * 2 * S->n, st) != cudaSuccess) return SPH_ERR_CUDA;
+    if (cudaMemsetAsync(racc, 0, sizeof(double) * S->n, st) != cudaSuccess) return SPH_ERR_CUDA;
+    const Dom& D = S->doms_host[0];
+    const unsigned gw = (unsigned)((S->nB + 3) / 4);
+    if (S->periodic)
+        k_mdbc_vjp<true><<<gw, 128, 0, st>>>((int)S->nB, S->bidx, S->uid, S->Xr, S->Xc, S->bnormal, S->bdist,
+                                             S->start, D.g, D.P, rhob_bar, xacc, racc);
+    else
+        k_mdbc_vjp<false><<<gw, 128, 0, st>>>((int)S->nB, S->bidx, S->uid, S->Xr, S->Xc, S->bnormal, S->bdist,
+                                              S->start, D.g, D.P, rhob_bar, xacc, racc);
+    k_wall_adjoint_fin<<<blocks_for(S->n), kBlock, 0, st>>>(S->n, (int)S->nF, S->uid, xacc, racc, xbar, rbar);
     return cudaGetLastError() == cudaSuccess ? SPH_OK : SPH_ERR_CUDA;
 }
 

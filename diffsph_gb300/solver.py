@@ -213,6 +213,9 @@ class Solver:
             ctypes.byref(self.params), self.nF, self.nB, ctypes.c_void_p(self._ws_ptr), nbytes.value, ctypes.byref(h)))
         self.handle = h
         self.upload(fluid, boundary if self.nB else None)
+        # the static wall particles (re-uploads of the fluid state pass them again)
+        self.boundary = ({k: _dev(boundary[k]) for k in ("positions", "normals", "distances")}
+                         if self.nB else None)
         sh = config.get("shifting", {})
         if sh.get("scheme", "deltaSPH") == "IPS":
             self.set_ips(rtol=float(sh.get("rtol", 1e-4)), max_iter=int(sh.get("maxSolveIter", 64)),
@@ -355,20 +358,27 @@ class Solver:
         return o
 
     # -- adjoint (fluid-only, viscid) -------------------------------------------------------
-    def vjp_rates(self, abar, drbar, xbar, ubar, rbar, gbar=None, nu_part=None):
+    def vjp_rates(self, abar, drbar, xbar, ubar, rbar, gbar=None, nu_part=None, rhob_bar=None):
         """Accumulates the pass-B vector-Jacobian product at the current state (see
-        sph_solver_vjp_rates); all arrays are CUDA float32 in the original order."""
+        sph_solver_vjp_rates); all arrays are CUDA float32 in the original order. With walls
+        the adjoint of the wall densities accumulates into rhob_bar (required)."""
         _lib.check("sph_solver_vjp_rates", self.lib.sph_solver_vjp_rates(
             self.handle, _ptr(abar), _ptr(drbar), _ptr(xbar), _ptr(ubar), _ptr(rbar), _ptr(gbar), _ptr(nu_part),
-            _stream()))
+            _ptr(rhob_bar), _stream()))
 
-    def vjp_gradient(self, gbar, xbar, rbar):
+    def vjp_gradient(self, gbar, xbar, rbar, rhob_bar=None):
         _lib.check("sph_solver_vjp_gradient", self.lib.sph_solver_vjp_gradient(
-            self.handle, _ptr(gbar), _ptr(xbar), _ptr(rbar), _stream()))
+            self.handle, _ptr(gbar), _ptr(xbar), _ptr(rbar), _ptr(rhob_bar), _stream()))
 
-    def vjp_shift(self, xbar_new, xbar, rbar, mach_part):
+    def vjp_shift(self, xbar_new, xbar, rbar, mach_part, rhob_bar=None):
         _lib.check("sph_solver_vjp_shift", self.lib.sph_solver_vjp_shift(
-            self.handle, _ptr(xbar_new), _ptr(xbar), _ptr(rbar), _ptr(mach_part), _stream()))
+            self.handle, _ptr(xbar_new), _ptr(xbar), _ptr(rbar), _ptr(mach_part), _ptr(rhob_bar), _stream()))
+
+    def vjp_walls(self, rhob_bar, xbar, rbar):
+        """Pulls the adjoint of the mDBC wall densities at the current state back to the
+        fluid positions and densities (sph_solver_vjp_walls)."""
+        _lib.check("sph_solver_vjp_walls", self.lib.sph_solver_vjp_walls(
+            self.handle, _ptr(rhob_bar), _ptr(xbar), _ptr(rbar), _stream()))
 
     def flags(self) -> int:
         f = ctypes.c_uint32()

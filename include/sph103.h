@@ -204,36 +204,52 @@ int sph_solver_rhs_walls(sph_solver_t* s, const float* rho_boundary_in, float* d
 
 /* ------------------------------------------------------------------------------------
  * Adjoint (vector-Jacobian products) of the step's operators at the current state, for a
- * single fluid-only domain with viscid viscosity (deltaSPH_viscid). No reference entry
- * point has these: the reference differentiates its torch operators with autograd
- * (simulationStep, deltaPlus.py:176-422, per step). Every VJP walks the exact neighbor
- * lists in gather form (each particle collects its own pair terms and its neighbors' terms
- * through the symmetric neighbor relation), so no atomics are used. Inputs and outputs
- * are in the original particle order; gradients ACCUMULATE (+=) into xbar[nF][2],
- * ubar[nF][2], rbar[nF], gbar[nF][2]. Positions are differentiated through the periodic
- * wrap as the identity. Other configurations return SPH_ERR_ARGUMENT.
+ * single domain (periodic or walled with mDBC), either viscosity scheme (deltaSPH_viscid
+ * or _inviscid, with the boundary viscosity), gravity, the continuity density and the
+ * delta+ shift without the free-surface handling. No reference entry point has these: the
+ * reference differentiates its torch operators with autograd (simulationStep,
+ * deltaPlus.py:176-422, per step). Every VJP walks the exact neighbor lists in gather form
+ * (each particle collects its own pair terms and its neighbors' terms through the
+ * symmetric neighbor relation), so no atomics are used except in sph_solver_vjp_walls.
+ * Inputs and outputs are in the original particle order; gradients ACCUMULATE (+=) into
+ * xbar[nF][2], ubar[nF][2], rbar[nF], gbar[nF][2] and, with walls, into the adjoint of
+ * the wall densities rhob_bar[nB] (their pressures' adjoint folded in through the EOS;
+ * required when the solver has walls, ignored otherwise). Positions are differentiated
+ * through the periodic wrap as the identity. Other configurations (summation density,
+ * implicit shifting, free-surface handling, packed batches) return SPH_ERR_ARGUMENT.
  * ------------------------------------------------------------------------------------ */
 
 /* Right-hand side (pass B: continuity, delta-diffusion, pressure with the Tait EOS,
- * viscosity): given the adjoints abar[nF][2] of dudt and drbar[nF] of drhodt (NULL = 0),
- * accumulates the adjoints of positions, velocities, densities and of gradRho^L (gbar,
- * NULL to drop), and writes per particle nu_part[nF] (NULL to skip) whose sum is the
- * adjoint of diffusion.nu. gradRho^L is an input here; its own dependence on the state is
- * sph_solver_vjp_gradient. */
+ * viscosity, boundary viscosity): given the adjoints abar[nF][2] of dudt and drbar[nF] of
+ * drhodt (NULL = 0), accumulates the adjoints of positions, velocities, densities, of
+ * gradRho^L (gbar, NULL to drop) and of the wall densities the mDBC extrapolation gives at
+ * this state, and writes per particle nu_part[nF] (NULL to skip) whose sum is the adjoint
+ * of diffusion.nu (0 for the inviscid scheme). gradRho^L is an input here; its own
+ * dependence on the state is sph_solver_vjp_gradient. */
 int sph_solver_vjp_rates(sph_solver_t* s, const float* abar, const float* drbar, float* xbar,
-                         float* ubar, float* rbar, float* gbar, float* nu_part, sph_stream_t stream);
+                         float* ubar, float* rbar, float* gbar, float* nu_part, float* rhob_bar,
+                         sph_stream_t stream);
 
-/* Renormalised density gradient (pass A: M, L = pinv(M), gradRho^L = m L g): given
- * gbar[nF][2], accumulates the adjoints of positions and densities. */
+/* Renormalised density gradient (pass A: M, L = pinv(M), gradRho^L = m (L g_fluid +
+ * g_walls)): given gbar[nF][2], accumulates the adjoints of positions, densities and the
+ * wall densities (mDBC at this state). */
 int sph_solver_vjp_gradient(sph_solver_t* s, const float* gbar, float* xbar, float* rbar,
-                            sph_stream_t stream);
+                            float* rhob_bar, sph_stream_t stream);
 
 /* delta+ shift x'' = x' + clamp(dx(x', rho', Ma)): given xbar_new[nF][2] (the adjoint of
- * x''), accumulates xbar (identity part included) and rbar, and writes mach_part[nF]
- * whose sum is the adjoint of Ma = max|u| / cs (0 when shifting.computeMach is off).
- * Clamped components carry no gradient. */
+ * x''), accumulates xbar (identity part included), rbar and the adjoint of the wall
+ * densities as uploaded (the fused step shifts with the second stage's mDBC densities), and
+ * writes mach_part[nF] whose sum is the adjoint of Ma = max|u| / cs (0 when
+ * shifting.computeMach is off). Clamped components carry no gradient. */
 int sph_solver_vjp_shift(sph_solver_t* s, const float* xbar_new, float* xbar, float* rbar,
-                         float* mach_part, sph_stream_t stream);
+                         float* mach_part, float* rhob_bar, sph_stream_t stream);
+
+/* mDBC wall densities (mDBC.py:50-163; the fp64 moment solve of sph_solver_rhs): given
+ * the adjoint rhob_bar[nB] of the wall densities extrapolated from the current fluid state,
+ * accumulates the adjoints of the fluid positions and densities. The derivatives are summed
+ * per fluid particle in fp64 with atomics and rounded to fp32 once. No-op without walls. */
+int sph_solver_vjp_walls(sph_solver_t* s, const float* rhob_bar, float* xbar, float* rbar,
+                         sph_stream_t stream);
 
 /* ------------------------------------------------------------------------------------
  * Implicit particle shifting (shifting.scheme = 'IPS'): computeShifting,

@@ -17,13 +17,14 @@ What it has to work around (all read from the reference sources):
 * ``diffSPH.v2.modules`` must be imported before the simulation schemes to
   avoid a circular import (``incompressible.py:367``);
 * ``torchCompactRadius`` (external pip package, unpinned, absent here) is
-  provided by a small brute-force shim. The reference re-filters every
+  provided by a small cell-list shim. The reference re-filters every
   candidate pair with its own code (``src/diffSPH/v2/modules/neighborhood.py:433-460``),
   so the final neighbor set only requires the shim to return a superset of all
   pairs within the exact radius; the shim returns all pairs with
   ``|x_i - x_j| <= verletScale * h_j`` (plus a small margin), in (i, j)
   lexicographic order.
 """
+import importlib.machinery
 import os
 import sys
 import types
@@ -39,6 +40,11 @@ REF_SRC = os.environ.get("DIFFSPH_REF_SRC")
 
 class _Stub(types.ModuleType):
     """Module stub whose every attribute is another callable stub."""
+
+    def __init__(self, name):
+        super().__init__(name)
+        # a spec, so that importlib.util.find_spec (used by torch's tracing rules) accepts it
+        self.__spec__ = importlib.machinery.ModuleSpec(name, None)
 
     def __getattr__(self, name):
         if name.startswith("__") and name.endswith("__"):
@@ -80,31 +86,106 @@ def _install_stubs():
         pass
 
 
-def _candidate_pairs(qpos, qsup, rpos, rsup, minD, maxD, periodic, scale):
-    """Brute-force candidate superset: all (i, j) with periodic |x_i-x_j| <= scale*h_j."""
-    q = qpos.double()
-    r = rpos.double()
+def _periodic_delta(d, ext, periodic):
+    for a in range(d.shape[-1]):
+        if bool(periodic[a]):
+            da = d[..., a]
+            d[..., a] = da - torch.round(da / ext[a]) * ext[a]
+    return d
+
+
+def _candidate_pairs_brute(q, r, rsup, ext, periodic, scale):
     out_i, out_j = [], []
-    dim = q.shape[1]
-    minD = torch.as_tensor(minD, dtype=torch.float64).reshape(-1).expand(dim)
-    maxD = torch.as_tensor(maxD, dtype=torch.float64).reshape(-1).expand(dim)
-    periodic = torch.as_tensor(periodic).reshape(-1).expand(dim)
-    ext = maxD - minD
     chunk = max(1, int(2e7 // max(1, r.shape[0])))
     for s in range(0, q.shape[0], chunk):
-        d = q[s:s + chunk, None, :] - r[None, :, :]
-        for a in range(d.shape[-1]):
-            if bool(periodic[a]):
-                da = d[..., a]
-                d[..., a] = da - torch.round(da / ext[a]) * ext[a]
+        d = _periodic_delta(q[s:s + chunk, None, :] - r[None, :, :], ext, periodic)
         dist = torch.linalg.norm(d, dim=-1)
         m = dist <= (scale * rsup.double()[None, :] * 1.001 + 1e-9)
         ii, jj = torch.nonzero(m, as_tuple=True)
         out_i.append(ii + s)
         out_j.append(jj)
-    i = torch.cat(out_i).to(torch.int64)
-    j = torch.cat(out_j).to(torch.int64)
-    return i, j
+    return torch.cat(out_i).to(torch.int64), torch.cat(out_j).to(torch.int64)
+
+
+def _candidate_pairs(qpos, qsup, rpos, rsup, minD, maxD, periodic, scale):
+    """Candidate superset: all (i, j) with periodic |x_i-x_j| <= scale*h_j (plus a margin),
+    in (i, j) lexicographic order. Cells of the largest such radius bin the reference points
+    and every query tests the 3^dim cells around its own; with fewer than 3 cells on an axis
+    every pair is tested instead."""
+    q = qpos.double()
+    r = rpos.double()
+    dim = q.shape[1]
+    minD = torch.as_tensor(minD, dtype=torch.float64).reshape(-1).expand(dim)
+    maxD = torch.as_tensor(maxD, dtype=torch.float64).reshape(-1).expand(dim)
+    periodic = torch.as_tensor(periodic).reshape(-1).expand(dim)
+    ext = maxD - minD
+    if r.shape[0] == 0 or q.shape[0] == 0:
+        e = torch.zeros(0, dtype=torch.int64)
+        return e, e
+    rad = float((scale * rsup.double() * 1.001 + 1e-9).max())
+    lo = torch.minimum(q.min(0).values, r.min(0).values)
+    hi = torch.maximum(q.max(0).values, r.max(0).values)
+    ncell, origin = [], []
+    for a in range(dim):
+        if bool(periodic[a]):
+            n = int(torch.floor(ext[a] / rad))
+            origin.append(float(minD[a]))
+        else:
+            n = int(torch.floor((hi[a] - lo[a]) / rad)) + 1
+            origin.append(float(lo[a]))
+        ncell.append(n)
+    if min(ncell) < 3 or r.shape[0] * q.shape[0] < 4e6:
+        return _candidate_pairs_brute(q, r, rsup, ext, periodic, scale)
+    csize = [float(ext[a]) / ncell[a] if bool(periodic[a]) else rad for a in range(dim)]
+
+    def cells(p):
+        c = []
+        for a in range(dim):
+            ca = torch.floor((p[:, a] - origin[a]) / csize[a]).to(torch.int64)
+            c.append(torch.remainder(ca, ncell[a]) if bool(periodic[a]) else ca.clamp(0, ncell[a] - 1))
+        return c
+
+    def flat(c):
+        f = torch.zeros_like(c[0])
+        for a in range(dim):
+            f = f * ncell[a] + c[a]
+        return f
+
+    rc = flat(cells(r))
+    order = torch.argsort(rc, stable=True)
+    total = 1
+    for n in ncell:
+        total *= n
+    counts = torch.bincount(rc, minlength=total)
+    start = torch.cumsum(counts, 0) - counts
+    qc = cells(q)
+    out_i, out_j = [], []
+    offsets = torch.cartesian_prod(*[torch.tensor([-1, 0, 1])] * dim).reshape(-1, dim)
+    qidx = torch.arange(q.shape[0])
+    for off in offsets:
+        c, ok = [], torch.ones(q.shape[0], dtype=torch.bool)
+        for a in range(dim):
+            ca = qc[a] + int(off[a])
+            if bool(periodic[a]):
+                ca = torch.remainder(ca, ncell[a])
+            else:
+                ok &= (ca >= 0) & (ca < ncell[a])
+                ca = ca.clamp(0, ncell[a] - 1)
+            c.append(ca)
+        cid = flat(c)
+        cnt = torch.where(ok, counts[cid], torch.zeros_like(cid))
+        ii = torch.repeat_interleave(qidx, cnt)
+        first = torch.repeat_interleave(start[cid], cnt)
+        base = torch.repeat_interleave(torch.cumsum(cnt, 0) - cnt, cnt)
+        jj = order[first + torch.arange(ii.shape[0]) - base]
+        d = _periodic_delta(q[ii] - r[jj], ext, periodic)
+        keep = torch.linalg.norm(d, dim=-1) <= (scale * rsup.double()[jj] * 1.001 + 1e-9)
+        out_i.append(ii[keep])
+        out_j.append(jj[keep])
+    i = torch.cat(out_i)
+    j = torch.cat(out_j)
+    key = torch.argsort(i * r.shape[0] + j)
+    return i[key].to(torch.int64), j[key].to(torch.int64)
 
 
 def _install_compact_radius_shim():

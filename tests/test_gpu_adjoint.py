@@ -211,8 +211,197 @@ def test_checkpoint_interval_does_not_change_the_gradient():
         assert abs(nn - n1) <= 1e-4 * abs(n1)
 
 
+def _advanced_dam_break(dx=1.0 / 32, steps=40):
+    """The dam break advanced a few steps on the GPU (the column has started to move):
+    (config, fluid state as fp32 numpy arrays, static walls)."""
+    from diffsph_gb300.solver import Solver
+    cfg, st = scenes.dam_break(dx)
+    sol = Solver(cfg, st["fluid"], st["boundary"])
+    sol.step(steps)
+    sol.check()
+    got = sol.download()
+    fl = dict(st["fluid"])
+    for k in ("positions", "velocities", "densities"):
+        fl[k] = _np(got[k])
+    return cfg, fl, st["boundary"]
+
+
+def _walled(fl, bd):
+    return {"fluid": _fluid64(fl), "boundary": _fluid64(bd)}
+
+
+@pytest.mark.gpu
+def test_walled_rates_vjp_matches_fp64_finite_differences():
+    """Pass B + pass A + the mDBC wall densities of a walled domain (inviscid viscosity,
+    boundary viscosity, gravity): the VJP chain rates -> gradient -> walls against FP64
+    central differences of the oracle's right-hand side, which extrapolates the wall
+    densities from the perturbed fluid."""
+    _gpu()
+    from diffsph_gb300.solver import Solver
+    cfg, fl, bd = _advanced_dam_break()
+    rng = np.random.default_rng(21)
+    n = fl["positions"].shape[0]
+    abar = rng.standard_normal((n, 2)).astype(np.float32)
+    drbar = rng.standard_normal(n).astype(np.float32)
+    sol = Solver(cfg, fl, bd)
+    dev = "cuda"
+    xbar = torch.zeros(n, 2, device=dev)
+    ubar = torch.zeros(n, 2, device=dev)
+    rbar = torch.zeros(n, device=dev)
+    gbar = torch.zeros(n, 2, device=dev)
+    wbar = torch.zeros(sol.nB, device=dev)
+    sol.vjp_rates(torch.as_tensor(abar, device=dev), torch.as_tensor(drbar, device=dev), xbar, ubar, rbar, gbar,
+                  None, wbar)
+    sol.vjp_gradient(gbar, xbar, rbar, wbar)
+    assert float(wbar.abs().max()) > 0
+    sol.vjp_walls(wbar, xbar, rbar)
+    grads = {"positions": _np(xbar), "velocities": _np(ubar), "densities": _np(rbar)}
+    base = _walled(fl, bd)
+
+    def phi(state):
+        (_, dudt, drho), _ = O.simulation_step(state, cfg)
+        return float(np.sum(abar * dudt) + np.sum(drbar * drho))
+
+    d = _dirs(cfg, fl, rng)
+    for key in ("positions", "velocities", "densities"):
+        sp, sm = copy.deepcopy(base), copy.deepcopy(base)
+        sp["fluid"][key] = sp["fluid"][key] + EPS * d[key]
+        sm["fluid"][key] = sm["fluid"][key] - EPS * d[key]
+        fd = (phi(sp) - phi(sm)) / (2 * EPS)
+        pred = float(np.sum(grads[key].astype(np.float64) * d[key]))
+        assert _rel(pred, fd) < RTOL, (key, pred, fd)
+
+
+@pytest.mark.gpu
+def test_wall_density_vjp_matches_fp64_finite_differences():
+    """sph_solver_vjp_walls alone: sum_b w_b rho_b(fluid) with the mDBC extrapolation
+    (fp64 moment solve; Shepard fallback where a ghost has few fluid neighbors)."""
+    _gpu()
+    from diffsph_gb300.solver import Solver
+    cfg, fl, bd = _advanced_dam_break(steps=20)
+    rng = np.random.default_rng(22)
+    sol = Solver(cfg, fl, bd)
+    nB = sol.nB
+    w = rng.standard_normal(nB).astype(np.float32)
+    n = fl["positions"].shape[0]
+    xbar = torch.zeros(n, 2, device="cuda")
+    rbar = torch.zeros(n, device="cuda")
+    sol.vjp_walls(torch.as_tensor(w, device="cuda"), xbar, rbar)
+    grads = {"positions": _np(xbar), "densities": _np(rbar)}
+    base = _walled(fl, bd)
+
+    def phi(state):
+        rho_b, _, _ = O.mdbc_density(state["boundary"], state["fluid"], cfg)
+        return float(np.sum(w * rho_b))
+
+    d = _dirs(cfg, fl, rng)
+    for key in ("positions", "densities"):
+        sp, sm = copy.deepcopy(base), copy.deepcopy(base)
+        sp["fluid"][key] = sp["fluid"][key] + EPS * d[key]
+        sm["fluid"][key] = sm["fluid"][key] - EPS * d[key]
+        fd = (phi(sp) - phi(sm)) / (2 * EPS)
+        pred = float(np.sum(grads[key].astype(np.float64) * d[key]))
+        assert _rel(pred, fd) < RTOL, (key, pred, fd)
+
+
+@pytest.mark.gpu
+def test_walled_shift_vjp_matches_fp64_finite_differences():
+    """The delta+ shift next to walls: the adjoint of the fluid positions and densities and
+    of the wall densities it reads (as uploaded), against the oracle's solveShifting."""
+    _gpu()
+    from diffsph_gb300.solver import Solver
+    cfg, fl, bd = _advanced_dam_break(steps=30)
+    rng = np.random.default_rng(23)
+    n = fl["positions"].shape[0]
+    bdd = dict(bd)
+    rho_b, _, _ = O.mdbc_density(_fluid64(bd), _fluid64(fl), cfg)
+    bdd["densities"] = rho_b.astype(np.float32)
+    sol = Solver(cfg, fl, bdd)
+    xbn = rng.standard_normal((n, 2)).astype(np.float32)
+    dev = "cuda"
+    xbar = torch.zeros(n, 2, device=dev)
+    rbar = torch.zeros(n, device=dev)
+    mach = torch.zeros(n, device=dev)
+    wbar = torch.zeros(sol.nB, device=dev)
+    sol.vjp_shift(torch.as_tensor(xbn, device=dev), xbar, rbar, mach, wbar)
+    u = np.asarray(fl["velocities"], np.float64)
+    sp_ = np.linalg.norm(u, axis=1)
+    k = int(np.argmax(sp_))
+    ubar = np.zeros((n, 2))
+    ubar[k] = float(mach.double().sum()) / float(cfg["fluid"]["cs"]) * u[k] / sp_[k]
+    grads = {"positions": _np(xbar), "velocities": ubar, "densities": _np(rbar)}
+    base = _walled(fl, bdd)
+
+    def phi(state):
+        dx, _ = O.solve_shifting(state, cfg)
+        return float(np.sum(xbn * (state["fluid"]["positions"] + dx)))
+
+    d = _dirs(cfg, fl, rng)
+    for key in ("positions", "velocities", "densities"):
+        a, b = copy.deepcopy(base), copy.deepcopy(base)
+        a["fluid"][key] = a["fluid"][key] + EPS * d[key]
+        b["fluid"][key] = b["fluid"][key] - EPS * d[key]
+        fd = (phi(a) - phi(b)) / (2 * EPS)
+        pred = float(np.sum(np.asarray(grads[key], np.float64) * d[key]))
+        assert _rel(pred, fd) < RTOL, (key, pred, fd)
+    # the wall densities move the shift only (its increments are ~1e-4 of the positions, so
+    # the differences take the increments alone, clear of the positions' rounding)
+    def phi_dx(state):
+        dx, _ = O.solve_shifting(state, cfg)
+        return float(np.sum(xbn * dx))
+
+    db = rng.standard_normal(sol.nB)
+    a, b = copy.deepcopy(base), copy.deepcopy(base)
+    a["boundary"]["densities"] = a["boundary"]["densities"] + EPS * db
+    b["boundary"]["densities"] = b["boundary"]["densities"] - EPS * db
+    fd = (phi_dx(a) - phi_dx(b)) / (2 * EPS)
+    pred = float(np.sum(_np(wbar).astype(np.float64) * db))
+    assert _rel(pred, fd) < RTOL, ("wall densities", pred, fd)
+
+
+@pytest.mark.gpu
+def test_walled_rollout_gradient_matches_fp64_finite_differences():
+    """A 10-step dam-break rollout (walls, inviscid and boundary viscosity, gravity):
+    gradients of a velocity loss with respect to the initial positions, velocities and
+    densities against FP64 central differences of the oracle's full steps."""
+    _gpu()
+    from diffsph_gb300.adjoint import rollout
+    cfg, fl, bd = _advanced_dam_break(steps=40)
+    steps = 10
+    n = fl["positions"].shape[0]
+    rng = np.random.default_rng(24)
+    target = rng.standard_normal((n, 2)) * 0.1
+    dev = "cuda"
+    u0 = torch.as_tensor(fl["velocities"], device=dev).clone().requires_grad_(True)
+    rho0 = torch.as_tensor(fl["densities"], device=dev).clone().requires_grad_(True)
+    x0 = torch.as_tensor(fl["positions"], device=dev).clone().requires_grad_(True)
+    _, u, _ = rollout(cfg, fl, steps, checkpoint_every=4, x0=x0, u0=u0, rho0=rho0, boundary=bd)
+    loss = torch.mean((u - torch.as_tensor(target, dtype=torch.float32, device=dev)) ** 2)
+    loss.backward()
+
+    def L(fluid):
+        s = {"fluid": _fluid64(fluid), "boundary": _fluid64(bd)}
+        for _ in range(steps):
+            s, _ = O.full_step(s, cfg)
+        return float(np.mean((s["fluid"]["velocities"] - target) ** 2))
+
+    f64 = _fluid64(fl)
+    ref64 = L(f64)
+    assert abs(float(loss.detach()) - ref64) <= 1e-4 * ref64
+    grads = {"positions": _np(x0.grad), "velocities": _np(u0.grad), "densities": _np(rho0.grad)}
+    d = _dirs(cfg, fl, rng)
+    for key in ("velocities", "positions", "densities"):
+        a, b = _fluid64(f64), _fluid64(f64)
+        a[key] = a[key] + EPS * d[key]
+        b[key] = b[key] - EPS * d[key]
+        fd = (L(a) - L(b)) / (2 * EPS)
+        pred = float(np.sum(grads[key].astype(np.float64) * d[key]))
+        assert _rel(pred, fd) < RTOL, (key, pred, fd)
+
+
 @pytest.mark.gpu
 def test_vjp_rejects_unsupported_configurations():
+    """The summation density has no adjoint; a walled solver needs the wall-density adjoint."""
     _gpu()
     from diffsph_gb300 import _lib
     from diffsph_gb300.solver import Solver
@@ -222,21 +411,38 @@ def test_vjp_rejects_unsupported_configurations():
     z2 = torch.zeros(n, 2, device="cuda")
     z1 = torch.zeros(n, device="cuda")
     with pytest.raises(_lib.SphError) as e:
-        sol.vjp_rates(z2, z1, z2, z2, z1)
+        sol.vjp_rates(z2, z1, z2, z2, z1)  # no rhob_bar with walls
+    assert e.value.code == 1
+    cfg2, st2 = scenes.fourier_periodic(24, seed=1)
+    cfg2["simulation"]["densityScheme"] = "summation"
+    sol2 = Solver(cfg2, st2["fluid"])
+    m = sol2.nF
+    with pytest.raises(_lib.SphError) as e:
+        sol2.vjp_rates(torch.zeros(m, 2, device="cuda"), torch.zeros(m, device="cuda"), torch.zeros(m, 2, device="cuda"),
+                       torch.zeros(m, 2, device="cuda"), torch.zeros(m, device="cuda"))
     assert e.value.code == 1
 
 
-def test_rollout_rejects_out_of_scope_configs():
+@pytest.mark.parametrize("change", ["summation", "free_surface", "ips", "regions"])
+def test_rollout_rejects_out_of_scope_configs(change):
     from diffsph_gb300.adjoint import rollout
     cfg, st = scenes.dam_break(1.0 / 32)
+    if change == "summation":
+        cfg["simulation"]["densityScheme"] = "summation"
+    elif change == "free_surface":
+        cfg["shifting"]["freeSurface"] = True
+    elif change == "ips":
+        cfg["shifting"]["scheme"] = "IPS"
+    else:
+        cfg["regions"] = [{"type": "outlet"}]
     with pytest.raises(ValueError):
-        rollout(cfg, st["fluid"], 2)
+        rollout(cfg, st["fluid"], 2, boundary=st["boundary"])
 
 
-def _adjoint_fixture():
+def _adjoint_fixture(name="fourier24_100"):
     import json
     import os
-    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "adjoint_fourier24_100.npz")
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", f"adjoint_{name}.npz")
     z = np.load(path)
     cfg = json.loads(bytes(z["config_json"]).decode())
     fl = {k.split("/")[-1]: z[k] for k in z.files if k.startswith("in/fluid/")}
@@ -260,14 +466,16 @@ def _rel_l2(a, b):
 
 
 @pytest.mark.gpu
-def test_rollout_gradient_matches_reference_autograd_100_steps():
+@pytest.mark.parametrize("name", ["fourier24_100", "fourier128_100"])
+def test_rollout_gradient_matches_reference_autograd_100_steps(name):
     """Gradients of the 100-step loss against the reference's own torch-autograd gradient
     (FP64 run): relative L2 error <= 1e-3 for the velocity, position and density blocks
     and relative error <= 1e-3 for nu. The reference's FP32 run is held to the same bar
-    as a statement of what FP32 rounding costs."""
+    as a statement of what FP32 rounding costs. Cases: 24x24 particles, and 128x128 (the
+    size of the 128^2 rollout of the adjoint benchmark; its first 100 steps)."""
     _gpu()
     from diffsph_gb300.adjoint import rollout
-    z, cfg, fl = _adjoint_fixture()
+    z, cfg, fl = _adjoint_fixture(name)
     steps = int(z["steps"])
     dev = "cuda"
     x0 = torch.as_tensor(fl["positions"], device=dev).clone().requires_grad_(True)
