@@ -16,16 +16,16 @@ the reference's own gradient. Each step composes, as the runner does
 * solveShifting (src/diffSPH/v2/modules/shifting.py:882-1019) added to the positions.
 
 Cases: random Fourier-mode periodic flows with 0.1 dx jitter, 24x24 particles (seeds 3 and
-99) and 128x128 particles (the size of the 128^2 adjoint rollout, seeds 0 and 1). Loss: mean
-squared difference between the velocity after 100 steps and a target field from the same
-generator with another seed. The gradients with respect to the initial velocity,
+99, 100 steps) and 128x128 particles (the 128^2 adjoint rollout, seeds 0 and 1: its first 100
+steps, and all 1000). Loss: mean squared difference between the final velocity and a
+target field from the same generator with another seed. The gradients with respect to the initial velocity,
 positions, densities and diffusion.nu are written for an fp32 and an fp64 run to
-``tests/golden/adjoint_fourier24_100.npz`` and ``adjoint_fourier128_100.npz``. The 128^2 run
+``tests/golden/adjoint_<case>.npz``. The 128^2 run
 keeps only every step's inputs from a forward pass without a graph and rebuilds one step's
 graph at a time in the backward pass (per-step checkpointing), so that memory stays at one
 step's graph; the gradients are those of the whole graph.
 
-    python tests/golden/make_adjoint_golden.py [fourier24_100 | fourier128_100]
+    python tests/golden/make_adjoint_golden.py [fourier24_100 | fourier128_100 | fourier128_1000]
 """
 import json
 import os
@@ -45,7 +45,8 @@ from diffsph_gb300 import scenes  # noqa: E402
 torch.set_num_threads(min(8, os.cpu_count() or 1))
 
 # name: (particles per side, seed, target seed, steps, checkpoint every step)
-CASES = {"fourier24_100": (24, 3, 99, 100, False), "fourier128_100": (128, 0, 1, 100, True)}
+CASES = {"fourier24_100": (24, 3, 99, 100, False), "fourier128_100": (128, 0, 1, 100, True),
+         "fourier128_1000": (128, 0, 1, 1000, True)}
 
 
 def case(name="fourier24_100"):
