@@ -81,6 +81,37 @@ __global__ void k_upload(int64_t nF, int64_t nB, const float* __restrict__ xf, c
     uid[i] = (int32_t)i;
 }
 
+// Upload into the current slot order (Verlet reuse): slot s takes the state of particle
+// uid[s]; the sort words are left as they are, so the next step's displacement check decides
+__global__ void k_upload_keep(int64_t n, int64_t nF, const int32_t* __restrict__ uid, const float* __restrict__ xf,
+                              const float* __restrict__ uf, const float* __restrict__ rf,
+                              const float* __restrict__ xb, const float* __restrict__ nb,
+                              const float* __restrict__ db, const float* __restrict__ rb, Phys P, float2* Xr,
+                              float4* X4, float4* V4, float2* bnormal, float* bdist) {
+    int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const int64_t o = uid[s];
+    float2 x, u = make_float2(0.f, 0.f);
+    float rho, rho_s;
+    if (o < nF) {
+        x = make_float2(xf[2 * o], xf[2 * o + 1]);
+        u = make_float2(uf[2 * o], uf[2 * o + 1]);
+        rho = rf[o];
+        rho_s = rho;
+    } else {
+        const int64_t b = o - nF;
+        x = make_float2(xb[2 * b], xb[2 * b + 1]);
+        rho = rb ? rb[b] : P.rho0;
+        rho_s = -rho;
+        bnormal[b] = make_float2(nb[2 * b], nb[2 * b + 1]);
+        bdist[b] = db[b];
+    }
+    Xr[s] = x;
+    const float2 w = wrap_pos(x, P.geo);
+    X4[s] = make_float4(w.x, w.y, rho_s, eos_p(rho, P.eos));
+    V4[s] = make_float4(u.x, u.y, 0.f, 0.f);
+}
+
 __global__ void k_download(int64_t n, int nF, const int32_t* __restrict__ uid, const float2* __restrict__ Xr,
                            const float4* __restrict__ X4, const float4* __restrict__ V4, float* xf, float* uf,
                            float* rf, float* rb) {
@@ -1959,12 +1990,24 @@ extern "C" int sph_solver_upload(sph_solver_t* S, const float* x_fluid, const fl
         if (cudaStreamSynchronize(st) != cudaSuccess) return SPH_ERR_CUDA;
         S->tables_uploaded = true;
     }
+    if (S->reuse && S->uploaded) {
+        // keep the current order (and the pending-sort and skin-list words): the next step's
+        // displacement check sorts when the new positions are too far from the last sort's
+        k_upload_keep<<<blocks_for(S->n), kBlock, 0, st>>>(S->n, S->nF, S->uid, x_fluid, u_fluid, rho_fluid,
+                                                             x_boundary, normal_boundary, dist_boundary,
+                                                             rho_boundary, S->doms_host[0].P, S->Xr, S->Xc, S->Vc,
+                                                             S->bnormal, S->bdist);
+        if (cudaMemsetAsync(S->words, 0, sizeof(uint32_t), st) != cudaSuccess) return SPH_ERR_CUDA;
+        if (cudaMemsetAsync(S->words + 5, 0, sizeof(uint32_t), st) != cudaSuccess) return SPH_ERR_CUDA;
+        return cudaGetLastError() == cudaSuccess ? SPH_OK : SPH_ERR_CUDA;
+    }
     k_upload<<<blocks_for(S->n), kBlock, 0, st>>>(S->nF, S->nB, x_fluid, u_fluid, rho_fluid, x_boundary,
                                                     normal_boundary, dist_boundary, rho_boundary, S->doms, S->dom_off,
                                                     S->nd, S->Xr, S->Xc, S->Vc, S->uid, S->did, S->bnormal, S->bdist);
     if (cudaMemsetAsync(S->words, 0, sizeof(uint32_t) * 8, st) != cudaSuccess) return SPH_ERR_CUDA;
     // a new state is always sorted first
     if (cudaMemsetAsync(S->words + 4, 1, sizeof(uint32_t), st) != cudaSuccess) return SPH_ERR_CUDA;
+    S->uploaded = true;
     return cudaGetLastError() == cudaSuccess ? SPH_OK : SPH_ERR_CUDA;
 }
 

@@ -460,6 +460,7 @@ struct sph_solver {
     // domain): a step sorts again only when a particle moved farther than reuse_lim since
     // the last sort, or the skin list of that sort went invalid
     bool reuse = false;
+    bool uploaded = false;  // a state was loaded (uid holds the slot order)
     float reuse_lim = 0.f;
     // captured step graph
     // captured step graphs, keyed by step count and buffer assignment (two slots: eager

@@ -162,7 +162,13 @@ int sph_solver_create(const sph_params_t* params, int64_t n_fluid, int64_t n_bou
 void sph_solver_destroy(sph_solver_t* solver);
 
 /* Loads the state (original order; float2 arrays as [n][2]). Boundary arrays may be NULL
- * when n_boundary == 0. normals point into the wall, distances are negative depths. */
+ * when n_boundary == 0. normals point into the wall, distances are negative depths.
+ * Under Verlet reuse (sph_solver_set_verlet_reuse) an upload after the first keeps the
+ * particles' current order: each particle's state is written into the slot it occupies, so
+ * the next step sorts again only if a particle is farther than the reuse limit from its
+ * position at the last sort (a state read back by sph_solver_download and uploaded again
+ * costs no sort). Otherwise the particles are loaded in the original order and the next
+ * step sorts. */
 int sph_solver_upload(sph_solver_t* s, const float* x_fluid, const float* u_fluid,
                       const float* rho_fluid, const float* x_boundary, const float* normal_boundary,
                       const float* dist_boundary, const float* rho_boundary, sph_stream_t stream);

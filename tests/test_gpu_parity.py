@@ -313,6 +313,30 @@ def test_autotune_per_pass_on_the_dam_break_leaves_the_state_and_the_steps_uncha
     assert rel_max(_np(ga["densities"]), _np(gb["densities"])) < 1e-6
 
 
+def test_reupload_keeps_the_order_under_verlet_reuse():
+    """A state read back and uploaded again keeps the particles' slots: no sort is forced,
+    and the run continues bit for bit as if it had never left the device."""
+    cfg, st = scenes.dam_break(dx=1.0 / 64)
+    a = _solver(cfg, st)
+    a.set_verlet_reuse(True)
+    b = _solver(cfg, st)
+    b.set_verlet_reuse(True)
+    a.step(4)
+    b.step(4)
+    got = b.download()
+    b.upload({k: got[k] for k in ("positions", "velocities", "densities")}, st["boundary"])
+    b.step(1)
+    s0 = a.sort_count()
+    a.step(1)
+    assert b.sort_count() == a.sort_count() - s0  # the same sorts as the run that stayed
+    a.step(3)
+    b.step(3)
+    b.check()
+    ga, gb = a.download(), b.download()
+    for k in ("positions", "velocities", "densities", "boundary_densities"):
+        assert torch.equal(ga[k], gb[k]), k
+
+
 def test_per_pass_shapes_mix_in_one_batched_step():
     """Different shapes per pass (persistent and one-block-per-tile grids mixed) on a packed
     batch give the same state as the default shape."""
