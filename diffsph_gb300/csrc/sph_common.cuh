@@ -169,8 +169,9 @@ __device__ inline void pinv3_f64(const double A[9], double P[9], double rtol) {
         I[8] = (A[0] * A[4] - A[1] * A[3]) * id;
         double fi = 0.0;
         for (int k = 0; k < 9; ++k) fi += I[k] * I[k];
-        // ||A||_F ||A^-1||_F >= cond_2(A): below 0.3 / rtol no singular value is truncated
-        if (sqrt(fa * fi) < 0.3 / rtol) {
+        // ||A||_F ||A^-1||_F >= cond_2(A) = sigma_max / sigma_min: below 0.9 / rtol every
+        // singular value exceeds rtol sigma_max, nothing is truncated and A^+ = A^-1
+        if (sqrt(fa * fi) < 0.9 / rtol) {
             for (int k = 0; k < 9; ++k) P[k] = I[k];
             return;
         }
