@@ -230,6 +230,19 @@ cudaError_t cell_sort(const float* xy, int stride, int64_t n, const Grid& g, int
 // ------------------------------------------------------------------------------------
 // Exact neighbor search, separate query and reference sets, per-particle h_j.
 // ------------------------------------------------------------------------------------
+// The largest fp32 s with fl(fl(sqrt(s)) / h) <= 1 (IEEE round-to-nearest): both steps are
+// monotone in s, so exact_in(s, h) holds exactly for s <= T. The searches reject most
+// stencil candidates (about two in three) by this one comparison and take the square root
+// and the division only for the accepted ones. -1 for a support that admits no pair.
+__device__ float exact_T(float h) {
+    if (!(h > 0.f) || !isfinite(h)) return -1.f;
+    auto ok = [&](float s) { return __fdiv_rn(__fsqrt_rn(s), h) <= 1.f; };
+    float s = __fmul_rn(h, h);
+    for (int k = 0; k < 64 && !ok(s); ++k) s = nextafterf(s, 0.f);
+    for (int k = 0; k < 64 && ok(nextafterf(s, INFINITY)); ++k) s = nextafterf(s, INFINITY);
+    return s;
+}
+
 struct NbWork {
     Grid grid;
     Geo geo;
@@ -238,7 +251,7 @@ struct NbWork {
     int64_t* scan64;
     float2* ref_tmp;    // wrapped reference positions, input order
     float2* ref_xy;     // sorted, wrapped reference positions
-    float* ref_h;       // sorted supports
+    float2* ref_hT;     // sorted supports h and their thresholds T (s <= T <=> fl(fl(sqrt(s)) / h) <= 1)
     int32_t* ref_idx;   // sorted -> original index
     float2* qry_xy;     // wrapped query positions
 };
@@ -260,7 +273,7 @@ static int nb_layout(int64_t nq, int64_t nr, const sph_domain_t* d, double hmax,
     w->scan64 = c.take<int64_t>(scan_tmp_elems(nq));
     w->ref_tmp = c.take<float2>(nr);
     w->ref_xy = c.take<float2>(nr);
-    w->ref_h = c.take<float>(nr);
+    w->ref_hT = c.take<float2>(nr);
     w->ref_idx = c.take<int32_t>(nr);
     w->qry_xy = c.take<float2>(nq);
     *bytes = c.off;
@@ -274,13 +287,13 @@ __global__ void k_wrap_copy(const float* __restrict__ x, int64_t n, Geo geo, flo
 }
 
 __global__ void k_ref_gather(int64_t n, const int32_t* __restrict__ perm, const float2* __restrict__ wrapped,
-                             const float* __restrict__ h, float2* __restrict__ sxy, float* __restrict__ sh,
+                             const float* __restrict__ h, float2* __restrict__ sxy, float2* __restrict__ shT,
                              int32_t* __restrict__ sidx) {
     int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= n) return;
     int o = perm[s];
     sxy[s] = wrapped[o];
-    sh[s] = h[o];
+    shT[s] = make_float2(h[o], exact_T(h[o]));
     sidx[s] = o;
 }
 
@@ -289,7 +302,7 @@ __global__ void k_ref_gather(int64_t n, const int32_t* __restrict__ perm, const 
 // rows longer than the warp fill's shared buffer).
 template <bool FILL>
 __device__ void nb_row(int64_t i, const float2* __restrict__ qxy, const float2* __restrict__ rxy,
-                       const float* __restrict__ rh, const int32_t* __restrict__ ridx,
+                       const float2* __restrict__ rhT, const int32_t* __restrict__ ridx,
                        const int32_t* __restrict__ start, const Grid& g, const Geo& geo, int32_t* __restrict__ counts,
                        const int64_t* __restrict__ offsets, int64_t* __restrict__ pi, int64_t* __restrict__ pj,
                        float* __restrict__ pq, float* __restrict__ px, float* __restrict__ ph) {
@@ -308,9 +321,12 @@ __device__ void nb_row(int64_t i, const float2* __restrict__ qxy, const float2* 
             for (int s = s0; s < s1; ++s) {
                 float x0, x1;
                 pair_vec<true>(p, rxy[s], geo, x0, x1);
-                float r, q;
-                if (!exact_in(sq_norm_ref(x0, x1), rh[s], r, q)) continue;
+                const float sq = sq_norm_ref(x0, x1);
+                const float2 hT = rhT[s];
+                if (!(sq <= hT.y)) continue;  // exactly the reference's q <= 1 (exact_T)
                 if (FILL) {
+                    float r, q;
+                    exact_in(sq, hT.x, r, q);
                     float den = __fadd_rn(r, 1e-7f);
                     int64_t o = w + cnt;
                     pi[o] = i;
@@ -318,7 +334,7 @@ __device__ void nb_row(int64_t i, const float2* __restrict__ qxy, const float2* 
                     pq[o] = q;
                     px[2 * o] = __fdiv_rn(x0, den);
                     px[2 * o + 1] = __fdiv_rn(x1, den);
-                    ph[o] = rh[s];
+                    ph[o] = hT.x;
                 }
                 ++cnt;
             }
@@ -351,13 +367,13 @@ __device__ void nb_row(int64_t i, const float2* __restrict__ qxy, const float2* 
 
 template <bool FILL>
 __global__ void k_nb_query(int64_t nq, const float2* __restrict__ qxy, const float2* __restrict__ rxy,
-                           const float* __restrict__ rh, const int32_t* __restrict__ ridx,
+                           const float2* __restrict__ rhT, const int32_t* __restrict__ ridx,
                            const int32_t* __restrict__ start, Grid g, Geo geo, int32_t* __restrict__ counts,
                            const int64_t* __restrict__ offsets, int64_t* __restrict__ pi, int64_t* __restrict__ pj,
                            float* __restrict__ pq, float* __restrict__ px, float* __restrict__ ph) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nq) return;
-    nb_row<FILL>(i, qxy, rxy, rh, ridx, start, g, geo, counts, offsets, pi, pj, pq, px, ph);
+    nb_row<FILL>(i, qxy, rxy, rhT, ridx, start, g, geo, counts, offsets, pi, pj, pq, px, ph);
 }
 
 // The Wendland C2 kernel and gradient of one pair from its stored q, unit vector and support
@@ -386,7 +402,7 @@ constexpr int kFillCap = 128;
 
 __global__ void __launch_bounds__(32 * kFillWarps)
     k_nb_fill_warp(int64_t nq, const float2* __restrict__ qxy, const float2* __restrict__ rxy,
-                   const float* __restrict__ rh, const int32_t* __restrict__ ridx, const int32_t* __restrict__ start,
+                   const float2* __restrict__ rhT, const int32_t* __restrict__ ridx, const int32_t* __restrict__ start,
                    Grid g, Geo geo, const int64_t* __restrict__ offsets, int64_t* __restrict__ pi,
                    int64_t* __restrict__ pj, float* __restrict__ pq, float* __restrict__ px, float* __restrict__ ph,
                    float* __restrict__ W, float* __restrict__ G) {
@@ -399,7 +415,7 @@ __global__ void __launch_bounds__(32 * kFillWarps)
     const int64_t w0 = offsets[i];
     const int cnt_row = (int)(offsets[i + 1] - w0);
     if (cnt_row > kFillCap) {
-        if (lane == 0) nb_row<true>(i, qxy, rxy, rh, ridx, start, g, geo, nullptr, offsets, pi, pj, pq, px, ph);
+        if (lane == 0) nb_row<true>(i, qxy, rxy, rhT, ridx, start, g, geo, nullptr, offsets, pi, pj, pq, px, ph);
         __syncwarp();
         if (W || G)
             for (int e = lane; e < cnt_row; e += 32) {
@@ -426,12 +442,14 @@ __global__ void __launch_bounds__(32 * kFillWarps)
                 ++nrg;
             }
         }
+    // phase 1: the exact test of every candidate is one comparison with the reference's
+    // threshold (exact_T); the accepted pairs are packed with their squared distance
     int base = 0;
     for (int t0 = 0; t0 < total; t0 += 32) {
         const int t = t0 + lane;
         bool acc = false;
         int jo = 0;
-        float q = 0.f, x0h = 0.f, x1h = 0.f, hh = 0.f;
+        float sq = 0.f, x0 = 0.f, x1 = 0.f, hh = 0.f;
         if (t < total) {
             int r = 0, off = t;
             while (off >= len[r]) {
@@ -439,29 +457,36 @@ __global__ void __launch_bounds__(32 * kFillWarps)
                 ++r;
             }
             const int sl = rs[r] + off;
-            float x0, x1;
             pair_vec<true>(p, rxy[sl], geo, x0, x1);
-            float rr, qq;
-            hh = rh[sl];
-            if (exact_in(sq_norm_ref(x0, x1), hh, rr, qq)) {
+            const float2 hT = rhT[sl];
+            hh = hT.x;
+            sq = sq_norm_ref(x0, x1);
+            if (sq <= hT.y) {
                 acc = true;
                 jo = ridx[sl];
-                q = qq;
-                const float den = __fadd_rn(rr, 1e-7f);
-                x0h = __fdiv_rn(x0, den);
-                x1h = __fdiv_rn(x1, den);
             }
         }
         const unsigned m = __ballot_sync(0xffffffffu, acc);
         const int pos = base + __popc(m & ((1u << lane) - 1u));
         if (acc && pos < kFillCap) {
             s_j[wid][pos] = jo;
-            s_q[wid][pos] = q;
-            s_x0[wid][pos] = x0h;
-            s_x1[wid][pos] = x1h;
+            s_q[wid][pos] = sq;
+            s_x0[wid][pos] = x0;
+            s_x1[wid][pos] = x1;
             s_h[wid][pos] = hh;
         }
         base += __popc(m);
+    }
+    __syncwarp();
+    // phase 2: the accepted pairs' q and unit vector (the reference's IEEE square root and
+    // divisions), every lane busy
+    for (int e = lane; e < base && e < kFillCap; e += 32) {
+        float rr, qq;
+        exact_in(s_q[wid][e], s_h[wid][e], rr, qq);
+        const float den = __fadd_rn(rr, 1e-7f);
+        s_q[wid][e] = qq;
+        s_x0[wid][e] = __fdiv_rn(s_x0[wid][e], den);
+        s_x1[wid][e] = __fdiv_rn(s_x1[wid][e], den);
     }
     __syncwarp();
     // the count pass found the same pairs (same candidates, same test); the bound only
@@ -485,7 +510,7 @@ __global__ void __launch_bounds__(32 * kFillWarps)
 
 // CSR only: original reference indices of each query's exact neighbors, in cell order
 __global__ void k_nb_csr(int64_t nq, const float2* __restrict__ qxy, const float2* __restrict__ rxy,
-                         const float* __restrict__ rh, const int32_t* __restrict__ ridx,
+                         const float2* __restrict__ rhT, const int32_t* __restrict__ ridx,
                          const int32_t* __restrict__ start, Grid g, Geo geo, const int64_t* __restrict__ offsets,
                          int32_t* __restrict__ nbr) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -505,8 +530,8 @@ __global__ void k_nb_csr(int64_t nq, const float2* __restrict__ qxy, const float
             for (int s = s0; s < s1; ++s) {
                 float x0, x1;
                 pair_vec<true>(p, rxy[s], geo, x0, x1);
-                float r, q;
-                if (!exact_in(sq_norm_ref(x0, x1), rh[s], r, q)) continue;
+                const float sq = sq_norm_ref(x0, x1);
+                if (!(sq <= rhT[s].y)) continue;  // exactly the reference's q <= 1 (exact_T)
                 if (w < wend) nbr[w] = ridx[s];
                 ++w;
             }
@@ -537,7 +562,7 @@ static int nb_prepare(const float* xq, int64_t nq, const float* xr, const float*
     if (cell_sort((const float*)w->ref_tmp, 2, nr, w->grid, w->ncells, w->key, w->perm, w->count, w->fill,
                   w->start, w->scan32, s) != cudaSuccess)
         return SPH_ERR_CUDA;
-    if (nr > 0) k_ref_gather<<<gr, kBlock, 0, s>>>(nr, w->perm, w->ref_tmp, hr, w->ref_xy, w->ref_h, w->ref_idx);
+    if (nr > 0) k_ref_gather<<<gr, kBlock, 0, s>>>(nr, w->perm, w->ref_tmp, hr, w->ref_xy, w->ref_hT, w->ref_idx);
     if (nq > 0) k_wrap_copy<<<gq, kBlock, 0, s>>>(xq, nq, w->geo, w->qry_xy);
     return cudaGetLastError() == cudaSuccess ? SPH_OK : SPH_ERR_CUDA;
 }
@@ -552,7 +577,7 @@ extern "C" int sph_neighbor_count(const float* x_query, int64_t n_query, const f
     if (!offsets || (n_query > 0 && !counts)) return SPH_ERR_ARGUMENT;
     if (n_query > 0)
         k_nb_query<false><<<(unsigned)((n_query + kBlock - 1) / kBlock), kBlock, 0, s>>>(
-            n_query, w.qry_xy, w.ref_xy, w.ref_h, w.ref_idx, w.start, w.grid, w.geo, counts, nullptr, nullptr,
+            n_query, w.qry_xy, w.ref_xy, w.ref_hT, w.ref_idx, w.start, w.grid, w.geo, counts, nullptr, nullptr,
             nullptr, nullptr, nullptr, nullptr);
     if (scan_exclusive(counts, offsets, n_query, w.scan64, s) != cudaSuccess) return SPH_ERR_CUDA;
     return cudaGetLastError() == cudaSuccess ? SPH_OK : SPH_ERR_CUDA;
@@ -574,7 +599,7 @@ extern "C" int sph_neighbor_fill(const float* x_query, int64_t n_query, const fl
     // the sorted reference set from sph_neighbor_count is still in the workspace
     if (n_query > 0)
         k_nb_fill_warp<<<(unsigned)((n_query + kFillWarps - 1) / kFillWarps), 32 * kFillWarps, 0, s>>>(
-            n_query, w.qry_xy, w.ref_xy, w.ref_h, w.ref_idx, w.start, w.grid, w.geo, offsets, pair_i, pair_j, q, xhat,
+            n_query, w.qry_xy, w.ref_xy, w.ref_hT, w.ref_idx, w.start, w.grid, w.geo, offsets, pair_i, pair_j, q, xhat,
             h_pair, kernels, gradients);
     return cudaGetLastError() == cudaSuccess ? SPH_OK : SPH_ERR_CUDA;
 }
@@ -592,7 +617,7 @@ extern "C" int sph_neighbor_fill_csr(const float* x_query, int64_t n_query, cons
     if (!offsets || (n_query > 0 && !neighbors)) return SPH_ERR_ARGUMENT;
     if (n_query > 0)
         k_nb_csr<<<(unsigned)((n_query + kBlock - 1) / kBlock), kBlock, 0, s>>>(
-            n_query, w.qry_xy, w.ref_xy, w.ref_h, w.ref_idx, w.start, w.grid, w.geo, offsets, neighbors);
+            n_query, w.qry_xy, w.ref_xy, w.ref_hT, w.ref_idx, w.start, w.grid, w.geo, offsets, neighbors);
     return cudaGetLastError() == cudaSuccess ? SPH_OK : SPH_ERR_CUDA;
 }
 
