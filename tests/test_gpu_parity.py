@@ -130,6 +130,25 @@ def test_neighbor_search_variable_supports(scene):
     assert rel_max(_np(nb["gradients"]), ref["gradients"]) < 1e-6
 
 
+def test_neighbor_search_rows_longer_than_the_warp_buffer():
+    """Supports of 1.6-2.2 H give rows of ~120-240 pairs: those over the warp fill's shared
+    buffer (128) take the one-thread path; all rows bit-exact against the oracle."""
+    from diffsph_gb300.neighborhood import neighborSearch
+    cfg, st = scenes.fourier_periodic(40, seed=13, jitter=0.2)
+    qs, rs = st["fluid"], dict(st["fluid"])
+    rng = np.random.default_rng(4)
+    H = float(cfg["particle"]["support"])
+    rs["supports"] = (H * rng.uniform(1.6, 2.2, rs["positions"].shape[0])).astype(np.float32)
+    ref = O.neighbor_search(qs, rs, cfg)
+    assert int(np.max(ref["numNeighbors"])) > 128
+    _, nb = neighborSearch({k: torch.from_numpy(np.asarray(v)) for k, v in qs.items()},
+                           {k: torch.from_numpy(np.asarray(v)) for k, v in rs.items()}, cfg)
+    assert np.array_equal(_np(nb["indices"][0]), ref["indices"][0])
+    assert np.array_equal(_np(nb["indices"][1]), ref["indices"][1])
+    for key in ("distances", "vectors", "supports"):
+        assert np.array_equal(_np(nb[key]), ref[key]), key
+
+
 def test_neighbor_search_empty_and_isolated():
     from diffsph_gb300.neighborhood import exact_pairs
     cfg, _ = scenes.taylor_green(16)
