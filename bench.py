@@ -81,6 +81,8 @@ WORKLOADS = {
 # the drop-in neighbor search (neighborSearch's reference-format output) on the fluid of the
 # 2.1M-particle dam break, query = reference set
 WORKLOADS["neighbors_dx1024"] = dict(scene="neighbors", dx=1.0 / 1024)
+# the same at dx = 1/512 (524 k particles, a 1.1 GB list): the size the search's ncu captures use
+WORKLOADS["neighbors_dx512"] = dict(scene="neighbors", dx=1.0 / 512)
 NEIGHBOR_METRIC = "neighbor pairs/s (exact scatter-mode search, reference-format pair list)"
 LEARNED_METRIC = "particle-steps/s (learned k=4 step, counted in plain-step equivalents)"
 ADJOINT_METRIC = "adjoint particle-steps/s (forward + backward of a checkpointed rollout)"
@@ -478,7 +480,11 @@ def run_ours(args):
     stream = torch.cuda.Stream()
     torch.cuda.synchronize()
     with torch.cuda.stream(stream):
-        shape, shape_ms = sol.autotune()
+        if args.shape is None:
+            shape, shape_ms = sol.autotune()
+        else:  # a fixed launch shape for every pass (profiler runs: timings under a profiler mislead the tuner)
+            sol.set_shape(args.shape)
+            shape, shape_ms = sol.shapes(), {}
         for _ in range(args.warmup):
             sol.step(1)
         sol.check()
@@ -1115,6 +1121,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="dambreak_dx1024", choices=list(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--shape", type=int, default=None,
+                    help="launch shape of every neighbor pass instead of the autotuner's choice")
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--no-train", action="store_true",
                     help="learned workload: time the step with untrained weights (no accuracy figures)")

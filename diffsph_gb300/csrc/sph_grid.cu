@@ -251,7 +251,9 @@ struct NbWork {
     int64_t* scan64;
     float2* ref_tmp;    // wrapped reference positions, input order
     float2* ref_xy;     // sorted, wrapped reference positions
-    float2* ref_hT;     // sorted supports h and their thresholds T (s <= T <=> fl(fl(sqrt(s)) / h) <= 1)
+    // per sorted reference slot s: [2 s] = (h, T) with T the exact threshold
+    // (s <= T <=> fl(fl(sqrt(s)) / h) <= 1), [2 s + 1] = the kernel's (C_d / h^2, C_d / h^3)
+    float2* ref_hT;
     int32_t* ref_idx;   // sorted -> original index
     float2* qry_xy;     // wrapped query positions
 };
@@ -273,7 +275,7 @@ static int nb_layout(int64_t nq, int64_t nr, const sph_domain_t* d, double hmax,
     w->scan64 = c.take<int64_t>(scan_tmp_elems(nq));
     w->ref_tmp = c.take<float2>(nr);
     w->ref_xy = c.take<float2>(nr);
-    w->ref_hT = c.take<float2>(nr);
+    w->ref_hT = c.take<float2>(2 * nr);
     w->ref_idx = c.take<int32_t>(nr);
     w->qry_xy = c.take<float2>(nq);
     *bytes = c.off;
@@ -293,7 +295,9 @@ __global__ void k_ref_gather(int64_t n, const int32_t* __restrict__ perm, const 
     if (s >= n) return;
     int o = perm[s];
     sxy[s] = wrapped[o];
-    shT[s] = make_float2(h[o], exact_T(h[o]));
+    const float hh = h[o];
+    shT[2 * s] = make_float2(hh, exact_T(hh));
+    shT[2 * s + 1] = make_float2(kCd / (hh * hh), kCd / (hh * hh * hh));
     sidx[s] = o;
 }
 
@@ -322,7 +326,7 @@ __device__ void nb_row(int64_t i, const float2* __restrict__ qxy, const float2* 
                 float x0, x1;
                 pair_vec<true>(p, rxy[s], geo, x0, x1);
                 const float sq = sq_norm_ref(x0, x1);
-                const float2 hT = rhT[s];
+                const float2 hT = rhT[2 * s];
                 if (!(sq <= hT.y)) continue;  // exactly the reference's q <= 1 (exact_T)
                 if (FILL) {
                     float r, q;
@@ -377,11 +381,8 @@ __global__ void k_nb_query(int64_t nq, const float2* __restrict__ qxy, const flo
 }
 
 // The Wendland C2 kernel and gradient of one pair from its stored q, unit vector and support
-__device__ __forceinline__ void pair_kernel(float qq, float x0h, float x1h, float hh, float* W, float* G,
+__device__ __forceinline__ void pair_kernel(float qq, float x0h, float x1h, KernelCoef kc, float* W, float* G,
                                             int64_t k) {
-    KernelCoef kc;
-    kc.cw = kCd / (hh * hh);
-    kc.cg = kCd / (hh * hh * hh);
     if (W) W[k] = wendland_w(qq, kc);
     if (G) {
         const float d = wendland_dw(qq, kc);
@@ -407,8 +408,8 @@ __global__ void __launch_bounds__(32 * kFillWarps)
                    int64_t* __restrict__ pj, float* __restrict__ pq, float* __restrict__ px, float* __restrict__ ph,
                    float* __restrict__ W, float* __restrict__ G) {
     __shared__ int32_t s_j[kFillWarps][kFillCap];
-    __shared__ float s_q[kFillWarps][kFillCap], s_x0[kFillWarps][kFillCap], s_x1[kFillWarps][kFillCap],
-        s_h[kFillWarps][kFillCap];
+    __shared__ float s_q[kFillWarps][kFillCap], s_x0[kFillWarps][kFillCap], s_x1[kFillWarps][kFillCap];
+    __shared__ int32_t s_sl[kFillWarps][kFillCap];  // the pair's reference slot
     const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int64_t i = (int64_t)blockIdx.x * kFillWarps + wid;
     if (i >= nq) return;  // warp-uniform
@@ -420,7 +421,9 @@ __global__ void __launch_bounds__(32 * kFillWarps)
         if (W || G)
             for (int e = lane; e < cnt_row; e += 32) {
                 const int64_t o = w0 + e;
-                pair_kernel(pq[o], px[2 * o], px[2 * o + 1], ph[o], W, G, o);
+                const float hh = ph[o];
+                pair_kernel(pq[o], px[2 * o], px[2 * o + 1], KernelCoef{kCd / (hh * hh), kCd / (hh * hh * hh)}, W,
+                            G, o);
             }
         return;
     }
@@ -445,23 +448,21 @@ __global__ void __launch_bounds__(32 * kFillWarps)
     // phase 1: the exact test of every candidate is one comparison with the reference's
     // threshold (exact_T); the accepted pairs are packed with their squared distance
     int base = 0;
+    int cr = 0, cbase = 0;  // the lane's current range and its first flat index (only advance)
     for (int t0 = 0; t0 < total; t0 += 32) {
         const int t = t0 + lane;
         bool acc = false;
-        int jo = 0;
-        float sq = 0.f, x0 = 0.f, x1 = 0.f, hh = 0.f;
+        int jo = 0, sl = 0;
+        float sq = 0.f, x0 = 0.f, x1 = 0.f;
         if (t < total) {
-            int r = 0, off = t;
-            while (off >= len[r]) {
-                off -= len[r];
-                ++r;
+            while (t >= cbase + len[cr]) {
+                cbase += len[cr];
+                ++cr;
             }
-            const int sl = rs[r] + off;
+            sl = rs[cr] + (t - cbase);
             pair_vec<true>(p, rxy[sl], geo, x0, x1);
-            const float2 hT = rhT[sl];
-            hh = hT.x;
             sq = sq_norm_ref(x0, x1);
-            if (sq <= hT.y) {
+            if (sq <= rhT[2 * sl].y) {
                 acc = true;
                 jo = ridx[sl];
             }
@@ -473,7 +474,7 @@ __global__ void __launch_bounds__(32 * kFillWarps)
             s_q[wid][pos] = sq;
             s_x0[wid][pos] = x0;
             s_x1[wid][pos] = x1;
-            s_h[wid][pos] = hh;
+            s_sl[wid][pos] = sl;
         }
         base += __popc(m);
     }
@@ -482,7 +483,7 @@ __global__ void __launch_bounds__(32 * kFillWarps)
     // divisions), every lane busy
     for (int e = lane; e < base && e < kFillCap; e += 32) {
         float rr, qq;
-        exact_in(s_q[wid][e], s_h[wid][e], rr, qq);
+        exact_in(s_q[wid][e], rhT[2 * s_sl[wid][e]].x, rr, qq);
         const float den = __fadd_rn(rr, 1e-7f);
         s_q[wid][e] = qq;
         s_x0[wid][e] = __fdiv_rn(s_x0[wid][e], den);
@@ -492,19 +493,36 @@ __global__ void __launch_bounds__(32 * kFillWarps)
     // the count pass found the same pairs (same candidates, same test); the bound only
     // keeps an inconsistent row inside its own range
     const int n_e = base < cnt_row ? base : cnt_row;
-    for (int e = lane; e < n_e; e += 32) {
-        const int je = s_j[wid][e];
-        int rank = 0;
-        for (int k = 0; k < n_e; ++k) rank += s_j[wid][k] < je ? 1 : 0;
+    auto put = [&](int e, int je, int rank) {
         const int64_t o = w0 + rank;
-        const float q = s_q[wid][e], x0h = s_x0[wid][e], x1h = s_x1[wid][e], hh = s_h[wid][e];
+        const float q = s_q[wid][e], x0h = s_x0[wid][e], x1h = s_x1[wid][e];
+        const int sl = s_sl[wid][e];
         pi[o] = i;
         pj[o] = je;
         pq[o] = q;
         px[2 * o] = x0h;
         px[2 * o + 1] = x1h;
-        ph[o] = hh;
-        if (W || G) pair_kernel(q, x0h, x1h, hh, W, G, o);
+        ph[o] = rhT[2 * sl].x;
+        if (W || G) {
+            const float2 c = rhT[2 * sl + 1];
+            pair_kernel(q, x0h, x1h, KernelCoef{c.x, c.y}, W, G, o);
+        }
+    };
+    // each lane ranks two entries (lane and lane + 32) in one sweep over the row's keys (rows
+    // over 64 pairs take a second sweep for entries 64 on)
+    for (int e0 = lane; e0 < n_e; e0 += 64) {
+        const int e1 = e0 + 32;
+        const int j0 = s_j[wid][e0];
+        const int j1 = e1 < n_e ? s_j[wid][e1] : 0x7fffffff;
+        int r0 = 0, r1 = 0;
+#pragma unroll 4
+        for (int k = 0; k < n_e; ++k) {
+            const int v = s_j[wid][k];
+            r0 += v < j0 ? 1 : 0;
+            r1 += v < j1 ? 1 : 0;
+        }
+        put(e0, j0, r0);
+        if (e1 < n_e) put(e1, j1, r1);
     }
 }
 
@@ -531,7 +549,7 @@ __global__ void k_nb_csr(int64_t nq, const float2* __restrict__ qxy, const float
                 float x0, x1;
                 pair_vec<true>(p, rxy[s], geo, x0, x1);
                 const float sq = sq_norm_ref(x0, x1);
-                if (!(sq <= rhT[s].y)) continue;  // exactly the reference's q <= 1 (exact_T)
+                if (!(sq <= rhT[2 * s].y)) continue;  // exactly the reference's q <= 1 (exact_T)
                 if (w < wend) nbr[w] = ridx[s];
                 ++w;
             }

@@ -128,7 +128,7 @@ int sph_neighbor_fill_csr(const float* x_query, int64_t n_query, const float* x_
  * calls on one device share the one array: calls that overlap on the GPU (other streams, or
  * another thread before the previous call's work has finished) race on it. Pass 2
  * (sph_neighbor_fill) needs the caller workspace of sph_neighbor_count, not this call. */
-#define SPH_NEIGHBOR_STATIC_SCRATCH_BYTES ((size_t)20 << 20)
+#define SPH_NEIGHBOR_STATIC_SCRATCH_BYTES ((size_t)24 << 20)
 int sph_neighbor_count_static(const float* x_query, int64_t n_query, const float* x_ref,
                               const float* h_ref, int64_t n_ref, const sph_domain_t* domain,
                               double max_support, int32_t* counts, int64_t* offsets,

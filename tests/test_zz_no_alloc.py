@@ -13,7 +13,7 @@ import pytest
 from diffsph_gb300 import _lib, build, scenes
 from diffsph_gb300.solver import domain_struct
 
-LIMIT = 20 << 20  # SPH_NEIGHBOR_STATIC_SCRATCH_BYTES
+LIMIT = 24 << 20  # SPH_NEIGHBOR_STATIC_SCRATCH_BYTES
 STATIC_LIMIT = 7  # SPH_ERR_STATIC_LIMIT
 
 
