@@ -33,19 +33,17 @@ REGIONS_METRIC = ("ghost updates/s (mirror-outlet ghosts: construction, neighbor
                   "interpolation of density and velocity)")
 # lattice of the host sample of the mirror-outlet workload (reference arm, CPU baseline)
 REGIONS_SAMPLE_NX = 128
-# dram__bytes_read + dram__bytes_write of one launch per fluid particle, from ncu captures of
-# the dam break at dx = 1/512 (524,288 fluid particles): pass A is the mean of the four
-# working launches of two steps under Verlet reuse (19.05 + 78.72, 78.89 + 18.56,
-# 79.05 + 18.85 and 78.91 + 18.46 MB), pass B one launch (74.60 + 4.14 MB)
-PASS_A_DRAM_BYTES_PER_PARTICLE = 186.2
-PASS_B_DRAM_BYTES_PER_PARTICLE = 150.2
+# dram__bytes_read + dram__bytes_write of one launch per particle slot, from ncu captures of
+# the dam break at dx = 1/512 (536,594 slots, launch shape 1): pass A is the mean of the four
+# working launches of two steps under Verlet reuse, pass B the mean of its two stages
+PASS_A_DRAM_BYTES_PER_PARTICLE = 180.1
+PASS_B_DRAM_BYTES_PER_PARTICLE = 159.1
 # measured DRAM bytes per particle of pass A / pass B by scene, with where they come from;
 # a scene without a capture of its own reports no traffic
 DRAM_BYTES = {
     "dam_break": (PASS_A_DRAM_BYTES_PER_PARTICLE, PASS_B_DRAM_BYTES_PER_PARTICLE,
-                  "ncu dram bytes of k_pass_a on dambreak_dx512 (186.2 B/particle, the mean of the "
-                  "skin-building and skin-filtering launches of two steps under Verlet reuse), scaled by "
-                  "the particle count"),
+                  "ncu dram bytes of k_pass_a on dambreak_dx512 (180.1 B/particle slot, the mean of the "
+                  "skin-filtering launches of two steps under Verlet reuse), scaled by the particle count"),
     "batched": (117.5, 183.0,
                 "ncu dram bytes of k_pass_a (stencil scan, 4 launches) and k_pass_b (2 half-step + 2 final "
                 "launches) on batched_64 (1,162,235 particles in 64 periodic domains), scaled by the "
