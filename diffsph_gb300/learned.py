@@ -325,8 +325,14 @@ def generate_trajectories(n_traj, n_frames, nx, seed=0, k=4, jitter=0.1, chunk=2
     return cfg, trajs
 
 
-def fit_scales(config, trajs, k):
-    t = torch.cat([targets(config, k, fr[i], fr[i + 1]) for fr in trajs for i in range(len(fr) - 1)])
+def fit_scales(config, trajs, k, max_pairs=512, seed=0):
+    """Per-output spread of the targets over the frame pairs (a seeded sample of at most
+    max_pairs of them for large data sets)."""
+    pairs = [(t, i) for t in range(len(trajs)) for i in range(len(trajs[t]) - 1)]
+    if len(pairs) > max_pairs:
+        pick = np.random.default_rng(seed).choice(len(pairs), size=max_pairs, replace=False)
+        pairs = [pairs[p] for p in sorted(pick)]
+    t = torch.cat([targets(config, k, trajs[a][i], trajs[a][i + 1]) for a, i in pairs])
     return t.std(dim=0).clamp_min(1e-12)
 
 
@@ -343,10 +349,14 @@ def train(net, config, trajs, iters, k=4, lr=1e-3, seed=0, log_every=0):
     for it in range(iters):
         t, i = pairs[int(rng.integers(0, len(pairs)))]
         a, b = trajs[t][i], trajs[t][i + 1]
-        if (t, i) not in graphs:
-            graphs[(t, i)] = Graph(a[0], config)
+        # (the graphs of small data sets are kept; large ones rebuild each sample's)
+        g = graphs.get((t, i))
+        if g is None:
+            g = Graph(a[0], config)
+            if len(pairs) <= 1024:
+                graphs[(t, i)] = g
         tgt = targets(config, k, a, b) / net.out_scale
-        out = net(features(a[1], a[2], stepper.rho0), graphs[(t, i)])
+        out = net(features(a[1], a[2], stepper.rho0), g)
         loss = torch.mean((out - tgt) ** 2)
         opt.zero_grad(set_to_none=True)
         loss.backward()
