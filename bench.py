@@ -625,7 +625,10 @@ def run_e2e(sol, scene, batched, nF, world, e_steps, stream, one_step_graph=Fals
     """Same metric through the public API with host buffers: every step uploads the state
     from pinned host memory (the state the previous step read back; the scene's initial
     state for the first), advances one step (a replayed one-step graph when one_step_graph)
-    and reads the state back."""
+    and reads the state back. The step's arrays share one pinned host buffer and one device
+    buffer: [fluid positions, velocities, densities, wall densities read back | wall
+    positions, normals, distances, densities uploaded]; every step copies the whole buffer
+    host to device and its first part device to host, one copy each way."""
     import torch
     if batched:
         fl = {k: torch.cat([torch.from_numpy(s["fluid"][k]) for _, s in scene]) for k in
@@ -635,31 +638,43 @@ def run_e2e(sol, scene, batched, nF, world, e_steps, stream, one_step_graph=Fals
         fl = {k: torch.from_numpy(scene["fluid"][k]) for k in ("positions", "velocities", "densities")}
         bd = ({k: torch.from_numpy(scene["boundary"][k]) for k in ("positions", "normals", "distances", "densities")}
               if "boundary" in scene else None)
-    host_in = {("f", k): v.pin_memory() for k, v in fl.items()}
-    if bd is not None:
-        host_in.update({("b", k): v.pin_memory() for k, v in bd.items()})
-    dev_in = {k: torch.empty(v.shape, device="cuda") for k, v in host_in.items()}
-    host_out = {k: torch.empty(v.shape).pin_memory() for k, v in fl.items()}
-    if bd is not None:
-        host_out["boundary_densities"] = torch.empty(bd["densities"].shape).pin_memory()
+    nB = int(bd["positions"].shape[0]) if bd is not None else 0
+    out_parts = [("positions", (nF, 2)), ("velocities", (nF, 2)), ("densities", (nF,))]
+    if nB:
+        out_parts.append(("boundary_densities", (nB,)))
+    in_parts = ([("b_positions", (nB, 2)), ("b_normals", (nB, 2)), ("b_distances", (nB,)), ("b_densities", (nB,))]
+                if nB else [])
+    sizes = [(k, sh, int(np.prod(sh))) for k, sh in out_parts + in_parts]
+    n_out = sum(c for k, _, c in sizes[:len(out_parts)])
+    total = sum(c for _, _, c in sizes)
+    host = torch.empty(total, dtype=torch.float32).pin_memory()
+    dev = torch.empty(total, dtype=torch.float32, device="cuda")
 
-    for k, v in fl.items():  # the first upload is the scene's state; later ones the last result
-        host_out[k].copy_(v)
+    def views(buf):
+        v, o = {}, 0
+        for k, sh, c in sizes:
+            v[k] = buf[o:o + c].view(*sh)
+            o += c
+        return v
+
+    hv, dv = views(host), views(dev)
+    for k in ("positions", "velocities", "densities"):  # the first upload: the scene's state
+        hv[k].copy_(fl[k].reshape(hv[k].shape))
+    for k in ("positions", "normals", "distances", "densities"):
+        if nB:
+            hv["b_" + k].copy_(bd[k].reshape(hv["b_" + k].shape))
 
     def one():
-        for k, v in host_in.items():
-            dev_in[k].copy_(host_out[k[1]] if k[0] == "f" else v, non_blocking=True)
-        f = {k: dev_in[("f", k)] for k in ("positions", "velocities", "densities")}
-        b = ({k: dev_in[("b", k)] for k in ("positions", "normals", "distances", "densities")}
-             if bd is not None else None)
+        dev.copy_(host, non_blocking=True)
+        f = {k: dv[k] for k in ("positions", "velocities", "densities")}
+        b = {k: dv["b_" + k] for k in ("positions", "normals", "distances", "densities")} if nB else None
         sol.upload(f, b)
         if one_step_graph:
             sol.graph_step(1)
         else:
             sol.step(1)
-        got = sol.download()
-        for k, v in host_out.items():
-            v.copy_(got[k], non_blocking=True)
+        sol.download({k: dv[k] for k, _ in out_parts})
+        host[:n_out].copy_(dev[:n_out], non_blocking=True)
 
     for _ in range(2):
         one()
@@ -671,10 +686,8 @@ def run_e2e(sol, scene, batched, nF, world, e_steps, stream, one_step_graph=Fals
     e1.record(stream)
     torch.cuda.synchronize()
     ms = reduce_max(e0.elapsed_time(e1), world)
-    h2d = sum(v.numel() * 4 for v in host_in.values())
-    d2h = sum(v.numel() * 4 for v in host_out.values())
     return {"value": world * nF * e_steps / (ms / 1e3), "unit": "particle-steps/s",
-            "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "steps": e_steps,
+            "h2d_bytes_per_step": total * 4, "d2h_bytes_per_step": n_out * 4, "steps": e_steps,
             "one_step_graph": bool(one_step_graph)}
 
 

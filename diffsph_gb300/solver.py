@@ -247,10 +247,19 @@ class Solver:
         self._keep = args
         _lib.check("sph_solver_upload", self.lib.sph_solver_upload(self.handle, *[_ptr(a) for a in args], _stream()))
 
-    def download(self):
-        out = {"positions": torch.empty(self.nF, 2, device="cuda"), "velocities": torch.empty(self.nF, 2, device="cuda"),
-               "densities": torch.empty(self.nF, device="cuda")}
-        rb = torch.empty(self.nB, device="cuda") if self.nB else None
+    def download(self, out=None):
+        """The state in the original order: positions, velocities, densities (and the wall
+        densities). ``out``: caller tensors (CUDA float32, contiguous) to write into."""
+        if out is None:
+            out = {"positions": torch.empty(self.nF, 2, device="cuda"),
+                   "velocities": torch.empty(self.nF, 2, device="cuda"),
+                   "densities": torch.empty(self.nF, device="cuda")}
+            rb = torch.empty(self.nB, device="cuda") if self.nB else None
+        else:
+            out = dict(out)
+            rb = out.get("boundary_densities") if self.nB else None
+            if self.nB and rb is None:
+                raise ValueError("out needs boundary_densities for a solver with walls")
         _lib.check("sph_solver_download", self.lib.sph_solver_download(
             self.handle, _ptr(out["positions"]), _ptr(out["velocities"]), _ptr(out["densities"]), _ptr(rb), _stream()))
         if self.nB:
