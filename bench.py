@@ -72,6 +72,9 @@ WORKLOADS = {
     "outlet_mirror_1024": dict(scene="regions", nx=1024, mirror_x=0.9),
     # gradient of a rollout loss: 128x128 periodic Fourier flow, 1000 steps, checkpoints every 25
     "adjoint_fourier128": dict(scene="adjoint", nx=128, seed=0, target_seed=1, rollout=1000, every=25),
+    # the walled adjoint: dam break dx = 1/128 (32,768 fluid + 3,090 wall particles), 200 steps
+    "adjoint_dambreak128": dict(scene="adjoint", ic="dam_break", dx=1.0 / 128, target_seed=1, rollout=200,
+                                every=25),
     # learned k=4 step: trained at 128x128 (dx = 1/64), evaluated on 32 domains of 256x256 (4x4 box)
     "learned_fourier_b32": dict(scene="learned", nx_train=128, nx_eval=256, L_eval=4.0, batch=32, k=4, traj=8,
                                 frames=24, iters=3000, rollout=200),
@@ -706,7 +709,12 @@ def run_adjoint(args):
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
     ge.build()
     w = WORKLOADS[args.workload]
-    cfg, st = scenes.fourier_periodic(w["nx"], seed=w["seed"], jitter=0.1)
+    bd = None
+    if w.get("ic") == "dam_break":  # walled: mDBC walls, inviscid and boundary viscosity, gravity
+        cfg, st = scenes.dam_break(w["dx"])
+        bd = st["boundary"]
+    else:
+        cfg, st = scenes.fourier_periodic(w["nx"], seed=w["seed"], jitter=0.1)
     fl = st["fluid"]
     nF = fl["positions"].shape[0]
     target = scenes.fourier_velocity(np.asarray(fl["positions"], np.float64), np.random.default_rng(w["target_seed"]))
@@ -728,7 +736,7 @@ def run_adjoint(args):
         nu = torch.tensor(float(cfg["diffusion"]["nu"]), dtype=torch.float64, requires_grad=True)
         ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
         ev[0].record(stream)
-        _, u, _ = rollout(cfg, fl, n_steps, nu=nu, checkpoint_every=every, x0=x0, u0=u0, rho0=r0)
+        _, u, _ = rollout(cfg, fl, n_steps, nu=nu, checkpoint_every=every, x0=x0, u0=u0, rho0=r0, boundary=bd)
         loss = torch.mean((u - tg) ** 2)
         ev[1].record(stream)
         loss.backward()
@@ -756,7 +764,9 @@ def run_adjoint(args):
         "metric": ADJOINT_METRIC, "value": nF * T / (ms / 1e3), "unit": "particle-steps/s", "n_gpus": 1,
         "steps": T, "warmup": max(args.warmup, 3), "ms_per_step": ms / T, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": args.workload, "fluid_particles": nF, "rollout_steps": T, "checkpoint_every": every,
+        "config": {"workload": args.workload, "fluid_particles": nF,
+                   "boundary_particles": int(bd["positions"].shape[0]) if bd is not None else 0,
+                   "rollout_steps": T, "checkpoint_every": every,
                    "loss": loss, "dloss_dnu": dnu, "forward_ms": times["forward_ms"],
                    "backward_ms": times["backward_ms"], "l2": "state below L2 size; no flush (latency-bound)"},
         "e2e": {"value": nF * T / (ms_e2e / 1e3), "unit": "particle-steps/s",
