@@ -184,24 +184,28 @@ __device__ inline void pinv3_f64(const double A[9], double P[9], double rtol) {
         double off = B[1] * B[1] + B[2] * B[2] + B[5] * B[5];
         double dg = B[0] * B[0] + B[4] * B[4] + B[8] * B[8];
         if (off <= 1e-30 * dg) break;
+#pragma unroll
         for (int pq = 0; pq < 3; ++pq) {
-            int p = (pq == 2) ? 1 : 0;
-            int q = (pq == 0) ? 1 : 2;
-            double bpq = B[3 * p + q];
+            const int p = (pq == 2) ? 1 : 0;
+            const int q = (pq == 0) ? 1 : 2;
+            const int r = 3 - p - q;
+            const double bpq = B[3 * p + q];
             if (bpq == 0.0) continue;
-            double tau = (B[3 * q + q] - B[3 * p + p]) / (2.0 * bpq);
-            double t = (tau >= 0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
-            double c = 1.0 / sqrt(1.0 + t * t), s = t * c;
-            for (int k = 0; k < 3; ++k) {  // B <- B J (columns p, q)
-                double bkp = B[3 * k + p], bkq = B[3 * k + q];
-                B[3 * k + p] = c * bkp - s * bkq;
-                B[3 * k + q] = s * bkp + c * bkq;
-            }
-            for (int k = 0; k < 3; ++k) {  // B <- J^T B (rows p, q)
-                double bpk = B[3 * p + k], bqk = B[3 * q + k];
-                B[3 * p + k] = c * bpk - s * bqk;
-                B[3 * q + k] = s * bpk + c * bqk;
-            }
+            // t = tan(theta) of the rotation that zeroes b_pq (the smaller root):
+            // sgn(d) e / (|d| + sqrt(d^2 + e^2)), d = b_qq - b_pp, e = 2 b_pq; one square root,
+            // one division and one reciprocal square root (FP64 is slow on this part)
+            const double d = B[3 * q + q] - B[3 * p + p], e = 2.0 * bpq;
+            const double t = (d >= 0.0 ? e : -e) / (fabs(d) + sqrt(d * d + e * e));
+            const double c = rsqrt(1.0 + t * t), s = t * c;
+            // B <- J^T B J in closed form: the (p, q) block becomes diagonal, row/column r rotates
+            const double tb = t * bpq;
+            B[3 * p + p] -= tb;
+            B[3 * q + q] += tb;
+            B[3 * p + q] = B[3 * q + p] = 0.0;
+            const double brp = B[3 * r + p], brq = B[3 * r + q];
+            const double nrp = c * brp - s * brq, nrq = s * brp + c * brq;
+            B[3 * r + p] = B[3 * p + r] = nrp;
+            B[3 * r + q] = B[3 * q + r] = nrq;
             for (int k = 0; k < 3; ++k) {
                 double vkp = V[3 * k + p], vkq = V[3 * k + q];
                 V[3 * k + p] = c * vkp - s * vkq;
