@@ -166,15 +166,23 @@ __global__ void k_copy_back(int64_t n, const float2* __restrict__ Xr_t, const fl
 }
 
 // Verlet reuse: words[4] (sort this step) is set when a particle moved farther than lim since
-// the last sort, or when the skin list of that sort went invalid (words[3])
+// the last sort, or when the skin list of that sort went invalid (words[3]). In a packed
+// batch (did != nullptr) the limit is each domain's: min(half h, 0.7 skin_lim).
 __global__ void k_verlet_check(int64_t n, const float2* __restrict__ Xr, const float2* __restrict__ Xs,
-                               uint32_t* __restrict__ words, float lim2) {
+                               uint32_t* __restrict__ words, float lim2, const Dom* __restrict__ doms,
+                               const int32_t* __restrict__ did, float half) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     bool far = false;
     if (i < n) {
         const float2 a = Xr[i], b = Xs[i];
         const float e0 = a.x - b.x, e1 = a.y - b.y;
-        far = e0 * e0 + e1 * e1 > lim2;
+        float l2 = lim2;
+        if (did) {
+            const Phys& P = doms[did[i]].P;
+            const float lim = fminf(half * P.h, 0.7f * P.skin_lim);
+            l2 = lim * lim;
+        }
+        far = e0 * e0 + e1 * e1 > l2;
     }
     if (i == 0 && words[3] != 0u) far = true;
     if (__any_sync(0xffffffffu, far) && (threadIdx.x & 31) == 0) atomicOr(&words[4], 1u);
@@ -352,6 +360,9 @@ __device__ __forceinline__ void pass_a_tile(const Dom& D0, int64_t i, int64_t n,
     bool unstored = false;
     const float cg20 = -20.0f * P.kc.cg;
     int16_t* __restrict__ nrow = nl + tile_row(i, kStoreCap);
+    // wrap flags of the row (neighbor_loop / row_count): the pairs take the minimum image only
+    // in a warp with a row whose stencil may wrap (set before the first pair)
+    int wf = 3;
     auto pair_a = [&](int j) {
         {  // keep the exact list (scan order) for pass B at the same positions
             int d = j - (int)i;
@@ -368,8 +379,8 @@ __device__ __forceinline__ void pass_a_tile(const Dom& D0, int64_t i, int64_t n,
         }
         const float4 xj = __ldg(&X4[j]);
         float2 xv;
-        if (PER) {
-            pair_vec<PER>(pi, make_float2(xj.x, xj.y), P.geo, xv.x, xv.y);
+        if (PER && (wf & 2)) {
+            pair_vec<true>(pi, make_float2(xj.x, xj.y), P.geo, xv.x, xv.y);
         } else {
             xv = __ffma2_rn(make_float2(xj.x, xj.y), make_float2(-1.f, -1.f), pi);
         }
@@ -397,37 +408,50 @@ __device__ __forceinline__ void pass_a_tile(const Dom& D0, int64_t i, int64_t n,
     // the skin radius. Otherwise skin_mode 1 filters the skin list when it is complete for
     // every lane of the warp (no overflow, displacements within skin_lim) and skin_mode 2
     // scans.
-    if (BUILD && !PER) {
+    if (BUILD) {
         // the scan's list holds the skin candidates; each flush stores them (lanes flush their
         // k-th entries together, so the stores coalesce) and passes the exact ones on, in
-        // scan order
+        // scan order. Periodic offsets are stored modulo the domain's slots, with the row's
+        // wrap flag in its count.
         int ns = 0;
         bool sbad = false;
         int16_t* __restrict__ srow = sl + tile_row(i, kSkinCap);
         auto skin_then_exact = [&](int j) {
-            const int d = j - (int)i;
+            int d = j - (int)i;
+            if (PER) {
+                const int h2 = g.nslots >> 1;
+                if (d > h2) d -= g.nslots;
+                else if (d < -h2) d += g.nslots;
+            }
             if (ns < kSkinCap && d >= -32768 && d <= 32767)
                 srow[ns * 32] = (int16_t)d;
             else
                 sbad = true;
             ++ns;
             float x0, x1;
-            pair_vec<PER>(pi, ldg_xy(X4, j), P.geo, x0, x1);
+            if (PER && (wf & 2))
+                pair_vec<true>(pi, ldg_xy(X4, j), P.geo, x0, x1);
+            else
+                pair_vec<false>(pi, ldg_xy(X4, j), P.geo, x0, x1);
             if (sq_norm_ref(x0, x1) <= P.T) pair_a(j);
         };
         neighbor_loop<PER, LT, decltype(skin_then_exact)&, true>(active, (int)i, pi, X4, start, g, P, lst, words,
-                                                                 skin_then_exact);
-        if (inb) slc[i] = active ? (sbad ? (int16_t)-1 : (int16_t)ns) : (int16_t)0;
+                                                                 skin_then_exact, &wf);
+        if (inb) slc[i] = active ? (sbad ? (int16_t)-1 : stored_count(ns, wf)) : (int16_t)0;
     } else {
-        // (periodic domains never use the skin list: the branch compiles away for them)
-        const int sk = (!PER && skin_mode == 1 && active) ? (int)slc[i] : 0;
-        const bool use_skin = !PER && skin_mode == 1 && __all_sync(kFull, sk >= 0) && words[3] == 0u;
-        if (use_skin)
-            skin_list_loop<PER, LT>((int)i, pi, X4, g, P, sl, sk, lst, pair_a);
-        else
-            neighbor_loop<PER, LT>(active, (int)i, pi, X4, start, g, P, lst, words, pair_a);
+        const int sraw = (skin_mode == 1 && active) ? (int)slc[i] : 0;
+        const int sk = row_count(sraw, wf);
+        const bool use_skin = skin_mode == 1 && __all_sync(kFull, sk >= 0) && words[3] == 0u;
+        if (use_skin) {
+            if (PER && (wf & 2))
+                skin_list_loop<PER, PER, LT>((int)i, pi, X4, g, P, sl, sk, lst, pair_a);
+            else
+                skin_list_loop<PER, false, LT>((int)i, pi, X4, g, P, sl, sk, lst, pair_a);
+        } else {
+            neighbor_loop<PER, LT>(active, (int)i, pi, X4, start, g, P, lst, words, pair_a, &wf);
+        }
     }
-    if (inb) nlc[i] = active ? (unstored ? (int16_t)-1 : (int16_t)nstored) : (int16_t)0;
+    if (inb) nlc[i] = active ? (unstored ? (int16_t)-1 : stored_count(nstored, wf)) : (int16_t)0;
     if (!active) return;
     float M00 = M0.x, M01 = M0.y;
     const float gf0 = gfv.x, gf1 = gfv.y, gb0 = gbv.x, gb1 = gbv.y;
@@ -513,6 +537,7 @@ __device__ __forceinline__ void pass_b_tile(const Dom& D0, int64_t i, int64_t n,
     float ac = 0.f, ad = 0.f;
     float2 apv = make_float2(0.f, 0.f), avv = make_float2(0.f, 0.f), abv = make_float2(0.f, 0.f);
     const float cg20 = -20.0f * P.kc.cg;
+    int wf = 3;  // wrap flags of the row (pass A's stored count, or the fallback scan)
     // gradW = gf x_ij with gf = dW/dr / (r + 1e-7) (wendland_gf); xhat = x_ij inv. The
     // x/y pairs use sm_100's packed fp32 operations (__ffma2_rn, __fadd2_rn; a - b as
     // fma(b, -1, a)): each component rounds exactly as the scalar operation, so the sums are
@@ -521,8 +546,8 @@ __device__ __forceinline__ void pass_b_tile(const Dom& D0, int64_t i, int64_t n,
         const float4 xj = __ldg(&X4[j]);
         const float4 vj = __ldg(&V4[j]);
         float2 xv;
-        if (PER) {
-            pair_vec<PER>(pi, make_float2(xj.x, xj.y), P.geo, xv.x, xv.y);
+        if (PER && (wf & 2)) {
+            pair_vec<true>(pi, make_float2(xj.x, xj.y), P.geo, xv.x, xv.y);
         } else {
             xv = __ffma2_rn(make_float2(xj.x, xj.y), make_float2(-1.f, -1.f), pi);
         }
@@ -559,9 +584,9 @@ __device__ __forceinline__ void pass_b_tile(const Dom& D0, int64_t i, int64_t n,
     };
     // the exact list pass A stored at these positions (same scan order, so the same sums);
     // a warp with a row that could not be stored scans the stencil itself
-    const int nst = active ? (int)nlc[i] : 0;
+    const int nst = row_count(active ? (int)nlc[i] : 0, wf);
     if (__any_sync(kFull, nst < 0)) {
-        neighbor_loop<PER, LT>(active, (int)i, pi, X4, start, g, P, lst, words, pair_b);
+        neighbor_loop<PER, LT>(active, (int)i, pi, X4, start, g, P, lst, words, pair_b, &wf);
     } else {
         const int16_t* __restrict__ row = nl + tile_row(i, kStoreCap);
         int k = 0;
@@ -695,11 +720,12 @@ __device__ __forceinline__ void shift_tile(const Dom& D0, int64_t i, int64_t n, 
     float rhoi = xi.z;
     float2 sacc = make_float2(0.f, 0.f);
     const float cg20 = -20.0f * P.kc.cg;
+    int wf = 3;  // wrap flags of the row (the skin list's count, or the scan)
     auto pair_s = [&](int j) {
         const float4 xj = __ldg(&X4[j]);
         float2 xv;
-        if (PER) {
-            pair_vec<PER>(pi, make_float2(xj.x, xj.y), P.geo, xv.x, xv.y);
+        if (PER && (wf & 2)) {
+            pair_vec<true>(pi, make_float2(xj.x, xj.y), P.geo, xv.x, xv.y);
         } else {
             xv = __ffma2_rn(make_float2(xj.x, xj.y), make_float2(-1.f, -1.f), pi);
         }
@@ -716,11 +742,15 @@ __device__ __forceinline__ void shift_tile(const Dom& D0, int64_t i, int64_t n, 
     };
     // the skin list of the step's first pass A holds every pair of the integrated positions
     // unless a particle moved farther than skin_lim (flag set by the integrator)
-    const int sk = (!PER && use_skin && active) ? (int)slc[i] : 0;
-    if (!PER && use_skin && __all_sync(kFull, sk >= 0) && words[3] == 0u)
-        skin_list_loop<PER, LT>((int)i, pi, X4, g, P, sl, sk, lst, pair_s);
-    else
-        neighbor_loop<PER, LT>(active, (int)i, pi, X4, start, g, P, lst, words, pair_s);
+    const int sk = row_count((use_skin && active) ? (int)slc[i] : 0, wf);
+    if (use_skin && __all_sync(kFull, sk >= 0) && words[3] == 0u) {
+        if (PER && (wf & 2))
+            skin_list_loop<PER, PER, LT>((int)i, pi, X4, g, P, sl, sk, lst, pair_s);
+        else
+            skin_list_loop<PER, false, LT>((int)i, pi, X4, g, P, sl, sk, lst, pair_s);
+    } else {
+        neighbor_loop<PER, LT>(active, (int)i, pi, X4, start, g, P, lst, words, pair_s, &wf);
+    }
     if (!inb) return;
     const float s0 = sacc.x, s1 = sacc.y;
     float4 vi = V4[i];
@@ -812,10 +842,12 @@ __device__ __forceinline__ void density_sum_tile(const Dom& D0, int64_t i, int64
     };
     // skin_mode 1 filters the skin list (complete for every lane of the warp, still valid);
     // 4 does the same when this step kept its sort (words[4] == 0) and scans otherwise; 2 scans
-    const bool try_skin = !PER && (skin_mode == 1 || (skin_mode == 4 && words[4] == 0u));
-    const int sk = (try_skin && active) ? (int)slc[i] : 0;
-    if (!PER && try_skin && __all_sync(kFull, sk >= 0) && words[3] == 0u)
-        skin_list_loop<PER, LT>((int)i, pi, X4, g, P, sl, sk, lst, pair_d);
+    // (the pairs here always take the minimum image on periodic domains)
+    const bool try_skin = skin_mode == 1 || (skin_mode == 4 && words[4] == 0u);
+    int wf;
+    const int sk = row_count((try_skin && active) ? (int)slc[i] : 0, wf);
+    if (try_skin && __all_sync(kFull, sk >= 0) && words[3] == 0u)
+        skin_list_loop<PER, PER, LT>((int)i, pi, X4, g, P, sl, sk, lst, pair_d);
     else
         neighbor_loop<PER, LT>(active, (int)i, pi, X4, start, g, P, lst, words, pair_d);
     if (!inb) return;
@@ -1990,7 +2022,7 @@ extern "C" int sph_solver_upload(sph_solver_t* S, const float* x_fluid, const fl
         if (cudaStreamSynchronize(st) != cudaSuccess) return SPH_ERR_CUDA;
         S->tables_uploaded = true;
     }
-    if (S->reuse && S->uploaded) {
+    if (S->reuse && S->uploaded && S->nd == 1) {
         // keep the current order (and the pending-sort and skin-list words): the next step's
         // displacement check sorts when the new positions are too far from the last sort's
         k_upload_keep<<<blocks_for(S->n), kBlock, 0, st>>>(S->n, S->nF, S->uid, x_fluid, u_fluid, rho_fluid,
@@ -2020,7 +2052,8 @@ static int rebuild(sph_solver* S, cudaStream_t st, bool in_step = false) {
     const uint32_t* gate = S->reuse ? S->words + 4 : nullptr;
     if (S->reuse)
         k_verlet_check<<<blocks_for(S->n), kBlock, 0, st>>>(S->n, S->Xr, S->Xs, S->words,
-                                                            S->reuse_lim * S->reuse_lim);
+                                                            S->reuse_lim * S->reuse_lim, S->doms,
+                                                            S->nd > 1 ? S->did : nullptr, S->reuse_half);
     else if (cudaMemsetAsync(S->words + 4, 1, sizeof(uint32_t), st) != cudaSuccess)
         return SPH_ERR_CUDA;
     k_sort_begin<<<1, 32, 0, st>>>(S->words, in_step ? 1 : 0);
@@ -2214,18 +2247,23 @@ static void launch_dsum(sph_solver* S, const float4* Xin, float4* Xout, cudaStre
 
 static bool summation(const sph_solver* S) { return S->prm.density_scheme == 1; }
 
+// the step keeps a skin list for its later passes (walled domains always; periodic ones
+// under Verlet reuse)
+static bool uses_skin(const sph_solver* S) { return !S->periodic || S->reuse; }
+
 static int run_stages(sph_solver* S, cudaStream_t st) {
     RhsOut none = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     int rc = rebuild(S, st, true);
     if (rc) return rc;
-    // skin list (non-periodic domains: there the stencil scan skips the minimum image on most
-    // ranges, which the skin filter cannot, and measured no faster)
-    const int skin = S->periodic ? 2 : 0;
+    // skin list: kept by the first pass A after a sort and filtered by the later passes;
+    // periodic domains keep it only under Verlet reuse (sorting every step, the cost of
+    // keeping it is not won back: the stencil scan skips the minimum image on most ranges)
+    const int skin = uses_skin(S) ? 0 : 2;
     // stage 1 at t^n. With the summation density the stage reads the state with the summed
     // densities from the spare buffer Xt (free between the sort and the next step)
     float4* X1 = S->Xc;
     if (summation(S)) {
-        launch_dsum(S, S->Xc, S->Xt, st, S->periodic ? 2 : (S->reuse ? 4 : 2));
+        launch_dsum(S, S->Xc, S->Xt, st, S->reuse ? 4 : 2);
         X1 = S->Xt;
     }
     launch_mdbc(S, X1, nullptr, st);
@@ -2298,7 +2336,7 @@ static int step_impl(sph_solver* S, int32_t n_steps, cudaStream_t st) {
             rc = ips_shift(S, S->Xf, S->Vf, S->Xc, S->Vc, nullptr, S->periodic ? 0 : 1, st);
             if (rc) return rc;
         } else {
-            launch_shift(S, S->Xf, S->Vf, S->Xc, S->Vc, nullptr, st, S->periodic ? 0 : 1);
+            launch_shift(S, S->Xf, S->Vf, S->Xc, S->Vc, nullptr, st, uses_skin(S) ? 1 : 0);
         }
         if (cudaGetLastError() != cudaSuccess) return SPH_ERR_CUDA;
     }
@@ -2405,20 +2443,20 @@ extern "C" int sph_solver_autotune(sph_solver_t* S, int32_t* shapes_out, float* 
     const bool saved_fs = S->fs_on;
     S->timing_mask = 0;
     S->fs_on = false;
-    const int skin_scan = S->periodic ? 2 : 0;
+    const bool skin = uses_skin(S);
     const int order[TP_COUNT] = {TP_A_SCAN, TP_A_FILTER, TP_SHIFT, TP_DENSITY, TP_B};
     rc = SPH_OK;
     for (int oi = 0; oi < TP_COUNT && rc == SPH_OK; ++oi) {
         const int tp = order[oi];
-        const bool applies = tp == TP_A_SCAN || tp == TP_B || (tp == TP_A_FILTER && !S->periodic) ||
+        const bool applies = tp == TP_A_SCAN || tp == TP_B || (tp == TP_A_FILTER && skin) ||
                              (tp == TP_SHIFT && !S->ips) || (tp == TP_DENSITY && summation(S));
         auto run = [&]() {
             switch (tp) {
-                case TP_A_SCAN: launch_a(S, S->Xc, S->Vc, none, st, skin_scan); break;
+                case TP_A_SCAN: launch_a(S, S->Xc, S->Vc, none, st, skin ? 0 : 2); break;
                 case TP_A_FILTER: launch_a(S, S->Xc, S->Vc, none, st, 1); break;
                 case TP_B: launch_b<1>(S, S->Xc, S->Vc, none, S->Xh, S->Vh, st); break;
-                case TP_SHIFT: launch_shift(S, S->Xc, S->Vc, S->Xt, S->Vt, nullptr, st, S->periodic ? 0 : 1); break;
-                default: launch_dsum(S, S->Xc, S->Xt, st, S->periodic ? 2 : 1); break;
+                case TP_SHIFT: launch_shift(S, S->Xc, S->Vc, S->Xt, S->Vt, nullptr, st, skin ? 1 : 0); break;
+                default: launch_dsum(S, S->Xc, S->Xt, st, skin ? 1 : 2); break;
             }
         };
         if (tp == TP_SHIFT && applies &&
@@ -2653,7 +2691,6 @@ extern "C" int sph_solver_launches_per_step(const sph_solver_t* S) {
 
 extern "C" int sph_solver_set_verlet_reuse(sph_solver_t* S, int32_t on) {
     if (!S || on < 0 || on > 1) return SPH_ERR_ARGUMENT;
-    if (on && (S->periodic || S->nd > 1)) return SPH_ERR_ARGUMENT;
     if (S->reuse != (on == 1)) {
         // the captured sequences differ (and so does the buffer rotation of a sort)
         for (int k = 0; k < 2; ++k) {
@@ -2677,6 +2714,7 @@ extern "C" int sph_solver_set_verlet_scale(sph_solver_t* S, double verlet_scale)
     const float ref_lim = (float)((verlet_scale - 1.0) * S->doms_host[0].P.h * 0.5);
     const float own_lim = 0.7f * S->doms_host[0].P.skin_lim;
     S->reuse_lim = ref_lim < own_lim ? ref_lim : own_lim;
+    S->reuse_half = (float)((verlet_scale - 1.0) * 0.5);
     return SPH_OK;
 }
 

@@ -194,8 +194,29 @@ constexpr int kStoreCap = 64;
 // first pass A of a step; the second pass A and the shift filter it instead of the stencil
 constexpr double kSkinFrac = 0.1;
 constexpr int kSkinCap = 80;
+// A stored row count (skin list, exact list) carries kRowWraps when the row's stencil held a
+// range whose pairs may cross the periodic boundary (stencil_ranges): only such rows need the
+// minimum image. A row without it and its candidates lie away from the edge cells and within
+// rad cells of each other, and stay so while they move less than a cell, so their raw
+// differences are the minimum image exactly. Counts stay below kRowCount; -1 marks a row that
+// was not stored.
+constexpr int kRowWraps = 0x4000;
+constexpr int kRowCount = 0x3fff;
 
 
+
+// The count of a stored row (negative: not stored) and the warp's wrap flags as
+// neighbor_loop sets them (bit 0 this row, bit 1 some row of the warp). Every lane calls it.
+__device__ __forceinline__ int row_count(int raw, int& wrap) {
+    const bool wl = raw > 0 && (raw & kRowWraps) != 0;
+    wrap = (wl ? 1 : 0) | (__any_sync(kFull, wl) ? 2 : 0);
+    return raw < 0 ? raw : (raw & kRowCount);
+}
+
+// The stored count of a row with its wrap flag (bit 0 of a neighbor_loop / row_count flag word)
+__device__ __forceinline__ int16_t stored_count(int cnt, int wrap) {
+    return (int16_t)(cnt | ((wrap & 1) ? kRowWraps : 0));
+}
 
 template <typename LT>
 __device__ __forceinline__ bool fits(int d) {
@@ -213,15 +234,22 @@ __device__ __forceinline__ int list_slot(int self, int d, const Grid& g) {
 }
 
 // SKIN: keep every candidate within the skin radius (T_skin) instead of the exact neighbors
+// wrap (optional): set before the first f call to bit 0 = this lane's stencil has a range
+// that may wrap, bit 1 = some lane of the warp's has.
 template <bool PER, typename LT, class F, bool SKIN = false>
 __device__ __forceinline__ void neighbor_loop(bool active, int self, float2 pi, const float4* __restrict__ X4,
                                               const int32_t* __restrict__ start, const Grid& g, const Phys& P,
-                                              LT* __restrict__ lst, uint32_t* __restrict__ words, F&& f) {
+                                              LT* __restrict__ lst, uint32_t* __restrict__ words, F&& f,
+                                              int* wrap = nullptr) {
     const float thr = SKIN ? P.T_skin : P.T;
     const int lane = threadIdx.x & 31;
     int rs[kMaxRanges], re[kMaxRanges];
     unsigned wmask = 0;
     int nrng = active ? stencil_ranges(pi, g, start, rs, re, PER ? &wmask : nullptr) : 0;
+    if (wrap) {
+        const bool wl = PER && wmask != 0u;
+        *wrap = (wl ? 1 : 0) | (__any_sync(kFull, wl) ? 2 : 0);
+    }
     int r = 0;
     int s = nrng > 0 ? rs[0] : 0, se = nrng > 0 ? re[0] : 0;
     int cnt = 0;
@@ -324,8 +352,8 @@ __device__ __forceinline__ void skin_loop(int self, float2 pi, const float4* __r
 // (list entry, neighbor position, the reference's exact test) fills the warp's shared-memory
 // list lst, then f(j) runs over the accepted entries with every lane busy, in the skin
 // list's order. Every lane of the warp must call it (it votes); lanes with cnt = 0 add no
-// pairs.
-template <bool PER, typename LT, class F>
+// pairs. WR: the filter takes the minimum image (some row of the warp carries kRowWraps).
+template <bool PER, bool WR, typename LT, class F>
 __device__ __forceinline__ void skin_list_loop(int self, float2 pi, const float4* __restrict__ X4, const Grid& g,
                                                const Phys& P, const int16_t* __restrict__ sl, int cnt,
                                                LT* __restrict__ lst, F&& f) {
@@ -345,7 +373,7 @@ __device__ __forceinline__ void skin_list_loop(int self, float2 pi, const float4
         for (int u = 0; u < 4; ++u) {
             if (k + u < cnt) {
                 float x0, x1;
-                pair_vec<PER>(pi, xj[u], P.geo, x0, x1);
+                pair_vec<WR>(pi, xj[u], P.geo, x0, x1);
                 if (sq_norm_ref(x0, x1) <= P.T) lst[(m++) * 32 + lane] = (LT)d[u];
             }
         }
@@ -456,12 +484,14 @@ struct sph_solver {
     int grid_cap[TP_COUNT][kNumShapes] = {};   // persistent grid per pass and shape (0: not yet known)
     bool attrs_set = false;
     bool tables_uploaded = false;
-    // Verlet reuse of the cell sort and the skin list across steps (single non-periodic
-    // domain): a step sorts again only when a particle moved farther than reuse_lim since
-    // the last sort, or the skin list of that sort went invalid
+    // Verlet reuse of the cell sort and the skin list across steps: a step sorts again only
+    // when a particle moved farther than its domain's limit since the last sort (reuse_lim
+    // for one domain; min(reuse_half h, 0.7 skin_lim) per domain of a batch), or the skin
+    // list of that sort went invalid
     bool reuse = false;
     bool uploaded = false;  // a state was loaded (uid holds the slot order)
     float reuse_lim = 0.f;
+    float reuse_half = 1e30f;  // (verletScale - 1) / 2: the reference's limit over h
     // captured step graph
     // captured step graphs, keyed by step count and buffer assignment (two slots: eager
     // steps between replays alternate the assignment)

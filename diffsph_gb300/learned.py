@@ -296,7 +296,8 @@ def generate_trajectories(n_traj, n_frames, nx, seed=0, k=4, jitter=0.1, chunk=2
     returns (config, [[(x, u, rho) per frame] per trajectory]) with frames every k steps.
     The trajectories are stepped together, up to `chunk` domains packed into one batched
     solver (same kernel launches for all of them, k steps per captured graph replay); the
-    batch steps every domain exactly as a solver of its own would."""
+    batch steps every domain as a solver of its own would, up to the order of each particle's
+    pair sums (the batch sorts when any of its domains needs it under Verlet reuse)."""
     from . import scenes
     from .solver import BatchSolver
     rng = np.random.default_rng(seed)

@@ -83,11 +83,8 @@ def verlet_scale(cfg) -> float:
 
 def wants_verlet_reuse(cfg, params: _lib.Params) -> bool:
     """Verlet reuse of the cell sort and skin list, as the reference reuses its neighbor
-    structure while neighborhood.verletScale > 1 (neighborhood.py:505-518): on for single
-    non-periodic domains."""
-    dom = params.domain
-    if dom.periodic[0] or dom.periodic[1]:
-        return False
+    structure while neighborhood.verletScale > 1 (neighborhood.py:505-518), on walled and
+    periodic domains alike."""
     return verlet_scale(cfg) > 1.0
 
 
@@ -433,7 +430,7 @@ class Solver:
 
     def set_verlet_reuse(self, on: bool):
         """Keep the cell sort and the skin list across steps until a particle moved 0.034 h
-        (single non-periodic domains; see sph_solver_set_verlet_reuse)."""
+        (see sph_solver_set_verlet_reuse)."""
         _lib.check("sph_solver_set_verlet_reuse", self.lib.sph_solver_set_verlet_reuse(self.handle, int(bool(on))))
         self.verlet_reuse = bool(on)
 
@@ -499,6 +496,16 @@ class BatchSolver(Solver):
             P, n_arr, nd, ctypes.c_void_p(self._ws_ptr), nbytes.value, ctypes.byref(h)))
         self.handle = h
         self.upload_domains(fluids)
+        # Verlet reuse as for one domain (every domain's verletScale > 1): any domain whose
+        # particles moved past its own limit sorts the batch
+        self.verlet_reuse = False
+        if all(wants_verlet_reuse(c, P[d]) for d, c in enumerate(configs)):
+            scales = {verlet_scale(c) for c in configs}
+            if len(scales) != 1:
+                raise ValueError("the domains of a batch share one neighborhood.verletScale")
+            self.set_verlet_reuse(True)
+            _lib.check("sph_solver_set_verlet_scale",
+                       self.lib.sph_solver_set_verlet_scale(self.handle, scales.pop()))
 
     def upload_domains(self, fluids):
         cat = {k: torch.cat([torch.as_tensor(f[k]).reshape(torch.as_tensor(f[k]).shape[0], -1).float()

@@ -164,7 +164,7 @@ void sph_solver_destroy(sph_solver_t* solver);
 /* Loads the state (original order; float2 arrays as [n][2]). Boundary arrays may be NULL
  * when n_boundary == 0. normals point into the wall, distances are negative depths.
  * Under Verlet reuse (sph_solver_set_verlet_reuse) an upload after the first keeps the
- * particles' current order: each particle's state is written into the slot it occupies, so
+ * particles' current order (one domain; a packed batch is loaded in the original order): each particle's state is written into the slot it occupies, so
  * the next step sorts again only if a particle is farther than the reuse limit from its
  * position at the last sort (a state read back by sph_solver_download and uploaded again
  * costs no sort). Otherwise the particles are loaded in the original order and the next
@@ -462,15 +462,16 @@ int sph_solver_flags(sph_solver_t* s, uint32_t* flags_host, sph_stream_t stream)
  * the default scale 1.5 at :603): a step sorts the particles by cell again, and rebuilds the
  * skin list of candidates within 1.1 h, only when a particle moved farther than 0.034 h
  * since the last sort (or the list went invalid); otherwise it keeps that order and filters
- * the kept list. Single non-periodic domains only (SPH_ERR_ARGUMENT otherwise); off after
- * sph_solver_create. The decision is taken on the device, so captured step graphs replay
- * both cases. Results differ from the sort-every-step ones only in the order of each
- * particle's pair sums. */
+ * the kept list. Walled, periodic and packed batches of domains (each domain's particles
+ * against its own limit; any domain past it sorts the batch); off after sph_solver_create.
+ * The decision is taken on the device, so captured step graphs replay both cases. Results
+ * differ from the sort-every-step ones only in the order of each particle's pair sums. */
 int sph_solver_set_verlet_reuse(sph_solver_t* s, int32_t on);
 /* The reference's rebuild rule for that reuse (neighborhood.py:509-513): a rebuild once
  * 2 max |x - x_sort| > (verletScale - 1) h. The solver sorts at the stricter of
  * (verletScale - 1) h / 2 and its own 0.034 h (the skin list's limit with a margin);
- * verlet_scale must exceed 1. With the default verletScale 1.5 the solver's limit applies. */
+ * verlet_scale must exceed 1. With the default verletScale 1.5 the solver's limit applies.
+ * In a batch each domain's limit follows from its own h. */
 int sph_solver_set_verlet_scale(sph_solver_t* s, double verlet_scale);
 /* Number of cell sorts since the last upload (device counter); synchronises the stream. */
 int sph_solver_sort_count(sph_solver_t* s, uint32_t* sorts, sph_stream_t stream);

@@ -151,7 +151,9 @@ def test_verlet_reuse_follows_the_reference_verlet_scale():
     assert wants_verlet_reuse(cfg, p)                  # the reference's default, 1.5
     cfg, st = scenes.taylor_green(16)
     p = params_from_config(cfg, float(st["fluid"]["masses"][0]))
-    assert not wants_verlet_reuse(cfg, p)              # periodic: sorted every step
+    assert wants_verlet_reuse(cfg, p)                  # periodic domains reuse too
+    cfg["neighborhood"]["verletScale"] = 1.0
+    assert not wants_verlet_reuse(cfg, p)
 
 
 def test_params_reject_what_the_kernels_do_not_implement():

@@ -190,7 +190,8 @@ def test_layer_gradients_match_oracle(C, rel):
 def test_training_data_comes_from_the_batched_solver():
     """generate_trajectories packs its trajectories into one batched solver (graph replays of
     k steps); every frame equals a single-domain solver's run of the same initial condition,
-    bit for bit."""
+    the first bit for bit, the later ones up to the order of each particle's pair sums (under
+    Verlet reuse the batch sorts when any of its domains needs it)."""
     from diffsph_gb300 import scenes
     from diffsph_gb300.learned import _wrap, generate_trajectories
     from diffsph_gb300.solver import Solver
@@ -202,9 +203,17 @@ def test_training_data_comes_from_the_batched_solver():
         sol = Solver(c, st["fluid"])
         for f in range(3):
             got = sol.download()
-            assert torch.equal(_wrap(got["positions"], c), trajs[t][f][0]), (t, f)
-            assert torch.equal(got["velocities"], trajs[t][f][1]), (t, f)
-            assert torch.equal(got["densities"], trajs[t][f][2]), (t, f)
+            x, u, r = _wrap(got["positions"], c), got["velocities"], got["densities"]
+            if f == 0:
+                assert torch.equal(x, trajs[t][f][0]) and torch.equal(u, trajs[t][f][1]), t
+                assert torch.equal(r, trajs[t][f][2]), t
+            else:
+                # (wrapped positions: a particle on the wrap may land on either side)
+                dxw = (x - trajs[t][f][0]).abs()
+                dxw = torch.minimum(dxw, 2.0 - dxw)
+                assert float(dxw.max()) < 1e-5, (t, f)
+                assert float((u - trajs[t][f][1]).abs().max()) < 1e-4 * float(u.abs().max()), (t, f)
+                assert float((r - trajs[t][f][2]).abs().max()) < 1e-5, (t, f)
             sol.step(4)
 
 

@@ -297,8 +297,9 @@ def test_autotune_picks_a_shape_and_keeps_parity():
     for p in ("pass_a_scan", "pass_b", "shift"):
         assert 0 <= shapes[p] < len(ms[p]) and ms[p][shapes[p]] > 0
         assert ms[p][shapes[p]] == min(v for v in ms[p] if v > 0)
-    # a periodic domain never filters a skin list; the continuity scheme sums no densities
-    assert max(ms["pass_a_filter"]) < 0 and max(ms["density_sum"]) < 0
+    # under Verlet reuse (the default at verletScale 1.5) a periodic domain filters a skin
+    # list too; the continuity scheme sums no densities
+    assert a.verlet_reuse and max(ms["pass_a_filter"]) > 0 and max(ms["density_sum"]) < 0
     a.step(1)
     b = _solver(cfg, st)
     b.step(1)
@@ -413,12 +414,16 @@ def test_batched_domains_equal_single_domain_solvers():
     from diffsph_gb300.solver import BatchSolver
     doms = scenes.batched_fourier(5, seed=11, n_min=256, n_max=4096)
     batch = BatchSolver([c for c, _ in doms], [s["fluid"] for _, s in doms])
+    # sorting every step (under Verlet reuse the batch sorts when any domain needs it, a
+    # solver of one domain when that domain does: the pair sums' order would differ)
+    batch.set_verlet_reuse(False)
     batch.step(3)
     batch.check()
     got = batch.download()
     parts = {k: batch.split(got[k]) for k in ("positions", "velocities", "densities")}
     for d, (cfg, st) in enumerate(doms):
         one = _solver(cfg, st)
+        one.set_verlet_reuse(False)
         one.step(3)
         ref = one.download()
         for k in ("positions", "velocities", "densities"):
@@ -559,16 +564,75 @@ def test_verlet_reuse_sorts_every_step_of_a_fast_flow():
         assert torch.equal(ga[k], gb[k]), k
 
 
-def test_verlet_reuse_is_rejected_on_periodic_domains():
+def _drifting_fourier(nx, seed):
+    """A jittered periodic Fourier flow at 0.3 of its speed plus a drift of (0.6, 0.35): about
+    0.015 h per step, so particles cross the periodic boundary between Verlet sorts."""
+    cfg, st = scenes.fourier_periodic(nx, seed=seed, jitter=0.1)
+    st = copy.deepcopy(st)
+    v = st["fluid"]["velocities"]
+    st["fluid"]["velocities"] = (np.float32(0.3) * v + np.array([0.6, 0.35], np.float32)).astype(np.float32)
+    return cfg, st
+
+
+def test_verlet_reuse_on_periodic_domains():
+    """Verlet reuse on a periodic domain (on by default at verletScale 1.5, as the reference
+    reuses its neighborhood on any domain): fewer sorts than steps while particles cross the
+    periodic boundary between sorts; the state equals that of a solver sorting every step up
+    to the order of each particle's pair sums, and one-step graph replays equal the eager
+    steps bit for bit. Rows away from the wrap filter the skin list without the minimum
+    image: a pair that needed it there would be lost and move the state by far more."""
     from diffsph_gb300._lib import SphError
-    cfg, st = scenes.taylor_green(16)
-    sol = _solver(cfg, st)
-    assert not getattr(sol, "verlet_reuse", False)
-    with pytest.raises(SphError):
-        sol.set_verlet_reuse(True)
-    # without reuse every step rotates the buffers: graphs hold an even number of steps
+    cfg, st = _drifting_fourier(48, seed=9)
+    a = _solver(cfg, st)
+    assert a.verlet_reuse
+    b = _solver(cfg, st)
+    b.set_verlet_reuse(False)
+    a.step(40)
+    b.step(40)
+    a.check()
+    b.check()
+    assert b.sort_count() == 40
+    assert 2 <= a.sort_count() <= 30, a.sort_count()
+    ga, gb = a.download(), b.download()
+    hi = torch.tensor(cfg["domain"]["maxExtent"], dtype=torch.float32)
+    assert bool((ga["positions"].cpu() > hi).any())  # raw positions past the wrap
+    assert rel_max(_np(ga["velocities"]), _np(gb["velocities"])) < 1e-3
+    assert rel_max(_np(ga["densities"]), _np(gb["densities"])) < 1e-5
+    assert float((ga["positions"] - gb["positions"]).abs().max()) < 1e-5
     s = torch.cuda.Stream()
+    c = _solver(cfg, st)
+    with torch.cuda.stream(s):
+        for _ in range(40):
+            c.graph_step(1)
+        gc = c.download()
+    s.synchronize()
+    assert c.sort_count() == a.sort_count()
+    for k in ("positions", "velocities", "densities"):
+        assert torch.equal(ga[k], gc[k]), k
+    # without reuse every step rotates the buffers: graphs hold an even number of steps
     with torch.cuda.stream(s):
         with pytest.raises(SphError):
-            sol.graph_step(1)
+            b.graph_step(1)
     s.synchronize()
+
+
+def test_batched_verlet_reuse_matches_sorting_every_step():
+    """A packed batch under Verlet reuse (domains of different dx: each particle against its
+    own domain's limit; any domain past it sorts the batch) equals the batch sorting every
+    step up to the order of each particle's pair sums, with fewer sorts."""
+    from diffsph_gb300.solver import BatchSolver
+    doms = [_drifting_fourier(nx, seed=30 + nx) for nx in (20, 33, 48)]
+    a = BatchSolver([c for c, _ in doms], [s["fluid"] for _, s in doms])
+    assert a.verlet_reuse
+    b = BatchSolver([c for c, _ in doms], [s["fluid"] for _, s in doms])
+    b.set_verlet_reuse(False)
+    a.step(30)
+    b.step(30)
+    a.check()
+    b.check()
+    assert b.sort_count() == 30
+    assert 2 <= a.sort_count() < 30, a.sort_count()
+    ga, gb = a.download(), b.download()
+    assert rel_max(_np(ga["velocities"]), _np(gb["velocities"])) < 1e-3
+    assert rel_max(_np(ga["densities"]), _np(gb["densities"])) < 1e-5
+    assert float((ga["positions"] - gb["positions"]).abs().max()) < 1e-5
