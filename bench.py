@@ -44,10 +44,10 @@ DRAM_BYTES = {
     "dam_break": (PASS_A_DRAM_BYTES_PER_PARTICLE, PASS_B_DRAM_BYTES_PER_PARTICLE,
                   "ncu dram bytes of k_pass_a on dambreak_dx512 (180.1 B/particle slot, the mean of the "
                   "skin-filtering launches of two steps under Verlet reuse), scaled by the particle count"),
-    "batched": (117.5, 183.0,
-                "ncu dram bytes of k_pass_a (stencil scan, 4 launches) and k_pass_b (2 half-step + 2 final "
-                "launches) on batched_64 (1,162,235 particles in 64 periodic domains), scaled by the "
-                "particle count"),
+    "batched": (281.3, 194.8,
+                "ncu dram bytes of k_pass_a (the 3 skin-filtering launches of two steps under Verlet reuse) "
+                "and k_pass_b (2 half-step + 2 final launches) on batched_256 (4,519,897 particles in 256 "
+                "periodic domains, launch shape 1), scaled by the particle count"),
 }
 # the same for one product of the implicit shift (k_ips_spmv) on the jittered periodic flow
 # of 512^2 particles ((192.06 + 3.65) MB and (189.98 + 3.62) MB / 262,144)

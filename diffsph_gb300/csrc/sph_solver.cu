@@ -25,6 +25,7 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <type_traits>
 #include <utility>
 #include <vector>
 
@@ -364,9 +365,10 @@ __device__ __forceinline__ void pass_a_tile(const Dom& D0, int64_t i, int64_t n,
     // in a warp with a row whose stencil may wrap (set before the first pair)
     int wf = 3;
     auto pair_a = [&](int j) {
-        {  // keep the exact list (scan order) for pass B at the same positions
+        {  // keep the exact list (scan order) for pass B at the same positions (offsets of a
+           // row that may wrap modulo the domain's slots, of any other row direct)
             int d = j - (int)i;
-            if (PER) {
+            if (PER && (wf & 1)) {
                 const int h2 = g.nslots >> 1;
                 if (d > h2) d -= g.nslots;
                 else if (d < -h2) d += g.nslots;
@@ -411,14 +413,14 @@ __device__ __forceinline__ void pass_a_tile(const Dom& D0, int64_t i, int64_t n,
     if (BUILD) {
         // the scan's list holds the skin candidates; each flush stores them (lanes flush their
         // k-th entries together, so the stores coalesce) and passes the exact ones on, in
-        // scan order. Periodic offsets are stored modulo the domain's slots, with the row's
-        // wrap flag in its count.
+        // scan order. The offsets of a row that may wrap are stored modulo the domain's slots
+        // (its count carries kRowWraps), those of any other row direct.
         int ns = 0;
         bool sbad = false;
         int16_t* __restrict__ srow = sl + tile_row(i, kSkinCap);
         auto skin_then_exact = [&](int j) {
             int d = j - (int)i;
-            if (PER) {
+            if (PER && (wf & 1)) {
                 const int h2 = g.nslots >> 1;
                 if (d > h2) d -= g.nslots;
                 else if (d < -h2) d += g.nslots;
@@ -589,15 +591,24 @@ __device__ __forceinline__ void pass_b_tile(const Dom& D0, int64_t i, int64_t n,
         neighbor_loop<PER, LT>(active, (int)i, pi, X4, start, g, P, lst, words, pair_b, &wf);
     } else {
         const int16_t* __restrict__ row = nl + tile_row(i, kStoreCap);
-        int k = 0;
-        for (; k + 4 <= nst; k += 4) {
-            const int d0 = row[k * 32], d1 = row[(k + 1) * 32], d2 = row[(k + 2) * 32], d3 = row[(k + 3) * 32];
-            pair_b(list_slot<PER>((int)i, d0, g));
-            pair_b(list_slot<PER>((int)i, d1, g));
-            pair_b(list_slot<PER>((int)i, d2, g));
-            pair_b(list_slot<PER>((int)i, d3, g));
-        }
-        for (; k < nst; ++k) pair_b(list_slot<PER>((int)i, (int)row[k * 32], g));
+        // the modular slot arithmetic only in a warp with a row that may wrap (the other rows'
+        // offsets are direct: the modular form leaves them as they are)
+        auto walk = [&](auto wr) {
+            constexpr bool WR = decltype(wr)::value;
+            int k = 0;
+            for (; k + 4 <= nst; k += 4) {
+                const int d0 = row[k * 32], d1 = row[(k + 1) * 32], d2 = row[(k + 2) * 32], d3 = row[(k + 3) * 32];
+                pair_b(list_slot<WR>((int)i, d0, g));
+                pair_b(list_slot<WR>((int)i, d1, g));
+                pair_b(list_slot<WR>((int)i, d2, g));
+                pair_b(list_slot<WR>((int)i, d3, g));
+            }
+            for (; k < nst; ++k) pair_b(list_slot<WR>((int)i, (int)row[k * 32], g));
+        };
+        if (PER && (wf & 2))
+            walk(std::integral_constant<bool, PER>{});
+        else
+            walk(std::integral_constant<bool, false>{});
     }
     if (!inb) return;
     if (!active) {  // boundary rows: static, carried over to the next stage

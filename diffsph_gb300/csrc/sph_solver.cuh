@@ -352,7 +352,8 @@ __device__ __forceinline__ void skin_loop(int self, float2 pi, const float4* __r
 // (list entry, neighbor position, the reference's exact test) fills the warp's shared-memory
 // list lst, then f(j) runs over the accepted entries with every lane busy, in the skin
 // list's order. Every lane of the warp must call it (it votes); lanes with cnt = 0 add no
-// pairs. WR: the filter takes the minimum image (some row of the warp carries kRowWraps).
+// pairs. WR: some row of the warp carries kRowWraps, so the filter takes the minimum image
+// and the slots the modular form (the offsets of the other rows are direct).
 template <bool PER, bool WR, typename LT, class F>
 __device__ __forceinline__ void skin_list_loop(int self, float2 pi, const float4* __restrict__ X4, const Grid& g,
                                                const Phys& P, const int16_t* __restrict__ sl, int cnt,
@@ -368,7 +369,7 @@ __device__ __forceinline__ void skin_list_loop(int self, float2 pi, const float4
         for (int u = 0; u < 4; ++u) d[u] = (k + u < cnt) ? (int)row[(k + u) * 32] : 0;
 #pragma unroll
         for (int u = 0; u < 4; ++u)
-            if (k + u < cnt) xj[u] = ldg_xy(X4, list_slot<PER>(self, d[u], g));
+            if (k + u < cnt) xj[u] = ldg_xy(X4, list_slot<WR>(self, d[u], g));
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
             if (k + u < cnt) {
@@ -380,13 +381,13 @@ __device__ __forceinline__ void skin_list_loop(int self, float2 pi, const float4
         if (__any_sync(kFull, m > kCap - 4)) {
             const int mc = (int)__reduce_max_sync(kFull, (unsigned)m);
             for (int q = 0; q < mc; ++q)
-                if (q < m) f(list_slot<PER>(self, (int)lst[q * 32 + lane], g));
+                if (q < m) f(list_slot<WR>(self, (int)lst[q * 32 + lane], g));
             m = 0;
         }
     }
     const int mc = (int)__reduce_max_sync(kFull, (unsigned)m);
     for (int q = 0; q < mc; ++q)
-        if (q < m) f(list_slot<PER>(self, (int)lst[q * 32 + lane], g));
+        if (q < m) f(list_slot<WR>(self, (int)lst[q * 32 + lane], g));
 }
 
 // Geometry of a pair that already passed the exact test: r, q = r / h and the reference's
