@@ -64,6 +64,9 @@ WORKLOADS = {
     "dambreak_fs_dx512": dict(scene="dam_break", dx=1.0 / 512, free_surface=True),
     "dambreak_dx256": dict(scene="dam_break", dx=1.0 / 256),
     "tgv_64": dict(scene="taylor_green", nx=64),
+    # one periodic domain of 2,096,704 particles (jittered Fourier flow, 1448 x 1448): the
+    # single-domain case of the packed batch, stepped with Verlet reuse and the skin list
+    "fourier_1448": dict(scene="fourier", nx=1448, seed=0, jitter=0.1),
     # implicit particle shifting (shifting.scheme 'IPS'): jittered periodic Fourier flow
     "ips_fourier1024": dict(scene="fourier", nx=1024, seed=0, jitter=0.1, ips=True),
     "ips_fourier512": dict(scene="fourier", nx=512, seed=0, jitter=0.1, ips=True),
@@ -88,6 +91,8 @@ WORKLOADS = {
 WORKLOADS["neighbors_dx1024"] = dict(scene="neighbors", dx=1.0 / 1024)
 # the same at dx = 1/512 (524 k particles, a 1.1 GB list): the size the search's ncu captures use
 WORKLOADS["neighbors_dx512"] = dict(scene="neighbors", dx=1.0 / 512)
+# learned steps between restarts from the evaluation state in the timed learned rollout
+LEARNED_SEGMENT = 5
 NEIGHBOR_METRIC = "neighbor pairs/s (exact scatter-mode search, reference-format pair list)"
 LEARNED_METRIC = "particle-steps/s (learned k=4 step, counted in plain-step equivalents)"
 ADJOINT_METRIC = "adjoint particle-steps/s (forward + backward of a checkpointed rollout)"
@@ -992,7 +997,7 @@ def run_learned(args):
     import __graft_entry__ as ge
     from diffsph_gb300 import scenes
     from diffsph_gb300.learned import (CConvNet, LearnedStepper, check_device_errors, generate_trajectories,
-                                       judged_rollout, train)
+                                       judged_rollout, take_row_overflow, train)
     from diffsph_gb300.solver import BatchSolver, Solver
 
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
@@ -1025,15 +1030,20 @@ def run_learned(args):
     stepper = LearnedStepper(cfg, net, k, n_domains=w["batch"])
     stream = torch.cuda.Stream()
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    # the timed learned steps start again from the evaluation state every LEARNED_SEGMENT
+    # steps, the segment a judged rollout checks before it goes on (an unjudged rollout of
+    # hundreds of learned steps drifts away from the flow it was trained on); every step does
+    # the full work on the state it is given
+    x0 = (fl["positions"], fl["velocities"], fl["densities"])
     with torch.cuda.stream(stream):
-        x, u, r = fl["positions"], fl["velocities"], fl["densities"]
-        for _ in range(max(args.warmup, 3)):
-            x, u, r = stepper.step(x, u, r)
+        x, u, r = x0
+        for s_ in range(max(args.warmup, 3)):
+            x, u, r = stepper.step(*(x0 if s_ % LEARNED_SEGMENT == 0 else (x, u, r)))
         torch.cuda.synchronize()
         with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
             ev[0].record(stream)
-            for _ in range(args.steps):
-                x, u, r = stepper.step(x, u, r)
+            for s_ in range(args.steps):
+                x, u, r = stepper.step(*(x0 if s_ % LEARNED_SEGMENT == 0 else (x, u, r)))
             ev[1].record(stream)
             torch.cuda.synchronize()
         check_device_errors()
@@ -1098,6 +1108,7 @@ def run_learned(args):
         ro = torch.as_tensor(s0["fluid"]["densities"]).cuda()
         for _ in range(w["rollout"] // k):
             xo, uo, ro = one.step(xo, uo, ro)
+        free_overflow = take_row_overflow()
         err = float(torch.linalg.norm(uo - ref["velocities"]) / torch.linalg.norm(ref["velocities"]))
         rho_dev = float(torch.max(torch.abs(ro - 1.0)))
         (_, uj, _), acc, rej = judged_rollout(one, s0["fluid"], w["rollout"] // k, segment=5)
@@ -1107,6 +1118,7 @@ def run_learned(args):
                       "iters": w["iters"], "seconds": round(t_train, 1), "generate_seconds": round(t_gen, 1),
                       "loss_first100": float(np.mean(hist[:100])), "loss_last100": float(np.mean(hist[-100:]))},
             "rollout_steps": w["rollout"], "velocity_rel_l2_vs_plain": err, "max_density_dev": rho_dev,
+            "free_rollout_row_overflow": free_overflow,
             "judged": {"segments_accepted": acc, "segments_rejected": rej, "velocity_rel_l2_vs_plain": err_j}}
     else:
         acc_info = {"train": "untrained weights (timing only)"}
@@ -1115,6 +1127,7 @@ def run_learned(args):
         "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": ms_learned, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "bf16 (fp32 accumulate)", "data": "synthetic",
         "config": {"workload": args.workload, "particles": n, "domains": w["batch"], "k": k,
+                   "restart_every": LEARNED_SEGMENT,
                    "plain_ms_per_step": ms_plain, "plain_particle_steps_per_s": n / (ms_plain / 1e3),
                    "learned_over_plain_simulated_time": (k * ms_plain) / ms_learned,
                    **acc_info,

@@ -62,6 +62,11 @@ def _err_word(device):
     return _ERR[key]
 
 
+# bit of the error word: a particle with more neighbors within the learned support than the
+# aggregation's 64-edge capacity (its row was truncated to 64 edges)
+ROW_OVERFLOW = 8
+
+
 def check_device_errors():
     """Raise if a tcgen05 kernel recorded a wait that did not complete or a neighbor row
     longer than its capacity (synchronises)."""
@@ -70,6 +75,21 @@ def check_device_errors():
         if v:
             w.zero_()
             raise RuntimeError(f"tcgen05 kernel error flags {v:#x} on device {k}")
+
+
+def take_row_overflow() -> bool:
+    """Read and clear the row-capacity flag (synchronises): True when a learned step since the
+    last call met a particle with more than 64 neighbors within the learned support, whose
+    aggregation was truncated. Any other flag raises as in check_device_errors."""
+    hit = False
+    for k, w in _ERR.items():
+        v = int(w.item())
+        if v:
+            w.zero_()
+            if v & ~ROW_OVERFLOW:
+                raise RuntimeError(f"tcgen05 kernel error flags {v:#x} on device {k}")
+            hit = True
+    return hit
 
 
 def gemm_tn(A, Bt, out=None, accumulate=False):
@@ -378,10 +398,11 @@ def kinetic_energy(u, m):
 def judged_rollout(stepper: LearnedStepper, fluid, n_learned, segment=8, rho_tol=0.02, ke_tol=0.05):
     """Rollout of n_learned learned steps (k plain steps each) with the solver as judge and
     fallback. Each segment of ``segment`` learned steps is accepted when the density stays
-    within rho_tol of rho0 and the kinetic energy stays within ke_tol (relative) of the
+    within rho_tol of rho0, the kinetic energy stays within ke_tol (relative) of the
     solver's prediction KE0 + t dKE/dt, dKE/dt = sum m u . a from one right-hand side at the
-    segment start; otherwise the segment is re-run by the solver. Returns the final state
-    and the counts of accepted and rejected segments."""
+    segment start, and no particle exceeded the aggregation's 64-neighbor capacity (a
+    clustering the learned steps brought about); otherwise the segment is re-run by the
+    solver. Returns the final state and the counts of accepted and rejected segments."""
     cfg = stepper.config
     m = float(fluid["masses"][0])
     sol = Solver(cfg, fluid)
@@ -396,11 +417,14 @@ def judged_rollout(stepper: LearnedStepper, fluid, n_learned, segment=8, rho_tol
         ke0 = kinetic_energy(u, m)
         dke = m * float(torch.sum(u * r["dudt"]))
         xs, us, rs = x, u, rho
+        take_row_overflow()  # (a flag left by earlier steps is not this segment's)
         for _ in range(nseg):
             xs, us, rs = stepper.step(xs, us, rs)
         T = nseg * stepper.k * stepper.dt
         ke_pred = ke0 + T * dke
-        ok = bool(torch.isfinite(us).all()) and float(torch.max(torch.abs(rs / stepper.rho0 - 1.0))) <= rho_tol
+        ok = not take_row_overflow()
+        ok = ok and bool(torch.isfinite(us).all())
+        ok = ok and float(torch.max(torch.abs(rs / stepper.rho0 - 1.0))) <= rho_tol
         ok = ok and abs(kinetic_energy(us, m) - ke_pred) <= ke_tol * max(ke0, 1e-30)
         if ok:
             x, u, rho = xs, us, rs

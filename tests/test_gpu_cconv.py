@@ -309,3 +309,24 @@ def test_graph_lists_equal_the_exact_neighbor_sets(n_domains):
         for i in range(per):
             row = np.sort(nbr[off[d * per + i]:off[d * per + i + 1]]) - d * per
             assert np.array_equal(row, j[o[i]:o[i + 1]]), (d, i)
+
+
+def test_row_over_the_aggregation_capacity_is_flagged_and_taken():
+    """A particle with more than 64 neighbors within the learned support (a cluster the
+    learned steps can bring about) is truncated to its first 64 edges by the tensor-core
+    aggregation, which sets the row-capacity flag: take_row_overflow reports it once and
+    clears it (a judged rollout then rejects the segment), and no other flag is left."""
+    from diffsph_gb300.learned import Graph, aggregate, check_device_errors, take_row_overflow
+    cfg, st = scenes.fourier_periodic(32, seed=3, jitter=0.0)
+    x = torch.as_tensor(st["fluid"]["positions"]).clone()
+    H = float(cfg["particle"]["support"])
+    gen = torch.Generator().manual_seed(0)
+    x[:80] = torch.tensor([0.1, 0.2]) + 0.05 * H * torch.rand(80, 2, generator=gen)
+    g = Graph(x.cuda(), cfg)
+    assert int((g.offsets[1:] - g.offsets[:-1]).max()) > 64
+    h = torch.randn(g.n, 16, device="cuda").to(torch.bfloat16)
+    assert not take_row_overflow()
+    aggregate(g, h)
+    assert take_row_overflow()
+    assert not take_row_overflow()
+    check_device_errors()
