@@ -446,9 +446,9 @@ __device__ __forceinline__ void pass_a_tile(const Dom& D0, int64_t i, int64_t n,
         const bool use_skin = skin_mode == 1 && __all_sync(kFull, sk >= 0) && words[3] == 0u;
         if (use_skin) {
             if (PER && (wf & 2))
-                skin_list_loop<PER, PER, LT>((int)i, pi, X4, g, P, sl, sk, lst, pair_a);
+                skin_list_loop<PER, PER, LT, decltype(pair_a)&, !BATCH>((int)i, pi, X4, g, P, sl, sk, lst, pair_a);
             else
-                skin_list_loop<PER, false, LT>((int)i, pi, X4, g, P, sl, sk, lst, pair_a);
+                skin_list_loop<PER, false, LT, decltype(pair_a)&, !BATCH>((int)i, pi, X4, g, P, sl, sk, lst, pair_a);
         } else {
             neighbor_loop<PER, LT>(active, (int)i, pi, X4, start, g, P, lst, words, pair_a, &wf);
         }
@@ -593,11 +593,26 @@ __device__ __forceinline__ void pass_b_tile(const Dom& D0, int64_t i, int64_t n,
         const int16_t* __restrict__ row = nl + tile_row(i, kStoreCap);
         // the modular slot arithmetic only in a warp with a row that may wrap (the other rows'
         // offsets are direct: the modular form leaves them as they are)
+        // the next group's entries are loaded before this group's pairs, so their latency
+        // (the list is read once, mostly from DRAM) hides behind the pair terms
         auto walk = [&](auto wr) {
             constexpr bool WR = decltype(wr)::value;
             int k = 0;
+            int n0 = 0, n1 = 0, n2 = 0, n3 = 0;
+            if (nst >= 4) {
+                n0 = row[0];
+                n1 = row[32];
+                n2 = row[64];
+                n3 = row[96];
+            }
             for (; k + 4 <= nst; k += 4) {
-                const int d0 = row[k * 32], d1 = row[(k + 1) * 32], d2 = row[(k + 2) * 32], d3 = row[(k + 3) * 32];
+                const int d0 = n0, d1 = n1, d2 = n2, d3 = n3;
+                if (k + 8 <= nst) {
+                    n0 = row[(k + 4) * 32];
+                    n1 = row[(k + 5) * 32];
+                    n2 = row[(k + 6) * 32];
+                    n3 = row[(k + 7) * 32];
+                }
                 pair_b(list_slot<WR>((int)i, d0, g));
                 pair_b(list_slot<WR>((int)i, d1, g));
                 pair_b(list_slot<WR>((int)i, d2, g));
@@ -756,9 +771,9 @@ __device__ __forceinline__ void shift_tile(const Dom& D0, int64_t i, int64_t n, 
     const int sk = row_count((use_skin && active) ? (int)slc[i] : 0, wf);
     if (use_skin && __all_sync(kFull, sk >= 0) && words[3] == 0u) {
         if (PER && (wf & 2))
-            skin_list_loop<PER, PER, LT>((int)i, pi, X4, g, P, sl, sk, lst, pair_s);
+            skin_list_loop<PER, PER, LT, decltype(pair_s)&, !BATCH>((int)i, pi, X4, g, P, sl, sk, lst, pair_s);
         else
-            skin_list_loop<PER, false, LT>((int)i, pi, X4, g, P, sl, sk, lst, pair_s);
+            skin_list_loop<PER, false, LT, decltype(pair_s)&, !BATCH>((int)i, pi, X4, g, P, sl, sk, lst, pair_s);
     } else {
         neighbor_loop<PER, LT>(active, (int)i, pi, X4, start, g, P, lst, words, pair_s, &wf);
     }

@@ -353,8 +353,9 @@ __device__ __forceinline__ void skin_loop(int self, float2 pi, const float4* __r
 // list lst, then f(j) runs over the accepted entries with every lane busy, in the skin
 // list's order. Every lane of the warp must call it (it votes); lanes with cnt = 0 add no
 // pairs. WR: some row of the warp carries kRowWraps, so the filter takes the minimum image
-// and the slots the modular form (the offsets of the other rows are direct).
-template <bool PER, bool WR, typename LT, class F>
+// and the slots the modular form (the offsets of the other rows are direct). PF: load the next
+// group's entries ahead (measured faster on single domains, slower in packed batches).
+template <bool PER, bool WR, typename LT, class F, bool PF = true>
 __device__ __forceinline__ void skin_list_loop(int self, float2 pi, const float4* __restrict__ X4, const Grid& g,
                                                const Phys& P, const int16_t* __restrict__ sl, int cnt,
                                                LT* __restrict__ lst, F&& f) {
@@ -362,11 +363,20 @@ __device__ __forceinline__ void skin_list_loop(int self, float2 pi, const float4
     const int kmax = (int)__reduce_max_sync(kFull, (unsigned)cnt);
     const int16_t* __restrict__ row = sl + tile_row(self, kSkinCap);
     int m = 0;
+    // PF: the next group's entries are loaded before this group's tests, so their latency
+    // (the list is read from DRAM) hides behind the work of this group
+    int dn[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) dn[u] = (PF && u < cnt) ? (int)row[u * 32] : 0;
     for (int k = 0; k < kmax; k += 4) {
         int d[4];
         float2 xj[4];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) d[u] = (k + u < cnt) ? (int)row[(k + u) * 32] : 0;
+        for (int u = 0; u < 4; ++u) d[u] = PF ? dn[u] : ((k + u < cnt) ? (int)row[(k + u) * 32] : 0);
+        if (PF) {
+#pragma unroll
+            for (int u = 0; u < 4; ++u) dn[u] = (k + 4 + u < cnt) ? (int)row[(k + 4 + u) * 32] : 0;
+        }
 #pragma unroll
         for (int u = 0; u < 4; ++u)
             if (k + u < cnt) xj[u] = ldg_xy(X4, list_slot<WR>(self, d[u], g));
