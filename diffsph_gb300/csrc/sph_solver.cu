@@ -43,7 +43,7 @@ __global__ void k_upload(int64_t nF, int64_t nB, const float* __restrict__ xf, c
                          const float* __restrict__ rf, const float* __restrict__ xb, const float* __restrict__ nb,
                          const float* __restrict__ db, const float* __restrict__ rb, const Dom* __restrict__ doms,
                          const int64_t* __restrict__ dom_off, int nd, float2* Xr, float4* X4, float4* V4,
-                         int32_t* uid, int32_t* did, float2* bnormal, float* bdist) {
+                         int32_t* uid, int32_t* slot, int32_t* did, float2* bnormal, float* bdist) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nF + nB) return;
     // domain of fluid particle i: dom_off[d] <= i < dom_off[d + 1]; boundaries belong to domain 0
@@ -80,23 +80,41 @@ __global__ void k_upload(int64_t nF, int64_t nB, const float* __restrict__ xf, c
     X4[i] = make_float4(w.x, w.y, rho_s, eos_p(rho, P.eos));
     V4[i] = make_float4(u.x, u.y, 0.f, 0.f);
     uid[i] = (int32_t)i;
+    slot[i] = (int32_t)i;
 }
 
-// Upload into the current slot order (Verlet reuse): slot s takes the state of particle
-// uid[s]; the sort words are left as they are, so the next step's displacement check decides
-__global__ void k_upload_keep(int64_t n, int64_t nF, const int32_t* __restrict__ uid, const float* __restrict__ xf,
+// Element o of a caller's [n][2] float array: one 8-byte access when the array is 8-byte
+// aligned (the same for every thread), so a warp's accesses fill whole lines of host memory
+__device__ __forceinline__ float2 ld_pair(const float* a, int64_t o) {
+    if ((reinterpret_cast<uintptr_t>(a) & 7u) == 0) return reinterpret_cast<const float2*>(a)[o];
+    return make_float2(a[2 * o], a[2 * o + 1]);
+}
+__device__ __forceinline__ void st_pair(float* a, int64_t o, float2 v) {
+    if ((reinterpret_cast<uintptr_t>(a) & 7u) == 0) {
+        reinterpret_cast<float2*>(a)[o] = v;
+    } else {
+        a[2 * o] = v.x;
+        a[2 * o + 1] = v.y;
+    }
+}
+
+// Upload into the current slot order (Verlet reuse): particle o's state goes to its slot
+// slot[o]; the sort words are left as they are, so the next step's displacement check decides.
+// The threads run over the original order, so the caller's arrays are read contiguously: they
+// may be page-locked host memory, which the kernel then reads over the host link itself.
+__global__ void k_upload_keep(int64_t n, int64_t nF, const int32_t* __restrict__ slot, const float* __restrict__ xf,
                               const float* __restrict__ uf, const float* __restrict__ rf,
                               const float* __restrict__ xb, const float* __restrict__ nb,
                               const float* __restrict__ db, const float* __restrict__ rb, Phys P, float2* Xr,
                               float4* X4, float4* V4, float2* bnormal, float* bdist) {
-    int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= n) return;
-    const int64_t o = uid[s];
+    const int64_t o = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (o >= n) return;
+    const int64_t s = slot[o];
     float2 x, u = make_float2(0.f, 0.f);
     float rho, rho_s;
     if (o < nF) {
-        x = make_float2(xf[2 * o], xf[2 * o + 1]);
-        u = make_float2(uf[2 * o], uf[2 * o + 1]);
+        x = ld_pair(xf, o);
+        u = ld_pair(uf, o);
         rho = rf[o];
         rho_s = rho;
     } else {
@@ -113,15 +131,19 @@ __global__ void k_upload_keep(int64_t n, int64_t nF, const int32_t* __restrict__
     V4[s] = make_float4(u.x, u.y, 0.f, 0.f);
 }
 
-__global__ void k_download(int64_t n, int nF, const int32_t* __restrict__ uid, const float2* __restrict__ Xr,
+// The state in the original order (particle o from its slot): the threads run over the
+// original order, so the caller's arrays are written contiguously (page-locked host memory
+// included, written over the host link by the kernel itself)
+__global__ void k_download(int64_t n, int nF, const int32_t* __restrict__ slot, const float2* __restrict__ Xr,
                            const float4* __restrict__ X4, const float4* __restrict__ V4, float* xf, float* uf,
                            float* rf, float* rb) {
-    int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= n) return;
-    int o = uid[s];
+    const int64_t o = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (o >= n) return;
+    const int s = slot[o];
     if (o < nF) {
-        if (xf) { xf[2 * o] = Xr[s].x; xf[2 * o + 1] = Xr[s].y; }
-        if (uf) { uf[2 * o] = V4[s].x; uf[2 * o + 1] = V4[s].y; }
+        const float4 v = V4[s];
+        if (xf) st_pair(xf, o, Xr[s]);
+        if (uf) st_pair(uf, o, make_float2(v.x, v.y));
         if (rf) rf[o] = X4[s].z;
     } else if (rb) {
         rb[o - nF] = fabsf(X4[s].z);
@@ -133,7 +155,8 @@ __global__ void k_gather(int64_t n, int nF, const int32_t* __restrict__ perm, co
                          const int32_t* __restrict__ uid_in, const int32_t* __restrict__ did_in,
                          float2* __restrict__ Xr_out, float4* __restrict__ X4_out, float4* __restrict__ V4_out,
                          int32_t* __restrict__ uid_out, int32_t* __restrict__ did_out, int32_t* __restrict__ bidx,
-                         uint32_t* __restrict__ words, float2* __restrict__ Xs, const uint32_t* __restrict__ gate) {
+                         uint32_t* __restrict__ words, float2* __restrict__ Xs, int32_t* __restrict__ slot,
+                         const uint32_t* __restrict__ gate) {
     if (gate && *gate == 0u) return;
     int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= n) return;
@@ -146,6 +169,7 @@ __global__ void k_gather(int64_t n, int nF, const int32_t* __restrict__ perm, co
     did_out[s] = did_in[o];
     int u = uid_in[o];
     uid_out[s] = u;
+    slot[u] = (int32_t)s;
     if (u >= nF) bidx[atomicAdd(&words[2], 1u)] = (int32_t)s;
 }
 
@@ -1805,6 +1829,7 @@ static size_t solver_layout(const sph_params_t* p, const int64_t* nF_d, int nd, 
     int32_t* did_t = c.take<int32_t>(n);
     int32_t* key = c.take<int32_t>(n);
     int32_t* perm = c.take<int32_t>(n);
+    int32_t* slot = c.take<int32_t>(n);
     int32_t* count = c.take<int32_t>(ncells);
     int32_t* fill = c.take<int32_t>(ncells);
     int32_t* start = c.take<int32_t>(ncells + 1);
@@ -1834,7 +1859,7 @@ static size_t solver_layout(const sph_params_t* p, const int64_t* nF_d, int nd, 
         S->Xr = Xr; S->Xr_t = Xr_t; S->Xs = Xs;
         S->Xc = X[0]; S->Xh = X[1]; S->Xf = X[2]; S->Xt = X[3];
         S->Vc = V[0]; S->Vh = V[1]; S->Vf = V[2]; S->Vt = V[3];
-        S->uid = uid; S->uid_t = uid_t; S->did = did; S->did_t = did_t;
+        S->uid = uid; S->uid_t = uid_t; S->did = did; S->did_t = did_t; S->slot = slot;
         S->key = key; S->perm = perm; S->count = count; S->fill = fill; S->start = start; S->scan32 = scan32;
         S->bidx = bidx; S->words = words; S->maxv = maxv; S->doms = doms; S->dom_off = dom_off;
         S->bnormal = bnormal; S->bdist = bdist;
@@ -2051,7 +2076,7 @@ extern "C" int sph_solver_upload(sph_solver_t* S, const float* x_fluid, const fl
     if (S->reuse && S->uploaded && S->nd == 1) {
         // keep the current order (and the pending-sort and skin-list words): the next step's
         // displacement check sorts when the new positions are too far from the last sort's
-        k_upload_keep<<<blocks_for(S->n), kBlock, 0, st>>>(S->n, S->nF, S->uid, x_fluid, u_fluid, rho_fluid,
+        k_upload_keep<<<blocks_for(S->n), kBlock, 0, st>>>(S->n, S->nF, S->slot, x_fluid, u_fluid, rho_fluid,
                                                              x_boundary, normal_boundary, dist_boundary,
                                                              rho_boundary, S->doms_host[0].P, S->Xr, S->Xc, S->Vc,
                                                              S->bnormal, S->bdist);
@@ -2061,7 +2086,8 @@ extern "C" int sph_solver_upload(sph_solver_t* S, const float* x_fluid, const fl
     }
     k_upload<<<blocks_for(S->n), kBlock, 0, st>>>(S->nF, S->nB, x_fluid, u_fluid, rho_fluid, x_boundary,
                                                     normal_boundary, dist_boundary, rho_boundary, S->doms, S->dom_off,
-                                                    S->nd, S->Xr, S->Xc, S->Vc, S->uid, S->did, S->bnormal, S->bdist);
+                                                    S->nd, S->Xr, S->Xc, S->Vc, S->uid, S->slot, S->did, S->bnormal,
+                                                    S->bdist);
     if (cudaMemsetAsync(S->words, 0, sizeof(uint32_t) * 8, st) != cudaSuccess) return SPH_ERR_CUDA;
     // a new state is always sorted first
     if (cudaMemsetAsync(S->words + 4, 1, sizeof(uint32_t), st) != cudaSuccess) return SPH_ERR_CUDA;
@@ -2094,7 +2120,7 @@ static int rebuild(sph_solver* S, cudaStream_t st, bool in_step = false) {
     tbeg(S, KC_GATHER, st);
     k_gather<<<blocks_for(S->n), kBlock, 0, st>>>(S->n, (int)S->nF, S->perm, S->Xr, S->Xc, S->Vc, S->uid, S->did,
                                                     S->Xr_t, S->Xt, S->Vt, S->uid_t, S->did_t, S->bidx, S->words,
-                                                    S->Xs, gate);
+                                                    S->Xs, S->slot, gate);
     if (S->reuse)
         k_copy_back<<<blocks_for(S->n), kBlock, 0, st>>>(S->n, S->Xr_t, S->Xt, S->Vt, S->uid_t, S->did_t, S->Xr,
                                                           S->Xc, S->Vc, S->uid, S->did, gate);
@@ -2688,8 +2714,8 @@ extern "C" int sph_solver_download(sph_solver_t* S, float* x_fluid, float* u_flu
                                    float* rho_boundary, sph_stream_t stream) {
     if (!S) return SPH_ERR_ARGUMENT;
     cudaStream_t st = (cudaStream_t)stream;
-    k_download<<<blocks_for(S->n), kBlock, 0, st>>>(S->n, (int)S->nF, S->uid, S->Xr, S->Xc, S->Vc, x_fluid, u_fluid,
-                                                      rho_fluid, rho_boundary);
+    k_download<<<blocks_for(S->n), kBlock, 0, st>>>(S->n, (int)S->nF, S->slot, S->Xr, S->Xc, S->Vc, x_fluid,
+                                                      u_fluid, rho_fluid, rho_boundary);
     return cudaGetLastError() == cudaSuccess ? SPH_OK : SPH_ERR_CUDA;
 }
 

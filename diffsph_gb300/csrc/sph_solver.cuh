@@ -476,6 +476,7 @@ struct sph_solver {
     float4 *Xc, *Xh, *Xf, *Xt;
     float4 *Vc, *Vh, *Vf, *Vt;
     int32_t *uid, *uid_t, *did, *did_t;
+    int32_t* slot;  // slot of each particle (original order): the inverse of uid
     int32_t *key, *perm, *count, *fill, *start, *scan32;
     int32_t* bidx;
     // [0] flags, [2] boundary count, [3] skin list invalid, [4] sort this step, [5] sorts done

@@ -177,6 +177,19 @@ def _ptr(t):
     return ctypes.c_void_p(t.data_ptr()) if t is not None else None
 
 
+def _pinned(t) -> bool:
+    """A page-locked float32 contiguous host tensor: the solver's upload and download kernels
+    read and write it directly (no staging copy)."""
+    return (isinstance(t, torch.Tensor) and not t.is_cuda and t.dtype == torch.float32 and t.is_contiguous()
+            and t.is_pinned())
+
+
+def _io(t):
+    """The array as the upload kernel reads it: a page-locked host tensor as it is, anything
+    else copied to the device."""
+    return t if _pinned(t) else _dev(t)
+
+
 def _stream():
     return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
 
@@ -236,17 +249,21 @@ class Solver:
 
     # -- state transfer ------------------------------------------------------------------
     def upload(self, fluid, boundary=None):
-        xf, uf, rf = _dev(fluid["positions"]), _dev(fluid["velocities"]), _dev(fluid["densities"])
+        """Load a state (original order). Page-locked float32 host tensors are read by the
+        upload kernel directly over the host link; other arrays are copied to the device."""
+        xf, uf, rf = _io(fluid["positions"]), _io(fluid["velocities"]), _io(fluid["densities"])
         args = [xf, uf, rf, None, None, None, None]
         if self.nB:
-            args[3:] = [_dev(boundary["positions"]), _dev(boundary["normals"]), _dev(boundary["distances"]),
-                        _dev(boundary["densities"]) if "densities" in boundary else None]
+            args[3:] = [_io(boundary["positions"]), _io(boundary["normals"]), _io(boundary["distances"]),
+                        _io(boundary["densities"]) if "densities" in boundary else None]
         self._keep = args
         _lib.check("sph_solver_upload", self.lib.sph_solver_upload(self.handle, *[_ptr(a) for a in args], _stream()))
 
     def download(self, out=None):
         """The state in the original order: positions, velocities, densities (and the wall
-        densities). ``out``: caller tensors (CUDA float32, contiguous) to write into."""
+        densities). ``out``: caller tensors to write into, float32 and contiguous, on the device
+        or page-locked on the host (written by the download kernel directly over the host link;
+        complete once the current stream has reached this call)."""
         if out is None:
             out = {"positions": torch.empty(self.nF, 2, device="cuda"),
                    "velocities": torch.empty(self.nF, 2, device="cuda"),
@@ -257,6 +274,16 @@ class Solver:
             rb = out.get("boundary_densities") if self.nB else None
             if self.nB and rb is None:
                 raise ValueError("out needs boundary_densities for a solver with walls")
+            need = {"positions": 2 * self.nF, "velocities": 2 * self.nF, "densities": self.nF,
+                    "boundary_densities": self.nB}
+            for k, n in need.items():
+                t = out.get(k)
+                if t is None or (k == "boundary_densities" and not self.nB):
+                    continue
+                if not (t.dtype == torch.float32 and t.is_contiguous() and (t.is_cuda or _pinned(t))):
+                    raise ValueError(f"out[{k!r}] must be float32, contiguous, on the device or page-locked")
+                if t.numel() != n:
+                    raise ValueError(f"out[{k!r}] holds {t.numel()} values, the state {n}")
         _lib.check("sph_solver_download", self.lib.sph_solver_download(
             self.handle, _ptr(out["positions"]), _ptr(out["velocities"]), _ptr(out["densities"]), _ptr(rb), _stream()))
         if self.nB:

@@ -168,7 +168,9 @@ void sph_solver_destroy(sph_solver_t* solver);
  * the next step sorts again only if a particle is farther than the reuse limit from its
  * position at the last sort (a state read back by sph_solver_download and uploaded again
  * costs no sort). Otherwise the particles are loaded in the original order and the next
- * step sorts. */
+ * step sorts. The arrays may be device memory or page-locked host memory (mapped into the
+ * device's address space, as sph_solver_download): the kernel reads host arrays itself
+ * over the host link, in the original order. */
 int sph_solver_upload(sph_solver_t* s, const float* x_fluid, const float* u_fluid,
                       const float* rho_fluid, const float* x_boundary, const float* normal_boundary,
                       const float* dist_boundary, const float* rho_boundary, sph_stream_t stream);
@@ -450,7 +452,11 @@ int sph_mdbc_density(const sph_pairs_t* nb, const float* m_f, const float* rho_f
                      const float* x_ghost, double support, double rho0, float* rho_out, float* shepard_out,
                      sph_stream_t stream);
 
-/* Writes the current state back in the original order (NULL entries are skipped). */
+/* Writes the current state back in the original order (NULL entries are skipped). The arrays
+ * may be device memory or page-locked host memory (cudaHostAlloc / cudaHostRegister; mapped
+ * into the device's address space): the kernel then writes the host arrays itself over the
+ * host link, one pass in the original order, with no staging copy. Host arrays are complete
+ * once the stream has reached this call. */
 int sph_solver_download(sph_solver_t* s, float* x_fluid, float* u_fluid, float* rho_fluid,
                         float* rho_boundary, sph_stream_t stream);
 

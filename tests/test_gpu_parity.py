@@ -357,6 +357,43 @@ def test_reupload_keeps_the_order_under_verlet_reuse():
         assert torch.equal(ga[k], gb[k]), k
 
 
+def test_page_locked_host_state_round_trip_equals_the_device_path():
+    """Upload from and download into page-locked host tensors (read and written by the
+    solver's kernels over the host link, no staging copy) give the device path's state bit
+    for bit, through a re-upload that keeps the order under Verlet reuse and through a sort."""
+    cfg, st = scenes.dam_break(dx=1.0 / 64)
+    a = _solver(cfg, st)
+    b = _solver(cfg, st)
+    nF, nB = st["fluid"]["positions"].shape[0], st["boundary"]["positions"].shape[0]
+    host = {"positions": torch.empty(nF, 2).pin_memory(), "velocities": torch.empty(nF, 2).pin_memory(),
+            "densities": torch.empty(nF).pin_memory(), "boundary_densities": torch.empty(nB).pin_memory()}
+    bnd = {k: torch.from_numpy(np.ascontiguousarray(st["boundary"][k], np.float32)).pin_memory()
+           for k in ("positions", "normals", "distances")}
+    for _ in range(3):
+        a.step(2)
+        b.step(2)
+        got = b.download(host)
+        torch.cuda.synchronize()
+        ref = a.download()
+        for k in host:
+            assert torch.equal(got[k], ref[k].cpu()), k
+        b.upload({k: host[k] for k in ("positions", "velocities", "densities")},
+                 dict(bnd, densities=host["boundary_densities"]))
+        dev = {k: ref[k] for k in ("positions", "velocities", "densities")}
+        a.upload(dev, dict({k: torch.from_numpy(np.ascontiguousarray(st["boundary"][k], np.float32)).cuda()
+                            for k in ("positions", "normals", "distances")}, densities=ref["boundary_densities"]))
+    a.step(3)
+    b.step(3)
+    b.check()
+    assert a.sort_count() == b.sort_count()
+    ga, gb = a.download(), b.download()
+    for k in ("positions", "velocities", "densities", "boundary_densities"):
+        assert torch.equal(ga[k], gb[k]), k
+    with pytest.raises(ValueError):
+        b.download({"positions": torch.empty(nF, 2), "velocities": host["velocities"],
+                    "densities": host["densities"], "boundary_densities": host["boundary_densities"]})
+
+
 def test_per_pass_shapes_mix_in_one_batched_step():
     """Different shapes per pass (persistent and one-block-per-tile grids mixed) on a packed
     batch give the same state as the default shape."""
