@@ -541,8 +541,8 @@ def test_taylor_green_decays_at_the_viscous_rate():
 
 
 def test_verlet_reuse_skips_sorts_and_matches_sorting_every_step():
-    """Verlet reuse (on by default for one non-periodic domain, as the reference reuses its
-    neighbor structure at neighborhood.verletScale = 1.5): in the dam break's first steps the
+    """Verlet reuse (on by default, as the reference reuses its neighbor structure at
+    neighborhood.verletScale = 1.5): in the dam break's first steps the
     column's foot moves 0.002-0.013 h per step, so only some steps sort (about one in three).
     The state equals that of a solver sorting every step up to the order of each particle's
     pair sums; a graph replay equals the eager steps bit for bit."""
