@@ -230,6 +230,7 @@ __global__ void k_sort_begin(uint32_t* words, int skin_rebuilt) {
 // Two kernels: one warp per wall particle sums the 13 moments of its ghost, its lanes
 // striding over the candidates of all stencil ranges (a fixed shuffle tree combines them);
 // then one thread per wall particle solves the fp64 3x3 system, 32 wall particles per warp.
+constexpr int kMdbcSolveBlock = 64;  // threads per block of the fp64 solve (one wall each)
 constexpr int kMdbcSums = 16;  // 13 used: num, den, gs0, gs1, vg0, vg1, ps0, ps1, pm00, pm01, pm10, pm11, count
 
 __device__ __forceinline__ float2 mdbc_ghost(const Phys& P, float2 xb, float2 nrm, float d) {
@@ -2150,7 +2151,9 @@ static void launch_mdbc(sph_solver* S, float4* X4, float* rho_b_out, cudaStream_
     else
         k_mdbc_sums<false><<<gw, 128, 0, st>>>((int)S->nB, S->bidx, S->uid, S->Xr, X4, S->bnormal, S->bdist, S->start,
                                                D.g, D.P, S->msums);
-    k_mdbc_solve<<<blocks_for(S->nB), kBlock, 0, st>>>((int)S->nB, S->bidx, S->uid, S->Xr, X4, S->bnormal, S->bdist,
+    // 64-thread blocks: the solve is bound by each SM's FP64 rate, so its warps are spread
+    // over every SM (24.6 k walls in 256-thread blocks filled 96 of the 152)
+    k_mdbc_solve<<<blocks_for(S->nB, kMdbcSolveBlock), kMdbcSolveBlock, 0, st>>>((int)S->nB, S->bidx, S->uid, S->Xr, X4, S->bnormal, S->bdist,
                                                        D.P, S->msums, rho_b_out);
     tend(S, KC_MDBC, st);
 }
